@@ -1,0 +1,279 @@
+/*
+ * mcg.h -- C ABI of the GB300 beam-lattice energy/gradient + L-BFGS library.
+ *
+ * The reference solver (projects/metamaterial-compression/industry-grade, "MC/"
+ * below) keeps this path behind one private C++ member,
+ *   Objective Simulator::objective(const std::vector<double>& z, double top,
+ *                                  bool trials) const          (MC/include/sim.hpp:49,
+ *                                                               MC/src/sim.cpp:138-172)
+ * and its caller Simulator::minimize (MC/src/sim.cpp:174-211).  The reference has no
+ * FFI of its own; the entry points below are what its solver binds to replace that
+ * member (the patch is shown in INTEGRATION.md): plain pointers and sizes, no C++ or
+ * torch types.  Every function returns an int status (MCG_OK = 0); mcg_last_error()
+ * gives the message.  Contexts own their device memory and are not thread-safe: use
+ * one context per host thread, as the reference uses one Simulator per thread.
+ *
+ * Layouts (all host arrays are caller-owned, copied in/out):
+ *   z, grad      6 doubles per node: [tx, ty, tz, rx, ry, rz]; translations in units of
+ *                translation_scale, rotations as a rotation vector (MC/src/sim.cpp:136).
+ *   base_x       3 doubles per node (m).       base_r   4 doubles per node (w, x, y, z).
+ *   plastic      7 doubles per beam: [epsp, alpha, rotp.x, rotp.y, rotp.z, alphaB, alphaT]
+ *                (PlasticState, MC/include/sim.hpp:28).
+ *   e0           3 doubles per beam (material director, MC/include/sim.hpp:29).
+ *   connected    pair keys (min << 32 | max) of node pairs excluded from self-contact
+ *                (Simulator::connected_, MC/src/sim.cpp:115-117; key as core.hpp:47 pairKey).
+ *   locked       one byte per DOF (Simulator::locked_, MC/src/sim.cpp:134).
+ */
+#ifndef MCG_H
+#define MCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCG_ABI_VERSION 1
+
+enum mcg_status {
+    MCG_OK = 0,
+    MCG_ERR_INVALID = 1,     /* bad argument, size or topology */
+    MCG_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    MCG_ERR_NO_DEVICE = 3,   /* no usable GPU */
+    MCG_ERR_STATE = 4,       /* call order (objective before topology, commit before minimize) */
+    MCG_ERR_EQUILIBRIUM = 5, /* run(): an increment failed after all bisections (the
+                                reference throws std::runtime_error, MC/src/sim.cpp:412-419) */
+    MCG_ERR_CAPACITY = 6,    /* an output buffer is too small; the needed count is returned */
+    MCG_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+};
+
+enum mcg_precision {
+    MCG_FP64 = 0,  /* plain form: FP64 throughout (the correctness oracle on the GPU) */
+    MCG_MIXED = 1, /* FP32 bulk element/contact arithmetic, FP64 reductions */
+};
+
+/* MaterialConfig, MC/include/sim.hpp:16 (the name string is not carried). */
+typedef struct mcg_material {
+    double density, young, nu, yield, hardening, bend_hardening, torsion_hardening;
+} mcg_material;
+
+/* SimulationConfig, MC/include/sim.hpp:17-26, field for field, plus two extensions at
+ * the end.  mcg_config_defaults() fills the reference defaults. */
+typedef struct mcg_config {
+    int32_t cells_x, cells_y, cells_z, elements_per_strut;
+    double cell_size, min_radius, max_radius, joint_scale, trigger_scale;
+    double imperfection, member_imperfection;
+    mcg_material material;
+    double gravity, shear_correction, contact_stiffness, contact_margin, centering_stiffness;
+    int32_t contact_samples, load_steps, unload_steps, max_iterations, history, max_line_search;
+    double max_strain, step_time, translation_scale, max_translation_step, max_rotation_step;
+    double gradient_rms_tolerance, gradient_max_tolerance, armijo, min_line_step;
+    double penetration_tolerance;
+    int32_t max_adaptive_refinements, fps, frames, threads;
+    uint64_t seed;
+    /* Extensions (no reference counterpart). */
+    double relative_gradient_tolerance; /* > 0: converge when rms(g)/rms(g at iteration 0)
+                                           <= this, in place of the absolute test */
+    int32_t precision;                  /* enum mcg_precision */
+    int32_t self_contact;               /* 1 = on (reference behaviour), 0 = off */
+} mcg_config;
+
+void mcg_config_defaults(mcg_config* cfg);
+
+/* The model arrays the objective reads (Node/Beam, MC/include/sim.hpp:27-29). */
+typedef struct mcg_topology {
+    int32_t n_nodes, n_beams;
+    const int32_t* beam_a;      /* [B] */
+    const int32_t* beam_b;      /* [B] */
+    const double* L0;           /* [B] */
+    const double* radius;       /* [B] */
+    const double* area;         /* [B] */
+    const double* I;            /* [B] */
+    const double* J;            /* [B] */
+    const double* e0;           /* [3B] */
+    const double* mass;         /* [N] */
+    const uint8_t* locked;      /* [6N] */
+    int64_t n_connected;
+    const uint64_t* connected;  /* [n_connected] */
+} mcg_topology;
+
+/* Specimen scalars used by the load schedule and diagnostics
+ * (Simulator::width_/height_/depth_/area_/mass_/top0_, MC/include/sim.hpp:46). */
+typedef struct mcg_geometry {
+    double width, height, depth, area, mass, top0;
+} mcg_geometry;
+
+/* ObjectiveDiag, MC/include/sim.hpp:31. */
+typedef struct mcg_diag {
+    double elastic, plastic, contact, reaction, max_pen;
+    int32_t contacts, pad_;
+} mcg_diag;
+
+/* OptStats, MC/include/sim.hpp:33. */
+typedef struct mcg_optstats {
+    int32_t iterations, backtracks;
+    double rms, max, energy;
+    int32_t converged, pad_;
+} mcg_optstats;
+
+/* FrameDiagnostics, MC/include/sim.hpp:8-14 (one per accepted increment of run()). */
+typedef struct mcg_frame {
+    double time, platen_y, displacement, engineering_strain, engineering_stress, reaction_force;
+    double loading_work, recovered_work, dissipated_work, specific_energy_absorption;
+    double elastic_energy, plastic_dissipation, contact_energy, residual_rms, residual_max;
+    double max_penetration, mean_plastic_strain, max_plastic_strain, mean_plastic_rotation;
+    double max_plastic_rotation, permanent_set;
+    int32_t active_contacts, plastic_beams, plastic_hinges, iterations, converged, loading;
+    int32_t refinement, pad_;
+} mcg_frame;
+
+typedef struct mcg_ctx mcg_ctx;
+
+/* ---- context ------------------------------------------------------------------- */
+
+/* Creates a context on CUDA device `device` with its own stream.  Replaces the
+ * construction of the solver state in Simulator::Simulator (MC/src/sim.cpp:49); the
+ * configuration is copied.  translation_scale is used as given (the reference sets it
+ * to cell_size in its constructor; mcg_config_defaults does not). */
+int mcg_create(const mcg_config* cfg, int device, mcg_ctx** out);
+void mcg_destroy(mcg_ctx* ctx);
+const char* mcg_last_error(const mcg_ctx* ctx);
+const char* mcg_status_string(int status);
+int mcg_abi_version(void);
+
+/* Uploads the model (MC/src/sim.cpp:51-134 produce it in the reference).  Validates
+ * indices, lengths and the connected keys; builds the node incidence lists used by the
+ * deterministic gradient gather.  Resets the base state to the rest state
+ * base_x = x0, base_r = R0 when x0/R0 are given (NULL leaves the state undefined until
+ * mcg_set_state), and plastic state to zero. */
+int mcg_upload_topology(mcg_ctx* ctx, const mcg_topology* topo, const mcg_geometry* geom,
+                        const double* x0, const double* r0);
+
+/* Base configuration (baseX_/baseR_, MC/include/sim.hpp:46) and plastic state
+ * (Beam::plastic).  Any pointer may be NULL to leave that part unchanged. */
+int mcg_set_state(mcg_ctx* ctx, const double* base_x, const double* base_r,
+                  const double* plastic);
+int mcg_get_state(mcg_ctx* ctx, double* base_x, double* base_r, double* plastic);
+
+/* ---- the energy/gradient evaluation --------------------------------------------- */
+
+/* Simulator::objective(z, top, trials), MC/src/sim.cpp:138-172.
+ *   z [6N] in; energy, grad [6N], diag out (grad/diag may be NULL).
+ *   With trials != 0 the per-beam trial plastic state is kept on the device for
+ *   mcg_commit and, when the pointers are non-NULL, copied out:
+ *     trial_next [7B]  TrialBeam::next (layout as `plastic`)
+ *     trial_aux  [7B]  strain, stress, moment.x, moment.y, moment.z, elastic, dissipation
+ *     trial_flags[3B]  axialPlastic, bendPlastic, torsionPlastic
+ *   Non-finite energy gives energy = +inf and grad = 0, as the reference does. */
+int mcg_objective(mcg_ctx* ctx, const double* z, double top, int trials, double* energy,
+                  double* grad, mcg_diag* diag, double* trial_next, double* trial_aux,
+                  uint8_t* trial_flags);
+
+/* Device-resident form used for throughput measurement: mcg_upload_z copies z once;
+ * mcg_objective_resident evaluates at that z, leaving energy/grad on the device;
+ * mcg_read_result copies them out.  The same kernels as mcg_objective. */
+int mcg_upload_z(mcg_ctx* ctx, const double* z);
+int mcg_objective_resident(mcg_ctx* ctx, double top, int trials);
+int mcg_read_result(mcg_ctx* ctx, double* energy, double* grad, mcg_diag* diag);
+
+/* Contact pair set of the most recent evaluation, sorted ascending, as pair keys over
+ * shape indices (nodes 0..N-1 are joint spheres, N+b is beam b's capsule;
+ * MC/src/sim.cpp:148-150).  Platen contacts are not pairs and are not listed.
+ * With capacity too small: MCG_ERR_CAPACITY and *count = the needed size. */
+int mcg_contact_pairs(mcg_ctx* ctx, uint64_t* keys, int64_t capacity, int64_t* count);
+
+/* ---- the solver ---------------------------------------------------------------- */
+
+/* Simulator::minimize(top, z, final), MC/src/sim.cpp:174-211: L-BFGS with Armijo
+ * backtracking, steepest-descent retry and best-state fallback; vectors stay on the
+ * device.  z [6N] in/out.  The final evaluation (with trials) is kept for mcg_commit.
+ * final_diag / final_energy may be NULL. */
+int mcg_minimize(mcg_ctx* ctx, double top, double* z, mcg_optstats* stats,
+                 double* final_energy, mcg_diag* final_diag);
+
+/* Simulator::commit(z, final), MC/src/sim.cpp:212: re-bases base_x/base_r at the
+ * minimizer's z and writes the plastic state from its final trial evaluation. */
+int mcg_commit(mcg_ctx* ctx);
+
+/* Simulator::run(), MC/src/sim.cpp:374-467: tare, load_steps loading and unload_steps
+ * unloading increments with adaptive bisection, trapezoidal work and per-increment
+ * diagnostics.  frames [capacity] out; *count = accepted increments.  Returns
+ * MCG_ERR_EQUILIBRIUM where the reference throws; the frames accepted so far are
+ * returned.  With `verbose` one line per increment goes to stdout in the reference's
+ * format (MC/src/sim.cpp:441-451). */
+int mcg_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* count, int verbose);
+
+/* The CUDA stream the context launches on (a cudaStream_t), for callers that time
+ * or order work around it. */
+void* mcg_stream(mcg_ctx* ctx);
+
+/* Number of kernel launches this context has issued since creation. */
+int64_t mcg_launch_count(const mcg_ctx* ctx);
+
+/* ---- synthetic lattices (no reference counterpart; the reference's own builder is
+ *      MC/src/sim.cpp:51-135) --------------------------------------------------- */
+
+enum mcg_lattice_kind {
+    MCG_LATTICE_CUBIC = 0,     /* cell-edge struts */
+    MCG_LATTICE_CUBIC_BCC = 1, /* cell edges + 8 centre-to-corner half-diagonals per cell */
+};
+
+enum mcg_radius_mode {
+    MCG_RADIUS_GRADED_Y = 0,   /* linear in height from r0 (bottom) to r1 (top) */
+    MCG_RADIUS_UNIFORM = 1,    /* uniform random in [r0, r1] per strut */
+};
+
+typedef struct mcg_lattice_spec {
+    int32_t kind, radius_mode;
+    int32_t cells_x, cells_y, cells_z, pad_;
+    double cell_size, r0, r1;
+    double jitter;            /* node jitter amplitude as a fraction of cell_size */
+    uint64_t seed;
+} mcg_lattice_spec;
+
+/* Arrays of a generated lattice; the memory belongs to the lattice object. */
+typedef struct mcg_lattice_view {
+    int32_t n_nodes, n_beams;
+    int64_t n_connected;
+    const double* x0;       /* [3N] rest positions */
+    const double* r0;       /* [4N] rest orientations (identity) */
+    const int32_t* layer;   /* [N] */
+    const double* mass;     /* [N] */
+    const uint8_t* locked;  /* [6N] */
+    const int32_t* beam_a;
+    const int32_t* beam_b;
+    const double* L0;
+    const double* radius;
+    const double* area;
+    const double* I;
+    const double* J;
+    const double* e0;       /* [3B] */
+    const uint64_t* connected;
+    mcg_geometry geometry;
+} mcg_lattice_view;
+
+typedef struct mcg_lattice mcg_lattice;
+
+/* Builds a lattice; mass and locks follow the reference rules
+ * (Simulator::distributeMass, MC/src/sim.cpp:134) with cfg's density, joint_scale and
+ * max_radius. */
+int mcg_lattice_generate(const mcg_lattice_spec* spec, const mcg_config* cfg,
+                         mcg_lattice** out);
+int mcg_lattice_view_of(const mcg_lattice* lat, mcg_lattice_view* view);
+void mcg_lattice_free(mcg_lattice* lat);
+/* Fills a topology description that points into the lattice's arrays. */
+int mcg_lattice_topology(const mcg_lattice* lat, mcg_topology* topo);
+
+/* Seeded deformed state: z translations ~ N(0, sigma_t) (units of cell), rotation
+ * vectors with uniform axis and angle ~ N(0, sigma_r); plastic epsp ~ U[0, epsp_max],
+ * alpha = epsp, the rest zero.  Locked DOFs are zero.  Either output may be NULL. */
+int mcg_random_state(int32_t n_nodes, int32_t n_beams, const uint8_t* locked,
+                     double sigma_t, double sigma_r, double epsp_max, uint64_t seed,
+                     double* z, double* plastic);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MCG_H */
