@@ -1,0 +1,330 @@
+"""Throughput of the beam-lattice energy/gradient evaluation on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mcg|reference]
+                    [--workload bcc64|cubic6|bcc32|bcc128]
+
+A step is one full evaluation of the objective (energy + 6-DOF gradient: node state, beam
+mechanics with return mapping, self-contact broad/narrow phase, platen contact, gather)
+on the 64x64x32 cubic+BCC specimen at its seeded deformed state.  Metric: evaluations/s.
+
+value      device-resident: z already in HBM, result left in HBM (mcg_objective_resident).
+e2e        the public C-ABI call mcg_objective with pinned host buffers: z host->device,
+           energy + gradient device->host, every step.
+roofline   the beam kernel (the dominant kernel): algorithmic bytes per launch (128 B per
+           beam: end indices, L0, radius, area, I, J, e0 and the 7 plastic values, FP64)
+           over its CUDA-event time, against the measured HBM copy bandwidth.
+cpu_baseline  the CPU restatement of the reference objective (oracle/), one core, on a
+           bounded sample of the same lattice family, scaled by beam count.
+
+--impl reference times the reference's CPU implementation of the same evaluation (the
+oracle port where the reference cannot be built, i.e. on the GPU machine) on all host cores,
+one process per core, each evaluating a bounded sample, scaled by beam count.
+
+Multi-GPU: replicas only (every rank evaluates its own copy; no collective), weak scaling.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+BEAM_BYTES = 128    # per beam, FP64: a, b (2 x 4 B) + 15 reals
+NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6], locked[6]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mcg", choices=["mcg", "reference"])
+    ap.add_argument("--workload", default="bcc64")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name):
+    from falling_dice_gb300 import workloads
+    return getattr(workloads, name)()
+
+
+def sample_spec(name):
+    """A bounded CPU sample of the same lattice family (cells scaled down)."""
+    from falling_dice_gb300 import workloads
+    if name.startswith("bcc"):
+        return workloads.bcc((12, 12, 6))
+    return workloads.cubic6()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if not self.rows:
+            return None
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample_eval_seconds(name, repeat=1):
+    """One-core time of the reference objective (CPU restatement) on the bounded sample."""
+    import falling_dice_gb300 as fd
+    from oracle import oracle as orc
+    orc.build("mco")
+    cfg, spec = sample_spec(name)
+    lat = fd.generate_lattice(spec, cfg)
+    m = orc.Model("mco", cfg, lattice=lat)
+    from falling_dice_gb300 import workloads
+    z, pl = fd.random_state(lat, **workloads.DEFORM)
+    m.set_state(plastic=pl)
+    top = lat.geometry.top0 + 0.01
+    m.objective(z, top)
+    t = time.perf_counter()
+    for _ in range(repeat):
+        m.objective(z, top)
+    return (time.perf_counter() - t) / repeat, lat.n_beams, lat.n_nodes
+
+
+def _ref_worker(args):
+    name, repeat = args
+    sys.path.insert(0, ROOT)
+    return cpu_sample_eval_seconds(name, repeat)
+
+
+def run_reference(a, rank, world):
+    """--impl reference: the reference CPU objective on all host cores."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    cfg, spec = workload(a.workload)
+    import falling_dice_gb300 as fd
+    lat = fd.generate_lattice(spec, cfg)
+    B_full = lat.n_beams
+    cores = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        for _ in range(a.warmup if a.warmup < 1 else 1):
+            pool.map(_ref_worker, [(a.workload, 1)] * cores)
+        t0 = time.perf_counter()
+        res = []
+        for _ in range(a.steps):
+            res += pool.map(_ref_worker, [(a.workload, 1)] * cores)
+        wall = time.perf_counter() - t0
+    per_eval = float(np.mean([r[0] for r in res]))
+    B_s = res[0][1]
+    # each worker's time includes its lattice build; use the measured evaluation time, all
+    # cores in parallel: evals/s at full size = cores / (t_sample * B_full / B_sample)
+    value = cores / (per_eval * B_full / B_s)
+    sample = (f"{sample_spec(a.workload)[1].cells_x}x{sample_spec(a.workload)[1].cells_y}x"
+              f"{sample_spec(a.workload)[1].cells_z} cubic+BCC sample ({B_s} beams) of the same "
+              f"generator; per-evaluation time scaled by beam count to {B_full} beams")
+    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmcref.so")) else "port"
+    line = {"impl": "reference", "metric": "beam energy-grad evals/s", "value": value, "unit": "evals/s",
+            "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{a.workload}: {lat.n_nodes} nodes, {B_full} beams",
+                       "parallelism": f"{cores} CPU processes"},
+            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": kind,
+                             "sample": sample, "seconds_per_sample_eval": per_eval,
+                             "wall_s": wall},
+            "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_info()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    import torch
+    import falling_dice_gb300 as fd
+    from falling_dice_gb300 import workloads
+    if not os.path.exists(fd.LIB_PATH):
+        import __graft_entry__
+        __graft_entry__.build()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    cfg, spec = workload(a.workload)
+    lat = fd.generate_lattice(spec, cfg)
+    z, pl = fd.random_state(lat, **workloads.DEFORM)
+    sol = fd.Solver(cfg, lat, device=local)
+    sol.set_state(plastic=pl)
+    top = lat.geometry.top0 + 0.01
+    sol.upload_z(z)
+    stream = torch.cuda.ExternalStream(sol.stream, device=local)
+    N, B = lat.n_nodes, lat.n_beams
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident throughput ----
+    for _ in range(max(a.warmup, 3)):
+        sol.objective_resident(top)
+    barrier()
+    launches0 = sol.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(a.steps):
+        sol.objective_resident(top)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sol.launch_count() - launches0
+    clk = clocks.stop()
+    if pg is not None:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / a.steps
+    value = world * 1e3 / ms_step
+    res = sol.read_result(grad=False)
+
+    # ---- end to end through the public C ABI, pinned host buffers ----
+    zh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
+    zh.numpy()[:] = z
+    gh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
+    import ctypes as C
+    from falling_dice_gb300 import abi
+    eout = C.c_double()
+    diag = abi.Diag()
+    zp = C.cast(zh.data_ptr(), C.POINTER(C.c_double))
+    gp = C.cast(gh.data_ptr(), C.POINTER(C.c_double))
+    for _ in range(max(a.warmup, 3)):
+        sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
+    barrier()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(a.steps):
+        rc = sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
+        assert rc == 0
+    e1.record(stream)
+    barrier()
+    ms_e2e = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    if pg is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = world * 1e3 * a.steps / ms_e2e
+    assert np.isfinite(eout.value) and eout.value == res["energy"]
+
+    # ---- phase timing for the roofline (separate pass: it synchronizes per evaluation) ----
+    sol.set_timing(True)
+    for _ in range(max(3, min(a.steps, 10))):
+        sol.objective_resident(top)
+    phases, nev = sol.phase_times()
+    sol.set_timing(False)
+    per_phase = {k: v / nev for k, v in phases.items()}
+    peak, peak_kind = measured_peaks()
+    beam_bytes = BEAM_BYTES * B
+    beam_ms = per_phase["beams"]
+    achieved = beam_bytes / (beam_ms * 1e-3) / 1e9
+    eval_bytes = BEAM_BYTES * B + NODE_BYTES * N
+
+    if rank != 0:
+        return
+    cpu = None
+    if not a.no_cpu_baseline:
+        t_s, B_s, N_s = cpu_sample_eval_seconds(a.workload, repeat=2)
+        cs = sample_spec(a.workload)[1]
+        cpu = {"value": 1.0 / (t_s * B / B_s), "unit": "evals/s", "cores": 1, "kind": "port",
+               "sample": f"{cs.cells_x}x{cs.cells_y}x{cs.cells_z} cubic+BCC ({B_s} beams), 2 evaluations "
+                         f"of {t_s:.2f} s each, scaled by beam count to {B} beams",
+               "seconds_per_sample_eval": t_s}
+    line = {
+        "metric": "beam energy-grad evals/s", "value": value, "unit": "evals/s",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"{a.workload}: cubic+BCC {spec.cells_x}x{spec.cells_y}x{spec.cells_z}, "
+                               f"{N} nodes, {B} beams, seeded deformed state",
+                   "precision": "fp64 plain form", "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2 (beam arrays alone exceed 129 MB)"},
+        "hbm_gbs_algorithmic": eval_bytes * value / world / 1e9,
+        "phase_ms": per_phase,
+        "roofline": {"bound": "hbm", "kernel": "k_beams", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": None, "bytes_per_launch": beam_bytes, "ms_per_launch": beam_ms},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": 8 * 6 * N,
+                "d2h_bytes_per_step": 8 * 6 * N + 8},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "energy": res["energy"], "contacts": res["diag"]["contacts"],
+    }
+    print(json.dumps(line), flush=True)
+    sol.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,151 @@
+// common.cuh -- shared device helpers: FP64 vector/quaternion algebra, deterministic
+// block reductions, launch geometry.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mcg {
+
+constexpr int kBlock = 256;          // threads per CTA for the streaming kernels
+constexpr double kPiD = 3.1415926535897932384626433832795;
+
+// ---- FP64 3-vectors and quaternions ----------------------------------------------------
+// Same algebra as the reference's Vec3/Quat (MC/include/core.hpp:37-41): a vector divided
+// by s is a multiplication with 1/s, and rotation is v + w t + q x t with t = 2 q x v.
+struct d3 { double x, y, z; };
+struct q4 { double w, x, y, z; };
+
+__device__ __forceinline__ d3 mk3(double x, double y, double z) { return d3{x, y, z}; }
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ d3 operator-(d3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ d3 operator*(d3 a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ double len2(d3 v) { return dot(v, v); }
+__device__ __forceinline__ double len(d3 v) { return sqrt(len2(v)); }
+__device__ __forceinline__ d3 unit(d3 v) {
+    const double l2 = len2(v);
+    return (isfinite(l2) && l2 > 1e-30) ? v * (1.0 / sqrt(l2)) : d3{0, 1, 0};
+}
+__device__ __forceinline__ double clampd(double x, double lo, double hi) { return fmax(lo, fmin(hi, x)); }
+__device__ __forceinline__ double sqr(double x) { return x * x; }
+
+__device__ __forceinline__ q4 conj(q4 q) { return {q.w, -q.x, -q.y, -q.z}; }
+__device__ __forceinline__ q4 qnorm(q4 q) {
+    const double n = sqrt(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z);
+    if (n < 1e-30) return q4{1, 0, 0, 0};
+    return {q.w / n, q.x / n, q.y / n, q.z / n};
+}
+__device__ __forceinline__ q4 qmul(q4 a, q4 b) {
+    return {a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z,
+            a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y,
+            a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x,
+            a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w};
+}
+__device__ __forceinline__ d3 qrot(q4 q, d3 v) {
+    const d3 u{q.x, q.y, q.z};
+    const d3 t = cross(u, v) * 2.0;
+    return (v + t * q.w) + cross(u, t);
+}
+__device__ __forceinline__ d3 qrot_inv(q4 q, d3 v) { return qrot(conj(q), v); }
+
+// Unit quaternion of the rotation vector v (MC/include/core.hpp:51 quatExp, :42 quatAxisAngle).
+__device__ __forceinline__ q4 exp_map(d3 v) {
+    const double a = len(v);
+    if (a < 1e-12) return qnorm(q4{1 - .125 * a * a, .5 * v.x, .5 * v.y, .5 * v.z});
+    const d3 axis = unit(v * (1.0 / a));
+    double s, c;
+    sincos(.5 * a, &s, &c);
+    return qnorm(q4{c, axis.x * s, axis.y * s, axis.z * s});
+}
+// Rotation vector of a unit quaternion (MC/include/core.hpp:52 quatLog).
+__device__ __forceinline__ d3 log_map(q4 q) {
+    q = qnorm(q);
+    if (q.w < 0) q = q4{-q.w, -q.x, -q.y, -q.z};
+    const double s = sqrt(q.x * q.x + q.y * q.y + q.z * q.z);
+    if (s < 1e-12) return {2 * q.x, 2 * q.y, 2 * q.z};
+    const double a = 2 * atan2(s, clampd(q.w, -1, 1));
+    return d3{q.x, q.y, q.z} * (a / s);
+}
+// J_l^{-T}(p) v, the SO(3) left-Jacobian inverse transpose applied to v
+// (MC/include/core.hpp:53): v + p x v / 2 + A p x (p x v),
+// A = 1/a^2 - (1 + cos a) / (2 a sin a), with the series value 1/12 below a = 1e-7.
+__device__ __forceinline__ d3 jl_inv_t(d3 p, d3 v) {
+    const double a = len(p);
+    const d3 c1 = cross(p, v);
+    const d3 c2 = cross(p, c1);
+    double A;
+    if (a < 1e-7) {
+        A = 1.0 / 12.0;
+    } else {
+        double s, c;
+        sincos(a, &s, &c);
+        A = 1 / (a * a) - (1 + c) / (2 * a * s);
+    }
+    return (v + c1 * .5) + c2 * A;
+}
+
+// ---- deterministic reductions ------------------------------------------------------------
+// Fixed shuffle tree inside a warp, fixed order across warps: the same inputs in the same
+// threads always give the same bits.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Sums NV values per thread over the block; thread 0 receives the totals.  `smem` needs
+// NV * (blockDim.x / 32) doubles.  blockDim.x must be a multiple of 32.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = warp_sum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) smem[k * nw + warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0;
+            for (int w = 0; w < nw; w++) s += smem[k * nw + w];
+            v[k] = s;
+        }
+    __syncthreads();
+}
+
+__device__ __forceinline__ double block_max(double v, double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_max(v);
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = smem[0];
+        for (int w = 1; w < nw; w++) m = fmax(m, smem[w]);
+        v = m;
+    }
+    __syncthreads();
+    return v;
+}
+
+inline unsigned grid_for(long long n, int block = kBlock) {
+    long long g = (n + block - 1) / block;
+    return unsigned(g < 1 ? 1 : g);
+}
+
+}  // namespace mcg

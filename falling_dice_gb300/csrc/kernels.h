@@ -1,0 +1,170 @@
+// kernels.h -- device data layout and the host-side launchers of the CUDA kernels.
+//
+// HBM layout (one context = one lattice):
+//   per beam (SoA, FP64): L0, area, radius, e0[3 arrays], and the section constants the
+//     reference recomputes on every call (E I/L0, G J/L0, yield moments, hardening
+//     moduli, shear and axial energy scales), precomputed once with the reference's own
+//     expressions so they are bit-identical; plastic state as 7 SoA arrays.
+//   per node: base position (3 FP64, AoS), base orientation (4 FP64, AoS), current
+//     position/orientation as 32-byte double4_32a records so each beam-end gather is one
+//     sector; the 6-DOF z/grad vectors in the ABI layout.
+//   incidence CSR: for every node the beams touching it in ascending beam order, as
+//     (beam << 1 | role) -- the order the reference's scatter adds them in.
+//   per-beam gradient slots: the beam kernel writes, for each end, the 6-vector it adds to
+//     that end's node, and the gather sums them per node; no atomics anywhere on the
+//     gradient path, so every evaluation is bitwise reproducible.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+
+namespace mcg {
+
+struct Material {
+    double E, G, sy, H, bend_h, torsion_h;
+};
+
+struct DevTopo {
+    int N, B;
+    const int2* ab;
+    const double *L0, *area, *radius;
+    const double *e0x, *e0y, *e0z;
+    const double *kb, *kt, *my, *ty, *hb, *ht, *cs, *aL, *aLsy;
+    const double* mass;
+    const uint8_t* locked;    // [6N]
+    const int* inc_start;     // [N+1]
+    const int* inc;           // [2B]
+    const int* conn_start;    // [N+1] connected-pair adjacency (both directions, sorted)
+    const int* conn_nbr;
+};
+
+struct PhysParams {
+    double translation_scale, gravity, centering, contact_k, contact_margin, joint_radius;
+    double broad_cell, top;
+    int self_contact;
+};
+
+// Totals of one evaluation, written by the finalize kernel.
+struct EvalOut {
+    double energy, elastic, plastic, contact, reaction, max_pen;
+    int contacts, nonfinite;
+    double beam_energy, node_energy, center_energy, contact_energy, platen_energy;
+    long long entries, candidates;   // broad-phase statistics
+    int overflow, pad_;
+};
+
+// Device scratch of the contact pipeline.
+struct ContactBufs {
+    // per shape (N + B)
+    int4* cell_lo;          // [S] first cell (i, j, k) relative to the grid origin
+    int4* cell_hi;          // [S] last cell
+    float4* bb_lo;          // [S] fp32 AABB, rounded outward
+    float4* bb_hi;
+    uint32_t* count;        // [S+1] cells per shape
+    uint32_t* offset;       // [S+1]
+    int* grid;              // [8]: origin i,j,k; dims i,j,k; Morton bits; valid
+    // (cell key, shape) entries, double-buffered for the radix sort
+    uint64_t* keys[2];
+    uint32_t* vals[2];
+    long long entry_cap;
+    uint32_t* ccount;       // [entry_cap + 1] contacts found per entry
+    uint32_t* coffset;      // [entry_cap + 1]
+    // contacts, in deterministic (cell, shape, shape) order
+    long long contact_cap;
+    uint32_t* c_a;          // lower shape index
+    uint32_t* c_b;          // higher shape index
+    double* c_s;            // closest-point parameters on a and b
+    double* c_t;
+    double* c_n;            // [3 * cap] unit normal from a to b
+    double* c_pen;          // penetration
+    // per-node contact force lists (CSR built per evaluation)
+    uint32_t* n_count;      // [N+1]
+    uint32_t* n_start;      // [N+1]
+    uint32_t* n_cursor;     // [N]
+    uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot)
+    double* part;           // [3 * contact_part_blocks] energy, max penetration, count
+    void* sort_tmp;
+    size_t sort_tmp_bytes;
+    uint32_t* dev_total;    // [4] flags: [2] bit0 coarsen grid, bit1 non-finite shape
+};
+
+struct EvalBufs {
+    double4_32a* x;             // [N]
+    double4_32a* R;             // [N]
+    double* slotA;          // [6B] (-F, Ga) per beam, added to node a
+    double* slotB;          // [6B] (+F, Gb) per beam, added to node b
+    double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
+    double* part_beam;      // [3 * nb_beams]
+    double* part_node;      // [5 * nb_nodes]
+    double* cen;            // [9] mean, min, max of the node positions
+    EvalOut* out;
+    double* trial_next;     // [7B] SoA
+    double* trial_aux;      // [7B] SoA
+    uint8_t* trial_flags;   // [3B] SoA
+};
+
+// ---- launch accounting -------------------------------------------------------------------
+extern std::atomic<long long> g_launch_count;
+inline void note_launches(int k) { g_launch_count += k; }
+
+// ---- launchers (objective.cu) ----------------------------------------------------------
+int nb_nodes(int N);
+int nb_beams(int B);
+void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
+                  const double* base_r, EvalBufs& e, cudaStream_t s);
+void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials,
+                  EvalBufs& e, cudaStream_t s);
+void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
+                   EvalBufs& e, cudaStream_t s);
+void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
+                     EvalBufs& e, cudaStream_t s);
+void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic,
+                   cudaStream_t s);
+// out6: sum|epsp|, max|epsp|, sum|rotp|, max|rotp|, #|epsp|>1e-5, #|rotp|>1e-4
+void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s);
+
+// ---- contact pipeline (contact.cu) ------------------------------------------------------
+int contact_part_blocks(long long contact_cap);
+// grid + per-shape cell ranges + scan of the per-shape cell counts
+void contact_shapes(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
+                    cudaStream_t s);
+// entries -> radix sort -> contacts per entry -> scan; returns the sort buffer index
+int contact_sort_and_count(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c,
+                           long long entries, int key_bits, cudaStream_t s);
+// writes the contact list, its reduction and the per-node force lists
+void contact_emit(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, long long entries,
+                  int res, long long ncontacts, cudaStream_t s);
+
+// ---- scan / radix sort (sort.cu) --------------------------------------------------------
+size_t scan_tmp_bytes(long long n);
+// Exclusive scan of n uint32 values; out[n] receives the total.
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+size_t radix_tmp_bytes(long long n);
+// Stable LSD radix sort of (key, value) pairs on bits [0, end_bit); returns the buffer
+// index (0 or 1) holding the result.
+int radix_sort_u64(uint64_t* keys[2], uint32_t* vals[2], long long n, int end_bit, void* tmp,
+                   const uint32_t* n_dev, cudaStream_t s);
+
+// ---- L-BFGS vector kernels (lbfgs.cu) ----------------------------------------------------
+size_t lbfgs_part_doubles();
+// k (1..3) dot products a_k . b_k into out[0..k-1] (device)
+void dots(int k, const double* a0, const double* b0, const double* a1, const double* b1, const double* a2,
+          const double* b2, long long n, double* part, double* out, cudaStream_t s);
+void rms_max(const double* g, const uint8_t* locked, long long n, long long n_free, double* part, double* out2,
+             cudaStream_t s);
+void vcopy(double* dst, const double* src, long long n, cudaStream_t s);
+// L-BFGS two-loop recursion (sim.cpp:184-187) into p, history oldest first
+void two_loop(double* p, const double* g, const double* const* S, const double* const* Y, const double* const* rho,
+              int m, double* alpha, double* scal, double* part, long long n, cudaStream_t s);
+// p = clamp(lock(-src)) per node (sim.cpp:188-190, 46)
+void finish_direction(double* p, const double* src, const uint8_t* locked, int N, double mt, double mr,
+                      cudaStream_t s);
+void candidate(double* zc, const double* z, const double* p, double step, const uint8_t* locked, long long n,
+               cudaStream_t s);
+void make_sy(double* sv, double* yv, const double* zc, const double* z, const double* gc, const double* g,
+             long long n, cudaStream_t s);
+void set_rho(double* rho, const double* sy, cudaStream_t s);
+
+}  // namespace mcg

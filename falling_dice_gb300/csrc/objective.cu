@@ -1,0 +1,512 @@
+// objective.cu -- FP64 kernels of the energy/gradient evaluation
+// (the reference's Simulator::state + objective, MC/src/sim.cpp:136-172).
+//
+//   k_state    per node: z -> current position/orientation; block partial sums of x
+//   k_center   one block: mean position for the centering term
+//   k_beams    per beam: axial/shear/bending/torsion energy with return mapping,
+//              the two end 6-vectors of its gradient, optional trial state
+//   k_gather   per node: deterministic CSR sum of the incident beams' end vectors in
+//              ascending beam order, gravity, centering, self-contact contributions
+//              (sorted), platen contact; packs, scales and locks the 6-DOF gradient
+//   k_finalize one block: fixed-order totals, diagnostics, non-finite guard
+#include "common.cuh"
+#include "kernels.h"
+
+namespace mcg {
+
+int nb_nodes(int N) { return int(grid_for(N)); }
+int nb_beams(int B) { return int(grid_for(B)); }
+
+// ---- node state: MC/src/sim.cpp:136 -------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uint8_t* __restrict__ locked,
+                                                  const double* __restrict__ z, const double* __restrict__ bx,
+                                                  const double* __restrict__ br, double4_32a* __restrict__ x4,
+                                                  double4_32a* __restrict__ R4, double* __restrict__ part) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[3] = {0, 0, 0};
+    const double ninf = __longlong_as_double(0xfff0000000000000LL);
+    double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+    if (i < N) {
+        const double* zi = z + 6 * size_t(i);
+        const uint8_t* li = locked + 6 * size_t(i);
+        double t[3], r[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            t[d] = li[d] ? 0.0 : zi[d];
+            r[d] = li[d + 3] ? 0.0 : zi[d + 3];
+        }
+        // x = base + s t, rounded exactly as the reference (no fused multiply-add), so that
+        // positions -- and with them the contact pair set -- are bit-identical.
+        const double ts = p.translation_scale;
+        const double xx = __dadd_rn(bx[3 * size_t(i)], __dmul_rn(ts, t[0]));
+        const double xy = __dadd_rn(bx[3 * size_t(i) + 1], __dmul_rn(ts, t[1]));
+        const double xz = __dadd_rn(bx[3 * size_t(i) + 2], __dmul_rn(ts, t[2]));
+        const q4 b{br[4 * size_t(i)], br[4 * size_t(i) + 1], br[4 * size_t(i) + 2], br[4 * size_t(i) + 3]};
+        const q4 R = qnorm(qmul(exp_map(d3{r[0], r[1], r[2]}), b));
+        x4[i] = make_double4_32a(xx, xy, xz, 0.0);
+        R4[i] = make_double4_32a(R.w, R.x, R.y, R.z);
+        acc[0] = xx; acc[1] = xy; acc[2] = xz;
+        // bounding box for the contact grid; fmin/fmax skip NaN coordinates
+        mx[0] = -xx; mx[1] = -xy; mx[2] = -xz; mx[3] = xx; mx[4] = xy; mx[5] = xz;
+    }
+    block_sum<3>(acc, sm);
+#pragma unroll
+    for (int k = 0; k < 6; k++) mx[k] = block_max(mx[k], smx);
+    if (threadIdx.x == 0) {
+        double* q = part + 9 * size_t(blockIdx.x);
+        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[3 + k] = mx[k];
+    }
+}
+
+// Mean position over all nodes (MC/src/sim.cpp:143) and the node bounding box, from the
+// k_state partials: cen[0..2] mean, cen[3..5] minimum, cen[6..8] maximum.
+__global__ void __launch_bounds__(kBlock) k_center(int N, int nparts, const double* __restrict__ part,
+                                                   double* __restrict__ cen) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    double acc[3] = {0, 0, 0};
+    const double ninf = __longlong_as_double(0xfff0000000000000LL);
+    double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+        const double* q = part + 9 * size_t(k);
+        acc[0] += q[0]; acc[1] += q[1]; acc[2] += q[2];
+#pragma unroll
+        for (int j = 0; j < 6; j++) mx[j] = fmax(mx[j], q[3 + j]);
+    }
+    block_sum<3>(acc, sm);
+#pragma unroll
+    for (int j = 0; j < 6; j++) mx[j] = block_max(mx[j], smx);
+    if (threadIdx.x == 0) {
+        const double inv = 1.0 / double(N);
+        cen[0] = acc[0] * inv; cen[1] = acc[1] * inv; cen[2] = acc[2] * inv;
+        cen[3] = -mx[0]; cen[4] = -mx[1]; cen[5] = -mx[2];
+        cen[6] = mx[3]; cen[7] = mx[4]; cen[8] = mx[5];
+    }
+}
+
+// ---- constitutive return maps: MC/src/sim.cpp:5-8 ------------------------------------------
+struct Ret1 { double force, p, a, dg, energy, hard; bool yielded; };
+__device__ __forceinline__ Ret1 return1(double total, double pc, double ac, double k, double y, double H) {
+    Ret1 r;
+    const double trial = k * (total - pc);
+    const double f = fabs(trial) - (y + H * ac);
+    if (f > 0) {
+        const double s = trial >= 0 ? 1.0 : -1.0;
+        r.dg = f / fmax(1e-20, k + H);
+        r.p = pc + s * r.dg;
+        r.a = ac + r.dg;
+        r.yielded = true;
+    } else {
+        r.dg = 0; r.p = pc; r.a = ac; r.yielded = false;
+    }
+    r.force = k * (total - r.p);
+    r.energy = .5 * k * sqr(total - r.p);
+    r.hard = .5 * H * sqr(r.a);
+    return r;
+}
+struct Ret3 { d3 force, p; double a, dg, energy, hard; bool yielded; };
+__device__ __forceinline__ Ret3 return3(d3 t, d3 pc, double ac, double k, double y, double H) {
+    Ret3 r;
+    const d3 trial = (t - pc) * k;
+    const double n = len(trial);
+    const double f = n - (y + H * ac);
+    if (f > 0 && n > 1e-20) {
+        const d3 d = trial * (1.0 / n);
+        r.dg = f / fmax(1e-20, k + H);
+        r.p = pc + d * r.dg;
+        r.a = ac + r.dg;
+        r.yielded = true;
+    } else {
+        r.dg = 0; r.p = pc; r.a = ac; r.yielded = false;
+    }
+    r.force = (t - r.p) * k;
+    r.energy = .5 * k * len2(t - r.p);
+    r.hard = .5 * H * sqr(r.a);
+    return r;
+}
+
+__device__ __forceinline__ q4 ldq(const double4_32a* R, int i) {
+    const double4_32a v = R[i];
+    return q4{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ d3 ldx(const double4_32a* x, int i) {
+    const double4_32a v = x[i];
+    return d3{v.x, v.y, v.z};
+}
+
+// ---- beam kernel: MC/src/sim.cpp:139-141 ---------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const double* __restrict__ plastic,
+                                                  int trials, EvalBufs e) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int B = t.B;
+    double acc[3] = {0, 0, 0};  // energy, elastic, plastic
+    if (b < B) {
+        const int2 ab = t.ab[b];
+        const d3 xa = ldx(e.x, ab.x), xb = ldx(e.x, ab.y);
+        const d3 d = xb - xa;
+        const double L = len(d);
+        double* sa = e.slotA + 6 * size_t(b);
+        double* sb = e.slotB + 6 * size_t(b);
+        if (L < 1e-10) {
+            // Degenerate element: penalty energy only, no gradient and a default trial.
+            acc[0] = 1e8 * sqr(1e-10 - L);
+#pragma unroll
+            for (int k = 0; k < 6; k++) { sa[k] = 0; sb[k] = 0; }
+            if (trials) {
+#pragma unroll
+                for (int k = 0; k < 7; k++) { e.trial_next[k * size_t(B) + b] = 0; e.trial_aux[k * size_t(B) + b] = 0; }
+#pragma unroll
+                for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
+            }
+        } else {
+            const double L0 = t.L0[b];
+            const double pl_epsp = plastic[b], pl_alpha = plastic[size_t(B) + b];
+            const d3 rotp{plastic[2 * size_t(B) + b], plastic[3 * size_t(B) + b], plastic[4 * size_t(B) + b]};
+            const double pl_alphaB = plastic[5 * size_t(B) + b], pl_alphaT = plastic[6 * size_t(B) + b];
+            const d3 tt = d * (1.0 / L);
+            // axial
+            const double eps = (L - L0) / L0;
+            const Ret1 ax = return1(eps, pl_epsp, pl_alpha, m.E, m.sy, m.H);
+            const double aL = t.aL[b];
+            const double uax = aL * (ax.energy + ax.hard);
+            const double dax = t.aLsy[b] * ax.dg;
+            const double Nf = t.area[b] * ax.force;
+            d3 F = tt * Nf;
+            // shear: the end directors against the chord
+            const q4 Ra = ldq(e.R, ab.x), Rb = ldq(e.R, ab.y);
+            const d3 e0{t.e0x[b], t.e0y[b], t.e0z[b]};
+            const d3 da = qrot(Ra, e0), db = qrot(Rb, e0);
+            const double cs = t.cs[b];
+            const d3 ma = da - tt, mb = db - tt;
+            const double us = .5 * cs * (len2(ma) + len2(mb));
+            const d3 gt = ((tt * 2.0 - da) - db) * cs;
+            const d3 trans = (gt - tt * dot(gt, tt)) * (1.0 / L);
+            F = F + trans;
+            d3 Ga = -(cross(da, tt) * cs);
+            d3 Gb = -(cross(db, tt) * cs);
+            // bending and torsion from the relative rotation
+            const q4 Q = qnorm(qmul(conj(Ra), Rb));
+            const d3 phi = log_map(Q);
+            const d3 axis = unit(qrot_inv(Ra, tt));
+            const double tw = dot(phi, axis), ptw = dot(rotp, axis);
+            const d3 bend = phi - axis * tw, pb = rotp - axis * ptw;
+            const double kb = t.kb[b], kt = t.kt[b], my = t.my[b], ty = t.ty[b];
+            const Ret3 br = return3(bend, pb, pl_alphaB, kb, my, t.hb[b]);
+            const Ret1 tor = return1(tw, ptw, pl_alphaT, kt, ty, t.ht[b]);
+            const d3 moment = br.force + axis * tor.force;
+            const double ur = br.energy + br.hard + tor.energy + tor.hard;
+            const double dr = my * br.dg + ty * tor.dg;
+            const d3 world = qrot(Ra, jl_inv_t(phi, moment));
+            Ga = Ga - world;
+            Gb = Gb + world;
+            acc[0] = (uax + dax) + us + (ur + dr);
+            acc[1] = uax + us + ur;
+            acc[2] = dax + dr;
+            sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
+            sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
+            if (trials) {
+                const size_t S = size_t(B);
+                const d3 nrot = br.p + axis * tor.p;
+                e.trial_next[b] = ax.p;
+                e.trial_next[S + b] = ax.a;
+                e.trial_next[2 * S + b] = nrot.x;
+                e.trial_next[3 * S + b] = nrot.y;
+                e.trial_next[4 * S + b] = nrot.z;
+                e.trial_next[5 * S + b] = br.a;
+                e.trial_next[6 * S + b] = tor.a;
+                e.trial_aux[b] = eps;
+                e.trial_aux[S + b] = ax.force;
+                e.trial_aux[2 * S + b] = moment.x;
+                e.trial_aux[3 * S + b] = moment.y;
+                e.trial_aux[4 * S + b] = moment.z;
+                e.trial_aux[5 * S + b] = uax + us + ur;
+                e.trial_aux[6 * S + b] = dax + dr;
+                e.trial_flags[b] = ax.yielded;
+                e.trial_flags[S + b] = br.yielded;
+                e.trial_flags[2 * S + b] = tor.yielded;
+            }
+        }
+    }
+    block_sum<3>(acc, sm);
+    if (threadIdx.x == 0) {
+        e.part_beam[3 * blockIdx.x] = acc[0];
+        e.part_beam[3 * blockIdx.x + 1] = acc[1];
+        e.part_beam[3 * blockIdx.x + 2] = acc[2];
+    }
+}
+
+// Contribution of one contact slot to its node (MC/src/sim.cpp:23 addShapeGradient):
+// slots 0/1 are shape a's ends, 2/3 shape b's; capsule ends split the force (1-u, u).
+__device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const PhysParams& p, int N,
+                                                 uint32_t item) {
+    const uint32_t ci = item >> 2, slot = item & 3u;
+    const d3 n{c.c_n[3 * size_t(ci)], c.c_n[3 * size_t(ci) + 1], c.c_n[3 * size_t(ci) + 2]};
+    const double mag = p.contact_k * c.c_pen[ci];
+    const bool side_b = slot >= 2;
+    const uint32_t shape = side_b ? c.c_b[ci] : c.c_a[ci];
+    const bool capsule = shape >= uint32_t(N);
+    const d3 v = n * (side_b ? -mag : mag);
+    if (!capsule) return v;
+    const double u = side_b ? c.c_t[ci] : c.c_s[ci];
+    return (slot & 1u) ? v * u : v * (1 - u);
+}
+
+// ---- per-node gather: the scatter of MC/src/sim.cpp:139-172, as a deterministic CSR sum ---
+__global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
+                                                   EvalBufs e, double* __restrict__ grad) {
+    __shared__ double sm[4 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int N = t.N;
+    double acc[4] = {0, 0, 0, 0};  // gravity energy, platen energy, reaction, platen contacts
+    double pen_max = 0;
+    if (i < N) {
+        d3 gx{0, 0, 0}, gr{0, 0, 0};
+        const int k0 = t.inc_start[i], k1 = t.inc_start[i + 1];
+        for (int k = k0; k < k1; k++) {
+            const int v = t.inc[k];
+            const double* s = ((v & 1) ? e.slotB : e.slotA) + 6 * size_t(v >> 1);
+            gx.x += s[0]; gx.y += s[1]; gx.z += s[2];
+            gr.x += s[3]; gr.y += s[4]; gr.z += s[5];
+        }
+        const d3 xi = ldx(e.x, i);
+        // gravity (sim.cpp:142)
+        const double mg = t.mass[i] * p.gravity;
+        acc[0] = mg * xi.y;
+        gx.y += mg;
+        // centering (sim.cpp:143)
+        gx.x += p.centering * e.cen[0] / double(N);
+        gx.z += p.centering * e.cen[2] / double(N);
+        // self-contact forces on this node, in ascending (contact, slot) order
+        if (use_contacts) {
+            const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
+            if (cnt <= 16) {
+                uint32_t items[16];
+                for (uint32_t k = 0; k < cnt; k++) items[k] = c.n_items[s0 + k];
+                for (uint32_t a = 1; a < cnt; a++) {  // insertion sort
+                    const uint32_t v = items[a];
+                    uint32_t q = a;
+                    while (q > 0 && items[q - 1] > v) { items[q] = items[q - 1]; q--; }
+                    items[q] = v;
+                }
+                for (uint32_t k = 0; k < cnt; k++) gx = gx + contact_slot_force(c, p, N, items[k]);
+            } else {
+                // long list: repeated minimum selection keeps the same order without storage
+                long long last = -1;
+                for (uint32_t k = 0; k < cnt; k++) {
+                    uint32_t best = 0xffffffffu;
+                    for (uint32_t q = 0; q < cnt; q++) {
+                        const uint32_t v = c.n_items[s0 + q];
+                        if ((long long)v > last && v < best) best = v;
+                    }
+                    gx = gx + contact_slot_force(c, p, N, best);
+                    last = best;
+                }
+            }
+        }
+        // platens (sim.cpp:168-171)
+        const double jr = p.joint_radius, kc = p.contact_k;
+        const double pb = jr - xi.y;
+        if (pb > 0) {
+            const double mm = kc * pb;
+            acc[1] += .5 * kc * pb * pb;
+            pen_max = fmax(pen_max, pb);
+            acc[3] += 1;
+            gx.y -= mm;
+        }
+        const double pt = xi.y + jr - p.top;
+        if (pt > 0) {
+            const double mm = kc * pt;
+            acc[1] += .5 * kc * pt * pt;
+            acc[2] += mm;
+            pen_max = fmax(pen_max, pt);
+            acc[3] += 1;
+            gx.y += mm;
+        }
+        // pack, scale and lock (sim.cpp:172)
+        const double ts = p.translation_scale;
+        const uint8_t* li = t.locked + 6 * size_t(i);
+        double* g = grad + 6 * size_t(i);
+        g[0] = li[0] ? 0.0 : ts * gx.x;
+        g[1] = li[1] ? 0.0 : ts * gx.y;
+        g[2] = li[2] ? 0.0 : ts * gx.z;
+        g[3] = li[3] ? 0.0 : gr.x;
+        g[4] = li[4] ? 0.0 : gr.y;
+        g[5] = li[5] ? 0.0 : gr.z;
+    }
+    block_sum<4>(acc, sm);
+    pen_max = block_max(pen_max, smx);
+    if (threadIdx.x == 0) {
+        double* q = e.part_node + 5 * size_t(blockIdx.x);
+        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = pen_max; q[4] = acc[3];
+    }
+}
+
+// ---- totals and the non-finite guard ---------------------------------------------------------
+__global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, PhysParams p,
+                                                     const double* __restrict__ pbeam,
+                                                     const double* __restrict__ pnode,
+                                                     const double* __restrict__ pcont,
+                                                     const double* __restrict__ cen, EvalOut* out) {
+    __shared__ double sm[6 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
+    double cacc[3] = {0, 0, 0};          // contactE, contacts(platen), contacts(self)
+    double pmax = 0;
+    for (int k = threadIdx.x; k < nbb; k += blockDim.x) {
+        acc[0] += pbeam[3 * k]; acc[1] += pbeam[3 * k + 1]; acc[2] += pbeam[3 * k + 2];
+    }
+    for (int k = threadIdx.x; k < nbn; k += blockDim.x) {
+        acc[3] += pnode[5 * k]; acc[4] += pnode[5 * k + 1]; acc[5] += pnode[5 * k + 2];
+        pmax = fmax(pmax, pnode[5 * k + 3]);
+        cacc[1] += pnode[5 * k + 4];
+    }
+    for (int k = threadIdx.x; k < ncp; k += blockDim.x) {
+        cacc[0] += pcont[3 * k];
+        pmax = fmax(pmax, pcont[3 * k + 1]);
+        cacc[2] += pcont[3 * k + 2];
+    }
+    block_sum<6>(acc, sm);
+    block_sum<3>(cacc, sm);
+    pmax = block_max(pmax, smx);
+    if (threadIdx.x == 0) {
+        const double center = .5 * p.centering * (sqr(cen[0]) + sqr(cen[2]));
+        const double contactE = cacc[0];
+        // Group order of the reference's accumulation: beams, gravity, centering,
+        // self-contact, platens (sim.cpp:139-171).
+        double energy = acc[0];
+        energy += acc[3];
+        energy += center;
+        energy += contactE;
+        energy += acc[4];
+        const int nonfinite = isfinite(energy) ? 0 : 1;
+        out->energy = nonfinite ? __longlong_as_double(0x7ff0000000000000LL) : energy;
+        out->elastic = acc[1];
+        out->plastic = acc[2];
+        out->contact = contactE + acc[4];
+        out->reaction = acc[5];
+        out->max_pen = pmax;
+        out->contacts = int(cacc[1] + cacc[2]);
+        out->nonfinite = nonfinite;
+        out->beam_energy = acc[0];
+        out->node_energy = acc[3];
+        out->center_energy = center;
+        out->contact_energy = contactE;
+        out->platen_energy = acc[4];
+    }
+}
+
+// Non-finite energy: the whole gradient is zero (sim.cpp:172).
+__global__ void k_zero_if_nonfinite(long long n, const EvalOut* out, double* grad) {
+    if (!out->nonfinite) return;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        grad[k] = 0;
+}
+
+// ---- commit (MC/src/sim.cpp:212): base state <- current state, plastic <- trial ----------
+__global__ void __launch_bounds__(kBlock) k_commit_nodes(int N, const double4_32a* __restrict__ x4,
+                                                         const double4_32a* __restrict__ R4, double* __restrict__ bx,
+                                                         double* __restrict__ br) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double4_32a x = x4[i], r = R4[i];
+    bx[3 * size_t(i)] = x.x; bx[3 * size_t(i) + 1] = x.y; bx[3 * size_t(i) + 2] = x.z;
+    br[4 * size_t(i)] = r.x; br[4 * size_t(i) + 1] = r.y; br[4 * size_t(i) + 2] = r.z; br[4 * size_t(i) + 3] = r.w;
+}
+
+// Plastic statistics of the committed state (MC/src/sim.cpp:339-362): sum and max of
+// |epsp|, sum and max of |rotp|, counts above 1e-5 and 1e-4.
+__global__ void __launch_bounds__(kBlock) k_plastic_part(int B, const double* __restrict__ pl, double* __restrict__ part) {
+    __shared__ double sm[4 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    double acc[4] = {0, 0, 0, 0};
+    double m0 = 0, m1 = 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        const double pa = fabs(pl[b]);
+        const d3 r{pl[2 * size_t(B) + b], pl[3 * size_t(B) + b], pl[4 * size_t(B) + b]};
+        const double pr = len(r);
+        acc[0] += pa; acc[1] += pr;
+        acc[2] += pa > 1e-5 ? 1.0 : 0.0;
+        acc[3] += pr > 1e-4 ? 1.0 : 0.0;
+        m0 = fmax(m0, pa); m1 = fmax(m1, pr);
+    }
+    block_sum<4>(acc, sm);
+    m0 = block_max(m0, smx);
+    m1 = block_max(m1, smx);
+    if (threadIdx.x == 0) {
+        double* q = part + 6 * size_t(blockIdx.x);
+        q[0] = acc[0]; q[1] = m0; q[2] = acc[1]; q[3] = m1; q[4] = acc[2]; q[5] = acc[3];
+    }
+}
+__global__ void __launch_bounds__(kBlock) k_plastic_final(int nparts, const double* __restrict__ part,
+                                                          double* __restrict__ out) {
+    __shared__ double sm[4 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    double acc[4] = {0, 0, 0, 0};
+    double m0 = 0, m1 = 0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+        const double* q = part + 6 * size_t(k);
+        acc[0] += q[0]; acc[1] += q[2]; acc[2] += q[4]; acc[3] += q[5];
+        m0 = fmax(m0, q[1]); m1 = fmax(m1, q[3]);
+    }
+    block_sum<4>(acc, sm);
+    m0 = block_max(m0, smx);
+    m1 = block_max(m1, smx);
+    if (threadIdx.x == 0) {
+        out[0] = acc[0]; out[1] = m0; out[2] = acc[1]; out[3] = m1; out[4] = acc[2]; out[5] = acc[3];
+    }
+}
+
+// ---- launchers ------------------------------------------------------------------------------
+void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
+                  const double* base_r, EvalBufs& e, cudaStream_t s) {
+    const int nb = nb_nodes(t.N);
+    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.part_state);
+    k_center<<<1, kBlock, 0, s>>>(t.N, nb, e.part_state, e.cen);
+    note_launches(2);
+}
+
+void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic, cudaStream_t s) {
+    k_commit_nodes<<<grid_for(N), kBlock, 0, s>>>(N, e.x, e.R, base_x, base_r);
+    note_launches(1);
+    if (B > 0) cudaMemcpyAsync(plastic, e.trial_next, 7 * size_t(B) * sizeof(double), cudaMemcpyDeviceToDevice, s);
+}
+
+void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s) {
+    constexpr int nparts = 64;
+    k_plastic_part<<<nparts, kBlock, 0, s>>>(B, plastic, part);
+    k_plastic_final<<<1, kBlock, 0, s>>>(nparts, part, out6);
+    note_launches(2);
+}
+
+void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials, EvalBufs& e,
+                  cudaStream_t s) {
+    if (t.B == 0) return;
+    k_beams<<<nb_beams(t.B), kBlock, 0, s>>>(t, m, plastic, trials ? 1 : 0, e);
+    note_launches(1);
+}
+
+void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
+                   cudaStream_t s) {
+    ContactBufs cc{};
+    if (c) cc = *c;
+    k_gather<<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
+    note_launches(1);
+}
+
+void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
+                     cudaStream_t s) {
+    const int ncp = c ? contact_part_blocks(c->contact_cap) : 0;
+    k_finalize<<<1, kBlock, 0, s>>>(t.B ? nb_beams(t.B) : 0, nb_nodes(t.N), ncp, p, e.part_beam, e.part_node,
+                                    c ? c->part : nullptr, e.cen, e.out);
+    const long long n = 6LL * t.N;
+    k_zero_if_nonfinite<<<grid_for(n < 152 * 4 * kBlock ? n : 152 * 4 * kBlock), kBlock, 0, s>>>(n, e.out, grad);
+    note_launches(2);
+}
+
+}  // namespace mcg

@@ -208,8 +208,15 @@ int mcg_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* count, i
  * or order work around it. */
 void* mcg_stream(mcg_ctx* ctx);
 
-/* Number of kernel launches this context has issued since creation. */
+/* Number of kernel launches the library has issued in this process. */
 int64_t mcg_launch_count(const mcg_ctx* ctx);
+
+/* Per-phase timing of evaluations with CUDA events on the context stream (no reference
+ * counterpart).  While on, every evaluation synchronizes at its end and adds its phase
+ * durations: [0] node state, [1] beam kernel, [2] self-contact pipeline, [3] gradient
+ * gather, [4] totals.  mcg_set_timing resets the sums. */
+int mcg_set_timing(mcg_ctx* ctx, int on);
+int mcg_phase_times(mcg_ctx* ctx, double* ms, int32_t n, int64_t* evaluations);
 
 /* ---- synthetic lattices (no reference counterpart; the reference's own builder is
  *      MC/src/sim.cpp:51-135) --------------------------------------------------- */

@@ -1,0 +1,133 @@
+"""Parity of the GPU energy/gradient (libmcg.so, FP64 plain form) with the reference.
+
+Bars (per evaluation): energy within 1e-10 relative; gradient within 1e-10 relative in
+the 2-norm (per-component relative error is meaningless where node forces cancel);
+diagnostics the same; contact pair sets bit-identical; maximum penetration and contact
+counts exact (they depend on positions only, which are bit-identical).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+from falling_dice_gb300 import abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+CASES = ["ref242", "cubic6", "bcc4"]
+
+
+def solver_for(fd, g, **cfg_over):
+    cfg = g.cfg
+    for k, v in cfg_over.items():
+        setattr(cfg, k, v)
+    return fd.Solver(cfg, g.lattice)
+
+
+def check_eval(r, s, ctx):
+    if np.isinf(s["energy"]):
+        assert np.isinf(r["energy"]) and r["energy"] > 0, ctx
+        assert not np.any(r["grad"]), ctx
+        return
+    assert abs(r["energy"] - s["energy"]) <= TOL * abs(s["energy"]), (ctx, r["energy"], s["energy"])
+    assert rel_err(r["grad"], s["grad"]) <= TOL, (ctx, rel_err(r["grad"], s["grad"]))
+    d = r["diag"]
+    ref = s["diag"]
+    for name, idx in (("elastic", 0), ("plastic", 1), ("contact", 2), ("reaction", 3)):
+        assert abs(d[name] - ref[idx]) <= TOL * max(abs(ref[idx]), 1e-12), (ctx, name, d[name], ref[idx])
+    assert d["max_pen"] == ref[4], (ctx, d["max_pen"], ref[4])
+    assert d["contacts"] == int(ref[5]), (ctx, d["contacts"], ref[5])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_objective_matches_reference_fixtures(mcg, case):
+    g = golden(case)
+    s0 = solver_for(mcg, g)
+    for k in range(g.n_states):
+        s = g.state(k)
+        s0.set_state(plastic=s["plastic"])
+        r = s0.objective(s["z"], s["top"], s["trials"])
+        check_eval(r, s, (case, k))
+        if np.isfinite(s["energy"]):
+            assert np.array_equal(s0.contact_pairs(), s["pairs"]), (case, k)
+        if s["trials"] and np.isfinite(s["energy"]):
+            assert rel_err(r["trial_next"], s["trial_next"]) <= TOL, (case, k)
+            assert rel_err(r["trial_aux"], s["trial_aux"]) <= TOL, (case, k)
+            assert np.array_equal(r["trial_flags"], s["trial_flags"]), (case, k)
+
+
+def test_objective_is_bitwise_deterministic(mcg):
+    g = golden("ref242")
+    s = g.state(3)
+    sol = solver_for(mcg, g)
+    sol.set_state(plastic=s["plastic"])
+    a = sol.objective(s["z"], s["top"], True)
+    b = sol.objective(s["z"], s["top"], True)
+    assert a["energy"] == b["energy"]
+    assert np.array_equal(a["grad"].view(np.uint64), b["grad"].view(np.uint64))
+    assert np.array_equal(a["trial_next"].view(np.uint64), b["trial_next"].view(np.uint64))
+
+
+def test_objective_matches_oracle_on_larger_lattices(mcg, mco):
+    """cubic+BCC 8x8x8 at two deformation levels against the CPU restatement run here."""
+    cfg, spec = workloads.bcc((8, 8, 8))
+    lat = mcg.generate_lattice(spec, cfg)
+    sol = mcg.Solver(cfg, lat)
+    orc = mco.Model("mco", cfg, lattice=lat)
+    for sig, seed in ((0.05, 1), (0.2, 2)):
+        z, pl = mcg.random_state(lat, sig, 0.1, 0.02, seed)
+        sol.set_state(plastic=pl)
+        orc.set_state(plastic=pl)
+        top = lat.geometry.top0 - 0.002
+        r = sol.objective(z, top, True)
+        o = orc.objective(z, top, True)
+        s = {"energy": o["energy"], "grad": o["grad"],
+             "diag": np.array([o["diag"][k] for k in ("elastic", "plastic", "contact", "reaction",
+                                                       "max_pen", "contacts")])}
+        check_eval(r, s, ("bcc8", sig))
+        assert np.array_equal(sol.contact_pairs(), orc.contact_pairs(z))
+        assert rel_err(r["trial_next"], o["trial_next"]) <= TOL
+
+
+def test_self_contact_off_drops_only_the_pair_terms(mcg):
+    g = golden("ref242")
+    s = g.state(3)
+    on = solver_for(mcg, g)
+    cfg = golden("ref242").cfg
+    cfg.self_contact = 0
+    off = mcg.Solver(cfg, g.lattice)
+    for sol in (on, off):
+        sol.set_state(plastic=s["plastic"])
+    a = on.objective(s["z"], s["top"])
+    b = off.objective(s["z"], s["top"])
+    assert b["diag"]["contacts"] < a["diag"]["contacts"]
+    assert b["energy"] < a["energy"]
+    assert len(off.contact_pairs()) == 0
+
+
+def test_translation_gradient_matches_finite_differences_at_full_size(mcg):
+    """Size-independent property on the 64x64x32 cubic+BCC workload: along a random
+    translation-only direction the central difference of the energy equals g.d."""
+    cfg, spec = workloads.bcc64()
+    lat = mcg.generate_lattice(spec, cfg)
+    sol = mcg.Solver(cfg, lat)
+    z, pl = mcg.random_state(lat, 0.02, 0.02, 0.02, 5)
+    sol.set_state(plastic=pl)
+    top = lat.geometry.top0 + 0.01
+    r = sol.objective(z, top)
+    assert np.isfinite(r["energy"])
+    rng = np.random.default_rng(3)
+    d = np.zeros_like(z)
+    for k in range(3):
+        d[k::6] = rng.normal(0, 1, lat.n_nodes)
+    d[lat.locked.astype(bool)] = 0
+    d /= np.linalg.norm(d)
+    h = 1e-6
+    ep = sol.objective(z + h * d, top)["energy"]
+    em = sol.objective(z - h * d, top)["energy"]
+    fd = (ep - em) / (2 * h)
+    an = float(r["grad"] @ d)
+    assert abs(fd - an) <= 1e-3 * max(abs(an), 1e-9), (fd, an)
+    # and twice in a row gives the same bits
+    r2 = sol.objective(z, top)
+    assert r2["energy"] == r["energy"] and np.array_equal(r2["grad"], r["grad"])
