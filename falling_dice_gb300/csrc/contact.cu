@@ -1,24 +1,30 @@
-// contact.cu -- self-contact broad and narrow phase (the reference's
-// MC/src/sim.cpp:144-165 hash grid + closest-shape penalty), rebuilt as a Morton-ordered
-// uniform grid over sorted (cell, shape) entries.
+// contact.cu -- self-contact broad and narrow phase (the reference's MC/src/sim.cpp:144-165
+// hash grid and closest-shape penalty), rebuilt as a Morton-ordered uniform grid.
 //
 // This translation unit is compiled with -fmad=false: the closest-point arithmetic must
 // round exactly like the reference so that the set of pairs with dist < target is the
 // reference's set bit for bit (positions are bit-identical, see k_state).
 //
 // Broad phase.  Every shape (N joint spheres, then B beam capsules, as sim.cpp:148-150)
-// enters every grid cell its margin-inflated AABB touches (sim.cpp:153-157, same cell size
-// and the same floor() cell coordinates).  Entries are keyed by the Morton code of the
-// cell relative to the grid origin and radix-sorted (stable, so a cell's entries stay in
-// ascending shape order).  A pair is examined only in the cell that is the minimum corner
-// of the intersection of the two shapes' cell ranges: every pair that shares a cell is
-// examined exactly once, which is the reference's `tested` set without a hash set.
+// enters every grid cell its margin-inflated AABB touches (sim.cpp:153-157; same cell size
+// and the same floor() cell coordinates).  Cells are numbered by the Morton code of their
+// coordinates relative to the grid origin (row-major when the Morton range does not fit),
+// and entries are counting-sorted into those bins: one atomic count per entry, a scan over
+// bins, one scatter.  The pair pass gives each occupied bin to one warp, which stages the
+// bin's shapes in shared memory in ascending shape order, so every result is independent
+// of the order the atomics handed out.  A pair is examined only in the cell that is the
+// minimum corner of the intersection of the two shapes' cell ranges: every pair that
+// shares a cell is examined exactly once -- the reference's `tested` set without a set.
 // A conservative FP32 AABB test and the local-shape exclusion (sim.cpp:24-39) run before
 // the FP64 narrow phase.
 //
-// Output order.  Contacts are written in (cell, first shape, second shape) order through
-// a count/scan/emit pass pair, so the contact list -- and every sum over it -- is
+// Output order.  Contacts are counted per bin, scanned, and written by a second pass over
+// the bins that have any, in (bin, pair) order: the contact list and every sum over it are
 // deterministic.  Per-node force lists are built with counters and sorted by the gather.
+//
+// No host synchronisation: sizes that can overflow a buffer (entries, bins, contacts, a
+// shape spanning too many cells) raise a flag instead of writing out of bounds, and the
+// host repeats the evaluation with larger buffers (or coarser cells) when it sees one.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -26,28 +32,39 @@ namespace mcg {
 
 namespace {
 
-constexpr long long kMaxCellsPerShape = 1 << 16;
+constexpr long long kMaxCellsPerShape = 1 << 12;
+constexpr int kWarpCap = 64;            // bins up to this size are staged in shared memory
+constexpr int kPairWarps = kBlock / 32;
 
-__device__ __forceinline__ uint64_t spread3(uint32_t v) {  // 21 bits -> every third bit
-    uint64_t x = v & 0x1fffffu;
-    x = (x | (x << 32)) & 0x1f00000000ffffULL;
-    x = (x | (x << 16)) & 0x1f0000ff0000ffULL;
-    x = (x | (x << 8)) & 0x100f00f00f00f00fULL;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ULL;
-    x = (x | (x << 2)) & 0x1249249249249249ULL;
-    return x;
+__device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
+    v &= 0x3ffu;
+    v = (v | (v << 16)) & 0x030000ffu;
+    v = (v | (v << 8)) & 0x0300f00fu;
+    v = (v | (v << 4)) & 0x030c30c3u;
+    v = (v | (v << 2)) & 0x09249249u;
+    return v;
 }
-__device__ __forceinline__ uint32_t compact3(uint64_t x) {
-    x &= 0x1249249249249249ULL;
-    x = (x ^ (x >> 2)) & 0x10c30c30c30c30c3ULL;
-    x = (x ^ (x >> 4)) & 0x100f00f00f00f00fULL;
-    x = (x ^ (x >> 8)) & 0x1f0000ff0000ffULL;
-    x = (x ^ (x >> 16)) & 0x1f00000000ffffULL;
-    x = (x ^ (x >> 32)) & 0x1fffffULL;
-    return uint32_t(x);
+__device__ __forceinline__ uint32_t compact3_10(uint32_t v) {
+    v &= 0x09249249u;
+    v = (v ^ (v >> 2)) & 0x030c30c3u;
+    v = (v ^ (v >> 4)) & 0x0300f00fu;
+    v = (v ^ (v >> 8)) & 0x030000ffu;
+    v = (v ^ (v >> 16)) & 0x000003ffu;
+    return v;
 }
-__device__ __forceinline__ uint64_t morton(uint32_t i, uint32_t j, uint32_t k) {
-    return spread3(i) | (spread3(j) << 1) | (spread3(k) << 2);
+
+// grid[]: 0-2 origin cell, 3-5 dims, 6 mode (0 Morton, 1 row-major), 7 valid,
+//         8 number of bins
+__device__ __forceinline__ uint32_t bin_of(const int* g, int i, int j, int k) {
+    if (g[6] == 0) return spread3_10(uint32_t(i)) | (spread3_10(uint32_t(j)) << 1) | (spread3_10(uint32_t(k)) << 2);
+    return uint32_t((k * g[4] + j) * g[3] + i);
+}
+__device__ __forceinline__ int3 cell_of(const int* g, uint32_t b) {
+    if (g[6] == 0) return make_int3(int(compact3_10(b)), int(compact3_10(b >> 1)), int(compact3_10(b >> 2)));
+    const int i = int(b % uint32_t(g[3]));
+    const int j = int((b / uint32_t(g[3])) % uint32_t(g[4]));
+    const int k = int(b / (uint32_t(g[3]) * uint32_t(g[4])));
+    return make_int3(i, j, k);
 }
 
 // ---- geometry (sim.cpp:9-22), rounding as the reference --------------------------------
@@ -87,9 +104,13 @@ __device__ Closest seg_seg(d3 p1, d3 q1, d3 p2, d3 q2) {
 struct ShapeRef {
     d3 a, b;
     double r;
-    int n0, n1;
     bool capsule;
 };
+
+__device__ __forceinline__ int2 shape_nodes(const DevTopo& t, uint32_t s) {
+    if (s < uint32_t(t.N)) return make_int2(int(s), -1);
+    return t.ab[s - uint32_t(t.N)];
+}
 
 __device__ __forceinline__ ShapeRef load_shape(const DevTopo& t, const double4_32a* x, double jr, uint32_t s) {
     ShapeRef sh;
@@ -97,8 +118,6 @@ __device__ __forceinline__ ShapeRef load_shape(const DevTopo& t, const double4_3
         const double4_32a v = x[s];
         sh.a = sh.b = d3{v.x, v.y, v.z};
         sh.r = jr;
-        sh.n0 = int(s);
-        sh.n1 = -1;
         sh.capsule = false;
     } else {
         const int bi = int(s) - t.N;
@@ -107,8 +126,6 @@ __device__ __forceinline__ ShapeRef load_shape(const DevTopo& t, const double4_3
         sh.a = d3{va.x, va.y, va.z};
         sh.b = d3{vb.x, vb.y, vb.z};
         sh.r = t.radius[bi];
-        sh.n0 = ab.x;
-        sh.n1 = ab.y;
         sh.capsule = true;
     }
     return sh;
@@ -139,25 +156,52 @@ __device__ __forceinline__ bool is_connected(const DevTopo& t, int u, int v) {
     return false;
 }
 
-// Same beam, a shared node, or a connected node pair (sim.cpp:24-39).
-__device__ __forceinline__ bool excluded(const DevTopo& t, const ShapeRef& a, const ShapeRef& b) {
-    const int an[2] = {a.n0, a.n1}, bn[2] = {b.n0, b.n1};
-    const int na = a.capsule ? 2 : 1, nb = b.capsule ? 2 : 1;
+// Same beam, a shared node, or a connected node pair (sim.cpp:24-39).  Shapes are
+// distinct here, so "same beam" cannot occur.
+__device__ __forceinline__ bool excluded(const DevTopo& t, int2 a, int2 b) {
+    const int an[2] = {a.x, a.y}, bn[2] = {b.x, b.y};
+    const int na = a.y >= 0 ? 2 : 1, nb = b.y >= 0 ? 2 : 1;
     for (int i = 0; i < na; ++i)
-        for (int j = 0; j < nb; ++j) {
+        for (int j = 0; j < nb; ++j)
             if (an[i] == bn[j]) return true;
+    for (int i = 0; i < na; ++i)
+        for (int j = 0; j < nb; ++j)
             if (is_connected(t, an[i], bn[j])) return true;
-        }
     return false;
 }
 
+// Full test of one candidate pair (sa < sb): exclusion, FP64 closest points, dist < target.
+struct PairHit {
+    bool hit;
+    double s, t, pen;
+    d3 n;
+};
+__device__ __forceinline__ PairHit test_pair(const DevTopo& t, const PhysParams& p, const double4_32a* x, uint32_t sa,
+                                             uint32_t sb) {
+    PairHit h;
+    h.hit = false;
+    if (excluded(t, shape_nodes(t, sa), shape_nodes(t, sb))) return h;
+    const ShapeRef A = load_shape(t, x, p.joint_radius, sa);
+    const ShapeRef B = load_shape(t, x, p.joint_radius, sb);
+    const Closest cp = shape_closest(A, B);
+    const d3 delta = cp.pb - cp.pa;
+    const double dist = len(delta), target = A.r + B.r + p.contact_margin;
+    if (!(dist < target)) return h;
+    h.hit = true;
+    h.s = cp.s;
+    h.t = cp.t;
+    h.pen = target - dist;
+    h.n = dist > 1e-12 ? delta * (1.0 / dist) : unit(d3{.37 + .001 * double(int(sa)), .73, -.41 + .001 * double(int(sb))});
+    return h;
+}
+
 // ---- kernels -------------------------------------------------------------------------------
-// Grid origin, extent and Morton width from the node bounding box (e.cen[3..8]).
-__global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, int* grid) {
+// Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
+__global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
+                              uint32_t* flags) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     bool ok = true;
     long long lo[3], dim[3];
-    int bits = 1;
     for (int d = 0; d < 3; d++) {
         const double a = floor((cen[3 + d] - pad) / cell) - 1.0;
         const double b = floor((cen[6 + d] + pad) / cell) + 1.0;
@@ -169,15 +213,31 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
         }
         lo[d] = (long long)a;
         dim[d] = (long long)b - lo[d] + 1;
-        if (dim[d] > (1LL << 21)) dim[d] = 1LL << 21;
+    }
+    int bits = 0;
+    for (int d = 0; d < 3; d++)
         while ((1LL << bits) < dim[d]) bits++;
+    long long nb;
+    int mode;
+    if (bits <= 10 && (1LL << (3 * bits)) <= bin_cap) {
+        mode = 0;
+        nb = 1LL << (3 * bits);
+    } else {
+        mode = 1;
+        nb = dim[0] * dim[1] * dim[2];
+    }
+    grid[9] = int(nb < (1LL << 30) ? nb : (1LL << 30));
+    if (ok && nb > bin_cap) {  // the host enlarges the bins or coarsens the cells
+        atomicOr(flags, uint32_t(kOverBins));
+        ok = false;
     }
     for (int d = 0; d < 3; d++) {
         grid[d] = int(lo[d]);
         grid[3 + d] = int(dim[d]);
     }
-    grid[6] = bits;
+    grid[6] = mode;
     grid[7] = ok ? 1 : 0;
+    grid[8] = ok ? int(nb) : 0;
 }
 
 __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
@@ -200,7 +260,7 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
         count[s] = 0;
         cell_lo[s] = make_int4(0, 0, 0, 0);
         cell_hi[s] = make_int4(-1, -1, -1, 0);
-        if (!finite_box) atomicOr(flags, 2u);
+        if (!finite_box) atomicOr(flags, uint32_t(kNonFinite));
         return;
     }
     const double cl[3] = {lo.x, lo.y, lo.z}, ch[3] = {hi.x, hi.y, hi.z};
@@ -209,106 +269,215 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const double dim = double(grid[3 + d]) - 1.0;
-        const double a = clampd(floor(cl[d] / p.broad_cell) - double(grid[d]), 0.0, dim);
-        const double b = clampd(floor(ch[d] / p.broad_cell) - double(grid[d]), 0.0, dim);
-        c0[d] = int(a);
-        c1[d] = int(b);
+        c0[d] = int(clampd(floor(cl[d] / p.broad_cell) - double(grid[d]), 0.0, dim));
+        c1[d] = int(clampd(floor(ch[d] / p.broad_cell) - double(grid[d]), 0.0, dim));
         n *= (long long)(c1[d] - c0[d] + 1);
     }
-    if (n > kMaxCellsPerShape) {  // the host coarsens the grid and runs this again
-        atomicOr(flags, 1u);
+    if (n > kMaxCellsPerShape) {  // the host coarsens the grid and evaluates again
+        atomicOr(flags, uint32_t(kOverSpan));
         n = 0;
+        c1[0] = c0[0] - 1;
     }
     count[s] = uint32_t(n);
     cell_lo[s] = make_int4(c0[0], c0[1], c0[2], 0);
     cell_hi[s] = make_int4(c1[0], c1[1], c1[2], 0);
 }
 
-__global__ void __launch_bounds__(kBlock) k_emit(int S, const int4* __restrict__ cell_lo,
-                                                 const int4* __restrict__ cell_hi,
-                                                 const uint32_t* __restrict__ offset, uint64_t* __restrict__ keys,
-                                                 uint32_t* __restrict__ vals) {
+// Entries of shape s: bin key and rank inside the bin (bin_count counts them).
+__global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ grid, const int4* __restrict__ cell_lo,
+                                                 const int4* __restrict__ cell_hi, const uint32_t* __restrict__ offset,
+                                                 long long cap, uint32_t* __restrict__ ekey,
+                                                 uint32_t* __restrict__ erank, uint32_t* __restrict__ bin_count,
+                                                 uint32_t* __restrict__ flags) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
+    if ((long long)offset[S] > cap) {
+        if (s == 0) atomicOr(flags, uint32_t(kOverEntries));
+        return;
+    }
     const int4 lo = cell_lo[s], hi = cell_hi[s];
     uint32_t o = offset[s];
-    const uint32_t end = offset[s + 1];
     for (int j = lo.y; j <= hi.y; j++)
         for (int k = lo.z; k <= hi.z; k++)
             for (int i = lo.x; i <= hi.x; i++) {
-                if (o >= end) return;
-                keys[o] = morton(uint32_t(i), uint32_t(j), uint32_t(k));
-                vals[o] = uint32_t(s);
+                const uint32_t b = bin_of(grid, i, j, k);
+                ekey[o] = b;
+                erank[o] = atomicAdd(&bin_count[b], 1u);
                 o++;
             }
 }
 
-// Pass 1 (emit == 0): contacts per entry into ccount.  Pass 2 (emit != 0): contacts written
-// at coffset[e] in partner order.
+__global__ void __launch_bounds__(kBlock) k_scatter(int S, const uint32_t* __restrict__ offset, long long cap,
+                                                    const uint32_t* __restrict__ ekey,
+                                                    const uint32_t* __restrict__ erank,
+                                                    const uint32_t* __restrict__ bin_start,
+                                                    uint32_t* __restrict__ sorted) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S || (long long)offset[S] > cap) return;
+    for (uint32_t o = offset[s]; o < offset[s + 1]; o++) sorted[bin_start[ekey[o]] + erank[o]] = uint32_t(s);
+}
+
+// Row and column of pair p in the strict upper triangle of an n x n matrix, pairs (i, j),
+// i < j, numbered row by row.
+__device__ __forceinline__ void pair_index(int n, int p, int& i, int& j) {
+    const float fn = float(2 * n - 1);
+    int r = int((fn - sqrtf(fmaxf(fn * fn - 8.f * float(p), 0.f))) * 0.5f);
+    r = max(0, min(r, n - 2));
+    while (r > 0 && r * (2 * n - r - 1) / 2 > p) r--;
+    while (r < n - 2 && (r + 1) * (2 * n - r - 2) / 2 <= p) r++;
+    i = r;
+    j = p - r * (2 * n - r - 1) / 2 + r + 1;
+}
+
+struct BinShape {
+    uint32_t s;
+    int lx, ly, lz;
+    float bx0, by0, bz0, bx1, by1, bz1;
+};
+
+__device__ __forceinline__ void write_contact(ContactBufs& c, uint32_t pos, uint32_t sa, uint32_t sb, const PairHit& h) {
+    if (pos >= uint32_t(c.contact_cap)) return;
+    c.c_a[pos] = sa;
+    c.c_b[pos] = sb;
+    c.c_s[pos] = h.s;
+    c.c_t[pos] = h.t;
+    c.c_n[3 * size_t(pos)] = h.n.x;
+    c.c_n[3 * size_t(pos) + 1] = h.n.y;
+    c.c_n[3 * size_t(pos) + 2] = h.n.z;
+    c.c_pen[pos] = h.pen;
+}
+
+// One warp per occupied bin.  emit == 0: contacts per bin into bcount.  emit != 0: the
+// contacts of bins with bcount > 0 written at boffset, in pair order.
 __global__ void __launch_bounds__(kBlock) k_pairs(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                  long long n, const uint64_t* __restrict__ keys,
-                                                  const uint32_t* __restrict__ vals,
+                                                  const int* __restrict__ grid, const uint32_t* __restrict__ bin_count,
+                                                  const uint32_t* __restrict__ bin_start,
+                                                  const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
                                                   const int4* __restrict__ cell_lo, const float4* __restrict__ bb_lo,
                                                   const float4* __restrict__ bb_hi, int emit,
-                                                  uint32_t* __restrict__ ccount, const uint32_t* __restrict__ coffset,
+                                                  uint32_t* __restrict__ bcount, const uint32_t* __restrict__ boffset,
                                                   ContactBufs c) {
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= n) return;
-    if (emit && ccount[e] == 0) return;
-    const uint64_t key = keys[e];
-    if (e + 1 >= n || keys[e + 1] != key) {
-        if (!emit) ccount[e] = 0;
-        return;
-    }
-    const uint32_t sa = vals[e];
-    const int ci = int(compact3(key)), cj = int(compact3(key >> 1)), ck = int(compact3(key >> 2));
-    const int4 la = cell_lo[sa];
-    const float4 alo = bb_lo[sa], ahi = bb_hi[sa];
-    const ShapeRef A = load_shape(t, x, p.joint_radius, sa);
-    uint32_t found = 0;
-    uint32_t out = emit ? coffset[e] : 0;
-    for (long long f = e + 1; f < n && keys[f] == key; f++) {
-        const uint32_t sb = vals[f];
-        const int4 lb = cell_lo[sb];
-        if (max(la.x, lb.x) != ci || max(la.y, lb.y) != cj || max(la.z, lb.z) != ck) continue;
-        const float4 blo = bb_lo[sb], bhi = bb_hi[sb];
-        if (alo.x > bhi.x || blo.x > ahi.x || alo.y > bhi.y || blo.y > ahi.y || alo.z > bhi.z || blo.z > ahi.z)
+    __shared__ BinShape sh[kPairWarps][kWarpCap];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long long nb = grid[8];
+    const long long warps = (long long)gridDim.x * kPairWarps;
+    for (long long b = (long long)blockIdx.x * kPairWarps + w; b < nb; b += warps) {
+        const int n = int(bin_count[b]);
+        if (n < 2 || (emit && bcount[b] == 0)) {
+            if (!emit && lane == 0) bcount[b] = 0;
             continue;
-        const ShapeRef Bs = load_shape(t, x, p.joint_radius, sb);
-        if (excluded(t, A, Bs)) continue;
-        const Closest cp = shape_closest(A, Bs);
-        const d3 delta = cp.pb - cp.pa;
-        const double dist = len(delta), target = A.r + Bs.r + p.contact_margin;
-        if (!(dist < target)) continue;
-        if (emit) {
-            const d3 nn = dist > 1e-12 ? delta * (1.0 / dist)
-                                       : unit(d3{.37 + .001 * double(int(sa)), .73, -.41 + .001 * double(int(sb))});
-            c.c_a[out] = sa;
-            c.c_b[out] = sb;
-            c.c_s[out] = cp.s;
-            c.c_t[out] = cp.t;
-            c.c_n[3 * size_t(out)] = nn.x;
-            c.c_n[3 * size_t(out) + 1] = nn.y;
-            c.c_n[3 * size_t(out) + 2] = nn.z;
-            c.c_pen[out] = target - dist;
-            out++;
         }
-        found++;
+        const uint32_t start = bin_start[b];
+        const int3 cc = cell_of(grid, uint32_t(b));
+        uint32_t found = 0;
+        uint32_t out = emit ? boffset[b] : 0;
+        if (n <= kWarpCap) {
+            // stage the bin in ascending shape order: rank = number of smaller shape ids
+            const uint32_t v0 = lane < n ? sorted[start + lane] : 0xffffffffu;
+            const uint32_t v1 = lane + 32 < n ? sorted[start + 32 + lane] : 0xffffffffu;
+            int r0 = 0, r1 = 0;
+            for (int q = 0; q < 32; q++) {
+                const uint32_t u0 = __shfl_sync(0xffffffffu, v0, q), u1 = __shfl_sync(0xffffffffu, v1, q);
+                r0 += (u0 < v0) + (u1 < v0);
+                r1 += (u0 < v1) + (u1 < v1);
+            }
+            __syncwarp();
+            if (v0 != 0xffffffffu) {
+                const int4 l = cell_lo[v0];
+                const float4 a = bb_lo[v0], z = bb_hi[v0];
+                sh[w][r0] = BinShape{v0, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z};
+            }
+            if (v1 != 0xffffffffu) {
+                const int4 l = cell_lo[v1];
+                const float4 a = bb_lo[v1], z = bb_hi[v1];
+                sh[w][r1] = BinShape{v1, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z};
+            }
+            __syncwarp();
+            const int P = n * (n - 1) / 2;
+            for (int base = 0; base < P; base += 32) {
+                const int pidx = base + lane;
+                bool hit = false;
+                PairHit h;
+                uint32_t sa = 0, sb = 0;
+                if (pidx < P) {
+                    int i, j;
+                    pair_index(n, pidx, i, j);
+                    const BinShape& A = sh[w][i];
+                    const BinShape& B = sh[w][j];
+                    if (max(A.lx, B.lx) == cc.x && max(A.ly, B.ly) == cc.y && max(A.lz, B.lz) == cc.z &&
+                        !(A.bx0 > B.bx1 || B.bx0 > A.bx1 || A.by0 > B.by1 || B.by0 > A.by1 || A.bz0 > B.bz1 ||
+                          B.bz0 > A.bz1)) {
+                        sa = A.s;
+                        sb = B.s;
+                        h = test_pair(t, p, x, sa, sb);
+                        hit = h.hit;
+                    }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (emit && hit) write_contact(c, out + __popc(m & ((1u << lane) - 1u)), sa, sb, h);
+                out += __popc(m);
+                found += __popc(m);
+            }
+            __syncwarp();
+        } else {
+            // large bin: ascending order through a scratch copy, pairs from global memory
+            for (int e = lane; e < n; e += 32) {
+                const uint32_t v = sorted[start + e];
+                int r = 0;
+                for (int q = 0; q < n; q++) r += sorted[start + q] < v;
+                sorted2[start + r] = v;
+            }
+            __syncwarp();
+            const long long P = (long long)n * (n - 1) / 2;
+            int i = 0;
+            long long row_end = n - 1;  // pairs of rows 0..i end here
+            for (long long base = 0; base < P; base += 32) {
+                const long long pidx = base + lane;
+                bool hit = false;
+                PairHit h;
+                uint32_t sa = 0, sb = 0;
+                if (pidx < P) {
+                    while (pidx >= row_end) {  // rows advance monotonically with base
+                        i++;
+                        row_end += n - 1 - i;
+                    }
+                    const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
+                    sa = sorted2[start + i];
+                    sb = sorted2[start + j];
+                    const int4 la = cell_lo[sa], lb = cell_lo[sb];
+                    const float4 a0 = bb_lo[sa], a1 = bb_hi[sa], b0 = bb_lo[sb], b1 = bb_hi[sb];
+                    if (max(la.x, lb.x) == cc.x && max(la.y, lb.y) == cc.y && max(la.z, lb.z) == cc.z &&
+                        !(a0.x > b1.x || b0.x > a1.x || a0.y > b1.y || b0.y > a1.y || a0.z > b1.z || b0.z > a1.z)) {
+                        h = test_pair(t, p, x, sa, sb);
+                        hit = h.hit;
+                    }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, hit);
+                if (emit && hit) write_contact(c, out + __popc(m & ((1u << lane) - 1u)), sa, sb, h);
+                out += __popc(m);
+                found += __popc(m);
+            }
+            __syncwarp();
+        }
+        if (!emit && lane == 0) bcount[b] = found;
     }
-    if (!emit) ccount[e] = found;
 }
 
 constexpr int kContactPartBlocks = 128;
+constexpr int kStreamBlocks = 4 * 152;
 
 // Fixed-partition reduction over the contact list: energy, max penetration, count.
-__global__ void __launch_bounds__(kBlock) k_contact_reduce(long long nc, double k, const double* __restrict__ pen,
-                                                           double* __restrict__ part) {
+__global__ void __launch_bounds__(kBlock) k_contact_reduce(const uint32_t* __restrict__ total, long long cap, double k,
+                                                           const double* __restrict__ pen, double* __restrict__ part,
+                                                           uint32_t* flags) {
     __shared__ double sm[2 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
+    const long long nc_all = *total;
+    if (nc_all > cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, uint32_t(kOverContacts));
+    const long long nc = nc_all > cap ? cap : nc_all;
     double acc[2] = {0, 0};
     double m = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc;
-         i += (long long)gridDim.x * blockDim.x) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
         const double pp = pen[i];
         acc[0] += .5 * k * pp * pp;
         acc[1] += 1;
@@ -329,64 +498,59 @@ __device__ __forceinline__ int slot_node(const DevTopo& t, uint32_t shape, int s
     return slot == 0 ? ab.x : ab.y;
 }
 
-__global__ void __launch_bounds__(kBlock) k_node_count(DevTopo t, long long nc, ContactBufs c) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
-    for (int slot = 0; slot < 4; slot++) {
-        const int node = slot_node(t, slot < 2 ? c.c_a[i] : c.c_b[i], slot & 1);
-        if (node >= 0) atomicAdd(&c.n_count[node], 1u);
-    }
+__global__ void __launch_bounds__(kBlock) k_node_count(DevTopo t, const uint32_t* __restrict__ total, ContactBufs c) {
+    const long long nc = min((long long)*total, c.contact_cap);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x)
+        for (int slot = 0; slot < 4; slot++) {
+            const int node = slot_node(t, slot < 2 ? c.c_a[i] : c.c_b[i], slot & 1);
+            if (node >= 0) atomicAdd(&c.n_count[node], 1u);
+        }
 }
 
-__global__ void __launch_bounds__(kBlock) k_node_fill(DevTopo t, long long nc, ContactBufs c) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nc) return;
-    for (int slot = 0; slot < 4; slot++) {
-        const int node = slot_node(t, slot < 2 ? c.c_a[i] : c.c_b[i], slot & 1);
-        if (node < 0) continue;
-        const uint32_t pos = atomicAdd(&c.n_cursor[node], 1u);
-        c.n_items[c.n_start[node] + pos] = (uint32_t(i) << 2) | uint32_t(slot);
-    }
+__global__ void __launch_bounds__(kBlock) k_node_fill(DevTopo t, const uint32_t* __restrict__ total, ContactBufs c) {
+    const long long nc = min((long long)*total, c.contact_cap);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x)
+        for (int slot = 0; slot < 4; slot++) {
+            const int node = slot_node(t, slot < 2 ? c.c_a[i] : c.c_b[i], slot & 1);
+            if (node < 0) continue;
+            const uint32_t pos = atomicAdd(&c.n_cursor[node], 1u);
+            c.n_items[c.n_start[node] + pos] = (uint32_t(i) << 2) | uint32_t(slot);
+        }
 }
 
 }  // namespace
 
 int contact_part_blocks(long long) { return kContactPartBlocks; }
 
-void contact_shapes(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                    cudaStream_t s) {
+void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
+                     cudaStream_t s) {
     const int S = t.N + t.B;
-    cudaMemsetAsync(c.dev_total, 0, 4 * sizeof(uint32_t), s);
-    (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad, p.broad_cell, c.grid), note_launches(1));
+    cudaMemsetAsync(c.flags, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(c.bin_count, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
+    (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad, p.broad_cell, c.bin_cap, c.grid, c.flags), note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.x, c.grid, c.cell_lo, c.cell_hi, c.bb_lo, c.bb_hi, c.count,
-                                                c.dev_total + 2), note_launches(1));
-    exclusive_scan_u32(c.count, c.offset, S, c.sort_tmp, s);
-}
-
-int contact_sort_and_count(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c,
-                           long long entries, int key_bits, cudaStream_t s) {
-    const int S = t.N + t.B;
-    (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.cell_lo, c.cell_hi, c.offset, c.keys[0], c.vals[0]), note_launches(1));
-    const int res = radix_sort_u64(c.keys, c.vals, entries, key_bits, c.sort_tmp, nullptr, s);
-    if (entries > 0) {
-        (k_pairs<<<grid_for(entries), kBlock, 0, s>>>(t, p, e.x, entries, c.keys[res], c.vals[res], c.cell_lo, c.bb_lo,
-                                                     c.bb_hi, 0, c.ccount, c.coffset, c), note_launches(1));
-    }
-    exclusive_scan_u32(c.ccount, c.coffset, entries, c.sort_tmp, s);
-    return res;
-}
-
-void contact_emit(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, long long entries,
-                  int res, long long ncontacts, cudaStream_t s) {
-    if (entries > 0 && ncontacts > 0)
-        (k_pairs<<<grid_for(entries), kBlock, 0, s>>>(t, p, e.x, entries, c.keys[res], c.vals[res], c.cell_lo, c.bb_lo,
-                                                     c.bb_hi, 1, c.ccount, c.coffset, c), note_launches(1));
-    (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(ncontacts, p.contact_k, c.c_pen, c.part), note_launches(1));
+                                                 c.flags), note_launches(1));
+    exclusive_scan_u32(c.count, c.offset, S, c.scan_tmp, s);
+    (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.offset, c.entry_cap, c.ekey, c.erank,
+                                           c.bin_count, c.flags), note_launches(1));
+    exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s);
+    (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted),
+     note_launches(1));
+    const unsigned pair_blocks = 152 * 8;
+    cudaMemsetAsync(c.bcount, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
+    (k_pairs<<<pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
+                                            c.bb_lo, c.bb_hi, 0, c.bcount, c.boffset, c), note_launches(1));
+    exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s);
+    (k_pairs<<<pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
+                                            c.bb_lo, c.bb_hi, 1, c.bcount, c.boffset, c), note_launches(1));
+    const uint32_t* total = c.boffset + c.bin_cap;
+    (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, p.contact_k, c.c_pen, c.part, c.flags),
+     note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);
-    if (ncontacts > 0) (k_node_count<<<grid_for(ncontacts), kBlock, 0, s>>>(t, ncontacts, c), note_launches(1));
-    exclusive_scan_u32(c.n_count, c.n_start, t.N, c.sort_tmp, s);
-    if (ncontacts > 0) (k_node_fill<<<grid_for(ncontacts), kBlock, 0, s>>>(t, ncontacts, c), note_launches(1));
+    (k_node_count<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));
+    exclusive_scan_u32(c.n_count, c.n_start, t.N, c.scan_tmp, s);
+    (k_node_fill<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));
 }
 
 }  // namespace mcg

@@ -139,7 +139,8 @@ struct mcg_ctx {
     void check_launch() { ck(cudaGetLastError(), "kernel launch"); }
 
     // ---- contact buffers ---------------------------------------------------------------
-    void alloc_contacts(long long entry_cap, long long contact_cap) {
+    double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
+    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap) {
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
@@ -149,14 +150,18 @@ struct mcg_ctx {
         c.bb_hi = contact_mem.get<float4>(size_t(S));
         c.count = contact_mem.get<uint32_t>(size_t(S + 1));
         c.offset = contact_mem.get<uint32_t>(size_t(S + 1));
-        c.grid = contact_mem.get<int>(8);
+        c.grid = contact_mem.get<int>(16);
+        c.flags = contact_mem.get<uint32_t>(4);
         c.entry_cap = entry_cap;
-        for (int k = 0; k < 2; k++) {
-            c.keys[k] = contact_mem.get<uint64_t>(size_t(entry_cap));
-            c.vals[k] = contact_mem.get<uint32_t>(size_t(entry_cap));
-        }
-        c.ccount = contact_mem.get<uint32_t>(size_t(entry_cap + 1));
-        c.coffset = contact_mem.get<uint32_t>(size_t(entry_cap + 1));
+        c.ekey = contact_mem.get<uint32_t>(size_t(entry_cap));
+        c.erank = contact_mem.get<uint32_t>(size_t(entry_cap));
+        c.sorted = contact_mem.get<uint32_t>(size_t(entry_cap));
+        c.sorted2 = contact_mem.get<uint32_t>(size_t(entry_cap));
+        c.bin_cap = bin_cap;
+        c.bin_count = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
+        c.bin_start = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
+        c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
+        c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.contact_cap = contact_cap;
         c.c_a = contact_mem.get<uint32_t>(size_t(contact_cap));
         c.c_b = contact_mem.get<uint32_t>(size_t(contact_cap));
@@ -169,57 +174,41 @@ struct mcg_ctx {
         c.n_cursor = contact_mem.get<uint32_t>(size_t(N));
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.part = contact_mem.get<double>(size_t(3 * contact_part_blocks(contact_cap)));
-        const long long scan_n = std::max(std::max(S + 1, entry_cap + 1), (long long)N + 1);
-        c.sort_tmp_bytes = std::max(radix_tmp_bytes(entry_cap), scan_tmp_bytes(scan_n));
-        c.sort_tmp = contact_mem.get<unsigned char>(c.sort_tmp_bytes);
-        c.dev_total = contact_mem.get<uint32_t>(4);
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max(std::max(S + 1, bin_cap + 1), (long long)N + 1));
+        c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
+        ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         cb = c;
     }
 
-    // Broad and narrow phase with the host reading back the two sizes it allocates for.
-    void contacts(PhysParams& p) {
+    // Grows whatever the last evaluation overflowed; false when nothing did.
+    bool grow_contacts(int flags) {
+        if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan))) return false;
         const long long S = (long long)N + B;
-        double cell = p.broad_cell;
-        long long entries = 0;
-        for (int attempt = 0;; attempt++) {
-            p.broad_cell = cell;
-            contact_shapes(topo, p, ev, cb, rmax + cfg.contact_margin, stream);
-            ck(cudaMemcpyAsync(&hp->u32[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-            ck(cudaMemcpyAsync(&hp->u32[1], cb.dev_total + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-            ck(cudaMemcpyAsync(hp->grid, cb.grid, 8 * sizeof(int), cudaMemcpyDeviceToHost, stream), "copy");
-            sync();
-            check_launch();
-            entries = hp->u32[0];
-            if ((hp->u32[1] & 1u) && attempt < 40) {  // a shape spans too many cells: coarsen
-                cell *= 2;
-                continue;
-            }
-            break;
-        }
-        if (entries > cb.entry_cap) {
-            alloc_contacts(entries + entries / 4 + 1024, cb.contact_cap);
-            // the shape pass wrote into the released buffers: run it again
-            contact_shapes(topo, p, ev, cb, rmax + cfg.contact_margin, stream);
-        }
-        const int bits = hp->grid[6];
-        const int res = contact_sort_and_count(topo, p, ev, cb, entries, 3 * bits, stream);
-        ck(cudaMemcpyAsync(&hp->u32[2], cb.coffset + entries, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        uint32_t need[2] = {0, 0};
+        int grid[16];
+        ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[1], cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
-        check_launch();
-        const long long nc = hp->u32[2];
-        if (nc > cb.contact_cap) {
-            // grow the contact list; the sorted entries and counts must survive, so keep them
-            throw Fail(MCG_ERR_CAPACITY, "contact list capacity");  // handled by the caller
+        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap;
+        if (flags & kOverSpan) broad_cell *= 2;
+        if (flags & kOverEntries) ecap = std::max(ecap, (long long)need[0] + need[0] / 4 + 1024);
+        if (flags & kOverContacts) ccap = std::max(ccap, (long long)need[1] + need[1] / 4 + 1024);
+        if (flags & kOverBins) {
+            const long long want = (long long)grid[9] + grid[9] / 4 + 1024;
+            if (want <= (1LL << 28)) bcap = std::max(bcap, want);
+            else broad_cell *= 2;  // a huge extent: coarser cells instead of more bins
         }
-        contact_emit(topo, p, ev, cb, entries, res, nc, stream);
-        last_contacts = nc;
-        last_sort_res = res;
+        alloc_contacts(ecap, ccap, bcap);
+        return true;
     }
 
     // One evaluation of the objective at device z; grad written to d_gout; totals in ev.out.
+    // Enqueues only: no host synchronisation.
     void eval(const double* dz, double top, bool trials, double* d_gout) {
         PhysParams p = phys;
         p.top = top;
+        p.broad_cell = broad_cell;
         mark(0);
         launch_state(topo, p, dz, d_baseX, d_baseR, ev, stream);
         mark(1);
@@ -227,16 +216,7 @@ struct mcg_ctx {
         mark(2);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
-            for (int tries = 0;; tries++) {
-                try {
-                    contacts(p);
-                    break;
-                } catch (const Fail& f) {
-                    if (f.code != MCG_ERR_CAPACITY || tries > 3) throw;
-                    const long long need = hp->u32[2];
-                    alloc_contacts(cb.entry_cap, need + need / 4 + 1024);
-                }
-            }
+            launch_contacts(topo, p, ev, cb, rmax + cfg.contact_margin, stream);
             cptr = &cb;
         }
         mark(3);
@@ -246,11 +226,47 @@ struct mcg_ctx {
         mark(5);
         check_launch();
         collect();
+        last_top = top;
+        last_z = dz;
+        last_trials = trials;
+        last_grad = d_gout;
     }
-    EvalOut read_out() {
+    double last_top = 0;
+    const double* last_z = nullptr;
+    bool last_trials = false;
+    double* last_grad = nullptr;
+
+    // Evaluation whose totals are read back; repeats it with larger contact buffers when a
+    // capacity was exceeded.
+    EvalOut eval_read(const double* dz, double top, bool trials, double* d_gout) {
+        eval(dz, top, trials, d_gout);
+        EvalOut o = read_out_raw();
+        for (int tries = 0; o.overflow && tries < 16; tries++) {
+            if (!grow_contacts(o.overflow)) break;
+            eval(dz, top, trials, d_gout);
+            o = read_out_raw();
+        }
+        if (o.overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
+        if (cfg.self_contact) last_contacts = read_contact_count();
+        return o;
+    }
+    long long read_contact_count() {
+        uint32_t nc = 0;
+        ck(cudaMemcpyAsync(&nc, cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        sync();
+        return nc;
+    }
+    EvalOut read_out_raw() {
         ck(cudaMemcpyAsync(&hp->out, ev.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
         return hp->out;
+    }
+    // Totals of the last evaluation, repeating it if it overflowed a contact buffer.
+    EvalOut read_out() {
+        EvalOut o = read_out_raw();
+        if (o.overflow) o = eval_read(last_z, last_top, last_trials, last_grad);
+        else if (cfg.self_contact) last_contacts = read_contact_count();
+        return o;
     }
     void read_rms_max(const double* g, double& rms, double& mx) {
         rms_max(g, topo.locked, 6LL * N, n_free, d_part, d_stats, stream);
@@ -273,8 +289,7 @@ struct mcg_ctx {
         HostStats st;
         int m = 0, head = 0;  // history: slots (head + h) % H, h = 0 oldest
         auto slot = [&](int h) { return (head + h) % std::max(H, 1); };
-        eval(d_z, top, false, d_g);
-        EvalOut cur = read_out();
+        EvalOut cur = eval_read(d_z, top, false, d_g);
         double cur_rms, cur_max;
         read_rms_max(d_g, cur_rms, cur_max);
         double best_energy = cur.energy;
@@ -292,8 +307,7 @@ struct mcg_ctx {
             double step = 1.0;
             for (int bt = 0; bt < cfg.max_line_search; bt++) {
                 candidate(d_zc, d_z, d_p, step, topo.locked, n, stream);
-                eval(d_zc, top, false, d_gc);
-                cand = read_out();
+                cand = eval_read(d_zc, top, false, d_gc);
                 st.backtracks++;
                 if (std::isfinite(cand.energy) && cand.energy <= cur.energy + cfg.armijo * step * dg) return true;
                 step *= .5;
@@ -370,8 +384,7 @@ struct mcg_ctx {
             }
         }
         if (!st.converged && best_energy < cur.energy) vcopy(d_z, d_best, n, stream);
-        eval(d_z, top, true, d_g);
-        fin = read_out();
+        fin = eval_read(d_z, top, true, d_g);
         read_rms_max(d_g, st.rms, st.max);
         st.energy = fin.energy;
         st.converged = converged(fin, st.rms, st.max);
@@ -633,6 +646,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         const double E = cf.material.young, G = E / (2 * (1 + cf.material.nu)), sy = cf.material.yield;
         std::vector<int2> ab(static_cast<size_t>(B));
         std::vector<double> kb(B), kt(B), my(B), ty(B), hb(B), ht(B), cs(B), aL(B), aLsy(B);
+        std::vector<double> invL0(B), inv_kbh(B), inv_kth(B);
         std::vector<double> e0x(B), e0y(B), e0z(B);
         double rmax = cf.joint_scale * cf.max_radius;
         std::vector<int> deg(size_t(N) + 1, 0);
@@ -660,6 +674,9 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
             cs[b] = .5 * cf.shear_correction * G * area * L0;
             aL[b] = area * L0;
             aLsy[b] = area * L0 * sy;
+            invL0[b] = 1.0 / L0;
+            inv_kbh[b] = 1.0 / std::max(1e-20, kb[b] + hb[b]);
+            inv_kth[b] = 1.0 / std::max(1e-20, kt[b] + ht[b]);
             e0x[b] = t->e0[3 * size_t(b)];
             e0y[b] = t->e0[3 * size_t(b) + 1];
             e0z[b] = t->e0[3 * size_t(b) + 2];
@@ -733,6 +750,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         T.e0x = upd(e0x); T.e0y = upd(e0y); T.e0z = upd(e0z);
         T.kb = upd(kb); T.kt = upd(kt); T.my = upd(my); T.ty = upd(ty); T.hb = upd(hb); T.ht = upd(ht);
         T.cs = upd(cs); T.aL = upd(aL); T.aLsy = upd(aLsy);
+        T.invL0 = upd(invL0); T.inv_kbh = upd(inv_kbh); T.inv_kth = upd(inv_kth);
         T.mass = upd(std::vector<double>(t->mass, t->mass + N));
         uint8_t* dl = M.get<uint8_t>(6 * size_t(N));
         h2d(dl, t->locked, 6 * size_t(N), s);
@@ -750,7 +768,8 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         if (!conn.empty()) h2d(dc, conn.data(), conn.size(), s);
         T.conn_nbr = dc;
         c->topo = T;
-        c->mat = Material{E, G, sy, cf.material.hardening, cf.material.bend_hardening, cf.material.torsion_hardening};
+        c->mat = Material{E, G, sy, cf.material.hardening, cf.material.bend_hardening, cf.material.torsion_hardening,
+                          1.0 / std::max(1e-20, E + cf.material.hardening)};
         PhysParams P{};
         P.translation_scale = cf.translation_scale;
         P.gravity = cf.gravity;
@@ -781,6 +800,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         EvalBufs e{};
         e.x = V.get<double4_32a>(size_t(N));
         e.R = V.get<double4_32a>(size_t(N));
+        e.M = V.get<double4_32a>(3 * size_t(N));
         e.slotA = V.get<double>(6 * size_t(B));
         e.slotB = V.get<double>(6 * size_t(B));
         e.part_state = V.get<double>(9 * size_t(nb_nodes(N)));
@@ -797,7 +817,25 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         ck(cudaMemsetAsync(c->d_zin, 0, 6 * size_t(N) * sizeof(double), s), "memset");
         // contact buffers: a first guess, grown on demand
         const long long S = (long long)N + B;
-        c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096));
+        c->broad_cell = P.broad_cell;
+        {
+            // bins: the Morton range of the rest-state extent, with room to grow
+            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+            if (x0)
+                for (int i = 0; i < N; i++)
+                    for (int d = 0; d < 3; d++) {
+                        lo[d] = std::min(lo[d], x0[3 * size_t(i) + d]);
+                        hi[d] = std::max(hi[d], x0[3 * size_t(i) + d]);
+                    }
+            long long dmax = 8;
+            if (x0)
+                for (int d = 0; d < 3; d++)
+                    dmax = std::max(dmax, (long long)((hi[d] - lo[d] + 2 * c->rmax) / P.broad_cell * 1.15) + 4);
+            int bits = 3;
+            while ((1LL << bits) < dmax && bits < 10) bits++;
+            const long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
+            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap);
+        }
         // solver vectors
         DevArena& Q = c->solver_mem;
         const size_t n = 6 * size_t(N);
@@ -863,10 +901,9 @@ int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* e
         cudaStream_t s = c->stream;
         const size_t n = 6 * size_t(c->N), B = size_t(c->B);
         h2d(c->d_zin, z, n, s);
-        c->eval(c->d_zin, top, trials != 0, c->d_grad);
+        const EvalOut o = c->eval_read(c->d_zin, top, trials != 0, c->d_grad);
         if (trials) c->have_final = false;
         if (grad) d2h(grad, c->d_grad, n, s);
-        const EvalOut o = c->read_out();
         if (energy) *energy = o.energy;
         if (diag) {
             diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
@@ -914,8 +951,10 @@ int mcg_objective_resident(mcg_ctx* c, double top, int trials) {
 int mcg_read_result(mcg_ctx* c, double* energy, double* grad, mcg_diag* diag) {
     return guarded(c, [&] {
         need_topo(c);
-        if (grad) d2h(grad, c->d_grad, 6 * size_t(c->N), c->stream);
+        if (!c->last_z) throw Fail(MCG_ERR_STATE, "no evaluation to read");
         const EvalOut o = c->read_out();
+        if (grad) d2h(grad, c->d_grad, 6 * size_t(c->N), c->stream);
+        c->sync();
         if (energy) *energy = o.energy;
         if (diag) {
             diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;

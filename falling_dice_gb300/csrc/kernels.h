@@ -24,6 +24,7 @@ namespace mcg {
 
 struct Material {
     double E, G, sy, H, bend_h, torsion_h;
+    double inv_EH;  // 1 / max(1e-20, E + H)
 };
 
 struct DevTopo {
@@ -32,6 +33,7 @@ struct DevTopo {
     const double *L0, *area, *radius;
     const double *e0x, *e0y, *e0z;
     const double *kb, *kt, *my, *ty, *hb, *ht, *cs, *aL, *aLsy;
+    const double *invL0, *inv_kbh, *inv_kth;  // 1/L0, 1/max(1e-20, kb+hb), 1/max(1e-20, kt+ht)
     const double* mass;
     const uint8_t* locked;    // [6N]
     const int* inc_start;     // [N+1]
@@ -51,27 +53,43 @@ struct EvalOut {
     double energy, elastic, plastic, contact, reaction, max_pen;
     int contacts, nonfinite;
     double beam_energy, node_energy, center_energy, contact_energy, platen_energy;
-    long long entries, candidates;   // broad-phase statistics
-    int overflow, pad_;
+    int overflow;                    // ContactFlag bits that invalidate this evaluation
+    int pad_;
 };
 
-// Device scratch of the contact pipeline.
+// Device scratch of the contact pipeline (contact.cu).  Capacities are host-chosen and
+// grown on demand: a kernel that would exceed one sets a bit in flags[0] instead.
+enum ContactFlag : uint32_t {
+    kOverEntries = 1,    // more (cell, shape) entries than entry_cap
+    kOverContacts = 2,   // more contacts than contact_cap
+    kOverBins = 4,       // the grid needs more bins than bin_cap
+    kNonFinite = 8,      // a shape has a non-finite bounding box (informational)
+    kOverSpan = 16,      // a shape spans more cells than allowed: coarsen the grid
+};
+
 struct ContactBufs {
-    // per shape (N + B)
+    // per shape (S = N + B)
     int4* cell_lo;          // [S] first cell (i, j, k) relative to the grid origin
     int4* cell_hi;          // [S] last cell
     float4* bb_lo;          // [S] fp32 AABB, rounded outward
     float4* bb_hi;
     uint32_t* count;        // [S+1] cells per shape
-    uint32_t* offset;       // [S+1]
-    int* grid;              // [8]: origin i,j,k; dims i,j,k; Morton bits; valid
-    // (cell key, shape) entries, double-buffered for the radix sort
-    uint64_t* keys[2];
-    uint32_t* vals[2];
+    uint32_t* offset;       // [S+1] exclusive scan of count
+    int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed
+    uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation
+    // entries in emission order (shape-major), then counting-sorted by bin
     long long entry_cap;
-    uint32_t* ccount;       // [entry_cap + 1] contacts found per entry
-    uint32_t* coffset;      // [entry_cap + 1]
-    // contacts, in deterministic (cell, shape, shape) order
+    uint32_t* ekey;         // [entry_cap] bin of the entry
+    uint32_t* erank;        // [entry_cap] rank of the entry inside its bin
+    uint32_t* sorted;       // [entry_cap] shape ids grouped by bin
+    uint32_t* sorted2;      // [entry_cap] scratch for bins too large for shared memory
+    // bins
+    long long bin_cap;
+    uint32_t* bin_count;    // [bin_cap+1]
+    uint32_t* bin_start;    // [bin_cap+1]
+    uint32_t* bcount;       // [bin_cap+1] contacts found per bin
+    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = contact count
+    // contacts, in deterministic (bin, pair) order
     long long contact_cap;
     uint32_t* c_a;          // lower shape index
     uint32_t* c_b;          // higher shape index
@@ -85,14 +103,14 @@ struct ContactBufs {
     uint32_t* n_cursor;     // [N]
     uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot)
     double* part;           // [3 * contact_part_blocks] energy, max penetration, count
-    void* sort_tmp;
-    size_t sort_tmp_bytes;
-    uint32_t* dev_total;    // [4] flags: [2] bit0 coarsen grid, bit1 non-finite shape
+    void* scan_tmp;
+    size_t scan_tmp_bytes;
 };
 
 struct EvalBufs {
     double4_32a* x;             // [N]
     double4_32a* R;             // [N]
+    double4_32a* M;             // [3N] rotation matrix rows of R (x, y, z, pad)
     double* slotA;          // [6B] (-F, Ga) per beam, added to node a
     double* slotB;          // [6B] (+F, Gb) per beam, added to node b
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
@@ -127,25 +145,14 @@ void launch_plastic_stats(int B, const double* plastic, double* part, double* ou
 
 // ---- contact pipeline (contact.cu) ------------------------------------------------------
 int contact_part_blocks(long long contact_cap);
-// grid + per-shape cell ranges + scan of the per-shape cell counts
-void contact_shapes(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                    cudaStream_t s);
-// entries -> radix sort -> contacts per entry -> scan; returns the sort buffer index
-int contact_sort_and_count(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c,
-                           long long entries, int key_bits, cudaStream_t s);
-// writes the contact list, its reduction and the per-node force lists
-void contact_emit(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, long long entries,
-                  int res, long long ncontacts, cudaStream_t s);
+// The whole broad/narrow phase: grid, entries, bins, pairs, contact list, node lists.
+void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
+                     cudaStream_t s);
 
-// ---- scan / radix sort (sort.cu) --------------------------------------------------------
+// ---- scan (sort.cu) -----------------------------------------------------------------------
 size_t scan_tmp_bytes(long long n);
 // Exclusive scan of n uint32 values; out[n] receives the total.
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
-size_t radix_tmp_bytes(long long n);
-// Stable LSD radix sort of (key, value) pairs on bits [0, end_bit); returns the buffer
-// index (0 or 1) holding the result.
-int radix_sort_u64(uint64_t* keys[2], uint32_t* vals[2], long long n, int end_bit, void* tmp,
-                   const uint32_t* n_dev, cudaStream_t s);
 
 // ---- L-BFGS vector kernels (lbfgs.cu) ----------------------------------------------------
 size_t lbfgs_part_doubles();

@@ -21,7 +21,8 @@ int nb_beams(int B) { return int(grid_for(B)); }
 __global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uint8_t* __restrict__ locked,
                                                   const double* __restrict__ z, const double* __restrict__ bx,
                                                   const double* __restrict__ br, double4_32a* __restrict__ x4,
-                                                  double4_32a* __restrict__ R4, double* __restrict__ part) {
+                                                  double4_32a* __restrict__ R4, double4_32a* __restrict__ M4,
+                                                  double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -47,6 +48,10 @@ __global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uin
         const q4 R = qnorm(qmul(exp_map(d3{r[0], r[1], r[2]}), b));
         x4[i] = make_double4_32a(xx, xy, xz, 0.0);
         R4[i] = make_double4_32a(R.w, R.x, R.y, R.z);
+        const m3 M = quat_matrix(R);
+        M4[3 * size_t(i)] = make_double4_32a(M.r0.x, M.r0.y, M.r0.z, 0.0);
+        M4[3 * size_t(i) + 1] = make_double4_32a(M.r1.x, M.r1.y, M.r1.z, 0.0);
+        M4[3 * size_t(i) + 2] = make_double4_32a(M.r2.x, M.r2.y, M.r2.z, 0.0);
         acc[0] = xx; acc[1] = xy; acc[2] = xz;
         // bounding box for the contact grid; fmin/fmax skip NaN coordinates
         mx[0] = -xx; mx[1] = -xy; mx[2] = -xz; mx[3] = xx; mx[4] = xy; mx[5] = xz;
@@ -90,13 +95,15 @@ __global__ void __launch_bounds__(kBlock) k_center(int N, int nparts, const doub
 
 // ---- constitutive return maps: MC/src/sim.cpp:5-8 ------------------------------------------
 struct Ret1 { double force, p, a, dg, energy, hard; bool yielded; };
-__device__ __forceinline__ Ret1 return1(double total, double pc, double ac, double k, double y, double H) {
+// inv_kH = 1 / max(1e-20, k + H), precomputed per beam (the reference divides).
+__device__ __forceinline__ Ret1 return1(double total, double pc, double ac, double k, double y, double H,
+                                        double inv_kH) {
     Ret1 r;
     const double trial = k * (total - pc);
     const double f = fabs(trial) - (y + H * ac);
     if (f > 0) {
         const double s = trial >= 0 ? 1.0 : -1.0;
-        r.dg = f / fmax(1e-20, k + H);
+        r.dg = f * inv_kH;
         r.p = pc + s * r.dg;
         r.a = ac + r.dg;
         r.yielded = true;
@@ -109,14 +116,14 @@ __device__ __forceinline__ Ret1 return1(double total, double pc, double ac, doub
     return r;
 }
 struct Ret3 { d3 force, p; double a, dg, energy, hard; bool yielded; };
-__device__ __forceinline__ Ret3 return3(d3 t, d3 pc, double ac, double k, double y, double H) {
+__device__ __forceinline__ Ret3 return3(d3 t, d3 pc, double ac, double k, double y, double H, double inv_kH) {
     Ret3 r;
     const d3 trial = (t - pc) * k;
     const double n = len(trial);
     const double f = n - (y + H * ac);
     if (f > 0 && n > 1e-20) {
         const d3 d = trial * (1.0 / n);
-        r.dg = f / fmax(1e-20, k + H);
+        r.dg = f * inv_kH;
         r.p = pc + d * r.dg;
         r.a = ac + r.dg;
         r.yielded = true;
@@ -137,6 +144,22 @@ __device__ __forceinline__ d3 ldx(const double4_32a* x, int i) {
     const double4_32a v = x[i];
     return d3{v.x, v.y, v.z};
 }
+__device__ __forceinline__ m3 ldm(const double4_32a* M, int i) {
+    const double4_32a a = M[3 * size_t(i)], b = M[3 * size_t(i) + 1], c = M[3 * size_t(i) + 2];
+    return m3{d3{a.x, a.y, a.z}, d3{b.x, b.y, b.z}, d3{c.x, c.y, c.z}};
+}
+// Unit quaternion by one reciprocal square root (the reference divides by the norm).
+__device__ __forceinline__ q4 qnorm_fast(q4 q) {
+    const double n2 = q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z;
+    if (n2 < 1e-60) return q4{1, 0, 0, 0};
+    const double r = rsqrt(n2);
+    return q4{q.w * r, q.x * r, q.y * r, q.z * r};
+}
+// normalize() of MC/include/core.hpp:39 with a reciprocal square root.
+__device__ __forceinline__ d3 unit_fast(d3 v) {
+    const double l2 = len2(v);
+    return (isfinite(l2) && l2 > 1e-30) ? v * rsqrt(l2) : d3{0, 1, 0};
+}
 
 // ---- beam kernel: MC/src/sim.cpp:139-141 ---------------------------------------------------
 __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const double* __restrict__ plastic,
@@ -148,8 +171,10 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
     if (b < B) {
         const int2 ab = t.ab[b];
         const d3 xa = ldx(e.x, ab.x), xb = ldx(e.x, ab.y);
-        const d3 d = xb - xa;
-        const double L = len(d);
+        // chord, length and tangent rounded as the reference (no fused multiply-add), so
+        // that a beam at its rest length has exactly zero strain here too
+        const d3 d{__dsub_rn(xb.x, xa.x), __dsub_rn(xb.y, xa.y), __dsub_rn(xb.z, xa.z)};
+        const double L = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d.x, d.x), __dmul_rn(d.y, d.y)), __dmul_rn(d.z, d.z)));
         double* sa = e.slotA + 6 * size_t(b);
         double* sb = e.slotB + 6 * size_t(b);
         if (L < 1e-10) {
@@ -164,44 +189,56 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
                 for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
             }
         } else {
-            const double L0 = t.L0[b];
             const double pl_epsp = plastic[b], pl_alpha = plastic[size_t(B) + b];
             const d3 rotp{plastic[2 * size_t(B) + b], plastic[3 * size_t(B) + b], plastic[4 * size_t(B) + b]};
             const double pl_alphaB = plastic[5 * size_t(B) + b], pl_alphaT = plastic[6 * size_t(B) + b];
-            const d3 tt = d * (1.0 / L);
+            const double invL = 1.0 / L;
+            const d3 tt{__dmul_rn(d.x, invL), __dmul_rn(d.y, invL), __dmul_rn(d.z, invL)};
             // axial
-            const double eps = (L - L0) / L0;
-            const Ret1 ax = return1(eps, pl_epsp, pl_alpha, m.E, m.sy, m.H);
+            const double eps = (L - t.L0[b]) * t.invL0[b];
+            const Ret1 ax = return1(eps, pl_epsp, pl_alpha, m.E, m.sy, m.H, m.inv_EH);
             const double aL = t.aL[b];
             const double uax = aL * (ax.energy + ax.hard);
             const double dax = t.aLsy[b] * ax.dg;
             const double Nf = t.area[b] * ax.force;
             d3 F = tt * Nf;
-            // shear: the end directors against the chord
-            const q4 Ra = ldq(e.R, ab.x), Rb = ldq(e.R, ab.y);
+            // shear: the end directors against the chord (rotations by the nodes' matrices)
+            const m3 Ma = ldm(e.M, ab.x), Mb = ldm(e.M, ab.y);
             const d3 e0{t.e0x[b], t.e0y[b], t.e0z[b]};
-            const d3 da = qrot(Ra, e0), db = qrot(Rb, e0);
+            const d3 da = mrot(Ma, e0), db = mrot(Mb, e0);
             const double cs = t.cs[b];
             const d3 ma = da - tt, mb = db - tt;
             const double us = .5 * cs * (len2(ma) + len2(mb));
             const d3 gt = ((tt * 2.0 - da) - db) * cs;
-            const d3 trans = (gt - tt * dot(gt, tt)) * (1.0 / L);
+            const d3 trans = (gt - tt * dot(gt, tt)) * invL;
             F = F + trans;
             d3 Ga = -(cross(da, tt) * cs);
             d3 Gb = -(cross(db, tt) * cs);
-            // bending and torsion from the relative rotation
-            const q4 Q = qnorm(qmul(conj(Ra), Rb));
-            const d3 phi = log_map(Q);
-            const d3 axis = unit(qrot_inv(Ra, tt));
+            // bending and torsion from the relative rotation Q = Ra^* Rb
+            const q4 Ra = ldq(e.R, ab.x), Rb = ldq(e.R, ab.y);
+            q4 Q = qnorm_fast(qmul(conj(Ra), Rb));
+            if (Q.w < 0) Q = q4{-Q.w, -Q.x, -Q.y, -Q.z};
+            d3 phi;
+            {  // log map (MC/include/core.hpp:52); Q is already unit
+                const double s2 = Q.x * Q.x + Q.y * Q.y + Q.z * Q.z;
+                const double sq = sqrt(s2);
+                if (sq < 1e-12) {
+                    phi = d3{2 * Q.x, 2 * Q.y, 2 * Q.z};
+                } else {
+                    const double ang = 2 * atan2(sq, clampd(Q.w, -1, 1));
+                    phi = d3{Q.x, Q.y, Q.z} * (ang / sq);
+                }
+            }
+            const d3 axis = unit_fast(mrot_t(Ma, tt));
             const double tw = dot(phi, axis), ptw = dot(rotp, axis);
             const d3 bend = phi - axis * tw, pb = rotp - axis * ptw;
             const double kb = t.kb[b], kt = t.kt[b], my = t.my[b], ty = t.ty[b];
-            const Ret3 br = return3(bend, pb, pl_alphaB, kb, my, t.hb[b]);
-            const Ret1 tor = return1(tw, ptw, pl_alphaT, kt, ty, t.ht[b]);
+            const Ret3 br = return3(bend, pb, pl_alphaB, kb, my, t.hb[b], t.inv_kbh[b]);
+            const Ret1 tor = return1(tw, ptw, pl_alphaT, kt, ty, t.ht[b], t.inv_kth[b]);
             const d3 moment = br.force + axis * tor.force;
             const double ur = br.energy + br.hard + tor.energy + tor.hard;
             const double dr = my * br.dg + ty * tor.dg;
-            const d3 world = qrot(Ra, jl_inv_t(phi, moment));
+            const d3 world = mrot(Ma, jl_inv_t(phi, moment));
             Ga = Ga - world;
             Gb = Gb + world;
             acc[0] = (uax + dax) + us + (ur + dr);
@@ -352,7 +389,8 @@ __global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, 
                                                      const double* __restrict__ pbeam,
                                                      const double* __restrict__ pnode,
                                                      const double* __restrict__ pcont,
-                                                     const double* __restrict__ cen, EvalOut* out) {
+                                                     const double* __restrict__ cen,
+                                                     const uint32_t* __restrict__ flags, EvalOut* out) {
     __shared__ double sm[6 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
@@ -398,6 +436,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, 
         out->center_energy = center;
         out->contact_energy = contactE;
         out->platen_energy = acc[4];
+        out->overflow = flags ? int(flags[0] & ~uint32_t(kNonFinite)) : 0;
     }
 }
 
@@ -466,7 +505,7 @@ __global__ void __launch_bounds__(kBlock) k_plastic_final(int nparts, const doub
 void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                   const double* base_r, EvalBufs& e, cudaStream_t s) {
     const int nb = nb_nodes(t.N);
-    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.part_state);
+    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.M, e.part_state);
     k_center<<<1, kBlock, 0, s>>>(t.N, nb, e.part_state, e.cen);
     note_launches(2);
 }
@@ -503,7 +542,7 @@ void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c
                      cudaStream_t s) {
     const int ncp = c ? contact_part_blocks(c->contact_cap) : 0;
     k_finalize<<<1, kBlock, 0, s>>>(t.B ? nb_beams(t.B) : 0, nb_nodes(t.N), ncp, p, e.part_beam, e.part_node,
-                                    c ? c->part : nullptr, e.cen, e.out);
+                                    c ? c->part : nullptr, e.cen, c ? c->flags : nullptr, e.out);
     const long long n = 6LL * t.N;
     k_zero_if_nonfinite<<<grid_for(n < 152 * 4 * kBlock ? n : 152 * 4 * kBlock), kBlock, 0, s>>>(n, e.out, grad);
     note_launches(2);

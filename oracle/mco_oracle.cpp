@@ -295,6 +295,11 @@ struct orc_model {
     double width = 0, height = 0, depth = 0, area = 0, mass = 0, top0 = 0;
     // run() bookkeeping (sim.hpp:47)
     double loadingWork = 0, recoveredWork = 0, prevDisp = 0, prevForce = 0, reactionOffset = 0;
+    // Rounding-order variant (0 = the reference's order).  Bits: 1 adds gravity to the node
+    // forces before the beam loop, 2 scatters the beams in descending order, 4 adds the
+    // centering force before the beam loop.  Each is the same sum in another order; runs
+    // under these variants measure how far rounding alone moves a load/unload trajectory.
+    int variant = 0;
     // last minimize, for commit
     std::vector<double> lastZ;
     Eval lastFinal;
@@ -520,7 +525,18 @@ struct orc_model {
         state(z, x, R);
         const double E = cfg.material.young, G = E / (2 * (1 + cfg.material.nu));
         const double sy = cfg.material.yield, H = cfg.material.hardening;
-        for (size_t bi = 0; bi < beams.size(); bi++) {  // sim.cpp:139-141
+        V3 cen;  // centering, sim.cpp:143
+        for (const V3& p : x) addTo(cen, p);
+        cen = divide(cen, double(x.size()));
+        if (variant & 1)
+            for (size_t i = 0; i < nodes.size(); i++) gx[i].y += nodes[i].mass * cfg.gravity;
+        if (variant & 4)
+            for (V3& g : gx) {
+                g.x += cfg.centering_stiffness * cen.x / x.size();
+                g.z += cfg.centering_stiffness * cen.z / x.size();
+            }
+        for (size_t bk = 0; bk < beams.size(); bk++) {  // sim.cpp:139-141
+            const size_t bi = (variant & 2) ? beams.size() - 1 - bk : bk;
             const BeamRec& e = beams[bi];
             const V3 d = x[size_t(e.b)] - x[size_t(e.a)];
             const double L = len(d);
@@ -577,16 +593,14 @@ struct orc_model {
         for (size_t i = 0; i < nodes.size(); i++) {  // gravity, sim.cpp:142
             const double u = nodes[i].mass * cfg.gravity * x[i].y;
             o.energy += u;
-            gx[i].y += nodes[i].mass * cfg.gravity;
+            if (!(variant & 1)) gx[i].y += nodes[i].mass * cfg.gravity;
         }
-        V3 cen;  // centering, sim.cpp:143
-        for (const V3& p : x) addTo(cen, p);
-        cen = divide(cen, double(x.size()));
         o.energy += .5 * cfg.centering_stiffness * (sqr(cen.x) + sqr(cen.z));
-        for (V3& g : gx) {
-            g.x += cfg.centering_stiffness * cen.x / x.size();
-            g.z += cfg.centering_stiffness * cen.z / x.size();
-        }
+        if (!(variant & 4))
+            for (V3& g : gx) {
+                g.x += cfg.centering_stiffness * cen.x / x.size();
+                g.z += cfg.centering_stiffness * cen.z / x.size();
+            }
         const double jr = jointRadius();
         if (cfg.self_contact) {
             const std::vector<Shape> shapes = shapesOf(x);
@@ -1156,5 +1170,10 @@ double orc_beam_potential(const orc_model* m, const double* x, const double* r) 
 }
 
 double orc_top_y(const orc_model* m, double s, int loading) { return m->topY(s, loading != 0); }
+
+int orc_set_variant(orc_model* m, int variant) {
+    m->variant = variant;
+    return 0;
+}
 
 }  // extern "C"

@@ -71,6 +71,10 @@ double orc_gradient_check_error(const orc_model* m);   /* MC/src/sim.cpp:538-577
 double orc_beam_potential(const orc_model* m, const double* x, const double* r); /* :468 */
 double orc_top_y(const orc_model* m, double s, int loading);                        /* :213 */
 
+/* Rounding-order variant of the restatement's gradient accumulation (0 = the reference's
+ * order; see mco_oracle.cpp).  The reference harness accepts only 0 and returns -1. */
+int orc_set_variant(orc_model* m, int variant);
+
 #ifdef __cplusplus
 }
 #endif

@@ -72,6 +72,7 @@ def load(which="mco"):
         "orc_gradient_check_error": (C.c_double, [P]),
         "orc_beam_potential": (C.c_double, [P, _d, _d]),
         "orc_top_y": (C.c_double, [P, C.c_double, C.c_int]),
+        "orc_set_variant": (C.c_int, [P, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -185,6 +186,10 @@ class Model:
 
     def beam_potential(self, x, r):
         return self.lib.orc_beam_potential(self.h, ptr(_f64(x)), ptr(_f64(r)))
+
+    def set_variant(self, v):
+        if self.lib.orc_set_variant(self.h, int(v)) != 0:
+            raise ValueError(f"variant {v} not supported by the {self.which} oracle")
 
     def top_y(self, s, loading):
         return self.lib.orc_top_y(self.h, s, int(loading))

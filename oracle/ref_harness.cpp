@@ -360,4 +360,6 @@ double orc_beam_potential(const orc_model* m, const double* x, const double* r) 
 
 double orc_top_y(const orc_model* m, double s, int loading) { return m->sim->topY(s, loading != 0); }
 
+int orc_set_variant(orc_model*, int variant) { return variant == 0 ? 0 : -1; }  // the reference has one order
+
 }  // extern "C"

@@ -14,6 +14,9 @@ reference's own Simulator (MC/src/sim.cpp) through oracle/ref_harness.cpp:
   bcc4.npz         a 4x4x4 cubic+BCC specimen at the heavy deformation of the
                    single-evaluation workload (many self-contacts).
   cubic6_run.npz   (--run-cubic6) the 6x6x6 specimen's full 200/200 load/unload run.
+  ref242_ensemble.npz  (--ensemble) the 20/14 run of the reference specimen under the CPU
+                   restatement's rounding-order variants 1..7: the same sums in other orders.
+                   Their spread is how far rounding alone moves the run-level results.
 """
 import argparse
 import os
@@ -217,15 +220,35 @@ def make_cubic6_run():
     np.savez_compressed(os.path.join(OUT, "cubic6_run.npz"), **out)
 
 
+def make_ensemble(variants=range(1, 8)):
+    print("ref242_ensemble")
+    cfg = reference_config_242()
+    orc.build("mco")
+    out = {"frame_keys": np.array(FRAME_KEYS), "variants": np.array(list(variants))}
+    for v in variants:
+        m = orc.Model("mco", cfg)
+        m.set_variant(v)
+        t = time.time()
+        rc, frames = m.run()
+        peak = max(f["reaction_force"] for f in frames) if frames else float("nan")
+        print(f"  variant {v}: rc={rc} frames={len(frames)} peak={peak:.4f} in {time.time() - t:.1f}s")
+        out[f"v{v}_rc"] = np.array([rc])
+        out[f"v{v}_frames"] = frames_array(frames)
+    np.savez_compressed(os.path.join(OUT, "ref242_ensemble.npz"), **out)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--run-cubic6", action="store_true")
+    ap.add_argument("--ensemble", action="store_true")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     if not orc.build("ref"):
         sys.exit("the reference sources are not available: fixtures cannot be generated here")
     fd.load()
-    if a.only in (None, "ref242"):
+    if a.only == "none":
+        pass
+    elif a.only in (None, "ref242"):
         make_ref242()
     if a.only in (None, "cubic6"):
         make_synthetic("cubic6", workloads.cubic6(), (0.05, 0.1))
@@ -233,6 +256,8 @@ def main():
         make_synthetic("bcc4", workloads.bcc((4, 4, 4)), (0.05, 0.1), minimize=False)
     if a.run_cubic6:
         make_cubic6_run()
+    if a.ensemble:
+        make_ensemble()
 
 
 if __name__ == "__main__":

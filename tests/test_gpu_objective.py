@@ -39,10 +39,33 @@ def check_eval(r, s, ctx):
     assert d["contacts"] == int(ref[5]), (ctx, d["contacts"], ref[5])
 
 
+def trial_scales(g):
+    """Per-column magnitude of the trial outputs over the fixture's deformed states, so that
+    states at rest (exactly zero strain in the reference, ~1e-16 here) compare on the same
+    absolute scale as deformed ones."""
+    nxt = np.zeros(7)
+    aux = np.zeros(7)
+    for k in range(g.n_states):
+        s = g.state(k)
+        if s["trials"] and np.isfinite(s["energy"]):
+            nxt = np.maximum(nxt, np.linalg.norm(s["trial_next"].reshape(-1, 7), axis=0))
+            aux = np.maximum(aux, np.linalg.norm(s["trial_aux"].reshape(-1, 7), axis=0))
+    return nxt, aux
+
+
+def close_cols(a, b, scale, tol=TOL):
+    a = a.reshape(-1, 7)
+    b = b.reshape(-1, 7)
+    err = np.linalg.norm(a - b, axis=0)
+    ref = np.maximum(np.linalg.norm(b, axis=0), scale)
+    return np.all(err <= tol * np.maximum(ref, 1e-300)), err / np.maximum(ref, 1e-300)
+
+
 @pytest.mark.parametrize("case", CASES)
 def test_objective_matches_reference_fixtures(mcg, case):
     g = golden(case)
     s0 = solver_for(mcg, g)
+    sn, sa = trial_scales(g)
     for k in range(g.n_states):
         s = g.state(k)
         s0.set_state(plastic=s["plastic"])
@@ -51,8 +74,10 @@ def test_objective_matches_reference_fixtures(mcg, case):
         if np.isfinite(s["energy"]):
             assert np.array_equal(s0.contact_pairs(), s["pairs"]), (case, k)
         if s["trials"] and np.isfinite(s["energy"]):
-            assert rel_err(r["trial_next"], s["trial_next"]) <= TOL, (case, k)
-            assert rel_err(r["trial_aux"], s["trial_aux"]) <= TOL, (case, k)
+            ok, err = close_cols(r["trial_next"], s["trial_next"], sn)
+            assert ok, (case, k, err)
+            ok, err = close_cols(r["trial_aux"], s["trial_aux"], sa)
+            assert ok, (case, k, err)
             assert np.array_equal(r["trial_flags"], s["trial_flags"]), (case, k)
 
 
@@ -86,7 +111,8 @@ def test_objective_matches_oracle_on_larger_lattices(mcg, mco):
                                                        "max_pen", "contacts")])}
         check_eval(r, s, ("bcc8", sig))
         assert np.array_equal(sol.contact_pairs(), orc.contact_pairs(z))
-        assert rel_err(r["trial_next"], o["trial_next"]) <= TOL
+        ok, err = close_cols(r["trial_next"], o["trial_next"], np.zeros(7))
+        assert ok, err
 
 
 def test_self_contact_off_drops_only_the_pair_terms(mcg):
