@@ -18,8 +18,9 @@
 // A conservative FP32 AABB test and the local-shape exclusion (sim.cpp:24-39) run before
 // the FP64 narrow phase.
 //
-// Output order.  Contacts are counted per bin, scanned, and written by a second pass over
-// the bins that have any, in (bin, pair) order: the contact list and every sum over it are
+// Output order.  Candidate pairs are counted per bin, scanned and written in (bin, pair)
+// order; the narrow phase flags the candidates in contact, a scan places them, and the
+// contact list keeps the candidate order: the list and every sum over it are
 // deterministic.  Per-node force lists are built with counters and sorted by the gather.
 //
 // No host synchronisation: sizes that can overflow a buffer (entries, bins, contacts, a
@@ -156,31 +157,34 @@ __device__ __forceinline__ bool is_connected(const DevTopo& t, int u, int v) {
     return false;
 }
 
-// Same beam, a shared node, or a connected node pair (sim.cpp:24-39).  Shapes are
-// distinct here, so "same beam" cannot occur.
-__device__ __forceinline__ bool excluded(const DevTopo& t, int2 a, int2 b) {
+// Local shapes (sim.cpp:24-39): a shared node, or a connected node pair.  Shapes are
+// distinct here, so "same beam" cannot occur.  The shared-node half is cheap and decides
+// most broad-phase candidates in a lattice; the connected half scans adjacency lists.
+__device__ __forceinline__ bool share_node(int2 a, int2 b) {
+    return a.x == b.x || (b.y >= 0 && a.x == b.y) || (a.y >= 0 && (a.y == b.x || (b.y >= 0 && a.y == b.y)));
+}
+__device__ __forceinline__ bool any_connected(const DevTopo& t, int2 a, int2 b) {
     const int an[2] = {a.x, a.y}, bn[2] = {b.x, b.y};
     const int na = a.y >= 0 ? 2 : 1, nb = b.y >= 0 ? 2 : 1;
-    for (int i = 0; i < na; ++i)
-        for (int j = 0; j < nb; ++j)
-            if (an[i] == bn[j]) return true;
     for (int i = 0; i < na; ++i)
         for (int j = 0; j < nb; ++j)
             if (is_connected(t, an[i], bn[j])) return true;
     return false;
 }
 
-// Full test of one candidate pair (sa < sb): exclusion, FP64 closest points, dist < target.
+// Rest of the test of a candidate pair (sa < sb) that shares no node: connected-pair
+// exclusion, FP64 closest points, dist < target.  Out of line: few candidates get here,
+// and keeping its registers out of the pair loop keeps that loop's occupancy up.
 struct PairHit {
     bool hit;
     double s, t, pen;
     d3 n;
 };
-__device__ __forceinline__ PairHit test_pair(const DevTopo& t, const PhysParams& p, const double4_32a* x, uint32_t sa,
-                                             uint32_t sb) {
+__device__ __noinline__ PairHit narrow_phase(const DevTopo& t, const PhysParams& p, const double4_32a* x, uint32_t sa,
+                                             uint32_t sb, int2 na, int2 nb) {
     PairHit h;
     h.hit = false;
-    if (excluded(t, shape_nodes(t, sa), shape_nodes(t, sb))) return h;
+    if (any_connected(t, na, nb)) return h;
     const ShapeRef A = load_shape(t, x, p.joint_radius, sa);
     const ShapeRef B = load_shape(t, x, p.joint_radius, sb);
     const Closest cp = shape_closest(A, B);
@@ -240,22 +244,29 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
     grid[8] = ok ? int(nb) : 0;
 }
 
-__global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                       const int* __restrict__ grid, int4* __restrict__ cell_lo,
-                                                       int4* __restrict__ cell_hi, float4* __restrict__ bb_lo,
-                                                       float4* __restrict__ bb_hi, uint32_t* __restrict__ count,
-                                                       uint32_t* __restrict__ flags) {
+// Per-shape bounding box and cell range, in single precision rounded outward: the box
+// contains the reference's double-precision box (sim.cpp:154), and cell indices are a
+// monotone function of it, so two shapes whose reference boxes overlap share a cell.
+__global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, const float4* __restrict__ xf_lo,
+                                                       const float4* __restrict__ xf_hi, const int* __restrict__ grid,
+                                                       int4* __restrict__ cell_lo, int4* __restrict__ cell_hi,
+                                                       float4* __restrict__ bb_lo, float4* __restrict__ bb_hi,
+                                                       uint32_t* __restrict__ count, uint32_t* __restrict__ flags) {
     const int S = t.N + t.B;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;
-    const ShapeRef sh = load_shape(t, x, p.joint_radius, uint32_t(s));
-    const double pad = sh.r + p.contact_margin;
-    const d3 lo{fmin(sh.a.x, sh.b.x) - pad, fmin(sh.a.y, sh.b.y) - pad, fmin(sh.a.z, sh.b.z) - pad};
-    const d3 hi{fmax(sh.a.x, sh.b.x) + pad, fmax(sh.a.y, sh.b.y) + pad, fmax(sh.a.z, sh.b.z) + pad};
-    bb_lo[s] = make_float4(__double2float_rd(lo.x), __double2float_rd(lo.y), __double2float_rd(lo.z), 0.f);
-    bb_hi[s] = make_float4(__double2float_ru(hi.x), __double2float_ru(hi.y), __double2float_ru(hi.z), 0.f);
-    const bool finite_box = isfinite(lo.x) && isfinite(lo.y) && isfinite(lo.z) && isfinite(hi.x) &&
-                            isfinite(hi.y) && isfinite(hi.z);
+    const int2 nd = shape_nodes(t, uint32_t(s));
+    const int n1 = nd.y >= 0 ? nd.y : nd.x;
+    const float4 al = xf_lo[nd.x], ah = xf_hi[nd.x], bl = xf_lo[n1], bh = xf_hi[n1];
+    const float pad = s < t.N ? p.joint_padf : t.padf[s - t.N];
+    const float lo[3] = {__fsub_rd(fminf(al.x, bl.x), pad), __fsub_rd(fminf(al.y, bl.y), pad),
+                         __fsub_rd(fminf(al.z, bl.z), pad)};
+    const float hi[3] = {__fadd_ru(fmaxf(ah.x, bh.x), pad), __fadd_ru(fmaxf(ah.y, bh.y), pad),
+                         __fadd_ru(fmaxf(ah.z, bh.z), pad)};
+    bb_lo[s] = make_float4(lo[0], lo[1], lo[2], 0.f);
+    bb_hi[s] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    const bool finite_box = isfinite(lo[0]) && isfinite(lo[1]) && isfinite(lo[2]) && isfinite(hi[0]) &&
+                            isfinite(hi[1]) && isfinite(hi[2]);
     if (!grid[7] || !finite_box) {
         count[s] = 0;
         cell_lo[s] = make_int4(0, 0, 0, 0);
@@ -263,14 +274,14 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
         if (!finite_box) atomicOr(flags, uint32_t(kNonFinite));
         return;
     }
-    const double cl[3] = {lo.x, lo.y, lo.z}, ch[3] = {hi.x, hi.y, hi.z};
     int c0[3], c1[3];
     long long n = 1;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        const double dim = double(grid[3 + d]) - 1.0;
-        c0[d] = int(clampd(floor(cl[d] / p.broad_cell) - double(grid[d]), 0.0, dim));
-        c1[d] = int(clampd(floor(ch[d] / p.broad_cell) - double(grid[d]), 0.0, dim));
+        const float dim = float(grid[3 + d] - 1);
+        const float org = float(grid[d]);
+        c0[d] = int(fminf(fmaxf(floorf(lo[d] * p.inv_cell_f) - org, 0.f), dim));
+        c1[d] = int(fminf(fmaxf(floorf(hi[d] * p.inv_cell_f) - org, 0.f), dim));
         n *= (long long)(c1[d] - c0[d] + 1);
     }
     if (n > kMaxCellsPerShape) {  // the host coarsens the grid and evaluates again
@@ -333,47 +344,102 @@ struct BinShape {
     uint32_t s;
     int lx, ly, lz;
     float bx0, by0, bz0, bx1, by1, bz1;
+    int n0, n1;
 };
 
-__device__ __forceinline__ void write_contact(ContactBufs& c, uint32_t pos, uint32_t sa, uint32_t sb, const PairHit& h) {
-    if (pos >= uint32_t(c.contact_cap)) return;
-    c.c_a[pos] = sa;
-    c.c_b[pos] = sb;
-    c.c_s[pos] = h.s;
-    c.c_t[pos] = h.t;
-    c.c_n[3 * size_t(pos)] = h.n.x;
-    c.c_n[3 * size_t(pos) + 1] = h.n.y;
-    c.c_n[3 * size_t(pos) + 2] = h.n.z;
-    c.c_pen[pos] = h.pen;
+__device__ __forceinline__ BinShape load_bin_shape(const DevTopo& t, uint32_t v, const int4* __restrict__ cell_lo,
+                                                   const float4* __restrict__ bb_lo, const float4* __restrict__ bb_hi) {
+    const int4 l = cell_lo[v];
+    const float4 a = bb_lo[v], z = bb_hi[v];
+    const int2 nd = shape_nodes(t, v);
+    return BinShape{v, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z, nd.x, nd.y};
 }
 
-// One warp per occupied bin.  emit == 0: contacts per bin into bcount.  emit != 0: the
-// contacts of bins with bcount > 0 written at boffset, in pair order.
-__global__ void __launch_bounds__(kBlock) k_pairs(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                  const int* __restrict__ grid, const uint32_t* __restrict__ bin_count,
-                                                  const uint32_t* __restrict__ bin_start,
-                                                  const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
-                                                  const int4* __restrict__ cell_lo, const float4* __restrict__ bb_lo,
-                                                  const float4* __restrict__ bb_hi, int emit,
-                                                  uint32_t* __restrict__ bcount, const uint32_t* __restrict__ boffset,
-                                                  ContactBufs c) {
+// Broad-phase filter of one pair in cell cc: first common cell, AABB overlap, no shared
+// node.  Survivors become narrow-phase candidates.
+__device__ __forceinline__ bool candidate(const BinShape& A, const BinShape& B, int3 cc) {
+    return max(A.lx, B.lx) == cc.x && max(A.ly, B.ly) == cc.y && max(A.lz, B.lz) == cc.z &&
+           !(A.bx0 > B.bx1 || B.bx0 > A.bx1 || A.by0 > B.by1 || B.by0 > A.by1 || A.bz0 > B.bz1 || B.bz0 > A.bz1) &&
+           !share_node(make_int2(A.n0, A.n1), make_int2(B.n0, B.n1));
+}
+
+__device__ __forceinline__ BinShape shfl_shape(const BinShape& v, int src) {
+    BinShape o;
+    o.s = __shfl_sync(0xffffffffu, v.s, src);
+    o.lx = __shfl_sync(0xffffffffu, v.lx, src);
+    o.ly = __shfl_sync(0xffffffffu, v.ly, src);
+    o.lz = __shfl_sync(0xffffffffu, v.lz, src);
+    o.bx0 = __shfl_sync(0xffffffffu, v.bx0, src);
+    o.by0 = __shfl_sync(0xffffffffu, v.by0, src);
+    o.bz0 = __shfl_sync(0xffffffffu, v.bz0, src);
+    o.bx1 = __shfl_sync(0xffffffffu, v.bx1, src);
+    o.by1 = __shfl_sync(0xffffffffu, v.by1, src);
+    o.bz1 = __shfl_sync(0xffffffffu, v.bz1, src);
+    o.n0 = __shfl_sync(0xffffffffu, v.n0, src);
+    o.n1 = __shfl_sync(0xffffffffu, v.n1, src);
+    return o;
+}
+
+// Candidate pairs of every occupied bin, one warp per bin.  write == 0: the count per bin
+// into bcount.  write != 0: the pairs (lower shape, higher shape) at boffset, in the
+// enumeration order, which is fixed:
+//   n <= 32  the bin's shapes are sorted across the warp's lanes (bitonic, by shape id)
+//            and every unordered pair is visited by rotation: in round k lane i meets
+//            lane (i + k) mod n, k = 1 .. n/2 (the last round of an even n only from the
+//            lower half), the partner's data arriving by register shuffles;
+//   n <= 64  the sorted shapes are staged in shared memory and the pairs enumerated by
+//            index;
+//   larger   sorted through a scratch copy, pairs read from global memory.
+__global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
+                                                      const uint32_t* __restrict__ bin_count,
+                                                      const uint32_t* __restrict__ bin_start,
+                                                      const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
+                                                      const int4* __restrict__ cell_lo, const float4* __restrict__ bb_lo,
+                                                      const float4* __restrict__ bb_hi, int write,
+                                                      uint32_t* __restrict__ bcount, const uint32_t* __restrict__ boffset,
+                                                      long long cand_cap, uint2* __restrict__ cand) {
     __shared__ BinShape sh[kPairWarps][kWarpCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
     const long long nb = grid[8];
     const long long warps = (long long)gridDim.x * kPairWarps;
     for (long long b = (long long)blockIdx.x * kPairWarps + w; b < nb; b += warps) {
         const int n = int(bin_count[b]);
-        if (n < 2 || (emit && bcount[b] == 0)) {
-            if (!emit && lane == 0) bcount[b] = 0;
+        if (n < 2 || (write && bcount[b] == 0)) {
+            if (!write && lane == 0) bcount[b] = 0;
             continue;
         }
         const uint32_t start = bin_start[b];
         const int3 cc = cell_of(grid, uint32_t(b));
-        uint32_t found = 0;
-        uint32_t out = emit ? boffset[b] : 0;
-        if (n <= kWarpCap) {
-            // stage the bin in ascending shape order: rank = number of smaller shape ids
-            const uint32_t v0 = lane < n ? sorted[start + lane] : 0xffffffffu;
+        uint32_t out = write ? boffset[b] : 0;
+        auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (write && hit) {
+                const uint32_t pos = out + __popc(m & below);
+                if (pos < uint32_t(cand_cap)) cand[pos] = make_uint2(sa, sb);
+            }
+            out += __popc(m);
+        };
+        if (n <= 32) {
+            uint32_t v = lane < n ? sorted[start + lane] : 0xffffffffu;
+            for (int k = 2; k <= 32; k <<= 1)  // bitonic sort, ascending
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+                    const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+                    v = (lower == up) ? min(v, o) : max(v, o);
+                }
+            BinShape me{};
+            if (lane < n) me = load_bin_shape(t, v, cell_lo, bb_lo, bb_hi);
+            const int half = n >> 1;
+            for (int k = 1; k <= half; k++) {
+                const int src = lane < n ? (lane + k < n ? lane + k : lane + k - n) : lane;
+                const BinShape o = shfl_shape(me, src);
+                const bool active = lane < n && !((n & 1) == 0 && k == half && lane >= half);
+                const bool hit = active && candidate(me, o, cc);
+                emit(hit, min(me.s, o.s), max(me.s, o.s));
+            }
+        } else if (n <= kWarpCap) {
+            const uint32_t v0 = sorted[start + lane];
             const uint32_t v1 = lane + 32 < n ? sorted[start + 32 + lane] : 0xffffffffu;
             int r0 = 0, r1 = 0;
             for (int q = 0; q < 32; q++) {
@@ -382,41 +448,22 @@ __global__ void __launch_bounds__(kBlock) k_pairs(DevTopo t, PhysParams p, const
                 r1 += (u0 < v1) + (u1 < v1);
             }
             __syncwarp();
-            if (v0 != 0xffffffffu) {
-                const int4 l = cell_lo[v0];
-                const float4 a = bb_lo[v0], z = bb_hi[v0];
-                sh[w][r0] = BinShape{v0, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z};
-            }
-            if (v1 != 0xffffffffu) {
-                const int4 l = cell_lo[v1];
-                const float4 a = bb_lo[v1], z = bb_hi[v1];
-                sh[w][r1] = BinShape{v1, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z};
-            }
+            sh[w][r0] = load_bin_shape(t, v0, cell_lo, bb_lo, bb_hi);
+            if (v1 != 0xffffffffu) sh[w][r1] = load_bin_shape(t, v1, cell_lo, bb_lo, bb_hi);
             __syncwarp();
             const int P = n * (n - 1) / 2;
             for (int base = 0; base < P; base += 32) {
                 const int pidx = base + lane;
                 bool hit = false;
-                PairHit h;
                 uint32_t sa = 0, sb = 0;
                 if (pidx < P) {
                     int i, j;
                     pair_index(n, pidx, i, j);
-                    const BinShape& A = sh[w][i];
-                    const BinShape& B = sh[w][j];
-                    if (max(A.lx, B.lx) == cc.x && max(A.ly, B.ly) == cc.y && max(A.lz, B.lz) == cc.z &&
-                        !(A.bx0 > B.bx1 || B.bx0 > A.bx1 || A.by0 > B.by1 || B.by0 > A.by1 || A.bz0 > B.bz1 ||
-                          B.bz0 > A.bz1)) {
-                        sa = A.s;
-                        sb = B.s;
-                        h = test_pair(t, p, x, sa, sb);
-                        hit = h.hit;
-                    }
+                    hit = candidate(sh[w][i], sh[w][j], cc);
+                    sa = sh[w][i].s;
+                    sb = sh[w][j].s;
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (emit && hit) write_contact(c, out + __popc(m & ((1u << lane) - 1u)), sa, sb, h);
-                out += __popc(m);
-                found += __popc(m);
+                emit(hit, sa, sb);
             }
             __syncwarp();
         } else {
@@ -434,7 +481,6 @@ __global__ void __launch_bounds__(kBlock) k_pairs(DevTopo t, PhysParams p, const
             for (long long base = 0; base < P; base += 32) {
                 const long long pidx = base + lane;
                 bool hit = false;
-                PairHit h;
                 uint32_t sa = 0, sb = 0;
                 if (pidx < P) {
                     while (pidx >= row_end) {  // rows advance monotonically with base
@@ -442,29 +488,55 @@ __global__ void __launch_bounds__(kBlock) k_pairs(DevTopo t, PhysParams p, const
                         row_end += n - 1 - i;
                     }
                     const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                    sa = sorted2[start + i];
-                    sb = sorted2[start + j];
-                    const int4 la = cell_lo[sa], lb = cell_lo[sb];
-                    const float4 a0 = bb_lo[sa], a1 = bb_hi[sa], b0 = bb_lo[sb], b1 = bb_hi[sb];
-                    if (max(la.x, lb.x) == cc.x && max(la.y, lb.y) == cc.y && max(la.z, lb.z) == cc.z &&
-                        !(a0.x > b1.x || b0.x > a1.x || a0.y > b1.y || b0.y > a1.y || a0.z > b1.z || b0.z > a1.z)) {
-                        h = test_pair(t, p, x, sa, sb);
-                        hit = h.hit;
-                    }
+                    const BinShape A = load_bin_shape(t, sorted2[start + i], cell_lo, bb_lo, bb_hi);
+                    const BinShape B = load_bin_shape(t, sorted2[start + j], cell_lo, bb_lo, bb_hi);
+                    hit = candidate(A, B, cc);
+                    sa = A.s;
+                    sb = B.s;
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, hit);
-                if (emit && hit) write_contact(c, out + __popc(m & ((1u << lane) - 1u)), sa, sb, h);
-                out += __popc(m);
-                found += __popc(m);
+                emit(hit, sa, sb);
             }
             __syncwarp();
         }
-        if (!emit && lane == 0) bcount[b] = found;
+        if (!write && lane == 0) bcount[b] = out;
     }
 }
 
 constexpr int kContactPartBlocks = 128;
-constexpr int kStreamBlocks = 4 * 152;
+constexpr int kStreamBlocks = 8 * 152;
+
+// Narrow phase over the candidate list, one thread per candidate.  write == 0: hit flags
+// (1/0) into hit.  write != 0: the contacts of the hits at hoffset (the candidate order).
+__global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
+                                                   const uint32_t* __restrict__ ncand_p, long long cand_cap,
+                                                   const uint2* __restrict__ cand, int write,
+                                                   uint32_t* __restrict__ hit, const uint32_t* __restrict__ hoffset,
+                                                   ContactBufs c, uint32_t* flags) {
+    const long long nall = *ncand_p;
+    if (nall > cand_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, uint32_t(kOverCandidates));
+        return;
+    }
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nall; i += (long long)gridDim.x * blockDim.x) {
+        if (write && !hit[i]) continue;
+        const uint2 q = cand[i];
+        const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
+        if (!write) {
+            hit[i] = h.hit ? 1u : 0u;
+            continue;
+        }
+        const uint32_t pos = hoffset[i];
+        if (pos >= uint32_t(c.contact_cap)) continue;
+        c.c_a[pos] = q.x;
+        c.c_b[pos] = q.y;
+        c.c_s[pos] = h.s;
+        c.c_t[pos] = h.t;
+        c.c_n[3 * size_t(pos)] = h.n.x;
+        c.c_n[3 * size_t(pos) + 1] = h.n.y;
+        c.c_n[3 * size_t(pos) + 2] = h.n.z;
+        c.c_pen[pos] = h.pen;
+    }
+}
 
 // Fixed-partition reduction over the contact list: energy, max penetration, count.
 __global__ void __launch_bounds__(kBlock) k_contact_reduce(const uint32_t* __restrict__ total, long long cap, double k,
@@ -528,22 +600,33 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     cudaMemsetAsync(c.flags, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(c.bin_count, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
     (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad, p.broad_cell, c.bin_cap, c.grid, c.flags), note_launches(1));
-    (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.x, c.grid, c.cell_lo, c.cell_hi, c.bb_lo, c.bb_hi, c.count,
-                                                 c.flags), note_launches(1));
+    (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.bb_lo,
+                                                 c.bb_hi, c.count, c.flags), note_launches(1));
     exclusive_scan_u32(c.count, c.offset, S, c.scan_tmp, s);
     (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.offset, c.entry_cap, c.ekey, c.erank,
                                            c.bin_count, c.flags), note_launches(1));
     exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s);
     (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted),
      note_launches(1));
+    // candidates: count per bin, scan, write
     const unsigned pair_blocks = 152 * 8;
     cudaMemsetAsync(c.bcount, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
-    (k_pairs<<<pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
-                                            c.bb_lo, c.bb_hi, 0, c.bcount, c.boffset, c), note_launches(1));
+    (k_bin_pairs<<<pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
+                                                c.bb_lo, c.bb_hi, 0, c.bcount, c.boffset, c.cand_cap, c.cand),
+     note_launches(1));
     exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s);
-    (k_pairs<<<pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
-                                            c.bb_lo, c.bb_hi, 1, c.bcount, c.boffset, c), note_launches(1));
-    const uint32_t* total = c.boffset + c.bin_cap;
+    (k_bin_pairs<<<pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
+                                                c.bb_lo, c.bb_hi, 1, c.bcount, c.boffset, c.cand_cap, c.cand),
+     note_launches(1));
+    const uint32_t* ncand = c.boffset + c.bin_cap;
+    // narrow phase: hit flags, scan, contacts
+    cudaMemsetAsync(c.hit, 0, size_t(c.cand_cap + 1) * sizeof(uint32_t), s);
+    (k_narrow<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, ncand, c.cand_cap, c.cand, 0, c.hit, c.hoffset, c, c.flags),
+     note_launches(1));
+    exclusive_scan_u32(c.hit, c.hoffset, c.cand_cap, c.scan_tmp, s);
+    (k_narrow<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, ncand, c.cand_cap, c.cand, 1, c.hit, c.hoffset, c, c.flags),
+     note_launches(1));
+    const uint32_t* total = c.hoffset + c.cand_cap;
     (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, p.contact_k, c.c_pen, c.part, c.flags),
      note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);

@@ -36,6 +36,13 @@ struct Fail : std::runtime_error {
     Fail(int c, const std::string& m) : std::runtime_error(m), code(c) {}
 };
 
+// Smallest float not below x.
+float round_up_float(double x) {
+    float f = float(x);
+    if (double(f) < x) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+
 void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw Fail(MCG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
@@ -140,7 +147,7 @@ struct mcg_ctx {
 
     // ---- contact buffers ---------------------------------------------------------------
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
-    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap) {
+    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, long long cand_cap) {
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
@@ -162,6 +169,10 @@ struct mcg_ctx {
         c.bin_start = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
+        c.cand_cap = cand_cap;
+        c.cand = contact_mem.get<uint2>(size_t(cand_cap));
+        c.hit = contact_mem.get<uint32_t>(size_t(cand_cap + 1));
+        c.hoffset = contact_mem.get<uint32_t>(size_t(cand_cap + 1));
         c.contact_cap = contact_cap;
         c.c_a = contact_mem.get<uint32_t>(size_t(contact_cap));
         c.c_b = contact_mem.get<uint32_t>(size_t(contact_cap));
@@ -174,7 +185,7 @@ struct mcg_ctx {
         c.n_cursor = contact_mem.get<uint32_t>(size_t(N));
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.part = contact_mem.get<double>(size_t(3 * contact_part_blocks(contact_cap)));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max(std::max(S + 1, bin_cap + 1), (long long)N + 1));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, cand_cap + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         cb = c;
@@ -182,15 +193,17 @@ struct mcg_ctx {
 
     // Grows whatever the last evaluation overflowed; false when nothing did.
     bool grow_contacts(int flags) {
-        if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan))) return false;
+        if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan | kOverCandidates))) return false;
         const long long S = (long long)N + B;
-        uint32_t need[2] = {0, 0};
+        uint32_t need[3] = {0, 0, 0};
         int grid[16];
         ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(&need[1], cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[1], cb.hoffset + cb.cand_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[2], cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
-        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap;
+        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap, qcap = cb.cand_cap;
+        if (flags & kOverCandidates) qcap = std::max(qcap, (long long)need[2] + need[2] / 4 + 1024);
         if (flags & kOverSpan) broad_cell *= 2;
         if (flags & kOverEntries) ecap = std::max(ecap, (long long)need[0] + need[0] / 4 + 1024);
         if (flags & kOverContacts) ccap = std::max(ccap, (long long)need[1] + need[1] / 4 + 1024);
@@ -199,7 +212,7 @@ struct mcg_ctx {
             if (want <= (1LL << 28)) bcap = std::max(bcap, want);
             else broad_cell *= 2;  // a huge extent: coarser cells instead of more bins
         }
-        alloc_contacts(ecap, ccap, bcap);
+        alloc_contacts(ecap, ccap, bcap, qcap);
         return true;
     }
 
@@ -209,6 +222,7 @@ struct mcg_ctx {
         PhysParams p = phys;
         p.top = top;
         p.broad_cell = broad_cell;
+        p.inv_cell_f = float(1.0 / broad_cell);
         mark(0);
         launch_state(topo, p, dz, d_baseX, d_baseR, ev, stream);
         mark(1);
@@ -252,7 +266,7 @@ struct mcg_ctx {
     }
     long long read_contact_count() {
         uint32_t nc = 0;
-        ck(cudaMemcpyAsync(&nc, cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&nc, cb.hoffset + cb.cand_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
         return nc;
     }
@@ -648,6 +662,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         std::vector<double> kb(B), kt(B), my(B), ty(B), hb(B), ht(B), cs(B), aL(B), aLsy(B);
         std::vector<double> invL0(B), inv_kbh(B), inv_kth(B);
         std::vector<double> e0x(B), e0y(B), e0z(B);
+        std::vector<float> padf(B);
         double rmax = cf.joint_scale * cf.max_radius;
         std::vector<int> deg(size_t(N) + 1, 0);
         for (int b = 0; b < B; b++) {
@@ -681,6 +696,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
             e0y[b] = t->e0[3 * size_t(b) + 1];
             e0z[b] = t->e0[3 * size_t(b) + 2];
             rmax = std::max(rmax, r);
+            padf[b] = round_up_float(r + cf.contact_margin);
         }
         // incidence CSR in ascending beam order (the reference's scatter order)
         std::vector<int> inc_start(size_t(N) + 1, 0), inc(2 * size_t(B));
@@ -764,6 +780,11 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         int* dcs = M.get<int>(conn_start.size());
         h2d(dcs, conn_start.data(), conn_start.size(), s);
         T.conn_start = dcs;
+        {
+            float* dp = M.get<float>(size_t(B));
+            if (B) h2d(dp, padf.data(), size_t(B), s);
+            T.padf = dp;
+        }
         int* dc = M.get<int>(conn.size());
         if (!conn.empty()) h2d(dc, conn.data(), conn.size(), s);
         T.conn_nbr = dc;
@@ -780,6 +801,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         P.broad_cell = std::max(2.8 * c->jr, .72 * cf.cell_size);
         P.top = g->top0;
         P.self_contact = cf.self_contact ? 1 : 0;
+        P.joint_padf = round_up_float(c->jr + cf.contact_margin);
         c->phys = P;
         // state
         c->d_baseX = M.get<double>(3 * size_t(N));
@@ -801,6 +823,8 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         e.x = V.get<double4_32a>(size_t(N));
         e.R = V.get<double4_32a>(size_t(N));
         e.M = V.get<double4_32a>(3 * size_t(N));
+        e.xf_lo = V.get<float4>(size_t(N));
+        e.xf_hi = V.get<float4>(size_t(N));
         e.slotA = V.get<double>(6 * size_t(B));
         e.slotB = V.get<double>(6 * size_t(B));
         e.part_state = V.get<double>(9 * size_t(nb_nodes(N)));
@@ -834,7 +858,8 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
             int bits = 3;
             while ((1LL << bits) < dmax && bits < 10) bits++;
             const long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
-            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap);
+            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap,
+                              std::max<long long>(4 * S, 4096));
         }
         // solver vectors
         DevArena& Q = c->solver_mem;
@@ -1014,6 +1039,18 @@ int mcg_commit(mcg_ctx* c) {
         need_topo(c);
         c->commit();
         c->sync();
+    });
+}
+
+int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, int64_t contacts, int64_t bins) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (entries < 0 || candidates < 0 || contacts < 0 || bins < 0 || bins > (1LL << 28))
+            throw Fail(MCG_ERR_INVALID, "capacities must be non-negative and bins at most 2^28");
+        const long long lo = 4096;
+        c->sync();
+        c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
+                          std::max<long long>(bins, lo), std::max<long long>(candidates, lo));
     });
 }
 

@@ -40,11 +40,14 @@ struct DevTopo {
     const int* inc;           // [2B]
     const int* conn_start;    // [N+1] connected-pair adjacency (both directions, sorted)
     const int* conn_nbr;
+    const float* padf;        // [B] radius + contact margin, rounded up to single precision
 };
 
 struct PhysParams {
     double translation_scale, gravity, centering, contact_k, contact_margin, joint_radius;
     double broad_cell, top;
+    float joint_padf;        // joint radius + margin, rounded up to single precision
+    float inv_cell_f;        // 1 / broad_cell in single precision (broad-phase cell index)
     int self_contact;
 };
 
@@ -65,6 +68,7 @@ enum ContactFlag : uint32_t {
     kOverBins = 4,       // the grid needs more bins than bin_cap
     kNonFinite = 8,      // a shape has a non-finite bounding box (informational)
     kOverSpan = 16,      // a shape spans more cells than allowed: coarsen the grid
+    kOverCandidates = 32 // more narrow-phase candidates than cand_cap
 };
 
 struct ContactBufs {
@@ -87,8 +91,13 @@ struct ContactBufs {
     long long bin_cap;
     uint32_t* bin_count;    // [bin_cap+1]
     uint32_t* bin_start;    // [bin_cap+1]
-    uint32_t* bcount;       // [bin_cap+1] contacts found per bin
-    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = contact count
+    uint32_t* bcount;       // [bin_cap+1] candidate pairs per bin
+    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = candidate count
+    // narrow-phase candidates in (bin, pair) order
+    long long cand_cap;
+    uint2* cand;            // [cand_cap] (lower shape, higher shape)
+    uint32_t* hit;          // [cand_cap+1] 1 where the candidate is in contact
+    uint32_t* hoffset;      // [cand_cap+1] scan of hit; hoffset[cand_cap] = contact count
     // contacts, in deterministic (bin, pair) order
     long long contact_cap;
     uint32_t* c_a;          // lower shape index
@@ -111,6 +120,8 @@ struct EvalBufs {
     double4_32a* x;             // [N]
     double4_32a* R;             // [N]
     double4_32a* M;             // [3N] rotation matrix rows of R (x, y, z, pad)
+    float4* xf_lo;              // [N] position rounded down to single precision
+    float4* xf_hi;              // [N] position rounded up
     double* slotA;          // [6B] (-F, Ga) per beam, added to node a
     double* slotB;          // [6B] (+F, Gb) per beam, added to node b
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block

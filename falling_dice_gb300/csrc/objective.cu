@@ -22,6 +22,7 @@ __global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uin
                                                   const double* __restrict__ z, const double* __restrict__ bx,
                                                   const double* __restrict__ br, double4_32a* __restrict__ x4,
                                                   double4_32a* __restrict__ R4, double4_32a* __restrict__ M4,
+                                                  float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
                                                   double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
@@ -47,6 +48,9 @@ __global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uin
         const q4 b{br[4 * size_t(i)], br[4 * size_t(i) + 1], br[4 * size_t(i) + 2], br[4 * size_t(i) + 3]};
         const q4 R = qnorm(qmul(exp_map(d3{r[0], r[1], r[2]}), b));
         x4[i] = make_double4_32a(xx, xy, xz, 0.0);
+        // single-precision bounds of the position for the contact broad phase
+        xf_lo[i] = make_float4(__double2float_rd(xx), __double2float_rd(xy), __double2float_rd(xz), 0.f);
+        xf_hi[i] = make_float4(__double2float_ru(xx), __double2float_ru(xy), __double2float_ru(xz), 0.f);
         R4[i] = make_double4_32a(R.w, R.x, R.y, R.z);
         const m3 M = quat_matrix(R);
         M4[3 * size_t(i)] = make_double4_32a(M.r0.x, M.r0.y, M.r0.z, 0.0);
@@ -505,7 +509,8 @@ __global__ void __launch_bounds__(kBlock) k_plastic_final(int nparts, const doub
 void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                   const double* base_r, EvalBufs& e, cudaStream_t s) {
     const int nb = nb_nodes(t.N);
-    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.M, e.part_state);
+    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.M, e.xf_lo, e.xf_hi,
+                                  e.part_state);
     k_center<<<1, kBlock, 0, s>>>(t.N, nb, e.part_state, e.cen);
     note_launches(2);
 }

@@ -211,6 +211,13 @@ void* mcg_stream(mcg_ctx* ctx);
 /* Number of kernel launches the library has issued in this process. */
 int64_t mcg_launch_count(const mcg_ctx* ctx);
 
+/* Capacities of the self-contact buffers (no reference counterpart): grid-cell entries,
+ * narrow-phase candidates, contacts and grid bins.  They grow by themselves when an
+ * evaluation needs more (the evaluation is then repeated); setting them ahead avoids that
+ * repeat for a known workload.  Values below the minimum (4096) are raised to it. */
+int mcg_set_contact_capacity(mcg_ctx* ctx, int64_t entries, int64_t candidates, int64_t contacts,
+                             int64_t bins);
+
 /* Per-phase timing of evaluations with CUDA events on the context stream (no reference
  * counterpart).  While on, every evaluation synchronizes at its end and adds its phase
  * durations: [0] node state, [1] beam kernel, [2] self-contact pipeline, [3] gradient

@@ -297,8 +297,10 @@ struct orc_model {
     double loadingWork = 0, recoveredWork = 0, prevDisp = 0, prevForce = 0, reactionOffset = 0;
     // Rounding-order variant (0 = the reference's order).  Bits: 1 adds gravity to the node
     // forces before the beam loop, 2 scatters the beams in descending order, 4 adds the
-    // centering force before the beam loop.  Each is the same sum in another order; runs
-    // under these variants measure how far rounding alone moves a load/unload trajectory.
+    // centering force before the beam loop, 8 adds the platen forces before the
+    // self-contact forces, 16 scatters the odd-numbered beams before the even-numbered
+    // ones.  Each is the same sum in another order; runs under these variants measure how
+    // far rounding alone moves a load/unload trajectory.
     int variant = 0;
     // last minimize, for commit
     std::vector<double> lastZ;
@@ -535,8 +537,11 @@ struct orc_model {
                 g.x += cfg.centering_stiffness * cen.x / x.size();
                 g.z += cfg.centering_stiffness * cen.z / x.size();
             }
-        for (size_t bk = 0; bk < beams.size(); bk++) {  // sim.cpp:139-141
-            const size_t bi = (variant & 2) ? beams.size() - 1 - bk : bk;
+        const size_t nbeams = beams.size(), nodd = nbeams / 2;
+        for (size_t bk = 0; bk < nbeams; bk++) {  // sim.cpp:139-141
+            size_t bj = (variant & 2) ? nbeams - 1 - bk : bk;
+            if (variant & 16) bj = bj < nodd ? 2 * bj + 1 : 2 * (bj - nodd);
+            const size_t bi = bj;
             const BeamRec& e = beams[bi];
             const V3 d = x[size_t(e.b)] - x[size_t(e.a)];
             const double L = len(d);
@@ -602,6 +607,24 @@ struct orc_model {
                 g.z += cfg.centering_stiffness * cen.z / x.size();
             }
         const double jr = jointRadius();
+        auto platens = [&]() {  // platens, sim.cpp:168-171
+            for (size_t i = 0; i < nodes.size(); i++) {
+                const double pb = jr - x[i].y;
+                if (pb > 0) {
+                    const double m = cfg.contact_stiffness * pb, en = .5 * cfg.contact_stiffness * pb * pb;
+                    o.energy += en; o.d.contact += en; o.d.maxPen = std::max(o.d.maxPen, pb); o.d.contacts++;
+                    gx[i].y -= m;
+                }
+                const double pt = x[i].y + jr - top;
+                if (pt > 0) {
+                    const double m = cfg.contact_stiffness * pt, en = .5 * cfg.contact_stiffness * pt * pt;
+                    o.energy += en; o.d.contact += en; o.d.reaction += m;
+                    o.d.maxPen = std::max(o.d.maxPen, pt); o.d.contacts++;
+                    gx[i].y += m;
+                }
+            }
+        };
+        if (variant & 8) platens();
         if (cfg.self_contact) {
             const std::vector<Shape> shapes = shapesOf(x);
             selfContact(shapes, [&](int ai, int bi, const Shape& a, const Shape& b, const Closest& cp,
@@ -614,21 +637,7 @@ struct orc_model {
                 spreadForce(gx, b, cp.t, scale(n, -mag));
             });
         }
-        for (size_t i = 0; i < nodes.size(); i++) {  // platens, sim.cpp:168-171
-            const double pb = jr - x[i].y;
-            if (pb > 0) {
-                const double m = cfg.contact_stiffness * pb, en = .5 * cfg.contact_stiffness * pb * pb;
-                o.energy += en; o.d.contact += en; o.d.maxPen = std::max(o.d.maxPen, pb); o.d.contacts++;
-                gx[i].y -= m;
-            }
-            const double pt = x[i].y + jr - top;
-            if (pt > 0) {
-                const double m = cfg.contact_stiffness * pt, en = .5 * cfg.contact_stiffness * pt * pt;
-                o.energy += en; o.d.contact += en; o.d.reaction += m;
-                o.d.maxPen = std::max(o.d.maxPen, pt); o.d.contacts++;
-                gx[i].y += m;
-            }
-        }
+        if (!(variant & 8)) platens();
         for (size_t i = 0; i < nodes.size(); i++) {  // pack, lock, guard: sim.cpp:172
             const size_t b = 6 * i;
             o.grad[b] = cfg.translation_scale * gx[i].x;

@@ -157,3 +157,16 @@ def test_translation_gradient_matches_finite_differences_at_full_size(mcg):
     # and twice in a row gives the same bits
     r2 = sol.objective(z, top)
     assert r2["energy"] == r["energy"] and np.array_equal(r2["grad"], r["grad"])
+
+
+def test_contact_buffers_grow_when_an_evaluation_overflows_them(mcg):
+    """Minimum capacities on the heavily deformed reference state: every buffer overflows on
+    the first try; the evaluation is repeated with grown buffers and matches the fixture."""
+    g = golden("ref242")
+    s = g.state(3)
+    sol = solver_for(mcg, g)
+    sol.set_contact_capacity(0, 0, 0, 0)
+    sol.set_state(plastic=s["plastic"])
+    r = sol.objective(s["z"], s["top"], s["trials"])
+    check_eval(r, s, ("ref242 small buffers", 3))
+    assert np.array_equal(sol.contact_pairs(), s["pairs"])
