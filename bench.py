@@ -37,6 +37,9 @@ import numpy as np  # noqa: E402
 
 BEAM_BYTES = 128    # per beam, FP64: a, b (2 x 4 B) + 15 reals
 NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6], locked[6]
+# DRAM bytes (read + write) per beam of one k_beams launch, from the ncu capture summarised in
+# profiles/k_beams_bcc32_fp64.md (40.35 MB for 184,400 beams), scaled by beam count.
+BEAM_TRAFFIC_PER_BEAM = 40.348160e6 / 184400
 
 
 def parse():
@@ -315,7 +318,8 @@ def main():
         "phase_ms": per_phase,
         "roofline": {"bound": "hbm", "kernel": "k_beams", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None, "bytes_per_launch": beam_bytes, "ms_per_launch": beam_ms},
+                     "traffic": BEAM_TRAFFIC_PER_BEAM * B, "traffic_source": "ncu capture at 184,400 beams, scaled",
+                     "bytes_per_launch": beam_bytes, "ms_per_launch": beam_ms},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": 8 * 6 * N,
                 "d2h_bytes_per_step": 8 * 6 * N + 8},
