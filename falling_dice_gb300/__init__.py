@@ -35,6 +35,7 @@ SIGNATURES = {
     "mcg_set_state": (C.c_int, [_P, _d, _d, _d]),
     "mcg_get_state": (C.c_int, [_P, _d, _d, _d]),
     "mcg_objective": (C.c_int, [_P, _d, C.c_double, C.c_int, _d, _d, C.POINTER(abi.Diag), _d, _d, _u8]),
+    "mcg_objective_noalloc": (C.c_int, [_P, _d, C.c_double, _d, _d, C.POINTER(abi.Diag)]),
     "mcg_upload_z": (C.c_int, [_P, _d]),
     "mcg_objective_resident": (C.c_int, [_P, C.c_double, C.c_int]),
     "mcg_read_result": (C.c_int, [_P, _d, _d, C.POINTER(abi.Diag)]),

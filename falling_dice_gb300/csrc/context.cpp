@@ -988,6 +988,71 @@ int mcg_read_result(mcg_ctx* c, double* energy, double* grad, mcg_diag* diag) {
     });
 }
 
+}  // extern "C"
+
+namespace mcg {
+
+// One evaluation whose self-contact scratch is `fixed` (caller-provided, never grown) and
+// which allocates nothing: the building block of mcg_objective_noalloc (noalloc.cu).
+int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* z, double top, double* energy,
+                                  double* grad, mcg_diag* diag) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!z) throw Fail(MCG_ERR_INVALID, "null z");
+        cudaStream_t s = c->stream;
+        const size_t n = 6 * size_t(c->N);
+        h2d(c->d_zin, z, n, s);
+        PhysParams p = c->phys;
+        p.top = top;
+        p.broad_cell = c->broad_cell;
+        p.inv_cell_f = float(1.0 / c->broad_cell);
+        launch_state(c->topo, p, c->d_zin, c->d_baseX, c->d_baseR, c->ev, s);
+        launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s);
+        const ContactBufs* cptr = nullptr;
+        if (p.self_contact) {
+            launch_contacts(c->topo, p, c->ev, fixed, c->rmax + c->cfg.contact_margin, s);
+            cptr = &fixed;
+        }
+        launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
+        launch_finalize(c->topo, p, cptr, c->d_grad, c->ev, s);
+        c->check_launch();
+        const EvalOut o = c->read_out_raw();
+        if (o.overflow) {
+            std::string what;
+            if (o.overflow & kOverEntries) what += " cell entries";
+            if (o.overflow & kOverBins) what += " grid bins";
+            if (o.overflow & kOverCandidates) what += " candidate pairs";
+            if (o.overflow & kOverContacts) what += " contacts";
+            if (o.overflow & kOverSpan) what += " cells spanned by one shape";
+            throw Fail(MCG_ERR_CAPACITY, "this state needs more" + what +
+                                             " than the fixed scratch of mcg_objective_noalloc holds");
+        }
+        if (grad) d2h(grad, c->d_grad, n, s);
+        c->sync();
+        if (energy) *energy = o.energy;
+        if (diag) {
+            diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
+            diag->reaction = o.reaction; diag->max_pen = o.max_pen; diag->contacts = o.contacts; diag->pad_ = 0;
+        }
+    });
+}
+
+int ctx_counts(const mcg_ctx* c, int* n_nodes, int* n_beams, int* device) {
+    if (!c || !c->have_topo) return MCG_ERR_STATE;
+    *n_nodes = c->N;
+    *n_beams = c->B;
+    *device = c->device;
+    return MCG_OK;
+}
+
+void ctx_set_error(mcg_ctx* c, const char* msg) {
+    if (c) c->err = msg;
+}
+
+}  // namespace mcg
+
+extern "C" {
+
 int mcg_contact_pairs(mcg_ctx* c, uint64_t* keys, int64_t capacity, int64_t* count) {
     if (!c || !count) return MCG_ERR_INVALID;
     int rc = guarded(c, [&] {

@@ -170,6 +170,20 @@ int mcg_objective(mcg_ctx* ctx, const double* z, double top, int trials, double*
                   double* grad, mcg_diag* diag, double* trial_next, double* trial_aux,
                   uint8_t* trial_flags);
 
+/* The same evaluation as mcg_objective (without trial states) for callers that must not
+ * allocate device memory when they evaluate: code inside a CUDA stream capture (where
+ * cudaMalloc/cudaFree are not permitted), fixed-budget real-time loops, hosts whose device
+ * memory belongs to another allocator.  mcg_objective may re-allocate its self-contact
+ * buffers to fit a state; this entry point uses a fixed 4 MiB __device__ array instead
+ * and calls no allocating routine.  Limits: at most 4096 nodes and 8192 nodes + beams, and
+ * per evaluation 65536 cell entries, 32768 grid bins, 32768 candidate pairs and 8192
+ * contacts; beyond them it returns MCG_ERR_CAPACITY, naming what overflowed.  The first
+ * call on a device looks up the array's device address, so make it before any stream
+ * capture.  All calls on a device share the array: calls that overlap on the GPU race.
+ * No counterpart in the reference. */
+int mcg_objective_noalloc(mcg_ctx* ctx, const double* z, double top, double* energy, double* grad,
+                          mcg_diag* diag);
+
 /* Device-resident form used for throughput measurement: mcg_upload_z copies z once;
  * mcg_objective_resident evaluates at that z, leaving energy/grad on the device;
  * mcg_read_result copies them out.  The same kernels as mcg_objective. */
