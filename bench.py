@@ -6,6 +6,9 @@
 A step is one full evaluation of the objective (energy + 6-DOF gradient: node state, beam
 mechanics with return mapping, self-contact broad/narrow phase, platen contact, gather)
 on the 64x64x32 cubic+BCC specimen at its seeded deformed state.  Metric: evaluations/s.
+The headline is the mixed-precision form (FP32 bulk arithmetic, FP64 base state and
+reductions), with its error against the plain FP64 form; the FP64 form is measured beside
+it under "fp64".
 
 value      device-resident: z already in HBM, result left in HBM (mcg_objective_resident).
 e2e        the public C-ABI call mcg_objective with pinned host buffers: z host->device,
@@ -40,6 +43,8 @@ NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6
 # DRAM bytes (read + write) per beam of one k_beams launch, from the ncu capture summarised in
 # profiles/k_beams_bcc32_fp64.md (40.35 MB for 184,400 beams), scaled by beam count.
 BEAM_TRAFFIC_PER_BEAM = 40.348160e6 / 184400
+BEAM_BYTES_MIXED = 68    # per beam, mixed: a, b (2 x 4 B) + 15 reals as FP32
+NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 + locked[6]
 
 
 def parse():
@@ -195,6 +200,79 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
+    """Times one precision form: device-resident evaluations, e2e through the C ABI, phases."""
+    import ctypes as C
+    from falling_dice_gb300 import abi
+    N, B = lat.n_nodes, lat.n_beams
+    sol = fd.Solver(cfg, lat, device=local)
+    sol.set_state(plastic=pl)
+    sol.upload_z(z)
+    stream = torch.cuda.ExternalStream(sol.stream, device=local)
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(warmup, 3)):
+        sol.objective_resident(top)
+    res0 = sol.read_result(grad=True)  # also sizes the contact buffers before timing
+    barrier()
+    launches0 = sol.launch_count()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(steps):
+        sol.objective_resident(top)
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = sol.launch_count() - launches0
+    clk = clocks.stop()
+    if pg is not None:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    res = sol.read_result(grad=False)
+    # end to end through the public C ABI, pinned host buffers
+    zh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
+    zh.numpy()[:] = z
+    gh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
+    eout = C.c_double()
+    diag = abi.Diag()
+    zp = C.cast(zh.data_ptr(), C.POINTER(C.c_double))
+    gp = C.cast(gh.data_ptr(), C.POINTER(C.c_double))
+    for _ in range(max(warmup, 3)):
+        sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
+    barrier()
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(steps):
+        rc = sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
+        assert rc == 0
+    e1.record(stream)
+    barrier()
+    ms_e2e = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
+    if pg is not None:
+        t = torch.tensor([ms_e2e], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    assert np.isfinite(eout.value) and eout.value == res["energy"]
+    # per-phase timing for the roofline (a separate pass: it synchronises per evaluation)
+    sol.set_timing(True)
+    for _ in range(max(3, min(steps, 10))):
+        sol.objective_resident(top)
+    phases, nev = sol.phase_times()
+    sol.set_timing(False)
+    sol.close()
+    return {"ms_step": ms / steps, "value": world * 1e3 * steps / ms, "e2e": world * 1e3 * steps / ms_e2e,
+            "launches": launches, "clocks": clk, "energy": res["energy"], "grad": res0["grad"],
+            "contacts": res["diag"]["contacts"], "phases": {k: v / nev for k, v in phases.items()}}
+
+
 def main():
     a = parse()
     rank, world, local = dist_info()
@@ -203,7 +281,7 @@ def main():
         return
     import torch
     import falling_dice_gb300 as fd
-    from falling_dice_gb300 import workloads
+    from falling_dice_gb300 import abi, workloads
     if not os.path.exists(fd.LIB_PATH):
         import __graft_entry__
         __graft_entry__.build()
@@ -216,87 +294,24 @@ def main():
     cfg, spec = workload(a.workload)
     lat = fd.generate_lattice(spec, cfg)
     z, pl = fd.random_state(lat, **workloads.DEFORM)
-    sol = fd.Solver(cfg, lat, device=local)
-    sol.set_state(plastic=pl)
     top = lat.geometry.top0 + 0.01
-    sol.upload_z(z)
-    stream = torch.cuda.ExternalStream(sol.stream, device=local)
     N, B = lat.n_nodes, lat.n_beams
-
-    def barrier():
-        if pg is not None:
-            pg.barrier()
-        torch.cuda.synchronize()
-
-    # ---- device-resident throughput ----
-    for _ in range(max(a.warmup, 3)):
-        sol.objective_resident(top)
-    sol.read_result(grad=False)  # sizes the contact buffers for this state before timing
-    barrier()
-    launches0 = sol.launch_count()
-    clocks = Clocks(local)
-    clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    e0.record(stream)
-    for _ in range(a.steps):
-        sol.objective_resident(top)
-    e1.record(stream)
-    barrier()
-    ms = e0.elapsed_time(e1)
-    launches = sol.launch_count() - launches0
-    clk = clocks.stop()
-    if pg is not None:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / a.steps
-    value = world * 1e3 / ms_step
-    res = sol.read_result(grad=False)
-
-    # ---- end to end through the public C ABI, pinned host buffers ----
-    zh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
-    zh.numpy()[:] = z
-    gh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
-    import ctypes as C
-    from falling_dice_gb300 import abi
-    eout = C.c_double()
-    diag = abi.Diag()
-    zp = C.cast(zh.data_ptr(), C.POINTER(C.c_double))
-    gp = C.cast(gh.data_ptr(), C.POINTER(C.c_double))
-    for _ in range(max(a.warmup, 3)):
-        sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
-    barrier()
-    t0 = time.perf_counter()
-    e0.record(stream)
-    for _ in range(a.steps):
-        rc = sol.lib.mcg_objective(sol.h, zp, top, 0, C.byref(eout), gp, C.byref(diag), None, None, None)
-        assert rc == 0
-    e1.record(stream)
-    barrier()
-    ms_e2e = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
-    if pg is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_e2e = float(t.item())
-    e2e = world * 1e3 * a.steps / ms_e2e
-    assert np.isfinite(eout.value) and eout.value == res["energy"]
-
-    # ---- phase timing for the roofline (separate pass: it synchronizes per evaluation) ----
-    sol.set_timing(True)
-    for _ in range(max(3, min(a.steps, 10))):
-        sol.objective_resident(top)
-    phases, nev = sol.phase_times()
-    sol.set_timing(False)
-    per_phase = {k: v / nev for k, v in phases.items()}
-    peak, peak_kind = measured_peaks()
-    beam_bytes = BEAM_BYTES * B
-    beam_ms = per_phase["beams"]
-    achieved = beam_bytes / (beam_ms * 1e-3) / 1e9
-    eval_bytes = BEAM_BYTES * B + NODE_BYTES * N
-
+    cfg_mixed = workload(a.workload)[0]
+    cfg_mixed.precision = abi.MCG_MIXED
+    mixed = measure(fd, torch, cfg_mixed, lat, z, pl, top, a.steps, a.warmup, local, pg, world)
+    plain = measure(fd, torch, cfg, lat, z, pl, top, a.steps, a.warmup, local, pg, world)
     if rank != 0:
         return
+    peak, peak_kind = measured_peaks()
+    beam_bytes_f64 = BEAM_BYTES * B
+    beam_bytes_mixed = BEAM_BYTES_MIXED * B
+
+    def roofline(r, nbytes, traffic):
+        ms = r["phases"]["beams"]
+        ach = nbytes / (ms * 1e-3) / 1e9
+        return {"bound": "hbm", "kernel": "k_beams_mixed" if r is mixed else "k_beams", "achieved": ach,
+                "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
+                "traffic": traffic, "bytes_per_launch": nbytes, "ms_per_launch": ms}
     cpu = None
     if not a.no_cpu_baseline:
         t_s, B_s, N_s = cpu_sample_eval_seconds(a.workload, repeat=2)
@@ -305,30 +320,35 @@ def main():
                "sample": f"{cs.cells_x}x{cs.cells_y}x{cs.cells_z} cubic+BCC ({B_s} beams), 2 evaluations "
                          f"of {t_s:.2f} s each, scaled by beam count to {B} beams",
                "seconds_per_sample_eval": t_s}
+    err_e = abs(mixed["energy"] - plain["energy"]) / abs(plain["energy"])
+    err_g = float(np.linalg.norm(mixed["grad"] - plain["grad"]) / np.linalg.norm(plain["grad"]))
+    eval_bytes_mixed = BEAM_BYTES_MIXED * B + NODE_BYTES_MIXED * N
     line = {
-        "metric": "beam energy-grad evals/s", "value": value, "unit": "evals/s",
-        "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "metric": "beam energy-grad evals/s", "value": mixed["value"], "unit": "evals/s",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": mixed["ms_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 reductions)",
         "data": "synthetic",
         "config": {"workload": f"{a.workload}: cubic+BCC {spec.cells_x}x{spec.cells_y}x{spec.cells_z}, "
                                f"{N} nodes, {B} beams, seeded deformed state",
-                   "precision": "fp64 plain form", "parallelism": "replicas" if world > 1 else "single",
+                   "precision": "mixed: FP32 bulk, FP64 base state and reductions",
+                   "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (beam arrays alone exceed 129 MB)"},
-        "hbm_gbs_algorithmic": eval_bytes * value / world / 1e9,
-        "phase_ms": per_phase,
-        "roofline": {"bound": "hbm", "kernel": "k_beams", "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": BEAM_TRAFFIC_PER_BEAM * B, "traffic_source": "ncu capture at 184,400 beams, scaled",
-                     "bytes_per_launch": beam_bytes, "ms_per_launch": beam_ms},
+        "error_vs_fp64": {"energy_rel": err_e, "grad_rel_2norm": err_g},
+        "hbm_gbs_algorithmic": eval_bytes_mixed * mixed["value"] / world / 1e9,
+        "phase_ms": mixed["phases"],
+        "roofline": roofline(mixed, beam_bytes_mixed, None),
+        "fp64": {"value": plain["value"], "ms_per_step": plain["ms_step"], "e2e": plain["e2e"],
+                 "phase_ms": plain["phases"], "gpu_launches": int(plain["launches"]),
+                 "hbm_gbs_algorithmic": (BEAM_BYTES * B + NODE_BYTES * N) * plain["value"] / world / 1e9,
+                 "roofline": roofline(plain, beam_bytes_f64, BEAM_TRAFFIC_PER_BEAM * B)},
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": 8 * 6 * N,
+        "e2e": {"value": mixed["e2e"], "unit": "evals/s", "h2d_bytes_per_step": 8 * 6 * N,
                 "d2h_bytes_per_step": 8 * 6 * N + 8},
-        "gpu_launches": int(launches),
-        "clocks": clk,
-        "energy": res["energy"], "contacts": res["diag"]["contacts"],
+        "gpu_launches": int(mixed["launches"]),
+        "clocks": mixed["clocks"] or plain["clocks"],
+        "energy": mixed["energy"], "contacts": mixed["contacts"],
     }
     print(json.dumps(line), flush=True)
-    sol.close()
 
 
 if __name__ == "__main__":

@@ -100,6 +100,13 @@ struct mcg_ctx {
     int last_sort_res = 0;
 
     double *d_baseX = nullptr, *d_baseR = nullptr, *d_plastic = nullptr;
+    bool mixed = false;  // MCG_MIXED: FP32 bulk arithmetic (objective_mixed.cu)
+    MixedBeams mb{};
+    MixedNodes mn{};
+    // Re-derives the mixed form's per-increment base terms after the base state changed.
+    void rebase() {
+        if (mixed) launch_rebase_mixed(topo, d_baseX, d_baseR, mb, mn, stream);
+    }
     double *d_zin = nullptr, *d_grad = nullptr;
     Pinned* hp = nullptr;
 
@@ -224,9 +231,11 @@ struct mcg_ctx {
         p.broad_cell = broad_cell;
         p.inv_cell_f = float(1.0 / broad_cell);
         mark(0);
-        launch_state(topo, p, dz, d_baseX, d_baseR, ev, stream);
+        if (mixed) launch_state_mixed(topo, p, dz, d_baseX, mn, ev, stream);
+        else launch_state(topo, p, dz, d_baseX, d_baseR, ev, stream);
         mark(1);
-        launch_beams(topo, mat, d_plastic, trials, ev, stream);
+        if (mixed) launch_beams_mixed(topo, mat, mb, mn, trials, ev, stream);
+        else launch_beams(topo, mat, d_plastic, trials, ev, stream);
         mark(2);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
@@ -234,7 +243,8 @@ struct mcg_ctx {
             cptr = &cb;
         }
         mark(3);
-        launch_gather(topo, p, cptr, d_gout, ev, stream);
+        if (mixed) launch_gather_mixed(topo, p, cptr, d_gout, ev, stream);
+        else launch_gather(topo, p, cptr, d_gout, ev, stream);
         mark(4);
         launch_finalize(topo, p, cptr, d_gout, ev, stream);
         mark(5);
@@ -414,7 +424,14 @@ struct mcg_ctx {
         if (!have_final) throw Fail(MCG_ERR_STATE, "commit without a preceding minimize");
         PhysParams p = phys;
         launch_state(topo, p, d_zfinal, d_baseX, d_baseR, ev, stream);
-        launch_commit(N, B, ev, d_baseX, d_baseR, d_plastic, stream);
+        if (mixed) {
+            launch_commit(N, B, ev, d_baseX, d_baseR, nullptr, stream);
+            launch_plastic_mixed(B, nullptr, ev.trial_nextf, mb, stream);
+            launch_plastic_mixed_to_f64(B, mb, d_plastic, stream);
+        } else {
+            launch_commit(N, B, ev, d_baseX, d_baseR, d_plastic, stream);
+        }
+        rebase();
         have_final = false;
         check_launch();
     }
@@ -835,6 +852,18 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         e.trial_next = V.get<double>(7 * size_t(B));
         e.trial_aux = V.get<double>(7 * size_t(B));
         e.trial_flags = V.get<uint8_t>(3 * size_t(B));
+        c->mixed = cf.precision == MCG_MIXED;
+        if (c->mixed) {
+            e.slotAf = V.get<float>(6 * size_t(B));
+            e.slotBf = V.get<float>(6 * size_t(B));
+            e.trial_nextf = V.get<float>(7 * size_t(B));
+            e.trial_auxf = V.get<float>(7 * size_t(B));
+            MixedBeams mb{};
+            float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B3, &mb.B4, &mb.B5, &mb.C0, &mb.C1, &mb.P0, &mb.P1};
+            for (float4** f : fields) *f = V.get<float4>(size_t(B));
+            c->mb = mb;
+            c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
+        }
         c->ev = e;
         c->d_zin = V.get<double>(6 * size_t(N));
         c->d_grad = V.get<double>(6 * size_t(N));
@@ -876,6 +905,11 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         c->d_part = Q.get<double>(lbfgs_part_doubles());
         c->d_stats = Q.get<double>(16);
         ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
+        if (c->mixed) {
+            launch_mixed_constants(c->topo, c->mb, s);
+            launch_plastic_mixed(B, c->d_plastic, nullptr, c->mb, s);
+            c->rebase();
+        }
         c->sync();
         c->have_topo = true;
     });
@@ -893,8 +927,10 @@ int mcg_set_state(mcg_ctx* c, const double* bx, const double* br, const double* 
             for (size_t b = 0; b < B; b++)
                 for (int k = 0; k < 7; k++) soa[size_t(k) * B + b] = pl[7 * b + size_t(k)];
             h2d(c->d_plastic, soa.data(), soa.size(), s);
+            if (c->mixed) launch_plastic_mixed(c->B, c->d_plastic, nullptr, c->mb, s);
             c->sync();
         }
+        if (bx || br) c->rebase();
         c->sync();
         c->have_final = false;
     });
@@ -933,6 +969,10 @@ int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* e
         if (diag) {
             diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
             diag->reaction = o.reaction; diag->max_pen = o.max_pen; diag->contacts = o.contacts; diag->pad_ = 0;
+        }
+        if (trials && c->mixed) {
+            launch_f32_to_f64(7LL * c->B, c->ev.trial_nextf, c->ev.trial_next, s);
+            launch_f32_to_f64(7LL * c->B, c->ev.trial_auxf, c->ev.trial_aux, s);
         }
         if (trials && (trial_next || trial_aux || trial_flags)) {
             std::vector<double> soa(7 * B);
@@ -1006,14 +1046,17 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         p.top = top;
         p.broad_cell = c->broad_cell;
         p.inv_cell_f = float(1.0 / c->broad_cell);
-        launch_state(c->topo, p, c->d_zin, c->d_baseX, c->d_baseR, c->ev, s);
-        launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s);
+        if (c->mixed) launch_state_mixed(c->topo, p, c->d_zin, c->d_baseX, c->mn, c->ev, s);
+        else launch_state(c->topo, p, c->d_zin, c->d_baseX, c->d_baseR, c->ev, s);
+        if (c->mixed) launch_beams_mixed(c->topo, c->mat, c->mb, c->mn, false, c->ev, s);
+        else launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
             launch_contacts(c->topo, p, c->ev, fixed, c->rmax + c->cfg.contact_margin, s);
             cptr = &fixed;
         }
-        launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
+        if (c->mixed) launch_gather_mixed(c->topo, p, cptr, c->d_grad, c->ev, s);
+        else launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
         launch_finalize(c->topo, p, cptr, c->d_grad, c->ev, s);
         c->check_launch();
         const EvalOut o = c->read_out_raw();

@@ -132,6 +132,31 @@ struct EvalBufs {
     double* trial_next;     // [7B] SoA
     double* trial_aux;      // [7B] SoA
     uint8_t* trial_flags;   // [3B] SoA
+    // mixed-precision form
+    float* slotAf;          // [6B]
+    float* slotBf;          // [6B]
+    float* trial_nextf;     // [7B] SoA
+    float* trial_auxf;      // [7B] SoA
+};
+
+// Per-beam data of the mixed-precision form (objective_mixed.cu), float4 SoA.
+struct MixedBeams {
+    float4* B0;  // base chord d0 (FP32-rounded), c0 = |d0|^2 - L0^2
+    float4* B1;  // base director d_a0, L0
+    float4* B2;  // base director d_b0, |d0|
+    float4* B3;  // base shear vector d_a0 - t0
+    float4* B4;  // base shear vector d_b0 - t0
+    float4* B5;  // base relative rotation Q0 as (w - 1, v)
+    float4* C0;  // kb, kt, my, ty
+    float4* C1;  // cs, area L0, area, area L0 yield
+    float4* P0;  // plastic: epsp, alpha, alphaB, alphaT
+    float4* P1;  // plastic: rotp
+};
+// Per-node data of the mixed-precision form.
+struct MixedNodes {
+    float4* U;    // increment displacement s t since the base state
+    float4* E;    // increment rotation exp(r) as (w - 1, v)
+    float4* R0f;  // base orientation (w, x, y, z)
 };
 
 // ---- launch accounting -------------------------------------------------------------------
@@ -151,6 +176,22 @@ void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c
                      EvalBufs& e, cudaStream_t s);
 void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic,
                    cudaStream_t s);
+void launch_center(int N, EvalBufs& e, cudaStream_t s);
+void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
+                         cudaStream_t s);
+
+// ---- mixed-precision form (objective_mixed.cu) ------------------------------------------
+void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
+                        const MixedNodes& mn, EvalBufs& e, cudaStream_t s);
+void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
+                        EvalBufs& e, cudaStream_t s);
+void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
+                         MixedNodes& mn, cudaStream_t s);
+void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s);
+// plastic state of the mixed form from the FP64 SoA array (trial32 == nullptr) or from an FP32 trial
+void launch_plastic_mixed(int B, const double* plastic64, const float* trial32, MixedBeams& mb, cudaStream_t s);
+void launch_plastic_mixed_to_f64(int B, const MixedBeams& mb, double* plastic64, cudaStream_t s);
+void launch_f32_to_f64(long long n, const float* a, double* o, cudaStream_t s);
 // out6: sum|epsp|, max|epsp|, sum|rotp|, max|rotp|, #|epsp|>1e-5, #|rotp|>1e-4
 void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s);
 

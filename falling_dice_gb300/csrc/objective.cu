@@ -298,6 +298,36 @@ __device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const Phy
 }
 
 // ---- per-node gather: the scatter of MC/src/sim.cpp:139-172, as a deterministic CSR sum ---
+// Sums the incident beams' end vectors of node i in ascending beam order: FP64 slots
+// directly, FP32 slots (mixed form) with compensated FP32 sums.
+template <bool F32>
+__device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, int i, d3& gx, d3& gr) {
+    const int k0 = t.inc_start[i], k1 = t.inc_start[i + 1];
+    if (!F32) {
+        for (int k = k0; k < k1; k++) {
+            const int v = t.inc[k];
+            const double* s = ((v & 1) ? e.slotB : e.slotA) + 6 * size_t(v >> 1);
+            gx.x += s[0]; gx.y += s[1]; gx.z += s[2];
+            gr.x += s[3]; gr.y += s[4]; gr.z += s[5];
+        }
+    } else {
+        float hi[6] = {0, 0, 0, 0, 0, 0}, lo[6] = {0, 0, 0, 0, 0, 0};
+        for (int k = k0; k < k1; k++) {
+            const int v = t.inc[k];
+            const float* s = ((v & 1) ? e.slotBf : e.slotAf) + 6 * size_t(v >> 1);
+#pragma unroll
+            for (int j = 0; j < 6; j++) {  // two-sum
+                const float a = s[j], sum = hi[j] + a, bp = sum - hi[j];
+                lo[j] += (hi[j] - (sum - bp)) + (a - bp);
+                hi[j] = sum;
+            }
+        }
+        gx = d3{double(hi[0]) + double(lo[0]), double(hi[1]) + double(lo[1]), double(hi[2]) + double(lo[2])};
+        gr = d3{double(hi[3]) + double(lo[3]), double(hi[4]) + double(lo[4]), double(hi[5]) + double(lo[5])};
+    }
+}
+
+template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
     __shared__ double sm[4 * (kBlock / 32)];
@@ -308,13 +338,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
     double pen_max = 0;
     if (i < N) {
         d3 gx{0, 0, 0}, gr{0, 0, 0};
-        const int k0 = t.inc_start[i], k1 = t.inc_start[i + 1];
-        for (int k = k0; k < k1; k++) {
-            const int v = t.inc[k];
-            const double* s = ((v & 1) ? e.slotB : e.slotA) + 6 * size_t(v >> 1);
-            gx.x += s[0]; gx.y += s[1]; gx.z += s[2];
-            gr.x += s[3]; gr.y += s[4]; gr.z += s[5];
-        }
+        sum_slots<F32>(t, e, i, gx, gr);
         const d3 xi = ldx(e.x, i);
         // gravity (sim.cpp:142)
         const double mg = t.mass[i] * p.gravity;
@@ -511,14 +535,20 @@ void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const 
     const int nb = nb_nodes(t.N);
     k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.M, e.xf_lo, e.xf_hi,
                                   e.part_state);
-    k_center<<<1, kBlock, 0, s>>>(t.N, nb, e.part_state, e.cen);
-    note_launches(2);
+    note_launches(1);
+    launch_center(t.N, e, s);
+}
+
+void launch_center(int N, EvalBufs& e, cudaStream_t s) {
+    k_center<<<1, kBlock, 0, s>>>(N, nb_nodes(N), e.part_state, e.cen);
+    note_launches(1);
 }
 
 void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic, cudaStream_t s) {
     k_commit_nodes<<<grid_for(N), kBlock, 0, s>>>(N, e.x, e.R, base_x, base_r);
     note_launches(1);
-    if (B > 0) cudaMemcpyAsync(plastic, e.trial_next, 7 * size_t(B) * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (B > 0 && plastic)
+        cudaMemcpyAsync(plastic, e.trial_next, 7 * size_t(B) * sizeof(double), cudaMemcpyDeviceToDevice, s);
 }
 
 void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s) {
@@ -539,7 +569,15 @@ void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, 
                    cudaStream_t s) {
     ContactBufs cc{};
     if (c) cc = *c;
-    k_gather<<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
+    k_gather<false><<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
+    note_launches(1);
+}
+
+void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
+                         cudaStream_t s) {
+    ContactBufs cc{};
+    if (c) cc = *c;
+    k_gather<true><<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
     note_launches(1);
 }
 

@@ -1,0 +1,471 @@
+// objective_mixed.cu -- the mixed-precision form of the energy/gradient evaluation.
+//
+// FP32 does the bulk arithmetic: every per-beam term of the reference's objective
+// (MC/src/sim.cpp:139-141).  FP64 stays where stability needs it: the base configuration,
+// the per-increment base terms below, node positions for contact and platen tests,
+// energy totals (compensated FP32 warp sums, FP64 across warps), node gradient totals
+// (compensated FP32 sums), and everything the L-BFGS solver does.
+//
+// Naively FP32 would lose the quantities the energy depends on by cancellation:
+//   * the chord length change L - L0 (strain ~1e-3 of a 5 mm chord);
+//   * the shear vectors d_a - t, d_b - t (directors nearly aligned with the chord);
+//   * the relative rotation Ra^* Rb between two nearly aligned nodes.
+// The configuration is therefore split into the base state of the increment (FP64; the
+// reference re-bases it at every commit, MC/src/sim.cpp:212, and every increment starts
+// from z = 0, sim.cpp:398) and the FP32 increment since it:
+//   x = x_base + u,  R = e R_base with e = exp(r) kept as (w - 1, v),
+// and the cancelling quantities are formed from small terms only:
+//   |d|^2 - L0^2 = c0 + 2 d0.du + du.du              c0 = |d0|^2 - L0^2   (base, FP64)
+//   d_a - t      = inc(e_a, d_a0) + s_a0 - (t - t0)   s_a0 = d_a0 - t0     (base, FP64)
+//   t - t0       = (du |d0| - d0 (L - |d0|)) / (L |d0|)
+//   Ra^* Rb      = (Ra0^* delta Ra0) Q0,  delta = e_a^* e_b              Q0 = Ra0^* Rb0
+// with inc(e, v) = R(e) v - v evaluated as 2w (u x v) + 2 u x (u x v) and the near-identity
+// quaternions held as (w - 1, v), so that every FP32 rounding is relative to an increment.
+// d0 is the base chord rounded to FP32 and c0, s_a0 are computed from that rounded chord,
+// so the split is exact for a base chord perturbed by one FP32 rounding (about 3e-10 m).
+#include "common.cuh"
+#include "kernels.h"
+
+namespace mcg {
+
+namespace {
+
+struct f3 { float x, y, z; };
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float fdot(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 fcross(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 xyz(float4 v) { return {v.x, v.y, v.z}; }
+
+// R(q) v - v for a unit quaternion q = (w, u).
+__device__ __forceinline__ f3 rot_inc(float w, f3 u, f3 v) {
+    const f3 t = fcross(u, v) * 2.f;
+    return t * w + fcross(u, t);
+}
+__device__ __forceinline__ f3 rot(float w, f3 u, f3 v) { return v + rot_inc(w, u, v); }
+__device__ __forceinline__ f3 rot_conj(float w, f3 u, f3 v) { return v + rot_inc(w, -u, v); }
+
+// Compensated FP32 sums: (hi, lo) with hi + lo carrying about twice the precision.
+struct fsum {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float v) {
+        const float s = hi + v;
+        const float bp = s - hi;
+        lo += (hi - (s - bp)) + (v - bp);
+        hi = s;
+    }
+};
+
+// Warp sum of compensated pairs, finished in FP64 by lane 0.
+__device__ __forceinline__ double warp_sum_comp(float hi, float lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
+        const float l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        const float s = hi + h2;
+        const float bp = s - hi;
+        lo += l2 + ((hi - (s - bp)) + (h2 - bp));
+        hi = s;
+    }
+    return double(hi) + double(lo);
+}
+
+// Sums NV per-thread FP32 values over the block into thread 0 (FP64 across warps).
+template <int NV>
+__device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[NV], double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+        const double s = warp_sum_comp(v[k], 0.f);
+        if (lane == 0) smem[k * nw + warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0;
+            for (int w = 0; w < nw; w++) s += smem[k * nw + w];
+            out[k] = s;
+        }
+    __syncthreads();
+}
+
+struct R1 { float force, p, a, dg, energy, hard; bool yielded; };
+__device__ __forceinline__ R1 ret1(float total, float pc, float ac, float k, float y, float H) {
+    R1 r;
+    const float trial = k * (total - pc);
+    const float f = fabsf(trial) - (y + H * ac);
+    if (f > 0.f) {
+        r.dg = f / fmaxf(1e-20f, k + H);
+        r.p = pc + (trial >= 0.f ? r.dg : -r.dg);
+        r.a = ac + r.dg;
+        r.yielded = true;
+    } else {
+        r.dg = 0.f; r.p = pc; r.a = ac; r.yielded = false;
+    }
+    const float e = total - r.p;
+    r.force = k * e;
+    r.energy = .5f * k * e * e;
+    r.hard = .5f * H * r.a * r.a;
+    return r;
+}
+struct R3 { f3 force, p; float a, dg, energy, hard; bool yielded; };
+__device__ __forceinline__ R3 ret3(f3 t, f3 pc, float ac, float k, float y, float H) {
+    R3 r;
+    const f3 e0 = t - pc;
+    const f3 trial = e0 * k;
+    const float n = sqrtf(fdot(trial, trial));
+    const float f = n - (y + H * ac);
+    if (f > 0.f && n > 1e-20f) {
+        r.dg = f / fmaxf(1e-20f, k + H);
+        r.p = pc + trial * (r.dg / n);
+        r.a = ac + r.dg;
+        r.yielded = true;
+    } else {
+        r.dg = 0.f; r.p = pc; r.a = ac; r.yielded = false;
+    }
+    const f3 e = t - r.p;
+    r.force = e * k;
+    r.energy = .5f * k * fdot(e, e);
+    r.hard = .5f * H * r.a * r.a;
+    return r;
+}
+
+// J_l^{-T}(p) v in FP32 (MC/include/core.hpp:53): series coefficient below 0.5 rad (four
+// terms reach FP32 precision there), closed form above.
+__device__ __forceinline__ f3 jl_inv_t_f(f3 p, f3 v) {
+    const float a2 = fdot(p, p);
+    const f3 c1 = fcross(p, v);
+    const f3 c2 = fcross(p, c1);
+    float A;
+    if (a2 < 0.25f) {
+        A = fmaf(fmaf(fmaf(1.f / 1209600.f, a2, 1.f / 30240.f), a2, 1.f / 720.f), a2, 1.f / 12.f);
+    } else {
+        const float a = sqrtf(a2);
+        float s, c;
+        sincosf(a, &s, &c);
+        A = 1.f / a2 - (1.f + c) / (2.f * a * s);
+    }
+    return (v + c1 * .5f) + c2 * A;
+}
+
+// ---- node state --------------------------------------------------------------------------
+// u = s t (FP32), e = exp(r) as (w - 1, v) (FP32), x = x_base + u (FP64, for contact,
+// platen and centering), FP32 position bounds; block partial sums and extrema of x.
+__global__ void __launch_bounds__(kBlock) k_state_mixed(int N, double ts, const uint8_t* __restrict__ locked,
+                                                        const double* __restrict__ z, const double* __restrict__ bx,
+                                                        float4* __restrict__ U, float4* __restrict__ Ei,
+                                                        double4_32a* __restrict__ x4, float4* __restrict__ xf_lo,
+                                                        float4* __restrict__ xf_hi, double* __restrict__ part) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    __shared__ double smx[kBlock / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[3] = {0, 0, 0};
+    const double ninf = __longlong_as_double(0xfff0000000000000LL);
+    double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+    if (i < N) {
+        const double* zi = z + 6 * size_t(i);
+        const uint8_t* li = locked + 6 * size_t(i);
+        float t[3], r[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            t[d] = li[d] ? 0.f : float(zi[d] * ts);
+            r[d] = li[d + 3] ? 0.f : float(zi[d + 3]);
+        }
+        U[i] = make_float4(t[0], t[1], t[2], 0.f);
+        const float th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        float wm1, sv;  // cos(th/2) - 1 and sin(th/2)/th
+        if (th2 < 1e-6f) {
+            wm1 = th2 * (-0.125f + th2 * (1.f / 384.f));
+            sv = 0.5f + th2 * (-1.f / 48.f + th2 * (1.f / 3840.f));
+        } else {
+            const float th = sqrtf(th2);
+            float s4 = sinf(0.25f * th);
+            float sh, ch;
+            sincosf(0.5f * th, &sh, &ch);
+            wm1 = -2.f * s4 * s4;
+            sv = sh / th;
+        }
+        Ei[i] = make_float4(wm1, r[0] * sv, r[1] * sv, r[2] * sv);
+        const double xx = bx[3 * size_t(i)] + double(t[0]);
+        const double xy = bx[3 * size_t(i) + 1] + double(t[1]);
+        const double xz = bx[3 * size_t(i) + 2] + double(t[2]);
+        x4[i] = make_double4_32a(xx, xy, xz, 0.0);
+        xf_lo[i] = make_float4(__double2float_rd(xx), __double2float_rd(xy), __double2float_rd(xz), 0.f);
+        xf_hi[i] = make_float4(__double2float_ru(xx), __double2float_ru(xy), __double2float_ru(xz), 0.f);
+        acc[0] = xx; acc[1] = xy; acc[2] = xz;
+        mx[0] = -xx; mx[1] = -xy; mx[2] = -xz; mx[3] = xx; mx[4] = xy; mx[5] = xz;
+    }
+    block_sum<3>(acc, sm);
+#pragma unroll
+    for (int k = 0; k < 6; k++) mx[k] = block_max(mx[k], smx);
+    if (threadIdx.x == 0) {
+        double* q = part + 9 * size_t(blockIdx.x);
+        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
+#pragma unroll
+        for (int k = 0; k < 6; k++) q[3 + k] = mx[k];
+    }
+}
+
+// ---- per-increment base terms (FP64, once per commit) ----------------------------------------
+__global__ void __launch_bounds__(kBlock) k_rebase_nodes(int N, const double* __restrict__ br, float4* __restrict__ R0f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const double* q = br + 4 * size_t(i);
+    R0f[i] = make_float4(float(q[0]), float(q[1]), float(q[2]), float(q[3]));
+}
+
+__global__ void __launch_bounds__(kBlock) k_rebase_beams(DevTopo t, const double* __restrict__ bx,
+                                                         const double* __restrict__ br, MixedBeams m) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= t.B) return;
+    const int2 ab = t.ab[b];
+    const d3 xa{bx[3 * size_t(ab.x)], bx[3 * size_t(ab.x) + 1], bx[3 * size_t(ab.x) + 2]};
+    const d3 xb{bx[3 * size_t(ab.y)], bx[3 * size_t(ab.y) + 1], bx[3 * size_t(ab.y) + 2]};
+    const q4 Ra{br[4 * size_t(ab.x)], br[4 * size_t(ab.x) + 1], br[4 * size_t(ab.x) + 2], br[4 * size_t(ab.x) + 3]};
+    const q4 Rb{br[4 * size_t(ab.y)], br[4 * size_t(ab.y) + 1], br[4 * size_t(ab.y) + 2], br[4 * size_t(ab.y) + 3]};
+    // base chord rounded to FP32; everything below is computed from that rounded chord
+    const float4 d0f = make_float4(float(xb.x - xa.x), float(xb.y - xa.y), float(xb.z - xa.z), 0.f);
+    const d3 d0{double(d0f.x), double(d0f.y), double(d0f.z)};
+    const double L0 = t.L0[b];
+    const double Lb = sqrt(dot(d0, d0));
+    const double c0 = dot(d0, d0) - L0 * L0;
+    const d3 t0 = d0 * (1.0 / Lb);
+    const d3 e0{t.e0x[b], t.e0y[b], t.e0z[b]};
+    const d3 da0 = qrot(Ra, e0), db0 = qrot(Rb, e0);
+    const d3 sa0 = da0 - t0, sb0 = db0 - t0;
+    q4 Q0 = qmul(conj(Ra), Rb);
+    if (Q0.w < 0) Q0 = q4{-Q0.w, -Q0.x, -Q0.y, -Q0.z};
+    const double v2 = Q0.x * Q0.x + Q0.y * Q0.y + Q0.z * Q0.z;
+    const double wm1 = -v2 / (1.0 + Q0.w);  // w - 1 without cancellation
+    m.B0[b] = make_float4(d0f.x, d0f.y, d0f.z, float(c0));
+    m.B1[b] = make_float4(float(da0.x), float(da0.y), float(da0.z), float(L0));
+    m.B2[b] = make_float4(float(db0.x), float(db0.y), float(db0.z), float(Lb));
+    m.B3[b] = make_float4(float(sa0.x), float(sa0.y), float(sa0.z), 0.f);
+    m.B4[b] = make_float4(float(sb0.x), float(sb0.y), float(sb0.z), 0.f);
+    m.B5[b] = make_float4(float(wm1), float(Q0.x), float(Q0.y), float(Q0.z));
+}
+
+// Section constants in FP32 (same expressions as the FP64 constants), once per upload.
+__global__ void __launch_bounds__(kBlock) k_mixed_constants(DevTopo t, MixedBeams m) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= t.B) return;
+    m.C0[b] = make_float4(float(t.kb[b]), float(t.kt[b]), float(t.my[b]), float(t.ty[b]));
+    m.C1[b] = make_float4(float(t.cs[b]), float(t.aL[b]), float(t.area[b]), float(t.aLsy[b]));
+}
+
+// ---- beam kernel (MC/src/sim.cpp:139-141, FP32 with the split above) ---------------------
+__global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
+                                                        const float4* __restrict__ U, const float4* __restrict__ Ei,
+                                                        const float4* __restrict__ R0f, EvalBufs e) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const int B = t.B;
+    float acc[3] = {0.f, 0.f, 0.f};
+    if (b < B) {
+        const int2 ab = t.ab[b];
+        const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B3 = m.B3[b], B4 = m.B4[b], B5 = m.B5[b];
+        const float4 ua4 = U[ab.x], ub4 = U[ab.y];
+        const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
+        const float c0 = B0.w, L0 = B1.w, Lb = B2.w;
+        const float q = c0 + 2.f * fdot(d0, du) + fdot(du, du);  // |d|^2 - L0^2
+        const f3 d = d0 + du;
+        const float L = sqrtf(fmaxf(L0 * L0 + q, 0.f));
+        float* sa = e.slotAf + 6 * size_t(b);
+        float* sb = e.slotBf + 6 * size_t(b);
+        if (L < 1e-10f) {
+            acc[0] = 1e8f * (1e-10f - L) * (1e-10f - L);
+#pragma unroll
+            for (int k = 0; k < 6; k++) { sa[k] = 0.f; sb[k] = 0.f; }
+            if (trials) {
+#pragma unroll
+                for (int k = 0; k < 7; k++) { e.trial_nextf[k * size_t(B) + b] = 0.f; e.trial_auxf[k * size_t(B) + b] = 0.f; }
+#pragma unroll
+                for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
+            }
+        } else {
+            const float invL = 1.f / L;
+            const f3 tt = d * invL;
+            const float eps = q / ((L + L0) * L0);
+            const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), rotp
+            const float4 C0 = m.C0[b], C1 = m.C1[b];  // (kb, kt, my, ty), (cs, aL, area, aLsy)
+            const float E = float(mat.E), H = float(mat.H), sy = float(mat.sy);
+            // axial
+            const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
+            const float uax = C1.y * (ax.energy + ax.hard);
+            const float dax = C1.w * ax.dg;
+            f3 F = tt * (C1.z * ax.force);
+            // shear from the split director/chord differences
+            const float4 ea = Ei[ab.x], eb = Ei[ab.y];
+            const f3 va = xyz(make_float4(ea.y, ea.z, ea.w, 0.f)), vb = xyz(make_float4(eb.y, eb.z, eb.w, 0.f));
+            const float wa = 1.f + ea.x, wb = 1.f + eb.x;
+            const f3 da0 = xyz(B1), db0 = xyz(B2);
+            const f3 dda = rot_inc(wa, va, da0), ddb = rot_inc(wb, vb, db0);
+            const f3 da = da0 + dda, db = db0 + ddb;
+            const float dLb = (2.f * fdot(d0, du) + fdot(du, du)) / (L + Lb);
+            const f3 tdiff = (du * Lb - d0 * dLb) * (1.f / (L * Lb));  // t - t0
+            const f3 ma = dda + xyz(B3) - tdiff, mb = ddb + xyz(B4) - tdiff;
+            const float cs = C1.x;
+            const float us = .5f * cs * (fdot(ma, ma) + fdot(mb, mb));
+            const f3 gt = (ma + mb) * (-cs);  // cs (2t - da - db)
+            const f3 trans = (gt - tt * fdot(gt, tt)) * invL;
+            F = F + trans;
+            f3 Ga = -(fcross(da, tt) * cs);
+            f3 Gb = -(fcross(db, tt) * cs);
+            // relative rotation (Ra0^* delta Ra0) Q0, delta = e_a^* e_b, near-identity forms
+            const float dw1 = ea.x + eb.x + ea.x * eb.x + fdot(va, vb);
+            const f3 dv0 = (vb - va) + vb * ea.x - va * eb.x - fcross(va, vb);
+            const float4 ra0 = R0f[ab.x];
+            const f3 ra0v{ra0.y, ra0.z, ra0.w};
+            const f3 dv = rot_conj(ra0.x, ra0v, dv0);
+            const float a0 = B5.x;
+            const f3 v0{B5.y, B5.z, B5.w};
+            const float qw1 = dw1 + a0 + dw1 * a0 - fdot(dv, v0);
+            f3 qv = dv + v0 + v0 * dw1 + dv * a0 + fcross(dv, v0);
+            float qw = 1.f + qw1;
+            if (qw < 0.f) { qw = -qw; qv = -qv; }
+            const float s = sqrtf(fdot(qv, qv));
+            const f3 phi = s < 1e-30f ? qv * (2.f / qw) : qv * (2.f * atan2f(s, qw) / s);
+            // axis = unit(Ra^T t), Ra = e_a Ra0
+            f3 ax_ = rot_conj(ra0.x, ra0v, rot_conj(wa, va, tt));
+            const float al2 = fdot(ax_, ax_);
+            const f3 axis = (isfinite(al2) && al2 > 1e-30f) ? ax_ * rsqrtf(al2) : f3{0.f, 1.f, 0.f};
+            const f3 rotp{P1.x, P1.y, P1.z};
+            const float tw = fdot(phi, axis), ptw = fdot(rotp, axis);
+            const f3 bend = phi - axis * tw, pbv = rotp - axis * ptw;
+            const float kb = C0.x, kt = C0.y, my = C0.z, ty = C0.w;
+            const R3 br = ret3(bend, pbv, P0.z, kb, my, float(mat.bend_h) * kb);
+            const R1 tor = ret1(tw, ptw, P0.w, kt, ty, float(mat.torsion_h) * kt);
+            const f3 moment = br.force + axis * tor.force;
+            const float ur = br.energy + br.hard + tor.energy + tor.hard;
+            const float dr = my * br.dg + ty * tor.dg;
+            const f3 world = rot(wa, va, rot(ra0.x, ra0v, jl_inv_t_f(phi, moment)));
+            Ga = Ga - world;
+            Gb = Gb + world;
+            acc[0] = (uax + dax) + us + (ur + dr);
+            acc[1] = uax + us + ur;
+            acc[2] = dax + dr;
+            sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
+            sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
+            if (trials) {
+                const size_t S = size_t(B);
+                const f3 nrot = br.p + axis * tor.p;
+                e.trial_nextf[b] = ax.p;
+                e.trial_nextf[S + b] = ax.a;
+                e.trial_nextf[2 * S + b] = nrot.x;
+                e.trial_nextf[3 * S + b] = nrot.y;
+                e.trial_nextf[4 * S + b] = nrot.z;
+                e.trial_nextf[5 * S + b] = br.a;
+                e.trial_nextf[6 * S + b] = tor.a;
+                e.trial_auxf[b] = eps;
+                e.trial_auxf[S + b] = ax.force;
+                e.trial_auxf[2 * S + b] = moment.x;
+                e.trial_auxf[3 * S + b] = moment.y;
+                e.trial_auxf[4 * S + b] = moment.z;
+                e.trial_auxf[5 * S + b] = uax + us + ur;
+                e.trial_auxf[6 * S + b] = dax + dr;
+                e.trial_flags[b] = ax.yielded;
+                e.trial_flags[S + b] = br.yielded;
+                e.trial_flags[2 * S + b] = tor.yielded;
+            }
+        }
+    }
+    double tot[3];
+    block_sum_f<3>(acc, tot, sm);
+    if (threadIdx.x == 0) {
+        e.part_beam[3 * blockIdx.x] = tot[0];
+        e.part_beam[3 * blockIdx.x + 1] = tot[1];
+        e.part_beam[3 * blockIdx.x + 2] = tot[2];
+    }
+}
+
+// Plastic state of the mixed form: (epsp, alpha, alphaB, alphaT) and rotp as float4 pairs,
+// from/to the 7-array SoA trial layout.
+__global__ void __launch_bounds__(kBlock) k_plastic_pack(int B, const float* __restrict__ soa7, float4* __restrict__ P0,
+                                                         float4* __restrict__ P1) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const size_t S = size_t(B);
+    P0[b] = make_float4(soa7[b], soa7[S + b], soa7[5 * S + b], soa7[6 * S + b]);
+    P1[b] = make_float4(soa7[2 * S + b], soa7[3 * S + b], soa7[4 * S + b], 0.f);
+}
+__global__ void __launch_bounds__(kBlock) k_plastic_from_f64(int B, const double* __restrict__ soa7,
+                                                             float4* __restrict__ P0, float4* __restrict__ P1) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const size_t S = size_t(B);
+    P0[b] = make_float4(float(soa7[b]), float(soa7[S + b]), float(soa7[5 * S + b]), float(soa7[6 * S + b]));
+    P1[b] = make_float4(float(soa7[2 * S + b]), float(soa7[3 * S + b]), float(soa7[4 * S + b]), 0.f);
+}
+__global__ void __launch_bounds__(kBlock) k_plastic_to_f64(int B, const float4* __restrict__ P0,
+                                                           const float4* __restrict__ P1, double* __restrict__ soa7) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    const size_t S = size_t(B);
+    const float4 p = P0[b], r = P1[b];
+    soa7[b] = p.x; soa7[S + b] = p.y; soa7[2 * S + b] = r.x; soa7[3 * S + b] = r.y; soa7[4 * S + b] = r.z;
+    soa7[5 * S + b] = p.z; soa7[6 * S + b] = p.w;
+}
+__global__ void k_f32_to_f64(long long n, const float* __restrict__ a, double* __restrict__ o) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        o[i] = a[i];
+}
+
+}  // namespace
+
+void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
+                        const MixedNodes& mn, EvalBufs& e, cudaStream_t s) {
+    const int nb = nb_nodes(t.N);
+    k_state_mixed<<<nb, kBlock, 0, s>>>(t.N, p.translation_scale, t.locked, z, base_x, mn.U, mn.E, e.x, e.xf_lo,
+                                        e.xf_hi, e.part_state);
+    note_launches(1);
+    launch_center(t.N, e, s);
+}
+
+void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
+                        EvalBufs& e, cudaStream_t s) {
+    if (t.B == 0) return;
+    k_beams_mixed<<<nb_beams(t.B), kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
+    note_launches(1);
+}
+
+void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
+                         MixedNodes& mn, cudaStream_t s) {
+    k_rebase_nodes<<<grid_for(t.N), kBlock, 0, s>>>(t.N, base_r, mn.R0f);
+    note_launches(1);
+    if (t.B) {
+        k_rebase_beams<<<grid_for(t.B), kBlock, 0, s>>>(t, base_x, base_r, mb);
+        note_launches(1);
+    }
+}
+
+void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s) {
+    if (!t.B) return;
+    k_mixed_constants<<<grid_for(t.B), kBlock, 0, s>>>(t, mb);
+    note_launches(1);
+}
+
+void launch_plastic_mixed(int B, const double* plastic64, const float* trial32, MixedBeams& mb, cudaStream_t s) {
+    if (!B) return;
+    if (trial32) k_plastic_pack<<<grid_for(B), kBlock, 0, s>>>(B, trial32, mb.P0, mb.P1);
+    else k_plastic_from_f64<<<grid_for(B), kBlock, 0, s>>>(B, plastic64, mb.P0, mb.P1);
+    note_launches(1);
+}
+
+void launch_plastic_mixed_to_f64(int B, const MixedBeams& mb, double* plastic64, cudaStream_t s) {
+    if (!B) return;
+    k_plastic_to_f64<<<grid_for(B), kBlock, 0, s>>>(B, mb.P0, mb.P1, plastic64);
+    note_launches(1);
+}
+
+void launch_f32_to_f64(long long n, const float* a, double* o, cudaStream_t s) {
+    if (n <= 0) return;
+    k_f32_to_f64<<<grid_for(n < 152 * 8 * kBlock ? n : 152 * 8 * kBlock), kBlock, 0, s>>>(n, a, o);
+    note_launches(1);
+}
+
+}  // namespace mcg
