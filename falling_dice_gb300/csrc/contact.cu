@@ -36,6 +36,7 @@ namespace {
 constexpr long long kMaxCellsPerShape = 1 << 12;
 constexpr int kWarpCap = 64;            // bins up to this size are staged in shared memory
 constexpr int kPairWarps = kBlock / 32;
+constexpr int kStreamBlocks = 8 * 152;
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
     v &= 0x3ffu;
@@ -380,9 +381,12 @@ __device__ __forceinline__ BinShape shfl_shape(const BinShape& v, int src) {
     return o;
 }
 
-// Candidate pairs of every occupied bin, one warp per bin.  write == 0: the count per bin
-// into bcount.  write != 0: the pairs (lower shape, higher shape) at boffset, in the
-// enumeration order, which is fixed:
+// Candidate pairs of every occupied bin.  Warp w of the fixed grid takes the occupied bins
+// occ[w], occ[w + W], ... in order and appends their candidate pairs (lower shape, higher
+// shape) to its own region cand[w R .. (w + 1) R), so the candidate list -- regions in warp
+// order, each in bin and enumeration order -- is deterministic without a second counting
+// pass.  A region that fills up flags kOverCandidates; wcount[w] keeps the full count so the
+// host can size R.  Enumeration inside a bin:
 //   n <= 32  the bin's shapes are sorted across the warp's lanes (bitonic, by shape id)
 //            and every unordered pair is visited by rotation: in round k lane i meets
 //            lane (i + k) mod n, k = 1 .. n/2 (the last round of an even n only from the
@@ -393,33 +397,33 @@ __device__ __forceinline__ BinShape shfl_shape(const BinShape& v, int src) {
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count,
                                                       const uint32_t* __restrict__ bin_start,
+                                                      const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
                                                       const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
                                                       const int4* __restrict__ cell_lo, const float4* __restrict__ bb_lo,
-                                                      const float4* __restrict__ bb_hi, int write,
-                                                      uint32_t* __restrict__ bcount, const uint32_t* __restrict__ boffset,
-                                                      long long cand_cap, uint2* __restrict__ cand) {
+                                                      const float4* __restrict__ bb_hi, int region,
+                                                      uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
+                                                      uint32_t* __restrict__ flags) {
     __shared__ BinShape sh[kPairWarps][kWarpCap];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    const long long nb = grid[8];
+    const long long nocc = *nocc_p;
+    const long long gw = (long long)blockIdx.x * kPairWarps + w;
     const long long warps = (long long)gridDim.x * kPairWarps;
-    for (long long b = (long long)blockIdx.x * kPairWarps + w; b < nb; b += warps) {
-        const int n = int(bin_count[b]);
-        if (n < 2 || (write && bcount[b] == 0)) {
-            if (!write && lane == 0) bcount[b] = 0;
-            continue;
+    uint2* mine = cand + gw * region;
+    uint32_t out = 0;
+    auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (hit) {
+            const uint32_t pos = out + __popc(m & below);
+            if (pos < uint32_t(region)) mine[pos] = make_uint2(sa, sb);
         }
+        out += __popc(m);
+    };
+    for (long long j = gw; j < nocc; j += warps) {
+        const uint32_t b = occ[j];
+        const int n = int(bin_count[b]);
         const uint32_t start = bin_start[b];
-        const int3 cc = cell_of(grid, uint32_t(b));
-        uint32_t out = write ? boffset[b] : 0;
-        auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
-            const unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (write && hit) {
-                const uint32_t pos = out + __popc(m & below);
-                if (pos < uint32_t(cand_cap)) cand[pos] = make_uint2(sa, sb);
-            }
-            out += __popc(m);
-        };
+        const int3 cc = cell_of(grid, b);
         if (n <= 32) {
             uint32_t v = lane < n ? sorted[start + lane] : 0xffffffffu;
             for (int k = 2; k <= 32; k <<= 1)  // bitonic sort, ascending
@@ -498,44 +502,76 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
             }
             __syncwarp();
         }
-        if (!write && lane == 0) bcount[b] = out;
+    }
+    if (lane == 0) {
+        wcount[gw] = out;
+        if (out > uint32_t(region)) atomicOr(flags, uint32_t(kOverCandidates));
     }
 }
 
-constexpr int kContactPartBlocks = 128;
-constexpr int kStreamBlocks = 8 * 152;
+// Occupied bins (two or more entries), in bin order: flags, then a scan, then this.
+__global__ void __launch_bounds__(kBlock) k_occ_flags(long long nb_cap, const int* __restrict__ grid,
+                                                      const uint32_t* __restrict__ bin_count, uint32_t* __restrict__ f) {
+    const long long nb = grid[8];
+    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
+        f[b] = (b < nb && bin_count[b] >= 2) ? 1u : 0u;
+}
+__global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const uint32_t* __restrict__ f,
+                                                      const uint32_t* __restrict__ off, uint32_t* __restrict__ occ) {
+    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
+        if (f[b]) occ[off[b]] = uint32_t(b);
+}
 
-// Narrow phase over the candidate list, one thread per candidate.  write == 0: hit flags
-// (1/0) into hit.  write != 0: the contacts of the hits at hoffset (the candidate order).
+constexpr int kContactPartBlocks = 128;
+
+// Narrow phase over the candidate regions, one warp per region (the region's owner in
+// k_bin_pairs).  Pass 0: test every candidate, keep one hit bit per candidate and the hit
+// count per region.  Pass 1 (after a scan of the counts): test the hits again and write
+// them as contacts, in region and candidate order.
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                   const uint32_t* __restrict__ ncand_p, long long cand_cap,
-                                                   const uint2* __restrict__ cand, int write,
-                                                   uint32_t* __restrict__ hit, const uint32_t* __restrict__ hoffset,
-                                                   ContactBufs c, uint32_t* flags) {
-    const long long nall = *ncand_p;
-    if (nall > cand_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, uint32_t(kOverCandidates));
-        return;
-    }
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nall; i += (long long)gridDim.x * blockDim.x) {
-        if (write && !hit[i]) continue;
-        const uint2 q = cand[i];
-        const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
-        if (!write) {
-            hit[i] = h.hit ? 1u : 0u;
-            continue;
+                                                   int region, const uint2* __restrict__ cand,
+                                                   const uint32_t* __restrict__ wcount, int pass,
+                                                   uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
+                                                   const uint32_t* __restrict__ hoff, ContactBufs c) {
+    const int lane = threadIdx.x & 31;
+    const long long gw = (long long)blockIdx.x * kPairWarps + (threadIdx.x >> 5);
+    const uint32_t nc = min(wcount[gw], uint32_t(region));
+    const uint2* mine = cand + gw * region;
+    uint32_t* bits = hitbits + gw * (region / 32);
+    const unsigned below = (1u << lane) - 1u;
+    uint32_t pos = pass ? hoff[gw] : 0;
+    for (uint32_t base = 0; base < nc; base += 32) {
+        const uint32_t i = base + lane;
+        if (pass) {
+            const unsigned m = bits[base / 32];
+            if (m & (1u << lane)) {
+                const uint2 q = mine[i];
+                const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
+                const uint32_t o = pos + __popc(m & below);
+                if (o < uint32_t(c.contact_cap)) {
+                    c.c_a[o] = q.x;
+                    c.c_b[o] = q.y;
+                    c.c_s[o] = h.s;
+                    c.c_t[o] = h.t;
+                    c.c_n[3 * size_t(o)] = h.n.x;
+                    c.c_n[3 * size_t(o) + 1] = h.n.y;
+                    c.c_n[3 * size_t(o) + 2] = h.n.z;
+                    c.c_pen[o] = h.pen;
+                }
+            }
+            pos += __popc(m);
+        } else {
+            bool hit = false;
+            if (i < nc) {
+                const uint2 q = mine[i];
+                hit = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) bits[base / 32] = m;
+            pos += __popc(m);
         }
-        const uint32_t pos = hoffset[i];
-        if (pos >= uint32_t(c.contact_cap)) continue;
-        c.c_a[pos] = q.x;
-        c.c_b[pos] = q.y;
-        c.c_s[pos] = h.s;
-        c.c_t[pos] = h.t;
-        c.c_n[3 * size_t(pos)] = h.n.x;
-        c.c_n[3 * size_t(pos) + 1] = h.n.y;
-        c.c_n[3 * size_t(pos) + 2] = h.n.z;
-        c.c_pen[pos] = h.pen;
     }
+    if (!pass && lane == 0) hcount[gw] = pos;
 }
 
 // Fixed-partition reduction over the contact list: energy, max penetration, count.
@@ -594,6 +630,11 @@ __global__ void __launch_bounds__(kBlock) k_node_fill(DevTopo t, const uint32_t*
 
 int contact_part_blocks(long long) { return kContactPartBlocks; }
 
+int contact_pair_blocks(long long shapes) {
+    const long long b = shapes / 256;
+    return int(b < 1 ? 1 : (b > 8 * 152 ? 8 * 152 : b));
+}
+
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
                      cudaStream_t s) {
     const int S = t.N + t.B;
@@ -608,25 +649,22 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s);
     (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted),
      note_launches(1));
-    // candidates: count per bin, scan, write
-    const unsigned pair_blocks = 152 * 8;
-    cudaMemsetAsync(c.bcount, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
-    (k_bin_pairs<<<pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
-                                                c.bb_lo, c.bb_hi, 0, c.bcount, c.boffset, c.cand_cap, c.cand),
-     note_launches(1));
+    // occupied bins, then candidates into per-warp regions
+    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount), note_launches(1));
     exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s);
-    (k_bin_pairs<<<pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.sorted, c.sorted2, c.cell_lo,
-                                                c.bb_lo, c.bb_hi, 1, c.bcount, c.boffset, c.cand_cap, c.cand),
+    (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ), note_launches(1));
+    const uint32_t* nocc = c.boffset + c.bin_cap;
+    const int W = c.pair_blocks * kPairWarps;
+    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted, c.sorted2,
+                                                c.cell_lo, c.bb_lo, c.bb_hi, c.region, c.cand, c.wcount, c.flags),
      note_launches(1));
-    const uint32_t* ncand = c.boffset + c.bin_cap;
-    // narrow phase: hit flags, scan, contacts
-    cudaMemsetAsync(c.hit, 0, size_t(c.cand_cap + 1) * sizeof(uint32_t), s);
-    (k_narrow<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, ncand, c.cand_cap, c.cand, 0, c.hit, c.hoffset, c, c.flags),
-     note_launches(1));
-    exclusive_scan_u32(c.hit, c.hoffset, c.cand_cap, c.scan_tmp, s);
-    (k_narrow<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, ncand, c.cand_cap, c.cand, 1, c.hit, c.hoffset, c, c.flags),
-     note_launches(1));
-    const uint32_t* total = c.hoffset + c.cand_cap;
+    // narrow phase: hit bits and counts per region, scan, contacts
+    (k_narrow<<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.region, c.cand, c.wcount, 0, c.hitbits, c.hcount,
+                                               c.hoff, c), note_launches(1));
+    exclusive_scan_u32(c.hcount, c.hoff, W, c.scan_tmp, s);
+    (k_narrow<<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.region, c.cand, c.wcount, 1, c.hitbits, c.hcount,
+                                               c.hoff, c), note_launches(1));
+    const uint32_t* total = c.hoff + W;
     (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, p.contact_k, c.c_pen, c.part, c.flags),
      note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);

@@ -154,7 +154,7 @@ struct mcg_ctx {
 
     // ---- contact buffers ---------------------------------------------------------------
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
-    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, long long cand_cap) {
+    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, int region) {
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
@@ -176,10 +176,15 @@ struct mcg_ctx {
         c.bin_start = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
-        c.cand_cap = cand_cap;
-        c.cand = contact_mem.get<uint2>(size_t(cand_cap));
-        c.hit = contact_mem.get<uint32_t>(size_t(cand_cap + 1));
-        c.hoffset = contact_mem.get<uint32_t>(size_t(cand_cap + 1));
+        c.occ = contact_mem.get<uint32_t>(size_t(bin_cap));
+        c.pair_blocks = contact_pair_blocks(S);
+        const long long W = (long long)c.pair_blocks * 8;
+        c.region = std::max(32, (region + 31) / 32 * 32);
+        c.cand = contact_mem.get<uint2>(size_t(W * c.region));
+        c.wcount = contact_mem.get<uint32_t>(size_t(W));
+        c.hitbits = contact_mem.get<uint32_t>(size_t(W * c.region / 32));
+        c.hcount = contact_mem.get<uint32_t>(size_t(W + 1));
+        c.hoff = contact_mem.get<uint32_t>(size_t(W + 1));
         c.contact_cap = contact_cap;
         c.c_a = contact_mem.get<uint32_t>(size_t(contact_cap));
         c.c_b = contact_mem.get<uint32_t>(size_t(contact_cap));
@@ -192,7 +197,7 @@ struct mcg_ctx {
         c.n_cursor = contact_mem.get<uint32_t>(size_t(N));
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.part = contact_mem.get<double>(size_t(3 * contact_part_blocks(contact_cap)));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, cand_cap + 1}));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         cb = c;
@@ -202,15 +207,21 @@ struct mcg_ctx {
     bool grow_contacts(int flags) {
         if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan | kOverCandidates))) return false;
         const long long S = (long long)N + B;
-        uint32_t need[3] = {0, 0, 0};
+        const long long W = (long long)cb.pair_blocks * 8;
+        uint32_t need[2] = {0, 0};
         int grid[16];
+        std::vector<uint32_t> wc(static_cast<size_t>(W));
         ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(&need[1], cb.hoffset + cb.cand_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(&need[2], cb.boffset + cb.bin_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[1], cb.hoff + W, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(wc.data(), cb.wcount, size_t(W) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
-        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap, qcap = cb.cand_cap;
-        if (flags & kOverCandidates) qcap = std::max(qcap, (long long)need[2] + need[2] / 4 + 1024);
+        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap;
+        int region = cb.region;
+        if (flags & kOverCandidates) {
+            const long long mx = *std::max_element(wc.begin(), wc.end());
+            region = int(std::min<long long>(std::max<long long>(region, mx + mx / 4 + 32), 1LL << 26));
+        }
         if (flags & kOverSpan) broad_cell *= 2;
         if (flags & kOverEntries) ecap = std::max(ecap, (long long)need[0] + need[0] / 4 + 1024);
         if (flags & kOverContacts) ccap = std::max(ccap, (long long)need[1] + need[1] / 4 + 1024);
@@ -219,7 +230,7 @@ struct mcg_ctx {
             if (want <= (1LL << 28)) bcap = std::max(bcap, want);
             else broad_cell *= 2;  // a huge extent: coarser cells instead of more bins
         }
-        alloc_contacts(ecap, ccap, bcap, qcap);
+        alloc_contacts(ecap, ccap, bcap, region);
         return true;
     }
 
@@ -276,7 +287,8 @@ struct mcg_ctx {
     }
     long long read_contact_count() {
         uint32_t nc = 0;
-        ck(cudaMemcpyAsync(&nc, cb.hoffset + cb.cand_cap, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&nc, cb.hoff + (long long)cb.pair_blocks * 8, sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           stream), "copy");
         sync();
         return nc;
     }
@@ -887,8 +899,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
             int bits = 3;
             while ((1LL << bits) < dmax && bits < 10) bits++;
             const long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
-            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap,
-                              std::max<long long>(4 * S, 4096));
+            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap, 1024);
         }
         // solver vectors
         DevArena& Q = c->solver_mem;
@@ -1157,8 +1168,9 @@ int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, in
             throw Fail(MCG_ERR_INVALID, "capacities must be non-negative and bins at most 2^28");
         const long long lo = 4096;
         c->sync();
+        const long long W = (long long)contact_pair_blocks((long long)c->N + c->B) * 8;
         c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
-                          std::max<long long>(bins, lo), std::max<long long>(candidates, lo));
+                          std::max<long long>(bins, lo), int(std::min<long long>((candidates + W - 1) / W, 1LL << 26)));
     });
 }
 

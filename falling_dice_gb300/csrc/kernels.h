@@ -68,7 +68,7 @@ enum ContactFlag : uint32_t {
     kOverBins = 4,       // the grid needs more bins than bin_cap
     kNonFinite = 8,      // a shape has a non-finite bounding box (informational)
     kOverSpan = 16,      // a shape spans more cells than allowed: coarsen the grid
-    kOverCandidates = 32 // more narrow-phase candidates than cand_cap
+    kOverCandidates = 32 // a warp found more narrow-phase candidates than its region holds
 };
 
 struct ContactBufs {
@@ -91,14 +91,17 @@ struct ContactBufs {
     long long bin_cap;
     uint32_t* bin_count;    // [bin_cap+1]
     uint32_t* bin_start;    // [bin_cap+1]
-    uint32_t* bcount;       // [bin_cap+1] candidate pairs per bin
-    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = candidate count
-    // narrow-phase candidates in (bin, pair) order
-    long long cand_cap;
-    uint2* cand;            // [cand_cap] (lower shape, higher shape)
-    uint32_t* hit;          // [cand_cap+1] 1 where the candidate is in contact
-    uint32_t* hoffset;      // [cand_cap+1] scan of hit; hoffset[cand_cap] = contact count
-    // contacts, in deterministic (bin, pair) order
+    uint32_t* bcount;       // [bin_cap+1] 1 where a bin holds two or more entries
+    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = occupied bins
+    uint32_t* occ;          // [bin_cap] occupied bins in bin order
+    // narrow-phase candidates: warp w of the pair grid owns cand[w * region, (w + 1) * region)
+    int pair_blocks;        // blocks of the pair and narrow-phase grids (8 warps each)
+    int region;             // candidate slots per warp, a multiple of 32
+    uint2* cand;            // [warps * region] (lower shape, higher shape)
+    uint32_t* wcount;       // [warps] candidates found per warp (may exceed region)
+    uint32_t* hitbits;      // [warps * region / 32] contact bit per candidate
+    uint32_t* hcount;       // [warps + 1] contacts per warp
+    uint32_t* hoff;         // [warps + 1] scan of hcount; hoff[warps] = contact count
     long long contact_cap;
     uint32_t* c_a;          // lower shape index
     uint32_t* c_b;          // higher shape index
@@ -197,6 +200,8 @@ void launch_plastic_stats(int B, const double* plastic, double* part, double* ou
 
 // ---- contact pipeline (contact.cu) ------------------------------------------------------
 int contact_part_blocks(long long contact_cap);
+// Blocks of the pair / narrow-phase grid for a model of `shapes` shapes (8 warps each).
+int contact_pair_blocks(long long shapes);
 // The whole broad/narrow phase: grid, entries, bins, pairs, contact list, node lists.
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
                      cudaStream_t s);

@@ -96,10 +96,15 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.bin_start = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.bcount = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.boffset = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
-    c.cand_cap = kNoAllocCandidates;
-    c.cand = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
-    c.hit = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocCandidates + 1) * 4));
-    c.hoffset = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocCandidates + 1) * 4));
+    c.occ = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * 4));
+    c.pair_blocks = contact_pair_blocks(S);
+    const long long W = (long long)c.pair_blocks * 8;
+    c.region = int((kNoAllocCandidates / W + 31) / 32 * 32);
+    c.cand = reinterpret_cast<uint2*>(take(size_t(W * c.region) * sizeof(uint2)));
+    c.wcount = reinterpret_cast<uint32_t*>(take(size_t(W) * 4));
+    c.hitbits = reinterpret_cast<uint32_t*>(take(size_t(W * c.region / 32) * 4));
+    c.hcount = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
+    c.hoff = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
     c.contact_cap = kNoAllocContacts;
     c.c_a = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocContacts) * 4));
     c.c_b = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocContacts) * 4));
@@ -114,7 +119,6 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.part = reinterpret_cast<double*>(take(size_t(3 * contact_part_blocks(kNoAllocContacts)) * 8));
     long long scan_n = S + 1;
     if (kNoAllocBins + 1 > scan_n) scan_n = kNoAllocBins + 1;
-    if (kNoAllocCandidates + 1 > scan_n) scan_n = kNoAllocCandidates + 1;
     c.scan_tmp_bytes = scan_tmp_bytes(scan_n);
     c.scan_tmp = take(c.scan_tmp_bytes);
     return off <= kNoAllocScratchBytes;

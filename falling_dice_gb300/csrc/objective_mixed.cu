@@ -21,8 +21,12 @@
 //   Ra^* Rb      = (Ra0^* delta Ra0) Q0,  delta = e_a^* e_b              Q0 = Ra0^* Rb0
 // with inc(e, v) = R(e) v - v evaluated as 2w (u x v) + 2 u x (u x v) and the near-identity
 // quaternions held as (w - 1, v), so that every FP32 rounding is relative to an increment.
-// d0 is the base chord rounded to FP32 and c0, s_a0 are computed from that rounded chord,
-// so the split is exact for a base chord perturbed by one FP32 rounding (about 3e-10 m).
+// d0 is the base chord rounded to FP32, while c0, |d0| and s_a0 are computed from the exact
+// chord: the rounding of d0 then only enters multiplied by an increment, and a beam at its
+// base state sees exactly the base strain and shear.  One case stays out of reach: the
+// reference's degenerate-beam branch (chord below 1e-10 m, sim.cpp:139) lies below the
+// FP32 resolution of a position increment, so the mixed form resolves chords only down to
+// about 1e-9 m.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -228,9 +232,11 @@ __global__ void __launch_bounds__(kBlock) k_rebase_beams(DevTopo t, const double
     const d3 xb{bx[3 * size_t(ab.y)], bx[3 * size_t(ab.y) + 1], bx[3 * size_t(ab.y) + 2]};
     const q4 Ra{br[4 * size_t(ab.x)], br[4 * size_t(ab.x) + 1], br[4 * size_t(ab.x) + 2], br[4 * size_t(ab.x) + 3]};
     const q4 Rb{br[4 * size_t(ab.y)], br[4 * size_t(ab.y) + 1], br[4 * size_t(ab.y) + 2], br[4 * size_t(ab.y) + 3]};
-    // base chord rounded to FP32; everything below is computed from that rounded chord
-    const float4 d0f = make_float4(float(xb.x - xa.x), float(xb.y - xa.y), float(xb.z - xa.z), 0.f);
-    const d3 d0{double(d0f.x), double(d0f.y), double(d0f.z)};
+    // The base chord is stored rounded to FP32; c0, |d0| and t0 come from the exact FP64
+    // chord, so a beam at its base state carries no prestrain or shear from that rounding
+    // (the rounding only enters multiplied by the increment).
+    const d3 d0{xb.x - xa.x, xb.y - xa.y, xb.z - xa.z};
+    const float4 d0f = make_float4(float(d0.x), float(d0.y), float(d0.z), 0.f);
     const double L0 = t.L0[b];
     const double Lb = sqrt(dot(d0, d0));
     const double c0 = dot(d0, d0) - L0 * L0;
@@ -314,8 +320,10 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
             const f3 gt = (ma + mb) * (-cs);  // cs (2t - da - db)
             const f3 trans = (gt - tt * fdot(gt, tt)) * invL;
             F = F + trans;
-            f3 Ga = -(fcross(da, tt) * cs);
-            f3 Gb = -(fcross(db, tt) * cs);
+            // -cs (d x t) = cs d x (d - t): the moment from the small shear vector, so the
+            // independent FP32 roundings of d and t leave no residual moment at rest
+            f3 Ga = fcross(da, ma) * cs;
+            f3 Gb = fcross(db, mb) * cs;
             // relative rotation (Ra0^* delta Ra0) Q0, delta = e_a^* e_b, near-identity forms
             const float dw1 = ea.x + eb.x + ea.x * eb.x + fdot(va, vb);
             const f3 dv0 = (vb - va) + vb * ea.x - va * eb.x - fcross(va, vb);
