@@ -47,6 +47,7 @@ SIGNATURES = {
     "mcg_launch_count": (C.c_int64, [_P]),
     "mcg_set_timing": (C.c_int, [_P, C.c_int]),
     "mcg_set_contact_capacity": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64]),
+    "mcg_set_contact_skin": (C.c_int, [_P, C.c_double]),
     "mcg_phase_times": (C.c_int, [_P, _d, C.c_int32, C.POINTER(C.c_int64)]),
     "mcg_lattice_generate": (C.c_int, [C.POINTER(abi.LatticeSpec), C.POINTER(abi.Config), C.POINTER(_P)]),
     "mcg_lattice_view_of": (C.c_int, [_P, C.POINTER(abi.LatticeView)]),
@@ -240,6 +241,10 @@ class Solver:
 
     def launch_count(self):
         return self.lib.mcg_launch_count(self.h)
+
+    def set_contact_skin(self, skin):
+        """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""
+        self._check(self.lib.mcg_set_contact_skin(self.h, float(skin)), "mcg_set_contact_skin")
 
     def set_contact_capacity(self, entries, candidates, contacts, bins):
         self._check(self.lib.mcg_set_contact_capacity(self.h, entries, candidates, contacts, bins),

@@ -34,6 +34,10 @@ namespace mcg {
 namespace {
 
 constexpr long long kMaxCellsPerShape = 1 << 12;
+constexpr float kBoxQuanta = 32000.f;   // quantization steps across the grid extent
+constexpr uint32_t kBoxMax = 32767u;    // 15-bit box coordinates
+constexpr uint32_t kGuard2 = 0x80008000u;
+constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kWarpCap = 64;            // bins up to this size are staged in shared memory
 constexpr int kPairWarps = kBlock / 32;
 constexpr int kStreamBlocks = 8 * 152;
@@ -67,6 +71,12 @@ __device__ __forceinline__ int3 cell_of(const int* g, uint32_t b) {
     const int j = int((b / uint32_t(g[3])) % uint32_t(g[4]));
     const int k = int(b / (uint32_t(g[3]) * uint32_t(g[4])));
     return make_int3(i, j, k);
+}
+
+// First cell of a shape packed for the pair test (10 bits per axis, relative to the grid
+// origin).
+__device__ __forceinline__ uint32_t pack_cell(int i, int j, int k) {
+    return (uint32_t(i) & 1023u) | ((uint32_t(j) & 1023u) << 10) | ((uint32_t(k) & 1023u) << 20);
 }
 
 // ---- geometry (sim.cpp:9-22), rounding as the reference --------------------------------
@@ -161,9 +171,6 @@ __device__ __forceinline__ bool is_connected(const DevTopo& t, int u, int v) {
 // Local shapes (sim.cpp:24-39): a shared node, or a connected node pair.  Shapes are
 // distinct here, so "same beam" cannot occur.  The shared-node half is cheap and decides
 // most broad-phase candidates in a lattice; the connected half scans adjacency lists.
-__device__ __forceinline__ bool share_node(int2 a, int2 b) {
-    return a.x == b.x || (b.y >= 0 && a.x == b.y) || (a.y >= 0 && (a.y == b.x || (b.y >= 0 && a.y == b.y)));
-}
 __device__ __forceinline__ bool any_connected(const DevTopo& t, int2 a, int2 b) {
     const int an[2] = {a.x, a.y}, bn[2] = {b.x, b.y};
     const int na = a.y >= 0 ? 2 : 1, nb = b.y >= 0 ? 2 : 1;
@@ -200,11 +207,51 @@ __device__ __noinline__ PairHit narrow_phase(const DevTopo& t, const PhysParams&
     return h;
 }
 
+// ---- candidate-list reuse -------------------------------------------------------------------
+// The list built with boxes inflated by `skin` holds every pair whose boxes overlap at any
+// state where no node has moved more than skin (per axis) from its position at the build:
+// each current box lies inside the inflated box of the build.  flags[1] = rebuild now.
+// A node's displacement is bounded from its FP32 interval [lo, hi] and the stored lower end
+// of its interval at the build (one FP32 ulp wide at most), rounding upward.
+__global__ void __launch_bounds__(kBlock) k_skin_check(int N, const float4* __restrict__ xf_lo,
+                                                       const float4* __restrict__ xf_hi,
+                                                       const float4* __restrict__ xref, float skin,
+                                                       uint32_t* __restrict__ flags) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool moved = false;
+    if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
+    if (i < N && !moved) {
+        const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
+        const float d = fmaxf(fmaxf(fmaxf(__fsub_ru(h.x, r.x), __fsub_ru(r.x, l.x)),
+                                    fmaxf(__fsub_ru(h.y, r.y), __fsub_ru(r.y, l.y))),
+                              fmaxf(__fsub_ru(h.z, r.z), __fsub_ru(r.z, l.z)));
+        const float ulp = 1.2e-7f * fmaxf(fmaxf(fabsf(r.x), fabsf(r.y)), fabsf(r.z)) + 1e-30f;
+        moved = !(__fadd_ru(d, ulp) <= skin);  // also when not finite
+    }
+    if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flags + 1, 1u);
+}
+
+// After a rebuild: the build positions and the end of a forced rebuild.
+__global__ void __launch_bounds__(kBlock) k_skin_commit(int N, const float4* __restrict__ xf_lo,
+                                                        float4* __restrict__ xref, uint32_t* __restrict__ flags) {
+    if (!flags[1]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) xref[i] = xf_lo[i];
+    if (i == 0) flags[2] = 0;
+}
+
+__global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __restrict__ a,
+                                                       const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        a[k] = 0;
+}
+
 // ---- kernels -------------------------------------------------------------------------------
 // Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
 __global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
                               uint32_t* flags) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
     bool ok = true;
     long long lo[3], dim[3];
     for (int d = 0; d < 3; d++) {
@@ -239,6 +286,9 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
     for (int d = 0; d < 3; d++) {
         grid[d] = int(lo[d]);
         grid[3 + d] = int(dim[d]);
+        // box quantization: kBoxQuanta steps across the grid's extent on each axis
+        grid[10 + d] = __float_as_int(float(double(kBoxQuanta) / (double(dim[d]) * cell)));
+        grid[13 + d] = __float_as_int(float(double(lo[d]) * cell));
     }
     grid[6] = mode;
     grid[7] = ok ? 1 : 0;
@@ -248,35 +298,40 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
 // Per-shape bounding box and cell range, in single precision rounded outward: the box
 // contains the reference's double-precision box (sim.cpp:154), and cell indices are a
 // monotone function of it, so two shapes whose reference boxes overlap share a cell.
+// The pair-test record holds the box quantized to 15 bits per axis (floor minus one
+// quantum for the low side, ceil plus one for the high side, so the quantized box contains
+// the FP32 box whatever the rounding of the scaling) with a guard bit over each high
+// value, and the first cell packed as three 10-bit fields.
 __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, const float4* __restrict__ xf_lo,
                                                        const float4* __restrict__ xf_hi, const int* __restrict__ grid,
                                                        int4* __restrict__ cell_lo, int4* __restrict__ cell_hi,
-                                                       float4* __restrict__ bb_lo, float4* __restrict__ bb_hi,
-                                                       uint32_t* __restrict__ count, uint32_t* __restrict__ flags) {
+                                                       uint4* __restrict__ rec, uint32_t* __restrict__ count,
+                                                       float skin, uint32_t* __restrict__ flags) {
     const int S = t.N + t.B;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S) return;
+    if (s >= S || !flags[1]) return;
     const int2 nd = shape_nodes(t, uint32_t(s));
     const int n1 = nd.y >= 0 ? nd.y : nd.x;
     const float4 al = xf_lo[nd.x], ah = xf_hi[nd.x], bl = xf_lo[n1], bh = xf_hi[n1];
-    const float pad = s < t.N ? p.joint_padf : t.padf[s - t.N];
+    const float pad = __fadd_ru(s < t.N ? p.joint_padf : t.padf[s - t.N], skin);
     const float lo[3] = {__fsub_rd(fminf(al.x, bl.x), pad), __fsub_rd(fminf(al.y, bl.y), pad),
                          __fsub_rd(fminf(al.z, bl.z), pad)};
     const float hi[3] = {__fadd_ru(fmaxf(ah.x, bh.x), pad), __fadd_ru(fmaxf(ah.y, bh.y), pad),
                          __fadd_ru(fmaxf(ah.z, bh.z), pad)};
-    bb_lo[s] = make_float4(lo[0], lo[1], lo[2], 0.f);
-    bb_hi[s] = make_float4(hi[0], hi[1], hi[2], 0.f);
     const bool finite_box = isfinite(lo[0]) && isfinite(lo[1]) && isfinite(lo[2]) && isfinite(hi[0]) &&
                             isfinite(hi[1]) && isfinite(hi[2]);
     if (!grid[7] || !finite_box) {
         count[s] = 0;
         cell_lo[s] = make_int4(0, 0, 0, 0);
         cell_hi[s] = make_int4(-1, -1, -1, 0);
+        rec[s] = make_uint4(0, 0, 0, 0);
         if (!finite_box) atomicOr(flags, uint32_t(kNonFinite));
         return;
     }
     int c0[3], c1[3];
+    uint32_t q0[3], q1[3];
     long long n = 1;
+    bool wide = false;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const float dim = float(grid[3 + d] - 1);
@@ -284,8 +339,12 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
         c0[d] = int(fminf(fmaxf(floorf(lo[d] * p.inv_cell_f) - org, 0.f), dim));
         c1[d] = int(fminf(fmaxf(floorf(hi[d] * p.inv_cell_f) - org, 0.f), dim));
         n *= (long long)(c1[d] - c0[d] + 1);
+        wide |= c1[d] - c0[d] >= 1024;
+        const float qs = __int_as_float(grid[10 + d]), qo = __int_as_float(grid[13 + d]);
+        q0[d] = uint32_t(fminf(fmaxf(floorf((lo[d] - qo) * qs) - 1.f, 0.f), float(kBoxMax)));
+        q1[d] = uint32_t(fminf(fmaxf(ceilf((hi[d] - qo) * qs) + 1.f, 0.f), float(kBoxMax)));
     }
-    if (n > kMaxCellsPerShape) {  // the host coarsens the grid and evaluates again
+    if (n > kMaxCellsPerShape || wide) {  // the host coarsens the grid and evaluates again
         atomicOr(flags, uint32_t(kOverSpan));
         n = 0;
         c1[0] = c0[0] - 1;
@@ -293,6 +352,8 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
     count[s] = uint32_t(n);
     cell_lo[s] = make_int4(c0[0], c0[1], c0[2], 0);
     cell_hi[s] = make_int4(c1[0], c1[1], c1[2], 0);
+    rec[s] = make_uint4(q0[0] | (q0[1] << 16), (q1[0] | (q1[1] << 16)) | kGuard2, q0[2] | ((q1[2] | 0x8000u) << 16),
+                        pack_cell(c0[0], c0[1], c0[2]));
 }
 
 // Entries of shape s: bin key and rank inside the bin (bin_count counts them).
@@ -302,7 +363,7 @@ __global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ 
                                                  uint32_t* __restrict__ erank, uint32_t* __restrict__ bin_count,
                                                  uint32_t* __restrict__ flags) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S) return;
+    if (s >= S || !flags[1]) return;
     if ((long long)offset[S] > cap) {
         if (s == 0) atomicOr(flags, uint32_t(kOverEntries));
         return;
@@ -323,9 +384,9 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int S, const uint32_t* __res
                                                     const uint32_t* __restrict__ ekey,
                                                     const uint32_t* __restrict__ erank,
                                                     const uint32_t* __restrict__ bin_start,
-                                                    uint32_t* __restrict__ sorted) {
+                                                    uint32_t* __restrict__ sorted, const uint32_t* __restrict__ gate) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S || (long long)offset[S] > cap) return;
+    if (s >= S || !*gate || (long long)offset[S] > cap) return;
     for (uint32_t o = offset[s]; o < offset[s + 1]; o++) sorted[bin_start[ekey[o]] + erank[o]] = uint32_t(s);
 }
 
@@ -341,45 +402,44 @@ __device__ __forceinline__ void pair_index(int n, int p, int& i, int& j) {
     j = p - r * (2 * n - r - 1) / 2 + r + 1;
 }
 
-struct BinShape {
-    uint32_t s;
-    int lx, ly, lz;
-    float bx0, by0, bz0, bx1, by1, bz1;
+// One shape as the pair test sees it inside one bin: id with the first-cell flags in the
+// top three bits (bit d set when the shape's first cell on axis d is the bin's cell), the
+// quantized box words and the shape's nodes (a joint's node twice).
+struct PairRec {
+    uint32_t id, w0, w1, w2;
     int n0, n1;
 };
 
-__device__ __forceinline__ BinShape load_bin_shape(const DevTopo& t, uint32_t v, const int4* __restrict__ cell_lo,
-                                                   const float4* __restrict__ bb_lo, const float4* __restrict__ bb_hi) {
-    const int4 l = cell_lo[v];
-    const float4 a = bb_lo[v], z = bb_hi[v];
-    const int2 nd = shape_nodes(t, v);
-    return BinShape{v, l.x, l.y, l.z, a.x, a.y, a.z, z.x, z.y, z.z, nd.x, nd.y};
+__device__ __forceinline__ PairRec load_rec(const DevTopo& t, uint32_t s, const uint4* __restrict__ rec, uint32_t ccp) {
+    const uint4 r = rec[s];
+    const int2 nd = s < uint32_t(t.N) ? make_int2(int(s), int(s)) : t.ab[s - uint32_t(t.N)];
+    // cell spans are below 1024 per axis, so the 10-bit fields compare exactly
+    const uint32_t e = ~(r.w ^ ccp);
+    const uint32_t f = ((e & 0x3ffu) == 0x3ffu) | (((e & 0xffc00u) == 0xffc00u) << 1) |
+                       (((e & 0x3ff00000u) == 0x3ff00000u) << 2);
+    return PairRec{s | (f << kShapeBits), r.x, r.y, r.z, nd.x, nd.y};
 }
 
-// Broad-phase filter of one pair in cell cc: first common cell, AABB overlap, no shared
-// node.  Survivors become narrow-phase candidates.
-__device__ __forceinline__ bool candidate(const BinShape& A, const BinShape& B, int3 cc) {
-    return max(A.lx, B.lx) == cc.x && max(A.ly, B.ly) == cc.y && max(A.lz, B.lz) == cc.z &&
-           !(A.bx0 > B.bx1 || B.bx0 > A.bx1 || A.by0 > B.by1 || B.by0 > A.by1 || A.bz0 > B.bz1 || B.bz0 > A.bz1) &&
-           !share_node(make_int2(A.n0, A.n1), make_int2(B.n0, B.n1));
+// Broad-phase filter of one pair in its bin: the bin is the first common cell (the OR of
+// the flags has all three bits), the quantized boxes overlap, and no node is shared.
+// Box overlap by guarded subtraction: with a guard bit over each 15-bit high value,
+// (hi | guard) - lo keeps the guard exactly when hi >= lo, two axes per word.
+__device__ __forceinline__ bool pair_test(const PairRec& A, const PairRec& B) {
+    const bool first = (A.id | B.id) >= 0xe0000000u;
+    const uint32_t d1 = B.w1 - A.w0, d2 = A.w1 - B.w0;
+    const uint32_t d3 = __byte_perm(B.w2, A.w2, 0x7632) - __byte_perm(A.w2, B.w2, 0x5410);
+    const bool box = (d1 & d2 & d3 & kGuard2) == kGuard2;
+    const bool share = A.n0 == B.n0 || A.n0 == B.n1 || A.n1 == B.n0 || A.n1 == B.n1;
+    return first && box && !share;
 }
 
-__device__ __forceinline__ BinShape shfl_shape(const BinShape& v, int src) {
-    BinShape o;
-    o.s = __shfl_sync(0xffffffffu, v.s, src);
-    o.lx = __shfl_sync(0xffffffffu, v.lx, src);
-    o.ly = __shfl_sync(0xffffffffu, v.ly, src);
-    o.lz = __shfl_sync(0xffffffffu, v.lz, src);
-    o.bx0 = __shfl_sync(0xffffffffu, v.bx0, src);
-    o.by0 = __shfl_sync(0xffffffffu, v.by0, src);
-    o.bz0 = __shfl_sync(0xffffffffu, v.bz0, src);
-    o.bx1 = __shfl_sync(0xffffffffu, v.bx1, src);
-    o.by1 = __shfl_sync(0xffffffffu, v.by1, src);
-    o.bz1 = __shfl_sync(0xffffffffu, v.bz1, src);
-    o.n0 = __shfl_sync(0xffffffffu, v.n0, src);
-    o.n1 = __shfl_sync(0xffffffffu, v.n1, src);
-    return o;
+__device__ __forceinline__ PairRec shfl_rec(const PairRec& v, int src) {
+    return PairRec{__shfl_sync(0xffffffffu, v.id, src), __shfl_sync(0xffffffffu, v.w0, src),
+                   __shfl_sync(0xffffffffu, v.w1, src), __shfl_sync(0xffffffffu, v.w2, src),
+                   __shfl_sync(0xffffffffu, v.n0, src), __shfl_sync(0xffffffffu, v.n1, src)};
 }
+
+constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 
 // Candidate pairs of every occupied bin.  Warp w of the fixed grid takes the occupied bins
 // occ[w], occ[w + W], ... in order and appends their candidate pairs (lower shape, higher
@@ -390,20 +450,20 @@ __device__ __forceinline__ BinShape shfl_shape(const BinShape& v, int src) {
 //   n <= 32  the bin's shapes are sorted across the warp's lanes (bitonic, by shape id)
 //            and every unordered pair is visited by rotation: in round k lane i meets
 //            lane (i + k) mod n, k = 1 .. n/2 (the last round of an even n only from the
-//            lower half), the partner's data arriving by register shuffles;
-//   n <= 64  the sorted shapes are staged in shared memory and the pairs enumerated by
+//            lower half), the partner's record arriving by six register shuffles;
+//   n <= 64  the sorted records are staged in shared memory and the pairs enumerated by
 //            index;
-//   larger   sorted through a scratch copy, pairs read from global memory.
+//   larger   sorted through a scratch copy, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count,
                                                       const uint32_t* __restrict__ bin_start,
                                                       const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
                                                       const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
-                                                      const int4* __restrict__ cell_lo, const float4* __restrict__ bb_lo,
-                                                      const float4* __restrict__ bb_hi, int region,
+                                                      const uint4* __restrict__ rec, int region,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
                                                       uint32_t* __restrict__ flags) {
-    __shared__ BinShape sh[kPairWarps][kWarpCap];
+    __shared__ PairRec sh[kPairWarps][kWarpCap];
+    if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
     const long long nocc = *nocc_p;
@@ -415,15 +475,16 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         const unsigned m = __ballot_sync(0xffffffffu, hit);
         if (hit) {
             const uint32_t pos = out + __popc(m & below);
-            if (pos < uint32_t(region)) mine[pos] = make_uint2(sa, sb);
+            if (pos < uint32_t(region)) mine[pos] = make_uint2(min(sa, sb), max(sa, sb));
         }
         out += __popc(m);
     };
-    for (long long j = gw; j < nocc; j += warps) {
-        const uint32_t b = occ[j];
+    for (long long jb = gw; jb < nocc; jb += warps) {
+        const uint32_t b = occ[jb];
         const int n = int(bin_count[b]);
         const uint32_t start = bin_start[b];
         const int3 cc = cell_of(grid, b);
+        const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
         if (n <= 32) {
             uint32_t v = lane < n ? sorted[start + lane] : 0xffffffffu;
             for (int k = 2; k <= 32; k <<= 1)  // bitonic sort, ascending
@@ -432,15 +493,15 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                     const bool up = (lane & k) == 0, lower = (lane & j) == 0;
                     v = (lower == up) ? min(v, o) : max(v, o);
                 }
-            BinShape me{};
-            if (lane < n) me = load_bin_shape(t, v, cell_lo, bb_lo, bb_hi);
+            PairRec me{};
+            if (lane < n) me = load_rec(t, v, rec, ccp);
             const int half = n >> 1;
+            int src = lane;
             for (int k = 1; k <= half; k++) {
-                const int src = lane < n ? (lane + k < n ? lane + k : lane + k - n) : lane;
-                const BinShape o = shfl_shape(me, src);
+                src = src + 1 < n ? src + 1 : 0;  // (lane + k) mod n for lanes below n
+                const PairRec o = shfl_rec(me, lane < n ? src : lane);
                 const bool active = lane < n && !((n & 1) == 0 && k == half && lane >= half);
-                const bool hit = active && candidate(me, o, cc);
-                emit(hit, min(me.s, o.s), max(me.s, o.s));
+                emit(active && pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
             }
         } else if (n <= kWarpCap) {
             const uint32_t v0 = sorted[start + lane];
@@ -452,8 +513,8 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                 r1 += (u0 < v1) + (u1 < v1);
             }
             __syncwarp();
-            sh[w][r0] = load_bin_shape(t, v0, cell_lo, bb_lo, bb_hi);
-            if (v1 != 0xffffffffu) sh[w][r1] = load_bin_shape(t, v1, cell_lo, bb_lo, bb_hi);
+            sh[w][r0] = load_rec(t, v0, rec, ccp);
+            if (v1 != 0xffffffffu) sh[w][r1] = load_rec(t, v1, rec, ccp);
             __syncwarp();
             const int P = n * (n - 1) / 2;
             for (int base = 0; base < P; base += 32) {
@@ -463,15 +524,16 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                 if (pidx < P) {
                     int i, j;
                     pair_index(n, pidx, i, j);
-                    hit = candidate(sh[w][i], sh[w][j], cc);
-                    sa = sh[w][i].s;
-                    sb = sh[w][j].s;
+                    const PairRec A = sh[w][i], B = sh[w][j];
+                    hit = pair_test(A, B);
+                    sa = A.id & kIdMask;
+                    sb = B.id & kIdMask;
                 }
                 emit(hit, sa, sb);
             }
             __syncwarp();
         } else {
-            // large bin: ascending order through a scratch copy, pairs from global memory
+            // large bin: ascending order through a scratch copy, records from global memory
             for (int e = lane; e < n; e += 32) {
                 const uint32_t v = sorted[start + e];
                 int r = 0;
@@ -492,11 +554,11 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                         row_end += n - 1 - i;
                     }
                     const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                    const BinShape A = load_bin_shape(t, sorted2[start + i], cell_lo, bb_lo, bb_hi);
-                    const BinShape B = load_bin_shape(t, sorted2[start + j], cell_lo, bb_lo, bb_hi);
-                    hit = candidate(A, B, cc);
-                    sa = A.s;
-                    sb = B.s;
+                    const PairRec A = load_rec(t, sorted2[start + i], rec, ccp);
+                    const PairRec B = load_rec(t, sorted2[start + j], rec, ccp);
+                    hit = pair_test(A, B);
+                    sa = A.id & kIdMask;
+                    sb = B.id & kIdMask;
                 }
                 emit(hit, sa, sb);
             }
@@ -511,26 +573,88 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
 
 // Occupied bins (two or more entries), in bin order: flags, then a scan, then this.
 __global__ void __launch_bounds__(kBlock) k_occ_flags(long long nb_cap, const int* __restrict__ grid,
-                                                      const uint32_t* __restrict__ bin_count, uint32_t* __restrict__ f) {
+                                                      const uint32_t* __restrict__ bin_count, uint32_t* __restrict__ f,
+                                                      const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
     const long long nb = grid[8];
     for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
         f[b] = (b < nb && bin_count[b] >= 2) ? 1u : 0u;
 }
 __global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const uint32_t* __restrict__ f,
-                                                      const uint32_t* __restrict__ off, uint32_t* __restrict__ occ) {
+                                                      const uint32_t* __restrict__ off, uint32_t* __restrict__ occ,
+                                                      const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
     for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
         if (f[b]) occ[off[b]] = uint32_t(b);
 }
 
 constexpr int kContactPartBlocks = 128;
 
+// Certified single-precision rejection of a candidate pair: true when the two shapes are
+// certainly farther apart than pad_a + pad_b (>= the reference's target ra + rb + margin),
+// so the reference's test dist < target fails and the pair is no contact.
+//
+// For any unit vector n, the distance between segments p1 + s d1 and p2 + t d2 (s, t in
+// [0, 1]) is at least  L(n) = n.(p1 - p2) + min(0, n.d1) - max(0, n.d2):  n.(P - Q) <= |P - Q|
+// and the minimum of the linear form over the parameter square is at a corner.  n is the
+// unit direction between approximate closest points (FP32, the clamped solution of
+// sim.cpp:9-18), which makes the bound nearly tight.  L is evaluated from FP32 endpoints
+// rounded down (|error| <= 2^-23 X per coordinate, X the largest endpoint coordinate); the
+// rounding of the differences, the three dot products and the sums adds at most about
+// 4e-6 X in total, bounded here by 3e-5 X + 1e-9 m, and |n| = 1 up to 1e-6.  A pair that
+// cannot be certified (touching segments, non-finite data) goes to the exact test.
+__device__ __forceinline__ bool certainly_apart(const DevTopo& t, const PhysParams& p, const float4* __restrict__ xf,
+                                                uint32_t sa, uint32_t sb) {
+    const int2 na = sa < uint32_t(t.N) ? make_int2(int(sa), int(sa)) : t.ab[sa - uint32_t(t.N)];
+    const int2 nb = sb < uint32_t(t.N) ? make_int2(int(sb), int(sb)) : t.ab[sb - uint32_t(t.N)];
+    const float pa = sa < uint32_t(t.N) ? p.joint_padf : t.padf[sa - uint32_t(t.N)];
+    const float pb = sb < uint32_t(t.N) ? p.joint_padf : t.padf[sb - uint32_t(t.N)];
+    const float4 a0 = xf[na.x], a1 = xf[na.y], b0 = xf[nb.x], b1 = xf[nb.y];
+    const float X = fmaxf(fmaxf(fmaxf(fabsf(a0.x), fabsf(a0.y)), fmaxf(fabsf(a0.z), fabsf(a1.x))),
+                          fmaxf(fmaxf(fabsf(a1.y), fabsf(a1.z)), fmaxf(fmaxf(fabsf(b0.x), fabsf(b0.y)),
+                                                                     fmaxf(fmaxf(fabsf(b0.z), fabsf(b1.x)),
+                                                                           fmaxf(fabsf(b1.y), fabsf(b1.z))))));
+    const float wx = a0.x - b0.x, wy = a0.y - b0.y, wz = a0.z - b0.z;
+    const float ux = a1.x - a0.x, uy = a1.y - a0.y, uz = a1.z - a0.z;
+    const float vx = b1.x - b0.x, vy = b1.y - b0.y, vz = b1.z - b0.z;
+    const float a = ux * ux + uy * uy + uz * uz, e = vx * vx + vy * vy + vz * vz;
+    const float f = vx * wx + vy * wy + vz * wz, c = ux * wx + uy * wy + uz * wz;
+    float s = 0.f, tt = 0.f;
+    if (a > 1e-20f && e > 1e-20f) {
+        const float b = ux * vx + uy * vy + uz * vz, den = a * e - b * b;
+        s = den > 1e-12f * a * e ? __saturatef(__fdividef(b * f - c * e, den)) : 0.f;
+        tt = __fdividef(b * s + f, e);
+        if (tt < 0.f) {
+            tt = 0.f;
+            s = __saturatef(__fdividef(-c, a));
+        } else if (tt > 1.f) {
+            tt = 1.f;
+            s = __saturatef(__fdividef(b - c, a));
+        }
+    } else if (a > 1e-20f) {
+        s = __saturatef(__fdividef(-c, a));
+    } else if (e > 1e-20f) {
+        tt = __saturatef(__fdividef(f, e));
+    }
+    const float nx = wx + ux * s - vx * tt, ny = wy + uy * s - vy * tt, nz = wz + uz * s - vz * tt;
+    const float nn = nx * nx + ny * ny + nz * nz;
+    if (!(nn > 1e-14f)) return false;  // closer than 1e-7 m (or not finite): no certificate
+    const float inv = rsqrtf(nn);
+    const float mx = nx * inv, my = ny * inv, mz = nz * inv;
+    const float nu = mx * ux + my * uy + mz * uz, nv = mx * vx + my * vy + mz * vz;
+    const float L = (mx * wx + my * wy + mz * wz) + fminf(0.f, nu) - fmaxf(0.f, nv);
+    return L * 0.999999f - (3e-5f * X + 1e-9f) > (pa + pb) * 1.000001f;
+}
+
 // Narrow phase over the candidate regions, one warp per region (the region's owner in
 // k_bin_pairs).  Pass 0: test every candidate, keep one hit bit per candidate and the hit
 // count per region.  Pass 1 (after a scan of the counts): test the hits again and write
 // them as contacts, in region and candidate order.
+template <int pass>
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                   int region, const uint2* __restrict__ cand,
-                                                   const uint32_t* __restrict__ wcount, int pass,
+                                                   const float4* __restrict__ xf, int region,
+                                                   const uint2* __restrict__ cand,
+                                                   const uint32_t* __restrict__ wcount,
                                                    uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
                                                    const uint32_t* __restrict__ hoff, ContactBufs c) {
     const int lane = threadIdx.x & 31;
@@ -539,10 +663,10 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
     const uint2* mine = cand + gw * region;
     uint32_t* bits = hitbits + gw * (region / 32);
     const unsigned below = (1u << lane) - 1u;
-    uint32_t pos = pass ? hoff[gw] : 0;
+    uint32_t pos = pass == 1 ? hoff[gw] : 0;
     for (uint32_t base = 0; base < nc; base += 32) {
         const uint32_t i = base + lane;
-        if (pass) {
+        if constexpr (pass == 1) {
             const unsigned m = bits[base / 32];
             if (m & (1u << lane)) {
                 const uint2 q = mine[i];
@@ -564,39 +688,39 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
             bool hit = false;
             if (i < nc) {
                 const uint2 q = mine[i];
-                hit = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
+                hit = !certainly_apart(t, p, xf, q.x, q.y) &&
+                      narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
             if (lane == 0) bits[base / 32] = m;
             pos += __popc(m);
         }
     }
-    if (!pass && lane == 0) hcount[gw] = pos;
+    if (pass == 0 && lane == 0) hcount[gw] = pos;
 }
 
-// Fixed-partition reduction over the contact list: energy, max penetration, count.
-__global__ void __launch_bounds__(kBlock) k_contact_reduce(const uint32_t* __restrict__ total, long long cap, double k,
+// Fixed-partition reduction over the contact list: max penetration and count (the energy
+// is summed per node by the gather, in an order independent of the list).
+__global__ void __launch_bounds__(kBlock) k_contact_reduce(const uint32_t* __restrict__ total, long long cap,
                                                            const double* __restrict__ pen, double* __restrict__ part,
                                                            uint32_t* flags) {
-    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ double sm[kBlock / 32];
     __shared__ double smx[kBlock / 32];
     const long long nc_all = *total;
     if (nc_all > cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, uint32_t(kOverContacts));
     const long long nc = nc_all > cap ? cap : nc_all;
-    double acc[2] = {0, 0};
+    double acc[1] = {0};
     double m = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
-        const double pp = pen[i];
-        acc[0] += .5 * k * pp * pp;
-        acc[1] += 1;
-        m = fmax(m, pp);
+        acc[0] += 1;
+        m = fmax(m, pen[i]);
     }
-    block_sum<2>(acc, sm);
+    block_sum<1>(acc, sm);
     m = block_max(m, smx);
     if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = acc[0];
+        part[3 * blockIdx.x] = 0;
         part[3 * blockIdx.x + 1] = m;
-        part[3 * blockIdx.x + 2] = acc[1];
+        part[3 * blockIdx.x + 2] = acc[0];
     }
 }
 
@@ -636,36 +760,42 @@ int contact_pair_blocks(long long shapes) {
 }
 
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                     cudaStream_t s) {
+                     float skin, cudaStream_t s) {
     const int S = t.N + t.B;
-    cudaMemsetAsync(c.flags, 0, sizeof(uint32_t), s);
-    cudaMemsetAsync(c.bin_count, 0, size_t(c.bin_cap + 1) * sizeof(uint32_t), s);
-    (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad, p.broad_cell, c.bin_cap, c.grid, c.flags), note_launches(1));
-    (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.bb_lo,
-                                                 c.bb_hi, c.count, c.flags), note_launches(1));
-    exclusive_scan_u32(c.count, c.offset, S, c.scan_tmp, s);
+    const uint32_t* gate = c.flags + 1;
+    cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
+    (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
+    // candidate list (only when rebuilding)
+    (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
+    (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad + double(skin > 0.f ? skin : 0.f), p.broad_cell, c.bin_cap, c.grid,
+                                    c.flags),
+     note_launches(1));
+    (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
+                                                 c.count, skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
+    exclusive_scan_u32(c.count, c.offset, S, c.scan_tmp, s, gate);
     (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.offset, c.entry_cap, c.ekey, c.erank,
                                            c.bin_count, c.flags), note_launches(1));
-    exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s);
-    (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted),
+    exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s, gate);
+    (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted, gate),
      note_launches(1));
     // occupied bins, then candidates into per-warp regions
-    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount), note_launches(1));
-    exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s);
-    (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ), note_launches(1));
+    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, gate), note_launches(1));
+    exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s, gate);
+    (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
     const uint32_t* nocc = c.boffset + c.bin_cap;
     const int W = c.pair_blocks * kPairWarps;
     (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted, c.sorted2,
-                                                c.cell_lo, c.bb_lo, c.bb_hi, c.region, c.cand, c.wcount, c.flags),
+                                                c.rec, c.region, c.cand, c.wcount, c.flags),
      note_launches(1));
-    // narrow phase: hit bits and counts per region, scan, contacts
-    (k_narrow<<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.region, c.cand, c.wcount, 0, c.hitbits, c.hcount,
+    (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
+    // narrow phase over the candidate list: hit bits and counts per region, scan, contacts
+    (k_narrow<0><<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, c.cand, c.wcount, c.hitbits, c.hcount,
                                                c.hoff, c), note_launches(1));
     exclusive_scan_u32(c.hcount, c.hoff, W, c.scan_tmp, s);
-    (k_narrow<<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, c.region, c.cand, c.wcount, 1, c.hitbits, c.hcount,
+    (k_narrow<1><<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, c.cand, c.wcount, c.hitbits, c.hcount,
                                                c.hoff, c), note_launches(1));
     const uint32_t* total = c.hoff + W;
-    (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, p.contact_k, c.c_pen, c.part, c.flags),
+    (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, c.c_pen, c.part, c.flags),
      note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);

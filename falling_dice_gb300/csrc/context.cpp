@@ -154,18 +154,19 @@ struct mcg_ctx {
 
     // ---- contact buffers ---------------------------------------------------------------
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
+    float contact_skin = 0;  // candidate-list reuse distance (m); 0 rebuilds every evaluation
     void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, int region) {
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
         c.cell_lo = contact_mem.get<int4>(size_t(S));
         c.cell_hi = contact_mem.get<int4>(size_t(S));
-        c.bb_lo = contact_mem.get<float4>(size_t(S));
-        c.bb_hi = contact_mem.get<float4>(size_t(S));
+        c.rec = contact_mem.get<uint4>(size_t(S));
         c.count = contact_mem.get<uint32_t>(size_t(S + 1));
         c.offset = contact_mem.get<uint32_t>(size_t(S + 1));
         c.grid = contact_mem.get<int>(16);
         c.flags = contact_mem.get<uint32_t>(4);
+        c.xref = contact_mem.get<float4>(size_t(std::max(N, 1)));
         c.entry_cap = entry_cap;
         c.ekey = contact_mem.get<uint32_t>(size_t(entry_cap));
         c.erank = contact_mem.get<uint32_t>(size_t(entry_cap));
@@ -200,6 +201,7 @@ struct mcg_ctx {
         c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
 
@@ -250,7 +252,7 @@ struct mcg_ctx {
         mark(2);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
-            launch_contacts(topo, p, ev, cb, rmax + cfg.contact_margin, stream);
+            launch_contacts(topo, p, ev, cb, rmax + cfg.contact_margin, contact_skin, stream);
             cptr = &cb;
         }
         mark(3);
@@ -858,7 +860,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         e.slotB = V.get<double>(6 * size_t(B));
         e.part_state = V.get<double>(9 * size_t(nb_nodes(N)));
         e.part_beam = V.get<double>(3 * size_t(nb_beams(std::max(B, 1))));
-        e.part_node = V.get<double>(5 * size_t(nb_nodes(N)));
+        e.part_node = V.get<double>(kNodeParts * size_t(nb_nodes(N)));
         e.cen = V.get<double>(9);
         e.out = V.get<EvalOut>(1);
         e.trial_next = V.get<double>(7 * size_t(B));
@@ -883,6 +885,7 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         // contact buffers: a first guess, grown on demand
         const long long S = (long long)N + B;
         c->broad_cell = P.broad_cell;
+        c->contact_skin = float(0.125 * cf.cell_size);
         {
             // bins: the Morton range of the rest-state extent, with room to grow
             double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
@@ -1063,7 +1066,7 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         else launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
-            launch_contacts(c->topo, p, c->ev, fixed, c->rmax + c->cfg.contact_margin, s);
+            launch_contacts(c->topo, p, c->ev, fixed, c->rmax + c->cfg.contact_margin, 0.f, s);  // always rebuilds
             cptr = &fixed;
         }
         if (c->mixed) launch_gather_mixed(c->topo, p, cptr, c->d_grad, c->ev, s);
@@ -1171,6 +1174,16 @@ int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, in
         const long long W = (long long)contact_pair_blocks((long long)c->N + c->B) * 8;
         c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
                           std::max<long long>(bins, lo), int(std::min<long long>((candidates + W - 1) / W, 1LL << 26)));
+    });
+}
+
+int mcg_set_contact_skin(mcg_ctx* c, double skin) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!(skin >= 0) || skin > 1e3) throw Fail(MCG_ERR_INVALID, "skin must be a distance >= 0 (m)");
+        c->contact_skin = float(skin);
+        // the stored list was built for the previous skin
+        ck(cudaMemsetAsync(c->cb.flags + 2, 1, 1, c->stream), "memset");
     });
 }
 

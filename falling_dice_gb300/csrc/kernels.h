@@ -75,12 +75,14 @@ struct ContactBufs {
     // per shape (S = N + B)
     int4* cell_lo;          // [S] first cell (i, j, k) relative to the grid origin
     int4* cell_hi;          // [S] last cell
-    float4* bb_lo;          // [S] fp32 AABB, rounded outward
-    float4* bb_hi;
+    uint4* rec;             // [S] pair-test record: quantized AABB (3 words), packed first cell
     uint32_t* count;        // [S+1] cells per shape
     uint32_t* offset;       // [S+1] exclusive scan of count
-    int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed
-    uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation
+    int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed;
+                            //       box quantization scale x,y,z and origin x,y,z (float bits)
+    uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation, [1] candidate list
+                            //      rebuilt by this evaluation, [2] rebuild forced by the host
+    float4* xref;           // [N] node positions (FP32, rounded down) when the list was built
     // entries in emission order (shape-major), then counting-sorted by bin
     long long entry_cap;
     uint32_t* ekey;         // [entry_cap] bin of the entry
@@ -114,10 +116,12 @@ struct ContactBufs {
     uint32_t* n_start;      // [N+1]
     uint32_t* n_cursor;     // [N]
     uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot)
-    double* part;           // [3 * contact_part_blocks] energy, max penetration, count
+    double* part;           // [3 * contact_part_blocks] (unused), max penetration, count
     void* scan_tmp;
     size_t scan_tmp_bytes;
 };
+
+constexpr int kNodeParts = 6;  // per node block: gravity E, platen E, reaction, max pen, platen contacts, self-contact E
 
 struct EvalBufs {
     double4_32a* x;             // [N]
@@ -129,7 +133,7 @@ struct EvalBufs {
     double* slotB;          // [6B] (+F, Gb) per beam, added to node b
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
     double* part_beam;      // [3 * nb_beams]
-    double* part_node;      // [5 * nb_nodes]
+    double* part_node;      // [kNodeParts * nb_nodes]
     double* cen;            // [9] mean, min, max of the node positions
     EvalOut* out;
     double* trial_next;     // [7B] SoA
@@ -203,13 +207,18 @@ int contact_part_blocks(long long contact_cap);
 // Blocks of the pair / narrow-phase grid for a model of `shapes` shapes (8 warps each).
 int contact_pair_blocks(long long shapes);
 // The whole broad/narrow phase: grid, entries, bins, pairs, contact list, node lists.
+// The candidate list is rebuilt only when a node has moved more than skin (m, per axis)
+// since the last build, or the host forced it (flags[2]); skin <= 0 rebuilds every time.
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                     cudaStream_t s);
+                     float skin, cudaStream_t s);
 
 // ---- scan (sort.cu) -----------------------------------------------------------------------
 size_t scan_tmp_bytes(long long n);
 // Exclusive scan of n uint32 values; out[n] receives the total.
-void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s);
+// Exclusive scan of n counts into out[0..n] (out[n] = total).  With a gate, every kernel
+// returns at once when *gate is 0 (the output keeps its previous contents).
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s,
+                        const uint32_t* gate = nullptr);
 
 // ---- L-BFGS vector kernels (lbfgs.cu) ----------------------------------------------------
 size_t lbfgs_part_doubles();

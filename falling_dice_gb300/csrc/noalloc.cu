@@ -80,12 +80,12 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c = ContactBufs{};
     c.cell_lo = reinterpret_cast<int4*>(take(size_t(S) * sizeof(int4)));
     c.cell_hi = reinterpret_cast<int4*>(take(size_t(S) * sizeof(int4)));
-    c.bb_lo = reinterpret_cast<float4*>(take(size_t(S) * sizeof(float4)));
-    c.bb_hi = reinterpret_cast<float4*>(take(size_t(S) * sizeof(float4)));
+    c.rec = reinterpret_cast<uint4*>(take(size_t(S) * sizeof(uint4)));
     c.count = reinterpret_cast<uint32_t*>(take(size_t(S + 1) * 4));
     c.offset = reinterpret_cast<uint32_t*>(take(size_t(S + 1) * 4));
     c.grid = reinterpret_cast<int*>(take(16 * sizeof(int)));
     c.flags = reinterpret_cast<uint32_t*>(take(4 * 4));
+    c.xref = reinterpret_cast<float4*>(take(size_t(N > 0 ? N : 1) * sizeof(float4)));
     c.entry_cap = kNoAllocEntries;
     c.ekey = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
     c.erank = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));

@@ -281,6 +281,13 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
     }
 }
 
+// Sort key of a per-node contact item (contact index << 2 | slot): the contact's shape pair
+// and the slot (shapes are below 2^29).  Two items of one node never share a key.
+__device__ __forceinline__ unsigned long long contact_item_key(const ContactBufs& c, uint32_t item) {
+    const uint32_t ci = item >> 2;
+    return ((unsigned long long)c.c_a[ci] << 31) | ((unsigned long long)c.c_b[ci] << 2) | (item & 3u);
+}
+
 // Contribution of one contact slot to its node (MC/src/sim.cpp:23 addShapeGradient):
 // slots 0/1 are shape a's ends, 2/3 shape b's; capsule ends split the force (1-u, u).
 __device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const PhysParams& p, int N,
@@ -295,6 +302,17 @@ __device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const Phy
     if (!capsule) return v;
     const double u = side_b ? c.c_t[ci] : c.c_s[ci];
     return (slot & 1u) ? v * u : v * (1 - u);
+}
+
+// One item of a node's contact list: its force, and for slot 0 (the first node of the
+// lower shape, present for every contact) the contact's penalty energy (sim.cpp:163).
+__device__ __forceinline__ void add_contact_item(const ContactBufs& c, const PhysParams& p, int N, uint32_t item,
+                                                 d3& gx, double& energy) {
+    gx = gx + contact_slot_force(c, p, N, item);
+    if ((item & 3u) == 0) {
+        const double pen = c.c_pen[item >> 2];
+        energy += .5 * p.contact_k * pen * pen;
+    }
 }
 
 // ---- per-node gather: the scatter of MC/src/sim.cpp:139-172, as a deterministic CSR sum ---
@@ -330,11 +348,11 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
 template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
-    __shared__ double sm[4 * (kBlock / 32)];
+    __shared__ double sm[5 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int N = t.N;
-    double acc[4] = {0, 0, 0, 0};  // gravity energy, platen energy, reaction, platen contacts
+    double acc[5] = {0, 0, 0, 0, 0};  // gravity E, platen E, reaction, platen contacts, self-contact E
     double pen_max = 0;
     if (i < N) {
         d3 gx{0, 0, 0}, gr{0, 0, 0};
@@ -347,29 +365,46 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         // centering (sim.cpp:143)
         gx.x += p.centering * e.cen[0] / double(N);
         gx.z += p.centering * e.cen[2] / double(N);
-        // self-contact forces on this node, in ascending (contact, slot) order
+        // self-contact forces on this node in ascending (lower shape, higher shape, slot)
+        // order, and the self-contact energy of each contact on the first node of its lower
+        // shape: both independent of the order of the contact list
         if (use_contacts) {
             const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
             if (cnt <= 16) {
+                unsigned long long keys[16];
                 uint32_t items[16];
-                for (uint32_t k = 0; k < cnt; k++) items[k] = c.n_items[s0 + k];
-                for (uint32_t a = 1; a < cnt; a++) {  // insertion sort
-                    const uint32_t v = items[a];
-                    uint32_t q = a;
-                    while (q > 0 && items[q - 1] > v) { items[q] = items[q - 1]; q--; }
-                    items[q] = v;
+                for (uint32_t k = 0; k < cnt; k++) {
+                    items[k] = c.n_items[s0 + k];
+                    keys[k] = contact_item_key(c, items[k]);
                 }
-                for (uint32_t k = 0; k < cnt; k++) gx = gx + contact_slot_force(c, p, N, items[k]);
+                for (uint32_t a = 1; a < cnt; a++) {  // insertion sort by key
+                    const unsigned long long v = keys[a];
+                    const uint32_t it = items[a];
+                    uint32_t q = a;
+                    while (q > 0 && keys[q - 1] > v) {
+                        keys[q] = keys[q - 1];
+                        items[q] = items[q - 1];
+                        q--;
+                    }
+                    keys[q] = v;
+                    items[q] = it;
+                }
+                for (uint32_t k = 0; k < cnt; k++) add_contact_item(c, p, N, items[k], gx, acc[4]);
             } else {
                 // long list: repeated minimum selection keeps the same order without storage
-                long long last = -1;
+                unsigned long long last = 0;
                 for (uint32_t k = 0; k < cnt; k++) {
-                    uint32_t best = 0xffffffffu;
+                    unsigned long long best = ~0ull;
+                    uint32_t best_item = 0;
                     for (uint32_t q = 0; q < cnt; q++) {
-                        const uint32_t v = c.n_items[s0 + q];
-                        if ((long long)v > last && v < best) best = v;
+                        const uint32_t it = c.n_items[s0 + q];
+                        const unsigned long long v = contact_item_key(c, it);
+                        if ((k == 0 || v > last) && v < best) {
+                            best = v;
+                            best_item = it;
+                        }
                     }
-                    gx = gx + contact_slot_force(c, p, N, best);
+                    add_contact_item(c, p, N, best_item, gx, acc[4]);
                     last = best;
                 }
             }
@@ -404,11 +439,11 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         g[4] = li[4] ? 0.0 : gr.y;
         g[5] = li[5] ? 0.0 : gr.z;
     }
-    block_sum<4>(acc, sm);
+    block_sum<5>(acc, sm);
     pen_max = block_max(pen_max, smx);
     if (threadIdx.x == 0) {
-        double* q = e.part_node + 5 * size_t(blockIdx.x);
-        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = pen_max; q[4] = acc[3];
+        double* q = e.part_node + kNodeParts * size_t(blockIdx.x);
+        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = pen_max; q[4] = acc[3]; q[5] = acc[4];
     }
 }
 
@@ -428,12 +463,13 @@ __global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, 
         acc[0] += pbeam[3 * k]; acc[1] += pbeam[3 * k + 1]; acc[2] += pbeam[3 * k + 2];
     }
     for (int k = threadIdx.x; k < nbn; k += blockDim.x) {
-        acc[3] += pnode[5 * k]; acc[4] += pnode[5 * k + 1]; acc[5] += pnode[5 * k + 2];
-        pmax = fmax(pmax, pnode[5 * k + 3]);
-        cacc[1] += pnode[5 * k + 4];
+        const double* q = pnode + kNodeParts * size_t(k);
+        acc[3] += q[0]; acc[4] += q[1]; acc[5] += q[2];
+        pmax = fmax(pmax, q[3]);
+        cacc[1] += q[4];
+        cacc[0] += q[5];
     }
     for (int k = threadIdx.x; k < ncp; k += blockDim.x) {
-        cacc[0] += pcont[3 * k];
         pmax = fmax(pmax, pcont[3 * k + 1]);
         cacc[2] += pcont[3 * k + 2];
     }

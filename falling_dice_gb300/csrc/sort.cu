@@ -37,7 +37,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 }
 
 __global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t* __restrict__ in, long long n,
-                                                        uint32_t* __restrict__ part) {
+                                                        uint32_t* __restrict__ part, const uint32_t* __restrict__ gate) {
+    if (gate && !*gate) return;
     __shared__ uint32_t sm[kBlock / 32];
     const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t s = 0;
@@ -50,7 +51,9 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t* __restri
 }
 
 // One block scans the tile partials in chunks, carrying the running total.
-__global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long long np, uint32_t* total_out) {
+__global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long long np, uint32_t* total_out,
+                                                          const uint32_t* __restrict__ gate) {
+    if (gate && !*gate) return;
     __shared__ uint32_t sm[kBlock / 32];
     uint32_t carry = 0;
     for (long long c = 0; c < np; c += kTile) {
@@ -73,7 +76,9 @@ __global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long l
 
 __global__ void __launch_bounds__(kBlock) k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                       long long n, const uint32_t* __restrict__ part,
-                                                      const uint32_t* __restrict__ total) {
+                                                      const uint32_t* __restrict__ total,
+                                                      const uint32_t* __restrict__ gate) {
+    if (gate && !*gate) return;
     __shared__ uint32_t sm[kBlock / 32];
     const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t v[kItems], s = 0;
@@ -96,17 +101,18 @@ size_t scan_tmp_bytes(long long n) {
     return size_t(np + 4) * sizeof(uint32_t);
 }
 
-void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s) {
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s,
+                        const uint32_t* gate) {
     uint32_t* part = static_cast<uint32_t*>(tmp);
     const long long np = (n + kTile - 1) / kTile;
     uint32_t* total = part + np + 1;
     if (n <= 0) {
-        cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+        if (!gate) cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
         return;
     }
-    (k_scan_reduce<<<unsigned(np), kBlock, 0, s>>>(in, n, part), note_launches(1));
-    (k_scan_partials<<<1, kBlock, 0, s>>>(part, np, total), note_launches(1));
-    (k_scan_down<<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total), note_launches(1));
+    (k_scan_reduce<<<unsigned(np), kBlock, 0, s>>>(in, n, part, gate), note_launches(1));
+    (k_scan_partials<<<1, kBlock, 0, s>>>(part, np, total, gate), note_launches(1));
+    (k_scan_down<<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate), note_launches(1));
 }
 
 }  // namespace mcg

@@ -232,6 +232,16 @@ int64_t mcg_launch_count(const mcg_ctx* ctx);
 int mcg_set_contact_capacity(mcg_ctx* ctx, int64_t entries, int64_t candidates, int64_t contacts,
                              int64_t bins);
 
+/* Reuse of the self-contact candidate list (no reference counterpart; results are
+ * unchanged).  The list of shape pairs whose boxes may overlap is built with boxes grown
+ * by `skin` metres and rebuilt only when some node has moved more than `skin` along an
+ * axis since the build (checked on the GPU at every evaluation), so consecutive solver
+ * evaluations skip the grid and pair enumeration.  Every pair the reference would test is
+ * still tested exactly, and contact sums do not depend on the list, so energies,
+ * gradients and pair sets are bitwise those of a rebuild.  0 rebuilds at every evaluation;
+ * the default after mcg_upload_topology is cell_size / 8. */
+int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
+
 /* Per-phase timing of evaluations with CUDA events on the context stream (no reference
  * counterpart).  While on, every evaluation synchronizes at its end and adds its phase
  * durations: [0] node state, [1] beam kernel, [2] self-contact pipeline, [3] gradient

@@ -134,3 +134,25 @@ def test_run_of_the_reference_specimen_lies_in_the_rounding_ensemble(mcg):
         hi = max(s[k] for s in sums)
         pad = 0.1 * (hi - lo)
         assert lo - pad <= v <= hi + pad, (k, v, lo, hi)
+
+
+def test_candidate_list_reuse_is_bitwise_transparent(mcg):
+    """The 2x4x2 specimen's run is chaotic (reordered sums move its peak force by 15 %), so any
+    difference in a single evaluation would show.  Reusing the self-contact candidate list
+    (default skin, and a wide one) must give bitwise the frames of rebuilding it at every
+    evaluation: the list only decides which pairs reach the exact test, and contact sums are
+    ordered by shape pair, not by list position."""
+    g = golden("ref242")
+    runs = []
+    for skin in (0.0, None, 2e-3):
+        sol = mcg.Solver(g.cfg, g.lattice)
+        if skin is not None:
+            sol.set_contact_skin(skin)
+        rc, frames = sol.run()
+        assert rc == 0
+        runs.append(frames)
+    keys = sorted(runs[0][0].keys())
+    ref = np.array([[f[k] for k in keys] for f in runs[0]])
+    for fr in runs[1:]:
+        got = np.array([[f[k] for k in keys] for f in fr])
+        assert got.shape == ref.shape and np.array_equal(got, ref)
