@@ -158,12 +158,17 @@ __device__ Closest shape_closest(const ShapeRef& a, const ShapeRef& b) {
     return {0, 0, a.a, b.a};
 }
 
+// Membership of the node pair (u, v) in the connected set (sim.cpp:24-39 reads
+// connected_.count(pairKey(u, v))): multiplicative hash, linear probing.
 __device__ __forceinline__ bool is_connected(const DevTopo& t, int u, int v) {
-    const int k1 = t.conn_start[u + 1];
-    for (int k = t.conn_start[u]; k < k1; k++) {
-        const int w = t.conn_nbr[k];
-        if (w == v) return true;
-        if (w > v) return false;
+    const unsigned long long key = u <= v ? ((unsigned long long)u << 32) | uint32_t(v)
+                                          : ((unsigned long long)v << 32) | uint32_t(u);
+    unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> t.conn_shift;
+    for (unsigned long long probe = 0; probe <= t.conn_mask; probe++) {
+        const unsigned long long k = t.conn_hash[h];
+        if (k == key) return true;
+        if (k == ~0ull) return false;
+        h = (h + 1) & t.conn_mask;
     }
     return false;
 }
@@ -461,7 +466,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                                                       const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
                                                       const uint4* __restrict__ rec, int region,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
-                                                      uint32_t* __restrict__ flags) {
+                                                      uint32_t* __restrict__ wcap, uint32_t* __restrict__ flags) {
     __shared__ PairRec sh[kPairWarps][kWarpCap];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -567,6 +572,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
     }
     if (lane == 0) {
         wcount[gw] = out;
+        wcap[gw] = min(out, uint32_t(region));
         if (out > uint32_t(region)) atomicOr(flags, uint32_t(kOverCandidates));
     }
 }
@@ -646,32 +652,45 @@ __device__ __forceinline__ bool certainly_apart(const DevTopo& t, const PhysPara
     return L * 0.999999f - (3e-5f * X + 1e-9f) > (pa + pb) * 1.000001f;
 }
 
-// Narrow phase over the candidate regions, one warp per region (the region's owner in
-// k_bin_pairs).  Pass 0: test every candidate, keep one hit bit per candidate and the hit
-// count per region.  Pass 1 (after a scan of the counts): test the hits again and write
-// them as contacts, in region and candidate order.
+// Global candidate index g (regions in warp order, each in its own order) -> its slot:
+// the warp whose prefix range [woff[w], woff[w + 1]) holds g, by binary search.
+__device__ __forceinline__ uint2 candidate_at(const uint2* __restrict__ cand, const uint32_t* __restrict__ woff,
+                                              int W, int region, uint32_t g) {
+    int lo = 0, hi = W;  // woff[lo] <= g < woff[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (woff[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return cand[(long long)lo * region + (g - woff[lo])];
+}
+
+// Narrow phase over the candidate list, flattened so that each thread takes one candidate
+// whatever region it sits in (a warp's region can hold far more candidates than another's).
+// Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
+// 32 (chunks past the list are zeroed for the scan).  Pass 1 (after a scan of the chunk
+// counts): test the hits again and write them as contacts, in candidate order.
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                   const float4* __restrict__ xf, int region,
+                                                   const float4* __restrict__ xf, int region, int W,
                                                    const uint2* __restrict__ cand,
-                                                   const uint32_t* __restrict__ wcount,
+                                                   const uint32_t* __restrict__ woff, long long chunks,
                                                    uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
                                                    const uint32_t* __restrict__ hoff, ContactBufs c) {
     const int lane = threadIdx.x & 31;
-    const long long gw = (long long)blockIdx.x * kPairWarps + (threadIdx.x >> 5);
-    const uint32_t nc = min(wcount[gw], uint32_t(region));
-    const uint2* mine = cand + gw * region;
-    uint32_t* bits = hitbits + gw * (region / 32);
     const unsigned below = (1u << lane) - 1u;
-    uint32_t pos = pass == 1 ? hoff[gw] : 0;
-    for (uint32_t base = 0; base < nc; base += 32) {
-        const uint32_t i = base + lane;
+    const uint32_t total = woff[W];
+    const long long nchunk = (total + 31) / 32;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < (pass == 0 ? chunks : nchunk);
+         ch += warps) {
+        const uint32_t g = uint32_t(ch * 32 + lane);
         if constexpr (pass == 1) {
-            const unsigned m = bits[base / 32];
+            const unsigned m = hitbits[ch];
             if (m & (1u << lane)) {
-                const uint2 q = mine[i];
+                const uint2 q = candidate_at(cand, woff, W, region, g);
                 const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
-                const uint32_t o = pos + __popc(m & below);
+                const uint32_t o = hoff[ch] + __popc(m & below);
                 if (o < uint32_t(c.contact_cap)) {
                     c.c_a[o] = q.x;
                     c.c_b[o] = q.y;
@@ -683,20 +702,20 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
                     c.c_pen[o] = h.pen;
                 }
             }
-            pos += __popc(m);
         } else {
             bool hit = false;
-            if (i < nc) {
-                const uint2 q = mine[i];
+            if (ch < nchunk && g < total) {
+                const uint2 q = candidate_at(cand, woff, W, region, g);
                 hit = !certainly_apart(t, p, xf, q.x, q.y) &&
                       narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
-            if (lane == 0) bits[base / 32] = m;
-            pos += __popc(m);
+            if (lane == 0) {
+                hitbits[ch] = m;
+                hcount[ch] = __popc(m);
+            }
         }
     }
-    if (pass == 0 && lane == 0) hcount[gw] = pos;
 }
 
 // Fixed-partition reduction over the contact list: max penetration and count (the energy
@@ -750,6 +769,60 @@ __global__ void __launch_bounds__(kBlock) k_node_fill(DevTopo t, const uint32_t*
         }
 }
 
+// Per-node contact lists in canonical order: by the contact's (lower shape, higher shape)
+// and the slot, which no two items of one node share.  The gather sums each list in this
+// order, so forces do not depend on the order of the contact list.
+__device__ __forceinline__ unsigned long long item_key(const ContactBufs& c, uint32_t item) {
+    const uint32_t ci = item >> 2;
+    return ((unsigned long long)c.c_a[ci] << 31) | ((unsigned long long)c.c_b[ci] << 2) | (item & 3u);
+}
+
+// One warp per node: lists of up to 32 items ranked by shuffles; longer lists are queued.
+__global__ void __launch_bounds__(kBlock) k_node_sort(int N, ContactBufs c) {
+    const int lane = threadIdx.x & 31;
+    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= N) return;  // warp-uniform
+    const uint32_t cnt = c.n_count[i], s0 = c.n_start[i];
+    if (cnt == 0) return;
+    if (cnt > 32) {
+        if (lane == 0) c.n_long[1 + atomicAdd(c.n_long, 1u)] = uint32_t(i);
+        return;
+    }
+    uint32_t item = 0;
+    unsigned long long key = ~0ull;
+    if (lane < int(cnt)) {
+        item = c.n_items[s0 + lane];
+        key = item_key(c, item);
+    }
+    uint32_t rank = 0;
+    for (uint32_t q = 0; q < cnt; q++) rank += __shfl_sync(0xffffffffu, key, int(q)) < key;
+    if (lane < int(cnt)) c.n_sorted[s0 + rank] = item;
+}
+
+constexpr int kLongCap = 2048;  // keys staged in shared memory per long list
+
+// One block per queued node (longer lists): each item's rank is the number of smaller keys.
+__global__ void __launch_bounds__(kBlock) k_node_sort_long(ContactBufs c) {
+    __shared__ unsigned long long keys[kLongCap];
+    const uint32_t nl = c.n_long[0];
+    for (uint32_t j = blockIdx.x; j < nl; j += gridDim.x) {
+        const uint32_t i = c.n_long[1 + j];
+        const uint32_t cnt = c.n_count[i], s0 = c.n_start[i];
+        const bool staged = cnt <= uint32_t(kLongCap);
+        if (staged)
+            for (uint32_t e = threadIdx.x; e < cnt; e += blockDim.x) keys[e] = item_key(c, c.n_items[s0 + e]);
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < cnt; e += blockDim.x) {
+            const uint32_t item = c.n_items[s0 + e];
+            const unsigned long long k = staged ? keys[e] : item_key(c, item);
+            uint32_t r = 0;
+            for (uint32_t q = 0; q < cnt; q++) r += (staged ? keys[q] : item_key(c, c.n_items[s0 + q])) < k;
+            c.n_sorted[s0 + r] = item;
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 int contact_part_blocks(long long) { return kContactPartBlocks; }
@@ -785,16 +858,18 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     const uint32_t* nocc = c.boffset + c.bin_cap;
     const int W = c.pair_blocks * kPairWarps;
     (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted, c.sorted2,
-                                                c.rec, c.region, c.cand, c.wcount, c.flags),
+                                                c.rec, c.region, c.cand, c.wcount, c.wcap, c.flags),
      note_launches(1));
+    exclusive_scan_u32(c.wcap, c.woff, W, c.scan_tmp, s, gate);
     (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
-    // narrow phase over the candidate list: hit bits and counts per region, scan, contacts
-    (k_narrow<0><<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, c.cand, c.wcount, c.hitbits, c.hcount,
-                                               c.hoff, c), note_launches(1));
-    exclusive_scan_u32(c.hcount, c.hoff, W, c.scan_tmp, s);
-    (k_narrow<1><<<c.pair_blocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, c.cand, c.wcount, c.hitbits, c.hcount,
-                                               c.hoff, c), note_launches(1));
-    const uint32_t* total = c.hoff + W;
+    // narrow phase over the candidate list: hit bits and counts per chunk, scan, contacts
+    const long long chunks = (long long)W * c.region / 32;
+    (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
+                                                c.hcount, c.hoff, c), note_launches(1));
+    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s);
+    (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
+                                                c.hcount, c.hoff, c), note_launches(1));
+    const uint32_t* total = c.hoff + chunks;
     (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, c.c_pen, c.part, c.flags),
      note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
@@ -802,6 +877,9 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_node_count<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));
     exclusive_scan_u32(c.n_count, c.n_start, t.N, c.scan_tmp, s);
     (k_node_fill<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));
+    cudaMemsetAsync(c.n_long, 0, sizeof(uint32_t), s);
+    (k_node_sort<<<unsigned((32LL * t.N + kBlock - 1) / kBlock), kBlock, 0, s>>>(t.N, c), note_launches(1));
+    (k_node_sort_long<<<kStreamBlocks, kBlock, 0, s>>>(c), note_launches(1));
 }
 
 }  // namespace mcg

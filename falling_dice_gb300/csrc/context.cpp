@@ -183,9 +183,12 @@ struct mcg_ctx {
         c.region = std::max(32, (region + 31) / 32 * 32);
         c.cand = contact_mem.get<uint2>(size_t(W * c.region));
         c.wcount = contact_mem.get<uint32_t>(size_t(W));
-        c.hitbits = contact_mem.get<uint32_t>(size_t(W * c.region / 32));
-        c.hcount = contact_mem.get<uint32_t>(size_t(W + 1));
-        c.hoff = contact_mem.get<uint32_t>(size_t(W + 1));
+        c.wcap = contact_mem.get<uint32_t>(size_t(W + 1));
+        c.woff = contact_mem.get<uint32_t>(size_t(W + 1));
+        const long long chunks = W * c.region / 32;
+        c.hitbits = contact_mem.get<uint32_t>(size_t(chunks));
+        c.hcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
+        c.hoff = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.contact_cap = contact_cap;
         c.c_a = contact_mem.get<uint32_t>(size_t(contact_cap));
         c.c_b = contact_mem.get<uint32_t>(size_t(contact_cap));
@@ -197,8 +200,10 @@ struct mcg_ctx {
         c.n_start = contact_mem.get<uint32_t>(size_t(N + 1));
         c.n_cursor = contact_mem.get<uint32_t>(size_t(N));
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
+        c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
+        c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
         c.part = contact_mem.get<double>(size_t(3 * contact_part_blocks(contact_cap)));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1}));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
@@ -214,7 +219,8 @@ struct mcg_ctx {
         int grid[16];
         std::vector<uint32_t> wc(static_cast<size_t>(W));
         ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(&need[1], cb.hoff + W, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[1], cb.hoff + W * cb.region / 32, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
+           "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(wc.data(), cb.wcount, size_t(W) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
@@ -289,8 +295,8 @@ struct mcg_ctx {
     }
     long long read_contact_count() {
         uint32_t nc = 0;
-        ck(cudaMemcpyAsync(&nc, cb.hoff + (long long)cb.pair_blocks * 8, sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                           stream), "copy");
+        ck(cudaMemcpyAsync(&nc, cb.hoff + (long long)cb.pair_blocks * 8 * cb.region / 32, sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, stream), "copy");
         sync();
         return nc;
     }
@@ -749,14 +755,26 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
             adj[u].push_back(int(v));
             if (u != v) adj[v].push_back(int(u));
         }
-        std::vector<int> conn_start(size_t(N) + 1, 0), conn;
+        // connected pairs as an open-addressing hash set (at most half full)
+        long long npairs = 0;
         for (int i = 0; i < N; i++) {
             auto& l = adj[size_t(i)];
             std::sort(l.begin(), l.end());
             l.erase(std::unique(l.begin(), l.end()), l.end());
-            conn_start[size_t(i) + 1] = conn_start[size_t(i)] + int(l.size());
-            conn.insert(conn.end(), l.begin(), l.end());
+            for (int v : l) npairs += v >= i ? 1 : 0;
         }
+        int hbits = 4;
+        while ((1LL << hbits) < 2 * npairs) hbits++;
+        std::vector<unsigned long long> conn_hash(size_t(1) << hbits, ~0ull);
+        const unsigned long long hmask = (1ull << hbits) - 1;
+        for (int i = 0; i < N; i++)
+            for (int v : adj[size_t(i)]) {
+                if (v < i) continue;
+                const unsigned long long key = ((unsigned long long)i << 32) | uint32_t(v);
+                unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> (64 - hbits);
+                while (conn_hash[h] != ~0ull) h = (h + 1) & hmask;
+                conn_hash[h] = key;
+            }
         long long nfree = 0;
         for (long long k = 0; k < 6LL * N; k++) {
             if (t->locked[k] > 1) throw Fail(MCG_ERR_INVALID, "locked flags must be 0 or 1");
@@ -808,17 +826,18 @@ int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g
         int* di = M.get<int>(inc.size());
         h2d(di, inc.data(), inc.size(), s);
         T.inc = di;
-        int* dcs = M.get<int>(conn_start.size());
-        h2d(dcs, conn_start.data(), conn_start.size(), s);
-        T.conn_start = dcs;
+        {
+            unsigned long long* dh = M.get<unsigned long long>(conn_hash.size());
+            h2d(dh, conn_hash.data(), conn_hash.size(), s);
+            T.conn_hash = dh;
+            T.conn_mask = hmask;
+            T.conn_shift = 64 - hbits;
+        }
         {
             float* dp = M.get<float>(size_t(B));
             if (B) h2d(dp, padf.data(), size_t(B), s);
             T.padf = dp;
         }
-        int* dc = M.get<int>(conn.size());
-        if (!conn.empty()) h2d(dc, conn.data(), conn.size(), s);
-        T.conn_nbr = dc;
         c->topo = T;
         c->mat = Material{E, G, sy, cf.material.hardening, cf.material.bend_hardening, cf.material.torsion_hardening,
                           1.0 / std::max(1e-20, E + cf.material.hardening)};

@@ -38,8 +38,11 @@ struct DevTopo {
     const uint8_t* locked;    // [6N]
     const int* inc_start;     // [N+1]
     const int* inc;           // [2B]
-    const int* conn_start;    // [N+1] connected-pair adjacency (both directions, sorted)
-    const int* conn_nbr;
+    // connected node pairs (the reference's connected_ set) as an open-addressing hash set
+    // of keys u << 32 | v, u <= v; empty slots hold ~0; at most half full
+    const unsigned long long* conn_hash;
+    unsigned long long conn_mask;  // slots - 1 (a power of two)
+    int conn_shift;                // 64 - log2(slots)
     const float* padf;        // [B] radius + contact margin, rounded up to single precision
 };
 
@@ -101,9 +104,12 @@ struct ContactBufs {
     int region;             // candidate slots per warp, a multiple of 32
     uint2* cand;            // [warps * region] (lower shape, higher shape)
     uint32_t* wcount;       // [warps] candidates found per warp (may exceed region)
-    uint32_t* hitbits;      // [warps * region / 32] contact bit per candidate
-    uint32_t* hcount;       // [warps + 1] contacts per warp
-    uint32_t* hoff;         // [warps + 1] scan of hcount; hoff[warps] = contact count
+    uint32_t* wcap;         // [warps + 1] the same capped at region
+    uint32_t* woff;         // [warps + 1] scan of wcap: warp w's candidates are [woff[w], woff[w + 1])
+    // narrow phase, per chunk of 32 consecutive candidates (chunks = warps * region / 32)
+    uint32_t* hitbits;      // [chunks] contact bit per candidate
+    uint32_t* hcount;       // [chunks + 1] contacts per chunk
+    uint32_t* hoff;         // [chunks + 1] scan of hcount; hoff[chunks] = contact count
     long long contact_cap;
     uint32_t* c_a;          // lower shape index
     uint32_t* c_b;          // higher shape index
@@ -115,7 +121,9 @@ struct ContactBufs {
     uint32_t* n_count;      // [N+1]
     uint32_t* n_start;      // [N+1]
     uint32_t* n_cursor;     // [N]
-    uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot)
+    uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot), in arrival order
+    uint32_t* n_sorted;     // [4 * contact_cap]  the same per node, by (lower shape, higher shape, slot)
+    uint32_t* n_long;       // [N + 1] count, then the nodes whose lists exceed one warp
     double* part;           // [3 * contact_part_blocks] (unused), max penetration, count
     void* scan_tmp;
     size_t scan_tmp_bytes;

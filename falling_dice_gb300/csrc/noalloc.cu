@@ -102,9 +102,12 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.region = int((kNoAllocCandidates / W + 31) / 32 * 32);
     c.cand = reinterpret_cast<uint2*>(take(size_t(W * c.region) * sizeof(uint2)));
     c.wcount = reinterpret_cast<uint32_t*>(take(size_t(W) * 4));
-    c.hitbits = reinterpret_cast<uint32_t*>(take(size_t(W * c.region / 32) * 4));
-    c.hcount = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
-    c.hoff = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
+    c.wcap = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
+    c.woff = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
+    const long long chunks = W * c.region / 32;
+    c.hitbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
+    c.hcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
+    c.hoff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.contact_cap = kNoAllocContacts;
     c.c_a = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocContacts) * 4));
     c.c_b = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocContacts) * 4));
@@ -116,9 +119,12 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.n_start = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
     c.n_cursor = reinterpret_cast<uint32_t*>(take(size_t(N) * 4));
     c.n_items = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
+    c.n_sorted = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
+    c.n_long = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
     c.part = reinterpret_cast<double*>(take(size_t(3 * contact_part_blocks(kNoAllocContacts)) * 8));
     long long scan_n = S + 1;
     if (kNoAllocBins + 1 > scan_n) scan_n = kNoAllocBins + 1;
+    if (chunks + 1 > scan_n) scan_n = chunks + 1;
     c.scan_tmp_bytes = scan_tmp_bytes(scan_n);
     c.scan_tmp = take(c.scan_tmp_bytes);
     return off <= kNoAllocScratchBytes;

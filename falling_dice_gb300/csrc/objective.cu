@@ -281,13 +281,6 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
     }
 }
 
-// Sort key of a per-node contact item (contact index << 2 | slot): the contact's shape pair
-// and the slot (shapes are below 2^29).  Two items of one node never share a key.
-__device__ __forceinline__ unsigned long long contact_item_key(const ContactBufs& c, uint32_t item) {
-    const uint32_t ci = item >> 2;
-    return ((unsigned long long)c.c_a[ci] << 31) | ((unsigned long long)c.c_b[ci] << 2) | (item & 3u);
-}
-
 // Contribution of one contact slot to its node (MC/src/sim.cpp:23 addShapeGradient):
 // slots 0/1 are shape a's ends, 2/3 shape b's; capsule ends split the force (1-u, u).
 __device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const PhysParams& p, int N,
@@ -366,48 +359,12 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         gx.x += p.centering * e.cen[0] / double(N);
         gx.z += p.centering * e.cen[2] / double(N);
         // self-contact forces on this node in ascending (lower shape, higher shape, slot)
-        // order, and the self-contact energy of each contact on the first node of its lower
-        // shape: both independent of the order of the contact list
+        // order (the list is sorted by the contact pipeline), and the self-contact energy of
+        // each contact on the first node of its lower shape: both independent of the order
+        // of the contact list
         if (use_contacts) {
             const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
-            if (cnt <= 16) {
-                unsigned long long keys[16];
-                uint32_t items[16];
-                for (uint32_t k = 0; k < cnt; k++) {
-                    items[k] = c.n_items[s0 + k];
-                    keys[k] = contact_item_key(c, items[k]);
-                }
-                for (uint32_t a = 1; a < cnt; a++) {  // insertion sort by key
-                    const unsigned long long v = keys[a];
-                    const uint32_t it = items[a];
-                    uint32_t q = a;
-                    while (q > 0 && keys[q - 1] > v) {
-                        keys[q] = keys[q - 1];
-                        items[q] = items[q - 1];
-                        q--;
-                    }
-                    keys[q] = v;
-                    items[q] = it;
-                }
-                for (uint32_t k = 0; k < cnt; k++) add_contact_item(c, p, N, items[k], gx, acc[4]);
-            } else {
-                // long list: repeated minimum selection keeps the same order without storage
-                unsigned long long last = 0;
-                for (uint32_t k = 0; k < cnt; k++) {
-                    unsigned long long best = ~0ull;
-                    uint32_t best_item = 0;
-                    for (uint32_t q = 0; q < cnt; q++) {
-                        const uint32_t it = c.n_items[s0 + q];
-                        const unsigned long long v = contact_item_key(c, it);
-                        if ((k == 0 || v > last) && v < best) {
-                            best = v;
-                            best_item = it;
-                        }
-                    }
-                    add_contact_item(c, p, N, best_item, gx, acc[4]);
-                    last = best;
-                }
-            }
+            for (uint32_t k = 0; k < cnt; k++) add_contact_item(c, p, N, c.n_sorted[s0 + k], gx, acc[4]);
         }
         // platens (sim.cpp:168-171)
         const double jr = p.joint_radius, kc = p.contact_k;

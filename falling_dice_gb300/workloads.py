@@ -11,9 +11,9 @@ reference publishes no dataset for this path.
                   evaluation at a seeded deformed state (displacement N(0, 0.05 cell), rotation
                   angle N(0, 0.1 rad), plastic strain U[0, 0.02]).
   bcc32           32x32x16 cubic+BCC, radius graded 0.25->0.7 mm, +/-3 % jitter, 60 % strain,
-                  400 loading + 400 unloading increments.
+                  400 loading + 400 unloading increments, penalty stiffness scaled to E.
   bcc128          128x128x64 cubic+BCC, radii uniform 0.3-0.6 mm, +/-2 % jitter, 50 % strain in
-                  100 increments.
+                  100 increments, penalty stiffness scaled to E.
 """
 from . import abi
 
@@ -22,6 +22,11 @@ SEED = abi.REFERENCE_SEED
 
 # material of the throughput specimens: E = 2.0 GPa, nu = 0.35, yield 50 MPa, H = 5 % E
 MATERIAL = dict(young=2.0e9, nu=0.35, yield_=50e6, hardening=1.0e8)
+
+# Penalty stiffness of the load/unload specimens: the reference's default (1.2e6 N/m) is
+# sized for its own 26 MPa material; scaled by the modulus ratio it keeps platen
+# penetration well inside the 0.12 mm tolerance at the forces a 2 GPa lattice carries.
+CONTACT_STIFF = 1.2e6 * 2.0e9 / 26e6
 
 
 def _cfg(r0, r1, **kw):
@@ -55,11 +60,11 @@ def bcc64():
 
 def bcc32():
     return bcc((32, 32, 16), 0.25e-3, 0.7e-3, 0.03, abi.MCG_RADIUS_GRADED_Y, max_strain=0.6,
-               load_steps=400, unload_steps=400)
+               load_steps=400, unload_steps=400, contact_stiffness=CONTACT_STIFF)
 
 
 def bcc128():
-    return bcc((128, 128, 64), max_strain=0.5, load_steps=100, unload_steps=0)
+    return bcc((128, 128, 64), max_strain=0.5, load_steps=100, unload_steps=0, contact_stiffness=CONTACT_STIFF)
 
 
 # deformed state of the single-evaluation workload
