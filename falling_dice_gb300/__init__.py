@@ -48,6 +48,11 @@ SIGNATURES = {
     "mcg_set_timing": (C.c_int, [_P, C.c_int]),
     "mcg_set_contact_capacity": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64]),
     "mcg_set_contact_skin": (C.c_int, [_P, C.c_double]),
+    "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
+                                   C.POINTER(_d), C.POINTER(_d), _d]),
+    "mcg_instance_count": (C.c_int32, [_P]),
+    "mcg_batch_objective": (C.c_int, [_P, _d, _d, _d, _d, C.POINTER(abi.Diag)]),
+    "mcg_batch_run": (C.c_int, [_P, C.POINTER(abi.Frame), C.c_int32, _i32, _i32]),
     "mcg_phase_times": (C.c_int, [_P, _d, C.c_int32, C.POINTER(C.c_int64)]),
     "mcg_lattice_generate": (C.c_int, [C.POINTER(abi.LatticeSpec), C.POINTER(abi.Config), C.POINTER(_P)]),
     "mcg_lattice_view_of": (C.c_int, [_P, C.POINTER(abi.LatticeView)]),
@@ -261,3 +266,51 @@ class Solver:
         n = C.c_int64()
         self._check(self.lib.mcg_phase_times(self.h, _ptr(ms), len(ms), C.byref(n)), "mcg_phase_times")
         return dict(zip(self.PHASES, ms)), n.value
+
+
+class BatchSolver(Solver):
+    """One device context holding many lattices (mcg_upload_batch): every evaluation,
+    minimizer step and load/unload increment of all of them runs in the same launches.
+    `yields` gives each lattice's yield stress (default: the configuration's)."""
+
+    def __init__(self, cfg, lattices, yields=None, device=0):
+        self.lib = load()
+        self.cfg = cfg
+        self.h = _P()
+        self._check(self.lib.mcg_create(C.byref(cfg), device, C.byref(self.h)), "mcg_create", ctx=False)
+        self.lattices = list(lattices)
+        k = len(self.lattices)
+        topos = (abi.Topology * k)()
+        geoms = (abi.Geometry * k)()
+        x0 = (_d * k)()
+        r0 = (_d * k)()
+        for i, lat in enumerate(self.lattices):
+            t, g = lat.topology()
+            topos[i], geoms[i] = t, g
+            x0[i], r0[i] = _ptr(lat.x0), _ptr(lat.r0)
+        self._keep = (topos, geoms, x0, r0, [lat.topology() for lat in self.lattices])
+        y = None if yields is None else np.ascontiguousarray(yields, dtype=np.float64)
+        self._check(self.lib.mcg_upload_batch(self.h, k, topos, geoms, x0, r0, _ptr(y)), "mcg_upload_batch")
+        self.count = k
+        self.node_offsets = np.cumsum([0] + [lat.n_nodes for lat in self.lattices])
+        self.n_nodes = int(self.node_offsets[-1])
+        self.n_beams = sum(lat.n_beams for lat in self.lattices)
+
+    def objective(self, z, tops):
+        z = _f64(z)
+        tops = _f64(tops)
+        e = np.zeros(self.count)
+        grad = np.zeros(6 * self.n_nodes)
+        diags = (abi.Diag * self.count)()
+        self._check(self.lib.mcg_batch_objective(self.h, _ptr(z), _ptr(tops), _ptr(e), _ptr(grad), diags),
+                    "mcg_batch_objective")
+        return {"energy": e, "grad": grad, "diag": [diags[i].as_dict() for i in range(self.count)]}
+
+    def run(self, verbose=False):
+        cap = self.cfg.load_steps + self.cfg.unload_steps + 1 + 4096
+        frames = (abi.Frame * (cap * self.count))()
+        counts = np.zeros(self.count, np.int32)
+        status = np.zeros(self.count, np.int32)
+        self._check(self.lib.mcg_batch_run(self.h, frames, cap, _ptr(counts, _i32), _ptr(status, _i32)),
+                    "mcg_batch_run")
+        return status, [[frames[i * cap + f].as_dict() for f in range(counts[i])] for i in range(self.count)]

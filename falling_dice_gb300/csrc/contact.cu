@@ -594,7 +594,6 @@ __global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const ui
         if (f[b]) occ[off[b]] = uint32_t(b);
 }
 
-constexpr int kContactPartBlocks = 128;
 
 // Certified single-precision rejection of a candidate pair: true when the two shapes are
 // certainly farther apart than pad_a + pad_b (>= the reference's target ra + rb + margin),
@@ -718,38 +717,16 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
     }
 }
 
-// Fixed-partition reduction over the contact list: max penetration and count (the energy
-// is summed per node by the gather, in an order independent of the list).
-__global__ void __launch_bounds__(kBlock) k_contact_reduce(const uint32_t* __restrict__ total, long long cap,
-                                                           const double* __restrict__ pen, double* __restrict__ part,
-                                                           uint32_t* flags) {
-    __shared__ double sm[kBlock / 32];
-    __shared__ double smx[kBlock / 32];
-    const long long nc_all = *total;
-    if (nc_all > cap && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(flags, uint32_t(kOverContacts));
-    const long long nc = nc_all > cap ? cap : nc_all;
-    double acc[1] = {0};
-    double m = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x) {
-        acc[0] += 1;
-        m = fmax(m, pen[i]);
-    }
-    block_sum<1>(acc, sm);
-    m = block_max(m, smx);
-    if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = 0;
-        part[3 * blockIdx.x + 1] = m;
-        part[3 * blockIdx.x + 2] = acc[0];
-    }
-}
-
 __device__ __forceinline__ int slot_node(const DevTopo& t, uint32_t shape, int slot) {
     if (shape < uint32_t(t.N)) return slot == 0 ? int(shape) : -1;
     const int2 ab = t.ab[shape - uint32_t(t.N)];
     return slot == 0 ? ab.x : ab.y;
 }
 
+// Per-node item counts; a contact list longer than its capacity flags kOverContacts.
 __global__ void __launch_bounds__(kBlock) k_node_count(DevTopo t, const uint32_t* __restrict__ total, ContactBufs c) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (long long)*total > c.contact_cap)
+        atomicOr(c.flags, uint32_t(kOverContacts));
     const long long nc = min((long long)*total, c.contact_cap);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += (long long)gridDim.x * blockDim.x)
         for (int slot = 0; slot < 4; slot++) {
@@ -825,7 +802,6 @@ __global__ void __launch_bounds__(kBlock) k_node_sort_long(ContactBufs c) {
 
 }  // namespace
 
-int contact_part_blocks(long long) { return kContactPartBlocks; }
 
 int contact_pair_blocks(long long shapes) {
     const long long b = shapes / 256;
@@ -840,8 +816,8 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
     // candidate list (only when rebuilding)
     (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
-    (k_grid_params<<<1, 32, 0, s>>>(e.cen, pad + double(skin > 0.f ? skin : 0.f), p.broad_cell, c.bin_cap, c.grid,
-                                    c.flags),
+    (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
+                                    c.bin_cap, c.grid, c.flags),
      note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
                                                  c.count, skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
@@ -870,8 +846,6 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
                                                 c.hcount, c.hoff, c), note_launches(1));
     const uint32_t* total = c.hoff + chunks;
-    (k_contact_reduce<<<kContactPartBlocks, kBlock, 0, s>>>(total, c.contact_cap, c.c_pen, c.part, c.flags),
-     note_launches(1));
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);
     (k_node_count<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));

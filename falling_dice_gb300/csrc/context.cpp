@@ -4,6 +4,13 @@
 // The solver logic follows the reference's Simulator::minimize / commit / run
 // (MC/src/sim.cpp:174-213, 312-467) decision for decision; the vectors live on the device
 // and only the scalars each decision needs are read back.
+//
+// A context holds I lattices (instances): one for the plain API, many for the batched sweep.
+// Every evaluation evaluates all of them in the same launches, and the minimizer and the
+// load/unload driver are per-instance state machines stepped together: in each round every
+// instance that needs one gets its direction, its next candidate and one evaluation, and
+// decides as the reference would.  An instance's arithmetic does not depend on the others,
+// so a lattice solved in a batch gives bit for bit what it gives alone.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -11,7 +18,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <functional>
 #include <limits>
 #include <new>
 #include <stdexcept>
@@ -47,13 +53,14 @@ void ck(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw Fail(MCG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-struct Pinned {
-    EvalOut out;
-    double rmsmax[2];
-    double dots[4];
-    uint32_t u32[8];
-    int grid[8];
-};
+template <class T>
+void h2d(T* d, const T* h, size_t n, cudaStream_t s) {
+    if (n) ck(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, s), "copy to device");
+}
+template <class T>
+void d2h(T* h, const T* d, size_t n, cudaStream_t s) {
+    if (n) ck(cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, s), "copy to host");
+}
 
 struct DevArena {
     std::vector<void*> ptrs;
@@ -71,10 +78,106 @@ struct DevArena {
     ~DevArena() { release(); }
 };
 
+// Page-locked staging for the per-instance scalars the host reads and writes every round.
+struct Pinned {
+    void* base = nullptr;
+    EvalOut* outs = nullptr;   // [I]
+    double* tops = nullptr;    // [I]
+    SolveCtl* ctl = nullptr;   // [I]
+    double* rho = nullptr;     // [I * H]
+    double* dg = nullptr;      // [I]
+    double* dots3 = nullptr;   // [3 I]
+    double* pstats = nullptr;  // [6 I]
+    double* cen = nullptr;     // [9 (I + 1)]
+    uint32_t* u32 = nullptr;   // [8]
+    void alloc(int I, int H) {
+        release();
+        const size_t Hn = size_t(std::max(H, 1));
+        const size_t bytes = I * sizeof(EvalOut) + I * sizeof(SolveCtl) +
+                             sizeof(double) * (I + I * Hn + I + 3 * I + 6 * I + 9 * (I + 1)) + 8 * 4 + 256;
+        ck(cudaMallocHost(&base, bytes), "cudaMallocHost");
+        std::memset(base, 0, bytes);
+        char* p = static_cast<char*>(base);
+        auto take = [&](size_t b) {
+            char* r = p;
+            p += (b + 15) & ~size_t(15);
+            return r;
+        };
+        outs = reinterpret_cast<EvalOut*>(take(I * sizeof(EvalOut)));
+        ctl = reinterpret_cast<SolveCtl*>(take(I * sizeof(SolveCtl)));
+        tops = reinterpret_cast<double*>(take(I * sizeof(double)));
+        rho = reinterpret_cast<double*>(take(I * Hn * sizeof(double)));
+        dg = reinterpret_cast<double*>(take(I * sizeof(double)));
+        dots3 = reinterpret_cast<double*>(take(3 * I * sizeof(double)));
+        pstats = reinterpret_cast<double*>(take(6 * I * sizeof(double)));
+        cen = reinterpret_cast<double*>(take(9 * (I + 1) * sizeof(double)));
+        u32 = reinterpret_cast<uint32_t*>(take(8 * sizeof(uint32_t)));
+    }
+    void release() {
+        if (base) cudaFreeHost(base);
+        base = nullptr;
+    }
+    ~Pinned() { release(); }
+};
+
 struct HostStats {
     int iterations = 0, backtracks = 0;
     double rms = kInf, max = kInf, energy = kInf;
     bool converged = false;
+};
+
+// One instance's Simulator::minimize (MC/src/sim.cpp:174-211) as a state machine.
+struct Minimizer {
+    enum Phase { kIdle, kStart, kIterate, kDirection, kSteepest, kTrial, kFinish, kDone };
+    Phase phase = kIdle;
+    double top = 0;
+    bool zero_first = false;  // z = 0 before the first evaluation (run(): zeroVars, sim.cpp:398)
+    bool restore = false;     // z = best before the final evaluation
+    HostStats st;
+    EvalOut cur{}, cand{}, fin{};
+    double cur_rms = 0, cur_max = 0, rms0 = 0, best_energy = 0, dg = 0, step = 1;
+    int it = 0, bt = 0;
+    bool retry = false;       // in the steepest-descent retry of this iteration
+    int m = 0, head = 0;      // history pairs held, oldest slot
+    int target = 0;           // slot of the pair of an accepted step
+};
+
+// One instance of the load/unload driver (Simulator::run, MC/src/sim.cpp:374-467).
+struct Task {
+    double top;
+    bool loading;
+    int refinement;
+};
+struct Runner {
+    bool done = false;
+    int status = MCG_OK;
+    std::string error;
+    int next_step = 0;  // 0: the settle at top0, then load steps, then unload steps
+    std::vector<Task> stack;
+    Task task{};
+    double time = 0, currentTop = 0;
+    bool first = true;
+    int accepted = 0;
+    double loadingWork = 0, recoveredWork = 0, prevDisp = 0, prevForce = 0, reactionOffset = 0;
+    std::vector<mcg_frame> frames;
+};
+
+// Host description of one instance.
+struct InstHost {
+    int node0 = 0, N = 0, beam0 = 0, B = 0;
+    long long n_free = 0;
+    mcg_geometry geom{};
+    double sy = 0;
+    float2 off{0.f, 0.f};
+};
+
+// One instance's input to the upload.
+struct InstIn {
+    const mcg_topology* t;
+    const mcg_geometry* g;
+    const double* x0;
+    const double* r0;
+    double sy;
 };
 
 }  // namespace
@@ -84,10 +187,9 @@ struct mcg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
-    int N = 0, B = 0;
-    long long n_free = 0;
+    int N = 0, B = 0, I = 0;
+    std::vector<InstHost> inst;
     bool have_topo = false;
-    mcg_geometry geom{};
     double jr = 0, rmax = 0;
 
     DevArena topo_mem, eval_mem, contact_mem, solver_mem;
@@ -97,7 +199,7 @@ struct mcg_ctx {
     EvalBufs ev{};
     ContactBufs cb{};
     long long last_contacts = 0;
-    int last_sort_res = 0;
+    Pinned hp;
 
     double *d_baseX = nullptr, *d_baseR = nullptr, *d_plastic = nullptr;
     bool mixed = false;  // MCG_MIXED: FP32 bulk arithmetic (objective_mixed.cu)
@@ -108,18 +210,17 @@ struct mcg_ctx {
         if (mixed) launch_rebase_mixed(topo, d_baseX, d_baseR, mb, mn, stream);
     }
     double *d_zin = nullptr, *d_grad = nullptr;
-    Pinned* hp = nullptr;
 
-    // solver vectors
-    double *d_z = nullptr, *d_zc = nullptr, *d_p = nullptr, *d_g = nullptr, *d_gc = nullptr, *d_best = nullptr;
-    std::vector<double*> d_S, d_Y;
-    double *d_rho = nullptr, *d_alpha = nullptr, *d_scal = nullptr, *d_part = nullptr, *d_stats = nullptr;
-    double* d_zfinal = nullptr;
-    bool have_final = false;
-    EvalOut final_out{};
-
-    // run() bookkeeping (sim.hpp:47)
-    double loadingWork = 0, recoveredWork = 0, prevDisp = 0, prevForce = 0, reactionOffset = 0;
+    // solver vectors (all instances), history H slots of 6N, per-instance scalars
+    int H = 0;
+    double *d_z = nullptr, *d_zeval = nullptr, *d_p = nullptr, *d_g = nullptr, *d_geval = nullptr,
+           *d_best = nullptr, *d_zfinal = nullptr, *d_S = nullptr, *d_Y = nullptr;
+    double *d_rho = nullptr, *d_alpha = nullptr, *d_part = nullptr, *d_dg = nullptr, *d_dots3 = nullptr,
+           *d_pstats = nullptr;
+    SolveCtl* d_ctl = nullptr;
+    uint8_t* d_mask = nullptr;
+    std::vector<Minimizer> mins;
+    bool have_final = false;  // instance 0 has a final state from minimize, not yet committed
 
     // optional per-phase timing of evaluations (events on the context stream)
     static constexpr int kPhases = 5;  // state, beams, contacts, gather, finalize
@@ -144,7 +245,6 @@ struct mcg_ctx {
     ~mcg_ctx() {
         for (auto& e : ev_t)
             if (e) cudaEventDestroy(e);
-        if (hp) cudaFreeHost(hp);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -202,13 +302,13 @@ struct mcg_ctx {
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
-        c.part = contact_mem.get<double>(size_t(3 * contact_part_blocks(contact_cap)));
         c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
+    long long contact_chunks() const { return (long long)cb.pair_blocks * 8 * cb.region / 32; }
 
     // Grows whatever the last evaluation overflowed; false when nothing did.
     bool grow_contacts(int flags) {
@@ -219,7 +319,7 @@ struct mcg_ctx {
         int grid[16];
         std::vector<uint32_t> wc(static_cast<size_t>(W));
         ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(&need[1], cb.hoff + W * cb.region / 32, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
+        ck(cudaMemcpyAsync(&need[1], cb.hoff + contact_chunks(), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
            "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(wc.data(), cb.wcount, size_t(W) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
@@ -242,11 +342,14 @@ struct mcg_ctx {
         return true;
     }
 
-    // One evaluation of the objective at device z; grad written to d_gout; totals in ev.out.
-    // Enqueues only: no host synchronisation.
-    void eval(const double* dz, double top, bool trials, double* d_gout) {
+    // ---- evaluation ----------------------------------------------------------------------
+    // Platen heights of all instances from hp.tops (the host changes them only after a sync).
+    void upload_tops() { h2d(ev.tops, hp.tops, size_t(I), stream); }
+
+    // One evaluation of every instance at device z; grad written to d_gout; totals in
+    // ev.out[0..I).  Enqueues only: no host synchronisation.
+    void eval(const double* dz, bool trials, double* d_gout) {
         PhysParams p = phys;
-        p.top = top;
         p.broad_cell = broad_cell;
         p.inv_cell_f = float(1.0 / broad_cell);
         mark(0);
@@ -269,213 +372,327 @@ struct mcg_ctx {
         mark(5);
         check_launch();
         collect();
-        last_top = top;
         last_z = dz;
         last_trials = trials;
         last_grad = d_gout;
     }
-    double last_top = 0;
     const double* last_z = nullptr;
     bool last_trials = false;
     double* last_grad = nullptr;
 
-    // Evaluation whose totals are read back; repeats it with larger contact buffers when a
-    // capacity was exceeded.
-    EvalOut eval_read(const double* dz, double top, bool trials, double* d_gout) {
-        eval(dz, top, trials, d_gout);
-        EvalOut o = read_out_raw();
-        for (int tries = 0; o.overflow && tries < 16; tries++) {
-            if (!grow_contacts(o.overflow)) break;
-            eval(dz, top, trials, d_gout);
-            o = read_out_raw();
+    // Evaluation whose totals are read back (hp.outs); repeats it with larger contact
+    // buffers when a capacity was exceeded.
+    const EvalOut* eval_read(const double* dz, bool trials, double* d_gout) {
+        eval(dz, trials, d_gout);
+        read_outs();
+        for (int tries = 0; hp.outs[0].overflow && tries < 16; tries++) {
+            if (!grow_contacts(hp.outs[0].overflow)) break;
+            eval(dz, trials, d_gout);
+            read_outs();
         }
-        if (o.overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
+        if (hp.outs[0].overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
         if (cfg.self_contact) last_contacts = read_contact_count();
-        return o;
+        return hp.outs;
     }
     long long read_contact_count() {
-        uint32_t nc = 0;
-        ck(cudaMemcpyAsync(&nc, cb.hoff + (long long)cb.pair_blocks * 8 * cb.region / 32, sizeof(uint32_t),
-                           cudaMemcpyDeviceToHost, stream), "copy");
+        d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
         sync();
-        return nc;
+        return hp.u32[0];
     }
-    EvalOut read_out_raw() {
-        ck(cudaMemcpyAsync(&hp->out, ev.out, sizeof(EvalOut), cudaMemcpyDeviceToHost, stream), "copy");
+    void read_outs() {
+        d2h(hp.outs, ev.out, size_t(I), stream);
         sync();
-        return hp->out;
     }
     // Totals of the last evaluation, repeating it if it overflowed a contact buffer.
     EvalOut read_out() {
-        EvalOut o = read_out_raw();
-        if (o.overflow) o = eval_read(last_z, last_top, last_trials, last_grad);
+        read_outs();
+        if (hp.outs[0].overflow) eval_read(last_z, last_trials, last_grad);
         else if (cfg.self_contact) last_contacts = read_contact_count();
-        return o;
-    }
-    void read_rms_max(const double* g, double& rms, double& mx) {
-        rms_max(g, topo.locked, 6LL * N, n_free, d_part, d_stats, stream);
-        ck(cudaMemcpyAsync(hp->rmsmax, d_stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
-        sync();
-        rms = hp->rmsmax[0];
-        mx = hp->rmsmax[1];
-    }
-    double read_dot(const double* a, const double* b) {
-        dots(1, a, b, nullptr, nullptr, nullptr, nullptr, 6LL * N, d_part, d_stats + 4, stream);
-        ck(cudaMemcpyAsync(hp->dots, d_stats + 4, sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
-        sync();
-        return hp->dots[0];
+        return hp.outs[0];
     }
 
-    // ---- Simulator::minimize, MC/src/sim.cpp:174-211 --------------------------------------
-    HostStats minimize(double top, EvalOut& fin) {
-        const long long n = 6LL * N;
-        const int H = std::max(0, cfg.history);
-        HostStats st;
-        int m = 0, head = 0;  // history: slots (head + h) % H, h = 0 oldest
-        auto slot = [&](int h) { return (head + h) % std::max(H, 1); };
-        EvalOut cur = eval_read(d_z, top, false, d_g);
-        double cur_rms, cur_max;
-        read_rms_max(d_g, cur_rms, cur_max);
-        double best_energy = cur.energy;
-        vcopy(d_best, d_z, n, stream);
-        const double rms0 = cur_rms;
-        auto converged = [&](const EvalOut& o, double rms, double mx) {
-            if (cfg.relative_gradient_tolerance > 0)
-                return (rms <= cfg.relative_gradient_tolerance * rms0) && o.max_pen <= cfg.penetration_tolerance;
-            const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.reaction));
-            const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < 1.5e-3;
-            return forceOK && o.max_pen <= cfg.penetration_tolerance;
-        };
-        EvalOut cand{};
-        auto line_search = [&](double dg) {
-            double step = 1.0;
-            for (int bt = 0; bt < cfg.max_line_search; bt++) {
-                candidate(d_zc, d_z, d_p, step, topo.locked, n, stream);
-                cand = eval_read(d_zc, top, false, d_gc);
-                st.backtracks++;
-                if (std::isfinite(cand.energy) && cand.energy <= cur.energy + cfg.armijo * step * dg) return true;
-                step *= .5;
-                if (step < cfg.min_line_step) break;
+    // ---- solver rounds --------------------------------------------------------------------
+    void upload_ctl() { h2d(d_ctl, hp.ctl, size_t(I), stream); }
+    void clear_ctl() {
+        for (int i = 0; i < I; i++) hp.ctl[i] = SolveCtl{0.0, 0, mins[size_t(i)].m, mins[size_t(i)].head, 0};
+    }
+    bool converged(const EvalOut& o, double rms, double mx, double rms0) const {
+        if (cfg.relative_gradient_tolerance > 0)
+            return (rms <= cfg.relative_gradient_tolerance * rms0) && o.max_pen <= cfg.penetration_tolerance;
+        const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.reaction));
+        const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < 1.5e-3;
+        return forceOK && o.max_pen <= cfg.penetration_tolerance;
+    }
+    // Host-only step of the iteration loop (sim.cpp:176-177): record, test convergence,
+    // continue with a direction or finish.
+    void iterate(Minimizer& s) {
+        if (s.it >= cfg.max_iterations) {
+            s.phase = Minimizer::kFinish;
+            s.restore = !s.st.converged && s.best_energy < s.cur.energy;
+            return;
+        }
+        s.st.iterations = s.it + 1;
+        s.st.rms = s.cur_rms;
+        s.st.max = s.cur_max;
+        s.st.energy = s.cur.energy;
+        if (converged(s.cur, s.cur_rms, s.cur_max, s.rms0)) {
+            s.st.converged = true;
+            s.phase = Minimizer::kFinish;
+            s.restore = false;
+            return;
+        }
+        s.phase = Minimizer::kDirection;
+    }
+    // Starts instance i's minimization at platen height `top` from the current d_z (or from
+    // z = 0 with zero_first), with an empty history.
+    void start_minimize(int i, double top, bool zero_first) {
+        Minimizer& s = mins[size_t(i)];
+        s = Minimizer{};
+        s.phase = Minimizer::kStart;
+        s.top = top;
+        s.zero_first = zero_first;
+    }
+
+    // One round for every instance with an unfinished minimization: directions, one
+    // evaluation each, decisions, accepted steps.  False when no instance had work.
+    bool minimize_round() {
+        using M = Minimizer;
+        const double mt = cfg.max_translation_step / cfg.translation_scale, mr = cfg.max_rotation_step;
+        // A. search directions: two-loop (sim.cpp:184-190), steepest descent when that is
+        //    not a descent direction (:191) or for the retry after a failed search (:193-196)
+        bool any_dir = false, any_sd = false;
+        clear_ctl();
+        int max_m = 0;
+        for (int i = 0; i < I; i++) {
+            const M& s = mins[size_t(i)];
+            if (s.phase == M::kDirection) {
+                hp.ctl[i].flags = kOpDirection;
+                any_dir = true;
+                max_m = std::max(max_m, s.m);
             }
-            return false;
-        };
-        std::vector<const double*> S(H), Y(H), R(H);
-        for (int it = 0; it < cfg.max_iterations; it++) {
-            st.iterations = it + 1;
-            st.rms = cur_rms;
-            st.max = cur_max;
-            st.energy = cur.energy;
-            if (converged(cur, cur_rms, cur_max)) {
-                st.converged = true;
-                break;
-            }
-            for (int h = 0; h < m; h++) {
-                S[h] = d_S[slot(h)];
-                Y[h] = d_Y[slot(h)];
-                R[h] = d_rho + slot(h);
-            }
-            two_loop(d_p, d_g, S.data(), Y.data(), R.data(), m, d_alpha, d_scal, d_part, n, stream);
-            finish_direction(d_p, d_p, topo.locked, N, cfg.max_translation_step / cfg.translation_scale,
-                             cfg.max_rotation_step, stream);
-            double dg = read_dot(d_g, d_p);
-            if (!(dg < 0)) {  // not a descent direction: steepest descent (sim.cpp:191)
-                m = 0;
-                finish_direction(d_p, d_g, topo.locked, N, cfg.max_translation_step / cfg.translation_scale,
-                                 cfg.max_rotation_step, stream);
-                dg = read_dot(d_g, d_p);
-            }
-            bool ok = line_search(dg);
-            if (!ok) {  // steepest-descent retry (sim.cpp:193-203)
-                m = 0;
-                finish_direction(d_p, d_g, topo.locked, N, cfg.max_translation_step / cfg.translation_scale,
-                                 cfg.max_rotation_step, stream);
-                dg = read_dot(d_g, d_p);
-                ok = line_search(dg);
-            }
-            if (!ok) break;
-            // curvature pair (sim.cpp:205-206) into the slot it would occupy
-            const int target = H == 0 ? 0 : (m < H ? slot(m) : slot(0));
-            double sy = 0, ss = 0, yy = 0;
-            if (H > 0) {
-                make_sy(d_S[target], d_Y[target], d_zc, d_z, d_gc, d_g, n, stream);
-                dots(3, d_S[target], d_Y[target], d_S[target], d_S[target], d_Y[target], d_Y[target], n, d_part,
-                     d_stats + 4, stream);
-            }
-            rms_max(d_gc, topo.locked, n, n_free, d_part, d_stats, stream);
-            ck(cudaMemcpyAsync(hp->rmsmax, d_stats, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
-            ck(cudaMemcpyAsync(hp->dots, d_stats + 4, 3 * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
+            any_sd |= s.phase == M::kSteepest;
+        }
+        if (any_dir) {
+            upload_ctl();
+            h2d(d_rho, hp.rho, size_t(I) * size_t(std::max(H, 1)), stream);
+            bl_direction(topo, d_ctl, std::max(H, 1), max_m, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_alpha, d_part,
+                         d_dg, mt, mr, stream);
+            d2h(hp.dg, d_dg, size_t(I), stream);
             sync();
-            if (H > 0) {
-                sy = hp->dots[0];
-                ss = hp->dots[1];
-                yy = hp->dots[2];
-                if (sy > 1e-12 * std::sqrt(std::max(1e-30, ss * yy))) {
-                    set_rho(d_rho + target, d_stats + 4, stream);
-                    if (m == H) head = (head + 1) % H;
-                    else m++;
+            for (int i = 0; i < I; i++) {
+                M& s = mins[size_t(i)];
+                if (s.phase != M::kDirection) continue;
+                s.dg = hp.dg[i];
+                if (!(s.dg < 0)) {  // not a descent direction: steepest descent (sim.cpp:191)
+                    s.m = 0;
+                    s.phase = M::kSteepest;
+                    any_sd = true;
                 } else {
-                    m = 0;
+                    s.phase = M::kTrial;
+                    s.step = 1.0;
+                    s.bt = 0;
                 }
             }
-            std::swap(d_z, d_zc);
-            std::swap(d_g, d_gc);
-            cur = cand;
-            cur_rms = hp->rmsmax[0];
-            cur_max = hp->rmsmax[1];
-            if (cur.energy < best_energy) {
-                best_energy = cur.energy;
-                vcopy(d_best, d_z, n, stream);
+        }
+        if (any_sd) {
+            clear_ctl();
+            for (int i = 0; i < I; i++)
+                if (mins[size_t(i)].phase == M::kSteepest) hp.ctl[i].flags = kOpSteepest;
+            upload_ctl();
+            bl_steepest(topo, d_ctl, d_p, d_g, d_part, d_dg, mt, mr, stream);
+            d2h(hp.dg, d_dg, size_t(I), stream);
+            sync();
+            for (int i = 0; i < I; i++) {
+                M& s = mins[size_t(i)];
+                if (s.phase != M::kSteepest) continue;
+                s.dg = hp.dg[i];
+                s.phase = M::kTrial;
+                s.step = 1.0;
+                s.bt = 0;
             }
         }
-        if (!st.converged && best_energy < cur.energy) vcopy(d_z, d_best, n, stream);
-        fin = eval_read(d_z, top, true, d_g);
-        read_rms_max(d_g, st.rms, st.max);
-        st.energy = fin.energy;
-        st.converged = converged(fin, st.rms, st.max);
-        vcopy(d_zfinal, d_z, n, stream);
-        have_final = true;
-        final_out = fin;
+        // B. one evaluation per instance: the start point, a line-search candidate
+        //    (sim.cpp:179) or the final state with trials (sim.cpp:210)
+        clear_ctl();
+        bool any = false, trials = false;
+        for (int i = 0; i < I; i++) {
+            const M& s = mins[size_t(i)];
+            SolveCtl& c = hp.ctl[i];
+            switch (s.phase) {
+                case M::kStart:
+                    c.flags = (s.zero_first ? kOpZero : 0) | kOpEvalAtZ | kOpKeepBest;
+                    any = true;
+                    break;
+                case M::kTrial:
+                    c.flags = kOpCandidate;
+                    c.step = s.step;
+                    any = true;
+                    break;
+                case M::kFinish:
+                    c.flags = (s.restore ? kOpRestore : 0) | kOpEvalAtZ | kOpFinal;
+                    any = true;
+                    trials = true;
+                    break;
+                default:
+                    break;
+            }
+            if (s.phase == M::kStart || s.phase == M::kTrial || s.phase == M::kFinish) hp.tops[i] = s.top;
+        }
+        if (!any) return false;
+        upload_ctl();
+        upload_tops();
+        bl_prepare(topo, d_ctl, d_z, d_best, d_zeval, d_p, d_zfinal, stream);
+        const EvalOut* out = eval_read(d_zeval, trials, d_geval);
+        // C. decisions (the reference's, per instance) and the vectors they imply
+        clear_ctl();
+        bool any_post = false, any_accept = false;
+        for (int i = 0; i < I; i++) {
+            M& s = mins[size_t(i)];
+            SolveCtl& c = hp.ctl[i];
+            const EvalOut& o = out[i];
+            switch (s.phase) {
+                case M::kStart:
+                    s.cur = o;
+                    s.cur_rms = o.rms;
+                    s.cur_max = o.gmax;
+                    s.best_energy = o.energy;
+                    s.rms0 = o.rms;
+                    s.it = 0;
+                    c.flags = kOpTakeGrad;
+                    any_post = true;
+                    s.phase = M::kIterate;
+                    break;
+                case M::kTrial: {
+                    s.cand = o;
+                    s.st.backtracks++;
+                    if (std::isfinite(o.energy) && o.energy <= s.cur.energy + cfg.armijo * s.step * s.dg) {
+                        c.flags = kOpAccept;
+                        if (H > 0) {
+                            s.target = s.m < H ? (s.head + s.m) % H : s.head;
+                            c.flags |= kOpPair;
+                            c.target = s.target;
+                        }
+                        if (o.energy < s.best_energy) c.flags |= kOpKeepBestAfter;
+                        any_post = any_accept = true;
+                        break;
+                    }
+                    s.step *= .5;
+                    s.bt++;
+                    if (!(s.step < cfg.min_line_step) && s.bt < cfg.max_line_search) break;
+                    // line search failed (sim.cpp:193-209)
+                    if (!s.retry) {
+                        s.retry = true;
+                        s.m = 0;
+                        s.phase = M::kSteepest;
+                    } else {
+                        s.phase = M::kFinish;
+                        s.restore = !s.st.converged && s.best_energy < s.cur.energy;
+                    }
+                    break;
+                }
+                case M::kFinish:
+                    s.fin = o;
+                    s.st.rms = o.rms;
+                    s.st.max = o.gmax;
+                    s.st.energy = o.energy;
+                    s.st.converged = converged(o, o.rms, o.gmax, s.rms0);
+                    c.flags = kOpTakeGrad;
+                    any_post = true;
+                    s.phase = M::kDone;
+                    break;
+                default:
+                    break;
+            }
+        }
+        if (any_post) {
+            upload_ctl();
+            bl_accept(topo, d_ctl, d_z, d_g, d_zeval, d_geval, d_S, d_Y, 6LL * N, d_best, d_part, d_dots3, stream);
+            if (any_accept) {
+                d2h(hp.dots3, d_dots3, 3 * size_t(I), stream);
+                sync();
+            }
+        }
+        // accepted steps: curvature pair (sim.cpp:205-206), current point, best point
+        for (int i = 0; i < I; i++) {
+            M& s = mins[size_t(i)];
+            if (s.phase == M::kTrial && (hp.ctl[i].flags & kOpAccept)) {
+                if (H > 0) {
+                    const double sy = hp.dots3[3 * i], ss = hp.dots3[3 * i + 1], yy = hp.dots3[3 * i + 2];
+                    if (sy > 1e-12 * std::sqrt(std::max(1e-30, ss * yy))) {
+                        hp.rho[size_t(i) * H + s.target] = 1 / sy;
+                        if (s.m == H) s.head = (s.head + 1) % H;
+                        else s.m++;
+                    } else {
+                        s.m = 0;
+                    }
+                }
+                s.cur = s.cand;
+                s.cur_rms = s.cand.rms;
+                s.cur_max = s.cand.gmax;
+                if (s.cur.energy < s.best_energy) s.best_energy = s.cur.energy;
+                s.retry = false;
+                s.it++;
+                s.phase = M::kIterate;
+            }
+            if (s.phase == M::kIterate) iterate(s);
+        }
         check_launch();
-        return st;
+        return true;
     }
 
-    // ---- Simulator::commit, MC/src/sim.cpp:212 --------------------------------------------
-    void commit() {
-        if (!have_final) throw Fail(MCG_ERR_STATE, "commit without a preceding minimize");
+    // Steps the minimizations started with start_minimize until all are done.
+    void minimize_all() {
+        while (minimize_round()) {
+        }
+    }
+
+    // ---- Simulator::commit, MC/src/sim.cpp:212, for the instances with m[i] != 0 ----------
+    void commit(const std::vector<uint8_t>& m) {
+        h2d(d_mask, m.data(), size_t(I), stream);
         PhysParams p = phys;
         launch_state(topo, p, d_zfinal, d_baseX, d_baseR, ev, stream);
         if (mixed) {
-            launch_commit(N, B, ev, d_baseX, d_baseR, nullptr, stream);
-            launch_plastic_mixed(B, nullptr, ev.trial_nextf, mb, stream);
-            launch_plastic_mixed_to_f64(B, mb, d_plastic, stream);
+            launch_commit(topo, d_mask, ev, d_baseX, d_baseR, nullptr, stream);
+            launch_plastic_mixed(topo, d_mask, nullptr, ev.trial_nextf, mb, stream);
+            launch_plastic_mixed_to_f64(topo, d_mask, mb, d_plastic, stream);
         } else {
-            launch_commit(N, B, ev, d_baseX, d_baseR, d_plastic, stream);
+            launch_commit(topo, d_mask, ev, d_baseX, d_baseR, d_plastic, stream);
         }
         rebase();
-        have_final = false;
         check_launch();
+        sync();  // the mask is pageable host memory
     }
 
-    double top_y(double s, bool loading) const {
-        const double compressed = geom.top0 - cfg.max_strain * geom.height;
+    double top_y(const mcg_geometry& g, double s, bool loading) const {
+        const double compressed = g.top0 - cfg.max_strain * g.height;
         const double t = std::max(0.0, std::min(1.0, s));
-        return loading ? geom.top0 * (1.0 - t) + compressed * t : compressed * (1.0 - t) + geom.top0 * t;
+        return loading ? g.top0 * (1.0 - t) + compressed * t : compressed * (1.0 - t) + g.top0 * t;
     }
 
     // ---- Simulator::diagnostics, MC/src/sim.cpp:312-372 -------------------------------------
-    mcg_frame diagnostics(double time, double top, bool loading, const EvalOut& o, const HostStats& s) {
+    // Reads the plastic statistics and node boxes of all instances after a commit.
+    void read_diagnostics() {
+        launch_plastic_stats(topo, d_plastic, d_part, d_pstats, stream);
+        d2h(hp.pstats, d_pstats, 6 * size_t(I), stream);
+        d2h(hp.cen, ev.cen, 9 * size_t(I + 1), stream);
+        sync();
+    }
+    mcg_frame diagnostics(int i, const Runner& r, double time, double top, bool loading, const EvalOut& o,
+                          const HostStats& s) const {
+        const mcg_geometry& g = inst[size_t(i)].geom;
+        const int Bi = inst[size_t(i)].B;
         mcg_frame d;
         std::memset(&d, 0, sizeof(d));
         d.time = time;
         d.platen_y = top;
-        d.displacement = geom.top0 - top;
-        d.engineering_strain = d.displacement / std::max(1e-12, geom.height);
-        d.reaction_force = std::max(0.0, o.reaction - reactionOffset);
-        d.engineering_stress = d.reaction_force / std::max(1e-12, geom.area);
-        d.loading_work = loadingWork;
-        d.recovered_work = recoveredWork;
-        d.dissipated_work = std::max(0.0, loadingWork - recoveredWork);
-        d.specific_energy_absorption = d.dissipated_work / std::max(1e-12, geom.mass);
+        d.displacement = g.top0 - top;
+        d.engineering_strain = d.displacement / std::max(1e-12, g.height);
+        d.reaction_force = std::max(0.0, o.reaction - r.reactionOffset);
+        d.engineering_stress = d.reaction_force / std::max(1e-12, g.area);
+        d.loading_work = r.loadingWork;
+        d.recovered_work = r.recoveredWork;
+        d.dissipated_work = std::max(0.0, r.loadingWork - r.recoveredWork);
+        d.specific_energy_absorption = d.dissipated_work / std::max(1e-12, g.mass);
         d.elastic_energy = o.elastic;
         d.plastic_dissipation = o.plastic;
         d.contact_energy = o.contact;
@@ -486,81 +703,128 @@ struct mcg_ctx {
         d.iterations = s.iterations;
         d.converged = s.converged;
         d.loading = loading;
-        // plastic statistics and the node height extent of the committed state
-        double ps[8];
-        launch_plastic_stats(B, d_plastic, d_part, d_stats, stream);
-        ck(cudaMemcpyAsync(ps, d_stats, 6 * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
-        double box[9];
-        ck(cudaMemcpyAsync(box, ev.cen, 9 * sizeof(double), cudaMemcpyDeviceToHost, stream), "copy");
-        sync();
-        if (B > 0) {
-            d.mean_plastic_strain = ps[0] / B;
+        const double* ps = hp.pstats + 6 * size_t(i);
+        if (Bi > 0) {
+            d.mean_plastic_strain = ps[0] / Bi;
             d.max_plastic_strain = ps[1];
-            d.mean_plastic_rotation = ps[2] / B;
+            d.mean_plastic_rotation = ps[2] / Bi;
             d.max_plastic_rotation = ps[3];
         }
         d.plastic_beams = int(ps[4]);
         d.plastic_hinges = int(ps[5]);
+        const double* box = hp.cen + 9 * size_t(i);
         const double currentHeight = std::max(0.0, box[7] - box[4]);
-        d.permanent_set = std::max(0.0, 1.0 - currentHeight / std::max(1e-12, geom.height));
+        d.permanent_set = std::max(0.0, 1.0 - currentHeight / std::max(1e-12, g.height));
         return d;
     }
 
-    // ---- Simulator::run, MC/src/sim.cpp:374-467 ----------------------------------------------
-    int run(std::vector<mcg_frame>& frames, bool verbose) {
-        loadingWork = recoveredWork = prevDisp = prevForce = reactionOffset = 0;
-        double time = 0, currentTop = geom.top0;
-        bool first = true;
-        int accepted = 0;
-        const long long n = 6LL * N;
-        std::function<void(double, bool, int)> advanceTo = [&](double targetTop, bool loading, int refinement) {
-            ck(cudaMemsetAsync(d_z, 0, size_t(n) * sizeof(double), stream), "memset");
-            EvalOut fin{};
-            const HostStats stats = minimize(targetTop, fin);
-            const bool acceptable = stats.converged && fin.max_pen <= cfg.penetration_tolerance && std::isfinite(fin.energy);
-            if (!acceptable && refinement < cfg.max_adaptive_refinements && std::abs(targetTop - currentTop) > 2.5e-5) {
-                const double midpoint = 0.5 * (currentTop + targetTop);
-                advanceTo(midpoint, loading, refinement + 1);
-                advanceTo(targetTop, loading, refinement + 1);
-                return;
+    // ---- Simulator::run, MC/src/sim.cpp:374-467, for every instance ---------------------------
+    // advanceTo's recursion (bisection of a failed increment) is an explicit stack per
+    // instance: a failed target is replaced by its midpoint followed by itself.
+    void run(std::vector<Runner>& rs, bool verbose) {
+        rs.assign(size_t(I), Runner{});
+        for (int i = 0; i < I; i++) {
+            rs[size_t(i)].currentTop = inst[size_t(i)].geom.top0;
+            mins[size_t(i)] = Minimizer{};
+        }
+        have_final = false;
+        auto next_task = [&](int i) -> bool {
+            Runner& r = rs[size_t(i)];
+            const mcg_geometry& g = inst[size_t(i)].geom;
+            if (!r.stack.empty()) {
+                r.task = r.stack.back();
+                r.stack.pop_back();
+                return true;
             }
-            if (!acceptable) {
+            const int L = cfg.load_steps, U = cfg.unload_steps;
+            const int k = r.next_step++;
+            if (k == 0) r.task = Task{g.top0, true, 0};
+            else if (k <= L) r.task = Task{top_y(g, double(k) / std::max(1, L), true), true, 0};
+            else if (k <= L + U) r.task = Task{top_y(g, double(k - L) / std::max(1, U), false), false, 0};
+            else return false;
+            return true;
+        };
+        std::vector<uint8_t> cm(size_t(I), 0);
+        for (;;) {
+            bool pending = false;
+            for (int i = 0; i < I; i++) {
+                Runner& r = rs[size_t(i)];
+                if (r.done) continue;
+                if (mins[size_t(i)].phase == Minimizer::kIdle) {
+                    if (!next_task(i)) {
+                        r.done = true;
+                        continue;
+                    }
+                    start_minimize(i, r.task.top, true);
+                }
+                pending = true;
+            }
+            if (!pending) break;
+            minimize_round();
+            bool any_commit = false;
+            std::fill(cm.begin(), cm.end(), uint8_t(0));
+            for (int i = 0; i < I; i++) {
+                Minimizer& s = mins[size_t(i)];
+                if (s.phase != Minimizer::kDone) continue;
+                Runner& r = rs[size_t(i)];
+                const Task t = r.task;
+                const bool acceptable = s.st.converged && s.fin.max_pen <= cfg.penetration_tolerance &&
+                                        std::isfinite(s.fin.energy);
+                if (acceptable) {
+                    cm[size_t(i)] = 1;
+                    any_commit = true;
+                    continue;
+                }
+                s.phase = Minimizer::kIdle;
+                if (t.refinement < cfg.max_adaptive_refinements && std::abs(t.top - r.currentTop) > 2.5e-5) {
+                    const double midpoint = 0.5 * (r.currentTop + t.top);
+                    r.stack.push_back(Task{t.top, t.loading, t.refinement + 1});
+                    r.stack.push_back(Task{midpoint, t.loading, t.refinement + 1});
+                    continue;
+                }
                 char msg[256];
                 std::snprintf(msg, sizeof msg,
-                              "quasi-static equilibrium failed at platen=%g m, residual=%g, penetration=%g mm after %d iterations",
-                              targetTop, stats.rms, fin.max_pen * 1000.0, stats.iterations);
-                throw Fail(MCG_ERR_EQUILIBRIUM, msg);
+                              "quasi-static equilibrium failed at platen=%g m, residual=%g, penetration=%g mm after %d "
+                              "iterations",
+                              t.top, s.st.rms, s.fin.max_pen * 1000.0, s.st.iterations);
+                r.status = MCG_ERR_EQUILIBRIUM;
+                r.error = msg;
+                r.done = true;
             }
-            commit();
-            if (first) reactionOffset = fin.reaction;
-            const double force = std::max(0.0, fin.reaction - reactionOffset);
-            const double displacement = geom.top0 - targetTop;
-            if (!first) {
-                const double dd = displacement - prevDisp;
-                const double work = 0.5 * (prevForce + force) * dd;
-                if (dd >= 0.0) loadingWork += std::max(0.0, work);
-                else recoveredWork += std::max(0.0, -work);
+            if (!any_commit) continue;
+            commit(cm);
+            read_diagnostics();
+            for (int i = 0; i < I; i++) {
+                if (!cm[size_t(i)]) continue;
+                Minimizer& s = mins[size_t(i)];
+                Runner& r = rs[size_t(i)];
+                const Task t = r.task;
+                if (r.first) r.reactionOffset = s.fin.reaction;
+                const double force = std::max(0.0, s.fin.reaction - r.reactionOffset);
+                const double displacement = inst[size_t(i)].geom.top0 - t.top;
+                if (!r.first) {
+                    const double dd = displacement - r.prevDisp;
+                    const double work = 0.5 * (r.prevForce + force) * dd;
+                    if (dd >= 0.0) r.loadingWork += std::max(0.0, work);
+                    else r.recoveredWork += std::max(0.0, -work);
+                }
+                r.prevDisp = displacement;
+                r.prevForce = force;
+                r.currentTop = t.top;
+                mcg_frame d = diagnostics(i, r, r.time, t.top, t.loading, s.fin, s.st);
+                d.refinement = t.refinement;
+                r.frames.push_back(d);
+                if (verbose)
+                    std::printf("[equilibrium] %3d %s strain=%.4f force=%.3f N residual=%.2e pen=%.3f mm iter=%d %s\n",
+                                r.accepted, t.loading ? "load  " : "unload", d.engineering_strain, d.reaction_force,
+                                d.residual_rms, d.max_penetration * 1000.0, d.iterations,
+                                t.refinement ? "[REFINED]" : "[OK]");
+                r.accepted++;
+                r.first = false;
+                r.time += cfg.step_time;
+                s.phase = Minimizer::kIdle;
             }
-            prevDisp = displacement;
-            prevForce = force;
-            currentTop = targetTop;
-            mcg_frame d = diagnostics(time, targetTop, loading, fin, stats);
-            d.refinement = refinement;
-            frames.push_back(d);
-            if (verbose)
-                std::printf("[equilibrium] %3d %s strain=%.4f force=%.3f N residual=%.2e pen=%.3f mm iter=%d %s\n",
-                            accepted, loading ? "load  " : "unload", d.engineering_strain, d.reaction_force,
-                            d.residual_rms, d.max_penetration * 1000.0, d.iterations, refinement ? "[REFINED]" : "[OK]");
-            accepted++;
-            first = false;
-            time += cfg.step_time;
-        };
-        advanceTo(geom.top0, true, 0);
-        for (int step = 1; step <= cfg.load_steps; ++step)
-            advanceTo(top_y(double(step) / std::max(1, cfg.load_steps), true), true, 0);
-        for (int step = 1; step <= cfg.unload_steps; ++step)
-            advanceTo(top_y(double(step) / std::max(1, cfg.unload_steps), false), false, 0);
-        return MCG_OK;
+        }
     }
 };
 
@@ -591,14 +855,408 @@ int guarded(mcg_ctx* c, F&& f) {
 void need_topo(const mcg_ctx* c) {
     if (!c->have_topo) throw Fail(MCG_ERR_STATE, "no topology uploaded");
 }
-
-template <class T>
-void h2d(T* d, const T* h, size_t n, cudaStream_t s) {
-    ck(cudaMemcpyAsync(d, h, n * sizeof(T), cudaMemcpyHostToDevice, s), "copy to device");
+void need_single(const mcg_ctx* c) {
+    need_topo(c);
+    if (c->I != 1) throw Fail(MCG_ERR_STATE, "a batched context: use the mcg_batch_* functions");
 }
-template <class T>
-void d2h(T* h, const T* d, size_t n, cudaStream_t s) {
-    ck(cudaMemcpyAsync(h, d, n * sizeof(T), cudaMemcpyDeviceToHost, s), "copy to host");
+
+// Builds the device model of one or more instances (stored one after another).
+void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
+    const mcg_config& cf = c->cfg;
+    const int I = int(ins.size());
+    if (I <= 0) throw Fail(MCG_ERR_INVALID, "no instance");
+    long long Nt = 0, Bt = 0;
+    for (int k = 0; k < I; k++) {
+        const mcg_topology* t = ins[size_t(k)].t;
+        if (!t || !ins[size_t(k)].g) throw Fail(MCG_ERR_INVALID, "null topology or geometry");
+        if (t->n_nodes <= 0 || t->n_beams < 0)
+            throw Fail(MCG_ERR_INVALID, "node count must be positive and beam count non-negative");
+        if (t->n_beams > 0 &&
+            (!t->beam_a || !t->beam_b || !t->L0 || !t->radius || !t->area || !t->I || !t->J || !t->e0))
+            throw Fail(MCG_ERR_INVALID, "missing beam array");
+        if (!t->mass || !t->locked) throw Fail(MCG_ERR_INVALID, "missing node array");
+        if (t->n_connected < 0 || (t->n_connected > 0 && !t->connected))
+            throw Fail(MCG_ERR_INVALID, "bad connected list");
+        if (!(ins[size_t(k)].sy > 0) || !std::isfinite(ins[size_t(k)].sy))
+            throw Fail(MCG_ERR_INVALID, "yield stress must be positive");
+        Nt += t->n_nodes;
+        Bt += t->n_beams;
+    }
+    if (Nt + Bt >= (1LL << 31) / 4) throw Fail(MCG_ERR_INVALID, "model too large for 32-bit shape indices");
+    const int N = int(Nt), B = int(Bt);
+    const double E = cf.material.young, G = E / (2 * (1 + cf.material.nu));
+    std::vector<int2> ab(static_cast<size_t>(B));
+    std::vector<double> kb(B), kt(B), my(B), ty(B), hb(B), ht(B), cs(B), aL(B), aLsy(B), syb(B);
+    std::vector<double> invL0(B), inv_kbh(B), inv_kth(B);
+    std::vector<double> e0x(B), e0y(B), e0z(B), L0v(B), areav(B), radv(B), massv(N);
+    std::vector<uint8_t> lockedv(6 * size_t(N));
+    std::vector<float> padf(B);
+    double rmax = cf.joint_scale * cf.max_radius;
+    std::vector<int> deg(size_t(N) + 1, 0);
+    std::vector<InstHost> ih(static_cast<size_t>(I));
+    std::vector<std::vector<int>> adj(static_cast<size_t>(N));
+    int node0 = 0, beam0 = 0;
+    for (int k = 0; k < I; k++) {
+        const mcg_topology* t = ins[size_t(k)].t;
+        const int Ni = t->n_nodes, Bi = t->n_beams;
+        const double sy = ins[size_t(k)].sy;
+        InstHost& h = ih[size_t(k)];
+        h.node0 = node0;
+        h.N = Ni;
+        h.beam0 = beam0;
+        h.B = Bi;
+        h.geom = *ins[size_t(k)].g;
+        h.sy = sy;
+        for (int b = 0; b < Bi; b++) {
+            const int a = t->beam_a[b], bb = t->beam_b[b];
+            if (a < 0 || a >= Ni || bb < 0 || bb >= Ni || a == bb)
+                throw Fail(MCG_ERR_INVALID, "beam " + std::to_string(b) + " has invalid end nodes");
+            const double L0 = t->L0[b], r = t->radius[b];
+            if (!(L0 > 0) || !std::isfinite(L0) || !(r > 0) || !std::isfinite(r) || !std::isfinite(t->area[b]) ||
+                !std::isfinite(t->I[b]) || !std::isfinite(t->J[b]))
+                throw Fail(MCG_ERR_INVALID, "beam " + std::to_string(b) + " has invalid section data");
+            const size_t g = size_t(beam0 + b);
+            ab[g] = make_int2(node0 + a, node0 + bb);
+            deg[size_t(node0 + a)]++;
+            deg[size_t(node0 + bb)]++;
+            // Section constants, evaluated with the reference's expressions
+            // (sim.cpp:139-141); this file is compiled without FMA contraction, so the
+            // values equal the ones the reference recomputes on every call.
+            const double area = t->area[b], Is = t->I[b], J = t->J[b];
+            kb[g] = E * Is / L0;
+            kt[g] = G * J / L0;
+            my[g] = sy * Is / r;
+            ty[g] = (sy / std::sqrt(3.0)) * J / r;
+            hb[g] = cf.material.bend_hardening * kb[g];
+            ht[g] = cf.material.torsion_hardening * kt[g];
+            cs[g] = .5 * cf.shear_correction * G * area * L0;
+            aL[g] = area * L0;
+            aLsy[g] = area * L0 * sy;
+            syb[g] = sy;
+            invL0[g] = 1.0 / L0;
+            inv_kbh[g] = 1.0 / std::max(1e-20, kb[g] + hb[g]);
+            inv_kth[g] = 1.0 / std::max(1e-20, kt[g] + ht[g]);
+            e0x[g] = t->e0[3 * size_t(b)];
+            e0y[g] = t->e0[3 * size_t(b) + 1];
+            e0z[g] = t->e0[3 * size_t(b) + 2];
+            L0v[g] = L0;
+            areav[g] = area;
+            radv[g] = r;
+            rmax = std::max(rmax, r);
+            padf[g] = round_up_float(r + cf.contact_margin);
+        }
+        for (int i = 0; i < Ni; i++) {
+            if (!std::isfinite(t->mass[i])) throw Fail(MCG_ERR_INVALID, "non-finite node mass");
+            massv[size_t(node0 + i)] = t->mass[i];
+        }
+        long long nfree = 0;
+        for (long long q = 0; q < 6LL * Ni; q++) {
+            if (t->locked[q] > 1) throw Fail(MCG_ERR_INVALID, "locked flags must be 0 or 1");
+            nfree += t->locked[q] ? 0 : 1;
+            lockedv[size_t(6LL * node0 + q)] = t->locked[q];
+        }
+        h.n_free = nfree;
+        for (int64_t q = 0; q < t->n_connected; q++) {
+            const uint64_t key = t->connected[q];
+            const uint32_t u = uint32_t(key >> 32), v = uint32_t(key & 0xffffffffu);
+            if (u >= uint32_t(Ni) || v >= uint32_t(Ni) || u > v)
+                throw Fail(MCG_ERR_INVALID, "connected key " + std::to_string(q) + " is not a node pair key");
+            adj[size_t(node0) + u].push_back(int(node0 + v));
+            if (u != v) adj[size_t(node0) + v].push_back(int(node0 + u));
+        }
+        node0 += Ni;
+        beam0 += Bi;
+    }
+    // incidence CSR in ascending beam order (the reference's scatter order)
+    std::vector<int> inc_start(size_t(N) + 1, 0), inc(2 * size_t(B));
+    for (int i = 0; i < N; i++) inc_start[size_t(i) + 1] = inc_start[size_t(i)] + deg[size_t(i)];
+    {
+        std::vector<int> cur(inc_start.begin(), inc_start.end() - 1);
+        for (int b = 0; b < B; b++) {
+            inc[size_t(cur[size_t(ab[size_t(b)].x)]++)] = (b << 1) | 0;
+            inc[size_t(cur[size_t(ab[size_t(b)].y)]++)] = (b << 1) | 1;
+        }
+    }
+    // connected pairs as an open-addressing hash set (at most half full)
+    long long npairs = 0;
+    for (int i = 0; i < N; i++) {
+        auto& l = adj[size_t(i)];
+        std::sort(l.begin(), l.end());
+        l.erase(std::unique(l.begin(), l.end()), l.end());
+        for (int v : l) npairs += v >= i ? 1 : 0;
+    }
+    int hbits = 4;
+    while ((1LL << hbits) < 2 * npairs) hbits++;
+    std::vector<unsigned long long> conn_hash(size_t(1) << hbits, ~0ull);
+    const unsigned long long hmask = (1ull << hbits) - 1;
+    for (int i = 0; i < N; i++)
+        for (int v : adj[size_t(i)]) {
+            if (v < i) continue;
+            const unsigned long long key = ((unsigned long long)i << 32) | uint32_t(v);
+            unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> (64 - hbits);
+            while (conn_hash[h] != ~0ull) h = (h + 1) & hmask;
+            conn_hash[h] = key;
+        }
+    // blocks that never straddle two instances
+    std::vector<int4> nblk, bblk, irange(static_cast<size_t>(I));
+    for (int k = 0; k < I; k++) {
+        const InstHost& h = ih[size_t(k)];
+        irange[size_t(k)].x = int(nblk.size());
+        for (int f = 0; f < h.N; f += kMapBlock)
+            nblk.push_back(make_int4(h.node0 + f, std::min(kMapBlock, h.N - f), k, 0));
+        irange[size_t(k)].y = int(nblk.size());
+        irange[size_t(k)].z = int(bblk.size());
+        for (int f = 0; f < h.B; f += kMapBlock)
+            bblk.push_back(make_int4(h.beam0 + f, std::min(kMapBlock, h.B - f), k, 0));
+        irange[size_t(k)].w = int(bblk.size());
+    }
+    // contact-grid offsets: instances side by side in x and z, far enough apart that no
+    // cell holds shapes of two instances (a lattice may widen under compression)
+    {
+        double span = 0;
+        for (int k = 0; k < I; k++) {
+            const InstIn& in = ins[size_t(k)];
+            if (!in.x0) continue;
+            for (int i = 0; i < in.t->n_nodes; i++)
+                span = std::max({span, std::abs(in.x0[3 * size_t(i)]), std::abs(in.x0[3 * size_t(i) + 2])});
+        }
+        const double pitch = std::ceil((4 * span + 8 * rmax + 0.01) * 1024.0) / 1024.0;  // exact in FP32
+        const int cols = int(std::ceil(std::sqrt(double(I))));
+        for (int k = 0; k < I; k++)
+            ih[size_t(k)].off = I == 1 ? float2{0.f, 0.f}
+                                       : float2{float(pitch * (k % cols)), float(pitch * (k / cols))};
+    }
+
+    c->sync();
+    c->topo_mem.release();
+    c->eval_mem.release();
+    c->contact_mem.release();
+    c->solver_mem.release();
+    c->have_topo = false;
+    c->have_final = false;
+    c->N = N;
+    c->B = B;
+    c->I = I;
+    c->inst = ih;
+    c->jr = cf.joint_scale * cf.max_radius;
+    c->rmax = rmax;
+    c->H = std::max(cf.history, 0);
+    c->hp.alloc(I, c->H);
+    cudaStream_t s = c->stream;
+    DevArena& M = c->topo_mem;
+    DevTopo T{};
+    T.N = N;
+    T.B = B;
+    auto upd = [&](const std::vector<double>& v) {
+        double* d = M.get<double>(v.size());
+        h2d(d, v.data(), v.size(), s);
+        return static_cast<const double*>(d);
+    };
+    int2* dab = M.get<int2>(size_t(B));
+    h2d(dab, ab.data(), size_t(B), s);
+    T.ab = dab;
+    T.L0 = upd(L0v);
+    T.area = upd(areav);
+    T.radius = upd(radv);
+    T.e0x = upd(e0x); T.e0y = upd(e0y); T.e0z = upd(e0z);
+    T.kb = upd(kb); T.kt = upd(kt); T.my = upd(my); T.ty = upd(ty); T.hb = upd(hb); T.ht = upd(ht);
+    T.cs = upd(cs); T.aL = upd(aL); T.aLsy = upd(aLsy);
+    T.invL0 = upd(invL0); T.inv_kbh = upd(inv_kbh); T.inv_kth = upd(inv_kth);
+    T.sy = upd(syb);
+    T.mass = upd(massv);
+    uint8_t* dl = M.get<uint8_t>(6 * size_t(N));
+    h2d(dl, lockedv.data(), 6 * size_t(N), s);
+    T.locked = dl;
+    int* dis = M.get<int>(inc_start.size());
+    h2d(dis, inc_start.data(), inc_start.size(), s);
+    T.inc_start = dis;
+    int* di = M.get<int>(inc.size());
+    h2d(di, inc.data(), inc.size(), s);
+    T.inc = di;
+    {
+        unsigned long long* dh = M.get<unsigned long long>(conn_hash.size());
+        h2d(dh, conn_hash.data(), conn_hash.size(), s);
+        T.conn_hash = dh;
+        T.conn_mask = hmask;
+        T.conn_shift = 64 - hbits;
+    }
+    {
+        float* dp = M.get<float>(size_t(B));
+        h2d(dp, padf.data(), size_t(B), s);
+        T.padf = dp;
+    }
+    T.I = I;
+    T.n_nblk = int(nblk.size());
+    T.n_bblk = int(bblk.size());
+    {
+        int4* d = M.get<int4>(nblk.size());
+        h2d(d, nblk.data(), nblk.size(), s);
+        T.nblk = d;
+        int4* e = M.get<int4>(bblk.size());
+        h2d(e, bblk.data(), bblk.size(), s);
+        T.bblk = e;
+        int4* r = M.get<int4>(irange.size());
+        h2d(r, irange.data(), irange.size(), s);
+        T.irange = r;
+        std::vector<int> nn(static_cast<size_t>(I));
+        std::vector<long long> nf(static_cast<size_t>(I));
+        std::vector<float2> off(static_cast<size_t>(I));
+        for (int k = 0; k < I; k++) {
+            nn[size_t(k)] = ih[size_t(k)].N;
+            nf[size_t(k)] = ih[size_t(k)].n_free;
+            off[size_t(k)] = ih[size_t(k)].off;
+        }
+        int* dn = M.get<int>(nn.size());
+        h2d(dn, nn.data(), nn.size(), s);
+        T.inst_n = dn;
+        long long* dnf = M.get<long long>(nf.size());
+        h2d(dnf, nf.data(), nf.size(), s);
+        T.inst_free = dnf;
+        float2* doff = M.get<float2>(off.size());
+        h2d(doff, off.data(), off.size(), s);
+        T.off = doff;
+        c->sync();  // the host vectors above go out of scope
+    }
+    c->topo = T;
+    c->mat = Material{E, G, cf.material.yield, cf.material.hardening, cf.material.bend_hardening,
+                      cf.material.torsion_hardening, 1.0 / std::max(1e-20, E + cf.material.hardening)};
+    PhysParams P{};
+    P.translation_scale = cf.translation_scale;
+    P.gravity = cf.gravity;
+    P.centering = cf.centering_stiffness;
+    P.contact_k = cf.contact_stiffness;
+    P.contact_margin = cf.contact_margin;
+    P.joint_radius = c->jr;
+    P.broad_cell = std::max(2.8 * c->jr, .72 * cf.cell_size);
+    P.top = ih[0].geom.top0;
+    P.self_contact = cf.self_contact ? 1 : 0;
+    P.joint_padf = round_up_float(c->jr + cf.contact_margin);
+    c->phys = P;
+    // state
+    c->d_baseX = M.get<double>(3 * size_t(N));
+    c->d_baseR = M.get<double>(4 * size_t(N));
+    c->d_plastic = M.get<double>(7 * size_t(B));
+    ck(cudaMemsetAsync(c->d_plastic, 0, 7 * size_t(B) * sizeof(double), s), "memset");
+    {
+        std::vector<double> x(3 * size_t(N), 0.0), r(4 * size_t(N), 0.0);
+        bool have_x = true;
+        for (int k = 0; k < I; k++) {
+            const InstIn& in = ins[size_t(k)];
+            const InstHost& h = ih[size_t(k)];
+            have_x &= in.x0 != nullptr;
+            if (in.x0) std::copy(in.x0, in.x0 + 3 * size_t(h.N), x.begin() + 3 * size_t(h.node0));
+            for (int i = 0; i < h.N; i++) {
+                double* q = r.data() + 4 * size_t(h.node0 + i);
+                if (in.r0) std::copy(in.r0 + 4 * size_t(i), in.r0 + 4 * size_t(i) + 4, q);
+                else q[0] = 1.0;
+            }
+        }
+        if (have_x) h2d(c->d_baseX, x.data(), x.size(), s);
+        h2d(c->d_baseR, r.data(), r.size(), s);
+        c->sync();
+    }
+    // evaluation buffers
+    DevArena& V = c->eval_mem;
+    EvalBufs e{};
+    e.x = V.get<double4_32a>(size_t(N));
+    e.R = V.get<double4_32a>(size_t(N));
+    e.M = V.get<double4_32a>(3 * size_t(N));
+    e.xf_lo = V.get<float4>(size_t(N));
+    e.xf_hi = V.get<float4>(size_t(N));
+    e.slotA = V.get<double>(6 * size_t(B));
+    e.slotB = V.get<double>(6 * size_t(B));
+    e.part_state = V.get<double>(9 * size_t(T.n_nblk));
+    e.part_beam = V.get<double>(3 * size_t(std::max(T.n_bblk, 1)));
+    e.part_node = V.get<double>(kNodeParts * size_t(T.n_nblk));
+    e.cen = V.get<double>(9 * size_t(I + 1));
+    e.tops = V.get<double>(size_t(I));
+    e.out = V.get<EvalOut>(size_t(I));
+    e.trial_next = V.get<double>(7 * size_t(B));
+    e.trial_aux = V.get<double>(7 * size_t(B));
+    e.trial_flags = V.get<uint8_t>(3 * size_t(B));
+    c->mixed = cf.precision == MCG_MIXED;
+    if (c->mixed) {
+        e.slotAf = V.get<float>(6 * size_t(B));
+        e.slotBf = V.get<float>(6 * size_t(B));
+        e.trial_nextf = V.get<float>(7 * size_t(B));
+        e.trial_auxf = V.get<float>(7 * size_t(B));
+        MixedBeams mb{};
+        float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B3, &mb.B4, &mb.B5, &mb.C0, &mb.C1, &mb.P0, &mb.P1};
+        for (float4** f : fields) *f = V.get<float4>(size_t(B));
+        c->mb = mb;
+        c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
+    }
+    c->ev = e;
+    for (int k = 0; k < I; k++) c->hp.tops[k] = ih[size_t(k)].geom.top0;
+    c->upload_tops();
+    c->d_zin = V.get<double>(6 * size_t(N));
+    c->d_grad = V.get<double>(6 * size_t(N));
+    ck(cudaMemsetAsync(c->d_zin, 0, 6 * size_t(N) * sizeof(double), s), "memset");
+    // contact buffers: a first guess, grown on demand
+    const long long S = (long long)N + B;
+    c->broad_cell = P.broad_cell;
+    c->contact_skin = float(0.125 * cf.cell_size);
+    {
+        // bins: the Morton range of the rest-state extent (in the grid's frame) with room to
+        // grow, or row-major bins when that range is too large
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        bool any = false;
+        for (int k = 0; k < I; k++) {
+            const InstIn& in = ins[size_t(k)];
+            if (!in.x0) continue;
+            any = true;
+            const double o[3] = {ih[size_t(k)].off.x, 0.0, ih[size_t(k)].off.y};
+            for (int i = 0; i < in.t->n_nodes; i++)
+                for (int d = 0; d < 3; d++) {
+                    lo[d] = std::min(lo[d], in.x0[3 * size_t(i) + d] + o[d]);
+                    hi[d] = std::max(hi[d], in.x0[3 * size_t(i) + d] + o[d]);
+                }
+        }
+        long long dims[3] = {8, 8, 8};
+        long long dmax = 8;
+        if (any)
+            for (int d = 0; d < 3; d++) {
+                dims[d] = (long long)((hi[d] - lo[d] + 2 * c->rmax) / P.broad_cell * 1.15) + 4;
+                dmax = std::max(dmax, dims[d]);
+            }
+        int bits = 3;
+        while ((1LL << bits) < dmax && bits < 10) bits++;
+        long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
+        if ((1LL << bits) < dmax) bin_cap = std::min(dims[0] * dims[1] * dims[2], 1LL << 28);
+        c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap, 1024);
+    }
+    // solver vectors
+    DevArena& Q = c->solver_mem;
+    const size_t n = 6 * size_t(N);
+    const int Hs = std::max(c->H, 1);
+    c->d_z = Q.get<double>(n); c->d_zeval = Q.get<double>(n); c->d_p = Q.get<double>(n);
+    c->d_g = Q.get<double>(n); c->d_geval = Q.get<double>(n); c->d_best = Q.get<double>(n);
+    c->d_zfinal = Q.get<double>(n);
+    c->d_S = Q.get<double>(size_t(Hs) * n);
+    c->d_Y = Q.get<double>(size_t(Hs) * n);
+    c->d_rho = Q.get<double>(size_t(I) * Hs);
+    c->d_alpha = Q.get<double>(size_t(I) * Hs);
+    c->d_part = Q.get<double>(std::max(lbfgs_part_doubles(std::max(T.n_nblk, T.n_bblk)), 6 * size_t(T.n_bblk) + 8));
+    c->d_dg = Q.get<double>(size_t(I));
+    c->d_dots3 = Q.get<double>(3 * size_t(I));
+    c->d_pstats = Q.get<double>(6 * size_t(I));
+    c->d_ctl = Q.get<SolveCtl>(size_t(I));
+    c->d_mask = Q.get<uint8_t>(size_t(I));
+    c->mins.assign(size_t(I), Minimizer{});
+    ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
+    if (c->mixed) {
+        launch_mixed_constants(c->topo, c->mb, s);
+        launch_plastic_mixed(c->topo, nullptr, c->d_plastic, nullptr, c->mb, s);
+        c->rebase();
+    }
+    c->sync();
+    c->have_topo = true;
+}
+
+void fill_diag(mcg_diag* d, const EvalOut& o) {
+    if (!d) return;
+    d->elastic = o.elastic; d->plastic = o.plastic; d->contact = o.contact;
+    d->reaction = o.reaction; d->max_pen = o.max_pen; d->contacts = o.contacts; d->pad_ = 0;
 }
 
 }  // namespace
@@ -642,7 +1300,8 @@ int mcg_create(const mcg_config* cfg, int device, mcg_ctx** out) {
     if (!cfg || !out) return MCG_ERR_INVALID;
     *out = nullptr;
     if (cfg->precision != MCG_FP64 && cfg->precision != MCG_MIXED) return MCG_ERR_INVALID;
-    if (!(cfg->translation_scale > 0) || cfg->history < 0 || cfg->max_line_search < 0) return MCG_ERR_INVALID;
+    if (!(cfg->translation_scale > 0) || cfg->history < 0 || cfg->history > 64 || cfg->max_line_search < 0)
+        return MCG_ERR_INVALID;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
         cudaGetLastError();
@@ -656,7 +1315,7 @@ int mcg_create(const mcg_config* cfg, int device, mcg_ctx** out) {
     try {
         c->set_device();
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        ck(cudaMallocHost(reinterpret_cast<void**>(&c->hp), sizeof(Pinned)), "cudaMallocHost");
+        c->hp.alloc(1, std::max(cfg->history, 1));
     } catch (const Fail&) {
         delete c;
         return MCG_ERR_CUDA;
@@ -673,6 +1332,7 @@ void mcg_destroy(mcg_ctx* c) {
     c->eval_mem.release();
     c->contact_mem.release();
     c->solver_mem.release();
+    c->hp.release();
     delete c;
 }
 
@@ -685,268 +1345,23 @@ int64_t mcg_launch_count(const mcg_ctx*) { return g_launch_count.load(); }
 int mcg_upload_topology(mcg_ctx* c, const mcg_topology* t, const mcg_geometry* g, const double* x0, const double* r0) {
     return guarded(c, [&] {
         if (!t || !g) throw Fail(MCG_ERR_INVALID, "null topology or geometry");
-        const int N = t->n_nodes, B = t->n_beams;
-        if (N <= 0 || B < 0) throw Fail(MCG_ERR_INVALID, "node count must be positive and beam count non-negative");
-        if ((long long)N + B >= (1LL << 31) / 4) throw Fail(MCG_ERR_INVALID, "model too large for 32-bit shape indices");
-        if (B > 0 && (!t->beam_a || !t->beam_b || !t->L0 || !t->radius || !t->area || !t->I || !t->J || !t->e0))
-            throw Fail(MCG_ERR_INVALID, "missing beam array");
-        if (!t->mass || !t->locked) throw Fail(MCG_ERR_INVALID, "missing node array");
-        if (t->n_connected < 0 || (t->n_connected > 0 && !t->connected))
-            throw Fail(MCG_ERR_INVALID, "bad connected list");
-        const mcg_config& cf = c->cfg;
-        const double E = cf.material.young, G = E / (2 * (1 + cf.material.nu)), sy = cf.material.yield;
-        std::vector<int2> ab(static_cast<size_t>(B));
-        std::vector<double> kb(B), kt(B), my(B), ty(B), hb(B), ht(B), cs(B), aL(B), aLsy(B);
-        std::vector<double> invL0(B), inv_kbh(B), inv_kth(B);
-        std::vector<double> e0x(B), e0y(B), e0z(B);
-        std::vector<float> padf(B);
-        double rmax = cf.joint_scale * cf.max_radius;
-        std::vector<int> deg(size_t(N) + 1, 0);
-        for (int b = 0; b < B; b++) {
-            const int a = t->beam_a[b], bb = t->beam_b[b];
-            if (a < 0 || a >= N || bb < 0 || bb >= N || a == bb)
-                throw Fail(MCG_ERR_INVALID, "beam " + std::to_string(b) + " has invalid end nodes");
-            const double L0 = t->L0[b], r = t->radius[b];
-            if (!(L0 > 0) || !std::isfinite(L0) || !(r > 0) || !std::isfinite(r) || !std::isfinite(t->area[b]) ||
-                !std::isfinite(t->I[b]) || !std::isfinite(t->J[b]))
-                throw Fail(MCG_ERR_INVALID, "beam " + std::to_string(b) + " has invalid section data");
-            ab[size_t(b)] = make_int2(a, bb);
-            deg[size_t(a)]++;
-            deg[size_t(bb)]++;
-            // Section constants, evaluated with the reference's expressions
-            // (sim.cpp:139-141); this file is compiled without FMA contraction, so the
-            // values equal the ones the reference recomputes on every call.
-            const double area = t->area[b], I = t->I[b], J = t->J[b];
-            kb[b] = E * I / L0;
-            kt[b] = G * J / L0;
-            my[b] = sy * I / r;
-            ty[b] = (sy / std::sqrt(3.0)) * J / r;
-            hb[b] = cf.material.bend_hardening * kb[b];
-            ht[b] = cf.material.torsion_hardening * kt[b];
-            cs[b] = .5 * cf.shear_correction * G * area * L0;
-            aL[b] = area * L0;
-            aLsy[b] = area * L0 * sy;
-            invL0[b] = 1.0 / L0;
-            inv_kbh[b] = 1.0 / std::max(1e-20, kb[b] + hb[b]);
-            inv_kth[b] = 1.0 / std::max(1e-20, kt[b] + ht[b]);
-            e0x[b] = t->e0[3 * size_t(b)];
-            e0y[b] = t->e0[3 * size_t(b) + 1];
-            e0z[b] = t->e0[3 * size_t(b) + 2];
-            rmax = std::max(rmax, r);
-            padf[b] = round_up_float(r + cf.contact_margin);
-        }
-        // incidence CSR in ascending beam order (the reference's scatter order)
-        std::vector<int> inc_start(size_t(N) + 1, 0), inc(2 * size_t(B));
-        for (int i = 0; i < N; i++) inc_start[size_t(i) + 1] = inc_start[size_t(i)] + deg[size_t(i)];
-        {
-            std::vector<int> cur(inc_start.begin(), inc_start.end() - 1);
-            for (int b = 0; b < B; b++) {
-                inc[size_t(cur[size_t(ab[size_t(b)].x)]++)] = (b << 1) | 0;
-                inc[size_t(cur[size_t(ab[size_t(b)].y)]++)] = (b << 1) | 1;
-            }
-        }
-        // connected-pair adjacency
-        std::vector<std::vector<int>> adj(static_cast<size_t>(N));
-        for (int64_t k = 0; k < t->n_connected; k++) {
-            const uint64_t key = t->connected[k];
-            const uint32_t u = uint32_t(key >> 32), v = uint32_t(key & 0xffffffffu);
-            if (u >= uint32_t(N) || v >= uint32_t(N) || u > v)
-                throw Fail(MCG_ERR_INVALID, "connected key " + std::to_string(k) + " is not a node pair key");
-            adj[u].push_back(int(v));
-            if (u != v) adj[v].push_back(int(u));
-        }
-        // connected pairs as an open-addressing hash set (at most half full)
-        long long npairs = 0;
-        for (int i = 0; i < N; i++) {
-            auto& l = adj[size_t(i)];
-            std::sort(l.begin(), l.end());
-            l.erase(std::unique(l.begin(), l.end()), l.end());
-            for (int v : l) npairs += v >= i ? 1 : 0;
-        }
-        int hbits = 4;
-        while ((1LL << hbits) < 2 * npairs) hbits++;
-        std::vector<unsigned long long> conn_hash(size_t(1) << hbits, ~0ull);
-        const unsigned long long hmask = (1ull << hbits) - 1;
-        for (int i = 0; i < N; i++)
-            for (int v : adj[size_t(i)]) {
-                if (v < i) continue;
-                const unsigned long long key = ((unsigned long long)i << 32) | uint32_t(v);
-                unsigned long long h = (key * 0x9E3779B97F4A7C15ull) >> (64 - hbits);
-                while (conn_hash[h] != ~0ull) h = (h + 1) & hmask;
-                conn_hash[h] = key;
-            }
-        long long nfree = 0;
-        for (long long k = 0; k < 6LL * N; k++) {
-            if (t->locked[k] > 1) throw Fail(MCG_ERR_INVALID, "locked flags must be 0 or 1");
-            nfree += t->locked[k] ? 0 : 1;
-        }
-        for (int i = 0; i < N; i++)
-            if (!std::isfinite(t->mass[i])) throw Fail(MCG_ERR_INVALID, "non-finite node mass");
-
-        c->sync();
-        c->topo_mem.release();
-        c->eval_mem.release();
-        c->contact_mem.release();
-        c->solver_mem.release();
-        c->have_topo = false;
-        c->have_final = false;
-        c->N = N;
-        c->B = B;
-        c->n_free = nfree;
-        c->geom = *g;
-        c->jr = cf.joint_scale * cf.max_radius;
-        c->rmax = rmax;
-        cudaStream_t s = c->stream;
-        DevArena& M = c->topo_mem;
-        DevTopo T{};
-        T.N = N;
-        T.B = B;
-        auto upd = [&](const std::vector<double>& v) {
-            double* d = M.get<double>(v.size());
-            h2d(d, v.data(), v.size(), s);
-            return static_cast<const double*>(d);
-        };
-        int2* dab = M.get<int2>(size_t(B));
-        h2d(dab, ab.data(), size_t(B), s);
-        T.ab = dab;
-        T.L0 = upd(std::vector<double>(t->L0, t->L0 + B));
-        T.area = upd(std::vector<double>(t->area, t->area + B));
-        T.radius = upd(std::vector<double>(t->radius, t->radius + B));
-        T.e0x = upd(e0x); T.e0y = upd(e0y); T.e0z = upd(e0z);
-        T.kb = upd(kb); T.kt = upd(kt); T.my = upd(my); T.ty = upd(ty); T.hb = upd(hb); T.ht = upd(ht);
-        T.cs = upd(cs); T.aL = upd(aL); T.aLsy = upd(aLsy);
-        T.invL0 = upd(invL0); T.inv_kbh = upd(inv_kbh); T.inv_kth = upd(inv_kth);
-        T.mass = upd(std::vector<double>(t->mass, t->mass + N));
-        uint8_t* dl = M.get<uint8_t>(6 * size_t(N));
-        h2d(dl, t->locked, 6 * size_t(N), s);
-        T.locked = dl;
-        int* dis = M.get<int>(inc_start.size());
-        h2d(dis, inc_start.data(), inc_start.size(), s);
-        T.inc_start = dis;
-        int* di = M.get<int>(inc.size());
-        h2d(di, inc.data(), inc.size(), s);
-        T.inc = di;
-        {
-            unsigned long long* dh = M.get<unsigned long long>(conn_hash.size());
-            h2d(dh, conn_hash.data(), conn_hash.size(), s);
-            T.conn_hash = dh;
-            T.conn_mask = hmask;
-            T.conn_shift = 64 - hbits;
-        }
-        {
-            float* dp = M.get<float>(size_t(B));
-            if (B) h2d(dp, padf.data(), size_t(B), s);
-            T.padf = dp;
-        }
-        c->topo = T;
-        c->mat = Material{E, G, sy, cf.material.hardening, cf.material.bend_hardening, cf.material.torsion_hardening,
-                          1.0 / std::max(1e-20, E + cf.material.hardening)};
-        PhysParams P{};
-        P.translation_scale = cf.translation_scale;
-        P.gravity = cf.gravity;
-        P.centering = cf.centering_stiffness;
-        P.contact_k = cf.contact_stiffness;
-        P.contact_margin = cf.contact_margin;
-        P.joint_radius = c->jr;
-        P.broad_cell = std::max(2.8 * c->jr, .72 * cf.cell_size);
-        P.top = g->top0;
-        P.self_contact = cf.self_contact ? 1 : 0;
-        P.joint_padf = round_up_float(c->jr + cf.contact_margin);
-        c->phys = P;
-        // state
-        c->d_baseX = M.get<double>(3 * size_t(N));
-        c->d_baseR = M.get<double>(4 * size_t(N));
-        c->d_plastic = M.get<double>(7 * size_t(B));
-        ck(cudaMemsetAsync(c->d_plastic, 0, 7 * size_t(B) * sizeof(double), s), "memset");
-        if (x0) h2d(c->d_baseX, x0, 3 * size_t(N), s);
-        if (r0) {
-            h2d(c->d_baseR, r0, 4 * size_t(N), s);
-        } else if (x0) {
-            std::vector<double> id(4 * size_t(N), 0.0);
-            for (int i = 0; i < N; i++) id[4 * size_t(i)] = 1.0;
-            h2d(c->d_baseR, id.data(), id.size(), s);
-            c->sync();
-        }
-        // evaluation buffers
-        DevArena& V = c->eval_mem;
-        EvalBufs e{};
-        e.x = V.get<double4_32a>(size_t(N));
-        e.R = V.get<double4_32a>(size_t(N));
-        e.M = V.get<double4_32a>(3 * size_t(N));
-        e.xf_lo = V.get<float4>(size_t(N));
-        e.xf_hi = V.get<float4>(size_t(N));
-        e.slotA = V.get<double>(6 * size_t(B));
-        e.slotB = V.get<double>(6 * size_t(B));
-        e.part_state = V.get<double>(9 * size_t(nb_nodes(N)));
-        e.part_beam = V.get<double>(3 * size_t(nb_beams(std::max(B, 1))));
-        e.part_node = V.get<double>(kNodeParts * size_t(nb_nodes(N)));
-        e.cen = V.get<double>(9);
-        e.out = V.get<EvalOut>(1);
-        e.trial_next = V.get<double>(7 * size_t(B));
-        e.trial_aux = V.get<double>(7 * size_t(B));
-        e.trial_flags = V.get<uint8_t>(3 * size_t(B));
-        c->mixed = cf.precision == MCG_MIXED;
-        if (c->mixed) {
-            e.slotAf = V.get<float>(6 * size_t(B));
-            e.slotBf = V.get<float>(6 * size_t(B));
-            e.trial_nextf = V.get<float>(7 * size_t(B));
-            e.trial_auxf = V.get<float>(7 * size_t(B));
-            MixedBeams mb{};
-            float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B3, &mb.B4, &mb.B5, &mb.C0, &mb.C1, &mb.P0, &mb.P1};
-            for (float4** f : fields) *f = V.get<float4>(size_t(B));
-            c->mb = mb;
-            c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
-        }
-        c->ev = e;
-        c->d_zin = V.get<double>(6 * size_t(N));
-        c->d_grad = V.get<double>(6 * size_t(N));
-        ck(cudaMemsetAsync(c->d_zin, 0, 6 * size_t(N) * sizeof(double), s), "memset");
-        // contact buffers: a first guess, grown on demand
-        const long long S = (long long)N + B;
-        c->broad_cell = P.broad_cell;
-        c->contact_skin = float(0.125 * cf.cell_size);
-        {
-            // bins: the Morton range of the rest-state extent, with room to grow
-            double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-            if (x0)
-                for (int i = 0; i < N; i++)
-                    for (int d = 0; d < 3; d++) {
-                        lo[d] = std::min(lo[d], x0[3 * size_t(i) + d]);
-                        hi[d] = std::max(hi[d], x0[3 * size_t(i) + d]);
-                    }
-            long long dmax = 8;
-            if (x0)
-                for (int d = 0; d < 3; d++)
-                    dmax = std::max(dmax, (long long)((hi[d] - lo[d] + 2 * c->rmax) / P.broad_cell * 1.15) + 4);
-            int bits = 3;
-            while ((1LL << bits) < dmax && bits < 10) bits++;
-            const long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
-            c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap, 1024);
-        }
-        // solver vectors
-        DevArena& Q = c->solver_mem;
-        const size_t n = 6 * size_t(N);
-        c->d_z = Q.get<double>(n); c->d_zc = Q.get<double>(n); c->d_p = Q.get<double>(n);
-        c->d_g = Q.get<double>(n); c->d_gc = Q.get<double>(n); c->d_best = Q.get<double>(n);
-        c->d_zfinal = Q.get<double>(n);
-        c->d_S.assign(size_t(cf.history), nullptr);
-        c->d_Y.assign(size_t(cf.history), nullptr);
-        for (int h = 0; h < cf.history; h++) { c->d_S[size_t(h)] = Q.get<double>(n); c->d_Y[size_t(h)] = Q.get<double>(n); }
-        c->d_rho = Q.get<double>(size_t(std::max(cf.history, 1)));
-        c->d_alpha = Q.get<double>(size_t(std::max(cf.history, 1)));
-        c->d_scal = Q.get<double>(8);
-        c->d_part = Q.get<double>(lbfgs_part_doubles());
-        c->d_stats = Q.get<double>(16);
-        ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
-        if (c->mixed) {
-            launch_mixed_constants(c->topo, c->mb, s);
-            launch_plastic_mixed(B, c->d_plastic, nullptr, c->mb, s);
-            c->rebase();
-        }
-        c->sync();
-        c->have_topo = true;
+        upload_instances(c, std::vector<InstIn>{InstIn{t, g, x0, r0, c->cfg.material.yield}});
     });
 }
+
+int mcg_upload_batch(mcg_ctx* c, int32_t count, const mcg_topology* topos, const mcg_geometry* geoms,
+                     const double* const* x0, const double* const* r0, const double* yield) {
+    return guarded(c, [&] {
+        if (count <= 0 || !topos || !geoms) throw Fail(MCG_ERR_INVALID, "empty batch");
+        std::vector<InstIn> ins;
+        for (int k = 0; k < count; k++)
+            ins.push_back(InstIn{topos + k, geoms + k, x0 ? x0[k] : nullptr, r0 ? r0[k] : nullptr,
+                                 yield ? yield[k] : c->cfg.material.yield});
+        upload_instances(c, ins);
+    });
+}
+
+int32_t mcg_instance_count(const mcg_ctx* c) { return c && c->have_topo ? c->I : 0; }
 
 int mcg_set_state(mcg_ctx* c, const double* bx, const double* br, const double* pl) {
     return guarded(c, [&] {
@@ -960,7 +1375,7 @@ int mcg_set_state(mcg_ctx* c, const double* bx, const double* br, const double* 
             for (size_t b = 0; b < B; b++)
                 for (int k = 0; k < 7; k++) soa[size_t(k) * B + b] = pl[7 * b + size_t(k)];
             h2d(c->d_plastic, soa.data(), soa.size(), s);
-            if (c->mixed) launch_plastic_mixed(c->B, c->d_plastic, nullptr, c->mb, s);
+            if (c->mixed) launch_plastic_mixed(c->topo, nullptr, c->d_plastic, nullptr, c->mb, s);
             c->sync();
         }
         if (bx || br) c->rebase();
@@ -990,19 +1405,18 @@ int mcg_get_state(mcg_ctx* c, double* bx, double* br, double* pl) {
 int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* energy, double* grad,
                   mcg_diag* diag, double* trial_next, double* trial_aux, uint8_t* trial_flags) {
     return guarded(c, [&] {
-        need_topo(c);
+        need_single(c);
         if (!z) throw Fail(MCG_ERR_INVALID, "null z");
         cudaStream_t s = c->stream;
         const size_t n = 6 * size_t(c->N), B = size_t(c->B);
         h2d(c->d_zin, z, n, s);
-        const EvalOut o = c->eval_read(c->d_zin, top, trials != 0, c->d_grad);
+        c->hp.tops[0] = top;
+        c->upload_tops();
+        const EvalOut o = c->eval_read(c->d_zin, trials != 0, c->d_grad)[0];
         if (trials) c->have_final = false;
         if (grad) d2h(grad, c->d_grad, n, s);
         if (energy) *energy = o.energy;
-        if (diag) {
-            diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
-            diag->reaction = o.reaction; diag->max_pen = o.max_pen; diag->contacts = o.contacts; diag->pad_ = 0;
-        }
+        fill_diag(diag, o);
         if (trials && c->mixed) {
             launch_f32_to_f64(7LL * c->B, c->ev.trial_nextf, c->ev.trial_next, s);
             launch_f32_to_f64(7LL * c->B, c->ev.trial_auxf, c->ev.trial_aux, s);
@@ -1029,6 +1443,25 @@ int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* e
     });
 }
 
+int mcg_batch_objective(mcg_ctx* c, const double* z, const double* tops, double* energies, double* grad,
+                        mcg_diag* diags) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!z || !tops) throw Fail(MCG_ERR_INVALID, "null z or platen heights");
+        const size_t n = 6 * size_t(c->N);
+        h2d(c->d_zin, z, n, c->stream);
+        for (int i = 0; i < c->I; i++) c->hp.tops[i] = tops[i];
+        c->upload_tops();
+        const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);
+        for (int i = 0; i < c->I; i++) {
+            if (energies) energies[i] = o[i].energy;
+            if (diags) fill_diag(diags + i, o[i]);
+        }
+        if (grad) d2h(grad, c->d_grad, n, c->stream);
+        c->sync();
+    });
+}
+
 int mcg_upload_z(mcg_ctx* c, const double* z) {
     return guarded(c, [&] {
         need_topo(c);
@@ -1040,24 +1473,26 @@ int mcg_upload_z(mcg_ctx* c, const double* z) {
 
 int mcg_objective_resident(mcg_ctx* c, double top, int trials) {
     return guarded(c, [&] {
-        need_topo(c);
-        c->eval(c->d_zin, top, trials != 0, c->d_grad);
+        need_single(c);
+        if (c->hp.tops[0] != top) {
+            c->sync();
+            c->hp.tops[0] = top;
+            c->upload_tops();
+        }
+        c->eval(c->d_zin, trials != 0, c->d_grad);
         if (trials) c->have_final = false;
     });
 }
 
 int mcg_read_result(mcg_ctx* c, double* energy, double* grad, mcg_diag* diag) {
     return guarded(c, [&] {
-        need_topo(c);
+        need_single(c);
         if (!c->last_z) throw Fail(MCG_ERR_STATE, "no evaluation to read");
         const EvalOut o = c->read_out();
         if (grad) d2h(grad, c->d_grad, 6 * size_t(c->N), c->stream);
         c->sync();
         if (energy) *energy = o.energy;
-        if (diag) {
-            diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
-            diag->reaction = o.reaction; diag->max_pen = o.max_pen; diag->contacts = o.contacts; diag->pad_ = 0;
-        }
+        fill_diag(diag, o);
     });
 }
 
@@ -1070,13 +1505,14 @@ namespace mcg {
 int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* z, double top, double* energy,
                                   double* grad, mcg_diag* diag) {
     return guarded(c, [&] {
-        need_topo(c);
+        need_single(c);
         if (!z) throw Fail(MCG_ERR_INVALID, "null z");
         cudaStream_t s = c->stream;
         const size_t n = 6 * size_t(c->N);
         h2d(c->d_zin, z, n, s);
+        c->hp.tops[0] = top;
+        c->upload_tops();
         PhysParams p = c->phys;
-        p.top = top;
         p.broad_cell = c->broad_cell;
         p.inv_cell_f = float(1.0 / c->broad_cell);
         if (c->mixed) launch_state_mixed(c->topo, p, c->d_zin, c->d_baseX, c->mn, c->ev, s);
@@ -1092,7 +1528,8 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         else launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
         launch_finalize(c->topo, p, cptr, c->d_grad, c->ev, s);
         c->check_launch();
-        const EvalOut o = c->read_out_raw();
+        c->read_outs();
+        const EvalOut o = c->hp.outs[0];
         if (o.overflow) {
             std::string what;
             if (o.overflow & kOverEntries) what += " cell entries";
@@ -1106,15 +1543,12 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         if (grad) d2h(grad, c->d_grad, n, s);
         c->sync();
         if (energy) *energy = o.energy;
-        if (diag) {
-            diag->elastic = o.elastic; diag->plastic = o.plastic; diag->contact = o.contact;
-            diag->reaction = o.reaction; diag->max_pen = o.max_pen; diag->contacts = o.contacts; diag->pad_ = 0;
-        }
+        fill_diag(diag, o);
     });
 }
 
 int ctx_counts(const mcg_ctx* c, int* n_nodes, int* n_beams, int* device) {
-    if (!c || !c->have_topo) return MCG_ERR_STATE;
+    if (!c || !c->have_topo || c->I != 1) return MCG_ERR_STATE;
     *n_nodes = c->N;
     *n_beams = c->B;
     *device = c->device;
@@ -1155,31 +1589,32 @@ int mcg_contact_pairs(mcg_ctx* c, uint64_t* keys, int64_t capacity, int64_t* cou
 
 int mcg_minimize(mcg_ctx* c, double top, double* z, mcg_optstats* stats, double* final_energy, mcg_diag* fd) {
     return guarded(c, [&] {
-        need_topo(c);
+        need_single(c);
         if (!z) throw Fail(MCG_ERR_INVALID, "null z");
         const size_t n = 6 * size_t(c->N);
         h2d(c->d_z, z, n, c->stream);
-        EvalOut fin{};
-        const HostStats st = c->minimize(top, fin);
+        c->start_minimize(0, top, false);
+        c->minimize_all();
+        const Minimizer& m = c->mins[0];
         d2h(z, c->d_z, n, c->stream);
         c->sync();
+        c->have_final = true;
         if (stats) {
-            stats->iterations = st.iterations; stats->backtracks = st.backtracks; stats->rms = st.rms;
-            stats->max = st.max; stats->energy = st.energy; stats->converged = st.converged; stats->pad_ = 0;
+            stats->iterations = m.st.iterations; stats->backtracks = m.st.backtracks; stats->rms = m.st.rms;
+            stats->max = m.st.max; stats->energy = m.st.energy; stats->converged = m.st.converged; stats->pad_ = 0;
         }
-        if (final_energy) *final_energy = fin.energy;
-        if (fd) {
-            fd->elastic = fin.elastic; fd->plastic = fin.plastic; fd->contact = fin.contact;
-            fd->reaction = fin.reaction; fd->max_pen = fin.max_pen; fd->contacts = fin.contacts; fd->pad_ = 0;
-        }
+        if (final_energy) *final_energy = m.fin.energy;
+        fill_diag(fd, m.fin);
+        c->mins[0].phase = Minimizer::kIdle;
     });
 }
 
 int mcg_commit(mcg_ctx* c) {
     return guarded(c, [&] {
-        need_topo(c);
-        c->commit();
-        c->sync();
+        need_single(c);
+        if (!c->have_final) throw Fail(MCG_ERR_STATE, "commit without a preceding minimize");
+        c->commit(std::vector<uint8_t>(1, 1));
+        c->have_final = false;
     });
 }
 
@@ -1225,19 +1660,50 @@ int mcg_phase_times(mcg_ctx* c, double* ms, int32_t n, int64_t* evaluations) {
 
 int mcg_run(mcg_ctx* c, mcg_frame* frames, int32_t capacity, int32_t* count, int verbose) {
     if (!c || !count) return MCG_ERR_INVALID;
-    std::vector<mcg_frame> out;
+    std::vector<Runner> rs;
     int rc = guarded(c, [&] {
-        need_topo(c);
-        c->run(out, verbose != 0);
+        need_single(c);
+        c->run(rs, verbose != 0);
     });
+    const std::vector<mcg_frame> none;
+    const std::vector<mcg_frame>& out = rs.empty() ? none : rs[0].frames;
     *count = int32_t(out.size());
     if (frames)
         for (size_t f = 0; f < out.size() && int32_t(f) < capacity; f++) frames[f] = out[f];
+    if (rc == MCG_OK && !rs.empty() && rs[0].status != MCG_OK) {
+        c->err = rs[0].error;
+        rc = rs[0].status;
+    }
     if (rc == MCG_OK && int32_t(out.size()) > capacity) {
         c->err = "frame buffer too small";
         return MCG_ERR_CAPACITY;
     }
     return rc;
+}
+
+int mcg_batch_run(mcg_ctx* c, mcg_frame* frames, int32_t capacity, int32_t* counts, int32_t* status) {
+    if (!c || !counts || !status) return MCG_ERR_INVALID;
+    std::vector<Runner> rs;
+    int rc = guarded(c, [&] {
+        need_topo(c);
+        c->run(rs, false);
+    });
+    if (rc != MCG_OK) return rc;
+    bool small = false;
+    for (int i = 0; i < c->I; i++) {
+        const std::vector<mcg_frame>& out = rs[size_t(i)].frames;
+        counts[i] = int32_t(out.size());
+        status[i] = rs[size_t(i)].status;
+        small |= int32_t(out.size()) > capacity;
+        if (frames)
+            for (size_t f = 0; f < out.size() && int32_t(f) < capacity; f++)
+                frames[size_t(i) * size_t(capacity) + f] = out[f];
+    }
+    if (small) {
+        c->err = "frame buffer too small";
+        return MCG_ERR_CAPACITY;
+    }
+    return MCG_OK;
 }
 
 }  // extern "C"

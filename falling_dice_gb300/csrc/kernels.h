@@ -44,7 +44,36 @@ struct DevTopo {
     unsigned long long conn_mask;  // slots - 1 (a power of two)
     int conn_shift;                // 64 - log2(slots)
     const float* padf;        // [B] radius + contact margin, rounded up to single precision
+    const double* sy;         // [B] yield stress (the beam's instance)
+    // Instances: a context holds I lattices stored one after another (I = 1 for a plain
+    // context).  Node and beam kernels run over blocks that never straddle two instances,
+    // so every block partial belongs to one instance and per-instance totals are sums over
+    // an instance's own blocks, in the same order as for that lattice alone.
+    int I;
+    int n_nblk, n_bblk;       // node blocks, beam blocks
+    const int4* nblk;         // [n_nblk] first node, node count, instance, 0
+    const int4* bblk;         // [n_bblk] first beam, beam count, instance, 0
+    const int4* irange;       // [I] node blocks [x, y), beam blocks [z, w) of the instance
+    const int* inst_n;        // [I] nodes of the instance
+    const long long* inst_free;  // [I] unlocked DOFs of the instance
+    const float2* off;        // [I] (x, z) offset of the instance in the contact grid
 };
+
+// Elements per mapped block (the launch block size of the mapped kernels).
+constexpr int kMapBlock = 256;
+
+#if defined(__CUDACC__)
+// Position of a thread of a mapped block: element index, instance; valid == false past the
+// block's element count.
+struct MapPos {
+    int i, inst;
+    bool valid;
+};
+__device__ __forceinline__ MapPos map_pos(const int4* __restrict__ blk) {
+    const int4 q = blk[blockIdx.x];
+    return MapPos{q.x + int(threadIdx.x), q.z, int(threadIdx.x) < q.y};
+}
+#endif
 
 struct PhysParams {
     double translation_scale, gravity, centering, contact_k, contact_margin, joint_radius;
@@ -61,6 +90,7 @@ struct EvalOut {
     double beam_energy, node_energy, center_energy, contact_energy, platen_energy;
     int overflow;                    // ContactFlag bits that invalidate this evaluation
     int pad_;
+    double rms, gmax;                // residual over free DOFs: sqrt(mean g^2), max |g| (sim.cpp:44-45)
 };
 
 // Device scratch of the contact pipeline (contact.cu).  Capacities are host-chosen and
@@ -124,12 +154,13 @@ struct ContactBufs {
     uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot), in arrival order
     uint32_t* n_sorted;     // [4 * contact_cap]  the same per node, by (lower shape, higher shape, slot)
     uint32_t* n_long;       // [N + 1] count, then the nodes whose lists exceed one warp
-    double* part;           // [3 * contact_part_blocks] (unused), max penetration, count
     void* scan_tmp;
     size_t scan_tmp_bytes;
 };
 
-constexpr int kNodeParts = 6;  // per node block: gravity E, platen E, reaction, max pen, platen contacts, self-contact E
+// per node block: gravity E, platen E, reaction, max penetration, contacts, self-contact E,
+// sum of squared free gradient entries, max |free gradient entry|
+constexpr int kNodeParts = 8;
 
 struct EvalBufs {
     double4_32a* x;             // [N]
@@ -142,8 +173,10 @@ struct EvalBufs {
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
     double* part_beam;      // [3 * nb_beams]
     double* part_node;      // [kNodeParts * nb_nodes]
-    double* cen;            // [9] mean, min, max of the node positions
-    EvalOut* out;
+    double* cen;            // [9 (I + 1)] per instance mean, min, max of the node positions (min/max
+                            //   in the contact grid's frame); then min/max over all instances
+    double* tops;           // [I] platen height per instance
+    EvalOut* out;           // [I]
     double* trial_next;     // [7B] SoA
     double* trial_aux;      // [7B] SoA
     uint8_t* trial_flags;   // [3B] SoA
@@ -189,9 +222,11 @@ void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, 
                    EvalBufs& e, cudaStream_t s);
 void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
                      EvalBufs& e, cudaStream_t s);
-void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic,
-                   cudaStream_t s);
-void launch_center(int N, EvalBufs& e, cudaStream_t s);
+// base state <- current state, plastic <- trial (plastic == nullptr skips it) for the
+// instances with mask[i] != 0 (mask == nullptr: all)
+void launch_commit(const DevTopo& t, const uint8_t* mask, const EvalBufs& e, double* base_x, double* base_r,
+                   double* plastic, cudaStream_t s);
+void launch_center(const DevTopo& t, EvalBufs& e, cudaStream_t s);
 void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
                          cudaStream_t s);
 
@@ -203,15 +238,18 @@ void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& m
 void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
                          MixedNodes& mn, cudaStream_t s);
 void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s);
-// plastic state of the mixed form from the FP64 SoA array (trial32 == nullptr) or from an FP32 trial
-void launch_plastic_mixed(int B, const double* plastic64, const float* trial32, MixedBeams& mb, cudaStream_t s);
-void launch_plastic_mixed_to_f64(int B, const MixedBeams& mb, double* plastic64, cudaStream_t s);
+// plastic state of the mixed form from the FP64 SoA array (trial32 == nullptr, all beams) or
+// from an FP32 trial (the beams of the instances with mask[i] != 0; mask == nullptr: all)
+void launch_plastic_mixed(const DevTopo& t, const uint8_t* mask, const double* plastic64, const float* trial32,
+                          MixedBeams& mb, cudaStream_t s);
+void launch_plastic_mixed_to_f64(const DevTopo& t, const uint8_t* mask, const MixedBeams& mb, double* plastic64,
+                                 cudaStream_t s);
 void launch_f32_to_f64(long long n, const float* a, double* o, cudaStream_t s);
-// out6: sum|epsp|, max|epsp|, sum|rotp|, max|rotp|, #|epsp|>1e-5, #|rotp|>1e-4
-void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s);
+// out6[6 i..]: per instance sum|epsp|, max|epsp|, sum|rotp|, max|rotp|, #|epsp|>1e-5, #|rotp|>1e-4
+// (part: 6 doubles per beam block)
+void launch_plastic_stats(const DevTopo& t, const double* plastic, double* part, double* out6, cudaStream_t s);
 
 // ---- contact pipeline (contact.cu) ------------------------------------------------------
-int contact_part_blocks(long long contact_cap);
 // Blocks of the pair / narrow-phase grid for a model of `shapes` shapes (8 warps each).
 int contact_pair_blocks(long long shapes);
 // The whole broad/narrow phase: grid, entries, bins, pairs, contact list, node lists.
@@ -228,24 +266,44 @@ size_t scan_tmp_bytes(long long n);
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s,
                         const uint32_t* gate = nullptr);
 
-// ---- L-BFGS vector kernels (lbfgs.cu) ----------------------------------------------------
-size_t lbfgs_part_doubles();
-// k (1..3) dot products a_k . b_k into out[0..k-1] (device)
-void dots(int k, const double* a0, const double* b0, const double* a1, const double* b1, const double* a2,
-          const double* b2, long long n, double* part, double* out, cudaStream_t s);
-void rms_max(const double* g, const uint8_t* locked, long long n, long long n_free, double* part, double* out2,
-             cudaStream_t s);
-void vcopy(double* dst, const double* src, long long n, cudaStream_t s);
-// L-BFGS two-loop recursion (sim.cpp:184-187) into p, history oldest first
-void two_loop(double* p, const double* g, const double* const* S, const double* const* Y, const double* const* rho,
-              int m, double* alpha, double* scal, double* part, long long n, cudaStream_t s);
-// p = clamp(lock(-src)) per node (sim.cpp:188-190, 46)
-void finish_direction(double* p, const double* src, const uint8_t* locked, int N, double mt, double mr,
-                      cudaStream_t s);
-void candidate(double* zc, const double* z, const double* p, double step, const uint8_t* locked, long long n,
-               cudaStream_t s);
-void make_sy(double* sv, double* yv, const double* zc, const double* z, const double* gc, const double* g,
-             long long n, cudaStream_t s);
-void set_rho(double* rho, const double* sy, cudaStream_t s);
+// ---- L-BFGS vector kernels (lbfgs.cu), all instances of a context per launch --------------
+// Operations an instance takes part in during one solver step (SolveCtl::flags).
+enum SolveOp : int {
+    kOpDirection = 1,      // two-loop direction from g, clamp, <g, p>
+    kOpSteepest = 2,       // p = clamp(-g), <g, p>
+    kOpZero = 4,           // z = 0
+    kOpRestore = 8,        // z = best
+    kOpKeepBest = 16,      // best = z
+    kOpCandidate = 32,     // zeval = z + step p
+    kOpEvalAtZ = 64,       // zeval = z
+    kOpFinal = 128,        // zfinal = z
+    kOpTakeGrad = 256,     // g = geval
+    kOpAccept = 512,       // s, y, curvature dots, z = zeval, g = geval
+    kOpPair = 1024,        // with kOpAccept: store (s, y) in history slot `target`
+    kOpKeepBestAfter = 2048  // with kOpAccept: best = the accepted z
+};
+// Per-instance solver control, written by the host before each step.
+struct SolveCtl {
+    double step;       // line-search step of the candidate
+    int flags;         // SolveOp bits
+    int m, head;       // history pairs held, ring slot of the oldest
+    int target;        // slot the next accepted pair goes to
+};
+size_t lbfgs_part_doubles(int n_nblk);
+// Two-loop recursion (sim.cpp:184-187) into p for the kOpDirection instances, then
+// p = clamp(lock(-p)) and dg[i] = <g, p>.  History: H slots of `stride` doubles; rho and
+// alpha [I * H].
+void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
+                  const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
+                  double* dg, double mt, double mr, cudaStream_t s);
+// p = clamp(lock(-g)) and dg[i] = <g, p> for the kOpSteepest instances (sim.cpp:191, 195).
+void bl_steepest(const DevTopo& t, const SolveCtl* ctl, double* p, const double* g, double* part, double* dg,
+                 double mt, double mr, cudaStream_t s);
+// kOpZero / kOpRestore / kOpKeepBest / kOpCandidate / kOpEvalAtZ / kOpFinal
+void bl_prepare(const DevTopo& t, const SolveCtl* ctl, double* z, double* best, double* zeval, const double* p,
+                double* zfinal, cudaStream_t s);
+// kOpTakeGrad / kOpAccept (+kOpPair, kOpKeepBestAfter); out3[3 i..] = <s, y>, <s, s>, <y, y>
+void bl_accept(const DevTopo& t, const SolveCtl* ctl, double* z, double* g, const double* zeval, const double* geval,
+               double* S, double* Y, long long stride, double* best, double* part, double* out3, cudaStream_t s);
 
 }  // namespace mcg

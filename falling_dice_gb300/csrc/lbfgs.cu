@@ -1,10 +1,16 @@
 // lbfgs.cu -- device vector kernels of the L-BFGS minimizer
-// (the reference's Simulator::minimize and helpers, MC/src/sim.cpp:42-46, 174-211).
+// (the reference's Simulator::minimize and helpers, MC/src/sim.cpp:42-46, 174-211), for every
+// instance of a context at once.
 //
-// The two-loop recursion, direction clamp, candidate steps and curvature products all run
-// on the device; scalars the recursion needs (alpha_h, beta_h, H0) never leave it.  Dot
-// products use a fixed two-level partition (a fixed grid of partial sums, then one block)
-// so that every value is reproducible bit for bit.
+// Vectors hold 6 entries per node in the ABI layout; all instances' nodes are stored one
+// after another and every kernel runs over the node blocks of the context (a block never
+// straddles two instances).  Each instance has its own solver state (history count, ring
+// head, line-search step, which operations it takes part in), written by the host into a
+// small control array before each step.  Dot products are per-block partial sums (each
+// thread its node's six products in order, then a fixed tree) and one block per instance
+// summing its blocks in order: the same partition whether an instance is solved alone or
+// with others, so a batch reproduces the separate runs bit for bit.  The two-loop scalars
+// (alpha_h, H0) never leave the device.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -12,230 +18,326 @@ namespace mcg {
 
 namespace {
 
-constexpr int kDotBlocks = 296;  // 2 x 148: fixed partition of every reduction
+__device__ __forceinline__ const double* hist(const double* base, long long stride, int slot) {
+    return base + stride * slot;
+}
 
-// Up to three dot products over the same index range: out[k] = sum a_k[i] * b_k[i].
+// Slot of the h-th oldest history pair of an instance.
+__device__ __forceinline__ int ring_slot(const SolveCtl& c, int H, int h) { return (c.head + h) % H; }
+
+// One instance's sum of its block partials part[k * nblk + b], b in its node-block range,
+// for k < K (one block per instance; fixed order).
 template <int K>
-__global__ void __launch_bounds__(kBlock) k_dots_part(const double* __restrict__ a0, const double* __restrict__ b0,
-                                                      const double* __restrict__ a1, const double* __restrict__ b1,
-                                                      const double* __restrict__ a2, const double* __restrict__ b2,
-                                                      long long n, double* __restrict__ part) {
-    __shared__ double sm[K * (kBlock / 32)];
-    double acc[K];
+__device__ __forceinline__ void instance_sum(const DevTopo& t, const double* __restrict__ part, int inst,
+                                             double (&acc)[K], double* sm) {
+    const int4 r = t.irange[inst];
 #pragma unroll
     for (int k = 0; k < K; k++) acc[k] = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        acc[0] += a0[i] * b0[i];
-        if (K > 1) acc[1 % K] += a1[i] * b1[i];
-        if (K > 2) acc[2 % K] += a2[i] * b2[i];
-    }
-    block_sum<K>(acc, sm);
-    if (threadIdx.x == 0)
+    for (int b = r.x + int(threadIdx.x); b < r.y; b += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < K; k++) part[k * kDotBlocks + blockIdx.x] = acc[k];
+        for (int k = 0; k < K; k++) acc[k] += part[size_t(k) * t.n_nblk + b];
+    block_sum<K>(acc, sm);
 }
 
-template <int K>
-__global__ void __launch_bounds__(kBlock) k_dots_final(const double* __restrict__ part, double* __restrict__ out) {
-    __shared__ double sm[K * (kBlock / 32)];
-    double acc[K];
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-        acc[k] = 0;
-        for (int j = threadIdx.x; j < kDotBlocks; j += blockDim.x) acc[k] += part[k * kDotBlocks + j];
-    }
-    block_sum<K>(acc, sm);
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < K; k++) out[k] = acc[k];
+__device__ __forceinline__ double dot6(const double* a, const double* b) {
+    double s = a[0] * b[0];
+    s += a[1] * b[1];
+    s += a[2] * b[2];
+    s += a[3] * b[3];
+    s += a[4] * b[4];
+    s += a[5] * b[5];
+    return s;
 }
 
-// Sum of squares and max |g| over unlocked DOFs (sim.cpp:44-45).
-__global__ void __launch_bounds__(kBlock) k_rms_max_part(const double* __restrict__ g, const uint8_t* __restrict__ locked,
-                                                         long long n, double* __restrict__ part) {
+// ---- two-loop recursion (sim.cpp:184-187) -----------------------------------------------
+// Partial <S[slot], p> (loop 1, newest first: h = m - 1 - j) or <Y[slot], p> (loop 2,
+// oldest first: h = j) for the instances computing a direction with j < m.
+template <int LOOP>
+__global__ void __launch_bounds__(kBlock) k_tl_dot(DevTopo t, const SolveCtl* __restrict__ ctl, int H, int j,
+                                                   const double* __restrict__ p, const double* __restrict__ S,
+                                                   const double* __restrict__ Y, long long stride,
+                                                   double* __restrict__ part) {
     __shared__ double sm[kBlock / 32];
-    __shared__ double smx[kBlock / 32];
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
+    const int slot = ring_slot(c, H, LOOP == 1 ? c.m - 1 - j : j);
+    const double* v = hist(LOOP == 1 ? S : Y, stride, slot);
     double acc[1] = {0};
-    double m = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        if (!locked[i]) {
-            const double v = g[i];
-            acc[0] += v * v;
-            m = fmax(m, fabs(v));
+    if (mp.valid) acc[0] = dot6(v + 6 * size_t(mp.i), p + 6 * size_t(mp.i));
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+}
+
+// Loop 1: alpha = rho <s, p> (kept), p -= alpha y.  Loop 2: beta = rho <y, p>, p += s (alpha - beta).
+// Every block of an instance sums the instance's partials itself (same order in each).
+template <int LOOP>
+__global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl* __restrict__ ctl, int H, int j,
+                                                      double* __restrict__ p, const double* __restrict__ S,
+                                                      const double* __restrict__ Y, long long stride,
+                                                      const double* __restrict__ rho, double* __restrict__ alpha,
+                                                      const double* __restrict__ part) {
+    __shared__ double sm[kBlock / 32];
+    __shared__ double coef;
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!(c.flags & kOpDirection) || j >= c.m) return;
+    const int h = LOOP == 1 ? c.m - 1 - j : j;
+    const int slot = ring_slot(c, H, h);
+    double acc[1];
+    instance_sum<1>(t, part, mp.inst, acc, sm);
+    if (threadIdx.x == 0) {
+        const double r = rho[size_t(mp.inst) * H + slot] * acc[0];
+        if (LOOP == 1) {
+            coef = r;
+            if (blockIdx.x == t.irange[mp.inst].x) alpha[size_t(mp.inst) * H + h] = r;
+        } else {
+            coef = alpha[size_t(mp.inst) * H + h] - r;
         }
     }
-    block_sum<1>(acc, sm);
-    m = block_max(m, smx);
+    __syncthreads();
+    if (!mp.valid) return;
+    const double k = coef;
+    double* pi = p + 6 * size_t(mp.i);
+    if (LOOP == 1) {
+        const double* y = hist(Y, stride, slot) + 6 * size_t(mp.i);
+#pragma unroll
+        for (int d = 0; d < 6; d++) pi[d] -= k * y[d];
+    } else {
+        const double* s = hist(S, stride, slot) + 6 * size_t(mp.i);
+#pragma unroll
+        for (int d = 0; d < 6; d++) pi[d] += s[d] * k;
+    }
+}
+
+// Partials of <s, y> and <y, y> of the newest pair (for H0) and the copy p = g that starts
+// the recursion.
+__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, int H,
+                                                     double* __restrict__ p, const double* __restrict__ g,
+                                                     const double* __restrict__ S, const double* __restrict__ Y,
+                                                     long long stride, double* __restrict__ part) {
+    __shared__ double sm[2 * (kBlock / 32)];
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!(c.flags & kOpDirection)) return;
+    if (mp.valid)
+#pragma unroll
+        for (int d = 0; d < 6; d++) p[6 * size_t(mp.i) + d] = g[6 * size_t(mp.i) + d];
+    if (c.m == 0) return;
+    const int slot = ring_slot(c, H, c.m - 1);
+    double acc[2] = {0, 0};
+    if (mp.valid) {
+        const double* s = hist(S, stride, slot) + 6 * size_t(mp.i);
+        const double* y = hist(Y, stride, slot) + 6 * size_t(mp.i);
+        acc[0] = dot6(s, y);
+        acc[1] = dot6(y, y);
+    }
+    block_sum<2>(acc, sm);
     if (threadIdx.x == 0) {
         part[blockIdx.x] = acc[0];
-        part[kDotBlocks + blockIdx.x] = m;
+        part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_rms_max_final(const double* __restrict__ part, long long n_free,
-                                                          double* __restrict__ out) {
+// p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186).
+__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                     double* __restrict__ p, const double* __restrict__ part) {
+    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ double h0;
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!(c.flags & kOpDirection)) return;
+    if (c.m > 0) {
+        double acc[2];
+        instance_sum<2>(t, part, mp.inst, acc, sm);
+        if (threadIdx.x == 0) {
+            double v = .10;
+            if (acc[0] > 1e-20 && acc[1] > 1e-20) v = clampd(acc[0] / acc[1], 1e-7, 1e4);
+            h0 = v;
+        }
+    } else if (threadIdx.x == 0) {
+        h0 = .10;
+    }
+    __syncthreads();
+    if (!mp.valid) return;
+    const double k = h0;
+#pragma unroll
+    for (int d = 0; d < 6; d++) p[6 * size_t(mp.i) + d] *= k;
+}
+
+// Direction finish for the instances with `bit` set: p = clamp(lock(-src)) per node
+// (sim.cpp:188-190, clampDirection sim.cpp:46), and the partial of <g, p>.
+__global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
+                                                   double* __restrict__ p, const double* __restrict__ src,
+                                                   const double* __restrict__ g, double mt, double mr,
+                                                   double* __restrict__ part) {
     __shared__ double sm[kBlock / 32];
-    __shared__ double smx[kBlock / 32];
+    const MapPos mp = map_pos(t.nblk);
+    if (!(ctl[mp.inst].flags & bit)) return;
     double acc[1] = {0};
-    double m = 0;
-    for (int j = threadIdx.x; j < kDotBlocks; j += blockDim.x) {
-        acc[0] += part[j];
-        m = fmax(m, part[kDotBlocks + j]);
+    if (mp.valid) {
+        const size_t b = 6 * size_t(mp.i);
+        const uint8_t* lk = t.locked + b;
+        double v[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            v[k] = -src[b + k];
+            if (lk[k]) v[k] = 0;
+        }
+        const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (lt > mt) {
+            const double f = mt / lt;
+            v[0] *= f; v[1] *= f; v[2] *= f;
+        }
+        const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+        if (lr > mr) {
+            const double f = mr / lr;
+            v[3] *= f; v[4] *= f; v[5] *= f;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            v[k] = lk[k] ? 0.0 : v[k];
+            p[b + k] = v[k];
+        }
+        acc[0] = dot6(g + b, v);
     }
     block_sum<1>(acc, sm);
-    m = block_max(m, smx);
-    if (threadIdx.x == 0) {
-        out[0] = n_free ? sqrt(acc[0] / double(n_free)) : 0.0;
-        out[1] = m;
-    }
+    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
 }
 
-__global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, long long n) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        dst[i] = src[i];
+// One block per instance with `bit` set: out[K i + k] = sum of its partials.
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_inst_final(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
+                                                       const double* __restrict__ part, double* __restrict__ out) {
+    __shared__ double sm[K * (kBlock / 32)];
+    const int inst = blockIdx.x;
+    if (!(ctl[inst].flags & bit)) return;
+    double acc[K];
+    instance_sum<K>(t, part, inst, acc, sm);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < K; k++) out[size_t(K) * inst + k] = acc[k];
 }
 
-// p -= (rho * <s, p>) y, with alpha = rho * dot stored for the second loop.
-__global__ void k_loop1_update(double* __restrict__ p, const double* __restrict__ y, long long n,
-                               const double* __restrict__ rho, const double* __restrict__ dotv,
-                               double* __restrict__ alpha_out) {
-    const double alpha = (*rho) * (*dotv);
-    if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = alpha;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        p[i] -= alpha * y[i];
-}
-
-// p *= H0 with H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186).
-__global__ void k_scale_h0(double* __restrict__ p, long long n, const double* __restrict__ syyy, int have) {
-    double H0 = .10;
-    if (have) {
-        const double sy = syyy[0], yy = syyy[1];
-        if (sy > 1e-20 && yy > 1e-20) H0 = clampd(sy / yy, 1e-7, 1e4);
-    }
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        p[i] *= H0;
-}
-
-// p += s (alpha - rho <y, p>).
-__global__ void k_loop2_update(double* __restrict__ p, const double* __restrict__ s, long long n,
-                               const double* __restrict__ rho, const double* __restrict__ dotv,
-                               const double* __restrict__ alpha) {
-    const double beta = (*rho) * (*dotv);
-    const double c = *alpha - beta;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        p[i] += s[i] * c;
-}
-
-// Direction finish: optional negation of src into p, lock, per-node step clamp, lock
-// (sim.cpp:188-190 and clampDirection, sim.cpp:46).
-__global__ void __launch_bounds__(kBlock) k_finish_dir(double* p, const double* src,
-                                                       const uint8_t* __restrict__ locked, int N, double mt,
-                                                       double mr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const size_t b = 6 * size_t(i);
-    double v[6];
+// ---- vectors around an evaluation ------------------------------------------------------------
+// Per node, in this order for each instance's flags: z = 0 (kOpZero), z = best (kOpRestore),
+// best = z (kOpKeepBest), zeval = z + step p with locked entries 0 (kOpCandidate, sim.cpp:179)
+// or zeval = z (kOpEvalAtZ), zfinal = z (kOpFinal).
+__global__ void __launch_bounds__(kBlock) k_prepare(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                    double* __restrict__ z, double* __restrict__ best,
+                                                    double* __restrict__ zeval, const double* __restrict__ p,
+                                                    double* __restrict__ zfinal) {
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!mp.valid || !(c.flags & (kOpZero | kOpRestore | kOpKeepBest | kOpCandidate | kOpEvalAtZ | kOpFinal))) return;
+    const size_t b = 6 * size_t(mp.i);
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-        v[k] = -src[b + k];
-        if (locked[b + k]) v[k] = 0;
+        double v = z[b + k];
+        if (c.flags & kOpZero) v = 0;
+        if (c.flags & kOpRestore) v = best[b + k];
+        z[b + k] = v;
+        if (c.flags & kOpKeepBest) best[b + k] = v;
+        if (c.flags & kOpCandidate) zeval[b + k] = t.locked[b + k] ? 0.0 : v + c.step * p[b + k];
+        if (c.flags & kOpEvalAtZ) zeval[b + k] = v;
+        if (c.flags & kOpFinal) zfinal[b + k] = v;
     }
-    const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-    if (lt > mt) {
-        const double f = mt / lt;
-        v[0] *= f; v[1] *= f; v[2] *= f;
-    }
-    const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
-    if (lr > mr) {
-        const double f = mr / lr;
-        v[3] *= f; v[4] *= f; v[5] *= f;
-    }
+}
+
+// After an evaluation: g = geval for the instances that evaluated at z (kOpTakeGrad), and
+// for accepted trials (kOpAccept, sim.cpp:205-206) s = zeval - z, y = geval - g into the
+// history slot `target` (kOpPair), the partials of <s, y>, <s, s>, <y, y>, then z = zeval,
+// g = geval; best = z afterwards when kOpKeepBestAfter.
+__global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                   double* __restrict__ z, double* __restrict__ g,
+                                                   const double* __restrict__ zeval, const double* __restrict__ geval,
+                                                   double* __restrict__ S, double* __restrict__ Y, long long stride,
+                                                   double* __restrict__ best, double* __restrict__ part) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    const MapPos mp = map_pos(t.nblk);
+    const SolveCtl c = ctl[mp.inst];
+    if (!(c.flags & (kOpTakeGrad | kOpAccept))) return;
+    const size_t b = 6 * size_t(mp.i);
+    if (c.flags & kOpTakeGrad) {
+        if (mp.valid)
 #pragma unroll
-    for (int k = 0; k < 6; k++) p[b + k] = locked[b + k] ? 0.0 : v[k];
-}
-
-// zc = z + step p, locked entries zero (sim.cpp:179).
-__global__ void k_candidate(double* __restrict__ zc, const double* __restrict__ z, const double* __restrict__ p,
-                            double step, const uint8_t* __restrict__ locked, long long n) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        zc[i] = locked[i] ? 0.0 : z[i] + step * p[i];
-}
-
-// s = zc - z, y = gc - g (sim.cpp:205).
-__global__ void k_sy(double* __restrict__ s, double* __restrict__ y, const double* __restrict__ zc,
-                     const double* __restrict__ z, const double* __restrict__ gc, const double* __restrict__ g,
-                     long long n) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        s[i] = zc[i] - z[i];
-        y[i] = gc[i] - g[i];
+            for (int k = 0; k < 6; k++) g[b + k] = geval[b + k];
+        return;
     }
-}
-
-__global__ void k_rho(double* __restrict__ rho, const double* __restrict__ sy) { *rho = 1 / *sy; }
-
-inline unsigned vgrid(long long n) {
-    const unsigned g = grid_for(n);
-    return g < 4 * 152 ? g : 4 * 152;
+    double acc[3] = {0, 0, 0};
+    if (mp.valid) {
+        double sv[6], yv[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            sv[k] = zeval[b + k] - z[b + k];
+            yv[k] = geval[b + k] - g[b + k];
+        }
+        if (c.flags & kOpPair) {
+            double* s = S + stride * c.target + b;
+            double* y = Y + stride * c.target + b;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                s[k] = sv[k];
+                y[k] = yv[k];
+            }
+        }
+        acc[0] = dot6(sv, yv);
+        acc[1] = dot6(sv, sv);
+        acc[2] = dot6(yv, yv);
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            z[b + k] = zeval[b + k];
+            g[b + k] = geval[b + k];
+        }
+        if (c.flags & kOpKeepBestAfter)
+#pragma unroll
+            for (int k = 0; k < 6; k++) best[b + k] = zeval[b + k];
+    }
+    block_sum<3>(acc, sm);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = acc[0];
+        part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
+        part[2 * size_t(t.n_nblk) + blockIdx.x] = acc[2];
+    }
 }
 
 }  // namespace
 
-size_t lbfgs_part_doubles() { return 3 * kDotBlocks + 8; }
+size_t lbfgs_part_doubles(int n_nblk) { return 3 * size_t(n_nblk) + 8; }
 
-void dots(int k, const double* a0, const double* b0, const double* a1, const double* b1, const double* a2,
-          const double* b2, long long n, double* part, double* out, cudaStream_t s) {
-    if (k == 1) {
-        (k_dots_part<1><<<kDotBlocks, kBlock, 0, s>>>(a0, b0, a1, b1, a2, b2, n, part), note_launches(1));
-        (k_dots_final<1><<<1, kBlock, 0, s>>>(part, out), note_launches(1));
-    } else if (k == 2) {
-        (k_dots_part<2><<<kDotBlocks, kBlock, 0, s>>>(a0, b0, a1, b1, a2, b2, n, part), note_launches(1));
-        (k_dots_final<2><<<1, kBlock, 0, s>>>(part, out), note_launches(1));
-    } else {
-        (k_dots_part<3><<<kDotBlocks, kBlock, 0, s>>>(a0, b0, a1, b1, a2, b2, n, part), note_launches(1));
-        (k_dots_final<3><<<1, kBlock, 0, s>>>(part, out), note_launches(1));
+void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
+                  const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
+                  double* dg, double mt, double mr, cudaStream_t s) {
+    const int nb = t.n_nblk;
+    (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, H, p, g, S, Y, stride, part + 2 * size_t(nb)), note_launches(1));
+    for (int j = 0; j < max_m; j++) {
+        (k_tl_dot<1><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, part), note_launches(1));
+        (k_tl_update<1><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, rho, alpha, part), note_launches(1));
     }
-}
-
-void rms_max(const double* g, const uint8_t* locked, long long n, long long n_free, double* part, double* out2,
-             cudaStream_t s) {
-    (k_rms_max_part<<<kDotBlocks, kBlock, 0, s>>>(g, locked, n, part), note_launches(1));
-    (k_rms_max_final<<<1, kBlock, 0, s>>>(part, n_free, out2), note_launches(1));
-}
-
-void vcopy(double* dst, const double* src, long long n, cudaStream_t s) {
-    (k_copy<<<vgrid(n), kBlock, 0, s>>>(dst, src, n), note_launches(1));
-}
-
-void two_loop(double* p, const double* g, const double* const* S, const double* const* Y, const double* const* rho,
-              int m, double* alpha, double* scal, double* part, long long n, cudaStream_t s) {
-    (k_copy<<<vgrid(n), kBlock, 0, s>>>(p, g, n), note_launches(1));
-    for (int h = m - 1; h >= 0; h--) {
-        dots(1, S[h], p, nullptr, nullptr, nullptr, nullptr, n, part, scal, s);
-        (k_loop1_update<<<vgrid(n), kBlock, 0, s>>>(p, Y[h], n, rho[h], scal, alpha + h), note_launches(1));
+    (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, p, part + 2 * size_t(nb)), note_launches(1));
+    for (int j = 0; j < max_m; j++) {
+        (k_tl_dot<2><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, part), note_launches(1));
+        (k_tl_update<2><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, rho, alpha, part), note_launches(1));
     }
-    if (m > 0) dots(2, S[m - 1], Y[m - 1], Y[m - 1], Y[m - 1], nullptr, nullptr, n, part, scal + 1, s);
-    (k_scale_h0<<<vgrid(n), kBlock, 0, s>>>(p, n, scal + 1, m > 0 ? 1 : 0), note_launches(1));
-    for (int h = 0; h < m; h++) {
-        dots(1, Y[h], p, nullptr, nullptr, nullptr, nullptr, n, part, scal, s);
-        (k_loop2_update<<<vgrid(n), kBlock, 0, s>>>(p, S[h], n, rho[h], scal, alpha + h), note_launches(1));
-    }
+    (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
+    (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
 }
 
-void finish_direction(double* p, const double* src, const uint8_t* locked, int N, double mt, double mr,
-                      cudaStream_t s) {
-    (k_finish_dir<<<grid_for(N), kBlock, 0, s>>>(p, src, locked, N, mt, mr), note_launches(1));
+void bl_steepest(const DevTopo& t, const SolveCtl* ctl, double* p, const double* g, double* part, double* dg,
+                 double mt, double mr, cudaStream_t s) {
+    (k_finish<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, kOpSteepest, p, g, g, mt, mr, part), note_launches(1));
+    (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpSteepest, part, dg), note_launches(1));
 }
 
-void candidate(double* zc, const double* z, const double* p, double step, const uint8_t* locked, long long n,
-               cudaStream_t s) {
-    (k_candidate<<<vgrid(n), kBlock, 0, s>>>(zc, z, p, step, locked, n), note_launches(1));
+void bl_prepare(const DevTopo& t, const SolveCtl* ctl, double* z, double* best, double* zeval, const double* p,
+                double* zfinal, cudaStream_t s) {
+    (k_prepare<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, z, best, zeval, p, zfinal), note_launches(1));
 }
 
-void make_sy(double* sv, double* yv, const double* zc, const double* z, const double* gc, const double* g,
-             long long n, cudaStream_t s) {
-    (k_sy<<<vgrid(n), kBlock, 0, s>>>(sv, yv, zc, z, gc, g, n), note_launches(1));
+void bl_accept(const DevTopo& t, const SolveCtl* ctl, double* z, double* g, const double* zeval, const double* geval,
+               double* S, double* Y, long long stride, double* best, double* part, double* out3, cudaStream_t s) {
+    (k_accept<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, z, g, zeval, geval, S, Y, stride, best, part), note_launches(1));
+    (k_inst_final<3><<<t.I, kBlock, 0, s>>>(t, ctl, kOpAccept, part, out3), note_launches(1));
 }
-
-void set_rho(double* rho, const double* sy, cudaStream_t s) { (k_rho<<<1, 1, 0, s>>>(rho, sy), note_launches(1)); }
 
 }  // namespace mcg

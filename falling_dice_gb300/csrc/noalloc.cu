@@ -121,7 +121,6 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.n_items = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_sorted = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_long = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
-    c.part = reinterpret_cast<double*>(take(size_t(3 * contact_part_blocks(kNoAllocContacts)) * 8));
     long long scan_n = S + 1;
     if (kNoAllocBins + 1 > scan_n) scan_n = kNoAllocBins + 1;
     if (chunks + 1 > scan_n) scan_n = chunks + 1;

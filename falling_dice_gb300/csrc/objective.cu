@@ -14,51 +14,58 @@
 
 namespace mcg {
 
+static_assert(kMapBlock == kBlock, "mapped blocks are launched with kBlock threads");
+
 int nb_nodes(int N) { return int(grid_for(N)); }
 int nb_beams(int B) { return int(grid_for(B)); }
 
 // ---- node state: MC/src/sim.cpp:136 -------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uint8_t* __restrict__ locked,
-                                                  const double* __restrict__ z, const double* __restrict__ bx,
-                                                  const double* __restrict__ br, double4_32a* __restrict__ x4,
-                                                  double4_32a* __restrict__ R4, double4_32a* __restrict__ M4,
-                                                  float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
-                                                  double* __restrict__ part) {
+__global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const double* __restrict__ z,
+                                                  const double* __restrict__ bx, const double* __restrict__ br,
+                                                  double4_32a* __restrict__ x4, double4_32a* __restrict__ R4,
+                                                  double4_32a* __restrict__ M4, float4* __restrict__ xf_lo,
+                                                  float4* __restrict__ xf_hi, double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const MapPos mp = map_pos(t.nblk);
+    const int i = mp.i;
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
     double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
-    if (i < N) {
+    if (mp.valid) {
         const double* zi = z + 6 * size_t(i);
-        const uint8_t* li = locked + 6 * size_t(i);
-        double t[3], r[3];
+        const uint8_t* li = t.locked + 6 * size_t(i);
+        double tr[3], r[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            t[d] = li[d] ? 0.0 : zi[d];
+            tr[d] = li[d] ? 0.0 : zi[d];
             r[d] = li[d + 3] ? 0.0 : zi[d + 3];
         }
         // x = base + s t, rounded exactly as the reference (no fused multiply-add), so that
         // positions -- and with them the contact pair set -- are bit-identical.
         const double ts = p.translation_scale;
-        const double xx = __dadd_rn(bx[3 * size_t(i)], __dmul_rn(ts, t[0]));
-        const double xy = __dadd_rn(bx[3 * size_t(i) + 1], __dmul_rn(ts, t[1]));
-        const double xz = __dadd_rn(bx[3 * size_t(i) + 2], __dmul_rn(ts, t[2]));
+        const double xx = __dadd_rn(bx[3 * size_t(i)], __dmul_rn(ts, tr[0]));
+        const double xy = __dadd_rn(bx[3 * size_t(i) + 1], __dmul_rn(ts, tr[1]));
+        const double xz = __dadd_rn(bx[3 * size_t(i) + 2], __dmul_rn(ts, tr[2]));
         const q4 b{br[4 * size_t(i)], br[4 * size_t(i) + 1], br[4 * size_t(i) + 2], br[4 * size_t(i) + 3]};
         const q4 R = qnorm(qmul(exp_map(d3{r[0], r[1], r[2]}), b));
         x4[i] = make_double4_32a(xx, xy, xz, 0.0);
-        // single-precision bounds of the position for the contact broad phase
-        xf_lo[i] = make_float4(__double2float_rd(xx), __double2float_rd(xy), __double2float_rd(xz), 0.f);
-        xf_hi[i] = make_float4(__double2float_ru(xx), __double2float_ru(xy), __double2float_ru(xz), 0.f);
+        // single-precision bounds of the position in the contact grid's frame (the
+        // instance's offset added with outward rounding)
+        const float2 o = t.off[mp.inst];
+        xf_lo[i] = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
+                               __fadd_rd(__double2float_rd(xz), o.y), 0.f);
+        xf_hi[i] = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
+                               __fadd_ru(__double2float_ru(xz), o.y), 0.f);
         R4[i] = make_double4_32a(R.w, R.x, R.y, R.z);
         const m3 M = quat_matrix(R);
         M4[3 * size_t(i)] = make_double4_32a(M.r0.x, M.r0.y, M.r0.z, 0.0);
         M4[3 * size_t(i) + 1] = make_double4_32a(M.r1.x, M.r1.y, M.r1.z, 0.0);
         M4[3 * size_t(i) + 2] = make_double4_32a(M.r2.x, M.r2.y, M.r2.z, 0.0);
         acc[0] = xx; acc[1] = xy; acc[2] = xz;
-        // bounding box for the contact grid; fmin/fmax skip NaN coordinates
-        mx[0] = -xx; mx[1] = -xy; mx[2] = -xz; mx[3] = xx; mx[4] = xy; mx[5] = xz;
+        // bounding box in the grid's frame; fmin/fmax skip NaN coordinates
+        const double gx = xx + double(o.x), gz = xz + double(o.y);
+        mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
     }
     block_sum<3>(acc, sm);
 #pragma unroll
@@ -71,16 +78,24 @@ __global__ void __launch_bounds__(kBlock) k_state(int N, PhysParams p, const uin
     }
 }
 
-// Mean position over all nodes (MC/src/sim.cpp:143) and the node bounding box, from the
-// k_state partials: cen[0..2] mean, cen[3..5] minimum, cen[6..8] maximum.
-__global__ void __launch_bounds__(kBlock) k_center(int N, int nparts, const double* __restrict__ part,
+// Mean position of each instance's nodes (MC/src/sim.cpp:143) and bounding boxes from the
+// k_state partials: block i < I writes instance i's cen[9i..9i+8] (mean, minimum, maximum);
+// block I the minimum and maximum over all instances at cen[9I + 3..8].
+__global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __restrict__ part,
                                                    double* __restrict__ cen) {
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
+    const int inst = blockIdx.x;
+    int k0 = 0, k1 = t.n_nblk;
+    if (inst < t.I) {
+        const int4 r = t.irange[inst];
+        k0 = r.x;
+        k1 = r.y;
+    }
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
     double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    for (int k = k0 + int(threadIdx.x); k < k1; k += blockDim.x) {
         const double* q = part + 9 * size_t(k);
         acc[0] += q[0]; acc[1] += q[1]; acc[2] += q[2];
 #pragma unroll
@@ -90,10 +105,13 @@ __global__ void __launch_bounds__(kBlock) k_center(int N, int nparts, const doub
 #pragma unroll
     for (int j = 0; j < 6; j++) mx[j] = block_max(mx[j], smx);
     if (threadIdx.x == 0) {
-        const double inv = 1.0 / double(N);
-        cen[0] = acc[0] * inv; cen[1] = acc[1] * inv; cen[2] = acc[2] * inv;
-        cen[3] = -mx[0]; cen[4] = -mx[1]; cen[5] = -mx[2];
-        cen[6] = mx[3]; cen[7] = mx[4]; cen[8] = mx[5];
+        double* c = cen + 9 * size_t(inst);
+        if (inst < t.I) {
+            const double inv = 1.0 / double(t.inst_n[inst]);
+            c[0] = acc[0] * inv; c[1] = acc[1] * inv; c[2] = acc[2] * inv;
+        }
+        c[3] = -mx[0]; c[4] = -mx[1]; c[5] = -mx[2];
+        c[6] = mx[3]; c[7] = mx[4]; c[8] = mx[5];
     }
 }
 
@@ -169,10 +187,11 @@ __device__ __forceinline__ d3 unit_fast(d3 v) {
 __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const double* __restrict__ plastic,
                                                   int trials, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const MapPos mp = map_pos(t.bblk);
+    const int b = mp.i;
     const int B = t.B;
     double acc[3] = {0, 0, 0};  // energy, elastic, plastic
-    if (b < B) {
+    if (mp.valid) {
         const int2 ab = t.ab[b];
         const d3 xa = ldx(e.x, ab.x), xb = ldx(e.x, ab.y);
         // chord, length and tangent rounded as the reference (no fused multiply-add), so
@@ -200,7 +219,7 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
             const d3 tt{__dmul_rn(d.x, invL), __dmul_rn(d.y, invL), __dmul_rn(d.z, invL)};
             // axial
             const double eps = (L - t.L0[b]) * t.invL0[b];
-            const Ret1 ax = return1(eps, pl_epsp, pl_alpha, m.E, m.sy, m.H, m.inv_EH);
+            const Ret1 ax = return1(eps, pl_epsp, pl_alpha, m.E, t.sy[b], m.H, m.inv_EH);
             const double aL = t.aL[b];
             const double uax = aL * (ax.energy + ax.hard);
             const double dax = t.aLsy[b] * ax.dg;
@@ -298,13 +317,16 @@ __device__ __forceinline__ d3 contact_slot_force(const ContactBufs& c, const Phy
 }
 
 // One item of a node's contact list: its force, and for slot 0 (the first node of the
-// lower shape, present for every contact) the contact's penalty energy (sim.cpp:163).
+// lower shape, present for every contact) the contact's penalty energy, count and
+// penetration (sim.cpp:163-164).
 __device__ __forceinline__ void add_contact_item(const ContactBufs& c, const PhysParams& p, int N, uint32_t item,
-                                                 d3& gx, double& energy) {
+                                                 d3& gx, double& energy, double& count, double& pen_max) {
     gx = gx + contact_slot_force(c, p, N, item);
     if ((item & 3u) == 0) {
         const double pen = c.c_pen[item >> 2];
         energy += .5 * p.contact_k * pen * pen;
+        count += 1;
+        pen_max = fmax(pen_max, pen);
     }
 }
 
@@ -341,13 +363,16 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
 template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
-    __shared__ double sm[5 * (kBlock / 32)];
+    __shared__ double sm[6 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const MapPos mp = map_pos(t.nblk);
+    const int i = mp.i;
     const int N = t.N;
-    double acc[5] = {0, 0, 0, 0, 0};  // gravity E, platen E, reaction, platen contacts, self-contact E
-    double pen_max = 0;
-    if (i < N) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};  // gravity E, platen E, reaction, contacts, self-contact E, |g|^2
+    double pen_max = 0, gmax = 0;
+    if (mp.valid) {
+        const double* cen = e.cen + 9 * size_t(mp.inst);
+        const double Ni = double(t.inst_n[mp.inst]);
         d3 gx{0, 0, 0}, gr{0, 0, 0};
         sum_slots<F32>(t, e, i, gx, gr);
         const d3 xi = ldx(e.x, i);
@@ -356,15 +381,16 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         acc[0] = mg * xi.y;
         gx.y += mg;
         // centering (sim.cpp:143)
-        gx.x += p.centering * e.cen[0] / double(N);
-        gx.z += p.centering * e.cen[2] / double(N);
+        gx.x += p.centering * cen[0] / Ni;
+        gx.z += p.centering * cen[2] / Ni;
         // self-contact forces on this node in ascending (lower shape, higher shape, slot)
         // order (the list is sorted by the contact pipeline), and the self-contact energy of
         // each contact on the first node of its lower shape: both independent of the order
         // of the contact list
         if (use_contacts) {
             const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
-            for (uint32_t k = 0; k < cnt; k++) add_contact_item(c, p, N, c.n_sorted[s0 + k], gx, acc[4]);
+            for (uint32_t k = 0; k < cnt; k++)
+                add_contact_item(c, p, N, c.n_sorted[s0 + k], gx, acc[4], acc[3], pen_max);
         }
         // platens (sim.cpp:168-171)
         const double jr = p.joint_radius, kc = p.contact_k;
@@ -376,7 +402,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
             acc[3] += 1;
             gx.y -= mm;
         }
-        const double pt = xi.y + jr - p.top;
+        const double pt = xi.y + jr - e.tops[mp.inst];
         if (pt > 0) {
             const double mm = kc * pt;
             acc[1] += .5 * kc * pt * pt;
@@ -389,52 +415,58 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         const double ts = p.translation_scale;
         const uint8_t* li = t.locked + 6 * size_t(i);
         double* g = grad + 6 * size_t(i);
-        g[0] = li[0] ? 0.0 : ts * gx.x;
-        g[1] = li[1] ? 0.0 : ts * gx.y;
-        g[2] = li[2] ? 0.0 : ts * gx.z;
-        g[3] = li[3] ? 0.0 : gr.x;
-        g[4] = li[4] ? 0.0 : gr.y;
-        g[5] = li[5] ? 0.0 : gr.z;
+        const double gv[6] = {ts * gx.x, ts * gx.y, ts * gx.z, gr.x, gr.y, gr.z};
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            g[k] = li[k] ? 0.0 : gv[k];
+            // residual over free DOFs for the solver's convergence test (sim.cpp:44-45)
+            if (!li[k]) {
+                acc[5] += gv[k] * gv[k];
+                gmax = fmax(gmax, fabs(gv[k]));
+            }
+        }
     }
-    block_sum<5>(acc, sm);
+    block_sum<6>(acc, sm);
     pen_max = block_max(pen_max, smx);
+    gmax = block_max(gmax, smx);
     if (threadIdx.x == 0) {
         double* q = e.part_node + kNodeParts * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = pen_max; q[4] = acc[3]; q[5] = acc[4];
+        q[6] = acc[5]; q[7] = gmax;
     }
 }
 
 // ---- totals and the non-finite guard ---------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, PhysParams p,
-                                                     const double* __restrict__ pbeam,
+__global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, const double* __restrict__ pbeam,
                                                      const double* __restrict__ pnode,
-                                                     const double* __restrict__ pcont,
                                                      const double* __restrict__ cen,
-                                                     const uint32_t* __restrict__ flags, EvalOut* out) {
+                                                     const uint32_t* __restrict__ flags, EvalOut* out_all) {
     __shared__ double sm[6 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
+    const int inst = blockIdx.x;
+    const int4 r = t.irange[inst];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
-    double cacc[3] = {0, 0, 0};          // contactE, contacts(platen), contacts(self)
-    double pmax = 0;
-    for (int k = threadIdx.x; k < nbb; k += blockDim.x) {
+    double cacc[3] = {0, 0, 0};          // self-contact E, contacts (platen and self), |g|^2
+    double pmax = 0, gmax = 0;
+    for (int k = r.z + int(threadIdx.x); k < r.w; k += blockDim.x) {
         acc[0] += pbeam[3 * k]; acc[1] += pbeam[3 * k + 1]; acc[2] += pbeam[3 * k + 2];
     }
-    for (int k = threadIdx.x; k < nbn; k += blockDim.x) {
+    for (int k = r.x + int(threadIdx.x); k < r.y; k += blockDim.x) {
         const double* q = pnode + kNodeParts * size_t(k);
         acc[3] += q[0]; acc[4] += q[1]; acc[5] += q[2];
         pmax = fmax(pmax, q[3]);
         cacc[1] += q[4];
         cacc[0] += q[5];
-    }
-    for (int k = threadIdx.x; k < ncp; k += blockDim.x) {
-        pmax = fmax(pmax, pcont[3 * k + 1]);
-        cacc[2] += pcont[3 * k + 2];
+        cacc[2] += q[6];
+        gmax = fmax(gmax, q[7]);
     }
     block_sum<6>(acc, sm);
     block_sum<3>(cacc, sm);
     pmax = block_max(pmax, smx);
+    gmax = block_max(gmax, smx);
     if (threadIdx.x == 0) {
-        const double center = .5 * p.centering * (sqr(cen[0]) + sqr(cen[2]));
+        const double* c = cen + 9 * size_t(inst);
+        const double center = .5 * p.centering * (sqr(c[0]) + sqr(c[2]));
         const double contactE = cacc[0];
         // Group order of the reference's accumulation: beams, gravity, centering,
         // self-contact, platens (sim.cpp:139-171).
@@ -444,13 +476,14 @@ __global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, 
         energy += contactE;
         energy += acc[4];
         const int nonfinite = isfinite(energy) ? 0 : 1;
+        EvalOut* out = out_all + inst;
         out->energy = nonfinite ? __longlong_as_double(0x7ff0000000000000LL) : energy;
         out->elastic = acc[1];
         out->plastic = acc[2];
         out->contact = contactE + acc[4];
         out->reaction = acc[5];
         out->max_pen = pmax;
-        out->contacts = int(cacc[1] + cacc[2]);
+        out->contacts = int(cacc[1]);
         out->nonfinite = nonfinite;
         out->beam_energy = acc[0];
         out->node_energy = acc[3];
@@ -458,35 +491,56 @@ __global__ void __launch_bounds__(kBlock) k_finalize(int nbb, int nbn, int ncp, 
         out->contact_energy = contactE;
         out->platen_energy = acc[4];
         out->overflow = flags ? int(flags[0] & ~uint32_t(kNonFinite)) : 0;
+        // a non-finite evaluation has a zero gradient (k_zero_if_nonfinite)
+        const long long nf = t.inst_free[inst];
+        out->rms = nonfinite ? 0.0 : (nf ? sqrt(cacc[2] / double(nf)) : 0.0);
+        out->gmax = nonfinite ? 0.0 : gmax;
     }
 }
 
-// Non-finite energy: the whole gradient is zero (sim.cpp:172).
-__global__ void k_zero_if_nonfinite(long long n, const EvalOut* out, double* grad) {
-    if (!out->nonfinite) return;
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-        grad[k] = 0;
+// Non-finite energy: the instance's whole gradient is zero (sim.cpp:172).
+__global__ void __launch_bounds__(kBlock) k_zero_if_nonfinite(DevTopo t, const EvalOut* __restrict__ out,
+                                                              double* __restrict__ grad) {
+    const MapPos mp = map_pos(t.nblk);
+    if (!mp.valid || !out[mp.inst].nonfinite) return;
+#pragma unroll
+    for (int k = 0; k < 6; k++) grad[6 * size_t(mp.i) + k] = 0;
 }
 
 // ---- commit (MC/src/sim.cpp:212): base state <- current state, plastic <- trial ----------
-__global__ void __launch_bounds__(kBlock) k_commit_nodes(int N, const double4_32a* __restrict__ x4,
+__global__ void __launch_bounds__(kBlock) k_commit_nodes(DevTopo t, const uint8_t* __restrict__ mask,
+                                                         const double4_32a* __restrict__ x4,
                                                          const double4_32a* __restrict__ R4, double* __restrict__ bx,
                                                          double* __restrict__ br) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
+    const MapPos mp = map_pos(t.nblk);
+    if (!mp.valid || (mask && !mask[mp.inst])) return;
+    const int i = mp.i;
     const double4_32a x = x4[i], r = R4[i];
     bx[3 * size_t(i)] = x.x; bx[3 * size_t(i) + 1] = x.y; bx[3 * size_t(i) + 2] = x.z;
     br[4 * size_t(i)] = r.x; br[4 * size_t(i) + 1] = r.y; br[4 * size_t(i) + 2] = r.z; br[4 * size_t(i) + 3] = r.w;
 }
 
-// Plastic statistics of the committed state (MC/src/sim.cpp:339-362): sum and max of
-// |epsp|, sum and max of |rotp|, counts above 1e-5 and 1e-4.
-__global__ void __launch_bounds__(kBlock) k_plastic_part(int B, const double* __restrict__ pl, double* __restrict__ part) {
+// plastic <- trial.next for the beams of the committed instances (7 SoA arrays)
+__global__ void __launch_bounds__(kBlock) k_commit_plastic(DevTopo t, const uint8_t* __restrict__ mask,
+                                                           const double* __restrict__ next, double* __restrict__ pl) {
+    const MapPos mp = map_pos(t.bblk);
+    if (!mp.valid || (mask && !mask[mp.inst])) return;
+#pragma unroll
+    for (int k = 0; k < 7; k++) pl[k * size_t(t.B) + mp.i] = next[k * size_t(t.B) + mp.i];
+}
+
+// Plastic statistics of the committed state (MC/src/sim.cpp:339-362), one partial per beam
+// block: sum and max of |epsp|, sum and max of |rotp|, counts above 1e-5 and 1e-4.
+__global__ void __launch_bounds__(kBlock) k_plastic_part(DevTopo t, const double* __restrict__ pl,
+                                                         double* __restrict__ part) {
     __shared__ double sm[4 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
+    const MapPos mp = map_pos(t.bblk);
+    const int B = t.B;
     double acc[4] = {0, 0, 0, 0};
     double m0 = 0, m1 = 0;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+    if (mp.valid) {
+        const int b = mp.i;
         const double pa = fabs(pl[b]);
         const d3 r{pl[2 * size_t(B) + b], pl[3 * size_t(B) + b], pl[4 * size_t(B) + b]};
         const double pr = len(r);
@@ -503,13 +557,15 @@ __global__ void __launch_bounds__(kBlock) k_plastic_part(int B, const double* __
         q[0] = acc[0]; q[1] = m0; q[2] = acc[1]; q[3] = m1; q[4] = acc[2]; q[5] = acc[3];
     }
 }
-__global__ void __launch_bounds__(kBlock) k_plastic_final(int nparts, const double* __restrict__ part,
+// One block per instance over its beam blocks.
+__global__ void __launch_bounds__(kBlock) k_plastic_final(DevTopo t, const double* __restrict__ part,
                                                           double* __restrict__ out) {
     __shared__ double sm[4 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
+    const int4 r = t.irange[blockIdx.x];
     double acc[4] = {0, 0, 0, 0};
     double m0 = 0, m1 = 0;
-    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    for (int k = r.z + int(threadIdx.x); k < r.w; k += blockDim.x) {
         const double* q = part + 6 * size_t(k);
         acc[0] += q[0]; acc[1] += q[2]; acc[2] += q[4]; acc[3] += q[5];
         m0 = fmax(m0, q[1]); m1 = fmax(m1, q[3]);
@@ -518,43 +574,45 @@ __global__ void __launch_bounds__(kBlock) k_plastic_final(int nparts, const doub
     m0 = block_max(m0, smx);
     m1 = block_max(m1, smx);
     if (threadIdx.x == 0) {
-        out[0] = acc[0]; out[1] = m0; out[2] = acc[1]; out[3] = m1; out[4] = acc[2]; out[5] = acc[3];
+        double* o = out + 6 * size_t(blockIdx.x);
+        o[0] = acc[0]; o[1] = m0; o[2] = acc[1]; o[3] = m1; o[4] = acc[2]; o[5] = acc[3];
     }
 }
 
 // ---- launchers ------------------------------------------------------------------------------
 void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                   const double* base_r, EvalBufs& e, cudaStream_t s) {
-    const int nb = nb_nodes(t.N);
-    k_state<<<nb, kBlock, 0, s>>>(t.N, p, t.locked, z, base_x, base_r, e.x, e.R, e.M, e.xf_lo, e.xf_hi,
-                                  e.part_state);
+    k_state<<<t.n_nblk, kBlock, 0, s>>>(t, p, z, base_x, base_r, e.x, e.R, e.M, e.xf_lo, e.xf_hi, e.part_state);
     note_launches(1);
-    launch_center(t.N, e, s);
+    launch_center(t, e, s);
 }
 
-void launch_center(int N, EvalBufs& e, cudaStream_t s) {
-    k_center<<<1, kBlock, 0, s>>>(N, nb_nodes(N), e.part_state, e.cen);
+void launch_center(const DevTopo& t, EvalBufs& e, cudaStream_t s) {
+    k_center<<<t.I + 1, kBlock, 0, s>>>(t, e.part_state, e.cen);
     note_launches(1);
 }
 
-void launch_commit(int N, int B, const EvalBufs& e, double* base_x, double* base_r, double* plastic, cudaStream_t s) {
-    k_commit_nodes<<<grid_for(N), kBlock, 0, s>>>(N, e.x, e.R, base_x, base_r);
+void launch_commit(const DevTopo& t, const uint8_t* mask, const EvalBufs& e, double* base_x, double* base_r,
+                   double* plastic, cudaStream_t s) {
+    k_commit_nodes<<<t.n_nblk, kBlock, 0, s>>>(t, mask, e.x, e.R, base_x, base_r);
     note_launches(1);
-    if (B > 0 && plastic)
-        cudaMemcpyAsync(plastic, e.trial_next, 7 * size_t(B) * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (t.B > 0 && plastic) {
+        k_commit_plastic<<<t.n_bblk, kBlock, 0, s>>>(t, mask, e.trial_next, plastic);
+        note_launches(1);
+    }
 }
 
-void launch_plastic_stats(int B, const double* plastic, double* part, double* out6, cudaStream_t s) {
-    constexpr int nparts = 64;
-    k_plastic_part<<<nparts, kBlock, 0, s>>>(B, plastic, part);
-    k_plastic_final<<<1, kBlock, 0, s>>>(nparts, part, out6);
+void launch_plastic_stats(const DevTopo& t, const double* plastic, double* part, double* out6, cudaStream_t s) {
+    if (t.B == 0) return;
+    k_plastic_part<<<t.n_bblk, kBlock, 0, s>>>(t, plastic, part);
+    k_plastic_final<<<t.I, kBlock, 0, s>>>(t, part, out6);
     note_launches(2);
 }
 
 void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials, EvalBufs& e,
                   cudaStream_t s) {
     if (t.B == 0) return;
-    k_beams<<<nb_beams(t.B), kBlock, 0, s>>>(t, m, plastic, trials ? 1 : 0, e);
+    k_beams<<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, trials ? 1 : 0, e);
     note_launches(1);
 }
 
@@ -562,7 +620,7 @@ void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, 
                    cudaStream_t s) {
     ContactBufs cc{};
     if (c) cc = *c;
-    k_gather<false><<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
+    k_gather<false><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
     note_launches(1);
 }
 
@@ -570,17 +628,14 @@ void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBuf
                          cudaStream_t s) {
     ContactBufs cc{};
     if (c) cc = *c;
-    k_gather<true><<<nb_nodes(t.N), kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
+    k_gather<true><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
     note_launches(1);
 }
 
 void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
                      cudaStream_t s) {
-    const int ncp = c ? contact_part_blocks(c->contact_cap) : 0;
-    k_finalize<<<1, kBlock, 0, s>>>(t.B ? nb_beams(t.B) : 0, nb_nodes(t.N), ncp, p, e.part_beam, e.part_node,
-                                    c ? c->part : nullptr, e.cen, c ? c->flags : nullptr, e.out);
-    const long long n = 6LL * t.N;
-    k_zero_if_nonfinite<<<grid_for(n < 152 * 4 * kBlock ? n : 152 * 4 * kBlock), kBlock, 0, s>>>(n, e.out, grad);
+    k_finalize<<<t.I, kBlock, 0, s>>>(t, p, e.part_beam, e.part_node, e.cen, c ? c->flags : nullptr, e.out);
+    k_zero_if_nonfinite<<<t.n_nblk, kBlock, 0, s>>>(t, e.out, grad);
     note_launches(2);
 }
 

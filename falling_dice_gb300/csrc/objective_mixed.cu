@@ -160,27 +160,28 @@ __device__ __forceinline__ f3 jl_inv_t_f(f3 p, f3 v) {
 // ---- node state --------------------------------------------------------------------------
 // u = s t (FP32), e = exp(r) as (w - 1, v) (FP32), x = x_base + u (FP64, for contact,
 // platen and centering), FP32 position bounds; block partial sums and extrema of x.
-__global__ void __launch_bounds__(kBlock) k_state_mixed(int N, double ts, const uint8_t* __restrict__ locked,
-                                                        const double* __restrict__ z, const double* __restrict__ bx,
-                                                        float4* __restrict__ U, float4* __restrict__ Ei,
-                                                        double4_32a* __restrict__ x4, float4* __restrict__ xf_lo,
-                                                        float4* __restrict__ xf_hi, double* __restrict__ part) {
+__global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, const double* __restrict__ z,
+                                                        const double* __restrict__ bx, float4* __restrict__ U,
+                                                        float4* __restrict__ Ei, double4_32a* __restrict__ x4,
+                                                        float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
+                                                        double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const MapPos mp = map_pos(t.nblk);
+    const int i = mp.i;
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
     double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
-    if (i < N) {
+    if (mp.valid) {
         const double* zi = z + 6 * size_t(i);
-        const uint8_t* li = locked + 6 * size_t(i);
-        float t[3], r[3];
+        const uint8_t* li = t.locked + 6 * size_t(i);
+        float tr[3], r[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            t[d] = li[d] ? 0.f : float(zi[d] * ts);
+            tr[d] = li[d] ? 0.f : float(zi[d] * ts);
             r[d] = li[d + 3] ? 0.f : float(zi[d + 3]);
         }
-        U[i] = make_float4(t[0], t[1], t[2], 0.f);
+        U[i] = make_float4(tr[0], tr[1], tr[2], 0.f);
         const float th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
         float wm1, sv;  // cos(th/2) - 1 and sin(th/2)/th
         if (th2 < 1e-6f) {
@@ -195,14 +196,18 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(int N, double ts, const 
             sv = sh / th;
         }
         Ei[i] = make_float4(wm1, r[0] * sv, r[1] * sv, r[2] * sv);
-        const double xx = bx[3 * size_t(i)] + double(t[0]);
-        const double xy = bx[3 * size_t(i) + 1] + double(t[1]);
-        const double xz = bx[3 * size_t(i) + 2] + double(t[2]);
+        const double xx = bx[3 * size_t(i)] + double(tr[0]);
+        const double xy = bx[3 * size_t(i) + 1] + double(tr[1]);
+        const double xz = bx[3 * size_t(i) + 2] + double(tr[2]);
         x4[i] = make_double4_32a(xx, xy, xz, 0.0);
-        xf_lo[i] = make_float4(__double2float_rd(xx), __double2float_rd(xy), __double2float_rd(xz), 0.f);
-        xf_hi[i] = make_float4(__double2float_ru(xx), __double2float_ru(xy), __double2float_ru(xz), 0.f);
+        const float2 o = t.off[mp.inst];
+        xf_lo[i] = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
+                               __fadd_rd(__double2float_rd(xz), o.y), 0.f);
+        xf_hi[i] = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
+                               __fadd_ru(__double2float_ru(xz), o.y), 0.f);
         acc[0] = xx; acc[1] = xy; acc[2] = xz;
-        mx[0] = -xx; mx[1] = -xy; mx[2] = -xz; mx[3] = xx; mx[4] = xy; mx[5] = xz;
+        const double gx = xx + double(o.x), gz = xz + double(o.y);
+        mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
     }
     block_sum<3>(acc, sm);
 #pragma unroll
@@ -269,10 +274,11 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    const MapPos mp = map_pos(t.bblk);
+    const int b = mp.i;
     const int B = t.B;
     float acc[3] = {0.f, 0.f, 0.f};
-    if (b < B) {
+    if (mp.valid) {
         const int2 ab = t.ab[b];
         const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B3 = m.B3[b], B4 = m.B4[b], B5 = m.B5[b];
         const float4 ua4 = U[ab.x], ub4 = U[ab.y];
@@ -299,7 +305,7 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
             const float eps = q / ((L + L0) * L0);
             const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), rotp
             const float4 C0 = m.C0[b], C1 = m.C1[b];  // (kb, kt, my, ty), (cs, aL, area, aLsy)
-            const float E = float(mat.E), H = float(mat.H), sy = float(mat.sy);
+            const float E = float(mat.E), H = float(mat.H), sy = float(t.sy[b]);
             // axial
             const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
             const float uax = C1.y * (ax.energy + ax.hard);
@@ -393,11 +399,13 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
 
 // Plastic state of the mixed form: (epsp, alpha, alphaB, alphaT) and rotp as float4 pairs,
 // from/to the 7-array SoA trial layout.
-__global__ void __launch_bounds__(kBlock) k_plastic_pack(int B, const float* __restrict__ soa7, float4* __restrict__ P0,
+__global__ void __launch_bounds__(kBlock) k_plastic_pack(DevTopo t, const uint8_t* __restrict__ mask,
+                                                         const float* __restrict__ soa7, float4* __restrict__ P0,
                                                          float4* __restrict__ P1) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    const size_t S = size_t(B);
+    const MapPos mp = map_pos(t.bblk);
+    if (!mp.valid || (mask && !mask[mp.inst])) return;
+    const int b = mp.i;
+    const size_t S = size_t(t.B);
     P0[b] = make_float4(soa7[b], soa7[S + b], soa7[5 * S + b], soa7[6 * S + b]);
     P1[b] = make_float4(soa7[2 * S + b], soa7[3 * S + b], soa7[4 * S + b], 0.f);
 }
@@ -409,11 +417,13 @@ __global__ void __launch_bounds__(kBlock) k_plastic_from_f64(int B, const double
     P0[b] = make_float4(float(soa7[b]), float(soa7[S + b]), float(soa7[5 * S + b]), float(soa7[6 * S + b]));
     P1[b] = make_float4(float(soa7[2 * S + b]), float(soa7[3 * S + b]), float(soa7[4 * S + b]), 0.f);
 }
-__global__ void __launch_bounds__(kBlock) k_plastic_to_f64(int B, const float4* __restrict__ P0,
+__global__ void __launch_bounds__(kBlock) k_plastic_to_f64(DevTopo t, const uint8_t* __restrict__ mask,
+                                                           const float4* __restrict__ P0,
                                                            const float4* __restrict__ P1, double* __restrict__ soa7) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B) return;
-    const size_t S = size_t(B);
+    const MapPos mp = map_pos(t.bblk);
+    if (!mp.valid || (mask && !mask[mp.inst])) return;
+    const int b = mp.i;
+    const size_t S = size_t(t.B);
     const float4 p = P0[b], r = P1[b];
     soa7[b] = p.x; soa7[S + b] = p.y; soa7[2 * S + b] = r.x; soa7[3 * S + b] = r.y; soa7[4 * S + b] = r.z;
     soa7[5 * S + b] = p.z; soa7[6 * S + b] = p.w;
@@ -427,17 +437,16 @@ __global__ void k_f32_to_f64(long long n, const float* __restrict__ a, double* _
 
 void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                         const MixedNodes& mn, EvalBufs& e, cudaStream_t s) {
-    const int nb = nb_nodes(t.N);
-    k_state_mixed<<<nb, kBlock, 0, s>>>(t.N, p.translation_scale, t.locked, z, base_x, mn.U, mn.E, e.x, e.xf_lo,
-                                        e.xf_hi, e.part_state);
+    k_state_mixed<<<t.n_nblk, kBlock, 0, s>>>(t, p.translation_scale, z, base_x, mn.U, mn.E, e.x, e.xf_lo, e.xf_hi,
+                                              e.part_state);
     note_launches(1);
-    launch_center(t.N, e, s);
+    launch_center(t, e, s);
 }
 
 void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
                         EvalBufs& e, cudaStream_t s) {
     if (t.B == 0) return;
-    k_beams_mixed<<<nb_beams(t.B), kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
+    k_beams_mixed<<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
     note_launches(1);
 }
 
@@ -457,16 +466,18 @@ void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s) {
     note_launches(1);
 }
 
-void launch_plastic_mixed(int B, const double* plastic64, const float* trial32, MixedBeams& mb, cudaStream_t s) {
-    if (!B) return;
-    if (trial32) k_plastic_pack<<<grid_for(B), kBlock, 0, s>>>(B, trial32, mb.P0, mb.P1);
-    else k_plastic_from_f64<<<grid_for(B), kBlock, 0, s>>>(B, plastic64, mb.P0, mb.P1);
+void launch_plastic_mixed(const DevTopo& t, const uint8_t* mask, const double* plastic64, const float* trial32,
+                          MixedBeams& mb, cudaStream_t s) {
+    if (!t.B) return;
+    if (trial32) k_plastic_pack<<<t.n_bblk, kBlock, 0, s>>>(t, mask, trial32, mb.P0, mb.P1);
+    else k_plastic_from_f64<<<grid_for(t.B), kBlock, 0, s>>>(t.B, plastic64, mb.P0, mb.P1);
     note_launches(1);
 }
 
-void launch_plastic_mixed_to_f64(int B, const MixedBeams& mb, double* plastic64, cudaStream_t s) {
-    if (!B) return;
-    k_plastic_to_f64<<<grid_for(B), kBlock, 0, s>>>(B, mb.P0, mb.P1, plastic64);
+void launch_plastic_mixed_to_f64(const DevTopo& t, const uint8_t* mask, const MixedBeams& mb, double* plastic64,
+                                 cudaStream_t s) {
+    if (!t.B) return;
+    k_plastic_to_f64<<<t.n_bblk, kBlock, 0, s>>>(t, mask, mb.P0, mb.P1, plastic64);
     note_launches(1);
 }
 

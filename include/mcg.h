@@ -232,6 +232,35 @@ int64_t mcg_launch_count(const mcg_ctx* ctx);
 int mcg_set_contact_capacity(mcg_ctx* ctx, int64_t entries, int64_t candidates, int64_t contacts,
                              int64_t bins);
 
+/* ---- batched contexts (no reference counterpart) ------------------------------------
+ * One context can hold `count` lattices of uneven size (the reference solves one).  They
+ * share the configuration except the yield stress, and every evaluation, minimizer step and
+ * load/unload increment of all of them runs in the same kernel launches; each lattice's
+ * arithmetic is independent of the others, so a lattice solved in a batch gives exactly the
+ * results it gives in a context of its own.  The single-lattice functions (mcg_objective,
+ * mcg_minimize, mcg_commit, mcg_run, ...) refuse a context with more than one lattice. */
+
+/* Uploads `count` lattices: topos[k], geoms[k], rest state x0[k] / r0[k] (NULL arrays or
+ * entries: undefined state / identity orientations) and yield[k] (NULL: the configuration's
+ * yield stress).  Replaces any model the context held. */
+int mcg_upload_batch(mcg_ctx* ctx, int32_t count, const mcg_topology* topos, const mcg_geometry* geoms,
+                     const double* const* x0, const double* const* r0, const double* yield);
+
+/* Number of lattices in the context (0 before an upload). */
+int32_t mcg_instance_count(const mcg_ctx* ctx);
+
+/* One evaluation of every lattice: z holds the lattices' 6-DOF vectors one after another
+ * (the order of the upload), tops[k] the platen heights; energies[k], diags[k] and the
+ * gradient in the layout of z are written (each may be NULL). */
+int mcg_batch_objective(mcg_ctx* ctx, const double* z, const double* tops, double* energies, double* grad,
+                        mcg_diag* diags);
+
+/* Simulator::run (MC/src/sim.cpp:374-467) for every lattice at once: lattice k's frames go
+ * to frames[k * capacity ...], counts[k] frames, status[k] = MCG_OK or
+ * MCG_ERR_EQUILIBRIUM (the frames before the failure are kept).  MCG_ERR_CAPACITY when some
+ * lattice produced more than `capacity` frames (counts[] holds the needed sizes). */
+int mcg_batch_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* counts, int32_t* status);
+
 /* Reuse of the self-contact candidate list (no reference counterpart; results are
  * unchanged).  The list of shape pairs whose boxes may overlap is built with boxes grown
  * by `skin` metres and rebuilt only when some node has moved more than `skin` along an

@@ -1,0 +1,71 @@
+"""Batched contexts (mcg_upload_batch): lattices of different sizes and yield stresses in
+one context, evaluated and solved in the same launches, against each lattice in a context
+of its own.  An instance's arithmetic never mixes with another's (blocks never straddle two
+lattices, per-instance reductions run in the same order, contact sums are ordered by shape
+pair), so the results must agree bit for bit."""
+import numpy as np
+import pytest
+
+from falling_dice_gb300 import abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [((4, 4, 4), 40e6, 11), ((5, 3, 4), 55e6, 12), ((3, 5, 3), 30e6, 13), ((6, 4, 5), 65e6, 14)]
+
+
+def make(mcg, load_steps=0, unload_steps=0, max_strain=0.2, precision=abi.MCG_FP64):
+    cfg, _ = workloads.bcc((4, 4, 4), contact_stiffness=workloads.CONTACT_STIFF)
+    cfg.load_steps, cfg.unload_steps, cfg.max_strain = load_steps, unload_steps, max_strain
+    cfg.precision = precision
+    lats = []
+    for cells, _, seed in SPECS:
+        _, spec = workloads.bcc(cells, 0.3e-3, 0.5e-3, 0.03, abi.MCG_RADIUS_GRADED_Y)
+        spec.seed = seed
+        lats.append(mcg.generate_lattice(spec, cfg))
+    return cfg, lats, [y for _, y, _ in SPECS]
+
+
+def single_cfg(cfg, y):
+    c = abi.Config.from_buffer_copy(cfg)
+    c.material.yield_ = y
+    return c
+
+
+@pytest.mark.parametrize("precision", [abi.MCG_FP64, abi.MCG_MIXED])
+def test_batched_evaluation_is_bitwise_the_single_one(mcg, precision):
+    cfg, lats, ys = make(mcg, precision=precision)
+    states = [mcg.random_state(lat, 0.04, 0.08, 0.02, 1000 + k) for k, lat in enumerate(lats)]
+    tops = [lat.geometry.top0 - 0.002 for lat in lats]
+    batch = mcg.BatchSolver(cfg, lats, yields=ys)
+    batch.set_state(plastic=np.concatenate([pl for _, pl in states]))
+    got = batch.objective(np.concatenate([z for z, _ in states]), tops)
+    off = batch.node_offsets
+    for k, lat in enumerate(lats):
+        sol = mcg.Solver(single_cfg(cfg, ys[k]), lat)
+        sol.set_state(plastic=states[k][1])
+        ref = sol.objective(states[k][0], tops[k])
+        assert got["energy"][k] == ref["energy"], (k, got["energy"][k], ref["energy"])
+        assert np.array_equal(got["grad"][6 * off[k]:6 * off[k + 1]], ref["grad"]), k
+        assert got["diag"][k] == ref["diag"], k
+
+
+def test_batched_run_is_bitwise_the_single_runs(mcg):
+    cfg, lats, ys = make(mcg, load_steps=10, unload_steps=4, max_strain=0.25)
+    batch = mcg.BatchSolver(cfg, lats, yields=ys)
+    status, runs = batch.run()
+    for k, lat in enumerate(lats):
+        rc, ref = mcg.Solver(single_cfg(cfg, ys[k]), lat).run()
+        assert status[k] == rc
+        assert len(runs[k]) == len(ref) and len(ref) == 15
+        keys = sorted(ref[0].keys())
+        a = np.array([[f[q] for q in keys] for f in runs[k]])
+        b = np.array([[f[q] for q in keys] for f in ref])
+        assert np.array_equal(a, b), (k, np.argwhere(a != b)[:5])
+
+
+def test_single_lattice_functions_refuse_a_batch(mcg):
+    cfg, lats, ys = make(mcg)
+    batch = mcg.BatchSolver(cfg, lats[:2], yields=ys[:2])
+    assert batch.lib.mcg_instance_count(batch.h) == 2
+    with pytest.raises(mcg.MCGError):
+        mcg.Solver.objective(batch, np.zeros(6 * batch.n_nodes), 0.0)
