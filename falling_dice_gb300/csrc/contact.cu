@@ -218,14 +218,14 @@ __device__ __noinline__ PairHit narrow_phase(const DevTopo& t, const PhysParams&
 // each current box lies inside the inflated box of the build.  flags[1] = rebuild now.
 // A node's displacement is bounded from its FP32 interval [lo, hi] and the stored lower end
 // of its interval at the build (one FP32 ulp wide at most), rounding upward.
-__global__ void __launch_bounds__(kBlock) k_skin_check(int N, const float4* __restrict__ xf_lo,
+__global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const float4* __restrict__ xf_lo,
                                                        const float4* __restrict__ xf_hi,
                                                        const float4* __restrict__ xref, float skin,
                                                        uint32_t* __restrict__ flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     bool moved = false;
     if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
-    if (i < N && !moved) {
+    if (i < N && !moved && t.active[t.node_inst[i]]) {
         const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
         const float d = fmaxf(fmaxf(fmaxf(__fsub_ru(h.x, r.x), __fsub_ru(r.x, l.x)),
                                     fmaxf(__fsub_ru(h.y, r.y), __fsub_ru(r.y, l.y))),
@@ -276,7 +276,7 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
         while ((1LL << bits) < dim[d]) bits++;
     long long nb;
     int mode;
-    if (bits <= 10 && (1LL << (3 * bits)) <= bin_cap) {
+    if (bits <= 10 && (1LL << (3 * bits)) <= bin_cap && (1LL << (3 * bits)) <= 4 * dim[0] * dim[1] * dim[2]) {
         mode = 0;
         nb = 1LL << (3 * bits);
     } else {
@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
                          __fadd_ru(fmaxf(ah.z, bh.z), pad)};
     const bool finite_box = isfinite(lo[0]) && isfinite(lo[1]) && isfinite(lo[2]) && isfinite(hi[0]) &&
                             isfinite(hi[1]) && isfinite(hi[2]);
-    if (!grid[7] || !finite_box) {
+    if (!grid[7] || !finite_box || !t.active[t.node_inst[nd.x]]) {  // inactive instances take no part
         count[s] = 0;
         cell_lo[s] = make_int4(0, 0, 0, 0);
         cell_hi[s] = make_int4(-1, -1, -1, 0);
@@ -667,8 +667,8 @@ __device__ __forceinline__ uint2 candidate_at(const uint2* __restrict__ cand, co
 // Narrow phase over the candidate list, flattened so that each thread takes one candidate
 // whatever region it sits in (a warp's region can hold far more candidates than another's).
 // Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
-// 32 (chunks past the list are zeroed for the scan).  Pass 1 (after a scan of the chunk
-// counts): test the hits again and write them as contacts, in candidate order.
+// 32.  Pass 1 (after a scan of the chunk counts of the list's length): test the hits again
+// and write them as contacts, in candidate order.
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
                                                    const float4* __restrict__ xf, int region, int W,
@@ -681,8 +681,7 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
     const uint32_t total = woff[W];
     const long long nchunk = (total + 31) / 32;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-    for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < (pass == 0 ? chunks : nchunk);
-         ch += warps) {
+    for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
         const uint32_t g = uint32_t(ch * 32 + lane);
         if constexpr (pass == 1) {
             const unsigned m = hitbits[ch];
@@ -703,9 +702,10 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
             }
         } else {
             bool hit = false;
-            if (ch < nchunk && g < total) {
+            if (g < total) {
                 const uint2 q = candidate_at(cand, woff, W, region, g);
-                hit = !certainly_apart(t, p, xf, q.x, q.y) &&
+                const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
+                hit = t.node_inst[na.x] == t.node_inst[nb.x] && !certainly_apart(t, p, xf, q.x, q.y) &&
                       narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -813,7 +813,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     const int S = t.N + t.B;
     const uint32_t* gate = c.flags + 1;
     cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
-    (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
+    (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t, t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
     // candidate list (only when rebuilding)
     (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
     (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
@@ -842,7 +842,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     const long long chunks = (long long)W * c.region / 32;
     (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
                                                 c.hcount, c.hoff, c), note_launches(1));
-    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s);
+    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, c.woff + W, 31, 5);
     (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
                                                 c.hcount, c.hoff, c), note_launches(1));
     const uint32_t* total = c.hoff + chunks;

@@ -219,7 +219,21 @@ struct mcg_ctx {
            *d_pstats = nullptr;
     SolveCtl* d_ctl = nullptr;
     uint8_t* d_mask = nullptr;
+    uint8_t *d_active = nullptr, *d_all = nullptr;  // instances evaluated / all instances
+    std::vector<uint8_t> active;                    // host copy of d_active
+    // Evaluates only the instances with a[i] != 0 from now on.  An instance that joins
+    // needs its shapes in the contact candidate list: the next evaluation rebuilds it.
+    void set_active(const std::vector<uint8_t>& a) {
+        if (a == active) return;
+        bool joined = false;
+        for (int i = 0; i < I; i++) joined |= a[size_t(i)] && !active[size_t(i)];
+        active = a;
+        h2d(d_active, active.data(), size_t(I), stream);
+        if (joined) ck(cudaMemsetAsync(cb.flags + 2, 1, 1, stream), "memset");
+        sync();  // the host vector may change before the copy runs
+    }
     std::vector<Minimizer> mins;
+    std::vector<uint8_t> fused;  // the instance's direction is computed by one CTA
     bool have_final = false;  // instance 0 has a final state from minimize, not yet committed
 
     // optional per-phase timing of evaluations (events on the context stream)
@@ -391,7 +405,7 @@ struct mcg_ctx {
             read_outs();
         }
         if (hp.outs[0].overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
-        if (cfg.self_contact) last_contacts = read_contact_count();
+        if (cfg.self_contact) last_contacts = hp.u32[0];
         return hp.outs;
     }
     long long read_contact_count() {
@@ -401,13 +415,14 @@ struct mcg_ctx {
     }
     void read_outs() {
         d2h(hp.outs, ev.out, size_t(I), stream);
+        if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
         sync();
     }
     // Totals of the last evaluation, repeating it if it overflowed a contact buffer.
     EvalOut read_out() {
         read_outs();
         if (hp.outs[0].overflow) eval_read(last_z, last_trials, last_grad);
-        else if (cfg.self_contact) last_contacts = read_contact_count();
+        else if (cfg.self_contact) last_contacts = hp.u32[0];
         return hp.outs[0];
     }
 
@@ -463,12 +478,17 @@ struct mcg_ctx {
         bool any_dir = false, any_sd = false;
         clear_ctl();
         int max_m = 0;
+        max_m = -1;
         for (int i = 0; i < I; i++) {
             const M& s = mins[size_t(i)];
             if (s.phase == M::kDirection) {
-                hp.ctl[i].flags = kOpDirection;
+                if (fused[size_t(i)]) {
+                    hp.ctl[i].flags = kOpDirFused;
+                } else {
+                    hp.ctl[i].flags = kOpDirection;
+                    max_m = std::max(max_m, s.m);
+                }
                 any_dir = true;
-                max_m = std::max(max_m, s.m);
             }
             any_sd |= s.phase == M::kSteepest;
         }
@@ -539,6 +559,14 @@ struct mcg_ctx {
             if (s.phase == M::kStart || s.phase == M::kTrial || s.phase == M::kFinish) hp.tops[i] = s.top;
         }
         if (!any) return false;
+        {
+            std::vector<uint8_t> a(size_t(I), 0);
+            for (int i = 0; i < I; i++) {
+                const M::Phase ph = mins[size_t(i)].phase;
+                a[size_t(i)] = ph == M::kStart || ph == M::kTrial || ph == M::kFinish;
+            }
+            set_active(a);
+        }
         upload_ctl();
         upload_tops();
         bl_prepare(topo, d_ctl, d_z, d_best, d_zeval, d_p, d_zfinal, stream);
@@ -650,7 +678,9 @@ struct mcg_ctx {
     void commit(const std::vector<uint8_t>& m) {
         h2d(d_mask, m.data(), size_t(I), stream);
         PhysParams p = phys;
-        launch_state(topo, p, d_zfinal, d_baseX, d_baseR, ev, stream);
+        DevTopo all = topo;  // the committed instances' states (others are recomputed before use)
+        all.active = d_all;
+        launch_state(all, p, d_zfinal, d_baseX, d_baseR, ev, stream);
         if (mixed) {
             launch_commit(topo, d_mask, ev, d_baseX, d_baseR, nullptr, stream);
             launch_plastic_mixed(topo, d_mask, nullptr, ev.trial_nextf, mb, stream);
@@ -1010,21 +1040,49 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
             bblk.push_back(make_int4(h.beam0 + f, std::min(kMapBlock, h.B - f), k, 0));
         irange[size_t(k)].w = int(bblk.size());
     }
-    // contact-grid offsets: instances side by side in x and z, far enough apart that no
-    // cell holds shapes of two instances (a lattice may widen under compression)
+    // contact-grid offsets: the instances' footprints (x-z extent with room to widen under
+    // compression) packed in rows, so that the shared grid stays small; offsets are
+    // multiples of 2^-10 m, exact in FP32.  (Pairs of two instances are never contacts in
+    // any case: the narrow phase rejects them.)
     {
-        double span = 0;
+        struct Fp {
+            int k;
+            double lo_x, lo_z, w, d;
+        };
+        std::vector<Fp> fp;
         for (int k = 0; k < I; k++) {
             const InstIn& in = ins[size_t(k)];
-            if (!in.x0) continue;
-            for (int i = 0; i < in.t->n_nodes; i++)
-                span = std::max({span, std::abs(in.x0[3 * size_t(i)]), std::abs(in.x0[3 * size_t(i) + 2])});
+            double lx = 0, hx = 0, lz = 0, hz = 0;
+            if (in.x0 && in.t->n_nodes > 0) {
+                lx = hx = in.x0[0];
+                lz = hz = in.x0[2];
+                for (int i = 0; i < in.t->n_nodes; i++) {
+                    lx = std::min(lx, in.x0[3 * size_t(i)]);
+                    hx = std::max(hx, in.x0[3 * size_t(i)]);
+                    lz = std::min(lz, in.x0[3 * size_t(i) + 2]);
+                    hz = std::max(hz, in.x0[3 * size_t(i) + 2]);
+                }
+            }
+            const double mw = 0.3 * (hx - lx) + 4 * rmax + 0.005, md = 0.3 * (hz - lz) + 4 * rmax + 0.005;
+            fp.push_back(Fp{k, lx - mw, lz - md, (hx - lx) + 2 * mw, (hz - lz) + 2 * md});
         }
-        const double pitch = std::ceil((4 * span + 8 * rmax + 0.01) * 1024.0) / 1024.0;  // exact in FP32
-        const int cols = int(std::ceil(std::sqrt(double(I))));
-        for (int k = 0; k < I; k++)
-            ih[size_t(k)].off = I == 1 ? float2{0.f, 0.f}
-                                       : float2{float(pitch * (k % cols)), float(pitch * (k / cols))};
+        double area = 0;
+        for (const Fp& f : fp) area += f.w * f.d;
+        const double row_max = std::sqrt(area) * 1.2;
+        std::vector<Fp> order = fp;
+        std::sort(order.begin(), order.end(), [](const Fp& a, const Fp& b) { return a.d > b.d || (a.d == b.d && a.k < b.k); });
+        double x = 0, z = 0, row_d = 0;
+        auto q = [](double v) { return std::ceil(v * 1024.0) / 1024.0; };
+        for (const Fp& f : order) {
+            if (x > 0 && x + f.w > row_max) {
+                z = q(z + row_d);
+                x = 0;
+                row_d = 0;
+            }
+            ih[size_t(f.k)].off = I == 1 ? float2{0.f, 0.f} : float2{float(q(x - f.lo_x)), float(q(z - f.lo_z))};
+            x = q(x + f.w + 1e-3);
+            row_d = std::max(row_d, f.d + 1e-3);
+        }
     }
 
     c->sync();
@@ -1115,6 +1173,19 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         float2* doff = M.get<float2>(off.size());
         h2d(doff, off.data(), off.size(), s);
         T.off = doff;
+        std::vector<int> ni(static_cast<size_t>(N));
+        for (int k = 0; k < I; k++)
+            std::fill(ni.begin() + ih[size_t(k)].node0, ni.begin() + ih[size_t(k)].node0 + ih[size_t(k)].N, k);
+        int* dni = M.get<int>(ni.size());
+        h2d(dni, ni.data(), ni.size(), s);
+        T.node_inst = dni;
+        std::vector<uint8_t> ones(static_cast<size_t>(I), 1);
+        c->d_active = M.get<uint8_t>(size_t(I));
+        c->d_all = M.get<uint8_t>(size_t(I));
+        h2d(c->d_active, ones.data(), ones.size(), s);
+        h2d(c->d_all, ones.data(), ones.size(), s);
+        T.active = c->d_active;
+        c->active = ones;
         c->sync();  // the host vectors above go out of scope
     }
     c->topo = T;
@@ -1221,8 +1292,10 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
             }
         int bits = 3;
         while ((1LL << bits) < dmax && bits < 10) bits++;
+        const long long dense = dims[0] * dims[1] * dims[2];
         long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
-        if ((1LL << bits) < dmax) bin_cap = std::min(dims[0] * dims[1] * dims[2], 1LL << 28);
+        // row-major bins when the Morton range does not fit or is mostly empty
+        if ((1LL << bits) < dmax || bin_cap > 4 * dense) bin_cap = std::min(dense, 1LL << 28);
         c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap, 1024);
     }
     // solver vectors
@@ -1243,6 +1316,11 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->d_ctl = Q.get<SolveCtl>(size_t(I));
     c->d_mask = Q.get<uint8_t>(size_t(I));
     c->mins.assign(size_t(I), Minimizer{});
+    c->fused.assign(size_t(I), 0);
+    for (int k = 0; k < I; k++) {
+        const int4 r = irange[size_t(k)];
+        c->fused[size_t(k)] = r.y - r.x <= fused_direction_limit() && c->H <= 64;
+    }
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
         launch_mixed_constants(c->topo, c->mb, s);
@@ -1412,6 +1490,7 @@ int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* e
         h2d(c->d_zin, z, n, s);
         c->hp.tops[0] = top;
         c->upload_tops();
+        c->set_active(std::vector<uint8_t>(1, 1));
         const EvalOut o = c->eval_read(c->d_zin, trials != 0, c->d_grad)[0];
         if (trials) c->have_final = false;
         if (grad) d2h(grad, c->d_grad, n, s);
@@ -1452,6 +1531,7 @@ int mcg_batch_objective(mcg_ctx* c, const double* z, const double* tops, double*
         h2d(c->d_zin, z, n, c->stream);
         for (int i = 0; i < c->I; i++) c->hp.tops[i] = tops[i];
         c->upload_tops();
+        c->set_active(std::vector<uint8_t>(size_t(c->I), 1));
         const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);
         for (int i = 0; i < c->I; i++) {
             if (energies) energies[i] = o[i].energy;
@@ -1474,6 +1554,7 @@ int mcg_upload_z(mcg_ctx* c, const double* z) {
 int mcg_objective_resident(mcg_ctx* c, double top, int trials) {
     return guarded(c, [&] {
         need_single(c);
+        c->set_active(std::vector<uint8_t>(1, 1));
         if (c->hp.tops[0] != top) {
             c->sync();
             c->hp.tops[0] = top;
@@ -1512,6 +1593,7 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         h2d(c->d_zin, z, n, s);
         c->hp.tops[0] = top;
         c->upload_tops();
+        c->set_active(std::vector<uint8_t>(1, 1));
         PhysParams p = c->phys;
         p.broad_cell = c->broad_cell;
         p.inv_cell_f = float(1.0 / c->broad_cell);

@@ -57,6 +57,8 @@ struct DevTopo {
     const int* inst_n;        // [I] nodes of the instance
     const long long* inst_free;  // [I] unlocked DOFs of the instance
     const float2* off;        // [I] (x, z) offset of the instance in the contact grid
+    const int* node_inst;     // [N] instance of each node
+    const uint8_t* active;    // [I] 0: the instance is not evaluated (its outputs keep old values)
 };
 
 // Elements per mapped block (the launch block size of the mapped kernels).
@@ -262,9 +264,11 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
 size_t scan_tmp_bytes(long long n);
 // Exclusive scan of n uint32 values; out[n] receives the total.
 // Exclusive scan of n counts into out[0..n] (out[n] = total).  With a gate, every kernel
-// returns at once when *gate is 0 (the output keeps its previous contents).
+// returns at once when *gate is 0 (the output keeps its previous contents).  With dn, only
+// the first min(n, (*dn + add) >> shift) counts are scanned (a count known on the device;
+// the total also goes to out[n]).
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s,
-                        const uint32_t* gate = nullptr);
+                        const uint32_t* gate = nullptr, const uint32_t* dn = nullptr, int add = 0, int shift = 0);
 
 // ---- L-BFGS vector kernels (lbfgs.cu), all instances of a context per launch --------------
 // Operations an instance takes part in during one solver step (SolveCtl::flags).
@@ -280,7 +284,8 @@ enum SolveOp : int {
     kOpTakeGrad = 256,     // g = geval
     kOpAccept = 512,       // s, y, curvature dots, z = zeval, g = geval
     kOpPair = 1024,        // with kOpAccept: store (s, y) in history slot `target`
-    kOpKeepBestAfter = 2048  // with kOpAccept: best = the accepted z
+    kOpKeepBestAfter = 2048, // with kOpAccept: best = the accepted z
+    kOpDirFused = 4096       // as kOpDirection, by one CTA for the instance (small instances)
 };
 // Per-instance solver control, written by the host before each step.
 struct SolveCtl {
@@ -290,9 +295,11 @@ struct SolveCtl {
     int target;        // slot the next accepted pair goes to
 };
 size_t lbfgs_part_doubles(int n_nblk);
-// Two-loop recursion (sim.cpp:184-187) into p for the kOpDirection instances, then
-// p = clamp(lock(-p)) and dg[i] = <g, p>.  History: H slots of `stride` doubles; rho and
-// alpha [I * H].
+// Largest instance (in node blocks) whose direction one CTA computes (kOpDirFused).
+int fused_direction_limit();
+// Two-loop recursion (sim.cpp:184-187) into p for the kOpDirection and kOpDirFused
+// instances, then p = clamp(lock(-p)) and dg[i] = <g, p>.  History: H slots of `stride`
+// doubles; rho and alpha [I * H].  max_m < 0: no kOpDirection instance (one launch).
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
                   double* dg, double mt, double mr, cudaStream_t s);

@@ -301,14 +301,189 @@ __global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __
     }
 }
 
+// ---- the whole direction in one CTA per instance ---------------------------------------------
+// For instances of at most kFuseChunks node blocks: the same steps as k_tl_start ...
+// k_finish + k_inst_final (each block partial here is one chunk of kBlock nodes reduced by the
+// same tree, each instance sum the same strided tree), so the result is bit for bit that of
+// the multi-launch path; one launch instead of 4 m + 4.
+constexpr int kFuseChunks = 64;
+
+// Partial of one chunk: thread t the node first + t (if valid), then the block tree.
+__device__ __forceinline__ double chunk_dot(const double* a, const double* b, int first, int count, double* sm) {
+    double acc[1] = {0};
+    if (int(threadIdx.x) < count) acc[0] = dot6(a + 6 * size_t(first + threadIdx.x), b + 6 * size_t(first + threadIdx.x));
+    block_sum<1>(acc, sm);
+    return acc[0];
+}
+
+// Sum of nchunk partials held in shared memory, strided as instance_sum.
+template <int K>
+__device__ __forceinline__ void chunk_sum(const double (*part)[kFuseChunks], int nchunk, double (&acc)[K], double* sm) {
+#pragma unroll
+    for (int k = 0; k < K; k++) acc[k] = 0;
+    for (int b = int(threadIdx.x); b < nchunk; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] += part[k][b];
+    block_sum<K>(acc, sm);
+}
+
+__global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const SolveCtl* __restrict__ ctl, int H,
+                                                            double* __restrict__ p, const double* __restrict__ g,
+                                                            const double* __restrict__ S, const double* __restrict__ Y,
+                                                            long long stride, const double* __restrict__ rho,
+                                                            double* __restrict__ dg, double mt, double mr) {
+    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ double part[2][kFuseChunks];
+    __shared__ double alpha[64];
+    __shared__ double coef;
+    const int inst = blockIdx.x;
+    const SolveCtl c = ctl[inst];
+    if (!(c.flags & kOpDirFused)) return;
+    const int4 r = t.irange[inst];
+    const int nchunk = r.y - r.x;
+    // p = g; partials of <s, y>, <y, y> of the newest pair
+    for (int b = 0; b < nchunk; b++) {
+        const int4 q = t.nblk[r.x + b];
+        if (int(threadIdx.x) < q.y)
+#pragma unroll
+            for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] = g[6 * size_t(q.x + threadIdx.x) + d];
+        if (c.m > 0) {
+            const int slot = ring_slot(c, H, c.m - 1);
+            double acc[2] = {0, 0};
+            if (int(threadIdx.x) < q.y) {
+                const double* sv = hist(S, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                const double* yv = hist(Y, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                acc[0] = dot6(sv, yv);
+                acc[1] = dot6(yv, yv);
+            }
+            block_sum<2>(acc, sm);
+            if (threadIdx.x == 0) {
+                part[0][b] = acc[0];
+                part[1][b] = acc[1];
+            }
+        }
+    }
+    __syncthreads();
+    double h0acc[2] = {0, 0};
+    if (c.m > 0) chunk_sum<2>(part, nchunk, h0acc, sm);
+    __syncthreads();
+    // loop 1, newest first
+    for (int j = 0; j < c.m; j++) {
+        const int h = c.m - 1 - j, slot = ring_slot(c, H, h);
+        for (int b = 0; b < nchunk; b++) {
+            const int4 q = t.nblk[r.x + b];
+            const double v = chunk_dot(hist(S, stride, slot), p, q.x, q.y, sm);
+            if (threadIdx.x == 0) part[0][b] = v;
+        }
+        __syncthreads();
+        double acc[1];
+        chunk_sum<1>(part, nchunk, acc, sm);
+        if (threadIdx.x == 0) {
+            coef = rho[size_t(inst) * H + slot] * acc[0];
+            alpha[h] = coef;
+        }
+        __syncthreads();
+        const double k = coef;
+        const double* yv = hist(Y, stride, slot);
+        for (int b = 0; b < nchunk; b++) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] -= k * yv[6 * size_t(q.x + threadIdx.x) + d];
+        }
+        __syncthreads();
+    }
+    // H0 (sim.cpp:186); the block sums are complete in thread 0 only
+    if (threadIdx.x == 0) {
+        double v = .10;
+        if (c.m > 0 && h0acc[0] > 1e-20 && h0acc[1] > 1e-20) v = clampd(h0acc[0] / h0acc[1], 1e-7, 1e4);
+        coef = v;
+    }
+    __syncthreads();
+    {
+        const double v = coef;
+        for (int b = 0; b < nchunk; b++) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] *= v;
+        }
+        __syncthreads();
+    }
+    // loop 2, oldest first
+    for (int j = 0; j < c.m; j++) {
+        const int slot = ring_slot(c, H, j);
+        for (int b = 0; b < nchunk; b++) {
+            const int4 q = t.nblk[r.x + b];
+            const double v = chunk_dot(hist(Y, stride, slot), p, q.x, q.y, sm);
+            if (threadIdx.x == 0) part[0][b] = v;
+        }
+        __syncthreads();
+        double acc[1];
+        chunk_sum<1>(part, nchunk, acc, sm);
+        if (threadIdx.x == 0) coef = alpha[j] - rho[size_t(inst) * H + slot] * acc[0];
+        __syncthreads();
+        const double k = coef;
+        const double* sv = hist(S, stride, slot);
+        for (int b = 0; b < nchunk; b++) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] += sv[6 * size_t(q.x + threadIdx.x) + d] * k;
+        }
+        __syncthreads();
+    }
+    // finish: clamp (sim.cpp:188-190, 46) and <g, p>
+    for (int b = 0; b < nchunk; b++) {
+        const int4 q = t.nblk[r.x + b];
+        double acc[1] = {0};
+        if (int(threadIdx.x) < q.y) {
+            const size_t o = 6 * size_t(q.x + threadIdx.x);
+            const uint8_t* lk = t.locked + o;
+            double v[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                v[k] = -p[o + k];
+                if (lk[k]) v[k] = 0;
+            }
+            const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (lt > mt) {
+                const double f = mt / lt;
+                v[0] *= f; v[1] *= f; v[2] *= f;
+            }
+            const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+            if (lr > mr) {
+                const double f = mr / lr;
+                v[3] *= f; v[4] *= f; v[5] *= f;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                v[k] = lk[k] ? 0.0 : v[k];
+                p[o + k] = v[k];
+            }
+            acc[0] = dot6(g + o, v);
+        }
+        block_sum<1>(acc, sm);
+        if (threadIdx.x == 0) part[0][b] = acc[0];
+    }
+    __syncthreads();
+    double acc[1];
+    chunk_sum<1>(part, nchunk, acc, sm);
+    if (threadIdx.x == 0) dg[inst] = acc[0];
+}
+
 }  // namespace
 
 size_t lbfgs_part_doubles(int n_nblk) { return 3 * size_t(n_nblk) + 8; }
+
+int fused_direction_limit() { return kFuseChunks; }
 
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
                   double* dg, double mt, double mr, cudaStream_t s) {
     const int nb = t.n_nblk;
+    (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
+    if (max_m < 0) return;  // no instance on the multi-launch path
     (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, H, p, g, S, Y, stride, part + 2 * size_t(nb)), note_launches(1));
     for (int j = 0; j < max_m; j++) {
         (k_tl_dot<1><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, part), note_launches(1));

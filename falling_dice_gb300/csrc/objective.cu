@@ -28,6 +28,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const MapPos mp = map_pos(t.nblk);
+    if (!t.active[mp.inst]) return;  // block-uniform
     const int i = mp.i;
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
@@ -188,6 +189,7 @@ __global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const d
                                                   int trials, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.bblk);
+    if (!t.active[mp.inst]) return;
     const int b = mp.i;
     const int B = t.B;
     double acc[3] = {0, 0, 0};  // energy, elastic, plastic
@@ -366,6 +368,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
     __shared__ double sm[6 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const MapPos mp = map_pos(t.nblk);
+    if (!t.active[mp.inst]) return;
     const int i = mp.i;
     const int N = t.N;
     double acc[6] = {0, 0, 0, 0, 0, 0};  // gravity E, platen E, reaction, contacts, self-contact E, |g|^2
@@ -444,6 +447,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, co
     __shared__ double sm[6 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const int inst = blockIdx.x;
+    if (!t.active[inst]) return;
     const int4 r = t.irange[inst];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
     double cacc[3] = {0, 0, 0};          // self-contact E, contacts (platen and self), |g|^2
@@ -502,7 +506,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, co
 __global__ void __launch_bounds__(kBlock) k_zero_if_nonfinite(DevTopo t, const EvalOut* __restrict__ out,
                                                               double* __restrict__ grad) {
     const MapPos mp = map_pos(t.nblk);
-    if (!mp.valid || !out[mp.inst].nonfinite) return;
+    if (!mp.valid || !t.active[mp.inst] || !out[mp.inst].nonfinite) return;
 #pragma unroll
     for (int k = 0; k < 6; k++) grad[6 * size_t(mp.i) + k] = 0;
 }

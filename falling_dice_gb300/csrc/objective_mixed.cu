@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
     __shared__ double sm[3 * (kBlock / 32)];
     __shared__ double smx[kBlock / 32];
     const MapPos mp = map_pos(t.nblk);
+    if (!t.active[mp.inst]) return;
     const int i = mp.i;
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
@@ -275,6 +276,7 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.bblk);
+    if (!t.active[mp.inst]) return;
     const int b = mp.i;
     const int B = t.B;
     float acc[3] = {0.f, 0.f, 0.f};

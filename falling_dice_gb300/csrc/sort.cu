@@ -36,9 +36,19 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
     return warp_base + x - v;
 }
 
-__global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t* __restrict__ in, long long n,
-                                                        uint32_t* __restrict__ part, const uint32_t* __restrict__ gate) {
+// Element count: n, or min(n, (*dn + add) >> shift) when the count is on the device.
+__device__ __forceinline__ long long scan_len(long long n, const uint32_t* dn, int add, int shift) {
+    if (!dn) return n;
+    const long long m = ((long long)*dn + add) >> shift;
+    return m < n ? m : n;
+}
+
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t* __restrict__ in, long long cap,
+                                                        uint32_t* __restrict__ part, const uint32_t* __restrict__ gate,
+                                                        const uint32_t* __restrict__ dn, int add, int shift) {
     if (gate && !*gate) return;
+    const long long n = scan_len(cap, dn, add, shift);
+    if ((long long)blockIdx.x * kTile >= n && blockIdx.x > 0) return;
     __shared__ uint32_t sm[kBlock / 32];
     const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t s = 0;
@@ -51,9 +61,12 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t* __restri
 }
 
 // One block scans the tile partials in chunks, carrying the running total.
-__global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long long np, uint32_t* total_out,
-                                                          const uint32_t* __restrict__ gate) {
+__global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long long np_cap, uint32_t* total_out,
+                                                          const uint32_t* __restrict__ gate,
+                                                          const uint32_t* __restrict__ dn, int add, int shift) {
     if (gate && !*gate) return;
+    const long long n = scan_len(np_cap * kTile, dn, add, shift);
+    const long long np = dn ? (n + kTile - 1) / kTile : np_cap;
     __shared__ uint32_t sm[kBlock / 32];
     uint32_t carry = 0;
     for (long long c = 0; c < np; c += kTile) {
@@ -75,10 +88,14 @@ __global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long l
 }
 
 __global__ void __launch_bounds__(kBlock) k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
-                                                      long long n, const uint32_t* __restrict__ part,
+                                                      long long cap, const uint32_t* __restrict__ part,
                                                       const uint32_t* __restrict__ total,
-                                                      const uint32_t* __restrict__ gate) {
+                                                      const uint32_t* __restrict__ gate,
+                                                      const uint32_t* __restrict__ dn, int add, int shift) {
     if (gate && !*gate) return;
+    const long long n = scan_len(cap, dn, add, shift);
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[cap] = *total;  // the total at a fixed place
+    if ((long long)blockIdx.x * kTile >= n) return;
     __shared__ uint32_t sm[kBlock / 32];
     const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t v[kItems], s = 0;
@@ -91,7 +108,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_down(const uint32_t* __restrict
 #pragma unroll
     for (int k = 0; k < kItems; k++)
         if (base + k < n) { out[base + k] = run; run += v[k]; }
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = *total;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n < cap) out[n] = *total;
 }
 
 }  // namespace
@@ -102,7 +119,7 @@ size_t scan_tmp_bytes(long long n) {
 }
 
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tmp, cudaStream_t s,
-                        const uint32_t* gate) {
+                        const uint32_t* gate, const uint32_t* dn, int add, int shift) {
     uint32_t* part = static_cast<uint32_t*>(tmp);
     const long long np = (n + kTile - 1) / kTile;
     uint32_t* total = part + np + 1;
@@ -110,9 +127,9 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tm
         if (!gate) cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
         return;
     }
-    (k_scan_reduce<<<unsigned(np), kBlock, 0, s>>>(in, n, part, gate), note_launches(1));
-    (k_scan_partials<<<1, kBlock, 0, s>>>(part, np, total, gate), note_launches(1));
-    (k_scan_down<<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate), note_launches(1));
+    (k_scan_reduce<<<unsigned(np), kBlock, 0, s>>>(in, n, part, gate, dn, add, shift), note_launches(1));
+    (k_scan_partials<<<1, kBlock, 0, s>>>(part, np, total, gate, dn, add, shift), note_launches(1));
+    (k_scan_down<<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate, dn, add, shift), note_launches(1));
 }
 
 }  // namespace mcg

@@ -14,6 +14,8 @@ reference publishes no dataset for this path.
                   400 loading + 400 unloading increments, penalty stiffness scaled to E.
   bcc128          128x128x64 cubic+BCC, radii uniform 0.3-0.6 mm, +/-2 % jitter, 50 % strain in
                   100 increments, penalty stiffness scaled to E.
+  sweep           256 cubic+BCC lattices of 4-16 cells per side with per-lattice radius
+                  grading and yield stress, 30 % strain in 100 increments (batched).
 """
 from . import abi
 
@@ -69,3 +71,25 @@ def bcc128():
 
 # deformed state of the single-evaluation workload
 DEFORM = dict(sigma_t=0.05, sigma_r=0.1, epsp_max=0.02, seed=SEED ^ 0xD3F0)
+
+
+def sweep(count=256, seed=SEED ^ 0x5357):
+    """The batched sweep: `count` cubic+BCC lattices with cells per side U{4..16} (cubic
+    blocks), radius graded in height from 0.3 mm with a slope U[0, 0.1] mm per cell and
+    capped at 0.7 mm (the largest radius of the other specimens; uncapped, a 16-cell lattice
+    would reach 1.9 mm struts in 5 mm cells, overlapping at rest), yield stress U[30, 70] MPa,
+    +/-2 % jitter, 30 % strain in 100 loading increments.  Returns (cfg, specs, yields); the
+    configuration is shared, the yield is per lattice."""
+    import numpy as np
+    rng = np.random.default_rng(seed & 0xFFFFFFFFFFFFFFFF)
+    cfg = _cfg(0.3e-3, 0.6e-3, max_strain=0.3, load_steps=100, unload_steps=0, contact_stiffness=CONTACT_STIFF)
+    specs, yields = [], []
+    for k in range(count):
+        n = int(rng.integers(4, 17))
+        slope = float(rng.uniform(0.0, 0.1e-3))
+        r0 = 0.3e-3
+        s = _spec(abi.MCG_LATTICE_CUBIC_BCC, abi.MCG_RADIUS_GRADED_Y, (n, n, n), r0, min(r0 + slope * n, 0.7e-3), 0.02,
+                  seed=(SEED + 7919 * (k + 1)) & 0xFFFFFFFFFFFFFFFF)
+        specs.append(s)
+        yields.append(float(rng.uniform(30e6, 70e6)))
+    return cfg, specs, yields
