@@ -45,6 +45,10 @@ NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6
 BEAM_TRAFFIC_PER_BEAM = 40.348160e6 / 184400
 BEAM_BYTES_MIXED = 68    # per beam, mixed: a, b (2 x 4 B) + 15 reals as FP32
 NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 + locked[6]
+# Pair enumeration (k_bin_pairs), algorithmic bytes: every cell entry's shape id (4 B), each
+# shape's pair-test record once (16 B box/cell record + 8 B nodes), each occupied bin's
+# count, start and list slot (12 B), each candidate written (8 B).
+PAIR_ENTRY_BYTES, PAIR_SHAPE_BYTES, PAIR_BIN_BYTES, PAIR_CAND_BYTES = 4, 24, 12, 8
 
 
 def parse():
@@ -55,6 +59,8 @@ def parse():
     ap.add_argument("--impl", default="mcg", choices=["mcg", "reference"])
     ap.add_argument("--workload", default="bcc64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the load/unload (32x32x16) and batched-sweep (256 lattices) measurements")
     return ap.parse_args()
 
 
@@ -268,10 +274,12 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
         sol.objective_resident(top)
     phases, nev = sol.phase_times()
     sol.set_timing(False)
+    stats = sol.contact_stats()
     sol.close()
     return {"ms_step": ms / steps, "value": world * 1e3 * steps / ms, "e2e": world * 1e3 * steps / ms_e2e,
             "launches": launches, "clocks": clk, "energy": res["energy"], "grad": res0["grad"],
-            "contacts": res["diag"]["contacts"], "phases": {k: v / nev for k, v in phases.items()}}
+            "contacts": res["diag"]["contacts"], "phases": {k: v / nev for k, v in phases.items()},
+            "contact_stats": stats}
 
 
 def main():
@@ -313,6 +321,17 @@ def main():
         return {"bound": "hbm", "kernel": "k_beams_mixed" if r is mixed else "k_beams", "achieved": ach,
                 "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
                 "traffic": traffic, "bytes_per_launch": nbytes, "ms_per_launch": ms}
+
+    def roofline_pairs(r):
+        st = r["contact_stats"]
+        nbytes = (PAIR_ENTRY_BYTES * st["entries"] + PAIR_SHAPE_BYTES * (N + B) +
+                  PAIR_BIN_BYTES * st["occupied_bins"] + PAIR_CAND_BYTES * st["candidates"])
+        ms = r["phases"]["pairs"]
+        ach = nbytes / (ms * 1e-3) / 1e9
+        return {"bound": "hbm", "kernel": "k_bin_pairs", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_source": peak_kind, "traffic": None, "bytes_per_launch": nbytes,
+                "ms_per_launch": ms, "share_of_evaluation": ms / r["ms_step"],
+                "counts": st, "note": "issue-bound integer work (pair tests); the fraction is of HBM"}
     cpu = None
     if not a.no_cpu_baseline:
         t_s, B_s, N_s = cpu_sample_eval_seconds(a.workload, repeat=2)
@@ -338,7 +357,8 @@ def main():
         "error_vs_fp64": {"energy_rel": err_e, "grad_rel_2norm": err_g},
         "hbm_gbs_algorithmic": eval_bytes_mixed * mixed["value"] / world / 1e9,
         "phase_ms": mixed["phases"],
-        "roofline": roofline(mixed, beam_bytes_mixed, None),
+        "roofline": roofline_pairs(mixed),
+        "roofline_beams": roofline(mixed, beam_bytes_mixed, None),
         "fp64": {"value": plain["value"], "ms_per_step": plain["ms_step"], "e2e": plain["e2e"],
                  "phase_ms": plain["phases"], "gpu_launches": int(plain["launches"]),
                  "hbm_gbs_algorithmic": (BEAM_BYTES * B + NODE_BYTES * N) * plain["value"] / world / 1e9,
@@ -350,7 +370,70 @@ def main():
         "clocks": mixed["clocks"] or plain["clocks"],
         "energy": mixed["energy"], "contacts": mixed["contacts"],
     }
+    if not a.no_extras and world == 1:
+        line["load_unload"] = load_unload(fd, abi, workloads)
+        line["sweep"] = sweep(fd, abi, workloads)
     print(json.dumps(line), flush=True)
+
+
+def run_summary(frames):
+    return {"frames": len(frames), "iterations": int(sum(f["iterations"] for f in frames)),
+            "peak_force": max(f["reaction_force"] for f in frames), "absorbed_energy": frames[-1]["loading_work"],
+            "dissipated_work": frames[-1]["dissipated_work"], "permanent_set": frames[-1]["permanent_set"]}
+
+
+def load_unload(fd, abi, workloads):
+    """The 32x32x16 cubic+BCC specimen, 60 % strain in 400 + 400 increments, mixed against
+    FP64: wall time of the whole run (minimize, commit, diagnostics on the device; host
+    decisions per round) and the run-level figures, with their errors against FP64."""
+    out = {}
+    for name, prec in (("mixed", abi.MCG_MIXED), ("fp64", abi.MCG_FP64)):
+        cfg, spec = workloads.bcc32()
+        cfg.precision = prec
+        lat = fd.generate_lattice(spec, cfg)
+        sol = fd.Solver(cfg, lat)
+        t0 = time.perf_counter()
+        rc, frames = sol.run()
+        dt = time.perf_counter() - t0
+        sol.close()
+        out[name] = dict(run_summary(frames), seconds=dt, status=int(rc))
+    m, f = out["mixed"], out["fp64"]
+    out["speedup_mixed_over_fp64"] = f["seconds"] / m["seconds"]
+    out["rel_err_mixed_vs_fp64"] = {k: abs(m[k] - f[k]) / abs(f[k]) for k in
+                                    ("peak_force", "absorbed_energy", "dissipated_work", "permanent_set")}
+    out["workload"] = "bcc32: cubic+BCC 32x32x16, radius 0.25->0.7 mm graded, 60 % strain, 400 + 400 increments"
+    return out
+
+
+def sweep(fd, abi, workloads, sample=4):
+    """The batched sweep: 256 lattices (4-16 cells per side) solved together in FP64, against
+    the same lattices solved one after another (a spread sample of `sample` lattices timed,
+    throughput in lattices per second)."""
+    cfg, specs, ys = workloads.sweep()
+    lats = [fd.generate_lattice(s, cfg) for s in specs]
+    b = fd.BatchSolver(cfg, lats, yields=ys)
+    t0 = time.perf_counter()
+    status, runs = b.run()
+    dt = time.perf_counter() - t0
+    b.close()
+    idx = np.linspace(0, len(lats) - 1, sample).astype(int)
+    t0 = time.perf_counter()
+    same = True
+    for k in idx:
+        c = abi.Config.from_buffer_copy(cfg)
+        c.material.yield_ = ys[k]
+        s = fd.Solver(c, lats[k])
+        rc, fr = s.run()
+        s.close()
+        same &= [x["reaction_force"] for x in fr] == [x["reaction_force"] for x in runs[k]]
+    ds = time.perf_counter() - t0
+    batched, seq = len(lats) / dt, sample / ds
+    return {"metric": "lattices/s", "batched_fp64": batched, "sequential_fp64": seq, "speedup": batched / seq,
+            "batched_seconds": dt, "sequential_sample": f"{sample} lattices spread over the sweep, {ds:.1f} s",
+            "completed": int((np.asarray(status) == 0).sum()), "lattices": len(lats),
+            "beams": int(sum(l.n_beams for l in lats)), "sample_frames_identical_to_batch": bool(same),
+            "workload": "256 cubic+BCC lattices, 4-16 cells per side, radius 0.3 mm + U[0, 0.1] mm/cell "
+                        "(capped 0.7 mm), yield U[30, 70] MPa, 30 % strain in 100 increments"}
 
 
 if __name__ == "__main__":

@@ -48,6 +48,7 @@ SIGNATURES = {
     "mcg_set_timing": (C.c_int, [_P, C.c_int]),
     "mcg_set_contact_capacity": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64]),
     "mcg_set_contact_skin": (C.c_int, [_P, C.c_double]),
+    "mcg_contact_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -247,6 +248,12 @@ class Solver:
     def launch_count(self):
         return self.lib.mcg_launch_count(self.h)
 
+    def contact_stats(self):
+        """Entries, occupied bins, candidates and contacts of the last list build / evaluation."""
+        out = (C.c_int64 * 4)()
+        self._check(self.lib.mcg_contact_stats(self.h, out), "mcg_contact_stats")
+        return dict(zip(("entries", "occupied_bins", "candidates", "contacts"), list(out)))
+
     def set_contact_skin(self, skin):
         """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""
         self._check(self.lib.mcg_set_contact_skin(self.h, float(skin)), "mcg_set_contact_skin")
@@ -255,17 +262,20 @@ class Solver:
         self._check(self.lib.mcg_set_contact_capacity(self.h, entries, candidates, contacts, bins),
                     "mcg_set_contact_capacity")
 
-    PHASES = ("state", "beams", "contacts", "gather", "finalize")
+    PHASES = ("state", "beams", "grid", "pairs", "narrow", "gather", "finalize")
 
     def set_timing(self, on):
         self._check(self.lib.mcg_set_timing(self.h, int(on)), "mcg_set_timing")
 
     def phase_times(self):
-        """Summed milliseconds per evaluation phase since timing was switched on."""
+        """Summed milliseconds per evaluation phase since timing was switched on; "contacts"
+        is grid + pairs + narrow."""
         ms = np.zeros(len(self.PHASES))
         n = C.c_int64()
         self._check(self.lib.mcg_phase_times(self.h, _ptr(ms), len(ms), C.byref(n)), "mcg_phase_times")
-        return dict(zip(self.PHASES, ms)), n.value
+        out = dict(zip(self.PHASES, ms))
+        out["contacts"] = out["grid"] + out["pairs"] + out["narrow"]
+        return out, n.value
 
 
 class BatchSolver(Solver):

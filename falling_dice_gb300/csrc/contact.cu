@@ -809,7 +809,7 @@ int contact_pair_blocks(long long shapes) {
 }
 
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                     float skin, cudaStream_t s) {
+                     float skin, cudaStream_t s, cudaEvent_t pairs_begin, cudaEvent_t pairs_end) {
     const int S = t.N + t.B;
     const uint32_t* gate = c.flags + 1;
     cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
@@ -833,9 +833,11 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
     const uint32_t* nocc = c.boffset + c.bin_cap;
     const int W = c.pair_blocks * kPairWarps;
+    if (pairs_begin) cudaEventRecord(pairs_begin, s);
     (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted, c.sorted2,
                                                 c.rec, c.region, c.cand, c.wcount, c.wcap, c.flags),
      note_launches(1));
+    if (pairs_end) cudaEventRecord(pairs_end, s);
     exclusive_scan_u32(c.wcap, c.woff, W, c.scan_tmp, s, gate);
     (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
     // narrow phase over the candidate list: hit bits and counts per chunk, scan, contacts

@@ -237,7 +237,9 @@ struct mcg_ctx {
     bool have_final = false;  // instance 0 has a final state from minimize, not yet committed
 
     // optional per-phase timing of evaluations (events on the context stream)
-    static constexpr int kPhases = 5;  // state, beams, contacts, gather, finalize
+    // state, beams, contact grid (up to the pair enumeration), pair enumeration (k_bin_pairs),
+    // narrow phase and contact lists, gather, finalize
+    static constexpr int kPhases = 7;
     bool timing = false;
     cudaEvent_t ev_t[kPhases + 1] = {};
     double phase_ms[kPhases] = {};
@@ -375,15 +377,19 @@ struct mcg_ctx {
         mark(2);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
-            launch_contacts(topo, p, ev, cb, rmax + cfg.contact_margin, contact_skin, stream);
+            launch_contacts(topo, p, ev, cb, rmax + cfg.contact_margin, contact_skin, stream,
+                            timing ? ev_t[3] : nullptr, timing ? ev_t[4] : nullptr);
             cptr = &cb;
+        } else {
+            mark(3);
+            mark(4);
         }
-        mark(3);
+        mark(5);
         if (mixed) launch_gather_mixed(topo, p, cptr, d_gout, ev, stream);
         else launch_gather(topo, p, cptr, d_gout, ev, stream);
-        mark(4);
+        mark(6);
         launch_finalize(topo, p, cptr, d_gout, ev, stream);
-        mark(5);
+        mark(7);
         check_launch();
         collect();
         last_z = dz;
@@ -1720,6 +1726,21 @@ int mcg_set_contact_skin(mcg_ctx* c, double skin) {
         c->contact_skin = float(skin);
         // the stored list was built for the previous skin
         ck(cudaMemsetAsync(c->cb.flags + 2, 1, 1, c->stream), "memset");
+    });
+}
+
+int mcg_contact_stats(mcg_ctx* c, int64_t* out4) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!out4) throw Fail(MCG_ERR_INVALID, "null output");
+        const long long S = (long long)c->N + c->B;
+        const long long W = (long long)c->cb.pair_blocks * 8;
+        d2h(c->hp.u32, c->cb.offset + S, 1, c->stream);
+        d2h(c->hp.u32 + 1, c->cb.boffset + c->cb.bin_cap, 1, c->stream);
+        d2h(c->hp.u32 + 2, c->cb.woff + W, 1, c->stream);
+        d2h(c->hp.u32 + 3, c->cb.hoff + c->contact_chunks(), 1, c->stream);
+        c->sync();
+        for (int k = 0; k < 4; k++) out4[k] = c->hp.u32[k];
     });
 }
 

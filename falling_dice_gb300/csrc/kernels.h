@@ -257,8 +257,9 @@ int contact_pair_blocks(long long shapes);
 // The whole broad/narrow phase: grid, entries, bins, pairs, contact list, node lists.
 // The candidate list is rebuilt only when a node has moved more than skin (m, per axis)
 // since the last build, or the host forced it (flags[2]); skin <= 0 rebuilds every time.
+// pairs_begin / pairs_end (may be null) are recorded around the pair enumeration.
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
-                     float skin, cudaStream_t s);
+                     float skin, cudaStream_t s, cudaEvent_t pairs_begin = nullptr, cudaEvent_t pairs_end = nullptr);
 
 // ---- scan (sort.cu) -----------------------------------------------------------------------
 size_t scan_tmp_bytes(long long n);

@@ -271,10 +271,15 @@ int mcg_batch_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* co
  * the default after mcg_upload_topology is cell_size / 8. */
 int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
 
+/* Sizes of the last self-contact candidate-list build and evaluation (no reference
+ * counterpart): out4 = {cell entries, occupied bins, narrow-phase candidates, contacts}. */
+int mcg_contact_stats(mcg_ctx* ctx, int64_t* out4);
+
 /* Per-phase timing of evaluations with CUDA events on the context stream (no reference
  * counterpart).  While on, every evaluation synchronizes at its end and adds its phase
- * durations: [0] node state, [1] beam kernel, [2] self-contact pipeline, [3] gradient
- * gather, [4] totals.  mcg_set_timing resets the sums. */
+ * durations: [0] node state, [1] beam kernel, [2] contact grid (skin check, cells, bins),
+ * [3] pair enumeration, [4] narrow phase and contact lists, [5] gradient gather,
+ * [6] totals.  mcg_set_timing resets the sums. */
 int mcg_set_timing(mcg_ctx* ctx, int on);
 int mcg_phase_times(mcg_ctx* ctx, double* ms, int32_t n, int64_t* evaluations);
 
