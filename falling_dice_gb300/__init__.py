@@ -249,10 +249,11 @@ class Solver:
         return self.lib.mcg_launch_count(self.h)
 
     def contact_stats(self):
-        """Entries, occupied bins, candidates and contacts of the last list build / evaluation."""
-        out = (C.c_int64 * 4)()
+        """Entries, occupied bins, candidates, filtered candidates and contacts of the last list
+        build / evaluation."""
+        out = (C.c_int64 * 5)()
         self._check(self.lib.mcg_contact_stats(self.h, out), "mcg_contact_stats")
-        return dict(zip(("entries", "occupied_bins", "candidates", "contacts"), list(out)))
+        return dict(zip(("entries", "occupied_bins", "candidates", "filtered", "contacts"), list(out)))
 
     def set_contact_skin(self, skin):
         """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""

@@ -595,9 +595,9 @@ __global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const ui
 }
 
 
-// Certified single-precision rejection of a candidate pair: true when the two shapes are
-// certainly farther apart than pad_a + pad_b (>= the reference's target ra + rb + margin),
-// so the reference's test dist < target fails and the pair is no contact.
+// Certified single-precision distance bounds of a candidate pair.  A pair certainly farther
+// apart than pad_a + pad_b (>= the reference's target ra + rb + margin) fails the reference's
+// test dist < target; a pair certainly closer than the target passes it.
 //
 // For any unit vector n, the distance between segments p1 + s d1 and p2 + t d2 (s, t in
 // [0, 1]) is at least  L(n) = n.(p1 - p2) + min(0, n.d1) - max(0, n.d2):  n.(P - Q) <= |P - Q|
@@ -608,8 +608,15 @@ __global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const ui
 // rounding of the differences, the three dot products and the sums adds at most about
 // 4e-6 X in total, bounded here by 3e-5 X + 1e-9 m, and |n| = 1 up to 1e-6.  A pair that
 // cannot be certified (touching segments, non-finite data) goes to the exact test.
-__device__ __forceinline__ bool certainly_apart(const DevTopo& t, const PhysParams& p, const float4* __restrict__ xf,
-                                                uint32_t sa, uint32_t sb) {
+struct DistBounds {
+    bool far_ok;      // far is a valid lower bound (the closest points are not within 1e-7 m)
+    float far;        // certified lower bound on the distance, already less its error
+    float near;       // certified upper bound on the distance between points at (s, tt)
+    float pad_sum;    // pad_a + pad_b >= the reference's target
+    float target_lo;  // <= the reference's target ra + rb + margin
+};
+__device__ __forceinline__ DistBounds dist_bounds(const DevTopo& t, const PhysParams& p, const float4* __restrict__ xf,
+                                                  uint32_t sa, uint32_t sb) {
     const int2 na = sa < uint32_t(t.N) ? make_int2(int(sa), int(sa)) : t.ab[sa - uint32_t(t.N)];
     const int2 nb = sb < uint32_t(t.N) ? make_int2(int(sb), int(sb)) : t.ab[sb - uint32_t(t.N)];
     const float pa = sa < uint32_t(t.N) ? p.joint_padf : t.padf[sa - uint32_t(t.N)];
@@ -643,39 +650,67 @@ __device__ __forceinline__ bool certainly_apart(const DevTopo& t, const PhysPara
     }
     const float nx = wx + ux * s - vx * tt, ny = wy + uy * s - vy * tt, nz = wz + uz * s - vz * tt;
     const float nn = nx * nx + ny * ny + nz * nz;
-    if (!(nn > 1e-14f)) return false;  // closer than 1e-7 m (or not finite): no certificate
-    const float inv = rsqrtf(nn);
-    const float mx = nx * inv, my = ny * inv, mz = nz * inv;
-    const float nu = mx * ux + my * uy + mz * uz, nv = mx * vx + my * vy + mz * vz;
-    const float L = (mx * wx + my * wy + mz * wz) + fminf(0.f, nu) - fmaxf(0.f, nv);
-    return L * 0.999999f - (3e-5f * X + 1e-9f) > (pa + pb) * 1.000001f;
+    const float err = 3e-5f * X + 1e-9f;
+    DistBounds r;
+    r.pad_sum = (pa + pb) * 1.000001f;
+    // the pads less one margin exceed the target by at most two FP32 roundings
+    r.target_lo = (pa + pb - float(p.contact_margin)) * 0.999999f;
+    r.near = isfinite(nn) ? sqrtf(nn) * 1.000001f + err : __int_as_float(0x7f800000);
+    r.far_ok = nn > 1e-14f;  // false also when not finite
+    r.far = 0.f;
+    if (r.far_ok) {
+        const float inv = rsqrtf(nn);
+        const float mx = nx * inv, my = ny * inv, mz = nz * inv;
+        const float nu = mx * ux + my * uy + mz * uz, nv = mx * vx + my * vy + mz * vz;
+        const float L = (mx * wx + my * wy + mz * wz) + fminf(0.f, nu) - fmaxf(0.f, nv);
+        r.far = L * 0.999999f - err;
+    }
+    return r;
 }
 
-// Global candidate index g (regions in warp order, each in its own order) -> its slot:
-// the warp whose prefix range [woff[w], woff[w + 1]) holds g, by binary search.
-__device__ __forceinline__ uint2 candidate_at(const uint2* __restrict__ cand, const uint32_t* __restrict__ woff,
-                                              int W, int region, uint32_t g) {
+// -1: certainly no contact; +1: certainly within the target (if not a local pair); 0: only
+// the exact test can tell.
+__device__ __forceinline__ int distance_class(const DevTopo& t, const PhysParams& p, const float4* __restrict__ xf,
+                                              uint32_t sa, uint32_t sb) {
+    const DistBounds d = dist_bounds(t, p, xf, sa, sb);
+    if (d.near < d.target_lo) return 1;
+    return d.far_ok && d.far > d.pad_sum ? -1 : 0;
+}
+
+// Global candidate index g (regions in warp order, each in its own order) -> the warp whose
+// prefix range [woff[w], woff[w + 1]) holds it, by binary search.
+__device__ __forceinline__ int candidate_warp(const uint32_t* __restrict__ woff, int W, uint32_t g) {
     int lo = 0, hi = W;  // woff[lo] <= g < woff[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (woff[mid] <= g) lo = mid;
         else hi = mid;
     }
-    return cand[(long long)lo * region + (g - woff[lo])];
+    return lo;
+}
+// The candidate at g, starting from the warp w0 that holds an earlier index of the same
+// chunk: a few steps forward, or a search when many regions in a row are short.
+__device__ __forceinline__ uint2 candidate_slot(const uint2* __restrict__ cand, const uint32_t* __restrict__ woff,
+                                                int W, int region, uint32_t g, int w0) {
+    int w = w0;
+    for (int k = 0; k < 8 && w + 1 < W && woff[w + 1] <= g; k++) w++;
+    if (w + 1 < W && woff[w + 1] <= g) w = candidate_warp(woff, W, g);
+    return cand[(long long)w * region + (g - woff[w])];
 }
 
-// Narrow phase over the candidate list, flattened so that each thread takes one candidate
-// whatever region it sits in (a warp's region can hold far more candidates than another's).
-// Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
-// 32.  Pass 1 (after a scan of the chunk counts of the list's length): test the hits again
-// and write them as contacts, in candidate order.
+// Candidate filter, once per list build: keeps, in order, the region candidates of one
+// instance whose certified distance lower bound at the build does not exceed the pads plus
+// `reach` (2 sqrt(3) skin: two endpoints that each move at most skin per axis close a gap by
+// at most that).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
+// counts): the kept candidates, compacted.
 template <int pass>
-__global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                   const float4* __restrict__ xf, int region, int W,
-                                                   const uint2* __restrict__ cand,
-                                                   const uint32_t* __restrict__ woff, long long chunks,
-                                                   uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
-                                                   const uint32_t* __restrict__ hoff, ContactBufs c) {
+__global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf, int region,
+                                                   int W, const uint2* __restrict__ cand,
+                                                   const uint32_t* __restrict__ woff, float reach,
+                                                   uint32_t* __restrict__ fbits, uint32_t* __restrict__ fcount,
+                                                   const uint32_t* __restrict__ foff, uint2* __restrict__ cand2,
+                                                   const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
     const uint32_t total = woff[W];
@@ -684,9 +719,52 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
     for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
         const uint32_t g = uint32_t(ch * 32 + lane);
         if constexpr (pass == 1) {
+            if (!fbits[ch]) continue;  // warp-uniform
+        }
+        const int w0 = candidate_warp(woff, W, uint32_t(ch * 32));
+        if constexpr (pass == 0) {
+            bool keep = false;
+            if (g < total) {
+                const uint2 q = candidate_slot(cand, woff, W, region, g, w0);
+                const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
+                if (t.node_inst[na.x] == t.node_inst[nb.x]) {
+                    const DistBounds d = dist_bounds(t, p, xf, q.x, q.y);
+                    keep = !(d.far_ok && d.far > d.pad_sum + reach);
+                }
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) {
+                fbits[ch] = m;
+                fcount[ch] = __popc(m);
+            }
+        } else {
+            const unsigned m = fbits[ch];
+            if (m & (1u << lane)) cand2[foff[ch] + __popc(m & below)] = candidate_slot(cand, woff, W, region, g, w0);
+        }
+    }
+}
+
+// Narrow phase over the filtered list (flat, in order), one candidate per thread.
+// Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
+// 32.  Pass 1 (after a scan of the chunk counts of the list's length): test the hits again
+// and write them as contacts, in candidate order.
+template <int pass>
+__global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
+                                                   const float4* __restrict__ xf, const uint2* __restrict__ cand2,
+                                                   const uint32_t* __restrict__ ntotal,
+                                                   uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
+                                                   const uint32_t* __restrict__ hoff, ContactBufs c) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const uint32_t total = *ntotal;
+    const long long nchunk = (total + 31) / 32;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
+        const uint32_t g = uint32_t(ch * 32 + lane);
+        if constexpr (pass == 1) {
             const unsigned m = hitbits[ch];
             if (m & (1u << lane)) {
-                const uint2 q = candidate_at(cand, woff, W, region, g);
+                const uint2 q = cand2[g];
                 const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
                 const uint32_t o = hoff[ch] + __popc(m & below);
                 if (o < uint32_t(c.contact_cap)) {
@@ -703,10 +781,11 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
         } else {
             bool hit = false;
             if (g < total) {
-                const uint2 q = candidate_at(cand, woff, W, region, g);
+                const uint2 q = cand2[g];
                 const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
-                hit = t.node_inst[na.x] == t.node_inst[nb.x] && !certainly_apart(t, p, xf, q.x, q.y) &&
-                      narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y)).hit;
+                const int cls = distance_class(t, p, xf, q.x, q.y);
+                if (cls > 0) hit = !any_connected(t, na, nb);  // certainly within the target
+                else if (cls == 0) hit = narrow_phase(t, p, x, q.x, q.y, na, nb).hit;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
             if (lane == 0) {
@@ -839,14 +918,22 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);
     exclusive_scan_u32(c.wcap, c.woff, W, c.scan_tmp, s, gate);
-    (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
-    // narrow phase over the candidate list: hit bits and counts per chunk, scan, contacts
+    // filtered list (only when rebuilding)
     const long long chunks = (long long)W * c.region / 32;
-    (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
-                                                c.hcount, c.hoff, c), note_launches(1));
-    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, c.woff + W, 31, 5);
-    (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.region, W, c.cand, c.woff, chunks, c.hitbits,
-                                                c.hcount, c.hoff, c), note_launches(1));
+    const float reach = skin > 0.f ? 3.4642f * skin : 0.f;  // >= 2 sqrt(3) skin
+    (k_filter<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.region, W, c.cand, c.woff, reach, c.fbits, c.fcount,
+                                                c.foff, c.cand2, gate), note_launches(1));
+    exclusive_scan_u32(c.fcount, c.foff, chunks, c.scan_tmp, s, gate, c.woff + W, 31, 5);
+    (k_filter<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.region, W, c.cand, c.woff, reach, c.fbits, c.fcount,
+                                                c.foff, c.cand2, gate), note_launches(1));
+    (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
+    // narrow phase over the filtered list: hit bits and counts per chunk, scan, contacts
+    const uint32_t* nkept = c.foff + chunks;
+    (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
+     note_launches(1));
+    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, nkept, 31, 5);
+    (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
+     note_launches(1));
     const uint32_t* total = c.hoff + chunks;
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);

@@ -302,6 +302,10 @@ struct mcg_ctx {
         c.wcap = contact_mem.get<uint32_t>(size_t(W + 1));
         c.woff = contact_mem.get<uint32_t>(size_t(W + 1));
         const long long chunks = W * c.region / 32;
+        c.cand2 = contact_mem.get<uint2>(size_t(W * c.region));
+        c.fbits = contact_mem.get<uint32_t>(size_t(chunks));
+        c.fcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
+        c.foff = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.hitbits = contact_mem.get<uint32_t>(size_t(chunks));
         c.hcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.hoff = contact_mem.get<uint32_t>(size_t(chunks + 1));
@@ -1272,7 +1276,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     // contact buffers: a first guess, grown on demand
     const long long S = (long long)N + B;
     c->broad_cell = P.broad_cell;
-    c->contact_skin = float(0.125 * cf.cell_size);
+    c->contact_skin = float(cf.cell_size / 32);
     {
         // bins: the Morton range of the rest-state extent (in the grid's frame) with room to
         // grow, or row-major bins when that range is too large
@@ -1729,18 +1733,19 @@ int mcg_set_contact_skin(mcg_ctx* c, double skin) {
     });
 }
 
-int mcg_contact_stats(mcg_ctx* c, int64_t* out4) {
+int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
     return guarded(c, [&] {
         need_topo(c);
-        if (!out4) throw Fail(MCG_ERR_INVALID, "null output");
+        if (!out5) throw Fail(MCG_ERR_INVALID, "null output");
         const long long S = (long long)c->N + c->B;
         const long long W = (long long)c->cb.pair_blocks * 8;
         d2h(c->hp.u32, c->cb.offset + S, 1, c->stream);
         d2h(c->hp.u32 + 1, c->cb.boffset + c->cb.bin_cap, 1, c->stream);
         d2h(c->hp.u32 + 2, c->cb.woff + W, 1, c->stream);
-        d2h(c->hp.u32 + 3, c->cb.hoff + c->contact_chunks(), 1, c->stream);
+        d2h(c->hp.u32 + 3, c->cb.foff + c->contact_chunks(), 1, c->stream);
+        d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
-        for (int k = 0; k < 4; k++) out4[k] = c->hp.u32[k];
+        for (int k = 0; k < 5; k++) out5[k] = c->hp.u32[k];
     });
 }
 

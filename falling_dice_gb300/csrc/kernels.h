@@ -138,7 +138,12 @@ struct ContactBufs {
     uint32_t* wcount;       // [warps] candidates found per warp (may exceed region)
     uint32_t* wcap;         // [warps + 1] the same capped at region
     uint32_t* woff;         // [warps + 1] scan of wcap: warp w's candidates are [woff[w], woff[w + 1])
-    // narrow phase, per chunk of 32 consecutive candidates (chunks = warps * region / 32)
+    // filtered candidates (the ones that can reach contact before the next build), in order
+    uint2* cand2;           // [warps * region]
+    uint32_t* fbits;        // [chunks] keep bit per region candidate (chunks = warps * region / 32)
+    uint32_t* fcount;       // [chunks + 1] kept per chunk
+    uint32_t* foff;         // [chunks + 1] scan of fcount; foff[chunks] = filtered list length
+    // narrow phase, per chunk of 32 consecutive filtered candidates
     uint32_t* hitbits;      // [chunks] contact bit per candidate
     uint32_t* hcount;       // [chunks + 1] contacts per chunk
     uint32_t* hoff;         // [chunks + 1] scan of hcount; hoff[chunks] = contact count

@@ -105,6 +105,10 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.wcap = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
     c.woff = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
     const long long chunks = W * c.region / 32;
+    c.cand2 = reinterpret_cast<uint2*>(take(size_t(W * c.region) * sizeof(uint2)));
+    c.fbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
+    c.fcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
+    c.foff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.hitbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
     c.hcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.hoff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));

@@ -268,12 +268,13 @@ int mcg_batch_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* co
  * evaluations skip the grid and pair enumeration.  Every pair the reference would test is
  * still tested exactly, and contact sums do not depend on the list, so energies,
  * gradients and pair sets are bitwise those of a rebuild.  0 rebuilds at every evaluation;
- * the default after mcg_upload_topology is cell_size / 8. */
+ * the default after mcg_upload_topology is cell_size / 32. */
 int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
 
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
- * counterpart): out4 = {cell entries, occupied bins, narrow-phase candidates, contacts}. */
-int mcg_contact_stats(mcg_ctx* ctx, int64_t* out4);
+ * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept
+ * by the distance filter, contacts}. */
+int mcg_contact_stats(mcg_ctx* ctx, int64_t* out5);
 
 /* Per-phase timing of evaluations with CUDA events on the context stream (no reference
  * counterpart).  While on, every evaluation synchronizes at its end and adds its phase
