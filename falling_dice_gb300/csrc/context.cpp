@@ -1199,8 +1199,17 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         c->sync();  // the host vectors above go out of scope
     }
     c->topo = T;
-    c->mat = Material{E, G, cf.material.yield, cf.material.hardening, cf.material.bend_hardening,
-                      cf.material.torsion_hardening, 1.0 / std::max(1e-20, E + cf.material.hardening)};
+    c->mat = Material{E,
+                      G,
+                      cf.material.yield,
+                      cf.material.hardening,
+                      cf.material.bend_hardening,
+                      cf.material.torsion_hardening,
+                      1.0 / std::max(1e-20, E + cf.material.hardening),
+                      float(E),
+                      float(cf.material.hardening),
+                      float(cf.material.bend_hardening),
+                      float(cf.material.torsion_hardening)};
     PhysParams P{};
     P.translation_scale = cf.translation_scale;
     P.gravity = cf.gravity;
@@ -1264,6 +1273,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         MixedBeams mb{};
         float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B3, &mb.B4, &mb.B5, &mb.C0, &mb.C1, &mb.P0, &mb.P1};
         for (float4** f : fields) *f = V.get<float4>(size_t(B));
+        mb.syf = V.get<float>(size_t(B));
         c->mb = mb;
         c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
     }

@@ -25,6 +25,7 @@ namespace mcg {
 struct Material {
     double E, G, sy, H, bend_h, torsion_h;
     double inv_EH;  // 1 / max(1e-20, E + H)
+    float Ef, Hf, bend_hf, torsion_hf;  // the same in single precision (mixed form)
 };
 
 struct DevTopo {
@@ -206,6 +207,7 @@ struct MixedBeams {
     float4* C1;  // cs, area L0, area, area L0 yield
     float4* P0;  // plastic: epsp, alpha, alphaB, alphaT
     float4* P1;  // plastic: rotp
+    float* syf;  // yield stress
 };
 // Per-node data of the mixed-precision form.
 struct MixedNodes {

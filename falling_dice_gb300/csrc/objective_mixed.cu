@@ -268,10 +268,11 @@ __global__ void __launch_bounds__(kBlock) k_mixed_constants(DevTopo t, MixedBeam
     if (b >= t.B) return;
     m.C0[b] = make_float4(float(t.kb[b]), float(t.kt[b]), float(t.my[b]), float(t.ty[b]));
     m.C1[b] = make_float4(float(t.cs[b]), float(t.aL[b]), float(t.area[b]), float(t.aLsy[b]));
+    m.syf[b] = float(t.sy[b]);
 }
 
 // ---- beam kernel (MC/src/sim.cpp:139-141, FP32 with the split above) ---------------------
-__global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
+__global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
@@ -307,7 +308,7 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
             const float eps = q / ((L + L0) * L0);
             const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), rotp
             const float4 C0 = m.C0[b], C1 = m.C1[b];  // (kb, kt, my, ty), (cs, aL, area, aLsy)
-            const float E = float(mat.E), H = float(mat.H), sy = float(t.sy[b]);
+            const float E = mat.Ef, H = mat.Hf, sy = m.syf[b];
             // axial
             const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
             const float uax = C1.y * (ax.energy + ax.hard);
@@ -354,8 +355,8 @@ __global__ void __launch_bounds__(kBlock) k_beams_mixed(DevTopo t, Material mat,
             const float tw = fdot(phi, axis), ptw = fdot(rotp, axis);
             const f3 bend = phi - axis * tw, pbv = rotp - axis * ptw;
             const float kb = C0.x, kt = C0.y, my = C0.z, ty = C0.w;
-            const R3 br = ret3(bend, pbv, P0.z, kb, my, float(mat.bend_h) * kb);
-            const R1 tor = ret1(tw, ptw, P0.w, kt, ty, float(mat.torsion_h) * kt);
+            const R3 br = ret3(bend, pbv, P0.z, kb, my, mat.bend_hf * kb);
+            const R1 tor = ret1(tw, ptw, P0.w, kt, ty, mat.torsion_hf * kt);
             const f3 moment = br.force + axis * tor.force;
             const float ur = br.energy + br.hard + tor.energy + tor.hard;
             const float dr = my * br.dg + ty * tor.dg;
