@@ -746,8 +746,8 @@ __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, cons
 
 // Narrow phase over the filtered list (flat, in order), one candidate per thread.
 // Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
-// 32.  Pass 1 (after a scan of the chunk counts of the list's length): test the hits again
-// and write them as contacts, in candidate order.
+// 32.  Pass 1 (after a scan of the chunk counts of the list's length): the hits' candidate
+// indices, compacted in candidate order (into c_a, overwritten by k_contacts).
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
                                                    const float4* __restrict__ xf, const uint2* __restrict__ cand2,
@@ -762,21 +762,11 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
     for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
         const uint32_t g = uint32_t(ch * 32 + lane);
         if constexpr (pass == 1) {
+            // the hits' candidates, compacted in order: contact o is candidate hits[o]
             const unsigned m = hitbits[ch];
             if (m & (1u << lane)) {
-                const uint2 q = cand2[g];
-                const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
                 const uint32_t o = hoff[ch] + __popc(m & below);
-                if (o < uint32_t(c.contact_cap)) {
-                    c.c_a[o] = q.x;
-                    c.c_b[o] = q.y;
-                    c.c_s[o] = h.s;
-                    c.c_t[o] = h.t;
-                    c.c_n[3 * size_t(o)] = h.n.x;
-                    c.c_n[3 * size_t(o) + 1] = h.n.y;
-                    c.c_n[3 * size_t(o) + 2] = h.n.z;
-                    c.c_pen[o] = h.pen;
-                }
+                if (o < uint32_t(c.contact_cap)) c.c_a[o] = g;
             }
         } else {
             bool hit = false;
@@ -793,6 +783,26 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
                 hcount[ch] = __popc(m);
             }
         }
+    }
+}
+
+// The contacts, one hit per thread (dense: the FP64 closest points run with full warps):
+// contact o is candidate c_a[o] of the filtered list, written in candidate order.
+__global__ void __launch_bounds__(kBlock) k_contacts(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
+                                                     const uint2* __restrict__ cand2,
+                                                     const uint32_t* __restrict__ total, ContactBufs c) {
+    const long long nc = min((long long)*total, c.contact_cap);
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < nc; o += (long long)gridDim.x * blockDim.x) {
+        const uint2 q = cand2[c.c_a[o]];
+        const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
+        c.c_a[o] = q.x;
+        c.c_b[o] = q.y;
+        c.c_s[o] = h.s;
+        c.c_t[o] = h.t;
+        c.c_n[3 * size_t(o)] = h.n.x;
+        c.c_n[3 * size_t(o) + 1] = h.n.y;
+        c.c_n[3 * size_t(o) + 2] = h.n.z;
+        c.c_pen[o] = h.pen;
     }
 }
 
@@ -934,6 +944,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, nkept, 31, 5);
     (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
      note_launches(1));
+    (k_contacts<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, c.cand2, c.hoff + chunks, c), note_launches(1));
     const uint32_t* total = c.hoff + chunks;
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);

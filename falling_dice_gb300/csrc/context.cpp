@@ -259,6 +259,7 @@ struct mcg_ctx {
     }
 
     ~mcg_ctx() {
+        drop_graphs();
         for (auto& e : ev_t)
             if (e) cudaEventDestroy(e);
         if (stream) cudaStreamDestroy(stream);
@@ -272,6 +273,7 @@ struct mcg_ctx {
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
     float contact_skin = 0;  // candidate-list reuse distance (m); 0 rebuilds every evaluation
     void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, int region) {
+        drop_graphs();
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
@@ -366,9 +368,56 @@ struct mcg_ctx {
     // Platen heights of all instances from hp.tops (the host changes them only after a sync).
     void upload_tops() { h2d(ev.tops, hp.tops, size_t(I), stream); }
 
+    // Captured evaluations: the launch sequence of eval_launches for one (z, gradient,
+    // trials) combination, replayed as one graph.  Any change of what the launches bake in
+    // (contact buffers, grid cell, skin) drops them.
+    struct EvalGraph {
+        const double* dz;
+        double* d_gout;
+        bool trials;
+        cudaGraphExec_t exec;
+        long long kernels;  // kernel launches a replay performs
+    };
+    std::vector<EvalGraph> graphs;
+    bool use_graphs = true;
+    void drop_graphs() {
+        for (EvalGraph& g : graphs) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
+    }
+
     // One evaluation of every instance at device z; grad written to d_gout; totals in
     // ev.out[0..I).  Enqueues only: no host synchronisation.
     void eval(const double* dz, bool trials, double* d_gout) {
+        if (!use_graphs || timing) {
+            eval_launches(dz, trials, d_gout);
+        } else {
+            const EvalGraph* found = nullptr;
+            for (const EvalGraph& g : graphs)
+                if (g.dz == dz && g.d_gout == d_gout && g.trials == trials) found = &g;
+            if (!found) {
+                cudaGraph_t graph = nullptr;
+                cudaGraphExec_t exec = nullptr;
+                const long long before = g_launch_count.load();
+                ck(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+                eval_launches(dz, trials, d_gout);
+                ck(cudaStreamEndCapture(stream, &graph), "cudaStreamEndCapture");
+                const long long kernels = g_launch_count.load() - before;
+                g_launch_count -= kernels;  // counted when the graph runs
+                const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+                cudaGraphDestroy(graph);
+                ck(e, "cudaGraphInstantiate");
+                graphs.push_back(EvalGraph{dz, d_gout, trials, exec, kernels});
+                found = &graphs.back();
+            }
+            ck(cudaGraphLaunch(found->exec, stream), "cudaGraphLaunch");
+            note_launches(int(found->kernels));
+        }
+        last_z = dz;
+        last_trials = trials;
+        last_grad = d_gout;
+    }
+
+    void eval_launches(const double* dz, bool trials, double* d_gout) {
         PhysParams p = phys;
         p.broad_cell = broad_cell;
         p.inv_cell_f = float(1.0 / broad_cell);
@@ -396,9 +445,6 @@ struct mcg_ctx {
         mark(7);
         check_launch();
         collect();
-        last_z = dz;
-        last_trials = trials;
-        last_grad = d_gout;
     }
     const double* last_z = nullptr;
     bool last_trials = false;
@@ -1096,6 +1142,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     }
 
     c->sync();
+    c->drop_graphs();
     c->topo_mem.release();
     c->eval_mem.release();
     c->contact_mem.release();
@@ -1426,6 +1473,7 @@ void mcg_destroy(mcg_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    c->drop_graphs();
     c->topo_mem.release();
     c->eval_mem.release();
     c->contact_mem.release();
@@ -1738,6 +1786,7 @@ int mcg_set_contact_skin(mcg_ctx* c, double skin) {
         need_topo(c);
         if (!(skin >= 0) || skin > 1e3) throw Fail(MCG_ERR_INVALID, "skin must be a distance >= 0 (m)");
         c->contact_skin = float(skin);
+        c->drop_graphs();
         // the stored list was built for the previous skin
         ck(cudaMemsetAsync(c->cb.flags + 2, 1, 1, c->stream), "memset");
     });
