@@ -49,6 +49,7 @@ SIGNATURES = {
     "mcg_set_contact_capacity": (C.c_int, [_P, C.c_int64, C.c_int64, C.c_int64, C.c_int64]),
     "mcg_set_contact_skin": (C.c_int, [_P, C.c_double]),
     "mcg_contact_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcg_set_contact_cell": (C.c_int, [_P, C.c_double]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -254,6 +255,10 @@ class Solver:
         out = (C.c_int64 * 5)()
         self._check(self.lib.mcg_contact_stats(self.h, out), "mcg_contact_stats")
         return dict(zip(("entries", "occupied_bins", "candidates", "filtered", "contacts"), list(out)))
+
+    def set_contact_cell(self, cell):
+        """Contact-grid cell size in metres (0: the reference's)."""
+        self._check(self.lib.mcg_set_contact_cell(self.h, float(cell)), "mcg_set_contact_cell")
 
     def set_contact_skin(self, skin):
         """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""

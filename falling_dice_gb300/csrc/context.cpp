@@ -83,8 +83,9 @@ struct Pinned {
     void* base = nullptr;
     EvalOut* outs = nullptr;   // [I]
     double* tops = nullptr;    // [I]
-    SolveCtl* ctl = nullptr;   // [I]
-    double* rho = nullptr;     // [I * H]
+    SolveCtl* ctl = nullptr;   // [3 I]: the three uploads of a solver round (directions,
+                               // evaluation, accept) each have their own, so none is
+                               // rewritten before its copy has run
     double* dg = nullptr;      // [I]
     double* dots3 = nullptr;   // [3 I]
     double* pstats = nullptr;  // [6 I]
@@ -93,8 +94,8 @@ struct Pinned {
     void alloc(int I, int H) {
         release();
         const size_t Hn = size_t(std::max(H, 1));
-        const size_t bytes = I * sizeof(EvalOut) + I * sizeof(SolveCtl) +
-                             sizeof(double) * (I + I * Hn + I + 3 * I + 6 * I + 9 * (I + 1)) + 8 * 4 + 256;
+        const size_t bytes = I * sizeof(EvalOut) + 3 * I * sizeof(SolveCtl) +
+                             sizeof(double) * (I + I * Hn + I + 3 * I + 6 * I + 9 * (I + 1)) + 8 * 4 + 512;
         ck(cudaMallocHost(&base, bytes), "cudaMallocHost");
         std::memset(base, 0, bytes);
         char* p = static_cast<char*>(base);
@@ -104,9 +105,8 @@ struct Pinned {
             return r;
         };
         outs = reinterpret_cast<EvalOut*>(take(I * sizeof(EvalOut)));
-        ctl = reinterpret_cast<SolveCtl*>(take(I * sizeof(SolveCtl)));
+        ctl = reinterpret_cast<SolveCtl*>(take(3 * I * sizeof(SolveCtl)));
         tops = reinterpret_cast<double*>(take(I * sizeof(double)));
-        rho = reinterpret_cast<double*>(take(I * Hn * sizeof(double)));
         dg = reinterpret_cast<double*>(take(I * sizeof(double)));
         dots3 = reinterpret_cast<double*>(take(3 * I * sizeof(double)));
         pstats = reinterpret_cast<double*>(take(6 * I * sizeof(double)));
@@ -138,8 +138,8 @@ struct Minimizer {
     double cur_rms = 0, cur_max = 0, rms0 = 0, best_energy = 0, dg = 0, step = 1;
     int it = 0, bt = 0;
     bool retry = false;       // in the steepest-descent retry of this iteration
-    int m = 0, head = 0;      // history pairs held, oldest slot
-    int target = 0;           // slot of the pair of an accepted step
+    bool fresh = false;       // the trial is the first of a new direction (dg to be read)
+    bool accepted = false;    // the trial of this round passed the Armijo test
 };
 
 // One instance of the load/unload driver (Simulator::run, MC/src/sim.cpp:374-467).
@@ -218,6 +218,8 @@ struct mcg_ctx {
     double *d_rho = nullptr, *d_alpha = nullptr, *d_part = nullptr, *d_dg = nullptr, *d_dots3 = nullptr,
            *d_pstats = nullptr;
     SolveCtl* d_ctl = nullptr;
+    int2* d_hist = nullptr;       // per instance: history pairs held, oldest slot
+    uint32_t* d_reset = nullptr;  // per instance: the last direction fell back to steepest descent
     uint8_t* d_mask = nullptr;
     uint8_t *d_active = nullptr, *d_all = nullptr;  // instances evaluated / all instances
     std::vector<uint8_t> active;                    // host copy of d_active
@@ -483,9 +485,12 @@ struct mcg_ctx {
     }
 
     // ---- solver rounds --------------------------------------------------------------------
-    void upload_ctl() { h2d(d_ctl, hp.ctl, size_t(I), stream); }
-    void clear_ctl() {
-        for (int i = 0; i < I; i++) hp.ctl[i] = SolveCtl{0.0, 0, mins[size_t(i)].m, mins[size_t(i)].head, 0};
+    // Control records of stage k (0 directions, 1 evaluation, 2 accept) of a round.
+    SolveCtl* ctl_stage(int k) { return hp.ctl + size_t(k) * size_t(I); }
+    void upload_ctl(int k) { h2d(d_ctl, ctl_stage(k), size_t(I), stream); }
+    void clear_ctl(int k) {
+        SolveCtl* c = ctl_stage(k);
+        for (int i = 0; i < I; i++) c[i] = SolveCtl{0.0, 0, 0, 0, 0};
     }
     bool converged(const EvalOut& o, double rms, double mx, double rms0) const {
         if (cfg.relative_gradient_tolerance > 0)
@@ -525,114 +530,85 @@ struct mcg_ctx {
     }
 
     // One round for every instance with an unfinished minimization: directions, one
-    // evaluation each, decisions, accepted steps.  False when no instance had work.
+    // evaluation each, decisions, accepted steps.  The history (pairs, slots, rho) and the
+    // fallback to steepest descent when a direction does not descend are decided on the
+    // device (the reference's rules, sim.cpp:191, 205-206); the host reads back once per
+    // round: the evaluation's totals and each instance's dg.  False when no instance had
+    // work.
     bool minimize_round() {
         using M = Minimizer;
         const double mt = cfg.max_translation_step / cfg.translation_scale, mr = cfg.max_rotation_step;
-        // A. search directions: two-loop (sim.cpp:184-190), steepest descent when that is
-        //    not a descent direction (:191) or for the retry after a failed search (:193-196)
-        bool any_dir = false, any_sd = false;
-        clear_ctl();
-        int max_m = 0;
-        max_m = -1;
+        // A. search directions: two-loop (sim.cpp:184-190), or steepest descent for the retry
+        //    after a failed line search (:193-196)
+        bool any_dir = false, any_multi = false, any_sd = false;
+        clear_ctl(0);
+        SolveCtl* ca = ctl_stage(0);
         for (int i = 0; i < I; i++) {
-            const M& s = mins[size_t(i)];
+            M& s = mins[size_t(i)];
             if (s.phase == M::kDirection) {
-                if (fused[size_t(i)]) {
-                    hp.ctl[i].flags = kOpDirFused;
-                } else {
-                    hp.ctl[i].flags = kOpDirection;
-                    max_m = std::max(max_m, s.m);
-                }
+                ca[i].flags = fused[size_t(i)] ? kOpDirFused : kOpDirection;
+                any_multi |= !fused[size_t(i)];
                 any_dir = true;
+            } else if (s.phase == M::kSteepest) {
+                ca[i].flags = kOpSteepest;
+                any_sd = true;
+            } else {
+                continue;
             }
-            any_sd |= s.phase == M::kSteepest;
+            s.phase = M::kTrial;  // first trial of the new direction, step 1
+            s.step = 1.0;
+            s.bt = 0;
+            s.fresh = true;
         }
-        if (any_dir) {
-            upload_ctl();
-            h2d(d_rho, hp.rho, size_t(I) * size_t(std::max(H, 1)), stream);
-            bl_direction(topo, d_ctl, std::max(H, 1), max_m, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_alpha, d_part,
-                         d_dg, mt, mr, stream);
-            d2h(hp.dg, d_dg, size_t(I), stream);
-            sync();
-            for (int i = 0; i < I; i++) {
-                M& s = mins[size_t(i)];
-                if (s.phase != M::kDirection) continue;
-                s.dg = hp.dg[i];
-                if (!(s.dg < 0)) {  // not a descent direction: steepest descent (sim.cpp:191)
-                    s.m = 0;
-                    s.phase = M::kSteepest;
-                    any_sd = true;
-                } else {
-                    s.phase = M::kTrial;
-                    s.step = 1.0;
-                    s.bt = 0;
-                }
-            }
-        }
-        if (any_sd) {
-            clear_ctl();
-            for (int i = 0; i < I; i++)
-                if (mins[size_t(i)].phase == M::kSteepest) hp.ctl[i].flags = kOpSteepest;
-            upload_ctl();
-            bl_steepest(topo, d_ctl, d_p, d_g, d_part, d_dg, mt, mr, stream);
-            d2h(hp.dg, d_dg, size_t(I), stream);
-            sync();
-            for (int i = 0; i < I; i++) {
-                M& s = mins[size_t(i)];
-                if (s.phase != M::kSteepest) continue;
-                s.dg = hp.dg[i];
-                s.phase = M::kTrial;
-                s.step = 1.0;
-                s.bt = 0;
-            }
+        if (any_dir || any_sd) {
+            upload_ctl(0);
+            if (any_dir)
+                bl_direction(topo, d_ctl, d_hist, std::max(H, 1), any_multi, d_p, d_g, d_S, d_Y, 6LL * N, d_rho,
+                             d_alpha, d_part, d_dg, d_reset, mt, mr, stream);
+            if (any_sd) bl_steepest(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, stream);
         }
         // B. one evaluation per instance: the start point, a line-search candidate
         //    (sim.cpp:179) or the final state with trials (sim.cpp:210)
-        clear_ctl();
+        clear_ctl(1);
+        SolveCtl* cb1 = ctl_stage(1);
         bool any = false, trials = false;
+        std::vector<uint8_t> a(size_t(I), 0);
         for (int i = 0; i < I; i++) {
             const M& s = mins[size_t(i)];
-            SolveCtl& c = hp.ctl[i];
+            SolveCtl& c = cb1[i];
             switch (s.phase) {
                 case M::kStart:
-                    c.flags = (s.zero_first ? kOpZero : 0) | kOpEvalAtZ | kOpKeepBest;
-                    any = true;
+                    c.flags = kOpResetHistory | (s.zero_first ? kOpZero : 0) | kOpEvalAtZ | kOpKeepBest;
                     break;
                 case M::kTrial:
                     c.flags = kOpCandidate;
                     c.step = s.step;
-                    any = true;
                     break;
                 case M::kFinish:
                     c.flags = (s.restore ? kOpRestore : 0) | kOpEvalAtZ | kOpFinal;
-                    any = true;
                     trials = true;
                     break;
                 default:
-                    break;
+                    continue;
             }
-            if (s.phase == M::kStart || s.phase == M::kTrial || s.phase == M::kFinish) hp.tops[i] = s.top;
+            any = true;
+            a[size_t(i)] = 1;
+            hp.tops[i] = s.top;
         }
         if (!any) return false;
-        {
-            std::vector<uint8_t> a(size_t(I), 0);
-            for (int i = 0; i < I; i++) {
-                const M::Phase ph = mins[size_t(i)].phase;
-                a[size_t(i)] = ph == M::kStart || ph == M::kTrial || ph == M::kFinish;
-            }
-            set_active(a);
-        }
-        upload_ctl();
+        set_active(a);
+        upload_ctl(1);
         upload_tops();
-        bl_prepare(topo, d_ctl, d_z, d_best, d_zeval, d_p, d_zfinal, stream);
+        bl_prepare(topo, d_ctl, d_hist, d_z, d_best, d_zeval, d_p, d_zfinal, stream);
+        d2h(hp.dg, d_dg, size_t(I), stream);  // read back with the evaluation's totals
         const EvalOut* out = eval_read(d_zeval, trials, d_geval);
         // C. decisions (the reference's, per instance) and the vectors they imply
-        clear_ctl();
-        bool any_post = false, any_accept = false;
+        clear_ctl(2);
+        SolveCtl* cc = ctl_stage(2);
+        bool any_post = false;
         for (int i = 0; i < I; i++) {
             M& s = mins[size_t(i)];
-            SolveCtl& c = hp.ctl[i];
+            SolveCtl& c = cc[i];
             const EvalOut& o = out[i];
             switch (s.phase) {
                 case M::kStart:
@@ -647,17 +623,16 @@ struct mcg_ctx {
                     s.phase = M::kIterate;
                     break;
                 case M::kTrial: {
+                    if (s.fresh) {
+                        s.dg = hp.dg[i];
+                        s.fresh = false;
+                    }
                     s.cand = o;
                     s.st.backtracks++;
                     if (std::isfinite(o.energy) && o.energy <= s.cur.energy + cfg.armijo * s.step * s.dg) {
-                        c.flags = kOpAccept;
-                        if (H > 0) {
-                            s.target = s.m < H ? (s.head + s.m) % H : s.head;
-                            c.flags |= kOpPair;
-                            c.target = s.target;
-                        }
-                        if (o.energy < s.best_energy) c.flags |= kOpKeepBestAfter;
-                        any_post = any_accept = true;
+                        c.flags = kOpAccept | (H > 0 ? kOpPair : 0) | (o.energy < s.best_energy ? kOpKeepBestAfter : 0);
+                        any_post = true;
+                        s.accepted = true;
                         break;
                     }
                     s.step *= .5;
@@ -666,7 +641,6 @@ struct mcg_ctx {
                     // line search failed (sim.cpp:193-209)
                     if (!s.retry) {
                         s.retry = true;
-                        s.m = 0;
                         s.phase = M::kSteepest;
                     } else {
                         s.phase = M::kFinish;
@@ -689,27 +663,15 @@ struct mcg_ctx {
             }
         }
         if (any_post) {
-            upload_ctl();
-            bl_accept(topo, d_ctl, d_z, d_g, d_zeval, d_geval, d_S, d_Y, 6LL * N, d_best, d_part, d_dots3, stream);
-            if (any_accept) {
-                d2h(hp.dots3, d_dots3, 3 * size_t(I), stream);
-                sync();
-            }
+            upload_ctl(2);
+            bl_accept(topo, d_ctl, d_hist, H, d_z, d_g, d_zeval, d_geval, d_S, d_Y, 6LL * N, d_best, d_rho, d_part,
+                      d_dots3, stream);
         }
-        // accepted steps: curvature pair (sim.cpp:205-206), current point, best point
+        // accepted steps: current point, best point (the curvature pair is the device's)
         for (int i = 0; i < I; i++) {
             M& s = mins[size_t(i)];
-            if (s.phase == M::kTrial && (hp.ctl[i].flags & kOpAccept)) {
-                if (H > 0) {
-                    const double sy = hp.dots3[3 * i], ss = hp.dots3[3 * i + 1], yy = hp.dots3[3 * i + 2];
-                    if (sy > 1e-12 * std::sqrt(std::max(1e-30, ss * yy))) {
-                        hp.rho[size_t(i) * H + s.target] = 1 / sy;
-                        if (s.m == H) s.head = (s.head + 1) % H;
-                        else s.m++;
-                    } else {
-                        s.m = 0;
-                    }
-                }
+            if (s.phase == M::kTrial && s.accepted) {
+                s.accepted = false;
                 s.cur = s.cand;
                 s.cur_rms = s.cand.rms;
                 s.cur_max = s.cand.gmax;
@@ -1381,6 +1343,11 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->d_dots3 = Q.get<double>(3 * size_t(I));
     c->d_pstats = Q.get<double>(6 * size_t(I));
     c->d_ctl = Q.get<SolveCtl>(size_t(I));
+    c->d_hist = Q.get<int2>(size_t(I));
+    c->d_reset = Q.get<uint32_t>(size_t(I));
+    ck(cudaMemsetAsync(c->d_hist, 0, size_t(I) * sizeof(int2), s), "memset");
+    ck(cudaMemsetAsync(c->d_rho, 0, size_t(I) * Hs * sizeof(double), s), "memset");
+    ck(cudaMemsetAsync(c->d_reset, 0, size_t(I) * sizeof(uint32_t), s), "memset");
     c->d_mask = Q.get<uint8_t>(size_t(I));
     c->mins.assign(size_t(I), Minimizer{});
     c->fused.assign(size_t(I), 0);
@@ -1805,6 +1772,16 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
         for (int k = 0; k < 5; k++) out5[k] = c->hp.u32[k];
+    });
+}
+
+int mcg_set_contact_cell(mcg_ctx* c, double cell) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!(cell >= 0) || cell > 1e3) throw Fail(MCG_ERR_INVALID, "cell must be a length >= 0 (m)");
+        c->broad_cell = cell > 0 ? cell : std::max(2.8 * c->jr, .72 * c->cfg.cell_size);
+        c->sync();
+        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.region);
     });
 }
 

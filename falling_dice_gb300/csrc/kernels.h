@@ -293,32 +293,39 @@ enum SolveOp : int {
     kOpAccept = 512,       // s, y, curvature dots, z = zeval, g = geval
     kOpPair = 1024,        // with kOpAccept: store (s, y) in history slot `target`
     kOpKeepBestAfter = 2048, // with kOpAccept: best = the accepted z
-    kOpDirFused = 4096       // as kOpDirection, by one CTA for the instance (small instances)
+    kOpDirFused = 4096,      // as kOpDirection, by one CTA for the instance (small instances)
+    kOpResetHistory = 8192   // the history starts empty (a new minimization)
 };
-// Per-instance solver control, written by the host before each step.
+// Per-instance solver control, written by the host before each step.  The history state
+// (pairs held m, oldest slot head) lives on the device (int2 per instance) and is filled in
+// by the kernels.
 struct SolveCtl {
     double step;       // line-search step of the candidate
     int flags;         // SolveOp bits
-    int m, head;       // history pairs held, ring slot of the oldest
-    int target;        // slot the next accepted pair goes to
+    int m, head;       // (device history, loaded by the kernels)
+    int pad_;
 };
 size_t lbfgs_part_doubles(int n_nblk);
 // Largest instance (in node blocks) whose direction one CTA computes (kOpDirFused).
 int fused_direction_limit();
-// Two-loop recursion (sim.cpp:184-187) into p for the kOpDirection and kOpDirFused
-// instances, then p = clamp(lock(-p)) and dg[i] = <g, p>.  History: H slots of `stride`
-// doubles; rho and alpha [I * H].  max_m < 0: no kOpDirection instance (one launch).
-void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
+// Two-loop recursion (sim.cpp:184-187) into p for the kOpDirFused (one CTA each) and, with
+// multi, the kOpDirection instances; then p = clamp(lock(-p)) and dg[i] = <g, p>; where
+// dg >= 0, steepest descent with the history cleared and reset[i] = 1 (sim.cpp:191).
+// History: H slots of `stride` doubles, state hist[I], rho and alpha [I * H].
+void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s);
-// p = clamp(lock(-g)) and dg[i] = <g, p> for the kOpSteepest instances (sim.cpp:191, 195).
-void bl_steepest(const DevTopo& t, const SolveCtl* ctl, double* p, const double* g, double* part, double* dg,
-                 double mt, double mr, cudaStream_t s);
-// kOpZero / kOpRestore / kOpKeepBest / kOpCandidate / kOpEvalAtZ / kOpFinal
-void bl_prepare(const DevTopo& t, const SolveCtl* ctl, double* z, double* best, double* zeval, const double* p,
-                double* zfinal, cudaStream_t s);
-// kOpTakeGrad / kOpAccept (+kOpPair, kOpKeepBestAfter); out3[3 i..] = <s, y>, <s, s>, <y, y>
-void bl_accept(const DevTopo& t, const SolveCtl* ctl, double* z, double* g, const double* zeval, const double* geval,
-               double* S, double* Y, long long stride, double* best, double* part, double* out3, cudaStream_t s);
+                  double* dg, uint32_t* reset, double mt, double mr, cudaStream_t s);
+// The steepest-descent retry for the kOpSteepest instances: history cleared,
+// p = clamp(lock(-g)), dg[i] = <g, p> (sim.cpp:193-196).
+void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
+                 double* dg, double mt, double mr, cudaStream_t s);
+// kOpResetHistory / kOpZero / kOpRestore / kOpKeepBest / kOpCandidate / kOpEvalAtZ / kOpFinal
+void bl_prepare(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* z, double* best, double* zeval,
+                const double* p, double* zfinal, cudaStream_t s);
+// kOpTakeGrad / kOpAccept (+kOpPair, kOpKeepBestAfter); out3[3 i..] = <s, y>, <s, s>, <y, y>;
+// then the history update of the accepted instances (sim.cpp:205-206).
+void bl_accept(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* z, double* g, const double* zeval,
+               const double* geval, double* S, double* Y, long long stride, double* best, double* rho, double* part,
+               double* out3, cudaStream_t s);
 
 }  // namespace mcg

@@ -18,12 +18,22 @@ namespace mcg {
 
 namespace {
 
-__device__ __forceinline__ const double* hist(const double* base, long long stride, int slot) {
+__device__ __forceinline__ const double* hist_slot(const double* base, long long stride, int slot) {
     return base + stride * slot;
 }
 
 // Slot of the h-th oldest history pair of an instance.
 __device__ __forceinline__ int ring_slot(const SolveCtl& c, int H, int h) { return (c.head + h) % H; }
+
+// An instance's control record with its history state (pairs held, oldest slot), which
+// lives on the device: the solver kernels update it themselves.
+__device__ __forceinline__ SolveCtl load_ctl(const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int inst) {
+    SolveCtl c = ctl[inst];
+    const int2 h = hist[inst];
+    c.m = h.x;
+    c.head = h.y;
+    return c;
+}
 
 // One instance's sum of its block partials part[k * nblk + b], b in its node-block range,
 // for k < K (one block per instance; fixed order).
@@ -53,16 +63,16 @@ __device__ __forceinline__ double dot6(const double* a, const double* b) {
 // Partial <S[slot], p> (loop 1, newest first: h = m - 1 - j) or <Y[slot], p> (loop 2,
 // oldest first: h = j) for the instances computing a direction with j < m.
 template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_dot(DevTopo t, const SolveCtl* __restrict__ ctl, int H, int j,
+__global__ void __launch_bounds__(kBlock) k_tl_dot(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H, int j,
                                                    const double* __restrict__ p, const double* __restrict__ S,
                                                    const double* __restrict__ Y, long long stride,
                                                    double* __restrict__ part) {
     __shared__ double sm[kBlock / 32];
     const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = ctl[mp.inst];
+    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
     const int slot = ring_slot(c, H, LOOP == 1 ? c.m - 1 - j : j);
-    const double* v = hist(LOOP == 1 ? S : Y, stride, slot);
+    const double* v = hist_slot(LOOP == 1 ? S : Y, stride, slot);
     double acc[1] = {0};
     if (mp.valid) acc[0] = dot6(v + 6 * size_t(mp.i), p + 6 * size_t(mp.i));
     block_sum<1>(acc, sm);
@@ -72,7 +82,7 @@ __global__ void __launch_bounds__(kBlock) k_tl_dot(DevTopo t, const SolveCtl* __
 // Loop 1: alpha = rho <s, p> (kept), p -= alpha y.  Loop 2: beta = rho <y, p>, p += s (alpha - beta).
 // Every block of an instance sums the instance's partials itself (same order in each).
 template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl* __restrict__ ctl, int H, int j,
+__global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H, int j,
                                                       double* __restrict__ p, const double* __restrict__ S,
                                                       const double* __restrict__ Y, long long stride,
                                                       const double* __restrict__ rho, double* __restrict__ alpha,
@@ -80,7 +90,7 @@ __global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl*
     __shared__ double sm[kBlock / 32];
     __shared__ double coef;
     const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = ctl[mp.inst];
+    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection) || j >= c.m) return;
     const int h = LOOP == 1 ? c.m - 1 - j : j;
     const int slot = ring_slot(c, H, h);
@@ -100,11 +110,11 @@ __global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl*
     const double k = coef;
     double* pi = p + 6 * size_t(mp.i);
     if (LOOP == 1) {
-        const double* y = hist(Y, stride, slot) + 6 * size_t(mp.i);
+        const double* y = hist_slot(Y, stride, slot) + 6 * size_t(mp.i);
 #pragma unroll
         for (int d = 0; d < 6; d++) pi[d] -= k * y[d];
     } else {
-        const double* s = hist(S, stride, slot) + 6 * size_t(mp.i);
+        const double* s = hist_slot(S, stride, slot) + 6 * size_t(mp.i);
 #pragma unroll
         for (int d = 0; d < 6; d++) pi[d] += s[d] * k;
     }
@@ -112,13 +122,13 @@ __global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl*
 
 // Partials of <s, y> and <y, y> of the newest pair (for H0) and the copy p = g that starts
 // the recursion.
-__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, int H,
+__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
                                                      double* __restrict__ p, const double* __restrict__ g,
                                                      const double* __restrict__ S, const double* __restrict__ Y,
                                                      long long stride, double* __restrict__ part) {
     __shared__ double sm[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = ctl[mp.inst];
+    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (mp.valid)
 #pragma unroll
@@ -127,8 +137,8 @@ __global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* 
     const int slot = ring_slot(c, H, c.m - 1);
     double acc[2] = {0, 0};
     if (mp.valid) {
-        const double* s = hist(S, stride, slot) + 6 * size_t(mp.i);
-        const double* y = hist(Y, stride, slot) + 6 * size_t(mp.i);
+        const double* s = hist_slot(S, stride, slot) + 6 * size_t(mp.i);
+        const double* y = hist_slot(Y, stride, slot) + 6 * size_t(mp.i);
         acc[0] = dot6(s, y);
         acc[1] = dot6(y, y);
     }
@@ -140,12 +150,12 @@ __global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* 
 }
 
 // p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186).
-__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl,
+__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
                                                      double* __restrict__ p, const double* __restrict__ part) {
     __shared__ double sm[2 * (kBlock / 32)];
     __shared__ double h0;
     const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = ctl[mp.inst];
+    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (c.m > 0) {
         double acc[2];
@@ -248,14 +258,14 @@ __global__ void __launch_bounds__(kBlock) k_prepare(DevTopo t, const SolveCtl* _
 // for accepted trials (kOpAccept, sim.cpp:205-206) s = zeval - z, y = geval - g into the
 // history slot `target` (kOpPair), the partials of <s, y>, <s, s>, <y, y>, then z = zeval,
 // g = geval; best = z afterwards when kOpKeepBestAfter.
-__global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __restrict__ ctl,
-                                                   double* __restrict__ z, double* __restrict__ g,
+__global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
+                                                   int H, double* __restrict__ z, double* __restrict__ g,
                                                    const double* __restrict__ zeval, const double* __restrict__ geval,
                                                    double* __restrict__ S, double* __restrict__ Y, long long stride,
                                                    double* __restrict__ best, double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = ctl[mp.inst];
+    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & (kOpTakeGrad | kOpAccept))) return;
     const size_t b = 6 * size_t(mp.i);
     if (c.flags & kOpTakeGrad) {
@@ -273,8 +283,9 @@ __global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __
             yv[k] = geval[b + k] - g[b + k];
         }
         if (c.flags & kOpPair) {
-            double* s = S + stride * c.target + b;
-            double* y = Y + stride * c.target + b;
+            const int target = c.m < H ? (c.head + c.m) % H : c.head;
+            double* s = S + stride * target + b;
+            double* y = Y + stride * target + b;
 #pragma unroll
             for (int k = 0; k < 6; k++) {
                 s[k] = sv[k];
@@ -327,7 +338,7 @@ __device__ __forceinline__ void chunk_sum(const double (*part)[kFuseChunks], int
     block_sum<K>(acc, sm);
 }
 
-__global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const SolveCtl* __restrict__ ctl, int H,
+__global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
                                                             double* __restrict__ p, const double* __restrict__ g,
                                                             const double* __restrict__ S, const double* __restrict__ Y,
                                                             long long stride, const double* __restrict__ rho,
@@ -337,7 +348,7 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
     __shared__ double alpha[64];
     __shared__ double coef;
     const int inst = blockIdx.x;
-    const SolveCtl c = ctl[inst];
+    const SolveCtl c = load_ctl(ctl, hist, inst);
     if (!(c.flags & kOpDirFused)) return;
     const int4 r = t.irange[inst];
     const int nchunk = r.y - r.x;
@@ -351,8 +362,8 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
             const int slot = ring_slot(c, H, c.m - 1);
             double acc[2] = {0, 0};
             if (int(threadIdx.x) < q.y) {
-                const double* sv = hist(S, stride, slot) + 6 * size_t(q.x + threadIdx.x);
-                const double* yv = hist(Y, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                const double* sv = hist_slot(S, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                const double* yv = hist_slot(Y, stride, slot) + 6 * size_t(q.x + threadIdx.x);
                 acc[0] = dot6(sv, yv);
                 acc[1] = dot6(yv, yv);
             }
@@ -372,7 +383,7 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
         const int h = c.m - 1 - j, slot = ring_slot(c, H, h);
         for (int b = 0; b < nchunk; b++) {
             const int4 q = t.nblk[r.x + b];
-            const double v = chunk_dot(hist(S, stride, slot), p, q.x, q.y, sm);
+            const double v = chunk_dot(hist_slot(S, stride, slot), p, q.x, q.y, sm);
             if (threadIdx.x == 0) part[0][b] = v;
         }
         __syncthreads();
@@ -384,7 +395,7 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
         }
         __syncthreads();
         const double k = coef;
-        const double* yv = hist(Y, stride, slot);
+        const double* yv = hist_slot(Y, stride, slot);
         for (int b = 0; b < nchunk; b++) {
             const int4 q = t.nblk[r.x + b];
             if (int(threadIdx.x) < q.y)
@@ -415,7 +426,7 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
         const int slot = ring_slot(c, H, j);
         for (int b = 0; b < nchunk; b++) {
             const int4 q = t.nblk[r.x + b];
-            const double v = chunk_dot(hist(Y, stride, slot), p, q.x, q.y, sm);
+            const double v = chunk_dot(hist_slot(Y, stride, slot), p, q.x, q.y, sm);
             if (threadIdx.x == 0) part[0][b] = v;
         }
         __syncthreads();
@@ -424,7 +435,7 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
         if (threadIdx.x == 0) coef = alpha[j] - rho[size_t(inst) * H + slot] * acc[0];
         __syncthreads();
         const double k = coef;
-        const double* sv = hist(S, stride, slot);
+        const double* sv = hist_slot(S, stride, slot);
         for (int b = 0; b < nchunk; b++) {
             const int4 q = t.nblk[r.x + b];
             if (int(threadIdx.x) < q.y)
@@ -472,47 +483,144 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
     if (threadIdx.x == 0) dg[inst] = acc[0];
 }
 
+// ---- decisions the device takes itself ------------------------------------------------------
+// Not a descent direction (sim.cpp:191): steepest descent instead.  For the instances that
+// computed a direction and found dg >= 0: p = clamp(lock(-g)) and the partial of <g, p>.
+__global__ void __launch_bounds__(kBlock) k_descent_fix(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                        const double* __restrict__ dg, double* __restrict__ p,
+                                                        const double* __restrict__ g, double mt, double mr,
+                                                        double* __restrict__ part) {
+    __shared__ double sm[kBlock / 32];
+    const MapPos mp = map_pos(t.nblk);
+    if (!(ctl[mp.inst].flags & (kOpDirection | kOpDirFused)) || dg[mp.inst] < 0) return;  // block-uniform
+    double acc[1] = {0};
+    if (mp.valid) {
+        const size_t b = 6 * size_t(mp.i);
+        const uint8_t* lk = t.locked + b;
+        double v[6];
+#pragma unroll
+        for (int k = 0; k < 6; k++) v[k] = lk[k] ? 0.0 : -g[b + k];
+        const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (lt > mt) {
+            const double f = mt / lt;
+            v[0] *= f; v[1] *= f; v[2] *= f;
+        }
+        const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+        if (lr > mr) {
+            const double f = mr / lr;
+            v[3] *= f; v[4] *= f; v[5] *= f;
+        }
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            v[k] = lk[k] ? 0.0 : v[k];
+            p[b + k] = v[k];
+        }
+        acc[0] = dot6(g + b, v);
+    }
+    block_sum<1>(acc, sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+}
+// ... and per instance: the new dg, history cleared (m = 0), reset[i] = 1 (0 otherwise).
+__global__ void __launch_bounds__(kBlock) k_descent_final(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                          const double* __restrict__ part, double* __restrict__ dg,
+                                                          int2* __restrict__ hist, uint32_t* __restrict__ reset) {
+    __shared__ double sm[kBlock / 32];
+    const int inst = blockIdx.x;
+    if (!(ctl[inst].flags & (kOpDirection | kOpDirFused))) return;
+    if (dg[inst] < 0) {
+        if (threadIdx.x == 0) reset[inst] = 0;
+        return;
+    }
+    double acc[1];
+    instance_sum<1>(t, part, inst, acc, sm);
+    if (threadIdx.x == 0) {
+        dg[inst] = acc[0];
+        hist[inst].x = 0;
+        reset[inst] = 1;
+    }
+}
+// The steepest-descent retry (sim.cpp:193-196) starts with an empty history.
+__global__ void k_clear_history(int I, const SolveCtl* __restrict__ ctl, int bits, int2* __restrict__ hist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < I && (ctl[i].flags & bits)) hist[i] = make_int2(0, 0);
+}
+__global__ void k_clear_history_m(int I, const SolveCtl* __restrict__ ctl, int bits, int2* __restrict__ hist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < I && (ctl[i].flags & bits)) hist[i].x = 0;
+}
+// History after an accepted step (sim.cpp:205-206): keep the pair when
+// s.y > 1e-12 sqrt(max(1e-30, s.s y.y)) (rho = 1 / s.y in its slot), else clear the history.
+__global__ void k_history_update(int I, int H, const SolveCtl* __restrict__ ctl, const double* __restrict__ dots3,
+                                 int2* __restrict__ hist, double* __restrict__ rho) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= I || !(ctl[i].flags & kOpAccept) || H <= 0) return;
+    const double sy = dots3[3 * i], ss = dots3[3 * i + 1], yy = dots3[3 * i + 2];
+    int2 h = hist[i];
+    if (sy > 1e-12 * sqrt(fmax(1e-30, ss * yy))) {
+        const int target = h.x < H ? (h.y + h.x) % H : h.y;
+        rho[size_t(i) * H + target] = 1 / sy;
+        if (h.x == H) h.y = (h.y + 1) % H;
+        else h.x++;
+    } else {
+        h.x = 0;
+    }
+    hist[i] = h;
+}
+
 }  // namespace
 
 size_t lbfgs_part_doubles(int n_nblk) { return 3 * size_t(n_nblk) + 8; }
 
 int fused_direction_limit() { return kFuseChunks; }
 
-void bl_direction(const DevTopo& t, const SolveCtl* ctl, int H, int max_m, double* p, const double* g,
+void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s) {
+                  double* dg, uint32_t* reset, double mt, double mr, cudaStream_t s) {
     const int nb = t.n_nblk;
-    (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
-    if (max_m < 0) return;  // no instance on the multi-launch path
-    (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, H, p, g, S, Y, stride, part + 2 * size_t(nb)), note_launches(1));
-    for (int j = 0; j < max_m; j++) {
-        (k_tl_dot<1><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, part), note_launches(1));
-        (k_tl_update<1><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, rho, alpha, part), note_launches(1));
+    (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
+    if (multi) {
+        (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, part + 2 * size_t(nb)),
+         note_launches(1));
+        for (int j = 0; j < H; j++) {
+            (k_tl_dot<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, part), note_launches(1));
+            (k_tl_update<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, part),
+             note_launches(1));
+        }
+        (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, hist, p, part + 2 * size_t(nb)), note_launches(1));
+        for (int j = 0; j < H; j++) {
+            (k_tl_dot<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, part), note_launches(1));
+            (k_tl_update<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, part),
+             note_launches(1));
+        }
+        (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
+        (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
     }
-    (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, p, part + 2 * size_t(nb)), note_launches(1));
-    for (int j = 0; j < max_m; j++) {
-        (k_tl_dot<2><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, part), note_launches(1));
-        (k_tl_update<2><<<nb, kBlock, 0, s>>>(t, ctl, H, j, p, S, Y, stride, rho, alpha, part), note_launches(1));
-    }
-    (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
-    (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
+    // not a descent direction: steepest descent, history cleared (sim.cpp:191)
+    (k_descent_fix<<<nb, kBlock, 0, s>>>(t, ctl, dg, p, g, mt, mr, part), note_launches(1));
+    (k_descent_final<<<t.I, kBlock, 0, s>>>(t, ctl, part, dg, hist, reset), note_launches(1));
 }
 
-void bl_steepest(const DevTopo& t, const SolveCtl* ctl, double* p, const double* g, double* part, double* dg,
-                 double mt, double mr, cudaStream_t s) {
+void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
+                 double* dg, double mt, double mr, cudaStream_t s) {
+    (k_clear_history_m<<<(t.I + kBlock - 1) / kBlock, kBlock, 0, s>>>(t.I, ctl, kOpSteepest, hist), note_launches(1));
     (k_finish<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, kOpSteepest, p, g, g, mt, mr, part), note_launches(1));
     (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpSteepest, part, dg), note_launches(1));
 }
 
-void bl_prepare(const DevTopo& t, const SolveCtl* ctl, double* z, double* best, double* zeval, const double* p,
-                double* zfinal, cudaStream_t s) {
+void bl_prepare(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* z, double* best, double* zeval,
+                const double* p, double* zfinal, cudaStream_t s) {
+    (k_clear_history<<<(t.I + kBlock - 1) / kBlock, kBlock, 0, s>>>(t.I, ctl, kOpResetHistory, hist),
+     note_launches(1));
     (k_prepare<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, z, best, zeval, p, zfinal), note_launches(1));
 }
 
-void bl_accept(const DevTopo& t, const SolveCtl* ctl, double* z, double* g, const double* zeval, const double* geval,
-               double* S, double* Y, long long stride, double* best, double* part, double* out3, cudaStream_t s) {
-    (k_accept<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, z, g, zeval, geval, S, Y, stride, best, part), note_launches(1));
+void bl_accept(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* z, double* g, const double* zeval,
+               const double* geval, double* S, double* Y, long long stride, double* best, double* rho, double* part,
+               double* out3, cudaStream_t s) {
+    (k_accept<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, hist, H, z, g, zeval, geval, S, Y, stride, best, part),
+     note_launches(1));
     (k_inst_final<3><<<t.I, kBlock, 0, s>>>(t, ctl, kOpAccept, part, out3), note_launches(1));
+    (k_history_update<<<(t.I + kBlock - 1) / kBlock, kBlock, 0, s>>>(t.I, H, ctl, out3, hist, rho), note_launches(1));
 }
 
 }  // namespace mcg

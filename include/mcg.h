@@ -271,6 +271,11 @@ int mcg_batch_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* co
  * the default after mcg_upload_topology is cell_size / 32. */
 int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
 
+/* Cell size of the self-contact grid in metres (no reference counterpart; 0: the
+ * reference's max(2.8 joint radius, 0.72 cell_size)).  Pair sets and results do not depend
+ * on it: a pair is examined once whatever the grid, and the narrow phase decides. */
+int mcg_set_contact_cell(mcg_ctx* ctx, double cell);
+
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
  * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept
  * by the distance filter, contacts}. */
