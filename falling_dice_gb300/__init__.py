@@ -50,6 +50,7 @@ SIGNATURES = {
     "mcg_set_contact_skin": (C.c_int, [_P, C.c_double]),
     "mcg_contact_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_set_contact_cell": (C.c_int, [_P, C.c_double]),
+    "mcg_autotune": (C.c_int, [_P, _d, _d, C.c_int32, C.POINTER(abi.Tuning)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -259,6 +260,22 @@ class Solver:
     def set_contact_cell(self, cell):
         """Contact-grid cell size in metres (0: the reference's)."""
         self._check(self.lib.mcg_set_contact_cell(self.h, float(cell)), "mcg_set_contact_cell")
+
+    def autotune(self, z=None, tops=None, reps=3):
+        """Times the broad-phase shape candidates (grid cell, pair-enumeration grid) at z
+        (None: 0) and platen heights tops (None: each lattice's top0), keeps the fastest and
+        returns the choice; the candidates must agree bit for bit (mcg_autotune)."""
+        zp = None if z is None else np.ascontiguousarray(z, np.float64)
+        if zp is not None and zp.size != 6 * self.n_nodes:
+            raise ValueError("z must hold 6 values per node")
+        tp = None if tops is None else np.ascontiguousarray(np.atleast_1d(tops), np.float64)
+        if tp is not None and tp.size != getattr(self, "count", 1):
+            raise ValueError("tops must hold one platen height per lattice")
+        t = abi.Tuning()
+        self._check(self.lib.mcg_autotune(self.h, _ptr(zp), _ptr(tp), int(reps), C.byref(t)),
+                    "mcg_autotune")
+        return {"cell": t.cell, "pair_blocks": t.pair_blocks, "tried": t.tried,
+                "ms_chosen": t.ms_chosen, "ms_default": t.ms_default}
 
     def set_contact_skin(self, skin):
         """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""

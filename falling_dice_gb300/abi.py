@@ -14,6 +14,7 @@ MCG_ERR_STATE = 4
 MCG_ERR_EQUILIBRIUM = 5
 MCG_ERR_CAPACITY = 6
 MCG_ERR_TIMEOUT = 7
+MCG_ERR_MISMATCH = 8
 
 MCG_FP64 = 0
 MCG_MIXED = 1
@@ -124,6 +125,11 @@ class Diag(C.Structure):
     def as_dict(self):
         return {k: getattr(self, k) for k in
                 ("elastic", "plastic", "contact", "reaction", "max_pen", "contacts")}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("cell", C.c_double), ("pair_blocks", C.c_int32), ("tried", C.c_int32),
+                ("ms_chosen", C.c_double), ("ms_default", C.c_double)]
 
 
 class OptStats(C.Structure):

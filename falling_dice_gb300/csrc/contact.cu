@@ -38,7 +38,6 @@ constexpr float kBoxQuanta = 32000.f;   // quantization steps across the grid ex
 constexpr uint32_t kBoxMax = 32767u;    // 15-bit box coordinates
 constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
-constexpr int kWarpCap = 64;            // bins up to this size are staged in shared memory
 constexpr int kPairWarps = kBlock / 32;
 constexpr int kStreamBlocks = 8 * 152;
 
@@ -395,18 +394,6 @@ __global__ void __launch_bounds__(kBlock) k_scatter(int S, const uint32_t* __res
     for (uint32_t o = offset[s]; o < offset[s + 1]; o++) sorted[bin_start[ekey[o]] + erank[o]] = uint32_t(s);
 }
 
-// Row and column of pair p in the strict upper triangle of an n x n matrix, pairs (i, j),
-// i < j, numbered row by row.
-__device__ __forceinline__ void pair_index(int n, int p, int& i, int& j) {
-    const float fn = float(2 * n - 1);
-    int r = int((fn - sqrtf(fmaxf(fn * fn - 8.f * float(p), 0.f))) * 0.5f);
-    r = max(0, min(r, n - 2));
-    while (r > 0 && r * (2 * n - r - 1) / 2 > p) r--;
-    while (r < n - 2 && (r + 1) * (2 * n - r - 2) / 2 <= p) r++;
-    i = r;
-    j = p - r * (2 * n - r - 1) / 2 + r + 1;
-}
-
 // One shape as the pair test sees it inside one bin: id with the first-cell flags in the
 // top three bits (bit d set when the shape's first cell on axis d is the bin's cell), the
 // quantized box words and the shape's nodes (a joint's node twice).
@@ -446,6 +433,21 @@ __device__ __forceinline__ PairRec shfl_rec(const PairRec& v, int src) {
 
 constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 
+// Every unordered pair of the records held by lanes 0 .. m-1 (m <= 32), by rotation: in
+// round k lane i meets lane (i + k) mod m, k = 1 .. m/2 (the last round of an even m only
+// from the lower half), the partner's record arriving by six register shuffles.
+template <typename Emit>
+__device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane, Emit emit) {
+    const int half = m >> 1;
+    int src = lane;
+    for (int k = 1; k <= half; k++) {
+        src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
+        const PairRec o = shfl_rec(me, lane < m ? src : lane);
+        const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
+        emit(active && pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
+    }
+}
+
 // Candidate pairs of every occupied bin.  Warp w of the fixed grid takes the occupied bins
 // occ[w], occ[w + W], ... in order and appends their candidate pairs (lower shape, higher
 // shape) to its own region cand[w R .. (w + 1) R), so the candidate list -- regions in warp
@@ -453,11 +455,10 @@ constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 // pass.  A region that fills up flags kOverCandidates; wcount[w] keeps the full count so the
 // host can size R.  Enumeration inside a bin:
 //   n <= 32  the bin's shapes are sorted across the warp's lanes (bitonic, by shape id)
-//            and every unordered pair is visited by rotation: in round k lane i meets
-//            lane (i + k) mod n, k = 1 .. n/2 (the last round of an even n only from the
-//            lower half), the partner's record arriving by six register shuffles;
-//   n <= 64  the sorted records are staged in shared memory and the pairs enumerated by
-//            index;
+//            and every unordered pair is visited by rotation (rotate_pairs);
+//   n <= 64  sorted as 64 keys, two per lane (lane i holds ranks i and 32 + i); pairs of
+//            the lower 32 by rotation, each upper record broadcast to the 32 lower ones,
+//            pairs of the upper records by rotation;
 //   larger   sorted through a scratch copy, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count,
@@ -467,14 +468,13 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                                                       const uint4* __restrict__ rec, int region,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
                                                       uint32_t* __restrict__ wcap, uint32_t* __restrict__ flags) {
-    __shared__ PairRec sh[kPairWarps][kWarpCap];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    const long long nocc = *nocc_p;
-    const long long gw = (long long)blockIdx.x * kPairWarps + w;
-    const long long warps = (long long)gridDim.x * kPairWarps;
-    uint2* mine = cand + gw * region;
+    const uint32_t nocc = *nocc_p;
+    const uint32_t gw = blockIdx.x * kPairWarps + w;
+    const uint32_t warps = gridDim.x * kPairWarps;
+    uint2* mine = cand + size_t(gw) * size_t(region);
     uint32_t out = 0;
     auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
         const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         }
         out += __popc(m);
     };
-    for (long long jb = gw; jb < nocc; jb += warps) {
+    for (uint32_t jb = gw; jb < nocc; jb += warps) {
         const uint32_t b = occ[jb];
         const int n = int(bin_count[b]);
         const uint32_t start = bin_start[b];
@@ -500,43 +500,36 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                 }
             PairRec me{};
             if (lane < n) me = load_rec(t, v, rec, ccp);
-            const int half = n >> 1;
-            int src = lane;
-            for (int k = 1; k <= half; k++) {
-                src = src + 1 < n ? src + 1 : 0;  // (lane + k) mod n for lanes below n
-                const PairRec o = shfl_rec(me, lane < n ? src : lane);
-                const bool active = lane < n && !((n & 1) == 0 && k == half && lane >= half);
-                emit(active && pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
-            }
-        } else if (n <= kWarpCap) {
-            const uint32_t v0 = sorted[start + lane];
-            const uint32_t v1 = lane + 32 < n ? sorted[start + 32 + lane] : 0xffffffffu;
-            int r0 = 0, r1 = 0;
-            for (int q = 0; q < 32; q++) {
-                const uint32_t u0 = __shfl_sync(0xffffffffu, v0, q), u1 = __shfl_sync(0xffffffffu, v1, q);
-                r0 += (u0 < v0) + (u1 < v0);
-                r1 += (u0 < v1) + (u1 < v1);
-            }
-            __syncwarp();
-            sh[w][r0] = load_rec(t, v0, rec, ccp);
-            if (v1 != 0xffffffffu) sh[w][r1] = load_rec(t, v1, rec, ccp);
-            __syncwarp();
-            const int P = n * (n - 1) / 2;
-            for (int base = 0; base < P; base += 32) {
-                const int pidx = base + lane;
-                bool hit = false;
-                uint32_t sa = 0, sb = 0;
-                if (pidx < P) {
-                    int i, j;
-                    pair_index(n, pidx, i, j);
-                    const PairRec A = sh[w][i], B = sh[w][j];
-                    hit = pair_test(A, B);
-                    sa = A.id & kIdMask;
-                    sb = B.id & kIdMask;
+            rotate_pairs(me, n, lane, emit);
+        } else if (n <= 64) {
+            uint32_t v0 = sorted[start + lane];
+            uint32_t v1 = lane + 32 < n ? sorted[start + 32 + lane] : 0xffffffffu;
+            // bitonic sort of the 64 keys, key e = lane + 32 h in register h, ascending
+            for (int k = 2; k <= 64; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    if (j == 32) {  // partners in the same lane (k = 64: ascending)
+                        const uint32_t lo = min(v0, v1), hi = max(v0, v1);
+                        v0 = lo;
+                        v1 = hi;
+                    } else {
+                        const uint32_t o0 = __shfl_xor_sync(0xffffffffu, v0, j);
+                        const uint32_t o1 = __shfl_xor_sync(0xffffffffu, v1, j);
+                        const bool lower = (lane & j) == 0;
+                        const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
+                        v0 = (lower == up0) ? min(v0, o0) : max(v0, o0);
+                        v1 = (lower == up1) ? min(v1, o1) : max(v1, o1);
+                    }
                 }
-                emit(hit, sa, sb);
+            const int m = n - 32;
+            const PairRec lo = load_rec(t, v0, rec, ccp);
+            PairRec up{};
+            if (lane < m) up = load_rec(t, v1, rec, ccp);
+            rotate_pairs(lo, 32, lane, emit);
+            for (int q = 0; q < m; q++) {  // the lower records against upper record q
+                const PairRec o = shfl_rec(up, q);
+                emit(pair_test(lo, o), lo.id & kIdMask, o.id & kIdMask);
             }
-            __syncwarp();
+            rotate_pairs(up, m, lane, emit);
         } else {
             // large bin: ascending order through a scratch copy, records from global memory
             for (int e = lane; e < n; e += 32) {

@@ -274,6 +274,11 @@ struct mcg_ctx {
     // ---- contact buffers ---------------------------------------------------------------
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
     float contact_skin = 0;  // candidate-list reuse distance (m); 0 rebuilds every evaluation
+    int pair_blocks_set = 0; // blocks of the pair enumeration; 0: contact_pair_blocks(shapes)
+    double default_cell() const { return std::max(2.8 * jr, .72 * cfg.cell_size); }
+    int pair_blocks_for(long long shapes) const {
+        return pair_blocks_set > 0 ? pair_blocks_set : contact_pair_blocks(shapes);
+    }
     void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, int region) {
         drop_graphs();
         contact_mem.release();
@@ -298,7 +303,7 @@ struct mcg_ctx {
         c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.occ = contact_mem.get<uint32_t>(size_t(bin_cap));
-        c.pair_blocks = contact_pair_blocks(S);
+        c.pair_blocks = pair_blocks_for(S);
         const long long W = (long long)c.pair_blocks * 8;
         c.region = std::max(32, (region + 31) / 32 * 32);
         c.cand = contact_mem.get<uint2>(size_t(W * c.region));
@@ -1742,7 +1747,7 @@ int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, in
             throw Fail(MCG_ERR_INVALID, "capacities must be non-negative and bins at most 2^28");
         const long long lo = 4096;
         c->sync();
-        const long long W = (long long)contact_pair_blocks((long long)c->N + c->B) * 8;
+        const long long W = (long long)c->pair_blocks_for((long long)c->N + c->B) * 8;
         c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
                           std::max<long long>(bins, lo), int(std::min<long long>((candidates + W - 1) / W, 1LL << 26)));
     });
@@ -1779,9 +1784,90 @@ int mcg_set_contact_cell(mcg_ctx* c, double cell) {
     return guarded(c, [&] {
         need_topo(c);
         if (!(cell >= 0) || cell > 1e3) throw Fail(MCG_ERR_INVALID, "cell must be a length >= 0 (m)");
-        c->broad_cell = cell > 0 ? cell : std::max(2.8 * c->jr, .72 * c->cfg.cell_size);
+        c->broad_cell = cell > 0 ? cell : c->default_cell();
         c->sync();
         c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.region);
+    });
+}
+
+int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, mcg_tuning* out) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (reps < 1 || reps > 1000) throw Fail(MCG_ERR_INVALID, "reps must be in 1 .. 1000");
+        if (!c->cfg.self_contact) throw Fail(MCG_ERR_INVALID, "self-contact is off: nothing to tune");
+        cudaStream_t s = c->stream;
+        const size_t n = 6 * size_t(c->N);
+        c->sync();
+        if (z) h2d(c->d_zin, z, n, s);
+        else ck(cudaMemsetAsync(c->d_zin, 0, n * sizeof(double), s), "memset");
+        for (int i = 0; i < c->I; i++) c->hp.tops[i] = tops ? tops[i] : c->inst[size_t(i)].geom.top0;
+        c->upload_tops();
+        c->set_active(std::vector<uint8_t>(size_t(c->I), 1));
+        const float skin = c->contact_skin;
+        c->contact_skin = 0.f;  // time full builds
+        const long long S = (long long)c->N + c->B;
+        const long long total_region = (long long)c->cb.pair_blocks * 8 * c->cb.region;
+        std::vector<int> blocks{0};
+        for (int b : {152, 304, 608, 1216})
+            if (b != contact_pair_blocks(S) && (long long)b * 8 * 32 <= std::max<long long>(S, 8 * 32)) blocks.push_back(b);
+        const double cell0 = c->default_cell();
+        std::vector<double> ref_e, e(size_t(c->I));
+        std::vector<double> ref_g, g(n);
+        cudaEvent_t t0 = nullptr, t1 = nullptr;
+        ck(cudaEventCreate(&t0), "cudaEventCreate");
+        ck(cudaEventCreate(&t1), "cudaEventCreate");
+        struct Pick { double cell; int blocks; double ms; };
+        Pick best{cell0, 0, 1e300};
+        double ms_default = 0;
+        int tried = 0;
+        try {
+            for (double scale : {1.0, 0.8, 1.25, 1.5})
+                for (int b : blocks) {
+                    c->broad_cell = scale * cell0;
+                    c->pair_blocks_set = b;
+                    const long long W = (long long)c->pair_blocks_for(S) * 8;
+                    c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap,
+                                      int(std::min<long long>((total_region + W - 1) / W, 1LL << 26)));
+                    const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);  // sizes the buffers
+                    for (int i = 0; i < c->I; i++) e[size_t(i)] = o[i].energy;
+                    d2h(g.data(), c->d_grad, n, s);
+                    c->sync();
+                    if (ref_e.empty()) {
+                        ref_e = e;
+                        ref_g = g;
+                    } else if (std::memcmp(e.data(), ref_e.data(), e.size() * sizeof(double)) != 0 ||
+                               std::memcmp(g.data(), ref_g.data(), n * sizeof(double)) != 0) {
+                        throw Fail(MCG_ERR_MISMATCH, "broad-phase shapes changed an evaluation");
+                    }
+                    c->eval(c->d_zin, false, c->d_grad);  // captures the graph
+                    ck(cudaEventRecord(t0, s), "cudaEventRecord");
+                    for (int r = 0; r < reps; r++) c->eval(c->d_zin, false, c->d_grad);
+                    ck(cudaEventRecord(t1, s), "cudaEventRecord");
+                    c->read_outs();
+                    if (c->hp.outs[0].overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers overflowed in tuning");
+                    float ms = 0;
+                    ck(cudaEventElapsedTime(&ms, t0, t1), "cudaEventElapsedTime");
+                    const double per = double(ms) / reps;
+                    if (tried == 0) ms_default = per;
+                    tried++;
+                    if (per < best.ms) best = Pick{c->broad_cell, b, per};
+                }
+        } catch (...) {
+            cudaEventDestroy(t0);
+            cudaEventDestroy(t1);
+            c->contact_skin = skin;
+            throw;
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        c->contact_skin = skin;
+        c->broad_cell = best.cell;
+        c->pair_blocks_set = best.blocks;
+        const long long W = (long long)c->pair_blocks_for(S) * 8;
+        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap,
+                          int(std::min<long long>((total_region + W - 1) / W, 1LL << 26)));
+        c->sync();
+        if (out) *out = mcg_tuning{best.cell, c->pair_blocks_for(S), tried, best.ms, ms_default};
     });
 }
 

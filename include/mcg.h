@@ -46,6 +46,7 @@ enum mcg_status {
                                 reference throws std::runtime_error, MC/src/sim.cpp:412-419) */
     MCG_ERR_CAPACITY = 6,    /* an output buffer is too small; the needed count is returned */
     MCG_ERR_TIMEOUT = 7,     /* a bounded device-side wait gave up */
+    MCG_ERR_MISMATCH = 8,    /* a self-check failed: results that must agree bit for bit did not */
 };
 
 enum mcg_precision {
@@ -275,6 +276,24 @@ int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
  * reference's max(2.8 joint radius, 0.72 cell_size)).  Pair sets and results do not depend
  * on it: a pair is examined once whatever the grid, and the narrow phase decides. */
 int mcg_set_contact_cell(mcg_ctx* ctx, double cell);
+
+/* Shapes of the self-contact broad phase picked by measurement (no reference
+ * counterpart).  Candidates: grid cells 0.8, 1, 1.25 and 1.5 times the reference's
+ * max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 .. 1216 blocks
+ * (at most one warp per 32 shapes) besides the default.  Each candidate evaluates every
+ * lattice `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL:
+ * z = 0) and platen heights `tops` (NULL: each lattice's top0), with the candidate list
+ * rebuilt at every evaluation; the fastest by CUDA-event time is kept for the context.
+ * The candidates must agree bit for bit on energies and gradients (pair sets and sums do
+ * not depend on the grid); MCG_ERR_MISMATCH if one does not. */
+typedef struct mcg_tuning {
+    double cell;          /* chosen grid cell (m) */
+    int32_t pair_blocks;  /* chosen blocks of the pair enumeration (8 warps each) */
+    int32_t tried;        /* candidates timed */
+    double ms_chosen;     /* ms per evaluation with the chosen shapes */
+    double ms_default;    /* ms per evaluation with the default shapes */
+} mcg_tuning;
+int mcg_autotune(mcg_ctx* ctx, const double* z, const double* tops, int32_t reps, mcg_tuning* out);
 
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
  * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept

@@ -41,7 +41,7 @@ def test_oracle_libraries_export_the_oracle_api(mco):
 STRUCTS = {"mcg_config": abi.Config, "mcg_material": abi.Material, "mcg_topology": abi.Topology,
            "mcg_geometry": abi.Geometry, "mcg_diag": abi.Diag, "mcg_optstats": abi.OptStats,
            "mcg_frame": abi.Frame, "mcg_lattice_spec": abi.LatticeSpec,
-           "mcg_lattice_view": abi.LatticeView}
+           "mcg_lattice_view": abi.LatticeView, "mcg_tuning": abi.Tuning}
 
 
 def test_struct_layouts_match_the_header():

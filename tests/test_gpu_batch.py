@@ -69,3 +69,27 @@ def test_single_lattice_functions_refuse_a_batch(mcg):
     assert batch.lib.mcg_instance_count(batch.h) == 2
     with pytest.raises(mcg.MCGError):
         mcg.Solver.objective(batch, np.zeros(6 * batch.n_nodes), 0.0)
+
+
+def test_autotuned_shapes_leave_evaluations_and_runs_unchanged(mcg):
+    """mcg_autotune times broad-phase cells and pair grids and keeps the fastest; the choice
+    must not change an evaluation or a run by a bit (it checks its candidates itself)."""
+    cfg, lats, ys = make(mcg, load_steps=6, unload_steps=2, max_strain=0.25)
+    states = [mcg.random_state(lat, 0.04, 0.08, 0.02, 2000 + k) for k, lat in enumerate(lats)]
+    z = np.concatenate([zz for zz, _ in states])
+    tops = [lat.geometry.top0 - 0.003 for lat in lats]
+    plain = mcg.BatchSolver(cfg, lats, yields=ys)
+    ref = plain.objective(z, tops)
+    _, ref_runs = plain.run()
+    tuned = mcg.BatchSolver(cfg, lats, yields=ys)
+    t = tuned.autotune(z, tops, reps=2)
+    assert t["tried"] >= 4 and t["ms_chosen"] <= t["ms_default"] * 1.0001
+    assert t["cell"] > 0 and t["pair_blocks"] >= 1
+    got = tuned.objective(z, tops)
+    assert np.array_equal(got["energy"], ref["energy"])
+    assert np.array_equal(got["grad"], ref["grad"])
+    _, runs = tuned.run()
+    for k in range(len(lats)):
+        assert [f["reaction_force"] for f in runs[k]] == [f["reaction_force"] for f in ref_runs[k]], k
+    with pytest.raises(ValueError):
+        tuned.autotune(z[:-1])
