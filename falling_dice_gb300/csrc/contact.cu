@@ -10,18 +10,20 @@
 // and the same floor() cell coordinates).  Cells are numbered by the Morton code of their
 // coordinates relative to the grid origin (row-major when the Morton range does not fit),
 // and entries are counting-sorted into those bins: one atomic count per entry, a scan over
-// bins, one scatter.  The pair pass gives each occupied bin to one warp, which stages the
-// bin's shapes in shared memory in ascending shape order, so every result is independent
-// of the order the atomics handed out.  A pair is examined only in the cell that is the
+// bins, one scatter.  The pair pass gives each occupied bin to one warp, which enumerates
+// the bin's pairs in the order the atomics handed out: the candidate list's order can vary
+// from run to run, its content cannot, and nothing computed from it depends on the order
+// (contact forces and energies are summed per node in shape-pair order, and pair sets are
+// reported sorted).  A pair is examined only in the cell that is the
 // minimum corner of the intersection of the two shapes' cell ranges: every pair that
 // shares a cell is examined exactly once -- the reference's `tested` set without a set.
 // A conservative FP32 AABB test and the local-shape exclusion (sim.cpp:24-39) run before
 // the FP64 narrow phase.
 //
-// Output order.  Candidate pairs are counted per bin, scanned and written in (bin, pair)
-// order; the narrow phase flags the candidates in contact, a scan places them, and the
-// contact list keeps the candidate order: the list and every sum over it are
-// deterministic.  Per-node force lists are built with counters and sorted by the gather.
+// Output order.  Candidate pairs are written per warp in (bin, pair) order; the narrow
+// phase flags the candidates in contact, a scan places them, and the contact list keeps
+// the candidate order.  Per-node force lists are built with counters and sorted by contact
+// key (lower shape, higher shape, slot), so every sum is independent of the list order.
 //
 // No host synchronisation: sizes that can overflow a buffer (entries, bins, contacts, a
 // shape spanning too many cells) raise a flag instead of writing out of bounds, and the
@@ -450,21 +452,20 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane,
 
 // Candidate pairs of every occupied bin.  Warp w of the fixed grid takes the occupied bins
 // occ[w], occ[w + W], ... in order and appends their candidate pairs (lower shape, higher
-// shape) to its own region cand[w R .. (w + 1) R), so the candidate list -- regions in warp
-// order, each in bin and enumeration order -- is deterministic without a second counting
-// pass.  A region that fills up flags kOverCandidates; wcount[w] keeps the full count so the
-// host can size R.  Enumeration inside a bin:
-//   n <= 32  the bin's shapes are sorted across the warp's lanes (bitonic, by shape id)
-//            and every unordered pair is visited by rotation (rotate_pairs);
-//   n <= 64  sorted as 64 keys, two per lane (lane i holds ranks i and 32 + i); pairs of
-//            the lower 32 by rotation, each upper record broadcast to the 32 lower ones,
-//            pairs of the upper records by rotation;
-//   larger   sorted through a scratch copy, records read from global memory.
+// shape) to its own region cand[w R .. (w + 1) R), without a second counting pass.  A
+// region that fills up flags kOverCandidates; wcount[w] keeps the full count so the host
+// can size R.  Enumeration inside a bin, entries in bin order:
+//   n <= 32  lane i holds entry i; every unordered pair is visited by rotation
+//            (rotate_pairs);
+//   n <= 64  lane i holds entries i and 32 + i; pairs of the lower 32 by rotation, each
+//            upper record broadcast to the 32 lower ones, pairs of the upper records by
+//            rotation;
+//   larger   pairs by index, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count,
                                                       const uint32_t* __restrict__ bin_start,
                                                       const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
-                                                      const uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted2,
+                                                      const uint32_t* __restrict__ sorted,
                                                       const uint4* __restrict__ rec, int region,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
                                                       uint32_t* __restrict__ wcap, uint32_t* __restrict__ flags) {
@@ -491,39 +492,14 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         const int3 cc = cell_of(grid, b);
         const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
         if (n <= 32) {
-            uint32_t v = lane < n ? sorted[start + lane] : 0xffffffffu;
-            for (int k = 2; k <= 32; k <<= 1)  // bitonic sort, ascending
-                for (int j = k >> 1; j > 0; j >>= 1) {
-                    const uint32_t o = __shfl_xor_sync(0xffffffffu, v, j);
-                    const bool up = (lane & k) == 0, lower = (lane & j) == 0;
-                    v = (lower == up) ? min(v, o) : max(v, o);
-                }
             PairRec me{};
-            if (lane < n) me = load_rec(t, v, rec, ccp);
+            if (lane < n) me = load_rec(t, sorted[start + lane], rec, ccp);
             rotate_pairs(me, n, lane, emit);
         } else if (n <= 64) {
-            uint32_t v0 = sorted[start + lane];
-            uint32_t v1 = lane + 32 < n ? sorted[start + 32 + lane] : 0xffffffffu;
-            // bitonic sort of the 64 keys, key e = lane + 32 h in register h, ascending
-            for (int k = 2; k <= 64; k <<= 1)
-                for (int j = k >> 1; j > 0; j >>= 1) {
-                    if (j == 32) {  // partners in the same lane (k = 64: ascending)
-                        const uint32_t lo = min(v0, v1), hi = max(v0, v1);
-                        v0 = lo;
-                        v1 = hi;
-                    } else {
-                        const uint32_t o0 = __shfl_xor_sync(0xffffffffu, v0, j);
-                        const uint32_t o1 = __shfl_xor_sync(0xffffffffu, v1, j);
-                        const bool lower = (lane & j) == 0;
-                        const bool up0 = (lane & k) == 0, up1 = ((lane + 32) & k) == 0;
-                        v0 = (lower == up0) ? min(v0, o0) : max(v0, o0);
-                        v1 = (lower == up1) ? min(v1, o1) : max(v1, o1);
-                    }
-                }
             const int m = n - 32;
-            const PairRec lo = load_rec(t, v0, rec, ccp);
+            const PairRec lo = load_rec(t, sorted[start + lane], rec, ccp);
             PairRec up{};
-            if (lane < m) up = load_rec(t, v1, rec, ccp);
+            if (lane < m) up = load_rec(t, sorted[start + 32 + lane], rec, ccp);
             rotate_pairs(lo, 32, lane, emit);
             for (int q = 0; q < m; q++) {  // the lower records against upper record q
                 const PairRec o = shfl_rec(up, q);
@@ -531,14 +507,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
             }
             rotate_pairs(up, m, lane, emit);
         } else {
-            // large bin: ascending order through a scratch copy, records from global memory
-            for (int e = lane; e < n; e += 32) {
-                const uint32_t v = sorted[start + e];
-                int r = 0;
-                for (int q = 0; q < n; q++) r += sorted[start + q] < v;
-                sorted2[start + r] = v;
-            }
-            __syncwarp();
+            // large bin: pairs by index, records from global memory
             const long long P = (long long)n * (n - 1) / 2;
             int i = 0;
             long long row_end = n - 1;  // pairs of rows 0..i end here
@@ -552,8 +521,8 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                         row_end += n - 1 - i;
                     }
                     const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                    const PairRec A = load_rec(t, sorted2[start + i], rec, ccp);
-                    const PairRec B = load_rec(t, sorted2[start + j], rec, ccp);
+                    const PairRec A = load_rec(t, sorted[start + i], rec, ccp);
+                    const PairRec B = load_rec(t, sorted[start + j], rec, ccp);
                     hit = pair_test(A, B);
                     sa = A.id & kIdMask;
                     sb = B.id & kIdMask;
@@ -916,7 +885,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     const uint32_t* nocc = c.boffset + c.bin_cap;
     const int W = c.pair_blocks * kPairWarps;
     if (pairs_begin) cudaEventRecord(pairs_begin, s);
-    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted, c.sorted2,
+    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted,
                                                 c.rec, c.region, c.cand, c.wcount, c.wcap, c.flags),
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);

@@ -296,7 +296,6 @@ struct mcg_ctx {
         c.ekey = contact_mem.get<uint32_t>(size_t(entry_cap));
         c.erank = contact_mem.get<uint32_t>(size_t(entry_cap));
         c.sorted = contact_mem.get<uint32_t>(size_t(entry_cap));
-        c.sorted2 = contact_mem.get<uint32_t>(size_t(entry_cap));
         c.bin_cap = bin_cap;
         c.bin_count = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.bin_start = contact_mem.get<uint32_t>(size_t(bin_cap + 1));

@@ -124,7 +124,6 @@ struct ContactBufs {
     uint32_t* ekey;         // [entry_cap] bin of the entry
     uint32_t* erank;        // [entry_cap] rank of the entry inside its bin
     uint32_t* sorted;       // [entry_cap] shape ids grouped by bin
-    uint32_t* sorted2;      // [entry_cap] scratch for bins too large for shared memory
     // bins
     long long bin_cap;
     uint32_t* bin_count;    // [bin_cap+1]

@@ -90,7 +90,6 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.ekey = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
     c.erank = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
     c.sorted = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
-    c.sorted2 = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
     c.bin_cap = kNoAllocBins;
     c.bin_count = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.bin_start = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));

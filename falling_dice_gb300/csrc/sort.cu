@@ -1,5 +1,7 @@
 // sort.cu -- deterministic exclusive scan of uint32 counts: reduce-then-scan over tiles of
-// 2048 items (256 threads x 8 consecutive items), one block scanning the tile totals.
+// 2048 items (256 threads x 8 consecutive items).  Up to 1024 tiles each block of the second
+// pass sums the tile totals before it itself (two launches); beyond, one block scans the
+// tile totals between the two passes.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -87,16 +89,45 @@ __global__ void __launch_bounds__(kBlock) k_scan_partials(uint32_t* part, long l
     if (threadIdx.x == 0) *total_out = carry;
 }
 
+// DIRECT: the tile partials are not scanned; each block sums those before it (and block 0
+// all of them), for at most kDirectTiles tiles.
+constexpr long long kDirectTiles = 1024;
+
+__device__ __forceinline__ uint32_t block_sum_u32(uint32_t v, uint32_t* smem) {
+    uint32_t tot;
+    block_exclusive_scan(v, smem, &tot);
+    return tot;
+}
+
+template <bool DIRECT>
 __global__ void __launch_bounds__(kBlock) k_scan_down(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                       long long cap, const uint32_t* __restrict__ part,
-                                                      const uint32_t* __restrict__ total,
+                                                      const uint32_t* __restrict__ total_p,
                                                       const uint32_t* __restrict__ gate,
                                                       const uint32_t* __restrict__ dn, int add, int shift) {
     if (gate && !*gate) return;
     const long long n = scan_len(cap, dn, add, shift);
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[cap] = *total;  // the total at a fixed place
-    if ((long long)blockIdx.x * kTile >= n) return;
     __shared__ uint32_t sm[kBlock / 32];
+    uint32_t prefix, total = 0;
+    if (DIRECT) {
+        const long long np = (n + kTile - 1) / kTile;
+        if (blockIdx.x > 0 && (long long)blockIdx.x * kTile >= n) return;
+        const long long upto = blockIdx.x == 0 ? np : (long long)blockIdx.x;
+        uint32_t a = 0, b = 0;  // partials before this block; all partials (block 0)
+        for (long long i = threadIdx.x; i < upto; i += kBlock) {
+            const uint32_t v = part[i];
+            if (i < (long long)blockIdx.x) a += v;
+            b += v;
+        }
+        prefix = block_sum_u32(a, sm);
+        if (blockIdx.x == 0) total = block_sum_u32(b, sm);
+    } else {
+        if (blockIdx.x == 0) total = *total_p;
+        if ((long long)blockIdx.x * kTile >= n && blockIdx.x > 0) return;
+        prefix = part[blockIdx.x];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) out[cap] = total;  // the total at a fixed place
+    if ((long long)blockIdx.x * kTile >= n) return;
     const long long base = (long long)blockIdx.x * kTile + (long long)threadIdx.x * kItems;
     uint32_t v[kItems], s = 0;
 #pragma unroll
@@ -104,11 +135,11 @@ __global__ void __launch_bounds__(kBlock) k_scan_down(const uint32_t* __restrict
         v[k] = base + k < n ? in[base + k] : 0;
         s += v[k];
     }
-    uint32_t run = part[blockIdx.x] + block_exclusive_scan(s, sm, nullptr);
+    uint32_t run = prefix + block_exclusive_scan(s, sm, nullptr);
 #pragma unroll
     for (int k = 0; k < kItems; k++)
         if (base + k < n) { out[base + k] = run; run += v[k]; }
-    if (blockIdx.x == 0 && threadIdx.x == 0 && n < cap) out[n] = *total;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n < cap) out[n] = total;
 }
 
 }  // namespace
@@ -128,8 +159,14 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, long long n, void* tm
         return;
     }
     (k_scan_reduce<<<unsigned(np), kBlock, 0, s>>>(in, n, part, gate, dn, add, shift), note_launches(1));
+    if (np <= kDirectTiles) {
+        (k_scan_down<true><<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate, dn, add, shift),
+         note_launches(1));
+        return;
+    }
     (k_scan_partials<<<1, kBlock, 0, s>>>(part, np, total, gate, dn, add, shift), note_launches(1));
-    (k_scan_down<<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate, dn, add, shift), note_launches(1));
+    (k_scan_down<false><<<unsigned(np), kBlock, 0, s>>>(in, out, n, part, total, gate, dn, add, shift),
+     note_launches(1));
 }
 
 }  // namespace mcg
