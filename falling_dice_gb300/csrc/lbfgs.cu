@@ -60,42 +60,28 @@ __device__ __forceinline__ double dot6(const double* a, const double* b) {
 }
 
 // ---- two-loop recursion (sim.cpp:184-187) -----------------------------------------------
-// Partial <S[slot], p> (loop 1, newest first: h = m - 1 - j) or <Y[slot], p> (loop 2,
-// oldest first: h = j) for the instances computing a direction with j < m.
+// Step j of loop LOOP for the instances computing a direction with j < m.  Every block of
+// an instance sums the instance's partials of step j's dot product (in `cur`, same order in
+// each block) into the coefficient and updates its nodes of p; when j + 1 < m it then writes
+// its partial of step j + 1's dot product with the updated p to `nxt`.
+//   loop 1 (newest first, h = m - 1 - j): alpha = rho <s, p> (kept), p -= alpha y;
+//   loop 2 (oldest first, h = j):         beta = rho <y, p>, p += s (alpha - beta).
 template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_dot(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H, int j,
-                                                   const double* __restrict__ p, const double* __restrict__ S,
-                                                   const double* __restrict__ Y, long long stride,
-                                                   double* __restrict__ part) {
-    __shared__ double sm[kBlock / 32];
-    const MapPos mp = map_pos(t.nblk);
-    const SolveCtl c = load_ctl(ctl, hist, mp.inst);
-    if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
-    const int slot = ring_slot(c, H, LOOP == 1 ? c.m - 1 - j : j);
-    const double* v = hist_slot(LOOP == 1 ? S : Y, stride, slot);
-    double acc[1] = {0};
-    if (mp.valid) acc[0] = dot6(v + 6 * size_t(mp.i), p + 6 * size_t(mp.i));
-    block_sum<1>(acc, sm);
-    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
-}
-
-// Loop 1: alpha = rho <s, p> (kept), p -= alpha y.  Loop 2: beta = rho <y, p>, p += s (alpha - beta).
-// Every block of an instance sums the instance's partials itself (same order in each).
-template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H, int j,
-                                                      double* __restrict__ p, const double* __restrict__ S,
-                                                      const double* __restrict__ Y, long long stride,
-                                                      const double* __restrict__ rho, double* __restrict__ alpha,
-                                                      const double* __restrict__ part) {
+__global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                    const int2* __restrict__ hist, int H, int j,
+                                                    double* __restrict__ p, const double* __restrict__ S,
+                                                    const double* __restrict__ Y, long long stride,
+                                                    const double* __restrict__ rho, double* __restrict__ alpha,
+                                                    const double* __restrict__ cur, double* __restrict__ nxt) {
     __shared__ double sm[kBlock / 32];
     __shared__ double coef;
     const MapPos mp = map_pos(t.nblk);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
-    if (!(c.flags & kOpDirection) || j >= c.m) return;
+    if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
     const int h = LOOP == 1 ? c.m - 1 - j : j;
     const int slot = ring_slot(c, H, h);
     double acc[1];
-    instance_sum<1>(t, part, mp.inst, acc, sm);
+    instance_sum<1>(t, cur, mp.inst, acc, sm);
     if (threadIdx.x == 0) {
         const double r = rho[size_t(mp.inst) * H + slot] * acc[0];
         if (LOOP == 1) {
@@ -106,27 +92,40 @@ __global__ void __launch_bounds__(kBlock) k_tl_update(DevTopo t, const SolveCtl*
         }
     }
     __syncthreads();
-    if (!mp.valid) return;
     const double k = coef;
-    double* pi = p + 6 * size_t(mp.i);
-    if (LOOP == 1) {
-        const double* y = hist_slot(Y, stride, slot) + 6 * size_t(mp.i);
+    double pn[6] = {0, 0, 0, 0, 0, 0};
+    if (mp.valid) {
+        double* pi = p + 6 * size_t(mp.i);
+        if (LOOP == 1) {
+            const double* y = hist_slot(Y, stride, slot) + 6 * size_t(mp.i);
 #pragma unroll
-        for (int d = 0; d < 6; d++) pi[d] -= k * y[d];
-    } else {
-        const double* s = hist_slot(S, stride, slot) + 6 * size_t(mp.i);
+            for (int d = 0; d < 6; d++) pn[d] = pi[d] - k * y[d];
+        } else {
+            const double* sv = hist_slot(S, stride, slot) + 6 * size_t(mp.i);
 #pragma unroll
-        for (int d = 0; d < 6; d++) pi[d] += s[d] * k;
+            for (int d = 0; d < 6; d++) pn[d] = pi[d] + sv[d] * k;
+        }
+#pragma unroll
+        for (int d = 0; d < 6; d++) pi[d] = pn[d];
     }
+    if (j + 1 >= c.m) return;  // block-uniform
+    const int slot2 = ring_slot(c, H, LOOP == 1 ? c.m - 2 - j : j + 1);
+    const double* v = hist_slot(LOOP == 1 ? S : Y, stride, slot2);
+    double a2[1] = {0};
+    if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
+    block_sum<1>(a2, sm);
+    if (threadIdx.x == 0) nxt[blockIdx.x] = a2[0];
 }
 
-// Partials of <s, y> and <y, y> of the newest pair (for H0) and the copy p = g that starts
-// the recursion.
+// Partials of <s, y> and <y, y> of the newest pair (for H0, into h0part), the copy p = g
+// that starts the recursion and the partial of loop 1's first dot product <s, g> (into
+// part0).
 __global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
                                                      double* __restrict__ p, const double* __restrict__ g,
                                                      const double* __restrict__ S, const double* __restrict__ Y,
-                                                     long long stride, double* __restrict__ part) {
-    __shared__ double sm[2 * (kBlock / 32)];
+                                                     long long stride, double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
+    __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
@@ -135,23 +134,28 @@ __global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* 
         for (int d = 0; d < 6; d++) p[6 * size_t(mp.i) + d] = g[6 * size_t(mp.i) + d];
     if (c.m == 0) return;
     const int slot = ring_slot(c, H, c.m - 1);
-    double acc[2] = {0, 0};
+    double acc[3] = {0, 0, 0};
     if (mp.valid) {
         const double* s = hist_slot(S, stride, slot) + 6 * size_t(mp.i);
         const double* y = hist_slot(Y, stride, slot) + 6 * size_t(mp.i);
         acc[0] = dot6(s, y);
         acc[1] = dot6(y, y);
+        acc[2] = dot6(s, g + 6 * size_t(mp.i));
     }
-    block_sum<2>(acc, sm);
+    block_sum<3>(acc, sm);
     if (threadIdx.x == 0) {
-        part[blockIdx.x] = acc[0];
-        part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
+        h0part[blockIdx.x] = acc[0];
+        h0part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
+        part0[blockIdx.x] = acc[2];
     }
 }
 
-// p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186).
+// p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186), and
+// the partial of loop 2's first dot product <y, p> (into part0).
 __global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
-                                                     double* __restrict__ p, const double* __restrict__ part) {
+                                                     int H, double* __restrict__ p, const double* __restrict__ Y,
+                                                     long long stride, const double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
     __shared__ double sm[2 * (kBlock / 32)];
     __shared__ double h0;
     const MapPos mp = map_pos(t.nblk);
@@ -159,7 +163,7 @@ __global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* 
     if (!(c.flags & kOpDirection)) return;
     if (c.m > 0) {
         double acc[2];
-        instance_sum<2>(t, part, mp.inst, acc, sm);
+        instance_sum<2>(t, h0part, mp.inst, acc, sm);
         if (threadIdx.x == 0) {
             double v = .10;
             if (acc[0] > 1e-20 && acc[1] > 1e-20) v = clampd(acc[0] / acc[1], 1e-7, 1e4);
@@ -169,10 +173,20 @@ __global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* 
         h0 = .10;
     }
     __syncthreads();
-    if (!mp.valid) return;
     const double k = h0;
+    double pn[6] = {0, 0, 0, 0, 0, 0};
+    if (mp.valid)
 #pragma unroll
-    for (int d = 0; d < 6; d++) p[6 * size_t(mp.i) + d] *= k;
+        for (int d = 0; d < 6; d++) {
+            pn[d] = p[6 * size_t(mp.i) + d] * k;
+            p[6 * size_t(mp.i) + d] = pn[d];
+        }
+    if (c.m == 0) return;  // block-uniform
+    const double* v = hist_slot(Y, stride, ring_slot(c, H, 0));
+    double a2[1] = {0};
+    if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
+    block_sum<1>(a2, sm);
+    if (threadIdx.x == 0) part0[blockIdx.x] = a2[0];
 }
 
 // Direction finish for the instances with `bit` set: p = clamp(lock(-src)) per node
@@ -316,7 +330,7 @@ __global__ void __launch_bounds__(kBlock) k_accept(DevTopo t, const SolveCtl* __
 // For instances of at most kFuseChunks node blocks: the same steps as k_tl_start ...
 // k_finish + k_inst_final (each block partial here is one chunk of kBlock nodes reduced by the
 // same tree, each instance sum the same strided tree), so the result is bit for bit that of
-// the multi-launch path; one launch instead of 4 m + 4.
+// the multi-launch path; one launch instead of 2 H + 4.
 constexpr int kFuseChunks = 64;
 
 // Partial of one chunk: thread t the node first + t (if valid), then the block tree.
@@ -569,7 +583,7 @@ __global__ void k_history_update(int I, int H, const SolveCtl* __restrict__ ctl,
 
 }  // namespace
 
-size_t lbfgs_part_doubles(int n_nblk) { return 3 * size_t(n_nblk) + 8; }
+size_t lbfgs_part_doubles(int n_nblk) { return 4 * size_t(n_nblk) + 8; }
 
 int fused_direction_limit() { return kFuseChunks; }
 
@@ -579,19 +593,19 @@ void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool
     const int nb = t.n_nblk;
     (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
     if (multi) {
-        (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, part + 2 * size_t(nb)),
-         note_launches(1));
-        for (int j = 0; j < H; j++) {
-            (k_tl_dot<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, part), note_launches(1));
-            (k_tl_update<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, part),
+        // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
+        double* pp[2] = {part, part + size_t(nb)};
+        double* h0part = part + 2 * size_t(nb);
+        (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, h0part, pp[0]), note_launches(1));
+        for (int j = 0; j < H; j++)
+            (k_tl_step<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
+                                                pp[(j + 1) & 1]),
              note_launches(1));
-        }
-        (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, hist, p, part + 2 * size_t(nb)), note_launches(1));
-        for (int j = 0; j < H; j++) {
-            (k_tl_dot<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, part), note_launches(1));
-            (k_tl_update<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, part),
+        (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, Y, stride, h0part, pp[0]), note_launches(1));
+        for (int j = 0; j < H; j++)
+            (k_tl_step<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
+                                                pp[(j + 1) & 1]),
              note_launches(1));
-        }
         (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
         (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
     }
