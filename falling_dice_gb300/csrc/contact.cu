@@ -41,6 +41,7 @@ constexpr uint32_t kBoxMax = 32767u;    // 15-bit box coordinates
 constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
+constexpr int kPairGrab = 2;             // occupied bins a warp claims at a time
 constexpr int kStreamBlocks = 8 * 152;
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
@@ -450,9 +451,10 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane,
     }
 }
 
-// Candidate pairs of every occupied bin.  Warp w of the fixed grid takes the occupied bins
-// occ[w], occ[w + W], ... in order and appends their candidate pairs (lower shape, higher
-// shape) to its own region cand[w R .. (w + 1) R), without a second counting pass.  A
+// Candidate pairs of every occupied bin.  Warps claim the occupied bins kPairGrab at a time
+// from a cursor (flags[3]), so bins of uneven size balance over the grid, and append their
+// candidate pairs (lower shape, higher shape) to their own region cand[w R .. (w + 1) R),
+// without a second counting pass.  A
 // region that fills up flags kOverCandidates; wcount[w] keeps the full count so the host
 // can size R.  Enumeration inside a bin, entries in bin order:
 //   n <= 32  lane i holds entry i; every unordered pair is visited by rotation
@@ -474,8 +476,8 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
     const unsigned below = (1u << lane) - 1u;
     const uint32_t nocc = *nocc_p;
     const uint32_t gw = blockIdx.x * kPairWarps + w;
-    const uint32_t warps = gridDim.x * kPairWarps;
     uint2* mine = cand + size_t(gw) * size_t(region);
+    uint32_t* cursor = flags + 3;
     uint32_t out = 0;
     auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
         const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -485,51 +487,58 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         }
         out += __popc(m);
     };
-    for (uint32_t jb = gw; jb < nocc; jb += warps) {
-        const uint32_t b = occ[jb];
-        const int n = int(bin_count[b]);
-        const uint32_t start = bin_start[b];
-        const int3 cc = cell_of(grid, b);
-        const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
-        if (n <= 32) {
-            PairRec me{};
-            if (lane < n) me = load_rec(t, sorted[start + lane], rec, ccp);
-            rotate_pairs(me, n, lane, emit);
-        } else if (n <= 64) {
-            const int m = n - 32;
-            const PairRec lo = load_rec(t, sorted[start + lane], rec, ccp);
-            PairRec up{};
-            if (lane < m) up = load_rec(t, sorted[start + 32 + lane], rec, ccp);
-            rotate_pairs(lo, 32, lane, emit);
-            for (int q = 0; q < m; q++) {  // the lower records against upper record q
-                const PairRec o = shfl_rec(up, q);
-                emit(pair_test(lo, o), lo.id & kIdMask, o.id & kIdMask);
-            }
-            rotate_pairs(up, m, lane, emit);
-        } else {
-            // large bin: pairs by index, records from global memory
-            const long long P = (long long)n * (n - 1) / 2;
-            int i = 0;
-            long long row_end = n - 1;  // pairs of rows 0..i end here
-            for (long long base = 0; base < P; base += 32) {
-                const long long pidx = base + lane;
-                bool hit = false;
-                uint32_t sa = 0, sb = 0;
-                if (pidx < P) {
-                    while (pidx >= row_end) {  // rows advance monotonically with base
-                        i++;
-                        row_end += n - 1 - i;
-                    }
-                    const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                    const PairRec A = load_rec(t, sorted[start + i], rec, ccp);
-                    const PairRec B = load_rec(t, sorted[start + j], rec, ccp);
-                    hit = pair_test(A, B);
-                    sa = A.id & kIdMask;
-                    sb = B.id & kIdMask;
+    for (;;) {
+        uint32_t jb0 = 0;
+        if (lane == 0) jb0 = atomicAdd(cursor, uint32_t(kPairGrab));
+        jb0 = __shfl_sync(0xffffffffu, jb0, 0);
+        if (jb0 >= nocc) break;
+        const uint32_t jend = min(jb0 + uint32_t(kPairGrab), nocc);
+        for (uint32_t jb = jb0; jb < jend; jb++) {
+            const uint32_t b = occ[jb];
+            const int n = int(bin_count[b]);
+            const uint32_t start = bin_start[b];
+            const int3 cc = cell_of(grid, b);
+            const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
+            if (n <= 32) {
+                PairRec me{};
+                if (lane < n) me = load_rec(t, sorted[start + lane], rec, ccp);
+                rotate_pairs(me, n, lane, emit);
+            } else if (n <= 64) {
+                const int m = n - 32;
+                const PairRec lo = load_rec(t, sorted[start + lane], rec, ccp);
+                PairRec up{};
+                if (lane < m) up = load_rec(t, sorted[start + 32 + lane], rec, ccp);
+                rotate_pairs(lo, 32, lane, emit);
+                for (int q = 0; q < m; q++) {  // the lower records against upper record q
+                    const PairRec o = shfl_rec(up, q);
+                    emit(pair_test(lo, o), lo.id & kIdMask, o.id & kIdMask);
                 }
-                emit(hit, sa, sb);
+                rotate_pairs(up, m, lane, emit);
+            } else {
+                // large bin: pairs by index, records from global memory
+                const long long P = (long long)n * (n - 1) / 2;
+                int i = 0;
+                long long row_end = n - 1;  // pairs of rows 0..i end here
+                for (long long base = 0; base < P; base += 32) {
+                    const long long pidx = base + lane;
+                    bool hit = false;
+                    uint32_t sa = 0, sb = 0;
+                    if (pidx < P) {
+                        while (pidx >= row_end) {  // rows advance monotonically with base
+                            i++;
+                            row_end += n - 1 - i;
+                        }
+                        const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
+                        const PairRec A = load_rec(t, sorted[start + i], rec, ccp);
+                        const PairRec B = load_rec(t, sorted[start + j], rec, ccp);
+                        hit = pair_test(A, B);
+                        sa = A.id & kIdMask;
+                        sb = B.id & kIdMask;
+                    }
+                    emit(hit, sa, sb);
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
     }
     if (lane == 0) {
@@ -864,6 +873,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     const int S = t.N + t.B;
     const uint32_t* gate = c.flags + 1;
     cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
+    cudaMemsetAsync(c.flags + 3, 0, sizeof(uint32_t), s);  // the pair pass's bin cursor
     (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t, t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
     // candidate list (only when rebuilding)
     (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));

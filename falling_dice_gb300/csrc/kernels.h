@@ -117,7 +117,8 @@ struct ContactBufs {
     int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed;
                             //       box quantization scale x,y,z and origin x,y,z (float bits)
     uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation, [1] candidate list
-                            //      rebuilt by this evaluation, [2] rebuild forced by the host
+                            //      rebuilt by this evaluation, [2] rebuild forced by the host,
+                            //      [3] the pair pass's occupied-bin cursor
     float4* xref;           // [N] node positions (FP32, rounded down) when the list was built
     // entries in emission order (shape-major), then counting-sorted by bin
     long long entry_cap;
