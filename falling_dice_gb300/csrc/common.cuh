@@ -161,6 +161,27 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* smem) {
     __syncthreads();
 }
 
+// NV maxima over the block into thread 0, one barrier pair for all of them; smem holds
+// NV * (blockDim.x / 32) doubles.
+template <int NV>
+__device__ __forceinline__ void block_max_n(double (&v)[NV], double* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = warp_max(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) smem[k * nw + warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double m = smem[k * nw];
+            for (int w = 1; w < nw; w++) m = fmax(m, smem[k * nw + w]);
+            v[k] = m;
+        }
+    __syncthreads();
+}
+
 __device__ __forceinline__ double block_max(double v, double* smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_max(v);

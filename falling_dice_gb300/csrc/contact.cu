@@ -42,6 +42,7 @@ constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
 constexpr int kPairGrab = 2;             // occupied bins a warp claims at a time
+constexpr int kPairStage = 256;          // candidates a warp stages before appending them
 constexpr int kStreamBlocks = 8 * 152;
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
@@ -257,8 +258,9 @@ __global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __
 // ---- kernels -------------------------------------------------------------------------------
 // Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
 __global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
-                              uint32_t* flags) {
+                              uint32_t* flags, uint32_t* ncand) {
     if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
+    *ncand = 0;  // the candidate list of this build
     bool ok = true;
     long long lo[3], dim[3];
     for (int d = 0; d < 3; d++) {
@@ -452,11 +454,12 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane,
 }
 
 // Candidate pairs of every occupied bin.  Warps claim the occupied bins kPairGrab at a time
-// from a cursor (flags[3]), so bins of uneven size balance over the grid, and append their
-// candidate pairs (lower shape, higher shape) to their own region cand[w R .. (w + 1) R),
-// without a second counting pass.  A
-// region that fills up flags kOverCandidates; wcount[w] keeps the full count so the host
-// can size R.  Enumeration inside a bin, entries in bin order:
+// from a cursor (flags[3]), so bins of uneven size balance over the grid, stage their
+// candidate pairs (lower shape, higher shape) in shared memory and append them to the flat
+// list in chunks (one atomic on ncand per chunk), without a counting pass.  The list's
+// length is the number of pairs, whatever the order; past cand_cap the pairs are counted
+// but not stored and kOverCandidates is raised, so the host can size the list exactly.
+// Enumeration inside a bin, entries in bin order:
 //   n <= 32  lane i holds entry i; every unordered pair is visited by rotation
 //            (rotate_pairs);
 //   n <= 64  lane i holds entries i and 32 + i; pairs of the lower 32 by rotation, each
@@ -468,24 +471,34 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                                                       const uint32_t* __restrict__ bin_start,
                                                       const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
                                                       const uint32_t* __restrict__ sorted,
-                                                      const uint4* __restrict__ rec, int region,
-                                                      uint2* __restrict__ cand, uint32_t* __restrict__ wcount,
-                                                      uint32_t* __restrict__ wcap, uint32_t* __restrict__ flags) {
+                                                      const uint4* __restrict__ rec, long long cand_cap,
+                                                      uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
+                                                      uint32_t* __restrict__ flags) {
+    __shared__ uint2 stage_all[kPairWarps][kPairStage];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
     const uint32_t nocc = *nocc_p;
-    const uint32_t gw = blockIdx.x * kPairWarps + w;
-    uint2* mine = cand + size_t(gw) * size_t(region);
+    uint2* stage = stage_all[w];
     uint32_t* cursor = flags + 3;
-    uint32_t out = 0;
+    uint32_t staged = 0;  // warp-uniform
+    // appends the staged candidates to the list: one atomic per chunk
+    auto flush = [&]() {
+        __syncwarp();
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(ncand, staged);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (uint32_t k = lane; k < staged; k += 32)
+            if ((long long)base + k < cand_cap) cand[base + k] = stage[k];
+        if (lane == 0 && (long long)base + staged > cand_cap) atomicOr(flags, uint32_t(kOverCandidates));
+        staged = 0;
+        __syncwarp();
+    };
     auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
         const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (hit) {
-            const uint32_t pos = out + __popc(m & below);
-            if (pos < uint32_t(region)) mine[pos] = make_uint2(min(sa, sb), max(sa, sb));
-        }
-        out += __popc(m);
+        if (hit) stage[staged + __popc(m & below)] = make_uint2(min(sa, sb), max(sa, sb));
+        staged += __popc(m);
+        if (staged > kPairStage - 32) flush();
     };
     for (;;) {
         uint32_t jb0 = 0;
@@ -541,11 +554,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
             }
         }
     }
-    if (lane == 0) {
-        wcount[gw] = out;
-        wcap[gw] = min(out, uint32_t(region));
-        if (out > uint32_t(region)) atomicOr(flags, uint32_t(kOverCandidates));
-    }
+    if (staged) flush();
 }
 
 // Occupied bins (two or more entries), in bin order: flags, then a scan, then this.
@@ -648,43 +657,22 @@ __device__ __forceinline__ int distance_class(const DevTopo& t, const PhysParams
     return d.far_ok && d.far > d.pad_sum ? -1 : 0;
 }
 
-// Global candidate index g (regions in warp order, each in its own order) -> the warp whose
-// prefix range [woff[w], woff[w + 1]) holds it, by binary search.
-__device__ __forceinline__ int candidate_warp(const uint32_t* __restrict__ woff, int W, uint32_t g) {
-    int lo = 0, hi = W;  // woff[lo] <= g < woff[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (woff[mid] <= g) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-// The candidate at g, starting from the warp w0 that holds an earlier index of the same
-// chunk: a few steps forward, or a search when many regions in a row are short.
-__device__ __forceinline__ uint2 candidate_slot(const uint2* __restrict__ cand, const uint32_t* __restrict__ woff,
-                                                int W, int region, uint32_t g, int w0) {
-    int w = w0;
-    for (int k = 0; k < 8 && w + 1 < W && woff[w + 1] <= g; k++) w++;
-    if (w + 1 < W && woff[w + 1] <= g) w = candidate_warp(woff, W, g);
-    return cand[(long long)w * region + (g - woff[w])];
-}
-
-// Candidate filter, once per list build: keeps, in order, the region candidates of one
+// Candidate filter, once per list build: keeps, in order, the candidates of one
 // instance whose certified distance lower bound at the build does not exceed the pads plus
 // `reach` (2 sqrt(3) skin: two endpoints that each move at most skin per axis close a gap by
 // at most that).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
 // counts): the kept candidates, compacted.
 template <int pass>
-__global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf, int region,
-                                                   int W, const uint2* __restrict__ cand,
-                                                   const uint32_t* __restrict__ woff, float reach,
+__global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf,
+                                                   long long cand_cap, const uint2* __restrict__ cand,
+                                                   const uint32_t* __restrict__ ncand, float reach,
                                                    uint32_t* __restrict__ fbits, uint32_t* __restrict__ fcount,
                                                    const uint32_t* __restrict__ foff, uint2* __restrict__ cand2,
                                                    const uint32_t* __restrict__ gate) {
     if (!*gate) return;
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    const uint32_t total = woff[W];
+    const uint32_t total = uint32_t(min((long long)*ncand, cand_cap));
     const long long nchunk = (total + 31) / 32;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
@@ -692,11 +680,10 @@ __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, cons
         if constexpr (pass == 1) {
             if (!fbits[ch]) continue;  // warp-uniform
         }
-        const int w0 = candidate_warp(woff, W, uint32_t(ch * 32));
         if constexpr (pass == 0) {
             bool keep = false;
             if (g < total) {
-                const uint2 q = candidate_slot(cand, woff, W, region, g, w0);
+                const uint2 q = cand[g];
                 const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
                 if (t.node_inst[na.x] == t.node_inst[nb.x]) {
                     const DistBounds d = dist_bounds(t, p, xf, q.x, q.y);
@@ -710,7 +697,7 @@ __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, cons
             }
         } else {
             const unsigned m = fbits[ch];
-            if (m & (1u << lane)) cand2[foff[ch] + __popc(m & below)] = candidate_slot(cand, woff, W, region, g, w0);
+            if (m & (1u << lane)) cand2[foff[ch] + __popc(m & below)] = cand[g];
         }
     }
 }
@@ -878,7 +865,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     // candidate list (only when rebuilding)
     (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
     (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
-                                    c.bin_cap, c.grid, c.flags),
+                                    c.bin_cap, c.grid, c.flags, c.ncand),
      note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
                                                  c.count, skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
@@ -888,26 +875,24 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s, gate);
     (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted, gate),
      note_launches(1));
-    // occupied bins, then candidates into per-warp regions
+    // occupied bins, then the candidate list
     (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, gate), note_launches(1));
     exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s, gate);
     (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
     const uint32_t* nocc = c.boffset + c.bin_cap;
-    const int W = c.pair_blocks * kPairWarps;
     if (pairs_begin) cudaEventRecord(pairs_begin, s);
     (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted,
-                                                c.rec, c.region, c.cand, c.wcount, c.wcap, c.flags),
+                                                c.rec, c.cand_cap, c.cand, c.ncand, c.flags),
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);
-    exclusive_scan_u32(c.wcap, c.woff, W, c.scan_tmp, s, gate);
     // filtered list (only when rebuilding)
-    const long long chunks = (long long)W * c.region / 32;
+    const long long chunks = c.cand_cap / 32;
     const float reach = skin > 0.f ? 3.4642f * skin : 0.f;  // >= 2 sqrt(3) skin
-    (k_filter<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.region, W, c.cand, c.woff, reach, c.fbits, c.fcount,
-                                                c.foff, c.cand2, gate), note_launches(1));
-    exclusive_scan_u32(c.fcount, c.foff, chunks, c.scan_tmp, s, gate, c.woff + W, 31, 5);
-    (k_filter<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.region, W, c.cand, c.woff, reach, c.fbits, c.fcount,
-                                                c.foff, c.cand2, gate), note_launches(1));
+    (k_filter<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.cand_cap, c.cand, c.ncand, reach, c.fbits,
+                                                c.fcount, c.foff, c.cand2, gate), note_launches(1));
+    exclusive_scan_u32(c.fcount, c.foff, chunks, c.scan_tmp, s, gate, c.ncand, 31, 5);
+    (k_filter<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.cand_cap, c.cand, c.ncand, reach, c.fbits,
+                                                c.fcount, c.foff, c.cand2, gate), note_launches(1));
     (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
     // narrow phase over the filtered list: hit bits and counts per chunk, scan, contacts
     const uint32_t* nkept = c.foff + chunks;

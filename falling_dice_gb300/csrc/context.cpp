@@ -279,7 +279,7 @@ struct mcg_ctx {
     int pair_blocks_for(long long shapes) const {
         return pair_blocks_set > 0 ? pair_blocks_set : contact_pair_blocks(shapes);
     }
-    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, int region) {
+    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, long long cand_cap) {
         drop_graphs();
         contact_mem.release();
         const long long S = (long long)N + B;
@@ -303,14 +303,11 @@ struct mcg_ctx {
         c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.occ = contact_mem.get<uint32_t>(size_t(bin_cap));
         c.pair_blocks = pair_blocks_for(S);
-        const long long W = (long long)c.pair_blocks * 8;
-        c.region = std::max(32, (region + 31) / 32 * 32);
-        c.cand = contact_mem.get<uint2>(size_t(W * c.region));
-        c.wcount = contact_mem.get<uint32_t>(size_t(W));
-        c.wcap = contact_mem.get<uint32_t>(size_t(W + 1));
-        c.woff = contact_mem.get<uint32_t>(size_t(W + 1));
-        const long long chunks = W * c.region / 32;
-        c.cand2 = contact_mem.get<uint2>(size_t(W * c.region));
+        c.cand_cap = std::max<long long>(1024, (cand_cap + 31) / 32 * 32);
+        c.cand = contact_mem.get<uint2>(size_t(c.cand_cap));
+        c.ncand = contact_mem.get<uint32_t>(1);
+        const long long chunks = c.cand_cap / 32;
+        c.cand2 = contact_mem.get<uint2>(size_t(c.cand_cap));
         c.fbits = contact_mem.get<uint32_t>(size_t(chunks));
         c.fcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.foff = contact_mem.get<uint32_t>(size_t(chunks + 1));
@@ -330,34 +327,29 @@ struct mcg_ctx {
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, W + 1, chunks + 1}));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.ncand, 0, sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
-    long long contact_chunks() const { return (long long)cb.pair_blocks * 8 * cb.region / 32; }
+    long long contact_chunks() const { return cb.cand_cap / 32; }
 
     // Grows whatever the last evaluation overflowed; false when nothing did.
     bool grow_contacts(int flags) {
         if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan | kOverCandidates))) return false;
         const long long S = (long long)N + B;
-        const long long W = (long long)cb.pair_blocks * 8;
-        uint32_t need[2] = {0, 0};
+        uint32_t need[3] = {0, 0, 0};
         int grid[16];
-        std::vector<uint32_t> wc(static_cast<size_t>(W));
         ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(&need[1], cb.hoff + contact_chunks(), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
            "copy");
+        ck(cudaMemcpyAsync(&need[2], cb.ncand, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
-        ck(cudaMemcpyAsync(wc.data(), cb.wcount, size_t(W) * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
-        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap;
-        int region = cb.region;
-        if (flags & kOverCandidates) {
-            const long long mx = *std::max_element(wc.begin(), wc.end());
-            region = int(std::min<long long>(std::max<long long>(region, mx + mx / 4 + 32), 1LL << 26));
-        }
+        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap, kcap = cb.cand_cap;
+        if (flags & kOverCandidates) kcap = std::max(kcap, (long long)need[2] + need[2] / 4 + 1024);
         if (flags & kOverSpan) broad_cell *= 2;
         if (flags & kOverEntries) ecap = std::max(ecap, (long long)need[0] + need[0] / 4 + 1024);
         if (flags & kOverContacts) ccap = std::max(ccap, (long long)need[1] + need[1] / 4 + 1024);
@@ -366,7 +358,7 @@ struct mcg_ctx {
             if (want <= (1LL << 28)) bcap = std::max(bcap, want);
             else broad_cell *= 2;  // a huge extent: coarser cells instead of more bins
         }
-        alloc_contacts(ecap, ccap, bcap, region);
+        alloc_contacts(ecap, ccap, bcap, kcap);
         return true;
     }
 
@@ -1372,7 +1364,8 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
         // row-major bins when the Morton range does not fit or is mostly empty
         if ((1LL << bits) < dmax || bin_cap > 4 * dense) bin_cap = std::min(dense, 1LL << 28);
-        c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap, 1024);
+        c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap,
+                          std::max<long long>(4 * S, 4096));
     }
     // solver vectors
     DevArena& Q = c->solver_mem;
@@ -1789,9 +1782,8 @@ int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, in
             throw Fail(MCG_ERR_INVALID, "capacities must be non-negative and bins at most 2^28");
         const long long lo = 4096;
         c->sync();
-        const long long W = (long long)c->pair_blocks_for((long long)c->N + c->B) * 8;
         c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
-                          std::max<long long>(bins, lo), int(std::min<long long>((candidates + W - 1) / W, 1LL << 26)));
+                          std::max<long long>(bins, lo), std::max<long long>(candidates, lo));
     });
 }
 
@@ -1811,10 +1803,9 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
         need_topo(c);
         if (!out5) throw Fail(MCG_ERR_INVALID, "null output");
         const long long S = (long long)c->N + c->B;
-        const long long W = (long long)c->cb.pair_blocks * 8;
         d2h(c->hp.u32, c->cb.offset + S, 1, c->stream);
         d2h(c->hp.u32 + 1, c->cb.boffset + c->cb.bin_cap, 1, c->stream);
-        d2h(c->hp.u32 + 2, c->cb.woff + W, 1, c->stream);
+        d2h(c->hp.u32 + 2, c->cb.ncand, 1, c->stream);
         d2h(c->hp.u32 + 3, c->cb.foff + c->contact_chunks(), 1, c->stream);
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
@@ -1828,7 +1819,7 @@ int mcg_set_contact_cell(mcg_ctx* c, double cell) {
         if (!(cell >= 0) || cell > 1e3) throw Fail(MCG_ERR_INVALID, "cell must be a length >= 0 (m)");
         c->broad_cell = cell > 0 ? cell : c->default_cell();
         c->sync();
-        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.region);
+        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
     });
 }
 
@@ -1848,7 +1839,6 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         const float skin = c->contact_skin;
         c->contact_skin = 0.f;  // time full builds
         const long long S = (long long)c->N + c->B;
-        const long long total_region = (long long)c->cb.pair_blocks * 8 * c->cb.region;
         std::vector<int> blocks{0};
         for (int b : {152, 304, 608, 1216})
             if (b != contact_pair_blocks(S) && (long long)b * 8 * 32 <= std::max<long long>(S, 8 * 32)) blocks.push_back(b);
@@ -1867,9 +1857,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
                 for (int b : blocks) {
                     c->broad_cell = scale * cell0;
                     c->pair_blocks_set = b;
-                    const long long W = (long long)c->pair_blocks_for(S) * 8;
-                    c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap,
-                                      int(std::min<long long>((total_region + W - 1) / W, 1LL << 26)));
+                    c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
                     const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);  // sizes the buffers
                     for (int i = 0; i < c->I; i++) e[size_t(i)] = o[i].energy;
                     d2h(g.data(), c->d_grad, n, s);
@@ -1905,9 +1893,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         c->contact_skin = skin;
         c->broad_cell = best.cell;
         c->pair_blocks_set = best.blocks;
-        const long long W = (long long)c->pair_blocks_for(S) * 8;
-        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap,
-                          int(std::min<long long>((total_region + W - 1) / W, 1LL << 26)));
+        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
         c->sync();
         if (out) *out = mcg_tuning{best.cell, c->pair_blocks_for(S), tried, best.ms, ms_default};
     });

@@ -132,16 +132,14 @@ struct ContactBufs {
     uint32_t* bcount;       // [bin_cap+1] 1 where a bin holds two or more entries
     uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = occupied bins
     uint32_t* occ;          // [bin_cap] occupied bins in bin order
-    // narrow-phase candidates: warp w of the pair grid owns cand[w * region, (w + 1) * region)
-    int pair_blocks;        // blocks of the pair and narrow-phase grids (8 warps each)
-    int region;             // candidate slots per warp, a multiple of 32
-    uint2* cand;            // [warps * region] (lower shape, higher shape)
-    uint32_t* wcount;       // [warps] candidates found per warp (may exceed region)
-    uint32_t* wcap;         // [warps + 1] the same capped at region
-    uint32_t* woff;         // [warps + 1] scan of wcap: warp w's candidates are [woff[w], woff[w + 1])
+    // narrow-phase candidates: one flat list, appended by the pair grid's warps in chunks
+    int pair_blocks;        // blocks of the pair grid (8 warps each)
+    long long cand_cap;     // candidate slots, a multiple of 32
+    uint2* cand;            // [cand_cap] (lower shape, higher shape)
+    uint32_t* ncand;        // [1] candidates found by the last build (may exceed cand_cap)
     // filtered candidates (the ones that can reach contact before the next build), in order
-    uint2* cand2;           // [warps * region]
-    uint32_t* fbits;        // [chunks] keep bit per region candidate (chunks = warps * region / 32)
+    uint2* cand2;           // [cand_cap]
+    uint32_t* fbits;        // [chunks] keep bit per candidate (chunks = cand_cap / 32)
     uint32_t* fcount;       // [chunks + 1] kept per chunk
     uint32_t* foff;         // [chunks + 1] scan of fcount; foff[chunks] = filtered list length
     // narrow phase, per chunk of 32 consecutive filtered candidates

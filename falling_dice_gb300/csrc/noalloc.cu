@@ -97,14 +97,11 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.boffset = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.occ = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * 4));
     c.pair_blocks = contact_pair_blocks(S);
-    const long long W = (long long)c.pair_blocks * 8;
-    c.region = int((kNoAllocCandidates / W + 31) / 32 * 32);
-    c.cand = reinterpret_cast<uint2*>(take(size_t(W * c.region) * sizeof(uint2)));
-    c.wcount = reinterpret_cast<uint32_t*>(take(size_t(W) * 4));
-    c.wcap = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
-    c.woff = reinterpret_cast<uint32_t*>(take(size_t(W + 1) * 4));
-    const long long chunks = W * c.region / 32;
-    c.cand2 = reinterpret_cast<uint2*>(take(size_t(W * c.region) * sizeof(uint2)));
+    c.cand_cap = kNoAllocCandidates;
+    c.cand = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
+    c.ncand = reinterpret_cast<uint32_t*>(take(4));
+    const long long chunks = kNoAllocCandidates / 32;
+    c.cand2 = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
     c.fbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
     c.fcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.foff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));

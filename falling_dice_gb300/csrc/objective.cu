@@ -26,7 +26,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
                                                   double4_32a* __restrict__ M4, float4* __restrict__ xf_lo,
                                                   float4* __restrict__ xf_hi, double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[kBlock / 32];
+    __shared__ double smx[6 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;  // block-uniform
     const int i = mp.i;
@@ -69,8 +69,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
         mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
     }
     block_sum<3>(acc, sm);
-#pragma unroll
-    for (int k = 0; k < 6; k++) mx[k] = block_max(mx[k], smx);
+    block_max_n<6>(mx, smx);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
@@ -85,7 +84,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
 __global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __restrict__ part,
                                                    double* __restrict__ cen) {
     __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[kBlock / 32];
+    __shared__ double smx[6 * (kBlock / 32)];
     const int inst = blockIdx.x;
     int k0 = 0, k1 = t.n_nblk;
     if (inst < t.I) {
@@ -96,6 +95,7 @@ __global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __re
     double acc[3] = {0, 0, 0};
     const double ninf = __longlong_as_double(0xfff0000000000000LL);
     double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+#pragma unroll 4
     for (int k = k0 + int(threadIdx.x); k < k1; k += blockDim.x) {
         const double* q = part + 9 * size_t(k);
         acc[0] += q[0]; acc[1] += q[1]; acc[2] += q[2];
@@ -103,8 +103,7 @@ __global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __re
         for (int j = 0; j < 6; j++) mx[j] = fmax(mx[j], q[3 + j]);
     }
     block_sum<3>(acc, sm);
-#pragma unroll
-    for (int j = 0; j < 6; j++) mx[j] = block_max(mx[j], smx);
+    block_max_n<6>(mx, smx);
     if (threadIdx.x == 0) {
         double* c = cen + 9 * size_t(inst);
         if (inst < t.I) {
@@ -338,7 +337,10 @@ __device__ __forceinline__ void add_contact_item(const ContactBufs& c, const Phy
 template <bool F32>
 __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, int i, d3& gx, d3& gr) {
     const int k0 = t.inc_start[i], k1 = t.inc_start[i + 1];
+    // unrolled so that the loads of several incident beams are in flight together; the
+    // additions keep their order
     if (!F32) {
+#pragma unroll 4
         for (int k = k0; k < k1; k++) {
             const int v = t.inc[k];
             const double* s = ((v & 1) ? e.slotB : e.slotA) + 6 * size_t(v >> 1);
@@ -347,6 +349,7 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
         }
     } else {
         float hi[6] = {0, 0, 0, 0, 0, 0}, lo[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll 4
         for (int k = k0; k < k1; k++) {
             const int v = t.inc[k];
             const float* s = ((v & 1) ? e.slotBf : e.slotAf) + 6 * size_t(v >> 1);
@@ -366,7 +369,7 @@ template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
     __shared__ double sm[6 * (kBlock / 32)];
-    __shared__ double smx[kBlock / 32];
+    __shared__ double smx[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
     const int i = mp.i;
@@ -430,12 +433,12 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         }
     }
     block_sum<6>(acc, sm);
-    pen_max = block_max(pen_max, smx);
-    gmax = block_max(gmax, smx);
+    double m2[2] = {pen_max, gmax};
+    block_max_n<2>(m2, smx);
     if (threadIdx.x == 0) {
         double* q = e.part_node + kNodeParts * size_t(blockIdx.x);
-        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = pen_max; q[4] = acc[3]; q[5] = acc[4];
-        q[6] = acc[5]; q[7] = gmax;
+        q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = m2[0]; q[4] = acc[3]; q[5] = acc[4];
+        q[6] = acc[5]; q[7] = m2[1];
     }
 }
 
@@ -445,16 +448,18 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, co
                                                      const double* __restrict__ cen,
                                                      const uint32_t* __restrict__ flags, EvalOut* out_all) {
     __shared__ double sm[6 * (kBlock / 32)];
-    __shared__ double smx[kBlock / 32];
+    __shared__ double smx[2 * (kBlock / 32)];
     const int inst = blockIdx.x;
     if (!t.active[inst]) return;
     const int4 r = t.irange[inst];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
     double cacc[3] = {0, 0, 0};          // self-contact E, contacts (platen and self), |g|^2
     double pmax = 0, gmax = 0;
+#pragma unroll 8
     for (int k = r.z + int(threadIdx.x); k < r.w; k += blockDim.x) {
         acc[0] += pbeam[3 * k]; acc[1] += pbeam[3 * k + 1]; acc[2] += pbeam[3 * k + 2];
     }
+#pragma unroll 4
     for (int k = r.x + int(threadIdx.x); k < r.y; k += blockDim.x) {
         const double* q = pnode + kNodeParts * size_t(k);
         acc[3] += q[0]; acc[4] += q[1]; acc[5] += q[2];
@@ -466,8 +471,10 @@ __global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, co
     }
     block_sum<6>(acc, sm);
     block_sum<3>(cacc, sm);
-    pmax = block_max(pmax, smx);
-    gmax = block_max(gmax, smx);
+    double m2[2] = {pmax, gmax};
+    block_max_n<2>(m2, smx);
+    pmax = m2[0];
+    gmax = m2[1];
     if (threadIdx.x == 0) {
         const double* c = cen + 9 * size_t(inst);
         const double center = .5 * p.centering * (sqr(c[0]) + sqr(c[2]));

@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
                                                         float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
                                                         double* __restrict__ part) {
     __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[kBlock / 32];
+    __shared__ double smx[6 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
     const int i = mp.i;
@@ -190,11 +190,10 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
             sv = 0.5f + th2 * (-1.f / 48.f + th2 * (1.f / 3840.f));
         } else {
             const float th = sqrtf(th2);
-            float s4 = sinf(0.25f * th);
-            float sh, ch;
-            sincosf(0.5f * th, &sh, &ch);
+            float s4, c4;  // sin, cos of th/4: cos(th/2) - 1 = -2 s4^2, sin(th/2) = 2 s4 c4
+            sincosf(0.25f * th, &s4, &c4);
             wm1 = -2.f * s4 * s4;
-            sv = sh / th;
+            sv = 2.f * s4 * c4 / th;
         }
         Ei[i] = make_float4(wm1, r[0] * sv, r[1] * sv, r[2] * sv);
         const double xx = bx[3 * size_t(i)] + double(tr[0]);
@@ -211,8 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
         mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
     }
     block_sum<3>(acc, sm);
-#pragma unroll
-    for (int k = 0; k < 6; k++) mx[k] = block_max(mx[k], smx);
+    block_max_n<6>(mx, smx);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
