@@ -123,15 +123,29 @@ __device__ __forceinline__ d3 mrot_t(const m3& m, d3 v) {
 
 // ---- deterministic reductions ------------------------------------------------------------
 // Fixed shuffle tree inside a warp, fixed order across warps: the same inputs in the same
-// threads always give the same bits.
+// threads always give the same bits.  The warp results are complete in lane 0 only; at
+// each level only the lanes whose sums lane 0 still needs add (the FP64 pipe is narrow).
 __device__ __forceinline__ double warp_sum(double v) {
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane < o) v += y;
+    }
     return v;
 }
 __device__ __forceinline__ double warp_max(double v) {
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane < o) v = fmax(v, y);
+    }
+    return v;
+}
+__device__ __forceinline__ float warp_max_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
     return v;
 }
 __device__ __forceinline__ long long warp_sum_ll(long long v) {
@@ -161,6 +175,31 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* smem) {
     __syncthreads();
 }
 
+// Sums NV values per thread over the block into thread 0 with few FP64 warp instructions
+// (GB300's FP64 pipe is narrow): the values go through shared memory, warp w reduces values
+// w, w + 8, ...: lane l adds entries l, l + 32, ... in order, then the warp's shuffle tree.
+// `smem` needs NV * blockDim.x doubles.  blockDim.x must be a multiple of 32.
+template <int NV>
+__device__ __forceinline__ void block_sum_t(double (&v)[NV], double* smem) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) smem[k * nt + tid] = v[k];
+    __syncthreads();
+    for (int k = warp; k < NV; k += nw) {
+        const double* a = smem + k * nt;
+        double s = a[lane];
+        for (int j = lane + 32; j < nt; j += 32) s += a[j];
+        s = warp_sum(s);
+        __syncwarp();
+        if (lane == 0) smem[k * nt] = s;
+    }
+    __syncthreads();
+    if (tid == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] = smem[k * nt];
+    __syncthreads();
+}
+
 // NV maxima over the block into thread 0, one barrier pair for all of them; smem holds
 // NV * (blockDim.x / 32) doubles.
 template <int NV>
@@ -177,6 +216,27 @@ __device__ __forceinline__ void block_max_n(double (&v)[NV], double* smem) {
         for (int k = 0; k < NV; k++) {
             double m = smem[k * nw];
             for (int w = 1; w < nw; w++) m = fmax(m, smem[k * nw + w]);
+            v[k] = m;
+        }
+    __syncthreads();
+}
+
+// The same in single precision (fmaxf skips NaN like fmax); smem holds NV * (blockDim.x / 32)
+// floats.
+template <int NV>
+__device__ __forceinline__ void block_max_nf(float (&v)[NV], float* smem) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) v[k] = warp_max_f(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) smem[k * nw + warp] = v[k];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            float m = smem[k * nw];
+            for (int w = 1; w < nw; w++) m = fmaxf(m, smem[k * nw + w]);
             v[k] = m;
         }
     __syncthreads();

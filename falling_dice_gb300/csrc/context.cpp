@@ -1306,6 +1306,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     e.part_state = V.get<double>(9 * size_t(T.n_nblk));
     e.part_beam = V.get<double>(3 * size_t(std::max(T.n_bblk, 1)));
     e.part_node = V.get<double>(kNodeParts * size_t(T.n_nblk));
+    e.part_fin = V.get<double>(size_t(kFinPartDoubles) * size_t(I));
     e.cen = V.get<double>(9 * size_t(I + 1));
     e.tops = V.get<double>(size_t(I));
     e.out = V.get<EvalOut>(size_t(I));

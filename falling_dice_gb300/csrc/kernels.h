@@ -167,6 +167,7 @@ struct ContactBufs {
 // per node block: gravity E, platen E, reaction, max penetration, contacts, self-contact E,
 // sum of squared free gradient entries, max |free gradient entry|
 constexpr int kNodeParts = 8;
+constexpr int kFinPartDoubles = 32 * 11;  // per instance: 32 first-stage blocks x 11 totals
 
 struct EvalBufs {
     double4_32a* x;             // [N]
@@ -179,6 +180,7 @@ struct EvalBufs {
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
     double* part_beam;      // [3 * nb_beams]
     double* part_node;      // [kNodeParts * nb_nodes]
+    double* part_fin;       // [I * kFinPartDoubles] first-stage totals of the finalize
     double* cen;            // [9 (I + 1)] per instance mean, min, max of the node positions (min/max
                             //   in the contact grid's frame); then min/max over all instances
     double* tops;           // [I] platen height per instance

@@ -25,14 +25,17 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
                                                   double4_32a* __restrict__ x4, double4_32a* __restrict__ R4,
                                                   double4_32a* __restrict__ M4, float4* __restrict__ xf_lo,
                                                   float4* __restrict__ xf_hi, double* __restrict__ part) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[6 * (kBlock / 32)];
+    __shared__ double sm[3 * kBlock];
+    __shared__ float smx[4 * (kBlock / 32)];
+    __shared__ double smy[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;  // block-uniform
     const int i = mp.i;
     double acc[3] = {0, 0, 0};
-    const double ninf = __longlong_as_double(0xfff0000000000000LL);
-    double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+    const float ninf = __int_as_float(0xff800000);
+    float mx[4] = {ninf, ninf, ninf, ninf};  // -min x, -min z, max x, max z (grid frame, FP32)
+    const double ninfd = __longlong_as_double(0xfff0000000000000LL);
+    double my[2] = {ninfd, ninfd};  // -min y, max y (FP64: the permanent set reads them)
     if (mp.valid) {
         const double* zi = z + 6 * size_t(i);
         const uint8_t* li = t.locked + 6 * size_t(i);
@@ -54,27 +57,31 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
         // single-precision bounds of the position in the contact grid's frame (the
         // instance's offset added with outward rounding)
         const float2 o = t.off[mp.inst];
-        xf_lo[i] = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
-                               __fadd_rd(__double2float_rd(xz), o.y), 0.f);
-        xf_hi[i] = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
-                               __fadd_ru(__double2float_ru(xz), o.y), 0.f);
+        const float4 lo = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
+                                      __fadd_rd(__double2float_rd(xz), o.y), 0.f);
+        const float4 hi = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
+                                      __fadd_ru(__double2float_ru(xz), o.y), 0.f);
+        xf_lo[i] = lo;
+        xf_hi[i] = hi;
         R4[i] = make_double4_32a(R.w, R.x, R.y, R.z);
         const m3 M = quat_matrix(R);
         M4[3 * size_t(i)] = make_double4_32a(M.r0.x, M.r0.y, M.r0.z, 0.0);
         M4[3 * size_t(i) + 1] = make_double4_32a(M.r1.x, M.r1.y, M.r1.z, 0.0);
         M4[3 * size_t(i) + 2] = make_double4_32a(M.r2.x, M.r2.y, M.r2.z, 0.0);
         acc[0] = xx; acc[1] = xy; acc[2] = xz;
-        // bounding box in the grid's frame; fmin/fmax skip NaN coordinates
-        const double gx = xx + double(o.x), gz = xz + double(o.y);
-        mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
+        // bounding box in the grid's frame: x and z from the outward-rounded bounds (they
+        // contain the FP64 positions), y exact; fmax/fmaxf skip NaN coordinates
+        mx[0] = -lo.x; mx[1] = -lo.z; mx[2] = hi.x; mx[3] = hi.z;
+        my[0] = -xy; my[1] = xy;
     }
-    block_sum<3>(acc, sm);
-    block_max_n<6>(mx, smx);
+    block_sum_t<3>(acc, sm);
+    block_max_nf<4>(mx, smx);
+    block_max_n<2>(my, smy);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
-#pragma unroll
-        for (int k = 0; k < 6; k++) q[3 + k] = mx[k];
+        q[3] = double(mx[0]); q[4] = my[0]; q[5] = double(mx[1]);
+        q[6] = double(mx[2]); q[7] = my[1]; q[8] = double(mx[3]);
     }
 }
 
@@ -368,7 +375,7 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
 template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
-    __shared__ double sm[6 * (kBlock / 32)];
+    __shared__ double sm[6 * kBlock];
     __shared__ double smx[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
@@ -432,7 +439,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
             }
         }
     }
-    block_sum<6>(acc, sm);
+    block_sum_t<6>(acc, sm);
     double m2[2] = {pen_max, gmax};
     block_max_n<2>(m2, smx);
     if (threadIdx.x == 0) {
@@ -443,38 +450,62 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
 }
 
 // ---- totals and the non-finite guard ---------------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, const double* __restrict__ pbeam,
-                                                     const double* __restrict__ pnode,
-                                                     const double* __restrict__ cen,
-                                                     const uint32_t* __restrict__ flags, EvalOut* out_all) {
-    __shared__ double sm[6 * (kBlock / 32)];
+// Two stages, so the FP64 additions spread over many SMs (GB300's FP64 pipe is narrow).
+// Stage 1: block (f, inst) sums the instance's block partials k = first + f + kFinFan j.
+constexpr int kFinFan = 32;
+constexpr int kFinVals = 11;  // beamE, elastic, plastic, gravityE, platenE, reaction, contactE,
+                              // contacts, |g|^2, max penetration, max |g|
+static_assert(kFinPartDoubles == kFinFan * kFinVals, "first-stage totals buffer");
+__global__ void __launch_bounds__(kBlock) k_finalize_parts(DevTopo t, const double* __restrict__ pbeam,
+                                                           const double* __restrict__ pnode,
+                                                           double* __restrict__ fpart) {
+    __shared__ double sm[9 * kBlock];
     __shared__ double smx[2 * (kBlock / 32)];
-    const int inst = blockIdx.x;
+    const int inst = blockIdx.y, f = blockIdx.x;
     if (!t.active[inst]) return;
     const int4 r = t.irange[inst];
     double acc[6] = {0, 0, 0, 0, 0, 0};  // beamE, elastic, plastic, gravityE, platenE, reaction
     double cacc[3] = {0, 0, 0};          // self-contact E, contacts (platen and self), |g|^2
-    double pmax = 0, gmax = 0;
-#pragma unroll 8
-    for (int k = r.z + int(threadIdx.x); k < r.w; k += blockDim.x) {
+    double m2[2] = {0, 0};               // max penetration, max |g|
+    for (int k = r.z + f + kFinFan * int(threadIdx.x); k < r.w; k += kFinFan * int(blockDim.x)) {
         acc[0] += pbeam[3 * k]; acc[1] += pbeam[3 * k + 1]; acc[2] += pbeam[3 * k + 2];
     }
-#pragma unroll 4
-    for (int k = r.x + int(threadIdx.x); k < r.y; k += blockDim.x) {
+    for (int k = r.x + f + kFinFan * int(threadIdx.x); k < r.y; k += kFinFan * int(blockDim.x)) {
         const double* q = pnode + kNodeParts * size_t(k);
         acc[3] += q[0]; acc[4] += q[1]; acc[5] += q[2];
-        pmax = fmax(pmax, q[3]);
+        m2[0] = fmax(m2[0], q[3]);
         cacc[1] += q[4];
         cacc[0] += q[5];
         cacc[2] += q[6];
-        gmax = fmax(gmax, q[7]);
+        m2[1] = fmax(m2[1], q[7]);
     }
-    block_sum<6>(acc, sm);
-    block_sum<3>(cacc, sm);
-    double m2[2] = {pmax, gmax};
+    double all[9] = {acc[0], acc[1], acc[2], acc[3], acc[4], acc[5], cacc[0], cacc[1], cacc[2]};
+    block_sum_t<9>(all, sm);
     block_max_n<2>(m2, smx);
-    pmax = m2[0];
-    gmax = m2[1];
+    if (threadIdx.x == 0) {
+        double* o = fpart + kFinVals * (size_t(inst) * kFinFan + f);
+        for (int k = 0; k < 9; k++) o[k] = all[k];
+        o[9] = m2[0]; o[10] = m2[1];
+    }
+}
+
+// Stage 2, one block per instance: the kFinFan stage-1 results in order, the energy in the
+// reference's group order, diagnostics, non-finite guard.
+__global__ void __launch_bounds__(kBlock) k_finalize(DevTopo t, PhysParams p, const double* __restrict__ fpart,
+                                                     const double* __restrict__ cen,
+                                                     const uint32_t* __restrict__ flags, EvalOut* out_all) {
+    static_assert(kFinFan == 32, "one stage-1 result per lane");
+    const int inst = blockIdx.x;
+    if (!t.active[inst]) return;
+    const double* q = fpart + kFinVals * (size_t(inst) * kFinFan + threadIdx.x);
+    double acc[6], cacc[3];  // beamE, elastic, plastic, gravityE, platenE, reaction; contactE,
+                             // contacts, |g|^2
+#pragma unroll
+    for (int k = 0; k < 6; k++) acc[k] = warp_sum(q[k]);
+#pragma unroll
+    for (int k = 0; k < 3; k++) cacc[k] = warp_sum(q[6 + k]);
+    const double pmax = warp_max(q[9]), gmax = warp_max(q[10]);
+    if (threadIdx.x != 0) return;
     if (threadIdx.x == 0) {
         const double* c = cen + 9 * size_t(inst);
         const double center = .5 * p.centering * (sqr(c[0]) + sqr(c[2]));
@@ -645,9 +676,10 @@ void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBuf
 
 void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
                      cudaStream_t s) {
-    k_finalize<<<t.I, kBlock, 0, s>>>(t, p, e.part_beam, e.part_node, e.cen, c ? c->flags : nullptr, e.out);
+    k_finalize_parts<<<dim3(kFinFan, t.I), kBlock, 0, s>>>(t, e.part_beam, e.part_node, e.part_fin);
+    k_finalize<<<t.I, 32, 0, s>>>(t, p, e.part_fin, e.cen, c ? c->flags : nullptr, e.out);
     k_zero_if_nonfinite<<<t.n_nblk, kBlock, 0, s>>>(t, e.out, grad);
-    note_launches(2);
+    note_launches(3);
 }
 
 }  // namespace mcg

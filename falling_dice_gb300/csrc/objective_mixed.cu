@@ -165,14 +165,17 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
                                                         float4* __restrict__ Ei, double4_32a* __restrict__ x4,
                                                         float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
                                                         double* __restrict__ part) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[6 * (kBlock / 32)];
+    __shared__ double sm[3 * kBlock];
+    __shared__ float smx[4 * (kBlock / 32)];
+    __shared__ double smy[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
     const int i = mp.i;
     double acc[3] = {0, 0, 0};
-    const double ninf = __longlong_as_double(0xfff0000000000000LL);
-    double mx[6] = {ninf, ninf, ninf, ninf, ninf, ninf};
+    const float ninf = __int_as_float(0xff800000);
+    float mx[4] = {ninf, ninf, ninf, ninf};  // -min x, -min z, max x, max z (grid frame, FP32)
+    const double ninfd = __longlong_as_double(0xfff0000000000000LL);
+    double my[2] = {ninfd, ninfd};  // -min y, max y (FP64: the permanent set reads them)
     if (mp.valid) {
         const double* zi = z + 6 * size_t(i);
         const uint8_t* li = t.locked + 6 * size_t(i);
@@ -201,21 +204,26 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
         const double xz = bx[3 * size_t(i) + 2] + double(tr[2]);
         x4[i] = make_double4_32a(xx, xy, xz, 0.0);
         const float2 o = t.off[mp.inst];
-        xf_lo[i] = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
-                               __fadd_rd(__double2float_rd(xz), o.y), 0.f);
-        xf_hi[i] = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
-                               __fadd_ru(__double2float_ru(xz), o.y), 0.f);
+        const float4 lo = make_float4(__fadd_rd(__double2float_rd(xx), o.x), __double2float_rd(xy),
+                                      __fadd_rd(__double2float_rd(xz), o.y), 0.f);
+        const float4 hi = make_float4(__fadd_ru(__double2float_ru(xx), o.x), __double2float_ru(xy),
+                                      __fadd_ru(__double2float_ru(xz), o.y), 0.f);
+        xf_lo[i] = lo;
+        xf_hi[i] = hi;
         acc[0] = xx; acc[1] = xy; acc[2] = xz;
-        const double gx = xx + double(o.x), gz = xz + double(o.y);
-        mx[0] = -gx; mx[1] = -xy; mx[2] = -gz; mx[3] = gx; mx[4] = xy; mx[5] = gz;
+        // bounding box in the grid's frame: x and z from the outward-rounded bounds (they
+        // contain the FP64 positions), y exact; fmax/fmaxf skip NaN coordinates
+        mx[0] = -lo.x; mx[1] = -lo.z; mx[2] = hi.x; mx[3] = hi.z;
+        my[0] = -xy; my[1] = xy;
     }
-    block_sum<3>(acc, sm);
-    block_max_n<6>(mx, smx);
+    block_sum_t<3>(acc, sm);
+    block_max_nf<4>(mx, smx);
+    block_max_n<2>(my, smy);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
-#pragma unroll
-        for (int k = 0; k < 6; k++) q[3 + k] = mx[k];
+        q[3] = double(mx[0]); q[4] = my[0]; q[5] = double(mx[1]);
+        q[6] = double(mx[2]); q[7] = my[1]; q[8] = double(mx[3]);
     }
 }
 
