@@ -200,6 +200,28 @@ __device__ __forceinline__ void block_sum_t(double (&v)[NV], double* smem) {
     __syncthreads();
 }
 
+// The same for maxima (fmax skips NaN); `smem` needs NV * blockDim.x doubles.
+template <int NV>
+__device__ __forceinline__ void block_max_t(double (&v)[NV], double* smem) {
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) smem[k * nt + tid] = v[k];
+    __syncthreads();
+    for (int k = warp; k < NV; k += nw) {
+        const double* a = smem + k * nt;
+        double m = a[lane];
+        for (int j = lane + 32; j < nt; j += 32) m = fmax(m, a[j]);
+        m = warp_max(m);
+        __syncwarp();
+        if (lane == 0) smem[k * nt] = m;
+    }
+    __syncthreads();
+    if (tid == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) v[k] = smem[k * nt];
+    __syncthreads();
+}
+
 // NV maxima over the block into thread 0, one barrier pair for all of them; smem holds
 // NV * (blockDim.x / 32) doubles.
 template <int NV>

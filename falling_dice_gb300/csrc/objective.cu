@@ -27,7 +27,6 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
                                                   float4* __restrict__ xf_hi, double* __restrict__ part) {
     __shared__ double sm[3 * kBlock];
     __shared__ float smx[4 * (kBlock / 32)];
-    __shared__ double smy[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;  // block-uniform
     const int i = mp.i;
@@ -76,7 +75,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
     }
     block_sum_t<3>(acc, sm);
     block_max_nf<4>(mx, smx);
-    block_max_n<2>(my, smy);
+    block_max_t<2>(my, sm);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
@@ -90,8 +89,7 @@ __global__ void __launch_bounds__(kBlock) k_state(DevTopo t, PhysParams p, const
 // block I the minimum and maximum over all instances at cen[9I + 3..8].
 __global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __restrict__ part,
                                                    double* __restrict__ cen) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double smx[6 * (kBlock / 32)];
+    __shared__ double sm[6 * kBlock];
     const int inst = blockIdx.x;
     int k0 = 0, k1 = t.n_nblk;
     if (inst < t.I) {
@@ -109,8 +107,8 @@ __global__ void __launch_bounds__(kBlock) k_center(DevTopo t, const double* __re
 #pragma unroll
         for (int j = 0; j < 6; j++) mx[j] = fmax(mx[j], q[3 + j]);
     }
-    block_sum<3>(acc, sm);
-    block_max_n<6>(mx, smx);
+    block_sum_t<3>(acc, sm);
+    block_max_t<6>(mx, sm);
     if (threadIdx.x == 0) {
         double* c = cen + 9 * size_t(inst);
         if (inst < t.I) {
@@ -376,7 +374,6 @@ template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
     __shared__ double sm[6 * kBlock];
-    __shared__ double smx[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
     const int i = mp.i;
@@ -441,7 +438,7 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
     }
     block_sum_t<6>(acc, sm);
     double m2[2] = {pen_max, gmax};
-    block_max_n<2>(m2, smx);
+    block_max_t<2>(m2, sm);
     if (threadIdx.x == 0) {
         double* q = e.part_node + kNodeParts * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2]; q[3] = m2[0]; q[4] = acc[3]; q[5] = acc[4];
@@ -460,7 +457,6 @@ __global__ void __launch_bounds__(kBlock) k_finalize_parts(DevTopo t, const doub
                                                            const double* __restrict__ pnode,
                                                            double* __restrict__ fpart) {
     __shared__ double sm[9 * kBlock];
-    __shared__ double smx[2 * (kBlock / 32)];
     const int inst = blockIdx.y, f = blockIdx.x;
     if (!t.active[inst]) return;
     const int4 r = t.irange[inst];
@@ -481,7 +477,7 @@ __global__ void __launch_bounds__(kBlock) k_finalize_parts(DevTopo t, const doub
     }
     double all[9] = {acc[0], acc[1], acc[2], acc[3], acc[4], acc[5], cacc[0], cacc[1], cacc[2]};
     block_sum_t<9>(all, sm);
-    block_max_n<2>(m2, smx);
+    block_max_t<2>(m2, sm);
     if (threadIdx.x == 0) {
         double* o = fpart + kFinVals * (size_t(inst) * kFinFan + f);
         for (int k = 0; k < 9; k++) o[k] = all[k];

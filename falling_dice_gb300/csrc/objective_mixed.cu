@@ -64,8 +64,8 @@ struct fsum {
     }
 };
 
-// Warp sum of compensated pairs, finished in FP64 by lane 0.
-__device__ __forceinline__ double warp_sum_comp(float hi, float lo) {
+// Warp sum of compensated pairs (hi, lo) into lane 0, in FP32.
+__device__ __forceinline__ void warp_sum_comp(float& hi, float& lo) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float h2 = __shfl_down_sync(0xffffffffu, hi, o);
@@ -75,25 +75,37 @@ __device__ __forceinline__ double warp_sum_comp(float hi, float lo) {
         lo += l2 + ((hi - (s - bp)) + (h2 - bp));
         hi = s;
     }
-    return double(hi) + double(lo);
 }
 
-// Sums NV per-thread FP32 values over the block into thread 0 (FP64 across warps).
+// Sums NV per-thread FP32 values over the block into thread 0: compensated FP32 sums in each
+// warp and across the warps (in warp order), rounded to FP64 once per block -- GB300's FP64
+// pipe is narrow, so no FP64 instruction runs per warp.  smem holds 2 NV (blockDim.x / 32)
+// floats.
 template <int NV>
-__device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[NV], double* smem) {
+__device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[NV], float* smem) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
 #pragma unroll
     for (int k = 0; k < NV; k++) {
-        const double s = warp_sum_comp(v[k], 0.f);
-        if (lane == 0) smem[k * nw + warp] = s;
+        float hi = v[k], lo = 0.f;
+        warp_sum_comp(hi, lo);
+        if (lane == 0) {
+            smem[2 * (k * nw + warp)] = hi;
+            smem[2 * (k * nw + warp) + 1] = lo;
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < NV; k++) {
-            double s = 0;
-            for (int w = 0; w < nw; w++) s += smem[k * nw + w];
-            out[k] = s;
+            float hi = smem[2 * k * nw], lo = smem[2 * k * nw + 1];
+            for (int w = 1; w < nw; w++) {
+                const float h2 = smem[2 * (k * nw + w)], l2 = smem[2 * (k * nw + w) + 1];
+                const float s = hi + h2;
+                const float bp = s - hi;
+                lo += l2 + ((hi - (s - bp)) + (h2 - bp));
+                hi = s;
+            }
+            out[k] = double(hi) + double(lo);
         }
     __syncthreads();
 }
@@ -167,7 +179,6 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
                                                         double* __restrict__ part) {
     __shared__ double sm[3 * kBlock];
     __shared__ float smx[4 * (kBlock / 32)];
-    __shared__ double smy[2 * (kBlock / 32)];
     const MapPos mp = map_pos(t.nblk);
     if (!t.active[mp.inst]) return;
     const int i = mp.i;
@@ -218,7 +229,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
     }
     block_sum_t<3>(acc, sm);
     block_max_nf<4>(mx, smx);
-    block_max_n<2>(my, smy);
+    block_max_t<2>(my, sm);
     if (threadIdx.x == 0) {
         double* q = part + 9 * size_t(blockIdx.x);
         q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
@@ -281,7 +292,7 @@ __global__ void __launch_bounds__(kBlock) k_mixed_constants(DevTopo t, MixedBeam
 __global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
-    __shared__ double sm[3 * (kBlock / 32)];
+    __shared__ float sm[2 * 3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
     const int b = mp.i;
