@@ -258,9 +258,11 @@ __global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __
 // ---- kernels -------------------------------------------------------------------------------
 // Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
 __global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
-                              uint32_t* flags, uint32_t* ncand) {
+                              uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
     if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
-    *ncand = 0;  // the candidate list of this build
+    *ncand = 0;  // the candidate list and entry counts of this build
+    nentries[0] = 0;
+    nentries[1] = 0;
     bool ok = true;
     long long lo[3], dim[3];
     for (int d = 0; d < 3; d++) {
@@ -314,8 +316,8 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
 __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, const float4* __restrict__ xf_lo,
                                                        const float4* __restrict__ xf_hi, const int* __restrict__ grid,
                                                        int4* __restrict__ cell_lo, int4* __restrict__ cell_hi,
-                                                       uint4* __restrict__ rec, uint32_t* __restrict__ count,
-                                                       float skin, uint32_t* __restrict__ flags) {
+                                                       uint4* __restrict__ rec, float skin,
+                                                       uint32_t* __restrict__ flags) {
     const int S = t.N + t.B;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S || !flags[1]) return;
@@ -330,7 +332,6 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
     const bool finite_box = isfinite(lo[0]) && isfinite(lo[1]) && isfinite(lo[2]) && isfinite(hi[0]) &&
                             isfinite(hi[1]) && isfinite(hi[2]);
     if (!grid[7] || !finite_box || !t.active[t.node_inst[nd.x]]) {  // inactive instances take no part
-        count[s] = 0;
         cell_lo[s] = make_int4(0, 0, 0, 0);
         cell_hi[s] = make_int4(-1, -1, -1, 0);
         rec[s] = make_uint4(0, 0, 0, 0);
@@ -358,45 +359,46 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
         n = 0;
         c1[0] = c0[0] - 1;
     }
-    count[s] = uint32_t(n);
     cell_lo[s] = make_int4(c0[0], c0[1], c0[2], 0);
     cell_hi[s] = make_int4(c1[0], c1[1], c1[2], 0);
     rec[s] = make_uint4(q0[0] | (q0[1] << 16), (q1[0] | (q1[1] << 16)) | kGuard2, q0[2] | ((q1[2] | 0x8000u) << 16),
                         pack_cell(c0[0], c0[1], c0[2]));
 }
 
-// Entries of shape s: bin key and rank inside the bin (bin_count counts them).
+// Entries of shape s: one per cell of its range, written straight into the bin's slot that
+// the bin counter hands out.  A bin that fills up keeps counting (kOverEntries, and the
+// largest count in nentries[1] so the host can size bin_slots); the cell entries of the
+// build are counted once per block into nentries[0].
 __global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ grid, const int4* __restrict__ cell_lo,
-                                                 const int4* __restrict__ cell_hi, const uint32_t* __restrict__ offset,
-                                                 long long cap, uint32_t* __restrict__ ekey,
-                                                 uint32_t* __restrict__ erank, uint32_t* __restrict__ bin_count,
-                                                 uint32_t* __restrict__ flags) {
+                                                 const int4* __restrict__ cell_hi, int bin_slots,
+                                                 uint32_t* __restrict__ bin_count, uint32_t* __restrict__ bin_items,
+                                                 uint32_t* __restrict__ nentries, uint32_t* __restrict__ flags) {
+    __shared__ uint32_t block_entries;
+    if (!flags[1]) return;  // grid-uniform
+    if (threadIdx.x == 0) block_entries = 0;
+    __syncthreads();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S || !flags[1]) return;
-    if ((long long)offset[S] > cap) {
-        if (s == 0) atomicOr(flags, uint32_t(kOverEntries));
-        return;
+    uint32_t n = 0;
+    if (s < S) {
+        const int4 lo = cell_lo[s], hi = cell_hi[s];
+        for (int j = lo.y; j <= hi.y; j++)
+            for (int k = lo.z; k <= hi.z; k++)
+                for (int i = lo.x; i <= hi.x; i++) {
+                    const uint32_t b = bin_of(grid, i, j, k);
+                    const uint32_t slot = atomicAdd(&bin_count[b], 1u);
+                    if (slot < uint32_t(bin_slots)) {
+                        bin_items[size_t(b) * size_t(bin_slots) + slot] = uint32_t(s);
+                    } else {
+                        atomicOr(flags, uint32_t(kOverEntries));
+                        atomicMax(nentries + 1, slot + 1);
+                    }
+                    n++;
+                }
     }
-    const int4 lo = cell_lo[s], hi = cell_hi[s];
-    uint32_t o = offset[s];
-    for (int j = lo.y; j <= hi.y; j++)
-        for (int k = lo.z; k <= hi.z; k++)
-            for (int i = lo.x; i <= hi.x; i++) {
-                const uint32_t b = bin_of(grid, i, j, k);
-                ekey[o] = b;
-                erank[o] = atomicAdd(&bin_count[b], 1u);
-                o++;
-            }
-}
-
-__global__ void __launch_bounds__(kBlock) k_scatter(int S, const uint32_t* __restrict__ offset, long long cap,
-                                                    const uint32_t* __restrict__ ekey,
-                                                    const uint32_t* __restrict__ erank,
-                                                    const uint32_t* __restrict__ bin_start,
-                                                    uint32_t* __restrict__ sorted, const uint32_t* __restrict__ gate) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S || !*gate || (long long)offset[S] > cap) return;
-    for (uint32_t o = offset[s]; o < offset[s + 1]; o++) sorted[bin_start[ekey[o]] + erank[o]] = uint32_t(s);
+    const uint32_t wn = __reduce_add_sync(0xffffffffu, n);
+    if ((threadIdx.x & 31) == 0 && wn) atomicAdd(&block_entries, wn);
+    __syncthreads();
+    if (threadIdx.x == 0 && block_entries) atomicAdd(nentries, block_entries);
 }
 
 // One shape as the pair test sees it inside one bin: id with the first-cell flags in the
@@ -467,10 +469,9 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane,
 //            rotation;
 //   larger   pairs by index, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
-                                                      const uint32_t* __restrict__ bin_count,
-                                                      const uint32_t* __restrict__ bin_start,
+                                                      const uint32_t* __restrict__ bin_count, int bin_slots,
                                                       const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
-                                                      const uint32_t* __restrict__ sorted,
+                                                      const uint32_t* __restrict__ bin_items,
                                                       const uint4* __restrict__ rec, long long cand_cap,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
                                                       uint32_t* __restrict__ flags) {
@@ -508,19 +509,19 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         const uint32_t jend = min(jb0 + uint32_t(kPairGrab), nocc);
         for (uint32_t jb = jb0; jb < jend; jb++) {
             const uint32_t b = occ[jb];
-            const int n = int(bin_count[b]);
-            const uint32_t start = bin_start[b];
+            const int n = int(min(bin_count[b], uint32_t(bin_slots)));  // a full bin repeats the build
+            const uint32_t* items = bin_items + size_t(b) * size_t(bin_slots);
             const int3 cc = cell_of(grid, b);
             const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
             if (n <= 32) {
                 PairRec me{};
-                if (lane < n) me = load_rec(t, sorted[start + lane], rec, ccp);
+                if (lane < n) me = load_rec(t, items[lane], rec, ccp);
                 rotate_pairs(me, n, lane, emit);
             } else if (n <= 64) {
                 const int m = n - 32;
-                const PairRec lo = load_rec(t, sorted[start + lane], rec, ccp);
+                const PairRec lo = load_rec(t, items[lane], rec, ccp);
                 PairRec up{};
-                if (lane < m) up = load_rec(t, sorted[start + 32 + lane], rec, ccp);
+                if (lane < m) up = load_rec(t, items[32 + lane], rec, ccp);
                 rotate_pairs(lo, 32, lane, emit);
                 for (int q = 0; q < m; q++) {  // the lower records against upper record q
                     const PairRec o = shfl_rec(up, q);
@@ -542,8 +543,8 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                             row_end += n - 1 - i;
                         }
                         const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                        const PairRec A = load_rec(t, sorted[start + i], rec, ccp);
-                        const PairRec B = load_rec(t, sorted[start + j], rec, ccp);
+                        const PairRec A = load_rec(t, items[i], rec, ccp);
+                        const PairRec B = load_rec(t, items[j], rec, ccp);
                         hit = pair_test(A, B);
                         sa = A.id & kIdMask;
                         sb = B.id & kIdMask;
@@ -865,23 +866,19 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     // candidate list (only when rebuilding)
     (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
     (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
-                                    c.bin_cap, c.grid, c.flags, c.ncand),
+                                    c.bin_cap, c.grid, c.flags, c.ncand, c.nentries),
      note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
-                                                 c.count, skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
-    exclusive_scan_u32(c.count, c.offset, S, c.scan_tmp, s, gate);
-    (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.offset, c.entry_cap, c.ekey, c.erank,
-                                           c.bin_count, c.flags), note_launches(1));
-    exclusive_scan_u32(c.bin_count, c.bin_start, c.bin_cap, c.scan_tmp, s, gate);
-    (k_scatter<<<grid_for(S), kBlock, 0, s>>>(S, c.offset, c.entry_cap, c.ekey, c.erank, c.bin_start, c.sorted, gate),
-     note_launches(1));
+                                                 skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
+    (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.bin_slots, c.bin_count, c.bin_items,
+                                           c.nentries, c.flags), note_launches(1));
     // occupied bins, then the candidate list
     (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, gate), note_launches(1));
     exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s, gate);
     (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
     const uint32_t* nocc = c.boffset + c.bin_cap;
     if (pairs_begin) cudaEventRecord(pairs_begin, s);
-    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_start, c.occ, nocc, c.sorted,
+    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_slots, c.occ, nocc, c.bin_items,
                                                 c.rec, c.cand_cap, c.cand, c.ncand, c.flags),
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);

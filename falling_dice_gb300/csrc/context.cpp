@@ -279,7 +279,8 @@ struct mcg_ctx {
     int pair_blocks_for(long long shapes) const {
         return pair_blocks_set > 0 ? pair_blocks_set : contact_pair_blocks(shapes);
     }
-    void alloc_contacts(long long entry_cap, long long contact_cap, long long bin_cap, long long cand_cap) {
+    // bin_slots: entries a grid bin holds (rounded up to a power of two, at least 8)
+    void alloc_contacts(long long bin_slots, long long contact_cap, long long bin_cap, long long cand_cap) {
         drop_graphs();
         contact_mem.release();
         const long long S = (long long)N + B;
@@ -287,18 +288,16 @@ struct mcg_ctx {
         c.cell_lo = contact_mem.get<int4>(size_t(S));
         c.cell_hi = contact_mem.get<int4>(size_t(S));
         c.rec = contact_mem.get<uint4>(size_t(S));
-        c.count = contact_mem.get<uint32_t>(size_t(S + 1));
-        c.offset = contact_mem.get<uint32_t>(size_t(S + 1));
         c.grid = contact_mem.get<int>(16);
         c.flags = contact_mem.get<uint32_t>(4);
         c.xref = contact_mem.get<float4>(size_t(std::max(N, 1)));
-        c.entry_cap = entry_cap;
-        c.ekey = contact_mem.get<uint32_t>(size_t(entry_cap));
-        c.erank = contact_mem.get<uint32_t>(size_t(entry_cap));
-        c.sorted = contact_mem.get<uint32_t>(size_t(entry_cap));
+        int slots = 8;
+        while (slots < bin_slots && slots < (1 << 20)) slots <<= 1;
+        c.bin_slots = slots;
         c.bin_cap = bin_cap;
         c.bin_count = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
-        c.bin_start = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
+        c.bin_items = contact_mem.get<uint32_t>(size_t(bin_cap) * size_t(slots));
+        c.nentries = contact_mem.get<uint32_t>(2);
         c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.occ = contact_mem.get<uint32_t>(size_t(bin_cap));
@@ -327,10 +326,11 @@ struct mcg_ctx {
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max({S + 1, bin_cap + 1, (long long)N + 1, chunks + 1}));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({bin_cap + 1, (long long)N + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.ncand, 0, sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.nentries, 0, 2 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
@@ -339,26 +339,25 @@ struct mcg_ctx {
     // Grows whatever the last evaluation overflowed; false when nothing did.
     bool grow_contacts(int flags) {
         if (!(flags & (kOverEntries | kOverContacts | kOverBins | kOverSpan | kOverCandidates))) return false;
-        const long long S = (long long)N + B;
         uint32_t need[3] = {0, 0, 0};
         int grid[16];
-        ck(cudaMemcpyAsync(&need[0], cb.offset + S, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
+        ck(cudaMemcpyAsync(&need[0], cb.nentries + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(&need[1], cb.hoff + contact_chunks(), sizeof(uint32_t), cudaMemcpyDeviceToHost, stream),
            "copy");
         ck(cudaMemcpyAsync(&need[2], cb.ncand, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream), "copy");
         ck(cudaMemcpyAsync(grid, cb.grid, sizeof(grid), cudaMemcpyDeviceToHost, stream), "copy");
         sync();
-        long long ecap = cb.entry_cap, ccap = cb.contact_cap, bcap = cb.bin_cap, kcap = cb.cand_cap;
+        long long slots = cb.bin_slots, ccap = cb.contact_cap, bcap = cb.bin_cap, kcap = cb.cand_cap;
         if (flags & kOverCandidates) kcap = std::max(kcap, (long long)need[2] + need[2] / 4 + 1024);
         if (flags & kOverSpan) broad_cell *= 2;
-        if (flags & kOverEntries) ecap = std::max(ecap, (long long)need[0] + need[0] / 4 + 1024);
+        if (flags & kOverEntries) slots = std::max(slots, (long long)need[0] + need[0] / 4);
         if (flags & kOverContacts) ccap = std::max(ccap, (long long)need[1] + need[1] / 4 + 1024);
         if (flags & kOverBins) {
             const long long want = (long long)grid[9] + grid[9] / 4 + 1024;
             if (want <= (1LL << 28)) bcap = std::max(bcap, want);
             else broad_cell *= 2;  // a huge extent: coarser cells instead of more bins
         }
-        alloc_contacts(ecap, ccap, bcap, kcap);
+        alloc_contacts(slots, ccap, bcap, kcap);
         return true;
     }
 
@@ -1365,8 +1364,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         long long bin_cap = std::min(1LL << (3 * bits), 1LL << 27);
         // row-major bins when the Morton range does not fit or is mostly empty
         if ((1LL << bits) < dmax || bin_cap > 4 * dense) bin_cap = std::min(dense, 1LL << 28);
-        c->alloc_contacts(std::max<long long>(8 * S, 4096), std::max<long long>(S / 2, 4096), bin_cap,
-                          std::max<long long>(4 * S, 4096));
+        c->alloc_contacts(64, std::max<long long>(S / 2, 4096), bin_cap, std::max<long long>(4 * S, 4096));
     }
     // solver vectors
     DevArena& Q = c->solver_mem;
@@ -1690,7 +1688,7 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         const EvalOut o = c->hp.outs[0];
         if (o.overflow) {
             std::string what;
-            if (o.overflow & kOverEntries) what += " cell entries";
+            if (o.overflow & kOverEntries) what += " entries in one grid bin";
             if (o.overflow & kOverBins) what += " grid bins";
             if (o.overflow & kOverCandidates) what += " candidate pairs";
             if (o.overflow & kOverContacts) what += " contacts";
@@ -1783,7 +1781,7 @@ int mcg_set_contact_capacity(mcg_ctx* c, int64_t entries, int64_t candidates, in
             throw Fail(MCG_ERR_INVALID, "capacities must be non-negative and bins at most 2^28");
         const long long lo = 4096;
         c->sync();
-        c->alloc_contacts(std::max<long long>(entries, lo), std::max<long long>(contacts, lo),
+        c->alloc_contacts(std::min<long long>(entries, 1LL << 20), std::max<long long>(contacts, lo),
                           std::max<long long>(bins, lo), std::max<long long>(candidates, lo));
     });
 }
@@ -1803,8 +1801,7 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
     return guarded(c, [&] {
         need_topo(c);
         if (!out5) throw Fail(MCG_ERR_INVALID, "null output");
-        const long long S = (long long)c->N + c->B;
-        d2h(c->hp.u32, c->cb.offset + S, 1, c->stream);
+        d2h(c->hp.u32, c->cb.nentries, 1, c->stream);
         d2h(c->hp.u32 + 1, c->cb.boffset + c->cb.bin_cap, 1, c->stream);
         d2h(c->hp.u32 + 2, c->cb.ncand, 1, c->stream);
         d2h(c->hp.u32 + 3, c->cb.foff + c->contact_chunks(), 1, c->stream);
@@ -1820,7 +1817,7 @@ int mcg_set_contact_cell(mcg_ctx* c, double cell) {
         if (!(cell >= 0) || cell > 1e3) throw Fail(MCG_ERR_INVALID, "cell must be a length >= 0 (m)");
         c->broad_cell = cell > 0 ? cell : c->default_cell();
         c->sync();
-        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
+        c->alloc_contacts(c->cb.bin_slots, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
     });
 }
 
@@ -1858,7 +1855,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
                 for (int b : blocks) {
                     c->broad_cell = scale * cell0;
                     c->pair_blocks_set = b;
-                    c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
+                    c->alloc_contacts(c->cb.bin_slots, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
                     const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);  // sizes the buffers
                     for (int i = 0; i < c->I; i++) e[size_t(i)] = o[i].energy;
                     d2h(g.data(), c->d_grad, n, s);
@@ -1894,7 +1891,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         c->contact_skin = skin;
         c->broad_cell = best.cell;
         c->pair_blocks_set = best.blocks;
-        c->alloc_contacts(c->cb.entry_cap, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
+        c->alloc_contacts(c->cb.bin_slots, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
         c->sync();
         if (out) *out = mcg_tuning{best.cell, c->pair_blocks_for(S), tried, best.ms, ms_default};
     });

@@ -99,12 +99,12 @@ struct EvalOut {
 // Device scratch of the contact pipeline (contact.cu).  Capacities are host-chosen and
 // grown on demand: a kernel that would exceed one sets a bit in flags[0] instead.
 enum ContactFlag : uint32_t {
-    kOverEntries = 1,    // more (cell, shape) entries than entry_cap
+    kOverEntries = 1,    // a bin holds more (cell, shape) entries than bin_slots
     kOverContacts = 2,   // more contacts than contact_cap
     kOverBins = 4,       // the grid needs more bins than bin_cap
     kNonFinite = 8,      // a shape has a non-finite bounding box (informational)
     kOverSpan = 16,      // a shape spans more cells than allowed: coarsen the grid
-    kOverCandidates = 32 // a warp found more narrow-phase candidates than its region holds
+    kOverCandidates = 32 // more narrow-phase candidates than cand_cap
 };
 
 struct ContactBufs {
@@ -112,23 +112,19 @@ struct ContactBufs {
     int4* cell_lo;          // [S] first cell (i, j, k) relative to the grid origin
     int4* cell_hi;          // [S] last cell
     uint4* rec;             // [S] pair-test record: quantized AABB (3 words), packed first cell
-    uint32_t* count;        // [S+1] cells per shape
-    uint32_t* offset;       // [S+1] exclusive scan of count
     int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed;
                             //       box quantization scale x,y,z and origin x,y,z (float bits)
     uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation, [1] candidate list
                             //      rebuilt by this evaluation, [2] rebuild forced by the host,
                             //      [3] the pair pass's occupied-bin cursor
     float4* xref;           // [N] node positions (FP32, rounded down) when the list was built
-    // entries in emission order (shape-major), then counting-sorted by bin
-    long long entry_cap;
-    uint32_t* ekey;         // [entry_cap] bin of the entry
-    uint32_t* erank;        // [entry_cap] rank of the entry inside its bin
-    uint32_t* sorted;       // [entry_cap] shape ids grouped by bin
-    // bins
+    // bins of fixed capacity: the shapes of bin b at bin_items[b * bin_slots ...]
     long long bin_cap;
-    uint32_t* bin_count;    // [bin_cap+1]
-    uint32_t* bin_start;    // [bin_cap+1]
+    int bin_slots;          // entries a bin holds, a power of two
+    uint32_t* bin_count;    // [bin_cap+1] entries counted per bin (may exceed bin_slots)
+    uint32_t* bin_items;    // [bin_cap * bin_slots]
+    uint32_t* nentries;     // [2]: [0] cell entries of the last build, [1] the largest bin count
+                            //      above bin_slots (0 when every bin fitted)
     uint32_t* bcount;       // [bin_cap+1] 1 where a bin holds two or more entries
     uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = occupied bins
     uint32_t* occ;          // [bin_cap] occupied bins in bin order

@@ -41,8 +41,8 @@ namespace {
 
 constexpr long long kNoAllocMaxNodes = 4096;
 constexpr long long kNoAllocMaxShapes = 8192;       // nodes + beams
-constexpr long long kNoAllocEntries = 8 * kNoAllocMaxShapes;
-constexpr long long kNoAllocBins = 32768;
+constexpr int kNoAllocBinSlots = 128;                // entries one grid bin holds
+constexpr long long kNoAllocBins = 4096;
 constexpr long long kNoAllocCandidates = 4 * kNoAllocMaxShapes;
 constexpr long long kNoAllocContacts = 8192;
 constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
@@ -81,18 +81,14 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.cell_lo = reinterpret_cast<int4*>(take(size_t(S) * sizeof(int4)));
     c.cell_hi = reinterpret_cast<int4*>(take(size_t(S) * sizeof(int4)));
     c.rec = reinterpret_cast<uint4*>(take(size_t(S) * sizeof(uint4)));
-    c.count = reinterpret_cast<uint32_t*>(take(size_t(S + 1) * 4));
-    c.offset = reinterpret_cast<uint32_t*>(take(size_t(S + 1) * 4));
     c.grid = reinterpret_cast<int*>(take(16 * sizeof(int)));
     c.flags = reinterpret_cast<uint32_t*>(take(4 * 4));
     c.xref = reinterpret_cast<float4*>(take(size_t(N > 0 ? N : 1) * sizeof(float4)));
-    c.entry_cap = kNoAllocEntries;
-    c.ekey = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
-    c.erank = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
-    c.sorted = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocEntries) * 4));
     c.bin_cap = kNoAllocBins;
+    c.bin_slots = kNoAllocBinSlots;
     c.bin_count = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
-    c.bin_start = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
+    c.bin_items = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * kNoAllocBinSlots * 4));
+    c.nentries = reinterpret_cast<uint32_t*>(take(2 * 4));
     c.bcount = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.boffset = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.occ = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * 4));
@@ -121,8 +117,7 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.n_items = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_sorted = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_long = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
-    long long scan_n = S + 1;
-    if (kNoAllocBins + 1 > scan_n) scan_n = kNoAllocBins + 1;
+    long long scan_n = kNoAllocBins + 1;
     if (chunks + 1 > scan_n) scan_n = chunks + 1;
     c.scan_tmp_bytes = scan_tmp_bytes(scan_n);
     c.scan_tmp = take(c.scan_tmp_bytes);

@@ -177,7 +177,7 @@ int mcg_objective(mcg_ctx* ctx, const double* z, double top, int trials, double*
  * memory belongs to another allocator.  mcg_objective may re-allocate its self-contact
  * buffers to fit a state; this entry point uses a fixed 4 MiB __device__ array instead
  * and calls no allocating routine.  Limits: at most 4096 nodes and 8192 nodes + beams, and
- * per evaluation 65536 cell entries, 32768 grid bins, 32768 candidate pairs and 8192
+ * per evaluation 4096 grid bins of at most 128 entries each, 32768 candidate pairs and 8192
  * contacts; beyond them it returns MCG_ERR_CAPACITY, naming what overflowed.  The first
  * call on a device looks up the array's device address, so make it before any stream
  * capture.  All calls on a device share the array: calls that overlap on the GPU race.
@@ -226,10 +226,11 @@ void* mcg_stream(mcg_ctx* ctx);
 /* Number of kernel launches the library has issued in this process. */
 int64_t mcg_launch_count(const mcg_ctx* ctx);
 
-/* Capacities of the self-contact buffers (no reference counterpart): grid-cell entries,
- * narrow-phase candidates, contacts and grid bins.  They grow by themselves when an
- * evaluation needs more (the evaluation is then repeated); setting them ahead avoids that
- * repeat for a known workload.  Values below the minimum (4096) are raised to it. */
+/* Capacities of the self-contact buffers (no reference counterpart): entries one grid bin
+ * holds (rounded up to a power of two, at least 8), narrow-phase candidates, contacts and
+ * grid bins.  They grow by themselves when an evaluation needs more (the evaluation is then
+ * repeated); setting them ahead avoids that repeat for a known workload.  Candidates,
+ * contacts and bins below the minimum (4096) are raised to it. */
 int mcg_set_contact_capacity(mcg_ctx* ctx, int64_t entries, int64_t candidates, int64_t contacts,
                              int64_t bins);
 
