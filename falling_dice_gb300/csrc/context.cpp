@@ -127,6 +127,9 @@ struct HostStats {
 };
 
 // One instance's Simulator::minimize (MC/src/sim.cpp:174-211) as a state machine.
+// Energy noise allowance of the mixed form's line search, relative to |E|.
+constexpr double kMixedArmijoSlack = 1e-9;
+
 struct Minimizer {
     enum Phase { kIdle, kStart, kIterate, kDirection, kSteepest, kTrial, kFinish, kDone };
     Phase phase = kIdle;
@@ -665,7 +668,12 @@ struct mcg_ctx {
                     }
                     s.cand = o;
                     s.st.backtracks++;
-                    if (std::isfinite(o.energy) && o.energy <= s.cur.energy + cfg.armijo * s.step * s.dg) {
+                    // Armijo (sim.cpp:180).  The mixed form's energy carries rounding noise of
+                    // ~3e-10 |E| (compensated FP32 sums of FP32 beam energies); near
+                    // equilibrium a step's decrease falls below it, so the mixed form allows
+                    // that much slack, kMixedArmijoSlack |E|.  The FP64 form tests exactly.
+                    const double slack = mixed ? kMixedArmijoSlack * std::abs(s.cur.energy) : 0.0;
+                    if (std::isfinite(o.energy) && o.energy <= s.cur.energy + cfg.armijo * s.step * s.dg + slack) {
                         c.flags = kOpAccept | (H > 0 ? kOpPair : 0) | (o.energy < s.best_energy ? kOpKeepBestAfter : 0);
                         any_post = true;
                         s.accepted = true;
