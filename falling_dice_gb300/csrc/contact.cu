@@ -42,7 +42,7 @@ constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
 constexpr int kPairGrab = 2;             // occupied bins a warp claims at a time
-constexpr int kPairStage = 256;          // candidates a warp stages before appending them
+constexpr int kPairStage = 128;          // candidates a warp stages before appending them
 constexpr int kStreamBlocks = 8 * 152;
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
@@ -432,24 +432,23 @@ __device__ __forceinline__ bool pair_test(const PairRec& A, const PairRec& B) {
     return first && box && !share;
 }
 
-__device__ __forceinline__ PairRec shfl_rec(const PairRec& v, int src) {
-    return PairRec{__shfl_sync(0xffffffffu, v.id, src), __shfl_sync(0xffffffffu, v.w0, src),
-                   __shfl_sync(0xffffffffu, v.w1, src), __shfl_sync(0xffffffffu, v.w2, src),
-                   __shfl_sync(0xffffffffu, v.n0, src), __shfl_sync(0xffffffffu, v.n1, src)};
-}
 
 constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 
-// Every unordered pair of the records held by lanes 0 .. m-1 (m <= 32), by rotation: in
-// round k lane i meets lane (i + k) mod m, k = 1 .. m/2 (the last round of an even m only
-// from the lower half), the partner's record arriving by six register shuffles.
+// Every unordered pair of the records at ranks base .. base + m - 1 (m <= 32; lane i holds
+// rank base + i in `me`, and all of them are staged in shared memory), by rotation: in
+// round k lane i meets rank base + (i + k) mod m, k = 1 .. m/2 (the last round of an even m
+// only from the lower half), the partner's record read from shared memory.
 template <typename Emit>
-__device__ __forceinline__ void rotate_pairs(const PairRec& me, int m, int lane, Emit emit) {
+__device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __restrict__ srec,
+                                             const int2* __restrict__ snd, int base, int m, int lane, Emit& emit) {
     const int half = m >> 1;
     int src = lane;
     for (int k = 1; k <= half; k++) {
         src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
-        const PairRec o = shfl_rec(me, lane < m ? src : lane);
+        const uint4 r = srec[base + src];
+        const int2 q = snd[base + src];
+        const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
         const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
         emit(active && pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
     }
@@ -476,11 +475,15 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
                                                       uint32_t* __restrict__ flags) {
     __shared__ uint2 stage_all[kPairWarps][kPairStage];
+    __shared__ uint4 rec_all[kPairWarps][64];  // the bin's records, staged for the partner reads
+    __shared__ int2 nd_all[kPairWarps][64];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
     const uint32_t nocc = *nocc_p;
     uint2* stage = stage_all[w];
+    uint4* srec = rec_all[w];
+    int2* snd = nd_all[w];
     uint32_t* cursor = flags + 3;
     uint32_t staged = 0;  // warp-uniform
     // appends the staged candidates to the list: one atomic per chunk
@@ -497,9 +500,15 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
     };
     auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
         const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (hit) stage[staged + __popc(m & below)] = make_uint2(min(sa, sb), max(sa, sb));
-        staged += __popc(m);
-        if (staged > kPairStage - 32) flush();
+        if (m) {  // warp-uniform; most rounds find nothing
+            if (hit) stage[staged + __popc(m & below)] = make_uint2(min(sa, sb), max(sa, sb));
+            staged += __popc(m);
+            if (staged > kPairStage - 32) flush();
+        }
+    };
+    auto stage_rec = [&](const PairRec& r, int rank) {
+        srec[rank] = make_uint4(r.id, r.w0, r.w1, r.w2);
+        snd[rank] = make_int2(r.n0, r.n1);
     };
     for (;;) {
         uint32_t jb0 = 0;
@@ -513,21 +522,33 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
             const uint32_t* items = bin_items + size_t(b) * size_t(bin_slots);
             const int3 cc = cell_of(grid, b);
             const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
+            __syncwarp();  // the previous bin's partner reads are done
             if (n <= 32) {
                 PairRec me{};
-                if (lane < n) me = load_rec(t, items[lane], rec, ccp);
-                rotate_pairs(me, n, lane, emit);
+                if (lane < n) {
+                    me = load_rec(t, items[lane], rec, ccp);
+                    stage_rec(me, lane);
+                }
+                __syncwarp();
+                rotate_pairs(me, srec, snd, 0, n, lane, emit);
             } else if (n <= 64) {
                 const int m = n - 32;
                 const PairRec lo = load_rec(t, items[lane], rec, ccp);
+                stage_rec(lo, lane);
                 PairRec up{};
-                if (lane < m) up = load_rec(t, items[32 + lane], rec, ccp);
-                rotate_pairs(lo, 32, lane, emit);
-                for (int q = 0; q < m; q++) {  // the lower records against upper record q
-                    const PairRec o = shfl_rec(up, q);
+                if (lane < m) {
+                    up = load_rec(t, items[32 + lane], rec, ccp);
+                    stage_rec(up, 32 + lane);
+                }
+                __syncwarp();
+                rotate_pairs(lo, srec, snd, 0, 32, lane, emit);
+                for (int q = 0; q < m; q++) {  // the lower records against upper rank 32 + q
+                    const uint4 r = srec[32 + q];
+                    const int2 nq = snd[32 + q];
+                    const PairRec o{r.x, r.y, r.z, r.w, nq.x, nq.y};
                     emit(pair_test(lo, o), lo.id & kIdMask, o.id & kIdMask);
                 }
-                rotate_pairs(up, m, lane, emit);
+                rotate_pairs(up, srec, snd, 32, m, lane, emit);
             } else {
                 // large bin: pairs by index, records from global memory
                 const long long P = (long long)n * (n - 1) / 2;
