@@ -367,18 +367,13 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
 
 // Entries of shape s: one per cell of its range, written straight into the bin's slot that
 // the bin counter hands out.  A bin that fills up keeps counting (kOverEntries, and the
-// largest count in nentries[1] so the host can size bin_slots); the cell entries of the
-// build are counted once per block into nentries[0].
+// largest count in nentries[1] so the host can size bin_slots).
 __global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ grid, const int4* __restrict__ cell_lo,
                                                  const int4* __restrict__ cell_hi, int bin_slots,
                                                  uint32_t* __restrict__ bin_count, uint32_t* __restrict__ bin_items,
                                                  uint32_t* __restrict__ nentries, uint32_t* __restrict__ flags) {
-    __shared__ uint32_t block_entries;
-    if (!flags[1]) return;  // grid-uniform
-    if (threadIdx.x == 0) block_entries = 0;
-    __syncthreads();
+    if (!flags[1]) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t n = 0;
     if (s < S) {
         const int4 lo = cell_lo[s], hi = cell_hi[s];
         for (int j = lo.y; j <= hi.y; j++)
@@ -392,13 +387,8 @@ __global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ 
                         atomicOr(flags, uint32_t(kOverEntries));
                         atomicMax(nentries + 1, slot + 1);
                     }
-                    n++;
                 }
     }
-    const uint32_t wn = __reduce_add_sync(0xffffffffu, n);
-    if ((threadIdx.x & 31) == 0 && wn) atomicAdd(&block_entries, wn);
-    __syncthreads();
-    if (threadIdx.x == 0 && block_entries) atomicAdd(nentries, block_entries);
 }
 
 // One shape as the pair test sees it inside one bin: id with the first-cell flags in the
@@ -580,13 +570,22 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
 }
 
 // Occupied bins (two or more entries), in bin order: flags, then a scan, then this.
+// Occupied-bin flags, and the build's cell entries counted into nentries[0] (one atomic per
+// warp).
 __global__ void __launch_bounds__(kBlock) k_occ_flags(long long nb_cap, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, uint32_t* __restrict__ f,
+                                                      uint32_t* __restrict__ nentries,
                                                       const uint32_t* __restrict__ gate) {
     if (!*gate) return;
     const long long nb = grid[8];
-    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
-        f[b] = (b < nb && bin_count[b] >= 2) ? 1u : 0u;
+    uint32_t entries = 0;
+    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x) {
+        const uint32_t n = b < nb ? bin_count[b] : 0u;
+        f[b] = n >= 2 ? 1u : 0u;
+        entries += n;
+    }
+    entries = __reduce_add_sync(0xffffffffu, entries);
+    if ((threadIdx.x & 31) == 0 && entries) atomicAdd(nentries, entries);
 }
 __global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const uint32_t* __restrict__ f,
                                                       const uint32_t* __restrict__ off, uint32_t* __restrict__ occ,
@@ -894,7 +893,8 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.bin_slots, c.bin_count, c.bin_items,
                                            c.nentries, c.flags), note_launches(1));
     // occupied bins, then the candidate list
-    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, gate), note_launches(1));
+    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, c.nentries, gate),
+     note_launches(1));
     exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s, gate);
     (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
     const uint32_t* nocc = c.boffset + c.bin_cap;

@@ -374,15 +374,24 @@ template <bool F32>
 __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
                                                    EvalBufs e, double* __restrict__ grad) {
     __shared__ double sm[6 * kBlock];
+    __shared__ double cforce[2];
     const MapPos mp = map_pos(t.nblk);
-    if (!t.active[mp.inst]) return;
+    if (!t.active[mp.inst]) return;  // block-uniform
     const int i = mp.i;
     const int N = t.N;
-    double acc[6] = {0, 0, 0, 0, 0, 0};  // gravity E, platen E, reaction, contacts, self-contact E, |g|^2
-    double pen_max = 0, gmax = 0;
-    if (mp.valid) {
+    // centering force of the block's instance (sim.cpp:143), the same for all its nodes:
+    // one FP64 division per block (GB300's FP64 pipe is narrow)
+    if (threadIdx.x == 0) {
         const double* cen = e.cen + 9 * size_t(mp.inst);
         const double Ni = double(t.inst_n[mp.inst]);
+        cforce[0] = p.centering * cen[0] / Ni;
+        cforce[1] = p.centering * cen[2] / Ni;
+    }
+    __syncthreads();
+    double acc[6] = {0, 0, 0, 0, 0, 0};  // gravity E, platen E, reaction, contacts, self-contact E, |g|^2
+    double pen_max = 0;
+    unsigned long long gbits = 0;  // max |g| as the bits of a non-negative double (integer max)
+    if (mp.valid) {
         d3 gx{0, 0, 0}, gr{0, 0, 0};
         sum_slots<F32>(t, e, i, gx, gr);
         const d3 xi = ldx(e.x, i);
@@ -391,8 +400,8 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
         acc[0] = mg * xi.y;
         gx.y += mg;
         // centering (sim.cpp:143)
-        gx.x += p.centering * cen[0] / Ni;
-        gx.z += p.centering * cen[2] / Ni;
+        gx.x += cforce[0];
+        gx.z += cforce[1];
         // self-contact forces on this node in ascending (lower shape, higher shape, slot)
         // order (the list is sorted by the contact pipeline), and the self-contact energy of
         // each contact on the first node of its lower shape: both independent of the order
@@ -432,12 +441,15 @@ __global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, Cont
             // residual over free DOFs for the solver's convergence test (sim.cpp:44-45)
             if (!li[k]) {
                 acc[5] += gv[k] * gv[k];
-                gmax = fmax(gmax, fabs(gv[k]));
+                // fmax(gmax, |g|) on the bit patterns; a NaN (above the infinity pattern) is
+                // skipped as fmax skips it
+                const unsigned long long b = (unsigned long long)__double_as_longlong(gv[k]) & 0x7fffffffffffffffULL;
+                if (b <= 0x7ff0000000000000ULL && b > gbits) gbits = b;
             }
         }
     }
     block_sum_t<6>(acc, sm);
-    double m2[2] = {pen_max, gmax};
+    double m2[2] = {pen_max, __longlong_as_double((long long)gbits)};
     block_max_t<2>(m2, sm);
     if (threadIdx.x == 0) {
         double* q = e.part_node + kNodeParts * size_t(blockIdx.x);
