@@ -822,26 +822,38 @@ __device__ __forceinline__ unsigned long long item_key(const ContactBufs& c, uin
     return ((unsigned long long)c.c_a[ci] << 31) | ((unsigned long long)c.c_b[ci] << 2) | (item & 3u);
 }
 
-// One warp per node: lists of up to 32 items ranked by shuffles; longer lists are queued.
+// One warp per node with contacts: lists of up to 32 items ranked by shuffles; longer lists
+// are queued.
 __global__ void __launch_bounds__(kBlock) k_node_sort(int N, ContactBufs c) {
     const int lane = threadIdx.x & 31;
-    const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= N) return;  // warp-uniform
-    const uint32_t cnt = c.n_count[i], s0 = c.n_start[i];
-    if (cnt == 0) return;
-    if (cnt > 32) {
-        if (lane == 0) c.n_long[1 + atomicAdd(c.n_long, 1u)] = uint32_t(i);
-        return;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    const long long groups = (N + 31) / 32;
+    // warp w takes the groups of 32 consecutive nodes w, w + warps, ...; one ballot finds the
+    // group's nodes that have contacts (most have none)
+    for (long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < groups; g += warps) {
+        const long long i0 = g * 32;
+        const uint32_t mine = i0 + lane < N ? c.n_count[i0 + lane] : 0u;
+        unsigned todo = __ballot_sync(0xffffffffu, mine != 0);
+        while (todo) {
+            const int b = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const long long i = i0 + b;
+            const uint32_t cnt = __shfl_sync(0xffffffffu, mine, b), s0 = c.n_start[i];
+            if (cnt > 32) {
+                if (lane == 0) c.n_long[1 + atomicAdd(c.n_long, 1u)] = uint32_t(i);
+                continue;
+            }
+            uint32_t item = 0;
+            unsigned long long key = ~0ull;
+            if (lane < int(cnt)) {
+                item = c.n_items[s0 + lane];
+                key = item_key(c, item);
+            }
+            uint32_t rank = 0;
+            for (uint32_t q = 0; q < cnt; q++) rank += __shfl_sync(0xffffffffu, key, int(q)) < key;
+            if (lane < int(cnt)) c.n_sorted[s0 + rank] = item;
+        }
     }
-    uint32_t item = 0;
-    unsigned long long key = ~0ull;
-    if (lane < int(cnt)) {
-        item = c.n_items[s0 + lane];
-        key = item_key(c, item);
-    }
-    uint32_t rank = 0;
-    for (uint32_t q = 0; q < cnt; q++) rank += __shfl_sync(0xffffffffu, key, int(q)) < key;
-    if (lane < int(cnt)) c.n_sorted[s0 + rank] = item;
 }
 
 constexpr int kLongCap = 2048;  // keys staged in shared memory per long list
@@ -927,7 +939,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     exclusive_scan_u32(c.n_count, c.n_start, t.N, c.scan_tmp, s);
     (k_node_fill<<<kStreamBlocks, kBlock, 0, s>>>(t, total, c), note_launches(1));
     cudaMemsetAsync(c.n_long, 0, sizeof(uint32_t), s);
-    (k_node_sort<<<unsigned((32LL * t.N + kBlock - 1) / kBlock), kBlock, 0, s>>>(t.N, c), note_launches(1));
+    (k_node_sort<<<kStreamBlocks, kBlock, 0, s>>>(t.N, c), note_launches(1));
     (k_node_sort_long<<<kStreamBlocks, kBlock, 0, s>>>(c), note_launches(1));
 }
 
