@@ -41,7 +41,7 @@ constexpr uint32_t kBoxMax = 32767u;    // 15-bit box coordinates
 constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
-constexpr int kPairGrab = 2;             // occupied bins a warp claims at a time
+constexpr int kPairGrab = 8;             // bins a warp claims at a time (<= 32)
 constexpr int kPairStage = 128;          // candidates a warp stages before appending them
 constexpr int kStreamBlocks = 8 * 152;
 
@@ -263,6 +263,7 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
     *ncand = 0;  // the candidate list and entry counts of this build
     nentries[0] = 0;
     nentries[1] = 0;
+    nentries[2] = 0;
     bool ok = true;
     long long lo[3], dim[3];
     for (int d = 0; d < 3; d++) {
@@ -444,8 +445,10 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
     }
 }
 
-// Candidate pairs of every occupied bin.  Warps claim the occupied bins kPairGrab at a time
-// from a cursor (flags[3]), so bins of uneven size balance over the grid, stage their
+// Candidate pairs of every bin holding two or more shapes.  Warps claim the grid's bins
+// kPairGrab at a time from a cursor (flags[3]) and skip the empty ones (one ballot), so bins
+// of uneven size balance over the grid; they count the build's cell entries and occupied
+// bins into nentries[0] and [2] on the way, stage their
 // candidate pairs (lower shape, higher shape) in shared memory and append them to the flat
 // list in chunks (one atomic on ncand per chunk), without a counting pass.  The list's
 // length is the number of pairs, whatever the order; past cand_cap the pairs are counted
@@ -459,7 +462,7 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
 //   larger   pairs by index, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, int bin_slots,
-                                                      const uint32_t* __restrict__ occ, const uint32_t* __restrict__ nocc_p,
+                                                      uint32_t* __restrict__ nentries,
                                                       const uint32_t* __restrict__ bin_items,
                                                       const uint4* __restrict__ rec, long long cand_cap,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
-    const uint32_t nocc = *nocc_p;
+    const uint32_t nbins = uint32_t(grid[8]);
     uint2* stage = stage_all[w];
     uint4* srec = rec_all[w];
     int2* snd = nd_all[w];
@@ -500,15 +503,22 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         srec[rank] = make_uint4(r.id, r.w0, r.w1, r.w2);
         snd[rank] = make_int2(r.n0, r.n1);
     };
+    uint32_t entries = 0, occupied = 0;  // this lane's share of the build's counts
     for (;;) {
-        uint32_t jb0 = 0;
-        if (lane == 0) jb0 = atomicAdd(cursor, uint32_t(kPairGrab));
-        jb0 = __shfl_sync(0xffffffffu, jb0, 0);
-        if (jb0 >= nocc) break;
-        const uint32_t jend = min(jb0 + uint32_t(kPairGrab), nocc);
-        for (uint32_t jb = jb0; jb < jend; jb++) {
-            const uint32_t b = occ[jb];
-            const int n = int(min(bin_count[b], uint32_t(bin_slots)));  // a full bin repeats the build
+        uint32_t b0 = 0;
+        if (lane == 0) b0 = atomicAdd(cursor, uint32_t(kPairGrab));
+        b0 = __shfl_sync(0xffffffffu, b0, 0);
+        if (b0 >= nbins) break;
+        const uint32_t cnt = lane < kPairGrab && b0 + lane < nbins ? bin_count[b0 + lane] : 0u;
+        entries += cnt;
+        unsigned todo = __ballot_sync(0xffffffffu, cnt >= 2);  // the claimed bins holding pairs
+        occupied += lane == 0 ? uint32_t(__popc(todo)) : 0u;
+        while (todo) {
+            const int j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t b = b0 + uint32_t(j);
+            // a full bin repeats the build (kOverEntries), so clamping only keeps reads in bounds
+            const int n = int(min(__shfl_sync(0xffffffffu, cnt, j), uint32_t(bin_slots)));
             const uint32_t* items = bin_items + size_t(b) * size_t(bin_slots);
             const int3 cc = cell_of(grid, b);
             const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
@@ -567,33 +577,13 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         }
     }
     if (staged) flush();
+    entries = __reduce_add_sync(0xffffffffu, entries);
+    if (lane == 0) {
+        if (entries) atomicAdd(nentries, entries);
+        if (occupied) atomicAdd(nentries + 2, occupied);
+    }
 }
 
-// Occupied bins (two or more entries), in bin order: flags, then a scan, then this.
-// Occupied-bin flags, and the build's cell entries counted into nentries[0] (one atomic per
-// warp).
-__global__ void __launch_bounds__(kBlock) k_occ_flags(long long nb_cap, const int* __restrict__ grid,
-                                                      const uint32_t* __restrict__ bin_count, uint32_t* __restrict__ f,
-                                                      uint32_t* __restrict__ nentries,
-                                                      const uint32_t* __restrict__ gate) {
-    if (!*gate) return;
-    const long long nb = grid[8];
-    uint32_t entries = 0;
-    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x) {
-        const uint32_t n = b < nb ? bin_count[b] : 0u;
-        f[b] = n >= 2 ? 1u : 0u;
-        entries += n;
-    }
-    entries = __reduce_add_sync(0xffffffffu, entries);
-    if ((threadIdx.x & 31) == 0 && entries) atomicAdd(nentries, entries);
-}
-__global__ void __launch_bounds__(kBlock) k_occ_write(long long nb_cap, const uint32_t* __restrict__ f,
-                                                      const uint32_t* __restrict__ off, uint32_t* __restrict__ occ,
-                                                      const uint32_t* __restrict__ gate) {
-    if (!*gate) return;
-    for (long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x; b < nb_cap; b += (long long)gridDim.x * blockDim.x)
-        if (f[b]) occ[off[b]] = uint32_t(b);
-}
 
 
 // Certified single-precision distance bounds of a candidate pair.  A pair certainly farther
@@ -905,13 +895,8 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     (k_emit<<<grid_for(S), kBlock, 0, s>>>(S, c.grid, c.cell_lo, c.cell_hi, c.bin_slots, c.bin_count, c.bin_items,
                                            c.nentries, c.flags), note_launches(1));
     // occupied bins, then the candidate list
-    (k_occ_flags<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.grid, c.bin_count, c.bcount, c.nentries, gate),
-     note_launches(1));
-    exclusive_scan_u32(c.bcount, c.boffset, c.bin_cap, c.scan_tmp, s, gate);
-    (k_occ_write<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap, c.bcount, c.boffset, c.occ, gate), note_launches(1));
-    const uint32_t* nocc = c.boffset + c.bin_cap;
     if (pairs_begin) cudaEventRecord(pairs_begin, s);
-    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_slots, c.occ, nocc, c.bin_items,
+    (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_slots, c.nentries, c.bin_items,
                                                 c.rec, c.cand_cap, c.cand, c.ncand, c.flags),
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);

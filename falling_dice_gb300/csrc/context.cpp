@@ -300,10 +300,7 @@ struct mcg_ctx {
         c.bin_cap = bin_cap;
         c.bin_count = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.bin_items = contact_mem.get<uint32_t>(size_t(bin_cap) * size_t(slots));
-        c.nentries = contact_mem.get<uint32_t>(2);
-        c.bcount = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
-        c.boffset = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
-        c.occ = contact_mem.get<uint32_t>(size_t(bin_cap));
+        c.nentries = contact_mem.get<uint32_t>(3);
         c.pair_blocks = pair_blocks_for(S);
         c.cand_cap = std::max<long long>(1024, (cand_cap + 31) / 32 * 32);
         c.cand = contact_mem.get<uint2>(size_t(c.cand_cap));
@@ -329,11 +326,11 @@ struct mcg_ctx {
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
-        c.scan_tmp_bytes = scan_tmp_bytes(std::max({bin_cap + 1, (long long)N + 1, chunks + 1}));
+        c.scan_tmp_bytes = scan_tmp_bytes(std::max({(long long)N + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.ncand, 0, sizeof(uint32_t), stream), "memset");
-        ck(cudaMemsetAsync(c.nentries, 0, 2 * sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.nentries, 0, 3 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
@@ -1810,7 +1807,7 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
         need_topo(c);
         if (!out5) throw Fail(MCG_ERR_INVALID, "null output");
         d2h(c->hp.u32, c->cb.nentries, 1, c->stream);
-        d2h(c->hp.u32 + 1, c->cb.boffset + c->cb.bin_cap, 1, c->stream);
+        d2h(c->hp.u32 + 1, c->cb.nentries + 2, 1, c->stream);
         d2h(c->hp.u32 + 2, c->cb.ncand, 1, c->stream);
         d2h(c->hp.u32 + 3, c->cb.foff + c->contact_chunks(), 1, c->stream);
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
@@ -1859,7 +1856,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         double ms_default = 0;
         int tried = 0;
         try {
-            for (double scale : {1.0, 0.8, 1.25, 1.5})
+            for (double scale : {1.0, 0.9, 1.1, 1.25, 1.4})
                 for (int b : blocks) {
                     c->broad_cell = scale * cell0;
                     c->pair_blocks_set = b;

@@ -123,11 +123,9 @@ struct ContactBufs {
     int bin_slots;          // entries a bin holds, a power of two
     uint32_t* bin_count;    // [bin_cap+1] entries counted per bin (may exceed bin_slots)
     uint32_t* bin_items;    // [bin_cap * bin_slots]
-    uint32_t* nentries;     // [2]: [0] cell entries of the last build, [1] the largest bin count
-                            //      above bin_slots (0 when every bin fitted)
-    uint32_t* bcount;       // [bin_cap+1] 1 where a bin holds two or more entries
-    uint32_t* boffset;      // [bin_cap+1] scan of bcount; boffset[bin_cap] = occupied bins
-    uint32_t* occ;          // [bin_cap] occupied bins in bin order
+    uint32_t* nentries;     // [3]: [0] cell entries of the last build, [1] the largest bin count
+                            //      above bin_slots (0 when every bin fitted), [2] bins holding
+                            //      two or more entries
     // narrow-phase candidates: one flat list, appended by the pair grid's warps in chunks
     int pair_blocks;        // blocks of the pair grid (8 warps each)
     long long cand_cap;     // candidate slots, a multiple of 32

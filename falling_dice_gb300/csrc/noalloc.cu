@@ -88,10 +88,7 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.bin_slots = kNoAllocBinSlots;
     c.bin_count = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.bin_items = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * kNoAllocBinSlots * 4));
-    c.nentries = reinterpret_cast<uint32_t*>(take(2 * 4));
-    c.bcount = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
-    c.boffset = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
-    c.occ = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * 4));
+    c.nentries = reinterpret_cast<uint32_t*>(take(3 * 4));
     c.pair_blocks = contact_pair_blocks(S);
     c.cand_cap = kNoAllocCandidates;
     c.cand = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
@@ -117,7 +114,7 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.n_items = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_sorted = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_long = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
-    long long scan_n = kNoAllocBins + 1;
+    long long scan_n = N + 1;
     if (chunks + 1 > scan_n) scan_n = chunks + 1;
     c.scan_tmp_bytes = scan_tmp_bytes(scan_n);
     c.scan_tmp = take(c.scan_tmp_bytes);

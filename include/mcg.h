@@ -279,7 +279,7 @@ int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
 int mcg_set_contact_cell(mcg_ctx* ctx, double cell);
 
 /* Shapes of the self-contact broad phase picked by measurement (no reference
- * counterpart).  Candidates: grid cells 0.8, 1, 1.25 and 1.5 times the reference's
+ * counterpart).  Candidates: grid cells 0.9, 1, 1.1, 1.25 and 1.4 times the reference's
  * max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 .. 1216 blocks
  * (at most one warp per 32 shapes) besides the default.  Each candidate evaluates every
  * lattice `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL:
