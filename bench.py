@@ -77,6 +77,21 @@ def dist_info():
     return rank, world, local
 
 
+def max_over_ranks(torch, x, pg, device):
+    """The largest of the ranks' values of x (a time): every replica waits for the slowest."""
+    if pg is None:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, ms):
+    """Whole-job evaluations per second: `world` replicas each ran `steps` evaluations in at
+    most `ms` milliseconds (the max over ranks)."""
+    return world * 1e3 * steps / ms
+
+
 def workload(name):
     from falling_dice_gb300 import workloads
     return getattr(workloads, name)()
@@ -249,10 +264,7 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
     ms = e0.elapsed_time(e1)
     launches = sol.launch_count() - launches0
     clk = clocks.stop()
-    if pg is not None:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(torch, ms, pg, "cuda")
     res = sol.read_result(grad=False)
     # end to end through the public C ABI, pinned host buffers
     zh = torch.empty(6 * N, dtype=torch.float64, pin_memory=True)
@@ -273,10 +285,7 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
     e1.record(stream)
     barrier()
     ms_e2e = max(e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3)
-    if pg is not None:
-        t = torch.tensor([ms_e2e], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks(torch, ms_e2e, pg, "cuda")
     assert np.isfinite(eout.value) and eout.value == res["energy"]
     # per-phase timing for the roofline (a separate pass: it synchronises per evaluation)
     sol.set_timing(True)
@@ -286,7 +295,8 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
     sol.set_timing(False)
     stats = sol.contact_stats()
     sol.close()
-    return {"ms_step": ms / steps, "value": world * 1e3 * steps / ms, "e2e": world * 1e3 * steps / ms_e2e,
+    return {"ms_step": ms / steps, "value": replica_throughput(world, steps, ms),
+            "e2e": replica_throughput(world, steps, ms_e2e),
             "launches": launches, "clocks": clk, "energy": res["energy"], "grad": res0["grad"],
             "contacts": res["diag"]["contacts"], "phases": {k: v / nev for k, v in phases.items()},
             "contact_stats": stats, "tuning": tune}
