@@ -53,16 +53,6 @@ __device__ __forceinline__ f3 rot_inc(float w, f3 u, f3 v) {
 __device__ __forceinline__ f3 rot(float w, f3 u, f3 v) { return v + rot_inc(w, u, v); }
 __device__ __forceinline__ f3 rot_conj(float w, f3 u, f3 v) { return v + rot_inc(w, -u, v); }
 
-// Compensated FP32 sums: (hi, lo) with hi + lo carrying about twice the precision.
-struct fsum {
-    float hi = 0.f, lo = 0.f;
-    __device__ __forceinline__ void add(float v) {
-        const float s = hi + v;
-        const float bp = s - hi;
-        lo += (hi - (s - bp)) + (v - bp);
-        hi = s;
-    }
-};
 
 // Warp sum of compensated pairs (hi, lo) into lane 0, in FP32.
 __device__ __forceinline__ void warp_sum_comp(float& hi, float& lo) {
