@@ -87,15 +87,13 @@ struct Pinned {
                                // evaluation, accept) each have their own, so none is
                                // rewritten before its copy has run
     double* dg = nullptr;      // [I]
-    double* dots3 = nullptr;   // [3 I]
     double* pstats = nullptr;  // [6 I]
     double* cen = nullptr;     // [9 (I + 1)]
     uint32_t* u32 = nullptr;   // [8]
-    void alloc(int I, int H) {
+    void alloc(int I) {
         release();
-        const size_t Hn = size_t(std::max(H, 1));
         const size_t bytes = I * sizeof(EvalOut) + 3 * I * sizeof(SolveCtl) +
-                             sizeof(double) * (I + I * Hn + I + 3 * I + 6 * I + 9 * (I + 1)) + 8 * 4 + 512;
+                             sizeof(double) * (I + I + 6 * I + 9 * (I + 1)) + 8 * 4 + 512;
         ck(cudaMallocHost(&base, bytes), "cudaMallocHost");
         std::memset(base, 0, bytes);
         char* p = static_cast<char*>(base);
@@ -108,7 +106,6 @@ struct Pinned {
         ctl = reinterpret_cast<SolveCtl*>(take(3 * I * sizeof(SolveCtl)));
         tops = reinterpret_cast<double*>(take(I * sizeof(double)));
         dg = reinterpret_cast<double*>(take(I * sizeof(double)));
-        dots3 = reinterpret_cast<double*>(take(3 * I * sizeof(double)));
         pstats = reinterpret_cast<double*>(take(6 * I * sizeof(double)));
         cen = reinterpret_cast<double*>(take(9 * (I + 1) * sizeof(double)));
         u32 = reinterpret_cast<uint32_t*>(take(8 * sizeof(uint32_t)));
@@ -222,7 +219,6 @@ struct mcg_ctx {
            *d_pstats = nullptr;
     SolveCtl* d_ctl = nullptr;
     int2* d_hist = nullptr;       // per instance: history pairs held, oldest slot
-    uint32_t* d_reset = nullptr;  // per instance: the last direction fell back to steepest descent
     uint8_t* d_mask = nullptr;
     uint8_t *d_active = nullptr, *d_all = nullptr;  // instances evaluated / all instances
     std::vector<uint8_t> active;                    // host copy of d_active
@@ -599,7 +595,7 @@ struct mcg_ctx {
             replay(1 | (any_dir ? 2 : 0) | (any_multi ? 4 : 0) | (any_sd ? 8 : 0), [&] {
                 if (any_dir)
                     bl_direction(topo, d_ctl, d_hist, std::max(H, 1), any_multi, d_p, d_g, d_S, d_Y, 6LL * N, d_rho,
-                                 d_alpha, d_part, d_dg, d_reset, mt, mr, stream);
+                                 d_alpha, d_part, d_dg, mt, mr, stream);
                 if (any_sd) bl_steepest(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, stream);
             });
         }
@@ -1161,7 +1157,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->jr = cf.joint_scale * cf.max_radius;
     c->rmax = rmax;
     c->H = std::max(cf.history, 0);
-    c->hp.alloc(I, c->H);
+    c->hp.alloc(I);
     cudaStream_t s = c->stream;
     DevArena& M = c->topo_mem;
     DevTopo T{};
@@ -1388,10 +1384,8 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->d_pstats = Q.get<double>(6 * size_t(I));
     c->d_ctl = Q.get<SolveCtl>(size_t(I));
     c->d_hist = Q.get<int2>(size_t(I));
-    c->d_reset = Q.get<uint32_t>(size_t(I));
     ck(cudaMemsetAsync(c->d_hist, 0, size_t(I) * sizeof(int2), s), "memset");
     ck(cudaMemsetAsync(c->d_rho, 0, size_t(I) * Hs * sizeof(double), s), "memset");
-    ck(cudaMemsetAsync(c->d_reset, 0, size_t(I) * sizeof(uint32_t), s), "memset");
     c->d_mask = Q.get<uint8_t>(size_t(I));
     c->mins.assign(size_t(I), Minimizer{});
     c->fused.assign(size_t(I), 0);
@@ -1471,7 +1465,7 @@ int mcg_create(const mcg_config* cfg, int device, mcg_ctx** out) {
     try {
         c->set_device();
         ck(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-        c->hp.alloc(1, std::max(cfg->history, 1));
+        c->hp.alloc(1);
     } catch (const Fail&) {
         delete c;
         return MCG_ERR_CUDA;

@@ -304,11 +304,11 @@ size_t lbfgs_part_doubles(int n_nblk);
 int fused_direction_limit();
 // Two-loop recursion (sim.cpp:184-187) into p for the kOpDirFused (one CTA each) and, with
 // multi, the kOpDirection instances; then p = clamp(lock(-p)) and dg[i] = <g, p>; where
-// dg >= 0, steepest descent with the history cleared and reset[i] = 1 (sim.cpp:191).
+// not dg < 0, steepest descent with the history cleared (sim.cpp:191).
 // History: H slots of `stride` doubles, state hist[I], rho and alpha [I * H].
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, uint32_t* reset, double mt, double mr, cudaStream_t s);
+                  double* dg, double mt, double mr, cudaStream_t s);
 // The steepest-descent retry for the kOpSteepest instances: history cleared,
 // p = clamp(lock(-g)), dg[i] = <g, p> (sim.cpp:193-196).
 void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,

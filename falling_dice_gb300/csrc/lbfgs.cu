@@ -534,23 +534,19 @@ __global__ void __launch_bounds__(kBlock) k_descent_fix(DevTopo t, const SolveCt
     block_sum<1>(acc, sm);
     if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
 }
-// ... and per instance: the new dg, history cleared (m = 0), reset[i] = 1 (0 otherwise).
+// ... and per instance: the new dg and the history cleared (m = 0).
 __global__ void __launch_bounds__(kBlock) k_descent_final(DevTopo t, const SolveCtl* __restrict__ ctl,
                                                           const double* __restrict__ part, double* __restrict__ dg,
-                                                          int2* __restrict__ hist, uint32_t* __restrict__ reset) {
+                                                          int2* __restrict__ hist) {
     __shared__ double sm[kBlock / 32];
     const int inst = blockIdx.x;
     if (!(ctl[inst].flags & (kOpDirection | kOpDirFused))) return;
-    if (dg[inst] < 0) {
-        if (threadIdx.x == 0) reset[inst] = 0;
-        return;
-    }
+    if (dg[inst] < 0) return;
     double acc[1];
     instance_sum<1>(t, part, inst, acc, sm);
     if (threadIdx.x == 0) {
         dg[inst] = acc[0];
         hist[inst].x = 0;
-        reset[inst] = 1;
     }
 }
 // The steepest-descent retry (sim.cpp:193-196) starts with an empty history.
@@ -589,7 +585,7 @@ int fused_direction_limit() { return kFuseChunks; }
 
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, uint32_t* reset, double mt, double mr, cudaStream_t s) {
+                  double* dg, double mt, double mr, cudaStream_t s) {
     const int nb = t.n_nblk;
     (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
     if (multi) {
@@ -611,7 +607,7 @@ void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool
     }
     // not a descent direction: steepest descent, history cleared (sim.cpp:191)
     (k_descent_fix<<<nb, kBlock, 0, s>>>(t, ctl, dg, p, g, mt, mr, part), note_launches(1));
-    (k_descent_final<<<t.I, kBlock, 0, s>>>(t, ctl, part, dg, hist, reset), note_launches(1));
+    (k_descent_final<<<t.I, kBlock, 0, s>>>(t, ctl, part, dg, hist), note_launches(1));
 }
 
 void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
