@@ -41,8 +41,9 @@ constexpr uint32_t kBoxMax = 32767u;    // 15-bit box coordinates
 constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
-constexpr int kPairGrab = 8;             // bins a warp claims at a time (<= 32)
+constexpr int kPairGrab = 2;             // bins a warp claims at a time (<= 32)
 constexpr int kPairStage = 128;          // candidates a warp stages before appending them
+constexpr int kPairRanks = 128;          // bins up to this size are enumerated from registers
 constexpr int kStreamBlocks = 8 * 152;
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t v) {  // 10 bits -> every third bit
@@ -446,20 +447,19 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
 }
 
 // Candidate pairs of every bin holding two or more shapes.  Warps claim the grid's bins
-// kPairGrab at a time from a cursor (flags[3]) and skip the empty ones (one ballot), so bins
-// of uneven size balance over the grid; they count the build's cell entries and occupied
+// kPairGrab at a time (single bins near the end) from a cursor (flags[3]) and skip the empty
+// ones (one ballot), so bins of uneven size balance over the grid; they count the build's cell entries and occupied
 // bins into nentries[0] and [2] on the way, stage their
 // candidate pairs (lower shape, higher shape) in shared memory and append them to the flat
 // list in chunks (one atomic on ncand per chunk), without a counting pass.  The list's
 // length is the number of pairs, whatever the order; past cand_cap the pairs are counted
 // but not stored and kOverCandidates is raised, so the host can size the list exactly.
 // Enumeration inside a bin, entries in bin order:
-//   n <= 32  lane i holds entry i; every unordered pair is visited by rotation
-//            (rotate_pairs);
-//   n <= 64  lane i holds entries i and 32 + i; pairs of the lower 32 by rotation, each
-//            upper record broadcast to the 32 lower ones, pairs of the upper records by
-//            rotation;
-//   larger   pairs by index, records read from global memory.
+//   n <= 128  the entries in groups of 32, lane i holding entry 32 g + i of group g and every
+//             record staged in shared memory: the pairs inside each group by rotation
+//             (rotate_pairs), then each full group against every record of the later groups
+//             (one record read by all lanes per round);
+//   larger    pairs by index, records read from global memory.
 __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, int bin_slots,
                                                       uint32_t* __restrict__ nentries,
@@ -468,8 +468,8 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
                                                       uint32_t* __restrict__ flags) {
     __shared__ uint2 stage_all[kPairWarps][kPairStage];
-    __shared__ uint4 rec_all[kPairWarps][64];  // the bin's records, staged for the partner reads
-    __shared__ int2 nd_all[kPairWarps][64];
+    __shared__ uint4 rec_all[kPairWarps][kPairRanks];  // the bin's records, staged for the partner reads
+    __shared__ int2 nd_all[kPairWarps][kPairRanks];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned below = (1u << lane) - 1u;
@@ -504,12 +504,18 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
         snd[rank] = make_int2(r.n0, r.n1);
     };
     uint32_t entries = 0, occupied = 0;  // this lane's share of the build's counts
+    // kPairGrab bins per claim, then single bins for the last 4 per warp of the grid, so that
+    // a few heavy bins do not end up queued behind one warp
+    const uint32_t tail = 4u * gridDim.x * kPairWarps;
+    const uint32_t single_from = nbins > tail ? nbins - tail : 0u;
+    uint32_t grab = kPairGrab;  // warp-uniform
     for (;;) {
         uint32_t b0 = 0;
-        if (lane == 0) b0 = atomicAdd(cursor, uint32_t(kPairGrab));
+        if (lane == 0) b0 = atomicAdd(cursor, grab);
         b0 = __shfl_sync(0xffffffffu, b0, 0);
         if (b0 >= nbins) break;
-        const uint32_t cnt = lane < kPairGrab && b0 + lane < nbins ? bin_count[b0 + lane] : 0u;
+        const uint32_t cnt = lane < int(grab) && b0 + lane < nbins ? bin_count[b0 + lane] : 0u;
+        if (b0 + grab >= single_from) grab = 1;
         entries += cnt;
         unsigned todo = __ballot_sync(0xffffffffu, cnt >= 2);  // the claimed bins holding pairs
         occupied += lane == 0 ? uint32_t(__popc(todo)) : 0u;
@@ -523,32 +529,29 @@ __global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __re
             const int3 cc = cell_of(grid, b);
             const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
             __syncwarp();  // the previous bin's partner reads are done
-            if (n <= 32) {
-                PairRec me{};
-                if (lane < n) {
-                    me = load_rec(t, items[lane], rec, ccp);
-                    stage_rec(me, lane);
-                }
+            if (n <= kPairRanks) {
+                // ranks 32 g + lane in group g = 0 .. G-1, all staged in shared memory
+                const int G = (n + 31) >> 5;
+                for (int g = 0; g < G; g++)
+                    if (32 * g + lane < n) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), 32 * g + lane);
                 __syncwarp();
-                rotate_pairs(me, srec, snd, 0, n, lane, emit);
-            } else if (n <= 64) {
-                const int m = n - 32;
-                const PairRec lo = load_rec(t, items[lane], rec, ccp);
-                stage_rec(lo, lane);
-                PairRec up{};
-                if (lane < m) {
-                    up = load_rec(t, items[32 + lane], rec, ccp);
-                    stage_rec(up, 32 + lane);
+                for (int g = 0; g < G; g++) {
+                    const int mg = min(32, n - 32 * g);
+                    PairRec me{};
+                    if (lane < mg) {
+                        const uint4 q = srec[32 * g + lane];
+                        const int2 nq = snd[32 * g + lane];
+                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                    }
+                    rotate_pairs(me, srec, snd, 32 * g, mg, lane, emit);  // within group g
+                    // group g (full: a later group exists) against each record of the later groups
+                    for (int r = 32 * (g + 1); r < n; r++) {
+                        const uint4 q = srec[r];
+                        const int2 nq = snd[r];
+                        const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                        emit(pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
+                    }
                 }
-                __syncwarp();
-                rotate_pairs(lo, srec, snd, 0, 32, lane, emit);
-                for (int q = 0; q < m; q++) {  // the lower records against upper rank 32 + q
-                    const uint4 r = srec[32 + q];
-                    const int2 nq = snd[32 + q];
-                    const PairRec o{r.x, r.y, r.z, r.w, nq.x, nq.y};
-                    emit(pair_test(lo, o), lo.id & kIdMask, o.id & kIdMask);
-                }
-                rotate_pairs(up, srec, snd, 32, m, lane, emit);
             } else {
                 // large bin: pairs by index, records from global memory
                 const long long P = (long long)n * (n - 1) / 2;
