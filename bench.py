@@ -44,11 +44,11 @@ NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6
 # captured with ncu on GB300 and scaled to the workload:
 #   k_beams (FP64), 32x32x16 cubic+BCC: 40.35 MB for 184,400 beams, scaled by beam count;
 #   k_beams_mixed, 64x64x32 cubic+BCC: 323.53 MB for 1,458,336 beams, scaled by beam count;
-#   k_bin_pairs, 64x64x32 cubic+BCC at the tuned cell: 135.08 MB where the algorithmic
-#   bytes below come to 123.55 MB, scaled by the algorithmic bytes.
+#   k_bin_pairs, 64x64x32 cubic+BCC at the tuned shapes (4.5 mm cell, 1216 blocks): 107.87 MB
+#   where the algorithmic bytes below come to 123.55 MB, scaled by the algorithmic bytes.
 BEAM_TRAFFIC_PER_BEAM = 40.348160e6 / 184400
-BEAM_TRAFFIC_PER_BEAM_MIXED = 323.525504e6 / 1458336
-PAIR_TRAFFIC_PER_ALGORITHMIC_BYTE = 135.081216e6 / 123.545196e6
+BEAM_TRAFFIC_PER_BEAM_MIXED = 322.980608e6 / 1458336
+PAIR_TRAFFIC_PER_ALGORITHMIC_BYTE = 107.870720e6 / 123.545196e6
 BEAM_BYTES_MIXED = 68    # per beam, mixed: a, b (2 x 4 B) + 15 reals as FP32
 NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 + locked[6]
 # Pair enumeration (k_bin_pairs), algorithmic bytes: every cell entry's shape id (4 B), each
@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mcg", choices=["mcg", "reference"])
     ap.add_argument("--workload", default="bcc64")
+    ap.add_argument("--shapes", default="", help="CELL,PAIR_BLOCKS: fixed broad-phase shapes instead of tuning")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the load/unload (32x32x16) and batched-sweep (256 lattices) measurements")
@@ -227,7 +228,7 @@ def run_reference(a, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
+def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world, shapes=None):
     """Times one precision form: device-resident evaluations, e2e through the C ABI, phases."""
     import ctypes as C
     from falling_dice_gb300 import abi
@@ -235,7 +236,11 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world):
     sol = fd.Solver(cfg, lat, device=local)
     sol.set_contact_skin(0.0)  # a full evaluation: grid, pairs and narrow phase every step
     sol.set_state(plastic=pl)
-    tune = sol.autotune(z, top, reps=3)  # broad-phase cell and pair grid, by measurement
+    if shapes:  # fixed broad-phase shapes (a saved tuning), e.g. for a profiler run
+        sol.set_contact_shapes(*shapes)
+        tune = {"cell": shapes[0], "pair_blocks": shapes[1], "tried": 0}
+    else:
+        tune = sol.autotune(z, top, reps=3)  # broad-phase cell and pair grid, by measurement
     sol.upload_z(z)
     stream = torch.cuda.ExternalStream(sol.stream, device=local)
 
@@ -327,8 +332,12 @@ def main():
     N, B = lat.n_nodes, lat.n_beams
     cfg_mixed = workload(a.workload)[0]
     cfg_mixed.precision = abi.MCG_MIXED
-    mixed = measure(fd, torch, cfg_mixed, lat, z, pl, top, a.steps, a.warmup, local, pg, world)
-    plain = measure(fd, torch, cfg, lat, z, pl, top, a.steps, a.warmup, local, pg, world)
+    shapes = None
+    if a.shapes:
+        cell, blocks = a.shapes.split(",")
+        shapes = (float(cell), int(blocks))
+    mixed = measure(fd, torch, cfg_mixed, lat, z, pl, top, a.steps, a.warmup, local, pg, world, shapes)
+    plain = measure(fd, torch, cfg, lat, z, pl, top, a.steps, a.warmup, local, pg, world, shapes)
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()

@@ -51,6 +51,7 @@ SIGNATURES = {
     "mcg_contact_stats": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_set_contact_cell": (C.c_int, [_P, C.c_double]),
     "mcg_autotune": (C.c_int, [_P, _d, _d, C.c_int32, C.POINTER(abi.Tuning)]),
+    "mcg_set_contact_shapes": (C.c_int, [_P, C.c_double, C.c_int32]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -276,6 +277,12 @@ class Solver:
                     "mcg_autotune")
         return {"cell": t.cell, "pair_blocks": t.pair_blocks, "tried": t.tried,
                 "ms_chosen": t.ms_chosen, "ms_default": t.ms_default}
+
+    def set_contact_shapes(self, cell, pair_blocks):
+        """Grid cell (m, 0: the reference's) and pair-enumeration blocks (0: default), as
+        autotune() reports them."""
+        self._check(self.lib.mcg_set_contact_shapes(self.h, float(cell), int(pair_blocks)),
+                    "mcg_set_contact_shapes")
 
     def set_contact_skin(self, skin):
         """Candidate-list reuse distance in metres (0: rebuild at every evaluation)."""

@@ -278,13 +278,19 @@ int mcg_set_contact_skin(mcg_ctx* ctx, double skin);
  * on it: a pair is examined once whatever the grid, and the narrow phase decides. */
 int mcg_set_contact_cell(mcg_ctx* ctx, double cell);
 
+/* Both broad-phase shapes at once, as mcg_autotune reports them (no reference counterpart):
+ * the grid cell in metres (0: the reference's) and the blocks of the pair enumeration (0: a
+ * default from the lattice size), e.g. to re-apply a tuning without timing again. */
+int mcg_set_contact_shapes(mcg_ctx* ctx, double cell, int32_t pair_blocks);
+
 /* Shapes of the self-contact broad phase picked by measurement (no reference
  * counterpart).  Candidates: grid cells 0.9, 1, 1.1, 1.25 and 1.4 times the reference's
  * max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 .. 1216 blocks
  * (at most one warp per 32 shapes) besides the default.  Each candidate evaluates every
  * lattice `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL:
  * z = 0) and platen heights `tops` (NULL: each lattice's top0), with the candidate list
- * rebuilt at every evaluation; the fastest by CUDA-event time is kept for the context.
+ * rebuilt at every evaluation; the fastest by CUDA-event time is kept for the context (among
+ * candidates within 1 % of it, the one with the most pair blocks, then the smallest cell).
  * The candidates must agree bit for bit on energies and gradients (pair sets and sums do
  * not depend on the grid); MCG_ERR_MISMATCH if one does not. */
 typedef struct mcg_tuning {

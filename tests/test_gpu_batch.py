@@ -83,7 +83,8 @@ def test_autotuned_shapes_leave_evaluations_and_runs_unchanged(mcg):
     _, ref_runs = plain.run()
     tuned = mcg.BatchSolver(cfg, lats, yields=ys)
     t = tuned.autotune(z, tops, reps=2)
-    assert t["tried"] >= 4 and t["ms_chosen"] <= t["ms_default"] * 1.0001
+    # the fastest, or within 1 % of it (the tie-break that keeps repeated tunings in agreement)
+    assert t["tried"] >= 4 and t["ms_chosen"] <= t["ms_default"] * 1.0101
     assert t["cell"] > 0 and t["pair_blocks"] >= 1
     got = tuned.objective(z, tops)
     assert np.array_equal(got["energy"], ref["energy"])
