@@ -94,3 +94,21 @@ def test_autotuned_shapes_leave_evaluations_and_runs_unchanged(mcg):
         assert [f["reaction_force"] for f in runs[k]] == [f["reaction_force"] for f in ref_runs[k]], k
     with pytest.raises(ValueError):
         tuned.autotune(z[:-1])
+
+
+def test_fixed_shapes_leave_evaluations_unchanged(mcg):
+    """mcg_set_contact_shapes (a saved tuning, or shapes pinned for a profiler) changes how
+    the broad phase splits its work, not an evaluation."""
+    cfg, lats, ys = make(mcg)
+    states = [mcg.random_state(lat, 0.04, 0.08, 0.02, 3000 + k) for k, lat in enumerate(lats)]
+    z = np.concatenate([zz for zz, _ in states])
+    tops = [lat.geometry.top0 - 0.003 for lat in lats]
+    ref = mcg.BatchSolver(cfg, lats, yields=ys).objective(z, tops)
+    for cell, blocks in ((0.0, 0), (0.004, 152), (0.0056, 1)):
+        b = mcg.BatchSolver(cfg, lats, yields=ys)
+        b.set_contact_shapes(cell, blocks)
+        got = b.objective(z, tops)
+        assert np.array_equal(got["energy"], ref["energy"]), (cell, blocks)
+        assert np.array_equal(got["grad"], ref["grad"]), (cell, blocks)
+    with pytest.raises(mcg.MCGError):
+        b.set_contact_shapes(-1.0, 0)
