@@ -9,24 +9,24 @@
 // enters every grid cell its margin-inflated AABB touches (sim.cpp:153-157; same cell size
 // and the same floor() cell coordinates).  Cells are numbered by the Morton code of their
 // coordinates relative to the grid origin (row-major when the Morton range does not fit),
-// and entries are counting-sorted into those bins: one atomic count per entry, a scan over
-// bins, one scatter.  The pair pass gives each occupied bin to one warp, which enumerates
-// the bin's pairs in the order the atomics handed out: the candidate list's order can vary
-// from run to run, its content cannot, and nothing computed from it depends on the order
-// (contact forces and energies are summed per node in shape-pair order, and pair sets are
-// reported sorted).  A pair is examined only in the cell that is the
+// and each entry goes straight into a slot of its bin (bins of fixed capacity, the slot
+// handed out by the bin's atomic counter).  The pair pass gives each occupied bin to one
+// warp, which enumerates the bin's pairs in the order the atomics handed out: the candidate
+// list's order can vary from run to run, its content cannot, and nothing computed from it
+// depends on the order (contact forces and energies are summed per node in shape-pair
+// order, and pair sets are reported sorted).  A pair is examined only in the cell that is the
 // minimum corner of the intersection of the two shapes' cell ranges: every pair that
 // shares a cell is examined exactly once -- the reference's `tested` set without a set.
 // A conservative FP32 AABB test and the local-shape exclusion (sim.cpp:24-39) run before
 // the FP64 narrow phase.
 //
-// Output order.  Candidate pairs are written per warp in (bin, pair) order; the narrow
-// phase flags the candidates in contact, a scan places them, and the contact list keeps
-// the candidate order.  Per-node force lists are built with counters and sorted by contact
+// Output order.  Candidate pairs are appended to one flat list in chunks staged per warp;
+// the narrow phase flags the candidates in contact, a scan places them, and the contact
+// list keeps the candidate order.  Per-node force lists are built with counters and sorted by contact
 // key (lower shape, higher shape, slot), so every sum is independent of the list order.
 //
-// No host synchronisation: sizes that can overflow a buffer (entries, bins, contacts, a
-// shape spanning too many cells) raise a flag instead of writing out of bounds, and the
+// No host synchronisation: sizes that can overflow a buffer (a bin's slots, bins,
+// candidates, contacts, a shape spanning too many cells) raise a flag instead of writing out of bounds, and the
 // host repeats the evaluation with larger buffers (or coarser cells) when it sees one.
 #include "common.cuh"
 #include "kernels.h"
