@@ -484,12 +484,15 @@ struct mcg_ctx {
 
     // Evaluation whose totals are read back (hp.outs); repeats it with larger contact
     // buffers when a capacity was exceeded.
-    const EvalOut* eval_read(const double* dz, bool trials, double* d_gout) {
+    // host_grad: the gradient is also copied there, in the same synchronisation.
+    const EvalOut* eval_read(const double* dz, bool trials, double* d_gout, double* host_grad = nullptr) {
         eval(dz, trials, d_gout);
+        if (host_grad) d2h(host_grad, d_gout, 6 * size_t(N), stream);
         read_outs();
         for (int tries = 0; hp.outs[0].overflow && tries < 16; tries++) {
             if (!grow_contacts(hp.outs[0].overflow)) break;
             eval(dz, trials, d_gout);
+            if (host_grad) d2h(host_grad, d_gout, 6 * size_t(N), stream);
             read_outs();
         }
         if (hp.outs[0].overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
@@ -1564,9 +1567,8 @@ int mcg_objective(mcg_ctx* c, const double* z, double top, int trials, double* e
         c->hp.tops[0] = top;
         c->upload_tops();
         c->set_active(std::vector<uint8_t>(1, 1));
-        const EvalOut o = c->eval_read(c->d_zin, trials != 0, c->d_grad)[0];
+        const EvalOut o = c->eval_read(c->d_zin, trials != 0, c->d_grad, grad)[0];
         if (trials) c->have_final = false;
-        if (grad) d2h(grad, c->d_grad, n, s);
         if (energy) *energy = o.energy;
         fill_diag(diag, o);
         if (trials && c->mixed) {
@@ -1605,13 +1607,11 @@ int mcg_batch_objective(mcg_ctx* c, const double* z, const double* tops, double*
         for (int i = 0; i < c->I; i++) c->hp.tops[i] = tops[i];
         c->upload_tops();
         c->set_active(std::vector<uint8_t>(size_t(c->I), 1));
-        const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);
+        const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad, grad);
         for (int i = 0; i < c->I; i++) {
             if (energies) energies[i] = o[i].energy;
             if (diags) fill_diag(diags + i, o[i]);
         }
-        if (grad) d2h(grad, c->d_grad, n, c->stream);
-        c->sync();
     });
 }
 
