@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from falling_dice_gb300 import abi
+from falling_dice_gb300 import abi, workloads
 
 HEADER = os.path.join(ROOT, "include", "mcg.h")
 
@@ -164,3 +164,22 @@ def test_random_state_is_seeded_and_respects_locks(mcg):
     pl = p1.reshape(-1, 7)
     assert np.all((pl[:, 0] >= 0) & (pl[:, 0] <= 0.02)) and np.array_equal(pl[:, 0], pl[:, 1])
     assert abs(np.std(z1[0::6]) - 0.05) < 0.01
+
+
+def test_sweep_workload_follows_its_specification():
+    """The batched sweep's 256 lattices: cells per side U{4..16} (cubic blocks), radius graded
+    from 0.3 mm with a slope up to 0.1 mm per cell and capped at 0.7 mm, yield U[30, 70] MPa,
+    30 % strain in 100 loading increments; the same draw every time."""
+    cfg, specs, ys = workloads.sweep()
+    assert len(specs) == len(ys) == 256
+    assert cfg.load_steps == 100 and cfg.unload_steps == 0 and abs(cfg.max_strain - 0.3) < 1e-12
+    cells = [s.cells_x for s in specs]
+    assert all(s.cells_x == s.cells_y == s.cells_z for s in specs)
+    assert min(cells) >= 4 and max(cells) <= 16 and len(set(cells)) >= 10
+    for s in specs:
+        assert s.kind == abi.MCG_LATTICE_CUBIC_BCC
+        assert abs(s.r0 - 0.3e-3) < 1e-15 and 0.3e-3 <= s.r1 <= 0.7e-3 + 1e-15
+        assert s.r1 - s.r0 <= 0.1e-3 * s.cells_x + 1e-15
+    assert all(30e6 <= y <= 70e6 for y in ys)
+    cfg2, specs2, ys2 = workloads.sweep()
+    assert ys2 == ys and [s.seed for s in specs2] == [s.seed for s in specs]
