@@ -50,8 +50,12 @@ enum mcg_status {
 };
 
 enum mcg_precision {
-    MCG_FP64 = 0,  /* plain form: FP64 throughout (the correctness oracle on the GPU) */
-    MCG_MIXED = 1, /* FP32 bulk element/contact arithmetic, FP64 reductions */
+    MCG_FP64 = 0,  /* plain form: FP64 throughout (the correctness oracle on the GPU); the
+                      solver takes the reference's decisions exactly */
+    MCG_MIXED = 1, /* FP32 bulk element/contact arithmetic, FP64 reductions; energies carry
+                      ~3e-10 relative rounding noise, so the line search accepts a step when
+                      E_new <= E + armijo step dg + 1e-9 |E| (convergence is still judged on
+                      the gradient) */
 };
 
 /* MaterialConfig, MC/include/sim.hpp:16 (the name string is not carried). */
