@@ -460,7 +460,7 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
 //             (rotate_pairs), then each full group against every record of the later groups
 //             (one record read by all lanes per round);
 //   larger    pairs by index, records read from global memory.
-__global__ void __launch_bounds__(kBlock) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
+__global__ void __launch_bounds__(kBlock, 7) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, int bin_slots,
                                                       uint32_t* __restrict__ nentries,
                                                       const uint32_t* __restrict__ bin_items,
