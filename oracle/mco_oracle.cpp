@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "oracle.h"
+#include "specimens.h"
 
 namespace {
 
@@ -306,6 +307,20 @@ struct orc_model {
     std::vector<double> lastZ;
     Eval lastFinal;
     bool haveFinal = false;
+    // Objective hook: when set, objective() forwards to this energy/gradient implementation
+    // (whose signature is mcg_objective's) instead of evaluating here, and commit() hands the
+    // re-based state to stateHook (mcg_set_state's signature).  minimize, run and the
+    // verification checks stay exactly as they are: this is the reference driver calling an
+    // external objective through its unchanged interface.  A non-zero hook status is kept in
+    // hookStatus and the evaluation reads as non-finite, which the driver rejects.
+    orc_objective_fn objHook = nullptr;
+    orc_state_fn stateHook = nullptr;
+    void* hookCtx = nullptr;
+    mutable int hookStatus = 0;
+    mutable long long hookCalls = 0;
+    // When on, each evaluation keeps its sorted self-contact pair set here.
+    bool recordPairs = false;
+    mutable std::vector<uint64_t> lastPairs;
 
     double jointRadius() const { return cfg.joint_scale * cfg.max_radius; }
 
@@ -519,9 +534,11 @@ struct orc_model {
 
     // -- Simulator::objective, sim.cpp:138-172 -----------------------------------------
     Eval objective(const std::vector<double>& z, double top, bool trials) const {
+        if (objHook) return hookedObjective(z, top, trials);
         Eval o;
         o.grad.assign(nodes.size() * 6, 0);
         if (trials) o.trial.resize(beams.size());
+        if (recordPairs) lastPairs.clear();
         std::vector<V3> x, gx(nodes.size()), gr(nodes.size());
         std::vector<Q4> R;
         state(z, x, R);
@@ -635,7 +652,9 @@ struct orc_model {
                 o.energy += en; o.d.contact += en; o.d.maxPen = std::max(o.d.maxPen, pen); o.d.contacts++;
                 spreadForce(gx, a, cp.s, scale(n, mag));
                 spreadForce(gx, b, cp.t, scale(n, -mag));
+                if (recordPairs) lastPairs.push_back(keyOf(ai, bi));
             });
+            if (recordPairs) std::sort(lastPairs.begin(), lastPairs.end());
         }
         if (!(variant & 8)) platens();
         for (size_t i = 0; i < nodes.size(); i++) {  // pack, lock, guard: sim.cpp:172
@@ -652,6 +671,69 @@ struct orc_model {
             std::fill(o.grad.begin(), o.grad.end(), 0);
         }
         return o;
+    }
+
+    // The evaluation through the objective hook, in the layouts of include/mcg.h.
+    Eval hookedObjective(const std::vector<double>& z, double top, bool trials) const {
+        const size_t N = nodes.size(), B = beams.size();
+        Eval o;
+        o.grad.assign(6 * N, 0);
+        std::vector<double> nxt, aux;
+        std::vector<uint8_t> fl;
+        if (trials) {
+            nxt.assign(7 * B, 0);
+            aux.assign(7 * B, 0);
+            fl.assign(3 * B, 0);
+        }
+        mcg_diag dg{};
+        double e = kInf;
+        hookCalls++;
+        const int rc = objHook(hookCtx, z.data(), top, trials ? 1 : 0, &e, o.grad.data(), &dg,
+                               trials ? nxt.data() : nullptr, trials ? aux.data() : nullptr,
+                               trials ? fl.data() : nullptr);
+        if (rc != 0) {
+            if (!hookStatus) hookStatus = rc;
+            o.energy = kInf;
+            std::fill(o.grad.begin(), o.grad.end(), 0);
+            return o;
+        }
+        o.energy = e;
+        o.d.elastic = dg.elastic; o.d.plastic = dg.plastic; o.d.contact = dg.contact;
+        o.d.reaction = dg.reaction; o.d.maxPen = dg.max_pen; o.d.contacts = dg.contacts;
+        if (trials) {
+            o.trial.resize(B);
+            for (size_t b = 0; b < B; b++) {
+                Trial& t = o.trial[b];
+                const double* q = &nxt[7 * b];
+                t.next.epsp = q[0]; t.next.alpha = q[1]; t.next.rotp = {q[2], q[3], q[4]};
+                t.next.alphaB = q[5]; t.next.alphaT = q[6];
+                const double* w = &aux[7 * b];
+                t.strain = w[0]; t.stress = w[1]; t.moment = {w[2], w[3], w[4]};
+                t.elastic = w[5]; t.dissipation = w[6];
+                t.axialPlastic = fl[3 * b] != 0; t.bendPlastic = fl[3 * b + 1] != 0;
+                t.torsionPlastic = fl[3 * b + 2] != 0;
+            }
+        }
+        return o;
+    }
+
+    // Hands the current base state and plastic state to the hook's implementation.
+    void pushStateToHook() const {
+        if (!stateHook) return;
+        const size_t N = nodes.size(), B = beams.size();
+        std::vector<double> bx(3 * N), br(4 * N), pl(7 * B);
+        for (size_t i = 0; i < N; i++) {
+            bx[3 * i] = baseX[i].x; bx[3 * i + 1] = baseX[i].y; bx[3 * i + 2] = baseX[i].z;
+            br[4 * i] = baseR[i].w; br[4 * i + 1] = baseR[i].x; br[4 * i + 2] = baseR[i].y; br[4 * i + 3] = baseR[i].z;
+        }
+        for (size_t b = 0; b < B; b++) {
+            const Plastic& p = beams[b].plastic;
+            double* q = &pl[7 * b];
+            q[0] = p.epsp; q[1] = p.alpha; q[2] = p.rotp.x; q[3] = p.rotp.y; q[4] = p.rotp.z;
+            q[5] = p.alphaB; q[6] = p.alphaT;
+        }
+        const int rc = stateHook(hookCtx, bx.data(), br.data(), pl.data());
+        if (rc != 0 && !hookStatus) hookStatus = rc;
     }
 
     // -- solver vector helpers, sim.cpp:42-46 --------------------------------------------
@@ -703,7 +785,13 @@ struct orc_model {
         hist.reserve(size_t(cfg.history));
         Eval cur = objective(z, top, false), best = cur;
         std::vector<double> bestZ = z;
+        // Extension (no reference counterpart): with relative_gradient_tolerance > 0 an
+        // iterate has converged when rms(g) <= tol * rms(g at the start point), in place of
+        // the reference's absolute and reaction-relative tests; the penetration bar stays.
+        const double rms0 = vrms(cur.grad);
         auto converged = [&](const Eval& o, double rms, double mx) {
+            if (cfg.relative_gradient_tolerance > 0)
+                return rms <= cfg.relative_gradient_tolerance * rms0 && o.d.maxPen <= cfg.penetration_tolerance;
             const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.d.reaction));
             const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < 1.5e-3;
             return forceOK && o.d.maxPen <= cfg.penetration_tolerance;
@@ -797,6 +885,7 @@ struct orc_model {
         if (o.trial.size() != beams.size()) throw std::runtime_error("missing constitutive trial states");
         for (size_t i = 0; i < nodes.size(); i++) { nodes[i].x = x[i]; nodes[i].R = R[i]; baseX[i] = x[i]; baseR[i] = R[i]; }
         for (size_t i = 0; i < beams.size(); i++) beams[i].plastic = o.trial[i].next;
+        pushStateToHook();
     }
     double topY(double s, bool loading) const {
         const double compressed = top0 - cfg.max_strain * height;
@@ -1082,6 +1171,48 @@ void orc_set_state(orc_model* m, const double* bx, const double* br, const doubl
             const double* q = pl + 7 * b;
             p.epsp = q[0]; p.alpha = q[1]; p.rotp = {q[2], q[3], q[4]}; p.alphaB = q[5]; p.alphaT = q[6];
         }
+    if (bx || br || pl) m->pushStateToHook();
+}
+
+void orc_set_objective_hook(orc_model* m, orc_objective_fn objective, orc_state_fn state, void* ctx) {
+    m->objHook = objective;
+    m->stateHook = objective ? state : nullptr;
+    m->hookCtx = objective ? ctx : nullptr;
+    m->hookStatus = 0;
+    m->hookCalls = 0;
+    m->pushStateToHook();
+}
+
+int orc_hook_status(const orc_model* m, int64_t* calls) {
+    if (calls) *calls = m->hookCalls;
+    return m->hookStatus;
+}
+
+void orc_record_pairs(orc_model* m, int on) {
+    m->recordPairs = on != 0;
+    m->lastPairs.clear();
+}
+
+int64_t orc_last_pairs(const orc_model* m, uint64_t* keys, int64_t cap) {
+    for (int64_t k = 0; k < int64_t(m->lastPairs.size()) && k < cap; k++) keys[k] = m->lastPairs[size_t(k)];
+    return int64_t(m->lastPairs.size());
+}
+
+orc_model* orc_create_specimen(const mcg_config* cfg, const mcg_lattice_spec* spec) {
+    orcspec::Specimen s;
+    if (!cfg || !spec || !orcspec::build(*spec, *cfg, s)) return nullptr;
+    mcg_topology t{};
+    t.n_nodes = int32_t(s.mass.size());
+    t.n_beams = int32_t(s.L0.size());
+    t.beam_a = s.beam_a.data(); t.beam_b = s.beam_b.data(); t.L0 = s.L0.data(); t.radius = s.radius.data();
+    t.area = s.area.data(); t.I = s.I.data(); t.J = s.J.data(); t.e0 = s.e0.data(); t.mass = s.mass.data();
+    t.locked = s.locked.data(); t.n_connected = int64_t(s.connected.size()); t.connected = s.connected.data();
+    return orc_create_injected(cfg, &t, &s.geometry, s.x0.data(), s.r0.data(), s.layer.data());
+}
+
+void orc_random_state(int32_t n_nodes, int32_t n_beams, const uint8_t* locked, double sigma_t, double sigma_r,
+                      double epsp_max, uint64_t seed, double* z, double* plastic) {
+    orcspec::random_state(n_nodes, n_beams, locked, sigma_t, sigma_r, epsp_max, seed, z, plastic);
 }
 
 void orc_get_state(const orc_model* m, double* bx, double* br, double* pl) {

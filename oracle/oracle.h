@@ -75,6 +75,34 @@ double orc_top_y(const orc_model* m, double s, int loading);                    
  * order; see mco_oracle.cpp).  The reference harness accepts only 0 and returns -1. */
 int orc_set_variant(orc_model* m, int variant);
 
+/* ---- restatement only (libmco.so) ---------------------------------------------------- */
+
+/* The drop-in seam.  With a hook set, the restatement's objective (MC/src/sim.cpp:138,
+ * called by minimize at :176,179,210 and by gradientCheck at :552,564-565) forwards every
+ * evaluation to `objective` with ctx as its first argument -- the signature is
+ * mcg_objective's, so libmcg's entry point can be passed as it is -- and commit()/set_state
+ * hand the base and plastic state to `state` (mcg_set_state's signature).  minimize, run and
+ * the checks are unchanged.  NULL objective removes the hook. */
+typedef int (*orc_objective_fn)(void* ctx, const double* z, double top, int trials, double* energy,
+                                double* grad, mcg_diag* diag, double* trial_next, double* trial_aux,
+                                uint8_t* trial_flags);
+typedef int (*orc_state_fn)(void* ctx, const double* base_x, const double* base_r, const double* plastic);
+void orc_set_objective_hook(orc_model* m, orc_objective_fn objective, orc_state_fn state, void* ctx);
+/* First non-zero status a hook returned since it was set (0: none); calls = evaluations. */
+int orc_hook_status(const orc_model* m, int64_t* calls);
+
+/* With on != 0 every evaluation keeps its sorted self-contact pair set (the same keys as
+ * orc_contact_pairs) for orc_last_pairs, so one evaluation gives both. */
+void orc_record_pairs(orc_model* m, int on);
+int64_t orc_last_pairs(const orc_model* m, uint64_t* keys, int64_t capacity);
+
+/* A model of the synthetic cubic / cubic+BCC specimen that mcg_lattice_generate builds
+ * for (spec, cfg), built here without the product library (oracle/specimens.cpp). */
+orc_model* orc_create_specimen(const mcg_config* cfg, const mcg_lattice_spec* spec);
+/* The seeded deformed state of mcg_random_state. */
+void orc_random_state(int32_t n_nodes, int32_t n_beams, const uint8_t* locked, double sigma_t,
+                      double sigma_r, double epsp_max, uint64_t seed, double* z, double* plastic);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,7 +32,8 @@ def build(which="mco", quiet=True):
     """Builds an oracle library with oracle/Makefile (the reference one needs its sources)."""
     if which == "ref" and not os.path.isdir(REF_ROOT):
         return False
-    out = subprocess.run(["make", "-s", "-C", HERE, which], capture_output=True, text=True)
+    cmd = ["make", "-s", "-C", HERE, which] + ([f"REF_ROOT={REF_ROOT}"] if which == "ref" else [])
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError(f"oracle build ({which}) failed:\n{out.stdout}\n{out.stderr}")
     return True
@@ -74,6 +75,21 @@ def load(which="mco"):
         "orc_top_y": (C.c_double, [P, C.c_double, C.c_int]),
         "orc_set_variant": (C.c_int, [P, C.c_int]),
     }
+    # restatement only
+    sig_mco = {
+        "orc_set_objective_hook": (None, [P, P, P, P]),
+        "orc_hook_status": (C.c_int, [P, C.POINTER(C.c_int64)]),
+        "orc_record_pairs": (None, [P, C.c_int]),
+        "orc_last_pairs": (C.c_int64, [P, _u64, C.c_int64]),
+        "orc_create_specimen": (P, [C.POINTER(abi.Config), C.POINTER(abi.LatticeSpec)]),
+        "orc_random_state": (None, [C.c_int32, C.c_int32, _u8, C.c_double, C.c_double, C.c_double,
+                                    C.c_uint64, _d, _d]),
+    }
+    if which == "mco":
+        sig.update(sig_mco)
+    else:
+        sig["orc_ref_write_outputs"] = (C.c_int, [C.POINTER(abi.Frame), C.c_int32, C.POINTER(abi.Config),
+                                                  C.c_double, C.c_char_p, C.c_char_p])
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res
@@ -87,13 +103,22 @@ def ptr(a, t=_d):
 
 
 class Model:
-    """One solver model inside an oracle library (a reference Simulator or its restatement)."""
+    """One solver model inside an oracle library (a reference Simulator or its restatement).
+
+    lattice: None (the reference's own builder), a LatticeArrays to inject, or a
+    LatticeSpec of a synthetic specimen built by the restatement itself (libmco only)."""
 
     def __init__(self, which, cfg, lattice=None):
         self.lib = load(which)
         self.which = which
         self.cfg = cfg
-        if lattice is None:
+        if isinstance(lattice, abi.LatticeSpec):
+            if which != "mco":
+                raise ValueError("synthetic specimens are built by the restatement only")
+            self.h = self.lib.orc_create_specimen(C.byref(cfg), C.byref(lattice))
+            if not self.h:
+                raise ValueError("invalid specimen")
+        elif lattice is None:
             self.h = self.lib.orc_create_builder(C.byref(cfg))
         else:
             topo, geom = lattice.topology()
@@ -193,6 +218,45 @@ class Model:
 
     def top_y(self, s, loading):
         return self.lib.orc_top_y(self.h, s, int(loading))
+
+    # -- restatement only ---------------------------------------------------------------
+    def set_objective_hook(self, objective_fn, state_fn, ctx):
+        """Forwards every evaluation to a C function with mcg_objective's signature (and the
+        state after each commit / set_state to one with mcg_set_state's), e.g. libmcg's own
+        entry points with a GPU context as ctx.  None removes the hook."""
+        as_ptr = (lambda f: None if f is None else C.cast(f, C.c_void_p))
+        self._hook_refs = (objective_fn, state_fn, ctx)  # keep them alive
+        self.lib.orc_set_objective_hook(self.h, as_ptr(objective_fn), as_ptr(state_fn), ctx)
+
+    def hook_status(self):
+        calls = C.c_int64()
+        rc = self.lib.orc_hook_status(self.h, C.byref(calls))
+        return rc, calls.value
+
+    def record_pairs(self, on=True):
+        self.lib.orc_record_pairs(self.h, int(on))
+
+    def last_pairs(self):
+        n = self.lib.orc_last_pairs(self.h, None, 0)
+        keys = np.zeros(max(n, 1), np.uint64)
+        self.lib.orc_last_pairs(self.h, ptr(keys, _u64), n)
+        return keys[:n]
+
+    def locked(self):
+        a = np.zeros(6 * self.n_nodes, np.uint8)
+        self.lib.orc_export(self.h, *([None] * 4), ptr(a, _u8), *([None] * 11))
+        return a
+
+
+def random_state(n_nodes, n_beams, locked, sigma_t, sigma_r, epsp_max, seed):
+    """The restatement of mcg_random_state: (z [6N], plastic [7B])."""
+    lib = load("mco")
+    z = np.zeros(6 * n_nodes)
+    pl = np.zeros(7 * n_beams)
+    lk = np.ascontiguousarray(locked, dtype=np.uint8)
+    lib.orc_random_state(n_nodes, n_beams, ptr(lk, _u8), sigma_t, sigma_r, epsp_max,
+                         seed & 0xFFFFFFFFFFFFFFFF, ptr(z), ptr(pl))
+    return z, pl
 
 
 def _f64(a):

@@ -14,11 +14,14 @@ reference's own Simulator (MC/src/sim.cpp) through oracle/ref_harness.cpp:
   bcc4.npz         a 4x4x4 cubic+BCC specimen at the heavy deformation of the
                    single-evaluation workload (many self-contacts).
   cubic6_run.npz   (--run-cubic6) the 6x6x6 specimen's full 200/200 load/unload run.
+  ref242_metrics.csv, ref242_summary.json  (--outputs) the reference CLI's own writers
+                   (MC/src/main.cpp:112-155) applied to the ref242 20/14 run.
   ref242_ensemble.npz  (--ensemble) the 20/14 run of the reference specimen under the CPU
                    restatement's rounding-order variants 1..31: the same sums in other orders.
                    Their spread is how far rounding alone moves the run-level results.
 """
 import argparse
+import ctypes as C
 import os
 import sys
 import time
@@ -244,10 +247,34 @@ def make_ensemble(variants=range(1, 32)):
     np.savez_compressed(os.path.join(OUT, "ref242_ensemble.npz"), **out)
 
 
+def frames_from_array(rows):
+    """abi.Frame structs from the rows of a fixture's frame table (exact doubles)."""
+    arr = (abi.Frame * max(len(rows), 1))()
+    for i, row in enumerate(rows):
+        for k, v in zip(FRAME_KEYS, row):
+            setattr(arr[i], k, int(v) if k in abi.FRAME_INTS else float(v))
+    return arr
+
+
+def make_outputs():
+    """The reference CLI's own metrics CSV and summary JSON (MC/src/main.cpp:112-155,
+    writeMetrics / writeSummary) of the reference specimen's 20/14 run in ref242.npz."""
+    print("ref242_metrics.csv, ref242_summary.json")
+    d = np.load(os.path.join(OUT, "ref242.npz"))
+    rows = d["run_frames"]
+    cfg = reference_config_242()
+    lib = orc.load("ref")
+    rc = lib.orc_ref_write_outputs(frames_from_array(rows), len(rows), C.byref(cfg), float(d["lat_geometry"][4]),
+                                   os.path.join(OUT, "ref242_metrics.csv").encode(),
+                                   os.path.join(OUT, "ref242_summary.json").encode())
+    assert rc == 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--run-cubic6", action="store_true")
     ap.add_argument("--ensemble", action="store_true")
+    ap.add_argument("--outputs", action="store_true", help="the reference CLI's CSV/JSON of the ref242 run")
     ap.add_argument("--only", default=None)
     a = ap.parse_args()
     if not orc.build("ref"):
@@ -265,6 +292,8 @@ def main():
         make_cubic6_run()
     if a.ensemble:
         make_ensemble()
+    if a.outputs:
+        make_outputs()
 
 
 if __name__ == "__main__":

@@ -125,3 +125,63 @@ def test_oracle_flags_nonfinite_energy(mco):
     g = golden("ref242")
     s = g.state(5)
     assert np.isinf(s["energy"]) and not np.any(s["grad"])
+
+
+@pytest.mark.parametrize("which", ["cubic6", "bcc32", "small_uniform"])
+def test_specimen_restatement_reproduces_the_product_generator(mco, mcg, which):
+    """The timed CPU baseline builds its inputs with the oracle's own restatement of the
+    workload generator (oracle/specimens.cpp), so that it loads no product library; the
+    arrays and the seeded deformed state must be the product's, bit for bit."""
+    from falling_dice_gb300 import workloads
+    if which == "small_uniform":
+        cfg, spec = workloads.bcc((5, 4, 3))
+    else:
+        cfg, spec = getattr(workloads, which)()
+    lat = mcg.generate_lattice(spec, cfg)
+    got = mco.Model("mco", cfg, lattice=spec).export()
+    for f in lat.FIELDS:
+        a, b = getattr(lat, f), getattr(got, f)
+        assert a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8)), f
+    for n, _ in abi.Geometry._fields_:
+        assert same_bits([getattr(lat.geometry, n)], [getattr(got.geometry, n)]), n
+    z, pl = mcg.random_state(lat, **workloads.DEFORM)
+    zo, plo = mco.random_state(lat.n_nodes, lat.n_beams, lat.locked, **workloads.DEFORM)
+    assert same_bits(z, zo) and same_bits(pl, plo)
+
+
+def test_objective_hook_is_transparent(mco):
+    """The seam plumbing on the CPU: a restatement whose objective hook forwards to a second,
+    plain restatement (through C callbacks with mcg_objective's and mcg_set_state's
+    signatures) runs minimize and a short load/unload run bit for bit like the plain one, and
+    keeps the plain one's state in step through the state hook."""
+    import ctypes as C
+    g = golden("cubic6")
+    cfg = g.cfg
+    cfg.load_steps, cfg.unload_steps = 6, 3
+    inner = mco.Model("mco", cfg, lattice=g.lattice)
+    dptr = C.POINTER(C.c_double)
+    OBJ = C.CFUNCTYPE(C.c_int, C.c_void_p, dptr, C.c_double, C.c_int, dptr, dptr, C.POINTER(abi.Diag),
+                      dptr, dptr, C.POINTER(C.c_uint8))
+    ST = C.CFUNCTYPE(C.c_int, C.c_void_p, dptr, dptr, dptr)
+
+    def objective(_ctx, z, top, trials, energy, grad, diag, nxt, aux, flags):
+        energy[0] = inner.lib.orc_objective(inner.h, z, top, trials, grad, diag, nxt, aux, flags)
+        return 0
+
+    def state(_ctx, bx, br, pl):
+        inner.lib.orc_set_state(inner.h, bx, br, pl)
+        return 0
+    obj_cb, st_cb = OBJ(objective), ST(state)
+    hooked = mco.Model("mco", cfg, lattice=g.lattice)
+    hooked.set_objective_hook(obj_cb, st_cb, None)
+    plain = mco.Model("mco", cfg, lattice=g.lattice)
+    top = float(g.d["min_top"][0])
+    z0 = np.zeros(6 * g.lattice.n_nodes)
+    a, b = hooked.minimize(top, z0), plain.minimize(top, z0)
+    assert same_bits(a[0], b[0]) and a[1] == b[1] and a[2] == b[2]
+    rc_a, fa = hooked.run()
+    rc_b, fb = plain.run()
+    assert rc_a == rc_b == 0 and fa == fb
+    assert all(same_bits(x, y) for x, y in zip(inner.get_state(), plain.get_state()))
+    status, calls = hooked.hook_status()
+    assert status == 0 and calls > 100
