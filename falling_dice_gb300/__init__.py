@@ -64,6 +64,9 @@ SIGNATURES = {
     "mcg_lattice_topology": (C.c_int, [_P, C.POINTER(abi.Topology)]),
     "mcg_random_state": (C.c_int, [C.c_int32, C.c_int32, _u8, C.c_double, C.c_double, C.c_double,
                                    C.c_uint64, _d, _d]),
+    "mcg_write_metrics_csv": (C.c_int, [C.POINTER(abi.Frame), C.c_int32, C.c_char_p]),
+    "mcg_write_summary_json": (C.c_int, [C.POINTER(abi.Frame), C.c_int32, C.POINTER(abi.Config), C.c_double,
+                                         C.c_char_p, C.c_char_p]),
 }
 
 
@@ -139,6 +142,29 @@ def random_state(lattice, sigma_t, sigma_r, epsp_max, seed):
     if rc:
         raise MCGError(rc, "mcg_random_state failed")
     return z, pl
+
+
+def _frames_array(frames):
+    arr = (abi.Frame * max(len(frames), 1))()
+    for i, f in enumerate(frames):
+        for k, v in f.items():
+            setattr(arr[i], k, v)
+    return arr
+
+
+def write_metrics_csv(frames, path):
+    """The reference CLI's per-increment metrics CSV of a run's frames (mcg_write_metrics_csv)."""
+    rc = load().mcg_write_metrics_csv(_frames_array(frames), len(frames), os.fsencode(path))
+    if rc:
+        raise MCGError(rc, f"cannot write {path}")
+
+
+def write_summary_json(frames, cfg, mass_kg, path, material=abi.REFERENCE_MATERIAL_NAME):
+    """The reference CLI's summary.json of a run (mcg_write_summary_json)."""
+    rc = load().mcg_write_summary_json(_frames_array(frames), len(frames), C.byref(cfg), float(mass_kg),
+                                       material.encode(), os.fsencode(path))
+    if rc:
+        raise MCGError(rc, f"cannot write {path}")
 
 
 class Solver:

@@ -21,10 +21,12 @@ MCG_MIXED = 1
 
 MCG_LATTICE_CUBIC = 0
 MCG_LATTICE_CUBIC_BCC = 1
+MCG_LATTICE_REFERENCE_BCC = 2
 MCG_RADIUS_GRADED_Y = 0
 MCG_RADIUS_UNIFORM = 1
 
 REFERENCE_SEED = 0x494E445553545259  # sim.hpp:25
+REFERENCE_MATERIAL_NAME = "FFF TPU 95A provisional isotropic baseline"  # MaterialConfig::name, sim.hpp:16
 
 
 class Material(C.Structure):

@@ -20,11 +20,11 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", f"-I{INC}",
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC", f"-I{INC}",
                      "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 # Per-unit extra flags.  contact.cu must round like the reference: no FMA contraction.
 EXTRA = {"contact.cu": ["-fmad=false"]}
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
+CXX_FLAGS = ["-O2", "-std=c++20", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              f"-I{CUDA_HOME}/include", f"-I{INC}"]
 
 

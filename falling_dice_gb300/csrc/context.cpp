@@ -199,6 +199,12 @@ struct mcg_ctx {
     EvalBufs ev{};
     ContactBufs cb{};
     long long last_contacts = 0;
+    // The last evaluation was mcg_objective_noalloc's: its contacts lived in the shared
+    // fixed scratch, so the pair and statistics queries have nothing current to report.
+    bool contacts_stale = false;
+    // Device address of mcg_objective_noalloc's fixed scratch on this context's device,
+    // looked up by that entry point's first call on this context (noalloc.cu).
+    void* noalloc_scratch = nullptr;
     Pinned hp;
 
     double *d_baseX = nullptr, *d_baseR = nullptr, *d_plastic = nullptr;
@@ -497,6 +503,7 @@ struct mcg_ctx {
         }
         if (hp.outs[0].overflow) throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
         if (cfg.self_contact) last_contacts = hp.u32[0];
+        contacts_stale = false;
         return hp.outs;
     }
     long long read_contact_count() {
@@ -514,6 +521,7 @@ struct mcg_ctx {
         read_outs();
         if (hp.outs[0].overflow) eval_read(last_z, last_trials, last_grad);
         else if (cfg.self_contact) last_contacts = hp.u32[0];
+        contacts_stale = false;
         return hp.outs[0];
     }
 
@@ -982,6 +990,11 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     std::vector<uint8_t> lockedv(6 * size_t(N));
     std::vector<float> padf(B);
     double rmax = cf.joint_scale * cf.max_radius;
+    // whether every section is the circular one (area pi r^2, I = pi r^4 / 4, J = 2 I,
+    // MC/src/sim.cpp:115): then the mixed form derives its section constants from r and L0
+    bool circular = true;
+    const double kPiD = 3.14159265358979323846;
+    auto near = [](double a, double b) { return std::abs(a - b) <= 1e-9 * std::abs(b); };
     std::vector<int> deg(size_t(N) + 1, 0);
     std::vector<InstHost> ih(static_cast<size_t>(I));
     std::vector<std::vector<int>> adj(static_cast<size_t>(N));
@@ -1026,6 +1039,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
             invL0[g] = 1.0 / L0;
             inv_kbh[g] = 1.0 / std::max(1e-20, kb[g] + hb[g]);
             inv_kth[g] = 1.0 / std::max(1e-20, kt[g] + ht[g]);
+            circular = circular && near(area, kPiD * r * r) && near(Is, .25 * kPiD * r * r * r * r) && near(J, 2 * Is);
             e0x[g] = t->e0[3 * size_t(b)];
             e0y[g] = t->e0[3 * size_t(b) + 1];
             e0z[g] = t->e0[3 * size_t(b) + 2];
@@ -1323,10 +1337,24 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         e.trial_nextf = V.get<float>(7 * size_t(B));
         e.trial_auxf = V.get<float>(7 * size_t(B));
         MixedBeams mb{};
-        float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B3, &mb.B4, &mb.B5, &mb.C0, &mb.C1, &mb.P0, &mb.P1};
+        float4** fields[] = {&mb.B0, &mb.B1, &mb.B2, &mb.B5, &mb.P0, &mb.P1};
         for (float4** f : fields) *f = V.get<float4>(size_t(B));
-        mb.syf = V.get<float>(size_t(B));
+        if (!circular) {
+            mb.C0 = V.get<float4>(size_t(B));
+            mb.C1 = V.get<float4>(size_t(B));
+        }
+        std::vector<float4> ic(static_cast<size_t>(I));
+        for (int k = 0; k < I; k++) {
+            const double sy = ih[size_t(k)].sy;
+            ic[size_t(k)] = make_float4(float(sy), float(sy * kPiD / 4), float(sy / std::sqrt(3.0) * kPiD / 2),
+                                        float(sy * kPiD));
+        }
+        mb.ic = V.get<float4>(size_t(I));
+        h2d(mb.ic, ic.data(), ic.size(), s);
+        mb.kg = make_float4(float(E * kPiD / 4), float(G * kPiD / 2), float(.5 * cf.shear_correction * G * kPiD),
+                            float(kPiD));
         c->mb = mb;
+        c->sync();  // ic goes out of scope
         c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
     }
     c->ev = e;
@@ -1683,7 +1711,9 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         else launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
         launch_finalize(c->topo, p, cptr, c->d_grad, c->ev, s);
         c->check_launch();
-        c->read_outs();
+        c->contacts_stale = p.self_contact != 0;
+        d2h(c->hp.outs, c->ev.out, 1, s);
+        c->sync();
         const EvalOut o = c->hp.outs[0];
         if (o.overflow) {
             std::string what;
@@ -1710,6 +1740,8 @@ int ctx_counts(const mcg_ctx* c, int* n_nodes, int* n_beams, int* device) {
     return MCG_OK;
 }
 
+void** ctx_noalloc_scratch(mcg_ctx* c) { return &c->noalloc_scratch; }
+
 void ctx_set_error(mcg_ctx* c, const char* msg) {
     if (c) c->err = msg;
 }
@@ -1722,6 +1754,8 @@ int mcg_contact_pairs(mcg_ctx* c, uint64_t* keys, int64_t capacity, int64_t* cou
     if (!c || !count) return MCG_ERR_INVALID;
     int rc = guarded(c, [&] {
         need_topo(c);
+        if (c->contacts_stale)
+            throw Fail(MCG_ERR_STATE, "the last evaluation was mcg_objective_noalloc's, whose contact pairs are not kept");
         const long long nc = c->phys.self_contact ? c->last_contacts : 0;
         *count = nc;
         if (nc > capacity) throw Fail(MCG_ERR_CAPACITY, "pair buffer too small");
@@ -1800,6 +1834,8 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
     return guarded(c, [&] {
         need_topo(c);
         if (!out5) throw Fail(MCG_ERR_INVALID, "null output");
+        if (c->contacts_stale)
+            throw Fail(MCG_ERR_STATE, "the last evaluation was mcg_objective_noalloc's, whose contact statistics are not kept");
         d2h(c->hp.u32, c->cb.nentries, 1, c->stream);
         d2h(c->hp.u32 + 1, c->cb.nentries + 2, 1, c->stream);
         d2h(c->hp.u32 + 2, c->cb.ncand, 1, c->stream);

@@ -192,16 +192,18 @@ struct EvalBufs {
 // Per-beam data of the mixed-precision form (objective_mixed.cu), float4 SoA.
 struct MixedBeams {
     float4* B0;  // base chord d0 (FP32-rounded), c0 = |d0|^2 - L0^2
-    float4* B1;  // base director d_a0, L0
-    float4* B2;  // base director d_b0, |d0|
-    float4* B3;  // base shear vector d_a0 - t0
-    float4* B4;  // base shear vector d_b0 - t0
+    float4* B1;  // base shear vector d_a0 - t0, L0
+    float4* B2;  // base shear vector d_b0 - t0, |d0|
     float4* B5;  // base relative rotation Q0 as (w - 1, v)
-    float4* C0;  // kb, kt, my, ty
-    float4* C1;  // cs, area L0, area, area L0 yield
     float4* P0;  // plastic: epsp, alpha, alphaB, alphaT
-    float4* P1;  // plastic: rotp
-    float* syf;  // yield stress
+    float4* P1;  // plastic: rotp; radius
+    // Section constants.  When every beam's area, I and J are the circular section's
+    // (pi r^2, pi r^4 / 4, 2 I, MC/src/sim.cpp:115) they are formed in the kernel from r and
+    // L0 with the factors below and C0/C1 stay null; otherwise they are streamed.
+    float4* C0;  // kb, kt, my, ty (streamed form only)
+    float4* C1;  // cs, area L0, area, area L0 yield (streamed form only)
+    float4* ic;  // [I] per instance: yield, yield pi/4, yield pi/(2 sqrt 3), yield pi
+    float4 kg;   // E pi/4, G pi/2, shear G pi/2, pi
 };
 // Per-node data of the mixed-precision form.
 struct MixedNodes {
@@ -240,6 +242,7 @@ void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& m
                         EvalBufs& e, cudaStream_t s);
 void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
                          MixedNodes& mn, cudaStream_t s);
+// The streamed section constants (mb.C0/C1, when allocated), once per upload.
 void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s);
 // plastic state of the mixed form from the FP64 SoA array (trial32 == nullptr, all beams) or
 // from an FP32 trial (the beams of the instances with mask[i] != 0; mask == nullptr: all)

@@ -3,28 +3,32 @@
 //
 // mcg_objective sizes its self-contact buffers on demand: when an evaluation needs more
 // cell entries, bins, candidate pairs or contacts than the context holds, it frees and
-// re-allocates them and evaluates again.  Some callers cannot let that happen: code
-// running while a CUDA stream is being captured into a graph (cudaMalloc and cudaFree are
-// not permitted there), real-time loops with a fixed memory budget, and hosts whose device
-// memory is owned by another allocator.  This entry point evaluates with the self-contact
-// scratch placed in one file-scope __device__ array of fixed size instead, and never calls
-// cudaMalloc, cudaFree or any allocating routine.  Everything else it uses (the lattice,
-// the base state, the per-node and per-beam buffers) was allocated when the context was
-// set up.
+// re-allocates them and evaluates again.  Some callers cannot let that happen: real-time
+// loops that run against a fixed device-memory budget, hosts whose device memory is owned
+// by another allocator (a framework's caching pool that has reserved it), and schedulers
+// that must not stall, since cudaFree waits for all work on the device.  This entry point
+// evaluates with the self-contact scratch placed in one file-scope __device__ array of
+// fixed size instead, and never calls cudaMalloc, cudaFree or any allocating routine.
+// Everything else it uses (the lattice, the base state, the per-node and per-beam buffers)
+// was allocated when the context was set up.
 //
 // The array is kNoAllocScratchBytes (4 MiB) and exists once on every GPU that loads the
 // library, for the life of the process.  It bounds the lattice: at most
 // kNoAllocMaxNodes nodes and kNoAllocMaxShapes nodes + beams, and per evaluation at most
 // the entry/bin/candidate/contact counts below; a larger lattice or state is rejected with
-// MCG_ERR_CAPACITY and a message naming what overflowed.
+// MCG_ERR_CAPACITY and a message naming what overflowed.  The bins cover the grid box of the
+// deformed specimen at the grid cell (the reference's max(2.8 joint radius, 0.72 cell)):
+// about 9 cells per axis of a cube-shaped specimen.
+//
+// Host code cannot use the array's name as an address: the first call on each context
+// looks the device address up with cudaGetSymbolAddress, with the context's device current,
+// and keeps it in the context (a context created after a cudaDeviceReset looks it up again).
 //
 // All calls on a device share the one array, which keeps the previous call's contents;
 // every buffer that must start at zero is cleared by the evaluation itself.  Two calls whose
 // work overlaps on the GPU (two contexts on two host threads, or two streams) race on the
 // array: callers must order them.
 #include <cuda_runtime.h>
-
-#include <mutex>
 
 #include "../../include/mcg.h"
 #include "common.cuh"
@@ -35,6 +39,7 @@ namespace mcg {
 int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* z, double top, double* energy,
                                   double* grad, mcg_diag* diag);
 int ctx_counts(const mcg_ctx* c, int* n_nodes, int* n_beams, int* device);
+void** ctx_noalloc_scratch(mcg_ctx* c);
 void ctx_set_error(mcg_ctx* c, const char* msg);
 
 namespace {
@@ -52,20 +57,17 @@ constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the array on the current device, looked up once per device.
-cudaError_t scratch_address(int device, unsigned char** out) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[device]) {
+// Device address of the array on the context's device (which is current), looked up by the
+// first call on the context and kept in it.
+cudaError_t scratch_address(mcg_ctx* ctx, unsigned char** out) {
+    void** slot = ctx_noalloc_scratch(ctx);
+    if (!*slot) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
-        g_scratch_ptr[device] = static_cast<unsigned char*>(p);
+        *slot = p;
     }
-    *out = g_scratch_ptr[device];
+    *out = static_cast<unsigned char*>(*slot);
     return cudaSuccess;
 }
 
@@ -135,13 +137,13 @@ extern "C" int mcg_objective_noalloc(mcg_ctx* ctx, const double* z, double top, 
                            "8192 nodes + beams)");
         return MCG_ERR_CAPACITY;
     }
-    if (device < 0 || device >= kMaxDevices) return MCG_ERR_INVALID;
+    // like every entry point, this one makes the context's device current on the calling thread
     if (cudaSetDevice(device) != cudaSuccess) {
         ctx_set_error(ctx, "mcg_objective_noalloc: cudaSetDevice failed");
         return MCG_ERR_CUDA;
     }
     unsigned char* base = nullptr;
-    const cudaError_t e = scratch_address(device, &base);
+    const cudaError_t e = scratch_address(ctx, &base);
     if (e != cudaSuccess) {
         ctx_set_error(ctx, cudaGetErrorString(e));
         return MCG_ERR_CUDA;

@@ -262,23 +262,40 @@ __global__ void __launch_bounds__(kBlock) k_rebase_beams(DevTopo t, const double
     const double v2 = Q0.x * Q0.x + Q0.y * Q0.y + Q0.z * Q0.z;
     const double wm1 = -v2 / (1.0 + Q0.w);  // w - 1 without cancellation
     m.B0[b] = make_float4(d0f.x, d0f.y, d0f.z, float(c0));
-    m.B1[b] = make_float4(float(da0.x), float(da0.y), float(da0.z), float(L0));
-    m.B2[b] = make_float4(float(db0.x), float(db0.y), float(db0.z), float(Lb));
-    m.B3[b] = make_float4(float(sa0.x), float(sa0.y), float(sa0.z), 0.f);
-    m.B4[b] = make_float4(float(sb0.x), float(sb0.y), float(sb0.z), 0.f);
+    m.B1[b] = make_float4(float(sa0.x), float(sa0.y), float(sa0.z), float(L0));
+    m.B2[b] = make_float4(float(sb0.x), float(sb0.y), float(sb0.z), float(Lb));
     m.B5[b] = make_float4(float(wm1), float(Q0.x), float(Q0.y), float(Q0.z));
 }
 
-// Section constants in FP32 (same expressions as the FP64 constants), once per upload.
+// Streamed section constants in FP32 (the FP64 constants rounded), once per upload; only for
+// sections that are not the circular section's (see MixedBeams).
 __global__ void __launch_bounds__(kBlock) k_mixed_constants(DevTopo t, MixedBeams m) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= t.B) return;
     m.C0[b] = make_float4(float(t.kb[b]), float(t.kt[b]), float(t.my[b]), float(t.ty[b]));
     m.C1[b] = make_float4(float(t.cs[b]), float(t.aL[b]), float(t.area[b]), float(t.aLsy[b]));
-    m.syf[b] = float(t.sy[b]);
+}
+
+// Section constants of beam b: (kb, kt, my, ty) and (cs, area L0, area, area L0 yield).  The
+// circular-section form derives them from r and L0 (area = pi r^2, I = pi r^4 / 4, J = 2 I:
+// kb = E I / L0, kt = G J / L0, my = yield I / r, ty = yield / sqrt 3 J / r,
+// cs = shear G area L0 / 2, MC/src/sim.cpp:115, 139-141); each is a few FP32 roundings from
+// the FP64 value, which the mixed form's tolerance covers.
+template <bool kStreamed>
+__device__ __forceinline__ void section_constants(const MixedBeams& m, int b, float r, float L0, const float4 ic,
+                                                  float4& C0, float4& C1) {
+    if (kStreamed) {
+        C0 = m.C0[b];
+        C1 = m.C1[b];
+    } else {
+        const float r2 = r * r, r3 = r2 * r, r4 = r2 * r2, inv = 1.f / L0, r2L = r2 * L0;
+        C0 = make_float4(m.kg.x * r4 * inv, m.kg.y * r4 * inv, ic.y * r3, ic.z * r3);
+        C1 = make_float4(m.kg.z * r2L, m.kg.w * r2L, m.kg.w * r2, ic.w * r2L);
+    }
 }
 
 // ---- beam kernel (MC/src/sim.cpp:139-141, FP32 with the split above) ---------------------
+template <bool kStreamed>
 __global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
@@ -290,7 +307,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material m
     float acc[3] = {0.f, 0.f, 0.f};
     if (mp.valid) {
         const int2 ab = t.ab[b];
-        const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B3 = m.B3[b], B4 = m.B4[b], B5 = m.B5[b];
+        const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B5 = m.B5[b];
         const float4 ua4 = U[ab.x], ub4 = U[ab.y];
         const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
         const float c0 = B0.w, L0 = B1.w, Lb = B2.w;
@@ -313,9 +330,11 @@ __global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material m
             const float invL = 1.f / L;
             const f3 tt = d * invL;
             const float eps = q / ((L + L0) * L0);
-            const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), rotp
-            const float4 C0 = m.C0[b], C1 = m.C1[b];  // (kb, kt, my, ty), (cs, aL, area, aLsy)
-            const float E = mat.Ef, H = mat.Hf, sy = m.syf[b];
+            const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), (rotp, r)
+            const float4 ic = m.ic[mp.inst];
+            float4 C0, C1;  // (kb, kt, my, ty), (cs, aL, area, aLsy)
+            section_constants<kStreamed>(m, b, P1.w, L0, ic, C0, C1);
+            const float E = mat.Ef, H = mat.Hf, sy = ic.x;
             // axial
             const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
             const float uax = C1.y * (ax.energy + ax.hard);
@@ -325,12 +344,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material m
             const float4 ea = Ei[ab.x], eb = Ei[ab.y];
             const f3 va = xyz(make_float4(ea.y, ea.z, ea.w, 0.f)), vb = xyz(make_float4(eb.y, eb.z, eb.w, 0.f));
             const float wa = 1.f + ea.x, wb = 1.f + eb.x;
-            const f3 da0 = xyz(B1), db0 = xyz(B2);
+            // base directors d_a0 = t0 + s_a0, d_b0 = t0 + s_b0: they only enter multiplied by
+            // a small vector (the rotation increment, the shear vector), so the ~1e-7 of the
+            // FP32 t0 is harmless; the small s_a0, s_b0 themselves come exact from FP64
+            const f3 sa0 = xyz(B1), sb0 = xyz(B2);
+            const f3 t0 = d0 * (1.f / Lb);
+            const f3 da0 = t0 + sa0, db0 = t0 + sb0;
             const f3 dda = rot_inc(wa, va, da0), ddb = rot_inc(wb, vb, db0);
             const f3 da = da0 + dda, db = db0 + ddb;
             const float dLb = (2.f * fdot(d0, du) + fdot(du, du)) / (L + Lb);
             const f3 tdiff = (du * Lb - d0 * dLb) * (1.f / (L * Lb));  // t - t0
-            const f3 ma = dda + xyz(B3) - tdiff, mb = ddb + xyz(B4) - tdiff;
+            const f3 ma = dda + sa0 - tdiff, mb = ddb + sb0 - tdiff;
             const float cs = C1.x;
             const float us = .5f * cs * (fdot(ma, ma) + fdot(mb, mb));
             const f3 gt = (ma + mb) * (-cs);  // cs (2t - da - db)
@@ -417,15 +441,16 @@ __global__ void __launch_bounds__(kBlock) k_plastic_pack(DevTopo t, const uint8_
     const int b = mp.i;
     const size_t S = size_t(t.B);
     P0[b] = make_float4(soa7[b], soa7[S + b], soa7[5 * S + b], soa7[6 * S + b]);
-    P1[b] = make_float4(soa7[2 * S + b], soa7[3 * S + b], soa7[4 * S + b], 0.f);
+    P1[b] = make_float4(soa7[2 * S + b], soa7[3 * S + b], soa7[4 * S + b], float(t.radius[b]));
 }
 __global__ void __launch_bounds__(kBlock) k_plastic_from_f64(int B, const double* __restrict__ soa7,
+                                                             const double* __restrict__ radius,
                                                              float4* __restrict__ P0, float4* __restrict__ P1) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     const size_t S = size_t(B);
     P0[b] = make_float4(float(soa7[b]), float(soa7[S + b]), float(soa7[5 * S + b]), float(soa7[6 * S + b]));
-    P1[b] = make_float4(float(soa7[2 * S + b]), float(soa7[3 * S + b]), float(soa7[4 * S + b]), 0.f);
+    P1[b] = make_float4(float(soa7[2 * S + b]), float(soa7[3 * S + b]), float(soa7[4 * S + b]), float(radius[b]));
 }
 __global__ void __launch_bounds__(kBlock) k_plastic_to_f64(DevTopo t, const uint8_t* __restrict__ mask,
                                                            const float4* __restrict__ P0,
@@ -456,7 +481,8 @@ void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, 
 void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
                         EvalBufs& e, cudaStream_t s) {
     if (t.B == 0) return;
-    k_beams_mixed<<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
+    if (mb.C0) k_beams_mixed<true><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
+    else k_beams_mixed<false><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
     note_launches(1);
 }
 
@@ -471,7 +497,7 @@ void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* b
 }
 
 void launch_mixed_constants(const DevTopo& t, MixedBeams& mb, cudaStream_t s) {
-    if (!t.B) return;
+    if (!t.B || !mb.C0) return;
     k_mixed_constants<<<grid_for(t.B), kBlock, 0, s>>>(t, mb);
     note_launches(1);
 }
@@ -480,7 +506,7 @@ void launch_plastic_mixed(const DevTopo& t, const uint8_t* mask, const double* p
                           MixedBeams& mb, cudaStream_t s) {
     if (!t.B) return;
     if (trial32) k_plastic_pack<<<t.n_bblk, kBlock, 0, s>>>(t, mask, trial32, mb.P0, mb.P1);
-    else k_plastic_from_f64<<<grid_for(t.B), kBlock, 0, s>>>(t.B, plastic64, mb.P0, mb.P1);
+    else k_plastic_from_f64<<<grid_for(t.B), kBlock, 0, s>>>(t.B, plastic64, t.radius, mb.P0, mb.P1);
     note_launches(1);
 }
 

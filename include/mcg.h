@@ -8,10 +8,11 @@
  *                                                               MC/src/sim.cpp:138-172)
  * and its caller Simulator::minimize (MC/src/sim.cpp:174-211).  The reference has no
  * FFI of its own; the entry points below are what its solver binds to replace that
- * member (the patch is shown in INTEGRATION.md): plain pointers and sizes, no C++ or
- * torch types.  Every function returns an int status (MCG_OK = 0); mcg_last_error()
- * gives the message.  Contexts own their device memory and are not thread-safe: use
- * one context per host thread, as the reference uses one Simulator per thread.
+ * member: plain pointers and sizes, no C++ or torch types.  Every function returns an int
+ * status (MCG_OK = 0); mcg_last_error() gives the message.  Contexts own their device
+ * memory and are not thread-safe: use one context per host thread, as the reference uses
+ * one Simulator per thread.  Every call on a context makes the context's CUDA device the
+ * current device of the calling thread.
  *
  * Layouts (all host arrays are caller-owned, copied in/out):
  *   z, grad      6 doubles per node: [tx, ty, tz, rx, ry, rz]; translations in units of
@@ -176,15 +177,19 @@ int mcg_objective(mcg_ctx* ctx, const double* z, double top, int trials, double*
                   uint8_t* trial_flags);
 
 /* The same evaluation as mcg_objective (without trial states) for callers that must not
- * allocate device memory when they evaluate: code inside a CUDA stream capture (where
- * cudaMalloc/cudaFree are not permitted), fixed-budget real-time loops, hosts whose device
- * memory belongs to another allocator.  mcg_objective may re-allocate its self-contact
- * buffers to fit a state; this entry point uses a fixed 4 MiB __device__ array instead
- * and calls no allocating routine.  Limits: at most 4096 nodes and 8192 nodes + beams, and
- * per evaluation 4096 grid bins of at most 128 entries each, 32768 candidate pairs and 8192
- * contacts; beyond them it returns MCG_ERR_CAPACITY, naming what overflowed.  The first
- * call on a device looks up the array's device address, so make it before any stream
- * capture.  All calls on a device share the array: calls that overlap on the GPU race.
+ * allocate device memory when they evaluate: real-time loops with a fixed device-memory
+ * budget, hosts whose device memory belongs to another allocator, schedulers that cannot
+ * afford cudaFree's wait for the whole device.  mcg_objective may re-allocate its
+ * self-contact buffers to fit a state; this entry point uses a fixed 4 MiB __device__ array
+ * instead and calls no allocating routine.  Limits: at most 4096 nodes and 8192 nodes +
+ * beams, and per evaluation 4096 grid bins (the grid box of the deformed specimen at the
+ * reference's grid cell: about 9 cells per axis of a cube) of at most 128 entries each,
+ * 32768 candidate pairs and 8192 contacts; beyond them it returns MCG_ERR_CAPACITY, naming
+ * what overflowed.  The first call on a context sets up: it looks up the array's device
+ * address on the context's device (cudaGetSymbolAddress) and keeps it in the context.  All
+ * calls on a device share the array, which keeps the last call's contents: calls that
+ * overlap on the GPU race.  After such a call mcg_contact_pairs and mcg_contact_stats
+ * return MCG_ERR_STATE until the next allocating evaluation (its contacts are not kept).
  * No counterpart in the reference. */
 int mcg_objective_noalloc(mcg_ctx* ctx, const double* z, double top, double* energy, double* grad,
                           mcg_diag* diag);
@@ -222,6 +227,17 @@ int mcg_commit(mcg_ctx* ctx);
  * returned.  With `verbose` one line per increment goes to stdout in the reference's
  * format (MC/src/sim.cpp:441-451). */
 int mcg_run(mcg_ctx* ctx, mcg_frame* frames, int32_t capacity, int32_t* count, int verbose);
+
+/* The reference CLI's run outputs from run() frames (host only, no context needed):
+ * mcg_write_metrics_csv writes the per-increment metrics CSV of MC/src/main.cpp:112-128
+ * (writeMetrics: 28 columns, 14 significant digits); mcg_write_summary_json the run summary
+ * of MC/src/main.cpp:130-155 (writeSummary: peak force and stress, works, SEA, permanent
+ * set, maximum penetration, unconverged increments; 12 significant digits).  `material` is
+ * the material's name (MaterialConfig::name, MC/include/sim.hpp:16; NULL: empty) and mass_kg
+ * the specimen's mass (mcg_geometry.mass).  MCG_ERR_INVALID when the file cannot be written. */
+int mcg_write_metrics_csv(const mcg_frame* frames, int32_t count, const char* path);
+int mcg_write_summary_json(const mcg_frame* frames, int32_t count, const mcg_config* cfg, double mass_kg,
+                           const char* material, const char* path);
 
 /* The CUDA stream the context launches on (a cudaStream_t), for callers that time
  * or order work around it. */
@@ -325,6 +341,14 @@ int mcg_phase_times(mcg_ctx* ctx, double* ms, int32_t n, int64_t* evaluations);
 enum mcg_lattice_kind {
     MCG_LATTICE_CUBIC = 0,     /* cell-edge struts */
     MCG_LATTICE_CUBIC_BCC = 1, /* cell edges + 8 centre-to-corner half-diagonals per cell */
+    MCG_LATTICE_REFERENCE_BCC = 2, /* the reference's own specimen, Simulator::build
+                                      (MC/src/sim.cpp:51-132) bit for bit: graded BCC with
+                                      face grids, seeded imperfections, elements_per_strut
+                                      (2..5) elements per strut.  Built from cfg (cells,
+                                      cell_size, radii, joint/trigger scales, imperfections,
+                                      elements_per_strut, seed); the spec's other fields are
+                                      ignored.  As in the reference, set translation_scale to
+                                      cell_size (MC/src/sim.cpp:49). */
 };
 
 enum mcg_radius_mode {
@@ -365,7 +389,7 @@ typedef struct mcg_lattice mcg_lattice;
 
 /* Builds a lattice; mass and locks follow the reference rules
  * (Simulator::distributeMass, MC/src/sim.cpp:134) with cfg's density, joint_scale and
- * max_radius. */
+ * max_radius.  For MCG_LATTICE_REFERENCE_BCC the whole lattice comes from cfg. */
 int mcg_lattice_generate(const mcg_lattice_spec* spec, const mcg_config* cfg,
                          mcg_lattice** out);
 int mcg_lattice_view_of(const mcg_lattice* lat, mcg_lattice_view* view);

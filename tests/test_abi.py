@@ -183,3 +183,61 @@ def test_sweep_workload_follows_its_specification():
     assert all(30e6 <= y <= 70e6 for y in ys)
     cfg2, specs2, ys2 = workloads.sweep()
     assert ys2 == ys and [s.seed for s in specs2] == [s.seed for s in specs]
+
+
+def test_run_outputs_match_the_reference_writers_byte_for_byte(mcg, tmp_path):
+    """mcg_write_metrics_csv / mcg_write_summary_json on the reference's own 20/14 run frames
+    (tests/golden/ref242.npz) write exactly the files the reference CLI's writeMetrics and
+    writeSummary (MC/src/main.cpp:112-155) wrote for them (tests/golden/ref242_metrics.csv,
+    ref242_summary.json, made by tests/golden/make_golden.py --outputs)."""
+    from conftest import GOLDEN, golden
+    g = golden("ref242")
+    frames = g.frames()
+    for f in frames:
+        for k in abi.FRAME_INTS:
+            if k in f:
+                f[k] = int(f[k])
+    csv = tmp_path / "metrics.csv"
+    js = tmp_path / "summary.json"
+    mcg.write_metrics_csv(frames, str(csv))
+    mcg.write_summary_json(frames, g.cfg, float(g.d["lat_geometry"][4]), str(js))
+    assert csv.read_bytes() == open(os.path.join(GOLDEN, "ref242_metrics.csv"), "rb").read()
+    assert js.read_bytes() == open(os.path.join(GOLDEN, "ref242_summary.json"), "rb").read()
+    with pytest.raises(mcg.MCGError):
+        mcg.write_metrics_csv(frames, str(tmp_path / "no" / "such" / "dir.csv"))
+
+
+def reference_spec():
+    s = abi.LatticeSpec()
+    s.kind = abi.MCG_LATTICE_REFERENCE_BCC
+    return s
+
+
+def same_arrays(a, b):
+    return all(getattr(a, f).shape == getattr(b, f).shape and
+               np.array_equal(getattr(a, f).view(np.uint8), getattr(b, f).view(np.uint8)) for f in a.FIELDS)
+
+
+def test_reference_builder_reproduces_the_reference_specimen(mcg):
+    """MCG_LATTICE_REFERENCE_BCC builds the reference's own 2x4x2 specimen
+    (Simulator::build, MC/src/sim.cpp:51-134) bit for bit: the arrays of tests/golden/ref242.npz
+    were exported from the reference's own Simulator."""
+    from conftest import golden
+    g = golden("ref242")
+    lat = mcg.generate_lattice(reference_spec(), g.cfg)
+    assert same_arrays(lat, g.lattice)
+    for n, _ in abi.Geometry._fields_:
+        assert getattr(lat.geometry, n) == getattr(g.lattice.geometry, n), n
+
+
+@pytest.mark.parametrize("cells,elements", [((3, 4, 3), 3), ((5, 6, 4), 2), ((4, 4, 4), 5), ((6, 3, 2), 4)])
+def test_reference_builder_matches_the_reference_live(mcg, ref_oracle, cells, elements):
+    """Against the reference's builder compiled here, over cell counts and 2-5 elements per
+    strut (3x4x3 with 3 elements is the reference's own ctest specimen: 788 nodes, 1008
+    beams)."""
+    cfg = abi.default_config(cells_x=cells[0], cells_y=cells[1], cells_z=cells[2], elements_per_strut=elements)
+    cfg.translation_scale = cfg.cell_size
+    lat = mcg.generate_lattice(reference_spec(), cfg)
+    assert same_arrays(lat, ref_oracle.Model("ref", cfg).export())
+    if cells == (3, 4, 3):
+        assert (lat.n_nodes, lat.n_beams) == (788, 1008)
