@@ -156,3 +156,71 @@ def test_candidate_list_reuse_is_bitwise_transparent(mcg):
     for fr in runs[1:]:
         got = np.array([[f[k] for k in keys] for f in fr])
         assert got.shape == ref.shape and np.array_equal(got, ref)
+
+
+def short_run_cfg(g, max_iterations):
+    """The 6x6x6 specimen in 3 loading + 2 unloading increments (13 % strain each) with an
+    iteration cap that makes increments fail.  At 39 iterations the first four loading
+    increments are bisected once (sim.cpp:405-411) and the run completes in 8 frames; at 6 the
+    first increment fails at every one of the 7 bisection levels and the run ends in the
+    equilibrium failure (:412-419).  Both caps were chosen so that the path is the same under
+    all 32 rounding-order variants of the CPU restatement (every increment's iteration count
+    is at least 2 away from the cap), i.e. it does not hinge on rounding."""
+    cfg = g.cfg
+    cfg.max_iterations = max_iterations
+    cfg.load_steps = 3
+    cfg.unload_steps = 2
+    return cfg
+
+
+@pytest.mark.parametrize("max_iterations,status,frames", [(39, 0, 8), (6, 5, 1)])
+def test_run_bisects_and_fails_like_the_oracle(mcg, mco, max_iterations, status, frames):
+    """Failed increments are replaced by their midpoint and themselves, at most
+    max_adaptive_refinements deep (sim.cpp:405-411); beyond that the run stops with the
+    equilibrium failure (:412-419).  The GPU run must take the same path as the CPU
+    restatement of the reference driver: same accepted increments at the same platen
+    positions and refinement levels, same outcome."""
+    g = golden("cubic6")
+    cfg = short_run_cfg(g, max_iterations)
+    rc_o, fo = mco.Model("mco", cfg, lattice=g.lattice).run()
+    sol = mcg.Solver(cfg, g.lattice)
+    rc_g, fg = sol.run()
+    err = sol.lib.mcg_last_error(sol.h).decode()
+    sol.close()
+    print(f"max_iterations {max_iterations}: status {rc_g} (oracle {rc_o}), {len(fg)} frames "
+          f"({sum(1 for f in fg if f['refinement'])} refined), {err}")
+    assert rc_o == status and rc_g == status
+    assert len(fg) == len(fo) == frames
+    assert [f["refinement"] for f in fg] == [f["refinement"] for f in fo]
+    assert [f["platen_y"] for f in fg] == [f["platen_y"] for f in fo]
+    # the increments are solved to the reference's tolerance, which at 13 % strain per increment
+    # leaves reactions agreeing to ~1e-5 of the peak between two rounding orders
+    peak = max(f["reaction_force"] for f in fo)
+    assert max(abs(a["reaction_force"] - b["reaction_force"]) for a, b in zip(fg, fo)) <= 1e-4 * max(peak, 1e-12)
+    if status:
+        assert "equilibrium failed" in err
+    else:
+        assert sum(1 for f in fg if f["refinement"]) == 4
+
+
+def test_relative_gradient_mode_reaches_1e8_on_a_loading_increment(mcg, mco):
+    """relative_gradient_tolerance = 1e-8 (rms(g) <= 1e-8 rms(g0), the solver setting of the
+    6x6x6 workload) on the specimen's first loading increment: ~550 L-BFGS iterations.  The
+    GPU and the CPU restatement must both converge there, to the same equilibrium."""
+    g = golden("cubic6")
+    cfg = g.cfg
+    cfg.relative_gradient_tolerance = 1e-8
+    cfg.max_iterations = 3000
+    top = float(g.d["min_top"][0])
+    z0 = np.zeros(6 * g.lattice.n_nodes)
+    sol = mcg.Solver(cfg, g.lattice)
+    zg, stg, feg, _ = sol.minimize(top, z0)
+    sol.close()
+    zo, sto, feo, _ = mco.Model("mco", cfg, lattice=g.lattice).minimize(top, z0)
+    print("relative 1e-8: GPU", stg, "oracle", sto, "z rel err", rel_err(zg, zo))
+    assert stg["converged"] == 1 and sto["converged"] == 1
+    assert stg["rms"] <= 1e-8 * 0.4632 and sto["rms"] <= 1e-8 * 0.4632  # rms(g0) = 0.4632
+    # both at the same minimum: energies within FP64 summation-order noise; the iterates agree
+    # to ~2e-5 (a gradient reduced 1e8-fold still leaves the soft modes of the lattice loose)
+    assert abs(feg - feo) <= 1e-10 * abs(feo)
+    assert rel_err(zg, zo) <= 1e-4
