@@ -98,14 +98,6 @@ def workload(name):
     return getattr(workloads, name)()
 
 
-def sample_spec(name):
-    """A bounded CPU sample of the same lattice family (cells scaled down)."""
-    from falling_dice_gb300 import workloads
-    if name.startswith("bcc"):
-        return workloads.bcc((12, 12, 6))
-    return workloads.cubic6()
-
-
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -162,70 +154,99 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_sample_eval_seconds(name, repeat=1):
-    """One-core time of the reference objective (CPU restatement) on the bounded sample."""
-    import falling_dice_gb300 as fd
+def cpu_model():
+    """The host CPU's model name and core count, for the CPU-baseline records."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"model": name or "unknown", "cores": os.cpu_count() or 1}
+
+
+# -- the reference's CPU path (the oracle's restatement of it; test infrastructure) ----------
+# Workers build the specimen and its seeded state with the oracle's own restatement of the
+# workload generator (oracle/specimens.cpp), so the CPU legs load no product library.
+_worker_model = None
+_worker_args = None
+
+
+def _worker_init(name):
+    global _worker_model, _worker_args
+    sys.path.insert(0, ROOT)
+    from falling_dice_gb300 import workloads
+    from oracle import oracle as orc
+    cfg, spec = getattr(workloads, name)()
+    m = orc.Model("mco", cfg, lattice=spec)
+    lat = m.export()
+    z, pl = orc.random_state(lat.n_nodes, lat.n_beams, lat.locked, **workloads.DEFORM)
+    m.set_state(plastic=pl)
+    _worker_model = m
+    _worker_args = (z, lat.geometry.top0 + 0.01, lat.n_nodes, lat.n_beams)
+
+
+def _worker_eval(_):
+    """One full evaluation of the reference objective at the benchmark state; (seconds, E)."""
+    z, top, _, _ = _worker_args
+    t = time.perf_counter()
+    e = _worker_model.objective(z, top)["energy"]
+    return time.perf_counter() - t, e
+
+
+def cpu_one_core(name):
+    """One full-size evaluation of the reference objective (the oracle port) on one core."""
     from oracle import oracle as orc
     orc.build("mco")
-    cfg, spec = sample_spec(name)
-    lat = fd.generate_lattice(spec, cfg)
-    m = orc.Model("mco", cfg, lattice=lat)
-    from falling_dice_gb300 import workloads
-    z, pl = fd.random_state(lat, **workloads.DEFORM)
-    m.set_state(plastic=pl)
-    top = lat.geometry.top0 + 0.01
-    m.objective(z, top)
-    t = time.perf_counter()
-    for _ in range(repeat):
-        m.objective(z, top)
-    return (time.perf_counter() - t) / repeat, lat.n_beams, lat.n_nodes
-
-
-def _ref_worker(args):
-    name, repeat = args
-    sys.path.insert(0, ROOT)
-    return cpu_sample_eval_seconds(name, repeat)
+    _worker_init(name)
+    dt, e = _worker_eval(0)
+    return dt, e, _worker_args[2], _worker_args[3]
 
 
 def run_reference(a, rank, world):
-    """--impl reference: the reference CPU objective on all host cores."""
+    """--impl reference: the reference CPU objective (the oracle port of it) on all host
+    cores, one process per core; every step is one full evaluation of the benchmark
+    specimen at the benchmark state, and the steps are spread over the processes."""
     if rank != 0:
         return
     import multiprocessing as mp
-    cfg, spec = workload(a.workload)
-    import falling_dice_gb300 as fd
-    lat = fd.generate_lattice(spec, cfg)
-    B_full = lat.n_beams
-    cores = os.cpu_count() or 1
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as orc
+    orc.build("mco")
+    host = cpu_model()
+    cores = host["cores"]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        for _ in range(a.warmup if a.warmup < 1 else 1):
-            pool.map(_ref_worker, [(a.workload, 1)] * cores)
+    with ctx.Pool(cores, initializer=_worker_init, initargs=(a.workload,)) as pool:
+        pool.map(_worker_eval, range(max(1, min(a.warmup, cores))), chunksize=1)  # untimed
         t0 = time.perf_counter()
-        res = []
-        for _ in range(a.steps):
-            res += pool.map(_ref_worker, [(a.workload, 1)] * cores)
+        res = pool.map(_worker_eval, range(a.steps), chunksize=1)
         wall = time.perf_counter() - t0
-    per_eval = float(np.mean([r[0] for r in res]))
-    B_s = res[0][1]
-    # each worker's time includes its lattice build; use the measured evaluation time, all
-    # cores in parallel: evals/s at full size = cores / (t_sample * B_full / B_sample)
-    value = cores / (per_eval * B_full / B_s)
-    sample = (f"{sample_spec(a.workload)[1].cells_x}x{sample_spec(a.workload)[1].cells_y}x"
-              f"{sample_spec(a.workload)[1].cells_z} cubic+BCC sample ({B_s} beams) of the same "
-              f"generator; per-evaluation time scaled by beam count to {B_full} beams")
-    kind = "reference" if os.path.exists(os.path.join(ROOT, "oracle", "_ref", "libmcref.so")) else "port"
+        N, B = pool.apply(_counts)
+    value = a.steps / wall
+    energies = {r[1] for r in res}
+    assert len(energies) == 1  # every process evaluated the same state
+    kind = "port"  # the CPU restatement, bit-identical to the reference (tests/test_oracle.py)
+    sample = (f"{a.steps} full evaluations of the {a.workload} specimen ({N} nodes, {B} beams) at the "
+              f"benchmark state, spread over {cores} processes; no scaling")
     line = {"impl": "reference", "metric": "beam energy-grad evals/s", "value": value, "unit": "evals/s",
             "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"{a.workload}: {lat.n_nodes} nodes, {B_full} beams",
-                       "parallelism": f"{cores} CPU processes"},
+            "config": {"workload": f"{a.workload}: {N} nodes, {B} beams, seeded deformed state",
+                       "parallelism": f"{cores} CPU processes", "cpu": host["model"]},
             "cpu_baseline": {"value": value, "unit": "evals/s", "cores": cores, "kind": kind,
-                             "sample": sample, "seconds_per_sample_eval": per_eval,
-                             "wall_s": wall},
+                             "sample": sample, "cpu": host["model"],
+                             "seconds_per_eval_mean": float(np.mean([r[0] for r in res])),
+                             "wall_s": wall, "energy": energies.pop()},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _counts():
+    return _worker_args[2], _worker_args[3]
 
 
 def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world, shapes=None):
@@ -364,12 +385,12 @@ def main():
                 "counts": st, "note": "issue-bound integer work (pair tests); the fraction is of HBM"}
     cpu = None
     if not a.no_cpu_baseline:
-        t_s, B_s, N_s = cpu_sample_eval_seconds(a.workload, repeat=2)
-        cs = sample_spec(a.workload)[1]
-        cpu = {"value": 1.0 / (t_s * B / B_s), "unit": "evals/s", "cores": 1, "kind": "port",
-               "sample": f"{cs.cells_x}x{cs.cells_y}x{cs.cells_z} cubic+BCC ({B_s} beams), 2 evaluations "
-                         f"of {t_s:.2f} s each, scaled by beam count to {B} beams",
-               "seconds_per_sample_eval": t_s}
+        t_s, e_cpu, N_s, B_s = cpu_one_core(a.workload)
+        cpu = {"value": 1.0 / t_s, "unit": "evals/s", "cores": 1, "kind": "port", "cpu": cpu_model()["model"],
+               "sample": f"one full evaluation of the {a.workload} specimen ({N_s} nodes, {B_s} beams) at the "
+                         f"benchmark state on one core, {t_s:.1f} s; no scaling",
+               "seconds_per_eval": t_s,
+               "energy_rel_err_vs_gpu_fp64": abs(e_cpu - plain["energy"]) / abs(e_cpu)}
     err_e = abs(mixed["energy"] - plain["energy"]) / abs(plain["energy"])
     err_g = float(np.linalg.norm(mixed["grad"] - plain["grad"]) / np.linalg.norm(plain["grad"]))
     eval_bytes_mixed = BEAM_BYTES_MIXED * B + NODE_BYTES_MIXED * N
@@ -418,6 +439,7 @@ def load_unload(fd, abi, workloads):
     FP64: wall time of the whole run (minimize, commit, diagnostics on the device; host
     decisions per round) and the run-level figures, with their errors against FP64."""
     out = {}
+    frames_of = {}
     for name, prec in (("mixed", abi.MCG_MIXED), ("fp64", abi.MCG_FP64)):
         cfg, spec = workloads.bcc32()
         cfg.precision = prec
@@ -427,19 +449,41 @@ def load_unload(fd, abi, workloads):
         rc, frames = sol.run()
         dt = time.perf_counter() - t0
         sol.close()
+        frames_of[name] = frames
         out[name] = dict(run_summary(frames), seconds=dt, status=int(rc))
     m, f = out["mixed"], out["fp64"]
     out["speedup_mixed_over_fp64"] = f["seconds"] / m["seconds"]
     out["rel_err_mixed_vs_fp64"] = {k: abs(m[k] - f[k]) / abs(f[k]) for k in
                                     ("peak_force", "absorbed_energy", "dissipated_work", "permanent_set")}
+    out["curve_mixed_vs_fp64"] = curve_divergence(frames_of["mixed"], frames_of["fp64"])
     out["workload"] = "bcc32: cubic+BCC 32x32x16, radius 0.25->0.7 mm graded, 60 % strain, 400 + 400 increments"
     return out
 
 
-def sweep(fd, abi, workloads, sample=4):
+def curve_divergence(a, b, bar=1e-5):
+    """Reaction-force curves of two runs compared at the schedule's own increments (frames
+    that were not bisected, matched by platen position): relative error against b's peak per
+    increment, its maximum and mean, and the first increment (with its strain) past `bar`."""
+    peak = max(f["reaction_force"] for f in b)
+    fb = {f["platen_y"]: f for f in b if f["refinement"] == 0}
+    errs = []
+    for k, f in enumerate(x for x in a if x["refinement"] == 0):
+        g = fb.get(f["platen_y"])
+        if g is not None and f["loading"] == g["loading"]:
+            errs.append((k, f["engineering_strain"], abs(f["reaction_force"] - g["reaction_force"]) / peak))
+    first = next(((k, s_) for k, s_, e in errs if e > bar), None)
+    return {"increments_compared": len(errs), "max_rel": max((e for _, _, e in errs), default=0.0),
+            "mean_rel": float(np.mean([e for _, _, e in errs])) if errs else 0.0,
+            "first_increment_beyond_1e-5": None if first is None else {"increment": first[0], "strain": first[1]},
+            "rel_by_increment_every_40": [round(e, 9) for _, _, e in errs[::40]]}
+
+
+def sweep(fd, abi, workloads, sample=32):
     """The batched sweep: 256 lattices (4-16 cells per side) solved together in FP64, against
-    the same lattices solved one after another (a spread sample of `sample` lattices timed,
-    throughput in lattices per second)."""
+    the same lattices solved one after another.  The sequential figure comes from a systematic
+    sample of `sample` lattices spread over the sweep's cost range (lattices ordered by beam
+    count, every 256/sample-th timed): mean time per lattice with its standard error, so the
+    sequential throughput and the speed-up carry an error bar."""
     cfg, specs, ys = workloads.sweep()
     lats = [fd.generate_lattice(s, cfg) for s in specs]
     b = fd.BatchSolver(cfg, lats, yields=ys)
@@ -448,20 +492,28 @@ def sweep(fd, abi, workloads, sample=4):
     status, runs = b.run()
     dt = time.perf_counter() - t0
     b.close()
-    idx = np.linspace(0, len(lats) - 1, sample).astype(int)
-    t0 = time.perf_counter()
+    order = np.argsort([l.n_beams for l in lats], kind="stable")
+    step = len(lats) / sample
+    idx = [int(order[int((j + 0.5) * step)]) for j in range(sample)]
+    times = []
     same = True
     for k in idx:
         c = abi.Config.from_buffer_copy(cfg)
         c.material.yield_ = ys[k]
         s = fd.Solver(c, lats[k])
+        t0 = time.perf_counter()
         rc, fr = s.run()
+        times.append(time.perf_counter() - t0)
         s.close()
         same &= [x["reaction_force"] for x in fr] == [x["reaction_force"] for x in runs[k]]
-    ds = time.perf_counter() - t0
-    batched, seq = len(lats) / dt, sample / ds
+    mean_t = float(np.mean(times))
+    se_t = float(np.std(times, ddof=1) / np.sqrt(len(times)))
+    batched, seq = len(lats) / dt, 1.0 / mean_t
     return {"metric": "lattices/s", "batched_fp64": batched, "sequential_fp64": seq, "speedup": batched / seq,
-            "batched_seconds": dt, "sequential_sample": f"{sample} lattices spread over the sweep, {ds:.1f} s",
+            "speedup_range_1se": [batched * (mean_t - se_t), batched * (mean_t + se_t)],
+            "batched_seconds": dt,
+            "sequential_sample": f"{sample} of {len(lats)} lattices, every {step:g}-th by beam count; "
+                                 f"{mean_t:.3f} +/- {se_t:.3f} s per lattice (standard error), {sum(times):.1f} s",
             "completed": int((np.asarray(status) == 0).sum()), "lattices": len(lats),
             "beams": int(sum(l.n_beams for l in lats)), "sample_frames_identical_to_batch": bool(same),
             "broad_phase": tune,
