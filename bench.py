@@ -64,10 +64,14 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mcg", choices=["mcg", "reference"])
     ap.add_argument("--workload", default="bcc64")
-    ap.add_argument("--shapes", default="", help="CELL,PAIR_BLOCKS: fixed broad-phase shapes instead of tuning")
+    ap.add_argument("--shapes", default="",
+                    help="CELL,PAIR_BLOCKS[,BEAM_BLOCKS,GATHER_BLOCKS]: fixed shapes instead of tuning "
+                         "(broad-phase cell and pair grid; CTAs per SM of the beam kernel and the gather)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the load/unload (32x32x16) and batched-sweep (256 lattices) measurements")
+    ap.add_argument("--largest-run", action="store_true",
+                    help="only the 128x128x64 load run (50 %% strain, 100 increments), mixed against FP64")
     return ap.parse_args()
 
 
@@ -257,9 +261,12 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world, sh
     sol = fd.Solver(cfg, lat, device=local)
     sol.set_contact_skin(0.0)  # a full evaluation: grid, pairs and narrow phase every step
     sol.set_state(plastic=pl)
-    if shapes:  # fixed broad-phase shapes (a saved tuning), e.g. for a profiler run
-        sol.set_contact_shapes(*shapes)
-        tune = {"cell": shapes[0], "pair_blocks": shapes[1], "tried": 0}
+    if shapes:  # fixed shapes (a saved tuning), e.g. for a profiler run
+        sol.set_contact_shapes(shapes[0], shapes[1])
+        kb = shapes[2:4] if len(shapes) >= 4 else (0, 0)
+        sol.set_kernel_shapes(*kb)
+        tune = {"cell": shapes[0], "pair_blocks": shapes[1], "beam_blocks": kb[0], "gather_blocks": kb[1],
+                "tried": 0}
     else:
         tune = sol.autotune(z, top, reps=3)  # broad-phase cell and pair grid, by measurement
     sol.upload_z(z)
@@ -334,6 +341,11 @@ def main():
     if a.impl == "reference":
         run_reference(a, rank, world)
         return
+    if a.largest_run:
+        import falling_dice_gb300 as fd
+        from falling_dice_gb300 import abi, workloads
+        print(json.dumps(largest_run(fd, abi, workloads)), flush=True)
+        return
     import torch
     import falling_dice_gb300 as fd
     from falling_dice_gb300 import abi, workloads
@@ -355,8 +367,8 @@ def main():
     cfg_mixed.precision = abi.MCG_MIXED
     shapes = None
     if a.shapes:
-        cell, blocks = a.shapes.split(",")
-        shapes = (float(cell), int(blocks))
+        parts = a.shapes.split(",")
+        shapes = (float(parts[0]),) + tuple(int(v) for v in parts[1:])
     mixed = measure(fd, torch, cfg_mixed, lat, z, pl, top, a.steps, a.warmup, local, pg, world, shapes)
     plain = measure(fd, torch, cfg, lat, z, pl, top, a.steps, a.warmup, local, pg, world, shapes)
     if rank != 0:
@@ -405,7 +417,10 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2 (beam arrays alone exceed 129 MB)",
                    "contact_list": "rebuilt at every evaluation (grid, pairs, narrow phase)",
-                   "broad_phase": {k: mixed["tuning"][k] for k in ("cell", "pair_blocks", "tried")}},
+                   "shapes": {k: mixed["tuning"].get(k) for k in ("cell", "pair_blocks", "beam_blocks",
+                                                                   "gather_blocks", "tried")},
+                   "shapes_fp64": {k: plain["tuning"].get(k) for k in ("cell", "pair_blocks", "beam_blocks",
+                                                                        "gather_blocks", "tried")}},
         "error_vs_fp64": {"energy_rel": err_e, "grad_rel_2norm": err_g},
         "hbm_gbs_algorithmic": eval_bytes_mixed * mixed["value"] / world / 1e9,
         "phase_ms": mixed["phases"],
@@ -457,6 +472,43 @@ def load_unload(fd, abi, workloads):
                                     ("peak_force", "absorbed_energy", "dissipated_work", "permanent_set")}
     out["curve_mixed_vs_fp64"] = curve_divergence(frames_of["mixed"], frames_of["fp64"])
     out["workload"] = "bcc32: cubic+BCC 32x32x16, radius 0.25->0.7 mm graded, 60 % strain, 400 + 400 increments"
+    return out
+
+
+def largest_run(fd, abi, workloads):
+    """The largest single instance: 128x128x64 cubic+BCC (11.6 M beams), 50 % strain in 100
+    increments with self-contact, mixed against FP64: wall time, run figures and their errors,
+    per-increment curve error, and the mixed beam kernel's HBM fraction at this size."""
+    out = {"workload": "bcc128: cubic+BCC 128x128x64, radii U[0.3, 0.6] mm, +/-2 % jitter, 50 % strain in "
+                       "100 increments, self-contact on"}
+    frames_of = {}
+    peak, peak_kind = measured_peaks()
+    for name, prec in (("mixed", abi.MCG_MIXED), ("fp64", abi.MCG_FP64)):
+        cfg, spec = workloads.bcc128()
+        cfg.precision = prec
+        lat = fd.generate_lattice(spec, cfg)
+        sol = fd.Solver(cfg, lat)
+        t0 = time.perf_counter()
+        rc, frames = sol.run()
+        dt = time.perf_counter() - t0
+        frames_of[name] = frames
+        out[name] = dict(run_summary(frames), seconds=dt, status=int(rc), beams=lat.n_beams, nodes=lat.n_nodes)
+        # one evaluation at the final committed state, phases timed, for the beam kernel's roofline
+        sol.set_timing(True)
+        for _ in range(5):
+            sol.objective_resident(lat.geometry.top0)
+        ph, nev = sol.phase_times()
+        sol.close()
+        ms = ph["beams"] / nev
+        nbytes = (BEAM_BYTES_MIXED if prec == abi.MCG_MIXED else BEAM_BYTES) * lat.n_beams
+        out[name]["beam_kernel"] = {"ms": ms, "gbs_algorithmic": nbytes / (ms * 1e-3) / 1e9,
+                                    "frac_of_hbm": nbytes / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind}
+        out[name]["eval_ms"] = sum(ph[k] for k in sol.PHASES) / nev
+    m, f = out["mixed"], out["fp64"]
+    out["speedup_mixed_over_fp64"] = f["seconds"] / m["seconds"]
+    out["rel_err_mixed_vs_fp64"] = {k: abs(m[k] - f[k]) / abs(f[k]) for k in
+                                    ("peak_force", "absorbed_energy", "permanent_set")}
+    out["curve_mixed_vs_fp64"] = curve_divergence(frames_of["mixed"], frames_of["fp64"])
     return out
 
 

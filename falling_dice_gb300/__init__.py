@@ -52,6 +52,7 @@ SIGNATURES = {
     "mcg_set_contact_cell": (C.c_int, [_P, C.c_double]),
     "mcg_autotune": (C.c_int, [_P, _d, _d, C.c_int32, C.POINTER(abi.Tuning)]),
     "mcg_set_contact_shapes": (C.c_int, [_P, C.c_double, C.c_int32]),
+    "mcg_set_kernel_shapes": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -302,7 +303,14 @@ class Solver:
         self._check(self.lib.mcg_autotune(self.h, _ptr(zp), _ptr(tp), int(reps), C.byref(t)),
                     "mcg_autotune")
         return {"cell": t.cell, "pair_blocks": t.pair_blocks, "tried": t.tried,
-                "ms_chosen": t.ms_chosen, "ms_default": t.ms_default}
+                "ms_chosen": t.ms_chosen, "ms_default": t.ms_default,
+                "beam_blocks": t.beam_blocks, "gather_blocks": t.gather_blocks}
+
+    def set_kernel_shapes(self, beam_blocks, gather_blocks):
+        """Occupancy of the beam kernel and the gather (CTAs per SM, 0: default), as autotune()
+        reports them."""
+        self._check(self.lib.mcg_set_kernel_shapes(self.h, int(beam_blocks), int(gather_blocks)),
+                    "mcg_set_kernel_shapes")
 
     def set_contact_shapes(self, cell, pair_blocks):
         """Grid cell (m, 0: the reference's) and pair-enumeration blocks (0: default), as

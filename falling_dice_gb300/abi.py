@@ -60,6 +60,7 @@ class Config(C.Structure):
         ("seed", C.c_uint64),
         ("relative_gradient_tolerance", C.c_double),
         ("precision", C.c_int32), ("self_contact", C.c_int32),
+        ("reaction_relative_tolerance", C.c_double),
     ]
 
 
@@ -91,6 +92,7 @@ def default_config(**overrides):
     c.relative_gradient_tolerance = 0.0
     c.precision = MCG_FP64
     c.self_contact = 1
+    c.reaction_relative_tolerance = 1.5e-3  # sim.cpp:177
     ts_given = "translation_scale" in overrides
     for k, v in overrides.items():
         if k in ("density", "young", "nu", "yield_", "hardening", "bend_hardening",
@@ -131,7 +133,8 @@ class Diag(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("cell", C.c_double), ("pair_blocks", C.c_int32), ("tried", C.c_int32),
-                ("ms_chosen", C.c_double), ("ms_default", C.c_double)]
+                ("ms_chosen", C.c_double), ("ms_default", C.c_double),
+                ("beam_blocks", C.c_int32), ("gather_blocks", C.c_int32)]
 
 
 class OptStats(C.Structure):

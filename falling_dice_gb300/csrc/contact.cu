@@ -42,7 +42,6 @@ constexpr uint32_t kGuard2 = 0x80008000u;
 constexpr uint32_t kShapeBits = 29;     // shape id below, first-cell flags above
 constexpr int kPairWarps = kBlock / 32;
 constexpr int kPairGrab = 2;             // bins a warp claims at a time (<= 32)
-constexpr int kPairStage = 128;          // candidates a warp stages before appending them
 constexpr int kPairRanks = 128;          // bins up to this size are enumerated from registers
 constexpr int kStreamBlocks = 8 * 152;
 
@@ -427,78 +426,96 @@ __device__ __forceinline__ bool pair_test(const PairRec& A, const PairRec& B) {
 
 constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 
+// Appends every lane's hits to the flat candidate list: lane l's hits are the set bits of
+// `bits`, bit k standing for its pair with the record partner(k) returns; the lanes' counts
+// are placed by a warp scan behind one atomic on ncand.  Past cand_cap the pairs are counted
+// but not stored and kOverCandidates is raised.  All lanes of the warp call it.
+template <typename Partner>
+__device__ __forceinline__ void append_bits(uint32_t bits, uint32_t me, Partner partner, int lane,
+                                            long long cand_cap, uint2* __restrict__ cand,
+                                            uint32_t* __restrict__ ncand, uint32_t* __restrict__ flags) {
+    const uint32_t cnt = uint32_t(__popc(bits));
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;  // warp-uniform
+    uint32_t base = 0;
+    if (lane == 0) {
+        base = atomicAdd(ncand, total);
+        if ((long long)base + total > cand_cap) atomicOr(flags, uint32_t(kOverCandidates));
+    }
+    long long at = (long long)__shfl_sync(0xffffffffu, base, 0) + (incl - cnt);
+    while (bits) {
+        const int k = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t o = partner(k);
+        if (at < cand_cap) cand[at] = make_uint2(min(me, o), max(me, o));
+        at++;
+    }
+}
+
 // Every unordered pair of the records at ranks base .. base + m - 1 (m <= 32; lane i holds
 // rank base + i in `me`, and all of them are staged in shared memory), by rotation: in
 // round k lane i meets rank base + (i + k) mod m, k = 1 .. m/2 (the last round of an even m
-// only from the lower half), the partner's record read from shared memory.
-template <typename Emit>
+// only from the lower half), the partner's record read from shared memory.  Hits are kept as
+// one bit per round and appended at the end.
 __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __restrict__ srec,
-                                             const int2* __restrict__ snd, int base, int m, int lane, Emit& emit) {
+                                             const int2* __restrict__ snd, int base, int m, int lane,
+                                             long long cand_cap, uint2* __restrict__ cand,
+                                             uint32_t* __restrict__ ncand, uint32_t* __restrict__ flags) {
     const int half = m >> 1;
     int src = lane;
+    uint32_t bits = 0;
     for (int k = 1; k <= half; k++) {
         src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
         const uint4 r = srec[base + src];
         const int2 q = snd[base + src];
         const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
         const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
-        emit(active && pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
+        bits |= uint32_t(active && pair_test(me, o)) << (k - 1);
     }
+    append_bits(bits, me.id & kIdMask,
+                [&](int k) {
+                    int j = lane + k + 1;
+                    j = j >= m ? j - m : j;
+                    return srec[base + j].x & kIdMask;
+                },
+                lane, cand_cap, cand, ncand, flags);
 }
 
 // Candidate pairs of every bin holding two or more shapes.  Warps claim the grid's bins
 // kPairGrab at a time (single bins near the end) from a cursor (flags[3]) and skip the empty
-// ones (one ballot), so bins of uneven size balance over the grid; they count the build's cell entries and occupied
-// bins into nentries[0] and [2] on the way, stage their
-// candidate pairs (lower shape, higher shape) in shared memory and append them to the flat
-// list in chunks (one atomic on ncand per chunk), without a counting pass.  The list's
-// length is the number of pairs, whatever the order; past cand_cap the pairs are counted
-// but not stored and kOverCandidates is raised, so the host can size the list exactly.
+// ones (one ballot), so bins of uneven size balance over the grid; they count the build's
+// cell entries and occupied bins into nentries[0] and [2] on the way, and append their
+// candidate pairs (lower shape, higher shape) to the flat list in warp-sized batches, one
+// atomic on ncand per batch, without a counting pass.  The list's length is the number of
+// pairs, whatever the order.
 // Enumeration inside a bin, entries in bin order:
 //   n <= 128  the entries in groups of 32, lane i holding entry 32 g + i of group g and every
 //             record staged in shared memory: the pairs inside each group by rotation
 //             (rotate_pairs), then each full group against every record of the later groups
-//             (one record read by all lanes per round);
+//             (one record read by all lanes per round), hits kept as bits over windows of 32
+//             partners;
 //   larger    pairs by index, records read from global memory.
-__global__ void __launch_bounds__(kBlock, 7) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
+__global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, int bin_slots,
                                                       uint32_t* __restrict__ nentries,
                                                       const uint32_t* __restrict__ bin_items,
                                                       const uint4* __restrict__ rec, long long cand_cap,
                                                       uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
                                                       uint32_t* __restrict__ flags) {
-    __shared__ uint2 stage_all[kPairWarps][kPairStage];
     __shared__ uint4 rec_all[kPairWarps][kPairRanks];  // the bin's records, staged for the partner reads
     __shared__ int2 nd_all[kPairWarps][kPairRanks];
     if (!flags[1]) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const unsigned below = (1u << lane) - 1u;
     const uint32_t nbins = uint32_t(grid[8]);
-    uint2* stage = stage_all[w];
     uint4* srec = rec_all[w];
     int2* snd = nd_all[w];
     uint32_t* cursor = flags + 3;
-    uint32_t staged = 0;  // warp-uniform
-    // appends the staged candidates to the list: one atomic per chunk
-    auto flush = [&]() {
-        __syncwarp();
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(ncand, staged);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        for (uint32_t k = lane; k < staged; k += 32)
-            if ((long long)base + k < cand_cap) cand[base + k] = stage[k];
-        if (lane == 0 && (long long)base + staged > cand_cap) atomicOr(flags, uint32_t(kOverCandidates));
-        staged = 0;
-        __syncwarp();
-    };
-    auto emit = [&](bool hit, uint32_t sa, uint32_t sb) {
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (m) {  // warp-uniform; most rounds find nothing
-            if (hit) stage[staged + __popc(m & below)] = make_uint2(min(sa, sb), max(sa, sb));
-            staged += __popc(m);
-            if (staged > kPairStage - 32) flush();
-        }
-    };
     auto stage_rec = [&](const PairRec& r, int rank) {
         srec[rank] = make_uint4(r.id, r.w0, r.w1, r.w2);
         snd[rank] = make_int2(r.n0, r.n1);
@@ -543,13 +560,21 @@ __global__ void __launch_bounds__(kBlock, 7) k_bin_pairs(DevTopo t, const int* _
                         const int2 nq = snd[32 * g + lane];
                         me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
                     }
-                    rotate_pairs(me, srec, snd, 32 * g, mg, lane, emit);  // within group g
-                    // group g (full: a later group exists) against each record of the later groups
-                    for (int r = 32 * (g + 1); r < n; r++) {
-                        const uint4 q = srec[r];
-                        const int2 nq = snd[r];
-                        const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                        emit(pair_test(me, o), me.id & kIdMask, o.id & kIdMask);
+                    rotate_pairs(me, srec, snd, 32 * g, mg, lane, cand_cap, cand, ncand, flags);  // within group g
+                    // group g (full: a later group exists) against the records of the later
+                    // groups, 32 partners per window of hit bits
+                    for (int r0 = 32 * (g + 1); r0 < n; r0 += 32) {
+                        const int rn = min(32, n - r0);
+                        uint32_t bits = 0;
+#pragma unroll 4
+                        for (int k = 0; k < rn; k++) {
+                            const uint4 q = srec[r0 + k];
+                            const int2 nq = snd[r0 + k];
+                            const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                            bits |= uint32_t(pair_test(me, o)) << k;
+                        }
+                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[r0 + k].x & kIdMask; }, lane,
+                                    cand_cap, cand, ncand, flags);
                     }
                 }
             } else {
@@ -566,20 +591,19 @@ __global__ void __launch_bounds__(kBlock, 7) k_bin_pairs(DevTopo t, const int* _
                             i++;
                             row_end += n - 1 - i;
                         }
-                        const int j = int(pidx - (row_end - (n - 1 - i))) + i + 1;
+                        const int jj = int(pidx - (row_end - (n - 1 - i))) + i + 1;
                         const PairRec A = load_rec(t, items[i], rec, ccp);
-                        const PairRec B = load_rec(t, items[j], rec, ccp);
+                        const PairRec B = load_rec(t, items[jj], rec, ccp);
                         hit = pair_test(A, B);
                         sa = A.id & kIdMask;
                         sb = B.id & kIdMask;
                     }
-                    emit(hit, sa, sb);
+                    append_bits(uint32_t(hit), sa, [&](int) { return sb; }, lane, cand_cap, cand, ncand, flags);
                 }
                 __syncwarp();
             }
         }
     }
-    if (staged) flush();
     entries = __reduce_add_sync(0xffffffffu, entries);
     if (lane == 0) {
         if (entries) atomicAdd(nentries, entries);

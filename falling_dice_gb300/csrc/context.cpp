@@ -276,6 +276,15 @@ struct mcg_ctx {
     void sync() { ck(cudaStreamSynchronize(stream), "stream sync"); }
     void check_launch() { ck(cudaGetLastError(), "kernel launch"); }
 
+    // occupancy variants of the beam kernel and the gather (shape_blocks), picked by
+    // mcg_autotune; results do not depend on them
+    int beam_variant = 0, gather_variant = 0;
+    void set_kernel_variants(int beams, int gather) {
+        if (beams != beam_variant || gather != gather_variant) drop_graphs();
+        beam_variant = beams;
+        gather_variant = gather;
+    }
+
     // ---- contact buffers ---------------------------------------------------------------
     double broad_cell = 0;   // current grid cell (the reference's size unless coarsened)
     float contact_skin = 0;  // candidate-list reuse distance (m); 0 rebuilds every evaluation
@@ -463,8 +472,8 @@ struct mcg_ctx {
         if (mixed) launch_state_mixed(topo, p, dz, d_baseX, mn, ev, stream);
         else launch_state(topo, p, dz, d_baseX, d_baseR, ev, stream);
         mark(1);
-        if (mixed) launch_beams_mixed(topo, mat, mb, mn, trials, ev, stream);
-        else launch_beams(topo, mat, d_plastic, trials, ev, stream);
+        if (mixed) launch_beams_mixed(topo, mat, mb, mn, trials, ev, stream, beam_variant);
+        else launch_beams(topo, mat, d_plastic, trials, ev, stream, beam_variant);
         mark(2);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
@@ -476,8 +485,8 @@ struct mcg_ctx {
             mark(4);
         }
         mark(5);
-        if (mixed) launch_gather_mixed(topo, p, cptr, d_gout, ev, stream);
-        else launch_gather(topo, p, cptr, d_gout, ev, stream);
+        if (mixed) launch_gather_mixed(topo, p, cptr, d_gout, ev, stream, gather_variant);
+        else launch_gather(topo, p, cptr, d_gout, ev, stream, gather_variant);
         mark(6);
         launch_finalize(topo, p, cptr, d_gout, ev, stream);
         mark(7);
@@ -537,7 +546,8 @@ struct mcg_ctx {
         if (cfg.relative_gradient_tolerance > 0)
             return (rms <= cfg.relative_gradient_tolerance * rms0) && o.max_pen <= cfg.penetration_tolerance;
         const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.reaction));
-        const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < 1.5e-3;
+        const double rrt = cfg.reaction_relative_tolerance == 0 ? 1.5e-3 : cfg.reaction_relative_tolerance;
+        const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < rrt;
         return forceOK && o.max_pen <= cfg.penetration_tolerance;
     }
     // Host-only step of the iteration loop (sim.cpp:176-177): record, test convergence,
@@ -1461,6 +1471,7 @@ void mcg_config_defaults(mcg_config* c) {
     c->min_line_step = 1e-9; c->penetration_tolerance = .00012; c->max_adaptive_refinements = 7;
     c->fps = 24; c->frames = 83; c->threads = 0; c->seed = 0x494e445553545259ULL;
     c->relative_gradient_tolerance = 0; c->precision = MCG_FP64; c->self_contact = 1;
+    c->reaction_relative_tolerance = 1.5e-3;
 }
 
 const char* mcg_status_string(int s) {
@@ -1700,15 +1711,15 @@ int objective_with_fixed_contacts(mcg_ctx* c, ContactBufs& fixed, const double* 
         p.inv_cell_f = float(1.0 / c->broad_cell);
         if (c->mixed) launch_state_mixed(c->topo, p, c->d_zin, c->d_baseX, c->mn, c->ev, s);
         else launch_state(c->topo, p, c->d_zin, c->d_baseX, c->d_baseR, c->ev, s);
-        if (c->mixed) launch_beams_mixed(c->topo, c->mat, c->mb, c->mn, false, c->ev, s);
-        else launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s);
+        if (c->mixed) launch_beams_mixed(c->topo, c->mat, c->mb, c->mn, false, c->ev, s, c->beam_variant);
+        else launch_beams(c->topo, c->mat, c->d_plastic, false, c->ev, s, c->beam_variant);
         const ContactBufs* cptr = nullptr;
         if (p.self_contact) {
             launch_contacts(c->topo, p, c->ev, fixed, c->rmax + c->cfg.contact_margin, 0.f, s);  // always rebuilds
             cptr = &fixed;
         }
-        if (c->mixed) launch_gather_mixed(c->topo, p, cptr, c->d_grad, c->ev, s);
-        else launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s);
+        if (c->mixed) launch_gather_mixed(c->topo, p, cptr, c->d_grad, c->ev, s, c->gather_variant);
+        else launch_gather(c->topo, p, cptr, c->d_grad, c->ev, s, c->gather_variant);
         launch_finalize(c->topo, p, cptr, c->d_grad, c->ev, s);
         c->check_launch();
         c->contacts_stale = p.self_contact != 0;
@@ -1868,6 +1879,22 @@ int mcg_set_contact_shapes(mcg_ctx* c, double cell, int32_t pair_blocks) {
     });
 }
 
+int mcg_set_kernel_shapes(mcg_ctx* c, int32_t beam_blocks, int32_t gather_blocks) {
+    return guarded(c, [&] {
+        need_topo(c);
+        const ShapeKernel bk = c->mixed ? ShapeKernel::kBeamsMixed : ShapeKernel::kBeams;
+        auto find = [](ShapeKernel k, int32_t blocks) {
+            if (blocks == 0) return 0;
+            for (int v = 0; v < shape_variants(k); v++)
+                if (shape_blocks(k, v) == blocks) return v;
+            throw Fail(MCG_ERR_INVALID, "no kernel variant with " + std::to_string(blocks) + " CTAs per SM");
+        };
+        const int bv = find(bk, beam_blocks), gv = find(ShapeKernel::kGather, gather_blocks);
+        c->sync();
+        c->set_kernel_variants(bv, gv);
+    });
+}
+
 int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, mcg_tuning* out) {
     return guarded(c, [&] {
         need_topo(c);
@@ -1948,8 +1975,60 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         c->broad_cell = best.cell;
         c->pair_blocks_set = best.blocks;
         c->alloc_contacts(c->cb.bin_slots, c->cb.contact_cap, c->cb.bin_cap, c->cb.cand_cap);
+        // then the occupancy variants of the beam kernel and of the gather, one after the
+        // other, timed on the same evaluation with the same bitwise check (ties within 1 %
+        // keep the default)
+        const ShapeKernel beam_kernel = c->mixed ? ShapeKernel::kBeamsMixed : ShapeKernel::kBeams;
+        double best_ms = best.ms;
+        ck(cudaEventCreate(&t0), "cudaEventCreate");
+        ck(cudaEventCreate(&t1), "cudaEventCreate");
+        c->contact_skin = 0.f;
+        auto time_variant = [&](int bv, int gv) {
+            c->set_kernel_variants(bv, gv);
+            const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);
+            for (int i = 0; i < c->I; i++) e[size_t(i)] = o[i].energy;
+            d2h(g.data(), c->d_grad, n, s);
+            c->sync();
+            if (std::memcmp(e.data(), ref_e.data(), e.size() * sizeof(double)) != 0 ||
+                std::memcmp(g.data(), ref_g.data(), n * sizeof(double)) != 0)
+                throw Fail(MCG_ERR_MISMATCH, "a kernel occupancy variant changed an evaluation");
+            c->eval(c->d_zin, false, c->d_grad);  // captures the graph
+            ck(cudaEventRecord(t0, s), "cudaEventRecord");
+            for (int r = 0; r < reps; r++) c->eval(c->d_zin, false, c->d_grad);
+            ck(cudaEventRecord(t1, s), "cudaEventRecord");
+            c->read_outs();
+            float ms = 0;
+            ck(cudaEventElapsedTime(&ms, t0, t1), "cudaEventElapsedTime");
+            tried++;
+            return double(ms) / reps;
+        };
+        try {
+            int bv = 0, gv = 0;
+            best_ms = time_variant(0, 0);
+            for (int v = 1; v < shape_variants(beam_kernel); v++) {
+                const double ms = time_variant(v, gv);
+                if (ms < 0.99 * best_ms) { best_ms = ms; bv = v; }
+            }
+            for (int v = 1; v < shape_variants(ShapeKernel::kGather); v++) {
+                const double ms = time_variant(bv, v);
+                if (ms < 0.99 * best_ms) { best_ms = ms; gv = v; }
+            }
+            c->set_kernel_variants(bv, gv);
+        } catch (...) {
+            cudaEventDestroy(t0);
+            cudaEventDestroy(t1);
+            c->contact_skin = skin;
+            c->set_kernel_variants(0, 0);
+            throw;
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        c->contact_skin = skin;
         c->sync();
-        if (out) *out = mcg_tuning{best.cell, c->pair_blocks_for(S), tried, best.ms, ms_default};
+        if (out)
+            *out = mcg_tuning{best.cell, c->pair_blocks_for(S), tried, best_ms, ms_default,
+                              shape_blocks(beam_kernel, c->beam_variant),
+                              shape_blocks(ShapeKernel::kGather, c->gather_variant)};
     });
 }
 

@@ -221,10 +221,17 @@ int nb_nodes(int N);
 int nb_beams(int B);
 void launch_state(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                   const double* base_r, EvalBufs& e, cudaStream_t s);
+// Occupancy variants of the beam kernels and the gather (CTAs per SM the register allocation
+// allows; the arithmetic is the same in every variant).  Variant 0 is the default.
+enum class ShapeKernel { kBeams, kBeamsMixed, kGather };
+int shape_variants(ShapeKernel k);
+int shape_blocks(ShapeKernel k, int variant);
+int beams_mixed_variants();
+int beams_mixed_blocks(int variant);
 void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials,
-                  EvalBufs& e, cudaStream_t s);
+                  EvalBufs& e, cudaStream_t s, int variant = 0);
 void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
-                   EvalBufs& e, cudaStream_t s);
+                   EvalBufs& e, cudaStream_t s, int variant = 0);
 void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
                      EvalBufs& e, cudaStream_t s);
 // base state <- current state, plastic <- trial (plastic == nullptr skips it) for the
@@ -233,13 +240,13 @@ void launch_commit(const DevTopo& t, const uint8_t* mask, const EvalBufs& e, dou
                    double* plastic, cudaStream_t s);
 void launch_center(const DevTopo& t, EvalBufs& e, cudaStream_t s);
 void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
-                         cudaStream_t s);
+                         cudaStream_t s, int variant = 0);
 
 // ---- mixed-precision form (objective_mixed.cu) ------------------------------------------
 void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                         const MixedNodes& mn, EvalBufs& e, cudaStream_t s);
 void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
-                        EvalBufs& e, cudaStream_t s);
+                        EvalBufs& e, cudaStream_t s, int variant = 0);
 void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
                          MixedNodes& mn, cudaStream_t s);
 // The streamed section constants (mb.C0/C1, when allocated), once per upload.

@@ -189,8 +189,11 @@ __device__ __forceinline__ d3 unit_fast(d3 v) {
 }
 
 // ---- beam kernel: MC/src/sim.cpp:139-141 ---------------------------------------------------
-__global__ void __launch_bounds__(kBlock) k_beams(DevTopo t, Material m, const double* __restrict__ plastic,
-                                                  int trials, EvalBufs e) {
+// kMinBlocks: CTAs per SM the register allocation must allow (an occupancy variant picked by
+// mcg_autotune; the arithmetic, and so the result, is the same in every variant).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams(DevTopo t, Material m, const double* __restrict__ plastic,
+                                                              int trials, EvalBufs e) {
     __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
@@ -370,9 +373,9 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
     }
 }
 
-template <bool F32>
-__global__ void __launch_bounds__(kBlock) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
-                                                   EvalBufs e, double* __restrict__ grad) {
+template <bool F32, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_gather(DevTopo t, PhysParams p, ContactBufs c, int use_contacts,
+                                                               EvalBufs e, double* __restrict__ grad) {
     __shared__ double sm[6 * kBlock];
     __shared__ double cforce[2];
     const MapPos mp = map_pos(t.nblk);
@@ -659,27 +662,59 @@ void launch_plastic_stats(const DevTopo& t, const double* plastic, double* part,
     note_launches(2);
 }
 
+// Occupancy variants (CTAs per SM) of the FP64 beam kernel and of the gather.
+constexpr int kBeamBlocks[] = {1, 2, 3};
+constexpr int kGatherBlocks[] = {1, 2, 4};
+
+int shape_variants(ShapeKernel k) {
+    switch (k) {
+        case ShapeKernel::kBeams: return 3;
+        case ShapeKernel::kGather: return 3;
+        default: return beams_mixed_variants();
+    }
+}
+int shape_blocks(ShapeKernel k, int v) {
+    switch (k) {
+        case ShapeKernel::kBeams: return kBeamBlocks[v];
+        case ShapeKernel::kGather: return kGatherBlocks[v];
+        default: return beams_mixed_blocks(v);
+    }
+}
+
 void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials, EvalBufs& e,
-                  cudaStream_t s) {
+                  cudaStream_t s, int variant) {
     if (t.B == 0) return;
-    k_beams<<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, trials ? 1 : 0, e);
+    const int tr = trials ? 1 : 0;
+    switch (variant) {
+        case 1: k_beams<kBeamBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, tr, e); break;
+        case 2: k_beams<kBeamBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, tr, e); break;
+        default: k_beams<kBeamBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, tr, e); break;
+    }
+    note_launches(1);
+}
+
+template <bool F32>
+void gather_variant(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
+                    cudaStream_t s, int variant) {
+    ContactBufs cc{};
+    if (c) cc = *c;
+    const int uc = c ? 1 : 0;
+    switch (variant) {
+        case 1: k_gather<F32, kGatherBlocks[1]><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, uc, e, grad); break;
+        case 2: k_gather<F32, kGatherBlocks[2]><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, uc, e, grad); break;
+        default: k_gather<F32, kGatherBlocks[0]><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, uc, e, grad); break;
+    }
     note_launches(1);
 }
 
 void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
-                   cudaStream_t s) {
-    ContactBufs cc{};
-    if (c) cc = *c;
-    k_gather<false><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
-    note_launches(1);
+                   cudaStream_t s, int variant) {
+    gather_variant<false>(t, p, c, grad, e, s, variant);
 }
 
 void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
-                         cudaStream_t s) {
-    ContactBufs cc{};
-    if (c) cc = *c;
-    k_gather<true><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, c ? 1 : 0, e, grad);
-    note_launches(1);
+                         cudaStream_t s, int variant) {
+    gather_variant<true>(t, p, c, grad, e, s, variant);
 }
 
 void launch_finalize(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,

@@ -295,8 +295,9 @@ __device__ __forceinline__ void section_constants(const MixedBeams& m, int b, fl
 }
 
 // ---- beam kernel (MC/src/sim.cpp:139-141, FP32 with the split above) ---------------------
-template <bool kStreamed>
-__global__ void __launch_bounds__(kBlock, 4) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
+// kMinBlocks: the occupancy variant (CTAs per SM), picked by mcg_autotune.
+template <bool kStreamed, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
     __shared__ float sm[2 * 3 * (kBlock / 32)];
@@ -478,11 +479,26 @@ void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, 
     launch_center(t, e, s);
 }
 
+// Occupancy variants (CTAs per SM) of the mixed beam kernel; the streamed-constants form
+// (sections that are not circular) has the default one only.
+constexpr int kMixedBlocks[] = {3, 4, 5, 6};
+int beams_mixed_variants() { return 4; }
+int beams_mixed_blocks(int v) { return kMixedBlocks[v]; }
+
 void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
-                        EvalBufs& e, cudaStream_t s) {
+                        EvalBufs& e, cudaStream_t s, int variant) {
     if (t.B == 0) return;
-    if (mb.C0) k_beams_mixed<true><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
-    else k_beams_mixed<false><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, trials ? 1 : 0, mn.U, mn.E, mn.R0f, e);
+    const int tr = trials ? 1 : 0;
+    if (mb.C0) {
+        k_beams_mixed<true, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e);
+    } else {
+        switch (variant) {
+            case 1: k_beams_mixed<false, kMixedBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            case 2: k_beams_mixed<false, kMixedBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            case 3: k_beams_mixed<false, kMixedBlocks[3]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            default: k_beams_mixed<false, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+        }
+    }
     note_launches(1);
 }
 

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define MCG_ABI_VERSION 1
+#define MCG_ABI_VERSION 2
 
 enum mcg_status {
     MCG_OK = 0,
@@ -83,6 +83,10 @@ typedef struct mcg_config {
                                            <= this, in place of the absolute test */
     int32_t precision;                  /* enum mcg_precision */
     int32_t self_contact;               /* 1 = on (reference behaviour), 0 = off */
+    double reaction_relative_tolerance; /* the alternative convergence test
+                                           rms/(translation_scale max(1, reaction)) < this
+                                           (sim.cpp:177); 0: the reference's 1.5e-3;
+                                           < 0: off (only the absolute rms/max test) */
 } mcg_config;
 
 void mcg_config_defaults(mcg_config* cfg);
@@ -303,24 +307,32 @@ int mcg_set_contact_cell(mcg_ctx* ctx, double cell);
  * default from the lattice size), e.g. to re-apply a tuning without timing again. */
 int mcg_set_contact_shapes(mcg_ctx* ctx, double cell, int32_t pair_blocks);
 
-/* Shapes of the self-contact broad phase picked by measurement (no reference
- * counterpart).  Candidates: grid cells 0.9, 1, 1.1, 1.25 and 1.4 times the reference's
- * max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 .. 1216 blocks
- * (at most one warp per 32 shapes) besides the default.  Each candidate evaluates every
- * lattice `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL:
- * z = 0) and platen heights `tops` (NULL: each lattice's top0), with the candidate list
- * rebuilt at every evaluation; the fastest by CUDA-event time is kept for the context (among
- * candidates within 1 % of it, the one with the most pair blocks, then the smallest cell).
- * The candidates must agree bit for bit on energies and gradients (pair sets and sums do
- * not depend on the grid); MCG_ERR_MISMATCH if one does not. */
+/* Shapes of the evaluation's kernels picked by measurement (no reference counterpart).
+ * First the self-contact broad phase: grid cells 0.9, 1, 1.1, 1.25 and 1.4 times the
+ * reference's max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 ..
+ * 1216 blocks (at most one warp per 32 shapes) besides the default; then the occupancy of the
+ * beam kernel (FP64: 1, 2 or 3 CTAs of 256 threads per SM; mixed: 3, 4, 5 or 6) and of the
+ * gradient gather (1, 2 or 4), one after the other.  Each candidate evaluates every lattice
+ * `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL: z = 0) and
+ * platen heights `tops` (NULL: each lattice's top0), with the candidate list rebuilt at
+ * every evaluation; the fastest by CUDA-event time is kept for the context (broad phase:
+ * among candidates within 1 % of it, the one with the most pair blocks, then the smallest
+ * cell; kernel occupancy: a variant must be 1 % faster than the one before to replace it).
+ * All candidates must agree bit for bit on energies and gradients (pair sets and sums do
+ * not depend on the grid, nor arithmetic on register allocation); MCG_ERR_MISMATCH if one
+ * does not. */
 typedef struct mcg_tuning {
-    double cell;          /* chosen grid cell (m) */
-    int32_t pair_blocks;  /* chosen blocks of the pair enumeration (8 warps each) */
-    int32_t tried;        /* candidates timed */
-    double ms_chosen;     /* ms per evaluation with the chosen shapes */
-    double ms_default;    /* ms per evaluation with the default shapes */
+    double cell;             /* chosen grid cell (m) */
+    int32_t pair_blocks;     /* chosen blocks of the pair enumeration (8 warps each) */
+    int32_t tried;           /* candidates timed */
+    double ms_chosen;        /* ms per evaluation with the chosen shapes */
+    double ms_default;       /* ms per evaluation with the default shapes */
+    int32_t beam_blocks;     /* chosen CTAs per SM of the beam kernel */
+    int32_t gather_blocks;   /* chosen CTAs per SM of the gather */
 } mcg_tuning;
 int mcg_autotune(mcg_ctx* ctx, const double* z, const double* tops, int32_t reps, mcg_tuning* out);
+/* Re-applies kernel occupancy shapes as mcg_autotune reports them (0: the default). */
+int mcg_set_kernel_shapes(mcg_ctx* ctx, int32_t beam_blocks, int32_t gather_blocks);
 
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
  * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept

@@ -793,7 +793,9 @@ struct orc_model {
             if (cfg.relative_gradient_tolerance > 0)
                 return rms <= cfg.relative_gradient_tolerance * rms0 && o.d.maxPen <= cfg.penetration_tolerance;
             const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.d.reaction));
-            const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < 1.5e-3;
+            // extension: reaction_relative_tolerance (0: the reference's 1.5e-3; < 0: off)
+            const double rrt = cfg.reaction_relative_tolerance == 0 ? 1.5e-3 : cfg.reaction_relative_tolerance;
+            const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < rrt;
             return forceOK && o.d.maxPen <= cfg.penetration_tolerance;
         };
         auto lineSearch = [&](const std::vector<double>& p, double dg, std::vector<double>& zc, Eval& cand) {

@@ -112,3 +112,29 @@ def test_fixed_shapes_leave_evaluations_unchanged(mcg):
         assert np.array_equal(got["grad"], ref["grad"]), (cell, blocks)
     with pytest.raises(mcg.MCGError):
         b.set_contact_shapes(-1.0, 0)
+
+
+@pytest.mark.parametrize("precision,beam_blocks", [(0, (1, 2, 3)), (1, (3, 4, 5, 6))])
+def test_kernel_occupancy_variants_leave_evaluations_unchanged(mcg, precision, beam_blocks):
+    """The beam kernel's and the gather's occupancy variants (CTAs per SM, which set their
+    register budgets; mcg_set_kernel_shapes / mcg_autotune) do the same arithmetic: every
+    variant gives the default's evaluation bit for bit, in both precision forms."""
+    cfg, lats, ys = make(mcg)
+    cfg.precision = precision
+    states = [mcg.random_state(lat, 0.04, 0.08, 0.02, 4000 + k) for k, lat in enumerate(lats)]
+    z = np.concatenate([zz for zz, _ in states])
+    tops = [lat.geometry.top0 - 0.003 for lat in lats]
+    ref = mcg.BatchSolver(cfg, lats, yields=ys).objective(z, tops)
+    b = mcg.BatchSolver(cfg, lats, yields=ys)
+    for bb in beam_blocks:
+        for gb in (1, 2, 4):
+            b.set_kernel_shapes(bb, gb)
+            got = b.objective(z, tops)
+            assert np.array_equal(got["energy"], ref["energy"]), (bb, gb)
+            assert np.array_equal(got["grad"], ref["grad"]), (bb, gb)
+    with pytest.raises(mcg.MCGError):
+        b.set_kernel_shapes(7, 1)
+    t = b.autotune(z, tops, reps=2)
+    assert t["beam_blocks"] in beam_blocks and t["gather_blocks"] in (1, 2, 4)
+    got = b.objective(z, tops)
+    assert np.array_equal(got["grad"], ref["grad"])
