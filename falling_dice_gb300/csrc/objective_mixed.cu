@@ -3,7 +3,7 @@
 // FP32 does the bulk arithmetic: every per-beam term of the reference's objective
 // (MC/src/sim.cpp:139-141).  FP64 stays where stability needs it: the base configuration,
 // the per-increment base terms below, node positions for contact and platen tests,
-// energy totals (compensated FP32 warp sums, FP64 across warps), node gradient totals
+// energy totals (compensated FP32 block sums, FP64 across blocks), node gradient totals
 // (compensated FP32 sums), and everything the L-BFGS solver does.
 //
 // Naively FP32 would lose the quantities the energy depends on by cancellation:
@@ -67,37 +67,21 @@ __device__ __forceinline__ void warp_sum_comp(float& hi, float& lo) {
     }
 }
 
-// Sums NV per-thread FP32 values over the block into thread 0: compensated FP32 sums in each
-// warp and across the warps (in warp order), rounded to FP64 once per block -- GB300's FP64
-// pipe is narrow, so no FP64 instruction runs per warp.  smem holds 2 NV (blockDim.x / 32)
-// floats.
-template <int NV>
-__device__ __forceinline__ void block_sum_f(const float (&v)[NV], double (&out)[NV], float* smem) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+// Sums kBlock per-thread FP32 values (v[t] in smem, written by thread t before the
+// caller's barrier) with one warp: lane l adds v[l], v[l + 32], ... in order with
+// compensation, then the lanes' compensated pairs are summed by a fixed shuffle tree.  The
+// result, one FP64 rounding of the compensated pair, is in lane 0.  The order is fixed, so
+// the sum is reproducible; only one warp spends instructions on it.
+__device__ __forceinline__ double warp_sum_smem(const float* v, int lane) {
+    float hi = v[lane], lo = 0.f;
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-        float hi = v[k], lo = 0.f;
-        warp_sum_comp(hi, lo);
-        if (lane == 0) {
-            smem[2 * (k * nw + warp)] = hi;
-            smem[2 * (k * nw + warp) + 1] = lo;
-        }
+    for (int k = 1; k < kBlock / 32; k++) {
+        const float a = v[lane + 32 * k], s = hi + a, bp = s - hi;
+        lo += (hi - (s - bp)) + (a - bp);
+        hi = s;
     }
-    __syncthreads();
-    if (threadIdx.x == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            float hi = smem[2 * k * nw], lo = smem[2 * k * nw + 1];
-            for (int w = 1; w < nw; w++) {
-                const float h2 = smem[2 * (k * nw + w)], l2 = smem[2 * (k * nw + w) + 1];
-                const float s = hi + h2;
-                const float bp = s - hi;
-                lo += l2 + ((hi - (s - bp)) + (h2 - bp));
-                hi = s;
-            }
-            out[k] = double(hi) + double(lo);
-        }
-    __syncthreads();
+    warp_sum_comp(hi, lo);
+    return double(hi) + double(lo);
 }
 
 struct R1 { float force, p, a, dg, energy, hard; bool yielded; };
@@ -106,7 +90,7 @@ __device__ __forceinline__ R1 ret1(float total, float pc, float ac, float k, flo
     const float trial = k * (total - pc);
     const float f = fabsf(trial) - (y + H * ac);
     if (f > 0.f) {
-        r.dg = f / fmaxf(1e-20f, k + H);
+        r.dg = __fdividef(f, fmaxf(1e-20f, k + H));
         r.p = pc + (trial >= 0.f ? r.dg : -r.dg);
         r.a = ac + r.dg;
         r.yielded = true;
@@ -127,8 +111,8 @@ __device__ __forceinline__ R3 ret3(f3 t, f3 pc, float ac, float k, float y, floa
     const float n = sqrtf(fdot(trial, trial));
     const float f = n - (y + H * ac);
     if (f > 0.f && n > 1e-20f) {
-        r.dg = f / fmaxf(1e-20f, k + H);
-        r.p = pc + trial * (r.dg / n);
+        r.dg = __fdividef(f, fmaxf(1e-20f, k + H));
+        r.p = pc + trial * __fdividef(r.dg, n);
         r.a = ac + r.dg;
         r.yielded = true;
     } else {
@@ -157,6 +141,27 @@ __device__ __forceinline__ f3 jl_inv_t_f(f3 p, f3 v) {
         A = 1.f / a2 - (1.f + c) / (2.f * a * s);
     }
     return (v + c1 * .5f) + c2 * A;
+}
+
+// Rotation vector of the unit quaternion (qw, qv), qw >= 0: qv 2 atan2(|qv|, qw) / |qv|
+// (MC/include/core.hpp:52).  Up to |qv| = qw / 4 (angles up to 28 degrees: nearly every
+// beam) the factor is (2 / qw) atan(x) / x, x^2 = |qv|^2 / qw^2, from the Gregory series
+// atan(x) / x = 1 - x^2/3 + x^4/5 - ...; stopping after x^10/11 leaves less than
+// x^12/13 < 5e-9.  Larger angles use atan2f.
+__device__ __forceinline__ f3 rotvec_f(float qw, f3 qv) {
+    const float s2 = fdot(qv, qv);
+    if (s2 <= 0.0625f * qw * qw) {
+        const float rq = __fdividef(1.f, qw);
+        const float u = s2 * rq * rq;
+        float P = fmaf(u, -1.f / 11.f, 1.f / 9.f);
+        P = fmaf(u, P, -1.f / 7.f);
+        P = fmaf(u, P, 1.f / 5.f);
+        P = fmaf(u, P, -1.f / 3.f);
+        P = fmaf(u, P, 1.f);
+        return qv * (2.f * rq * P);
+    }
+    const float s = sqrtf(s2);
+    return qv * __fdividef(2.f * atan2f(s, qw), s);
 }
 
 // ---- node state --------------------------------------------------------------------------
@@ -300,16 +305,23 @@ template <bool kStreamed, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
                                                         const float4* __restrict__ U, const float4* __restrict__ Ei,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
-    __shared__ float sm[2 * 3 * (kBlock / 32)];
+    __shared__ float sm[2 * kBlock];  // per-thread elastic and plastic energies
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
     const int b = mp.i;
     const int B = t.B;
-    float acc[3] = {0.f, 0.f, 0.f};
+    float ue = 0.f, up = 0.f;  // elastic energy, plastic dissipation of this beam
     if (mp.valid) {
+        // Every load is issued here, before any arithmetic: the streamed beam records and,
+        // one step behind the end indices, the node increments, so that each thread keeps
+        // all of its memory requests in flight at once (the kernel is latency-bound).
         const int2 ab = t.ab[b];
         const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B5 = m.B5[b];
+        const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), (rotp, r)
         const float4 ua4 = U[ab.x], ub4 = U[ab.y];
+        const float4 ea = Ei[ab.x], eb = Ei[ab.y];
+        const float4 ra0 = R0f[ab.x];
+        const float4 ic = m.ic[mp.inst];
         const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
         const float c0 = B0.w, L0 = B1.w, Lb = B2.w;
         const float q = c0 + 2.f * fdot(d0, du) + fdot(du, du);  // |d|^2 - L0^2
@@ -318,7 +330,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
         float* sa = e.slotAf + 6 * size_t(b);
         float* sb = e.slotBf + 6 * size_t(b);
         if (L < 1e-10f) {
-            acc[0] = 1e8f * (1e-10f - L) * (1e-10f - L);
+            ue = 1e8f * (1e-10f - L) * (1e-10f - L);
 #pragma unroll
             for (int k = 0; k < 6; k++) { sa[k] = 0.f; sb[k] = 0.f; }
             if (trials) {
@@ -328,11 +340,12 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
                 for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
             }
         } else {
-            const float invL = 1.f / L;
+            // Divisions are the approximate single-instruction form (__fdividef, relative
+            // error ~2 ulp): every divisor is a length or a small positive sum, well inside
+            // its range, and the form's error budget is set by FP32 itself.
+            const float invL = __fdividef(1.f, L);
             const f3 tt = d * invL;
-            const float eps = q / ((L + L0) * L0);
-            const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), (rotp, r)
-            const float4 ic = m.ic[mp.inst];
+            const float eps = __fdividef(q, (L + L0) * L0);
             float4 C0, C1;  // (kb, kt, my, ty), (cs, aL, area, aLsy)
             section_constants<kStreamed>(m, b, P1.w, L0, ic, C0, C1);
             const float E = mat.Ef, H = mat.Hf, sy = ic.x;
@@ -342,19 +355,19 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
             const float dax = C1.w * ax.dg;
             f3 F = tt * (C1.z * ax.force);
             // shear from the split director/chord differences
-            const float4 ea = Ei[ab.x], eb = Ei[ab.y];
             const f3 va = xyz(make_float4(ea.y, ea.z, ea.w, 0.f)), vb = xyz(make_float4(eb.y, eb.z, eb.w, 0.f));
             const float wa = 1.f + ea.x, wb = 1.f + eb.x;
             // base directors d_a0 = t0 + s_a0, d_b0 = t0 + s_b0: they only enter multiplied by
             // a small vector (the rotation increment, the shear vector), so the ~1e-7 of the
             // FP32 t0 is harmless; the small s_a0, s_b0 themselves come exact from FP64
             const f3 sa0 = xyz(B1), sb0 = xyz(B2);
-            const f3 t0 = d0 * (1.f / Lb);
+            const float invLb = __fdividef(1.f, Lb);
+            const f3 t0 = d0 * invLb;
             const f3 da0 = t0 + sa0, db0 = t0 + sb0;
             const f3 dda = rot_inc(wa, va, da0), ddb = rot_inc(wb, vb, db0);
             const f3 da = da0 + dda, db = db0 + ddb;
-            const float dLb = (2.f * fdot(d0, du) + fdot(du, du)) / (L + Lb);
-            const f3 tdiff = (du * Lb - d0 * dLb) * (1.f / (L * Lb));  // t - t0
+            const float dLb = __fdividef(2.f * fdot(d0, du) + fdot(du, du), L + Lb);
+            const f3 tdiff = (du * Lb - d0 * dLb) * (invL * invLb);  // t - t0
             const f3 ma = dda + sa0 - tdiff, mb = ddb + sb0 - tdiff;
             const float cs = C1.x;
             const float us = .5f * cs * (fdot(ma, ma) + fdot(mb, mb));
@@ -368,7 +381,6 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
             // relative rotation (Ra0^* delta Ra0) Q0, delta = e_a^* e_b, near-identity forms
             const float dw1 = ea.x + eb.x + ea.x * eb.x + fdot(va, vb);
             const f3 dv0 = (vb - va) + vb * ea.x - va * eb.x - fcross(va, vb);
-            const float4 ra0 = R0f[ab.x];
             const f3 ra0v{ra0.y, ra0.z, ra0.w};
             const f3 dv = rot_conj(ra0.x, ra0v, dv0);
             const float a0 = B5.x;
@@ -377,8 +389,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
             f3 qv = dv + v0 + v0 * dw1 + dv * a0 + fcross(dv, v0);
             float qw = 1.f + qw1;
             if (qw < 0.f) { qw = -qw; qv = -qv; }
-            const float s = sqrtf(fdot(qv, qv));
-            const f3 phi = s < 1e-30f ? qv * (2.f / qw) : qv * (2.f * atan2f(s, qw) / s);
+            const f3 phi = rotvec_f(qw, qv);
             // axis = unit(Ra^T t), Ra = e_a Ra0
             f3 ax_ = rot_conj(ra0.x, ra0v, rot_conj(wa, va, tt));
             const float al2 = fdot(ax_, ax_);
@@ -395,9 +406,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
             const f3 world = rot(wa, va, rot(ra0.x, ra0v, jl_inv_t_f(phi, moment)));
             Ga = Ga - world;
             Gb = Gb + world;
-            acc[0] = (uax + dax) + us + (ur + dr);
-            acc[1] = uax + us + ur;
-            acc[2] = dax + dr;
+            ue = uax + us + ur;
+            up = dax + dr;
             sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
             sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
             if (trials) {
@@ -415,20 +425,28 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
                 e.trial_auxf[2 * S + b] = moment.x;
                 e.trial_auxf[3 * S + b] = moment.y;
                 e.trial_auxf[4 * S + b] = moment.z;
-                e.trial_auxf[5 * S + b] = uax + us + ur;
-                e.trial_auxf[6 * S + b] = dax + dr;
+                e.trial_auxf[5 * S + b] = ue;
+                e.trial_auxf[6 * S + b] = up;
                 e.trial_flags[b] = ax.yielded;
                 e.trial_flags[S + b] = br.yielded;
                 e.trial_flags[2 * S + b] = tor.yielded;
             }
         }
     }
-    double tot[3];
-    block_sum_f<3>(acc, tot, sm);
-    if (threadIdx.x == 0) {
-        e.part_beam[3 * blockIdx.x] = tot[0];
-        e.part_beam[3 * blockIdx.x + 1] = tot[1];
-        e.part_beam[3 * blockIdx.x + 2] = tot[2];
+    // Block totals: warp 0 sums the elastic and the plastic energies of the block
+    // (compensated, fixed order) while the other warps only store theirs; the beam energy
+    // total is the FP64 sum of the two.
+    sm[threadIdx.x] = ue;
+    sm[kBlock + threadIdx.x] = up;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const double se = warp_sum_smem(sm, threadIdx.x);
+        const double sp = warp_sum_smem(sm + kBlock, threadIdx.x);
+        if (threadIdx.x == 0) {
+            e.part_beam[3 * blockIdx.x] = se + sp;
+            e.part_beam[3 * blockIdx.x + 1] = se;
+            e.part_beam[3 * blockIdx.x + 2] = sp;
+        }
     }
 }
 
