@@ -53,6 +53,7 @@ SIGNATURES = {
     "mcg_autotune": (C.c_int, [_P, _d, _d, C.c_int32, C.POINTER(abi.Tuning)]),
     "mcg_set_contact_shapes": (C.c_int, [_P, C.c_double, C.c_int32]),
     "mcg_set_kernel_shapes": (C.c_int, [_P, C.c_int32, C.c_int32]),
+    "mcg_contact_builds": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -284,6 +285,12 @@ class Solver:
         out = (C.c_int64 * 5)()
         self._check(self.lib.mcg_contact_stats(self.h, out), "mcg_contact_stats")
         return dict(zip(("entries", "occupied_bins", "candidates", "filtered", "contacts"), list(out)))
+
+    def contact_builds(self):
+        """Candidate-list builds since the upload (mcg_contact_builds)."""
+        n = C.c_int64()
+        self._check(self.lib.mcg_contact_builds(self.h, C.byref(n)), "mcg_contact_builds")
+        return n.value
 
     def set_contact_cell(self, cell):
         """Contact-grid cell size in metres (0: the reference's)."""

@@ -239,13 +239,18 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const f
     if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flags + 1, 1u);
 }
 
-// After a rebuild: the build positions and the end of a forced rebuild.
+// After a rebuild: the build positions and the end of a forced rebuild.  A build that
+// overflowed a buffer (bins, bin slots, cell span, candidates) left an incomplete list:
+// the next evaluation must build again, whatever the skin says, so that the overflow is
+// raised again there (the overflow bits are per evaluation; a caller that enqueues several
+// evaluations before reading sees only the last one's).
 __global__ void __launch_bounds__(kBlock) k_skin_commit(int N, const float4* __restrict__ xf_lo,
                                                         float4* __restrict__ xref, uint32_t* __restrict__ flags) {
     if (!flags[1]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < N) xref[i] = xf_lo[i];
-    if (i == 0) flags[2] = 0;
+    if (i == 0)
+        flags[2] = (flags[0] & uint32_t(kOverEntries | kOverBins | kOverSpan | kOverCandidates)) ? 1u : 0u;
 }
 
 __global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __restrict__ a,
@@ -260,6 +265,7 @@ __global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __
 __global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
                               uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
     if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
+    flags[4]++;  // builds since the buffers were allocated
     *ncand = 0;  // the candidate list and entry counts of this build
     nentries[0] = 0;
     nentries[1] = 0;
@@ -500,7 +506,8 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
 //             (rotate_pairs), then each full group against every record of the later groups
 //             (one record read by all lanes per round), hits kept as bits over windows of 32
 //             partners;
-//   larger    pairs by index, records read from global memory.
+//   larger    the same by groups of 32: each group is staged in turn and then meets every
+//             later group, staged 32 records at a time.
 __global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
                                                       const uint32_t* __restrict__ bin_count, int bin_slots,
                                                       uint32_t* __restrict__ nentries,
@@ -578,27 +585,40 @@ __global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* _
                     }
                 }
             } else {
-                // large bin: pairs by index, records from global memory
-                const long long P = (long long)n * (n - 1) / 2;
-                int i = 0;
-                long long row_end = n - 1;  // pairs of rows 0..i end here
-                for (long long base = 0; base < P; base += 32) {
-                    const long long pidx = base + lane;
-                    bool hit = false;
-                    uint32_t sa = 0, sb = 0;
-                    if (pidx < P) {
-                        while (pidx >= row_end) {  // rows advance monotonically with base
-                            i++;
-                            row_end += n - 1 - i;
-                        }
-                        const int jj = int(pidx - (row_end - (n - 1 - i))) + i + 1;
-                        const PairRec A = load_rec(t, items[i], rec, ccp);
-                        const PairRec B = load_rec(t, items[jj], rec, ccp);
-                        hit = pair_test(A, B);
-                        sa = A.id & kIdMask;
-                        sb = B.id & kIdMask;
+                // large bin: its groups of 32 entries in turn.  Group g is staged in shared
+                // ranks 0..31 (lane i holding entry 32 g + i) and its pairs found by
+                // rotation; each later group is then staged in ranks 32..63 and met 32
+                // partners per window of hit bits.  A group with a later group is full, so
+                // every lane holds an entry there.
+                const int G = (n + 31) >> 5;
+                for (int g = 0; g < G; g++) {
+                    const int mg = min(32, n - 32 * g);
+                    __syncwarp();  // the previous group's partner reads are done
+                    if (lane < mg) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), lane);
+                    __syncwarp();
+                    PairRec me{};
+                    if (lane < mg) {
+                        const uint4 q = srec[lane];
+                        const int2 nq = snd[lane];
+                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
                     }
-                    append_bits(uint32_t(hit), sa, [&](int) { return sb; }, lane, cand_cap, cand, ncand, flags);
+                    rotate_pairs(me, srec, snd, 0, mg, lane, cand_cap, cand, ncand, flags);
+                    for (int h = g + 1; h < G; h++) {
+                        const int rn = min(32, n - 32 * h);
+                        __syncwarp();
+                        if (lane < rn) stage_rec(load_rec(t, items[32 * h + lane], rec, ccp), 32 + lane);
+                        __syncwarp();
+                        uint32_t bits = 0;
+#pragma unroll 4
+                        for (int k = 0; k < rn; k++) {
+                            const uint4 q = srec[32 + k];
+                            const int2 nq = snd[32 + k];
+                            const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                            bits |= uint32_t(pair_test(me, o)) << k;
+                        }
+                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[32 + k].x & kIdMask; }, lane,
+                                    cand_cap, cand, ncand, flags);
+                    }
                 }
                 __syncwarp();
             }
@@ -647,11 +667,13 @@ __device__ __forceinline__ DistBounds dist_bounds(const DevTopo& t, const PhysPa
     const float wx = a0.x - b0.x, wy = a0.y - b0.y, wz = a0.z - b0.z;
     const float ux = a1.x - a0.x, uy = a1.y - a0.y, uz = a1.z - a0.z;
     const float vx = b1.x - b0.x, vy = b1.y - b0.y, vz = b1.z - b0.z;
-    const float a = ux * ux + uy * uy + uz * uz, e = vx * vx + vy * vy + vz * vz;
-    const float f = vx * wx + vy * wy + vz * wz, c = ux * wx + uy * wy + uz * wz;
+    // dot products by explicit FMAs (this unit is compiled without contraction, which only
+    // the FP64 closest-point arithmetic needs; one rounding per FMA only tightens the bound)
+    const float a = fmaf(ux, ux, fmaf(uy, uy, uz * uz)), e = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+    const float f = fmaf(vx, wx, fmaf(vy, wy, vz * wz)), c = fmaf(ux, wx, fmaf(uy, wy, uz * wz));
     float s = 0.f, tt = 0.f;
     if (a > 1e-20f && e > 1e-20f) {
-        const float b = ux * vx + uy * vy + uz * vz, den = a * e - b * b;
+        const float b = fmaf(ux, vx, fmaf(uy, vy, uz * vz)), den = fmaf(a, e, -b * b);
         s = den > 1e-12f * a * e ? __saturatef(__fdividef(b * f - c * e, den)) : 0.f;
         tt = __fdividef(b * s + f, e);
         if (tt < 0.f) {
@@ -666,8 +688,9 @@ __device__ __forceinline__ DistBounds dist_bounds(const DevTopo& t, const PhysPa
     } else if (e > 1e-20f) {
         tt = __saturatef(__fdividef(f, e));
     }
-    const float nx = wx + ux * s - vx * tt, ny = wy + uy * s - vy * tt, nz = wz + uz * s - vz * tt;
-    const float nn = nx * nx + ny * ny + nz * nz;
+    const float nx = fmaf(-vx, tt, fmaf(ux, s, wx)), ny = fmaf(-vy, tt, fmaf(uy, s, wy)),
+                nz = fmaf(-vz, tt, fmaf(uz, s, wz));
+    const float nn = fmaf(nx, nx, fmaf(ny, ny, nz * nz));
     const float err = 3e-5f * X + 1e-9f;
     DistBounds r;
     r.pad_sum = (pa + pb) * 1.000001f;
@@ -679,8 +702,8 @@ __device__ __forceinline__ DistBounds dist_bounds(const DevTopo& t, const PhysPa
     if (r.far_ok) {
         const float inv = rsqrtf(nn);
         const float mx = nx * inv, my = ny * inv, mz = nz * inv;
-        const float nu = mx * ux + my * uy + mz * uz, nv = mx * vx + my * vy + mz * vz;
-        const float L = (mx * wx + my * wy + mz * wz) + fminf(0.f, nu) - fmaxf(0.f, nv);
+        const float nu = fmaf(mx, ux, fmaf(my, uy, mz * uz)), nv = fmaf(mx, vx, fmaf(my, vy, mz * vz));
+        const float L = fmaf(mx, wx, fmaf(my, wy, mz * wz)) + fminf(0.f, nu) - fmaxf(0.f, nv);
         r.far = L * 0.999999f - err;
     }
     return r;
@@ -943,7 +966,8 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, nkept, 31, 5);
     (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
      note_launches(1));
-    (k_contacts<<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, c.cand2, c.hoff + chunks, c), note_launches(1));
+    // one warp per block: the few thousand contacts spread over every SM's FP64 pipe
+    (k_contacts<<<8 * kStreamBlocks, 32, 0, s>>>(t, p, e.x, c.cand2, c.hoff + chunks, c), note_launches(1));
     const uint32_t* total = c.hoff + chunks;
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);

@@ -294,8 +294,14 @@ struct mcg_ctx {
         return pair_blocks_set > 0 ? pair_blocks_set : contact_pair_blocks(shapes);
     }
     // bin_slots: entries a grid bin holds (rounded up to a power of two, at least 8)
+    long long builds_before = 0;  // candidate-list builds counted by buffers since released
     void alloc_contacts(long long bin_slots, long long contact_cap, long long bin_cap, long long cand_cap) {
         drop_graphs();
+        if (cb.flags) {
+            d2h(hp.u32, cb.flags + 4, 1, stream);
+            sync();
+            builds_before += hp.u32[0];
+        }
         contact_mem.release();
         const long long S = (long long)N + B;
         ContactBufs c{};
@@ -303,7 +309,7 @@ struct mcg_ctx {
         c.cell_hi = contact_mem.get<int4>(size_t(S));
         c.rec = contact_mem.get<uint4>(size_t(S));
         c.grid = contact_mem.get<int>(16);
-        c.flags = contact_mem.get<uint32_t>(4);
+        c.flags = contact_mem.get<uint32_t>(5);
         c.xref = contact_mem.get<float4>(size_t(std::max(N, 1)));
         int slots = 8;
         while (slots < bin_slots && slots < (1 << 20)) slots <<= 1;
@@ -339,7 +345,7 @@ struct mcg_ctx {
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
         c.scan_tmp_bytes = scan_tmp_bytes(std::max({(long long)N + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
-        ck(cudaMemsetAsync(c.flags, 0, 4 * sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.flags, 0, 5 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.ncand, 0, sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.nentries, 0, 3 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
@@ -1854,6 +1860,20 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
         for (int k = 0; k < 5; k++) out5[k] = c->hp.u32[k];
+    });
+}
+
+int mcg_contact_builds(mcg_ctx* c, int64_t* builds) {
+    return guarded(c, [&] {
+        need_topo(c);
+        if (!builds) throw Fail(MCG_ERR_INVALID, "null output");
+        long long n = c->builds_before;
+        if (c->cb.flags) {
+            d2h(c->hp.u32, c->cb.flags + 4, 1, c->stream);
+            c->sync();
+            n += c->hp.u32[0];
+        }
+        *builds = n;
     });
 }
 

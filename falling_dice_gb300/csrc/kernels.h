@@ -114,9 +114,10 @@ struct ContactBufs {
     uint4* rec;             // [S] pair-test record: quantized AABB (3 words), packed first cell
     int* grid;              // [16]: origin i,j,k; dims i,j,k; mode; valid; bins; bins needed;
                             //       box quantization scale x,y,z and origin x,y,z (float bits)
-    uint32_t* flags;        // [4]: [0] ContactFlag bits of this evaluation, [1] candidate list
-                            //      rebuilt by this evaluation, [2] rebuild forced by the host,
-                            //      [3] the pair pass's occupied-bin cursor
+    uint32_t* flags;        // [5]: [0] ContactFlag bits of this evaluation, [1] candidate list
+                            //      rebuilt by this evaluation, [2] rebuild forced (by the host,
+                            //      or by a build that overflowed), [3] the pair pass's
+                            //      occupied-bin cursor, [4] builds since allocation
     float4* xref;           // [N] node positions (FP32, rounded down) when the list was built
     // bins of fixed capacity: the shapes of bin b at bin_items[b * bin_slots ...]
     long long bin_cap;

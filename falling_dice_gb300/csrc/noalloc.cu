@@ -84,7 +84,7 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.cell_hi = reinterpret_cast<int4*>(take(size_t(S) * sizeof(int4)));
     c.rec = reinterpret_cast<uint4*>(take(size_t(S) * sizeof(uint4)));
     c.grid = reinterpret_cast<int*>(take(16 * sizeof(int)));
-    c.flags = reinterpret_cast<uint32_t*>(take(4 * 4));
+    c.flags = reinterpret_cast<uint32_t*>(take(5 * 4));
     c.xref = reinterpret_cast<float4*>(take(size_t(N > 0 ? N : 1) * sizeof(float4)));
     c.bin_cap = kNoAllocBins;
     c.bin_slots = kNoAllocBinSlots;

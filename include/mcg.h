@@ -334,6 +334,11 @@ int mcg_autotune(mcg_ctx* ctx, const double* z, const double* tops, int32_t reps
 /* Re-applies kernel occupancy shapes as mcg_autotune reports them (0: the default). */
 int mcg_set_kernel_shapes(mcg_ctx* ctx, int32_t beam_blocks, int32_t gather_blocks);
 
+/* Candidate-list builds of the self-contact broad phase since the lattice was uploaded
+ * (no reference counterpart): every evaluation checks whether a node moved farther than the
+ * skin from its position at the last build and builds again if so (mcg_set_contact_skin). */
+int mcg_contact_builds(mcg_ctx* ctx, int64_t* builds);
+
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
  * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept
  * by the distance filter, contacts}. */

@@ -170,3 +170,30 @@ def test_contact_buffers_grow_when_an_evaluation_overflows_them(mcg):
     r = sol.objective(s["z"], s["top"], s["trials"])
     check_eval(r, s, ("ref242 small buffers", 3))
     assert np.array_equal(sol.contact_pairs(), s["pairs"])
+
+
+def test_an_overflowed_build_is_not_reused(mcg):
+    """Evaluations enqueued back to back without reading (the device-resident path) with the
+    candidate list kept between them: a build that overflowed its buffers forces the next
+    evaluation to build again, so the overflow reaches the read and the evaluation is
+    repeated with grown buffers, instead of the incomplete list being reused."""
+    g = golden("ref242")
+    s = g.state(3)
+    sol = solver_for(mcg, g)
+    sol.set_contact_skin(g.cfg.cell_size / 32)
+    sol.set_contact_capacity(0, 0, 0, 0)
+    sol.set_state(plastic=s["plastic"])
+    b0 = sol.contact_builds()
+    sol.upload_z(s["z"])
+    for _ in range(3):
+        sol.objective_resident(s["top"])
+    r = sol.read_result()
+    assert sol.contact_builds() - b0 >= 3  # every overflowed build was repeated
+    check_eval(r, s, ("ref242 resident", 3))
+    assert np.array_equal(sol.contact_pairs(), s["pairs"])
+    # with the buffers grown, repeated evaluations at the same state reuse the list
+    b1 = sol.contact_builds()
+    for _ in range(3):
+        sol.objective_resident(s["top"])
+    r2 = sol.read_result()
+    assert sol.contact_builds() == b1 and r2["energy"] == r["energy"]
