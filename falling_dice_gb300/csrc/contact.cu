@@ -188,19 +188,19 @@ __device__ __forceinline__ bool any_connected(const DevTopo& t, int2 a, int2 b) 
     return false;
 }
 
-// Rest of the test of a candidate pair (sa < sb) that shares no node: connected-pair
-// exclusion, FP64 closest points, dist < target.  Out of line: few candidates get here,
-// and keeping its registers out of the pair loop keeps that loop's occupancy up.
+// Rest of the test of a candidate pair (sa < sb) that is not a local pair (shared or
+// connected nodes, excluded by the pair pass and the filter): FP64 closest points,
+// dist < target.  Out of line: few candidates get here, and keeping its registers out of the
+// calling loops keeps their occupancy up.
 struct PairHit {
     bool hit;
     double s, t, pen;
     d3 n;
 };
 __device__ __noinline__ PairHit narrow_phase(const DevTopo& t, const PhysParams& p, const double4_32a* x, uint32_t sa,
-                                             uint32_t sb, int2 na, int2 nb) {
+                                             uint32_t sb) {
     PairHit h;
     h.hit = false;
-    if (any_connected(t, na, nb)) return h;
     const ShapeRef A = load_shape(t, x, p.joint_radius, sa);
     const ShapeRef B = load_shape(t, x, p.joint_radius, sb);
     const Closest cp = shape_closest(A, B);
@@ -721,7 +721,7 @@ __device__ __forceinline__ int distance_class(const DevTopo& t, const PhysParams
 // Candidate filter, once per list build: keeps, in order, the candidates of one
 // instance whose certified distance lower bound at the build does not exceed the pads plus
 // `reach` (2 sqrt(3) skin: two endpoints that each move at most skin per axis close a gap by
-// at most that).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
+// at most that) and whose nodes are not connected (sim.cpp:24-39).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
 // counts): the kept candidates, compacted.
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf,
@@ -749,6 +749,9 @@ __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, cons
                 if (t.node_inst[na.x] == t.node_inst[nb.x]) {
                     const DistBounds d = dist_bounds(t, p, xf, q.x, q.y);
                     keep = !(d.far_ok && d.far > d.pad_sum + reach);
+                    // local pairs (sim.cpp:24-39) never make contact: dropped here, once per
+                    // build, so the narrow phase of every evaluation needs no hash lookups
+                    if (keep) keep = !any_connected(t, na, nb);
                 }
             }
             const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -790,11 +793,10 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
         } else {
             bool hit = false;
             if (g < total) {
-                const uint2 q = cand2[g];
-                const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
+                const uint2 q = cand2[g];  // not a local pair (k_filter)
                 const int cls = distance_class(t, p, xf, q.x, q.y);
-                if (cls > 0) hit = !any_connected(t, na, nb);  // certainly within the target
-                else if (cls == 0) hit = narrow_phase(t, p, x, q.x, q.y, na, nb).hit;
+                if (cls > 0) hit = true;  // certainly within the target
+                else if (cls == 0) hit = narrow_phase(t, p, x, q.x, q.y).hit;
             }
             const unsigned m = __ballot_sync(0xffffffffu, hit);
             if (lane == 0) {
@@ -813,7 +815,7 @@ __global__ void __launch_bounds__(kBlock) k_contacts(DevTopo t, PhysParams p, co
     const long long nc = min((long long)*total, c.contact_cap);
     for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < nc; o += (long long)gridDim.x * blockDim.x) {
         const uint2 q = cand2[c.c_a[o]];
-        const PairHit h = narrow_phase(t, p, x, q.x, q.y, shape_nodes(t, q.x), shape_nodes(t, q.y));
+        const PairHit h = narrow_phase(t, p, x, q.x, q.y);
         c.c_a[o] = q.x;
         c.c_b[o] = q.y;
         c.c_s[o] = h.s;
