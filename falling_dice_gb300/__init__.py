@@ -54,6 +54,8 @@ SIGNATURES = {
     "mcg_set_contact_shapes": (C.c_int, [_P, C.c_double, C.c_int32]),
     "mcg_set_kernel_shapes": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "mcg_contact_builds": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "mcg_set_solver_loop": (C.c_int, [_P, C.c_int]),
+    "mcg_solver_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -285,6 +287,17 @@ class Solver:
         out = (C.c_int64 * 5)()
         self._check(self.lib.mcg_contact_stats(self.h, out), "mcg_contact_stats")
         return dict(zip(("entries", "occupied_bins", "candidates", "filtered", "contacts"), list(out)))
+
+    def set_solver_loop(self, device):
+        """Solver rounds as a device-resident graph loop (True, the default) or stepped from the
+        host (False); mcg_set_solver_loop."""
+        self._check(self.lib.mcg_set_solver_loop(self.h, int(bool(device))), "mcg_set_solver_loop")
+
+    def solver_loop(self):
+        """(device loop in use, why not when it was switched off)."""
+        v = C.c_int32()
+        self._check(self.lib.mcg_solver_loop(self.h, C.byref(v)), "mcg_solver_loop")
+        return bool(v.value), ("" if v.value else self.lib.mcg_last_error(self.h).decode())
 
     def contact_builds(self):
         """Candidate-list builds since the upload (mcg_contact_builds)."""

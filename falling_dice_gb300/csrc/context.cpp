@@ -26,6 +26,7 @@
 
 #include "../../include/mcg.h"
 #include "kernels.h"
+#include "minimize.h"
 
 namespace mcg {
 std::atomic<long long> g_launch_count{0};
@@ -90,10 +91,13 @@ struct Pinned {
     double* pstats = nullptr;  // [6 I]
     double* cen = nullptr;     // [9 (I + 1)]
     uint32_t* u32 = nullptr;   // [8]
+    Minimizer* mins = nullptr; // [I] the device-resident solver's minimizers, in and out
+    MzStatus* mz = nullptr;    // its status word
     void alloc(int I) {
         release();
         const size_t bytes = I * sizeof(EvalOut) + 3 * I * sizeof(SolveCtl) +
-                             sizeof(double) * (I + I + 6 * I + 9 * (I + 1)) + 8 * 4 + 512;
+                             sizeof(double) * (I + I + 6 * I + 9 * (I + 1)) + 8 * 4 + I * sizeof(Minimizer) +
+                             sizeof(MzStatus) + 1024;
         ck(cudaMallocHost(&base, bytes), "cudaMallocHost");
         std::memset(base, 0, bytes);
         char* p = static_cast<char*>(base);
@@ -109,6 +113,8 @@ struct Pinned {
         pstats = reinterpret_cast<double*>(take(6 * I * sizeof(double)));
         cen = reinterpret_cast<double*>(take(9 * (I + 1) * sizeof(double)));
         u32 = reinterpret_cast<uint32_t*>(take(8 * sizeof(uint32_t)));
+        mins = reinterpret_cast<Minimizer*>(take(I * sizeof(Minimizer)));
+        mz = reinterpret_cast<MzStatus*>(take(sizeof(MzStatus)));
     }
     void release() {
         if (base) cudaFreeHost(base);
@@ -117,30 +123,9 @@ struct Pinned {
     ~Pinned() { release(); }
 };
 
-struct HostStats {
-    int iterations = 0, backtracks = 0;
-    double rms = kInf, max = kInf, energy = kInf;
-    bool converged = false;
-};
-
-// One instance's Simulator::minimize (MC/src/sim.cpp:174-211) as a state machine.
-// Energy noise allowance of the mixed form's line search, relative to |E|.
+// Energy noise allowance of the mixed form's line search, relative to |E| (the state
+// machine of one instance's Simulator::minimize is in minimize.h).
 constexpr double kMixedArmijoSlack = 1e-9;
-
-struct Minimizer {
-    enum Phase { kIdle, kStart, kIterate, kDirection, kSteepest, kTrial, kFinish, kDone };
-    Phase phase = kIdle;
-    double top = 0;
-    bool zero_first = false;  // z = 0 before the first evaluation (run(): zeroVars, sim.cpp:398)
-    bool restore = false;     // z = best before the final evaluation
-    HostStats st;
-    EvalOut cur{}, cand{}, fin{};
-    double cur_rms = 0, cur_max = 0, rms0 = 0, best_energy = 0, dg = 0, step = 1;
-    int it = 0, bt = 0;
-    bool retry = false;       // in the steepest-descent retry of this iteration
-    bool fresh = false;       // the trial is the first of a new direction (dg to be read)
-    bool accepted = false;    // the trial of this round passed the Armijo test
-};
 
 // One instance of the load/unload driver (Simulator::run, MC/src/sim.cpp:374-467).
 struct Task {
@@ -243,6 +228,22 @@ struct mcg_ctx {
     std::vector<uint8_t> fused;  // the instance's direction is computed by one CTA
     bool have_final = false;  // instance 0 has a final state from minimize, not yet committed
 
+    // ---- the device-resident round loop ------------------------------------------------
+    // Rounds run as the body of a CUDA-graph WHILE node (minimize_dev.cu): the host launches
+    // the loop once and reads the minimizers back when an instance has finished (or a round
+    // cap was reached, or an evaluation overflowed a contact buffer), instead of
+    // synchronising after every round.  Off while timing phases (direct launches) or when
+    // the graph cannot be built (loop_error says why); the host-stepped rounds then run.
+    Minimizer* d_mins = nullptr;
+    uint8_t* d_fused = nullptr;
+    uint8_t* d_trial = nullptr;   // per-instance trial mask of the loop's evaluations
+    MzStatus* d_mz = nullptr;
+    cudaGraphExec_t loop_exec = nullptr;
+    cudaStream_t side = nullptr;  // captures the bodies of the loop's conditional nodes
+    bool device_loop = true;
+    std::string loop_error;
+    static constexpr int kLoopRoundCap = 4096;
+
     // optional per-phase timing of evaluations (events on the context stream)
     // state, beams, contact grid (up to the pair enumeration), pair enumeration (k_bin_pairs),
     // narrow phase and contact lists, gather, finalize
@@ -269,6 +270,7 @@ struct mcg_ctx {
         drop_graphs();
         for (auto& e : ev_t)
             if (e) cudaEventDestroy(e);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -404,6 +406,8 @@ struct mcg_ctx {
     };
     std::vector<SeqGraph> seq_graphs;
     void drop_graphs() {
+        if (loop_exec) cudaGraphExecDestroy(loop_exec);
+        loop_exec = nullptr;
         for (EvalGraph& g : graphs) cudaGraphExecDestroy(g.exec);
         graphs.clear();
         for (SeqGraph& g : seq_graphs) cudaGraphExecDestroy(g.exec);
@@ -470,7 +474,8 @@ struct mcg_ctx {
         last_grad = d_gout;
     }
 
-    void eval_launches(const double* dz, bool trials, double* d_gout) {
+    // trials: 0 none, 1 every instance, 2 the instances of d_trial (device-resident loop)
+    void eval_launches(const double* dz, int trials, double* d_gout) {
         PhysParams p = phys;
         p.broad_cell = broad_cell;
         p.inv_cell_f = float(1.0 / broad_cell);
@@ -548,33 +553,25 @@ struct mcg_ctx {
         SolveCtl* c = ctl_stage(k);
         for (int i = 0; i < I; i++) c[i] = SolveCtl{0.0, 0, 0, 0, 0};
     }
-    bool converged(const EvalOut& o, double rms, double mx, double rms0) const {
-        if (cfg.relative_gradient_tolerance > 0)
-            return (rms <= cfg.relative_gradient_tolerance * rms0) && o.max_pen <= cfg.penetration_tolerance;
-        const double rel = rms / std::max(1e-6, cfg.translation_scale * std::max(1.0, o.reaction));
-        const double rrt = cfg.reaction_relative_tolerance == 0 ? 1.5e-3 : cfg.reaction_relative_tolerance;
-        const bool forceOK = (rms <= cfg.gradient_rms_tolerance && mx <= cfg.gradient_max_tolerance) || rel < rrt;
-        return forceOK && o.max_pen <= cfg.penetration_tolerance;
-    }
-    // Host-only step of the iteration loop (sim.cpp:176-177): record, test convergence,
-    // continue with a direction or finish.
-    void iterate(Minimizer& s) {
-        if (s.it >= cfg.max_iterations) {
-            s.phase = Minimizer::kFinish;
-            s.restore = !s.st.converged && s.best_energy < s.cur.energy;
-            return;
-        }
-        s.st.iterations = s.it + 1;
-        s.st.rms = s.cur_rms;
-        s.st.max = s.cur_max;
-        s.st.energy = s.cur.energy;
-        if (converged(s.cur, s.cur_rms, s.cur_max, s.rms0)) {
-            s.st.converged = true;
-            s.phase = Minimizer::kFinish;
-            s.restore = false;
-            return;
-        }
-        s.phase = Minimizer::kDirection;
+    // The configuration the minimize decisions read (minimize.h).
+    MzParams mz_params() const {
+        MzParams p{};
+        p.max_iterations = cfg.max_iterations;
+        p.max_line_search = cfg.max_line_search;
+        p.H = H;
+        p.relative_gradient_tolerance = cfg.relative_gradient_tolerance;
+        p.translation_scale = cfg.translation_scale;
+        p.reaction_relative_tolerance = cfg.reaction_relative_tolerance;
+        p.gradient_rms_tolerance = cfg.gradient_rms_tolerance;
+        p.gradient_max_tolerance = cfg.gradient_max_tolerance;
+        p.penetration_tolerance = cfg.penetration_tolerance;
+        p.armijo = cfg.armijo;
+        p.min_line_step = cfg.min_line_step;
+        // The mixed form's energy carries rounding noise of ~3e-10 |E| (compensated FP32
+        // sums of FP32 beam energies); near equilibrium a step's decrease falls below it, so
+        // its Armijo test allows that much slack.  The FP64 form tests exactly.
+        p.slack_rel = mixed ? kMixedArmijoSlack : 0.0;
+        return p;
     }
     // Starts instance i's minimization at platen height `top` from the current d_z (or from
     // z = 0 with zero_first), with an empty history.
@@ -585,37 +582,32 @@ struct mcg_ctx {
         s.top = top;
         s.zero_first = zero_first;
     }
+    bool pending() const {
+        for (const Minimizer& s : mins)
+            if (s.phase != Minimizer::kIdle && s.phase != Minimizer::kDone) return true;
+        return false;
+    }
 
-    // One round for every instance with an unfinished minimization: directions, one
-    // evaluation each, decisions, accepted steps.  The history (pairs, slots, rho) and the
-    // fallback to steepest descent when a direction does not descend are decided on the
-    // device (the reference's rules, sim.cpp:191, 205-206); the host reads back once per
-    // round: the evaluation's totals and each instance's dg.  False when no instance had
-    // work.
+    // One round for every instance with an unfinished minimization, stepped from the host:
+    // directions, one evaluation each, decisions, accepted steps.  The decisions are
+    // minimize.h's (the reference's, sim.cpp:174-211); the history (pairs, slots, rho) and
+    // the fallback to steepest descent when a direction does not descend are decided on the
+    // device (sim.cpp:191, 205-206); the host reads back once per round: the evaluation's
+    // totals and each instance's dg.  False when no instance had work.
     bool minimize_round() {
-        using M = Minimizer;
         const double mt = cfg.max_translation_step / cfg.translation_scale, mr = cfg.max_rotation_step;
+        const MzParams P = mz_params();
         // A. search directions: two-loop (sim.cpp:184-190), or steepest descent for the retry
         //    after a failed line search (:193-196)
         bool any_dir = false, any_multi = false, any_sd = false;
         clear_ctl(0);
         SolveCtl* ca = ctl_stage(0);
         for (int i = 0; i < I; i++) {
-            M& s = mins[size_t(i)];
-            if (s.phase == M::kDirection) {
-                ca[i].flags = fused[size_t(i)] ? kOpDirFused : kOpDirection;
-                any_multi |= !fused[size_t(i)];
-                any_dir = true;
-            } else if (s.phase == M::kSteepest) {
-                ca[i].flags = kOpSteepest;
-                any_sd = true;
-            } else {
-                continue;
-            }
-            s.phase = M::kTrial;  // first trial of the new direction, step 1
-            s.step = 1.0;
-            s.bt = 0;
-            s.fresh = true;
+            const int f = mz_stage_direction(mins[size_t(i)], fused[size_t(i)] != 0);
+            ca[i].flags = f;
+            any_dir |= f == kOpDirFused || f == kOpDirection;
+            any_multi |= f == kOpDirection;
+            any_sd |= f == kOpSteepest;
         }
         if (any_dir || any_sd) {
             upload_ctl(0);
@@ -633,26 +625,16 @@ struct mcg_ctx {
         bool any = false, trials = false;
         std::vector<uint8_t> a(size_t(I), 0);
         for (int i = 0; i < I; i++) {
-            const M& s = mins[size_t(i)];
-            SolveCtl& c = cb1[i];
-            switch (s.phase) {
-                case M::kStart:
-                    c.flags = kOpResetHistory | (s.zero_first ? kOpZero : 0) | kOpEvalAtZ | kOpKeepBest;
-                    break;
-                case M::kTrial:
-                    c.flags = kOpCandidate;
-                    c.step = s.step;
-                    break;
-                case M::kFinish:
-                    c.flags = (s.restore ? kOpRestore : 0) | kOpEvalAtZ | kOpFinal;
-                    trials = true;
-                    break;
-                default:
-                    continue;
-            }
+            double step = 0;
+            bool tr = false;
+            const int f = mz_stage_eval(mins[size_t(i)], step, tr);
+            if (!f) continue;
+            cb1[i].flags = f;
+            cb1[i].step = step;
+            trials |= tr;
             any = true;
             a[size_t(i)] = 1;
-            hp.tops[i] = s.top;
+            hp.tops[i] = mins[size_t(i)].top;
         }
         if (!any) return false;
         set_active(a);
@@ -666,65 +648,9 @@ struct mcg_ctx {
         SolveCtl* cc = ctl_stage(2);
         bool any_post = false;
         for (int i = 0; i < I; i++) {
-            M& s = mins[size_t(i)];
-            SolveCtl& c = cc[i];
-            const EvalOut& o = out[i];
-            switch (s.phase) {
-                case M::kStart:
-                    s.cur = o;
-                    s.cur_rms = o.rms;
-                    s.cur_max = o.gmax;
-                    s.best_energy = o.energy;
-                    s.rms0 = o.rms;
-                    s.it = 0;
-                    c.flags = kOpTakeGrad;
-                    any_post = true;
-                    s.phase = M::kIterate;
-                    break;
-                case M::kTrial: {
-                    if (s.fresh) {
-                        s.dg = hp.dg[i];
-                        s.fresh = false;
-                    }
-                    s.cand = o;
-                    s.st.backtracks++;
-                    // Armijo (sim.cpp:180).  The mixed form's energy carries rounding noise of
-                    // ~3e-10 |E| (compensated FP32 sums of FP32 beam energies); near
-                    // equilibrium a step's decrease falls below it, so the mixed form allows
-                    // that much slack, kMixedArmijoSlack |E|.  The FP64 form tests exactly.
-                    const double slack = mixed ? kMixedArmijoSlack * std::abs(s.cur.energy) : 0.0;
-                    if (std::isfinite(o.energy) && o.energy <= s.cur.energy + cfg.armijo * s.step * s.dg + slack) {
-                        c.flags = kOpAccept | (H > 0 ? kOpPair : 0) | (o.energy < s.best_energy ? kOpKeepBestAfter : 0);
-                        any_post = true;
-                        s.accepted = true;
-                        break;
-                    }
-                    s.step *= .5;
-                    s.bt++;
-                    if (!(s.step < cfg.min_line_step) && s.bt < cfg.max_line_search) break;
-                    // line search failed (sim.cpp:193-209)
-                    if (!s.retry) {
-                        s.retry = true;
-                        s.phase = M::kSteepest;
-                    } else {
-                        s.phase = M::kFinish;
-                        s.restore = !s.st.converged && s.best_energy < s.cur.energy;
-                    }
-                    break;
-                }
-                case M::kFinish:
-                    s.fin = o;
-                    s.st.rms = o.rms;
-                    s.st.max = o.gmax;
-                    s.st.energy = o.energy;
-                    s.st.converged = converged(o, o.rms, o.gmax, s.rms0);
-                    c.flags = kOpTakeGrad;
-                    any_post = true;
-                    s.phase = M::kDone;
-                    break;
-                default:
-                    break;
-            }
+            const int f = mz_stage_decide(P, mins[size_t(i)], out[i], hp.dg[i]);
+            cc[i].flags = f;
+            any_post |= f != 0;
         }
         if (any_post) {
             upload_ctl(2);
@@ -733,28 +659,178 @@ struct mcg_ctx {
                           d_part, d_dots3, stream);
             });
         }
-        // accepted steps: current point, best point (the curvature pair is the device's)
-        for (int i = 0; i < I; i++) {
-            M& s = mins[size_t(i)];
-            if (s.phase == M::kTrial && s.accepted) {
-                s.accepted = false;
-                s.cur = s.cand;
-                s.cur_rms = s.cand.rms;
-                s.cur_max = s.cand.gmax;
-                if (s.cur.energy < s.best_energy) s.best_energy = s.cur.energy;
-                s.retry = false;
-                s.it++;
-                s.phase = M::kIterate;
-            }
-            if (s.phase == M::kIterate) iterate(s);
-        }
         check_launch();
         return true;
     }
 
+    // Adds, to the graph being captured on `stream`, an IF node on handle h whose body is
+    // what inner(side) launches (captured on the side stream).
+    template <typename F>
+    void capture_if(cudaGraphConditionalHandle h, F&& inner) {
+        cudaStreamCaptureStatus st;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        const cudaGraphEdgeData* edges = nullptr;
+        size_t nd = 0;
+        ck(cudaStreamGetCaptureInfo(stream, &st, nullptr, &g, &deps, &edges, &nd), "cudaStreamGetCaptureInfo");
+        cudaGraphNodeParams prm{};
+        prm.type = cudaGraphNodeTypeConditional;
+        prm.conditional.handle = h;
+        prm.conditional.type = cudaGraphCondTypeIf;
+        prm.conditional.size = 1;
+        cudaGraphNode_t node;
+        ck(cudaGraphAddNode(&node, g, deps, edges, nd, &prm), "cudaGraphAddNode (IF)");
+        cudaGraph_t body = prm.conditional.phGraph_out[0];
+        ck(cudaStreamUpdateCaptureDependencies(stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies),
+           "cudaStreamUpdateCaptureDependencies");
+        ck(cudaStreamBeginCaptureToGraph(side, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+           "cudaStreamBeginCaptureToGraph");
+        inner(side);
+        cudaGraph_t out = nullptr;
+        ck(cudaStreamEndCapture(side, &out), "cudaStreamEndCapture (IF body)");
+    }
+
+    MzDev mz_dev() {
+        MzDev d{};
+        d.I = I;
+        d.mins = d_mins;
+        d.fused = d_fused;
+        d.ctl = d_ctl;
+        d.active = d_active;
+        d.trial_inst = d_trial;
+        d.tops = ev.tops;
+        d.dg = d_dg;
+        d.out = ev.out;
+        d.contact_flags = cfg.self_contact ? cb.flags : nullptr;
+        d.status = d_mz;
+        d.round_cap = kLoopRoundCap;
+        return d;
+    }
+
+    // The round loop as one graph: WHILE(loop) { A; IF(fused) one-CTA directions;
+    // IF(multi) two-loop; IF(any direction) descent fix; IF(steepest) retry; B; prepare;
+    // evaluation (trial states per instance); C; IF(accept) accept step }.
+    void build_loop() {
+        if (!side) ck(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking), "cudaStreamCreate");
+        const double mt = cfg.max_translation_step / cfg.translation_scale, mr = cfg.max_rotation_step;
+        const MzDev md = mz_dev();
+        const MzParams P = mz_params();
+        cudaGraph_t g = nullptr;
+        ck(cudaGraphCreate(&g, 0), "cudaGraphCreate");
+        try {
+            cudaGraphConditionalHandle h_loop;
+            ck(cudaGraphConditionalHandleCreate(&h_loop, g, 1, cudaGraphCondAssignDefault), "conditional handle");
+            cudaGraphNodeParams wp{};
+            wp.type = cudaGraphNodeTypeConditional;
+            wp.conditional.handle = h_loop;
+            wp.conditional.type = cudaGraphCondTypeWhile;
+            wp.conditional.size = 1;
+            cudaGraphNode_t wnode;
+            ck(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp), "cudaGraphAddNode (WHILE)");
+            cudaGraph_t body = wp.conditional.phGraph_out[0];
+            cudaGraphConditionalHandle hf, hm, hd, hs, hpost;
+            for (cudaGraphConditionalHandle* h : {&hf, &hm, &hd, &hs, &hpost})
+                ck(cudaGraphConditionalHandleCreate(h, body, 0, cudaGraphCondAssignDefault), "conditional handle");
+            const long long before = g_launch_count.load();
+            ck(cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCaptureToGraph");
+            try {
+                const int Hs = std::max(H, 1);
+                launch_mz_direction(md, hf, hm, hd, hs, stream);
+                capture_if(hf, [&](cudaStream_t s2) {
+                    bl_direction_fused(topo, d_ctl, d_hist, Hs, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_dg, mt, mr, s2);
+                });
+                capture_if(hm, [&](cudaStream_t s2) {
+                    bl_direction_multi(topo, d_ctl, d_hist, Hs, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_alpha, d_part,
+                                       d_dg, mt, mr, s2);
+                });
+                capture_if(hd, [&](cudaStream_t s2) {
+                    bl_descent_fix(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, s2);
+                });
+                capture_if(hs, [&](cudaStream_t s2) {
+                    bl_steepest(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, s2);
+                });
+                launch_mz_eval(md, stream);
+                bl_prepare(topo, d_ctl, d_hist, d_z, d_best, d_zeval, d_p, d_zfinal, stream);
+                eval_launches(d_zeval, 2, d_geval);
+                launch_mz_decide(md, P, hpost, h_loop, stream);
+                capture_if(hpost, [&](cudaStream_t s2) {
+                    bl_accept(topo, d_ctl, d_hist, H, d_z, d_g, d_zeval, d_geval, d_S, d_Y, 6LL * N, d_best, d_rho,
+                              d_part, d_dots3, s2);
+                });
+            } catch (...) {
+                cudaGraph_t junk = nullptr;
+                cudaStreamEndCapture(stream, &junk);
+                cudaGetLastError();
+                throw;
+            }
+            cudaGraph_t out = nullptr;
+            ck(cudaStreamEndCapture(stream, &out), "cudaStreamEndCapture (loop body)");
+            loop_round_kernels = g_launch_count.load() - before;
+            g_launch_count -= loop_round_kernels;  // counted per round run (rounds_device)
+            ck(cudaGraphInstantiate(&loop_exec, g, 0), "cudaGraphInstantiate (loop)");
+        } catch (...) {
+            cudaGraphDestroy(g);
+            throw;
+        }
+        cudaGraphDestroy(g);
+    }
+
+    // Rounds on the device until an instance finishes, none has work, the round cap is
+    // reached or an evaluation overflows a contact buffer (then the buffers grow and the
+    // loop runs again from that evaluation).  The host minimizers are copied in before and
+    // out after.  False when no instance had work.
+    bool rounds_device() {
+        if (!pending()) return false;
+        for (int tries = 0;; tries++) {
+            if (!loop_exec) build_loop();
+            std::copy(mins.begin(), mins.end(), hp.mins);
+            h2d(d_mins, hp.mins, size_t(I), stream);
+            launch_mz_reset(mz_dev(), stream);
+            ck(cudaGraphLaunch(loop_exec, stream), "cudaGraphLaunch (loop)");
+            d2h(hp.mins, d_mins, size_t(I), stream);
+            d2h(hp.mz, d_mz, 1, stream);
+            d2h(hp.outs, ev.out, size_t(I), stream);
+            if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
+            sync();
+            check_launch();
+            note_launches(int(hp.mz->rounds) * int(loop_kernels_per_round()));
+            std::copy(hp.mins, hp.mins + I, mins.begin());
+            active.assign(size_t(I), 2);  // the loop wrote d_active: the host mirror is unknown
+            last_z = d_zeval;
+            last_trials = false;
+            last_grad = d_geval;
+            if (!hp.mz->overflow) break;
+            if (tries >= 16 || !grow_contacts(hp.outs[0].overflow))
+                throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
+        }
+        if (cfg.self_contact) last_contacts = hp.u32[0];
+        contacts_stale = false;
+        return true;
+    }
+    // Kernels one loop round launches (the device counts no launches; this estimate keeps
+    // the library's launch counter meaningful): stage kernels plus the evaluation's.
+    long long loop_kernels_per_round() const { return loop_round_kernels; }
+    long long loop_round_kernels = 0;
+
+    // One step of rounds: on the device when the loop is available, else host-stepped.
+    bool step_rounds() {
+        if (device_loop && use_graphs && !timing) {
+            try {
+                return rounds_device();
+            } catch (const Fail& f) {
+                if (f.code == MCG_ERR_CAPACITY) throw;
+                device_loop = false;  // e.g. the driver refuses the conditional nodes
+                loop_error = f.what();
+                drop_graphs();
+            }
+        }
+        return minimize_round();
+    }
+
     // Steps the minimizations started with start_minimize until all are done.
     void minimize_all() {
-        while (minimize_round()) {
+        while (step_rounds()) {
         }
     }
 
@@ -874,7 +950,7 @@ struct mcg_ctx {
                 pending = true;
             }
             if (!pending) break;
-            minimize_round();
+            step_rounds();
             bool any_commit = false;
             std::fill(cm.begin(), cm.end(), uint8_t(0));
             for (int i = 0; i < I; i++) {
@@ -1277,6 +1353,9 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         h2d(c->d_all, ones.data(), ones.size(), s);
         T.active = c->d_active;
         c->active = ones;
+        c->d_trial = M.get<uint8_t>(size_t(I));
+        ck(cudaMemsetAsync(c->d_trial, 0, size_t(I), s), "memset");
+        T.trial_inst = c->d_trial;
         c->sync();  // the host vectors above go out of scope
     }
     c->topo = T;
@@ -1440,6 +1519,10 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         const int4 r = irange[size_t(k)];
         c->fused[size_t(k)] = r.y - r.x <= fused_direction_limit() && c->H <= 64;
     }
+    c->d_mins = Q.get<Minimizer>(size_t(I));
+    c->d_mz = Q.get<MzStatus>(1);
+    c->d_fused = Q.get<uint8_t>(size_t(I));
+    h2d(c->d_fused, c->fused.data(), size_t(I), s);
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
         launch_mixed_constants(c->topo, c->mb, s);
@@ -1860,6 +1943,23 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
         for (int k = 0; k < 5; k++) out5[k] = c->hp.u32[k];
+    });
+}
+
+int mcg_set_solver_loop(mcg_ctx* c, int device) {
+    return guarded(c, [&] {
+        c->sync();
+        c->device_loop = device != 0;
+        c->loop_error.clear();
+        c->drop_graphs();
+    });
+}
+
+int mcg_solver_loop(mcg_ctx* c, int32_t* device) {
+    return guarded(c, [&] {
+        if (!device) throw Fail(MCG_ERR_INVALID, "null output");
+        *device = c->device_loop ? 1 : 0;
+        if (!c->device_loop && !c->loop_error.empty()) c->err = c->loop_error;
     });
 }
 

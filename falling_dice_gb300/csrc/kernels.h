@@ -60,6 +60,7 @@ struct DevTopo {
     const float2* off;        // [I] (x, z) offset of the instance in the contact grid
     const int* node_inst;     // [N] instance of each node
     const uint8_t* active;    // [I] 0: the instance is not evaluated (its outputs keep old values)
+    const uint8_t* trial_inst;  // [I] with trials == 2: 1 where the instance writes its trial states
 };
 
 // Elements per mapped block (the launch block size of the mapped kernels).
@@ -229,7 +230,7 @@ int shape_variants(ShapeKernel k);
 int shape_blocks(ShapeKernel k, int variant);
 int beams_mixed_variants();
 int beams_mixed_blocks(int variant);
-void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials,
+void launch_beams(const DevTopo& t, const Material& m, const double* plastic, int trials,
                   EvalBufs& e, cudaStream_t s, int variant = 0);
 void launch_gather(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad,
                    EvalBufs& e, cudaStream_t s, int variant = 0);
@@ -246,7 +247,7 @@ void launch_gather_mixed(const DevTopo& t, const PhysParams& p, const ContactBuf
 // ---- mixed-precision form (objective_mixed.cu) ------------------------------------------
 void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                         const MixedNodes& mn, EvalBufs& e, cudaStream_t s);
-void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
+void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, int trials,
                         EvalBufs& e, cudaStream_t s, int variant = 0);
 void launch_rebase_mixed(const DevTopo& t, const double* base_x, const double* base_r, MixedBeams& mb,
                          MixedNodes& mn, cudaStream_t s);
@@ -320,6 +321,17 @@ int fused_direction_limit();
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
                   double* dg, double mt, double mr, cudaStream_t s);
+// The pieces of bl_direction, for callers that launch them under separate conditions: the
+// one-CTA directions (kOpDirFused), the multi-block two-loop (kOpDirection), and the
+// steepest-descent fallback of either kind where <g, p> >= 0.
+void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
+                        const double* S, const double* Y, long long stride, const double* rho, double* dg, double mt,
+                        double mr, cudaStream_t s);
+void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
+                        const double* S, const double* Y, long long stride, const double* rho, double* alpha,
+                        double* part, double* dg, double mt, double mr, cudaStream_t s);
+void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
+                    double* dg, double mt, double mr, cudaStream_t s);
 // The steepest-descent retry for the kOpSteepest instances: history cleared,
 // p = clamp(lock(-g)), dg[i] = <g, p> (sim.cpp:193-196).
 void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,

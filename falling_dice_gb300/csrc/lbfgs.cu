@@ -583,31 +583,46 @@ size_t lbfgs_part_doubles(int n_nblk) { return 4 * size_t(n_nblk) + 8; }
 
 int fused_direction_limit() { return kFuseChunks; }
 
+void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
+                        const double* S, const double* Y, long long stride, const double* rho, double* dg, double mt,
+                        double mr, cudaStream_t s) {
+    (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
+}
+
+void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
+                        const double* S, const double* Y, long long stride, const double* rho, double* alpha,
+                        double* part, double* dg, double mt, double mr, cudaStream_t s) {
+    const int nb = t.n_nblk;
+    // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
+    double* pp[2] = {part, part + size_t(nb)};
+    double* h0part = part + 2 * size_t(nb);
+    (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, h0part, pp[0]), note_launches(1));
+    for (int j = 0; j < H; j++)
+        (k_tl_step<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
+                                            pp[(j + 1) & 1]),
+         note_launches(1));
+    (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, Y, stride, h0part, pp[0]), note_launches(1));
+    for (int j = 0; j < H; j++)
+        (k_tl_step<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
+                                            pp[(j + 1) & 1]),
+         note_launches(1));
+    (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
+    (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
+}
+
+void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
+                    double* dg, double mt, double mr, cudaStream_t s) {
+    // not a descent direction: steepest descent, history cleared (sim.cpp:191)
+    (k_descent_fix<<<t.n_nblk, kBlock, 0, s>>>(t, ctl, dg, p, g, mt, mr, part), note_launches(1));
+    (k_descent_final<<<t.I, kBlock, 0, s>>>(t, ctl, part, dg, hist), note_launches(1));
+}
+
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
                   double* dg, double mt, double mr, cudaStream_t s) {
-    const int nb = t.n_nblk;
-    (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
-    if (multi) {
-        // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
-        double* pp[2] = {part, part + size_t(nb)};
-        double* h0part = part + 2 * size_t(nb);
-        (k_tl_start<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, h0part, pp[0]), note_launches(1));
-        for (int j = 0; j < H; j++)
-            (k_tl_step<1><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
-                                                pp[(j + 1) & 1]),
-             note_launches(1));
-        (k_tl_scale<<<nb, kBlock, 0, s>>>(t, ctl, hist, H, p, Y, stride, h0part, pp[0]), note_launches(1));
-        for (int j = 0; j < H; j++)
-            (k_tl_step<2><<<nb, kBlock, 0, s>>>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1],
-                                                pp[(j + 1) & 1]),
-             note_launches(1));
-        (k_finish<<<nb, kBlock, 0, s>>>(t, ctl, kOpDirection, p, p, g, mt, mr, part), note_launches(1));
-        (k_inst_final<1><<<t.I, kBlock, 0, s>>>(t, ctl, kOpDirection, part, dg), note_launches(1));
-    }
-    // not a descent direction: steepest descent, history cleared (sim.cpp:191)
-    (k_descent_fix<<<nb, kBlock, 0, s>>>(t, ctl, dg, p, g, mt, mr, part), note_launches(1));
-    (k_descent_final<<<t.I, kBlock, 0, s>>>(t, ctl, part, dg, hist), note_launches(1));
+    bl_direction_fused(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s);
+    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s);
+    bl_descent_fix(t, ctl, hist, p, g, part, dg, mt, mr, s);
 }
 
 void bl_steepest(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,

@@ -197,6 +197,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams(DevTopo t, Materia
     __shared__ double sm[3 * (kBlock / 32)];
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
+    if (trials == 2) trials = t.trial_inst[mp.inst];  // per instance (device-resident solver)
     const int b = mp.i;
     const int B = t.B;
     double acc[3] = {0, 0, 0};  // energy, elastic, plastic
@@ -411,8 +412,29 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_gather(DevTopo t, PhysPa
         // of the contact list
         if (use_contacts) {
             const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
-            for (uint32_t k = 0; k < cnt; k++)
-                add_contact_item(c, p, N, c.n_sorted[s0 + k], gx, acc[4], acc[3], pen_max);
+            uint32_t k = 0;
+            // four items at a time: their loads in flight together (a joint of a densely
+            // compressed lattice can hold a few hundred items), the additions in list order
+            for (; k + 4 <= cnt; k += 4) {
+                d3 f[4];
+                double pen[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint32_t item = c.n_sorted[s0 + k + j];
+                    f[j] = contact_slot_force(c, p, N, item);
+                    pen[j] = (item & 3u) == 0 ? c.c_pen[item >> 2] : -1.0;  // a contact's pen > 0
+                }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    gx = gx + f[j];
+                    if (pen[j] >= 0) {
+                        acc[4] += .5 * p.contact_k * pen[j] * pen[j];
+                        acc[3] += 1;
+                        pen_max = fmax(pen_max, pen[j]);
+                    }
+                }
+            }
+            for (; k < cnt; k++) add_contact_item(c, p, N, c.n_sorted[s0 + k], gx, acc[4], acc[3], pen_max);
         }
         // platens (sim.cpp:168-171)
         const double jr = p.joint_radius, kc = p.contact_k;
@@ -681,10 +703,10 @@ int shape_blocks(ShapeKernel k, int v) {
     }
 }
 
-void launch_beams(const DevTopo& t, const Material& m, const double* plastic, bool trials, EvalBufs& e,
+void launch_beams(const DevTopo& t, const Material& m, const double* plastic, int trials, EvalBufs& e,
                   cudaStream_t s, int variant) {
     if (t.B == 0) return;
-    const int tr = trials ? 1 : 0;
+    const int tr = trials;  // 0, 1, or 2: per instance (t.trial_inst)
     switch (variant) {
         case 1: k_beams<kBeamBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, tr, e); break;
         case 2: k_beams<kBeamBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, plastic, tr, e); break;

@@ -308,6 +308,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
     __shared__ float sm[2 * kBlock];  // per-thread elastic and plastic energies
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
+    if (trials == 2) trials = t.trial_inst[mp.inst];  // per instance (device-resident solver)
     const int b = mp.i;
     const int B = t.B;
     float ue = 0.f, up = 0.f;  // elastic energy, plastic dissipation of this beam
@@ -503,10 +504,10 @@ constexpr int kMixedBlocks[] = {3, 4, 5, 6};
 int beams_mixed_variants() { return 4; }
 int beams_mixed_blocks(int v) { return kMixedBlocks[v]; }
 
-void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, bool trials,
+void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, int trials,
                         EvalBufs& e, cudaStream_t s, int variant) {
     if (t.B == 0) return;
-    const int tr = trials ? 1 : 0;
+    const int tr = trials;  // 0, 1, or 2: per instance (t.trial_inst)
     if (mb.C0) {
         k_beams_mixed<true, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e);
     } else {

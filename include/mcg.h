@@ -334,6 +334,18 @@ int mcg_autotune(mcg_ctx* ctx, const double* z, const double* tops, int32_t reps
 /* Re-applies kernel occupancy shapes as mcg_autotune reports them (0: the default). */
 int mcg_set_kernel_shapes(mcg_ctx* ctx, int32_t beam_blocks, int32_t gather_blocks);
 
+/* Where the solver's rounds are stepped (no reference counterpart).  With device != 0
+ * (the default) mcg_minimize, mcg_run and mcg_batch_run run their rounds as one CUDA-graph
+ * loop on the device: each round's directions, evaluation, decisions and accepted step are
+ * graph nodes, the decisions (the reference's, sim.cpp:174-211) are taken by device kernels
+ * from the same FP64 numbers, and the host synchronises only when an instance has finished
+ * its minimization.  With device == 0 the host takes the decisions after every round.  Both
+ * give the same results bit for bit.  While phase timing is on (mcg_set_timing) the host
+ * steps the rounds.  mcg_solver_loop reports whether the device loop is in use; when it
+ * could not be built it is switched off, and mcg_last_error then says why. */
+int mcg_set_solver_loop(mcg_ctx* ctx, int device);
+int mcg_solver_loop(mcg_ctx* ctx, int32_t* device);
+
 /* Candidate-list builds of the self-contact broad phase since the lattice was uploaded
  * (no reference counterpart): every evaluation checks whether a node moved farther than the
  * skin from its position at the last build and builds again if so (mcg_set_contact_skin). */

@@ -138,3 +138,20 @@ def test_kernel_occupancy_variants_leave_evaluations_unchanged(mcg, precision, b
     assert t["beam_blocks"] in beam_blocks and t["gather_blocks"] in (1, 2, 4)
     got = b.objective(z, tops)
     assert np.array_equal(got["grad"], ref["grad"])
+
+
+def test_batched_run_is_the_same_with_host_stepped_rounds(mcg):
+    """The batch run with its rounds in the device-resident graph loop (the default; the
+    loop returns to the host whenever a lattice finishes an increment) and stepped from the
+    host: the same frames bit for bit."""
+    cfg, lats, ys = make(mcg, load_steps=10, unload_steps=4, max_strain=0.25)
+    out = {}
+    for device in (True, False):
+        batch = mcg.BatchSolver(cfg, lats, yields=ys)
+        batch.set_solver_loop(device)
+        out[device] = batch.run()
+        assert batch.solver_loop()[0] == device, batch.solver_loop()[1]
+    (sa, ra), (sb, rb) = out[True], out[False]
+    assert list(sa) == list(sb)
+    for k in range(len(lats)):
+        assert ra[k] == rb[k], k

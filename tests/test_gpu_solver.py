@@ -224,3 +224,42 @@ def test_relative_gradient_mode_reaches_1e8_on_a_loading_increment(mcg, mco):
     # to ~2e-5 (a gradient reduced 1e8-fold still leaves the soft modes of the lattice loose)
     assert abs(feg - feo) <= 1e-10 * abs(feo)
     assert rel_err(zg, zo) <= 1e-4
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_device_loop_takes_the_host_loops_decisions(mcg, precision):
+    """The solver's rounds as a device-resident graph loop (decisions by device kernels,
+    the host synchronising once per finished minimization) against the same rounds stepped
+    from the host: the chaotic 2x4x2 run (reordered sums move its peak force by 15 %) and a
+    minimize of the 6x6x6 specimen give the same frames, iterations and states bit for bit,
+    in both precision forms."""
+    from falling_dice_gb300 import abi
+    g = golden("ref242")
+    cfg = g.cfg
+    cfg.precision = precision
+    out = {}
+    for device in (True, False):
+        sol = mcg.Solver(cfg, g.lattice)
+        sol.set_solver_loop(device)
+        rc, frames = sol.run()
+        assert rc == 0
+        used, why = sol.solver_loop()
+        assert used == device, why
+        out[device] = (frames, sol.get_state())
+    fa, sa = out[True]
+    fb, sb = out[False]
+    assert fa == fb
+    for x, y in zip(sa, sb):
+        assert np.array_equal(x, y)
+    c6 = golden("cubic6")
+    cfg6 = c6.cfg
+    cfg6.precision = precision
+    res = {}
+    for device in (True, False):
+        sol = mcg.Solver(cfg6, c6.lattice)
+        sol.set_solver_loop(device)
+        top = c6.lattice.geometry.top0 - 0.02 * c6.lattice.geometry.height
+        z, st, fe, fd = sol.minimize(top, np.zeros(6 * c6.lattice.n_nodes))
+        res[device] = (z, st, fe, fd)
+    assert np.array_equal(res[True][0], res[False][0])
+    assert res[True][1] == res[False][1] and res[True][2] == res[False][2] and res[True][3] == res[False][3]
