@@ -56,6 +56,7 @@ SIGNATURES = {
     "mcg_contact_builds": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_set_solver_loop": (C.c_int, [_P, C.c_int]),
     "mcg_solver_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
+    "mcg_solver_times": (C.c_int, [_P, _d, C.POINTER(C.c_int64)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
     "mcg_instance_count": (C.c_int32, [_P]),
@@ -292,6 +293,14 @@ class Solver:
         """Solver rounds as a device-resident graph loop (True, the default) or stepped from the
         host (False); mcg_set_solver_loop."""
         self._check(self.lib.mcg_set_solver_loop(self.h, int(bool(device))), "mcg_set_solver_loop")
+
+    def solver_times(self):
+        """Device-resident loop time by stage (ms) and rounds (mcg_solver_times)."""
+        ms = np.zeros(4)
+        n = C.c_int64()
+        self._check(self.lib.mcg_solver_times(self.h, _ptr(ms), C.byref(n)), "mcg_solver_times")
+        return {"directions": ms[0], "evaluations": ms[1], "decisions_accept": ms[2], "loop_wall": ms[3],
+                "rounds": n.value}
 
     def solver_loop(self):
         """(device loop in use, why not when it was switched off)."""

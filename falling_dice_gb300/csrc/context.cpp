@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -218,7 +219,7 @@ struct mcg_ctx {
     void set_active(const std::vector<uint8_t>& a) {
         if (a == active) return;
         bool joined = false;
-        for (int i = 0; i < I; i++) joined |= a[size_t(i)] && !active[size_t(i)];
+        for (int i = 0; i < I; i++) joined |= a[size_t(i)] && active[size_t(i)] != 1;  // 2: unknown
         active = a;
         h2d(d_active, active.data(), size_t(I), stream);
         if (joined) ck(cudaMemsetAsync(cb.flags + 2, 1, 1, stream), "memset");
@@ -243,6 +244,11 @@ struct mcg_ctx {
     bool device_loop = true;
     std::string loop_error;
     static constexpr int kLoopRoundCap = 4096;
+    // the loop's device time by stage (ns; minimize_dev.cu), its rounds, and the host's wall
+    // time from each loop launch to the synchronisation that ends it
+    unsigned long long loop_ns[3] = {0, 0, 0};
+    long long loop_rounds = 0;
+    double loop_wall_ms = 0;
 
     // optional per-phase timing of evaluations (events on the context stream)
     // state, beams, contact grid (up to the pair enumeration), pair enumeration (k_bin_pairs),
@@ -787,6 +793,7 @@ struct mcg_ctx {
             std::copy(mins.begin(), mins.end(), hp.mins);
             h2d(d_mins, hp.mins, size_t(I), stream);
             launch_mz_reset(mz_dev(), stream);
+            const auto w0 = std::chrono::steady_clock::now();
             ck(cudaGraphLaunch(loop_exec, stream), "cudaGraphLaunch (loop)");
             d2h(hp.mins, d_mins, size_t(I), stream);
             d2h(hp.mz, d_mz, 1, stream);
@@ -794,15 +801,25 @@ struct mcg_ctx {
             if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
             sync();
             check_launch();
+            loop_wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+            loop_ns[0] += hp.mz->t_dir;
+            loop_ns[1] += hp.mz->t_eval;
+            loop_ns[2] += hp.mz->t_post;
+            loop_rounds += hp.mz->rounds;
             note_launches(int(hp.mz->rounds) * int(loop_kernels_per_round()));
             std::copy(hp.mins, hp.mins + I, mins.begin());
             active.assign(size_t(I), 2);  // the loop wrote d_active: the host mirror is unknown
             last_z = d_zeval;
             last_trials = false;
             last_grad = d_geval;
-            if (!hp.mz->overflow) break;
-            if (tries >= 16 || !grow_contacts(hp.outs[0].overflow))
-                throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
+            if (hp.mz->overflow) {
+                if (tries >= 16 || !grow_contacts(hp.outs[0].overflow))
+                    throw Fail(MCG_ERR_CAPACITY, "contact buffers could not be sized");
+                continue;
+            }
+            if (hp.mz->rounds <= 0)  // the body did not run: never loop on the host for it
+                throw Fail(MCG_ERR_CUDA, "the device-resident round loop ran no round");
+            break;
         }
         if (cfg.self_contact) last_contacts = hp.u32[0];
         contacts_stale = false;
@@ -1951,7 +1968,19 @@ int mcg_set_solver_loop(mcg_ctx* c, int device) {
         c->sync();
         c->device_loop = device != 0;
         c->loop_error.clear();
+        for (auto& v : c->loop_ns) v = 0;
+        c->loop_rounds = 0;
+        c->loop_wall_ms = 0;
         c->drop_graphs();
+    });
+}
+
+int mcg_solver_times(mcg_ctx* c, double* ms4, int64_t* rounds) {
+    return guarded(c, [&] {
+        if (!ms4) throw Fail(MCG_ERR_INVALID, "null output");
+        for (int k = 0; k < 3; k++) ms4[k] = double(c->loop_ns[k]) * 1e-6;
+        ms4[3] = c->loop_wall_ms;
+        if (rounds) *rounds = c->loop_rounds;
     });
 }
 

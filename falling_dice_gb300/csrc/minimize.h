@@ -196,6 +196,10 @@ struct MzStatus {
     int overflow;   // the last evaluation overflowed a contact buffer (nothing was decided)
     int done;       // an instance finished its minimization
     int pad_;
+    // device time of the launch's rounds by stage (global timer, ns): directions (stage A
+    // to B), evaluations (B to C, with the vector preparation), decisions and accept steps
+    // (C to the next round's A); t_last is the last stage boundary
+    unsigned long long t_dir, t_eval, t_post, t_last;
 };
 struct MzDev {
     int I;

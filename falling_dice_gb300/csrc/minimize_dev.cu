@@ -17,6 +17,18 @@ namespace {
 
 constexpr int kMzThreads = 256;  // one block walks all instances
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Adds the time since the last stage boundary to *acc and moves the boundary (thread 0).
+__device__ __forceinline__ void stage_mark(MzStatus* st, unsigned long long* acc) {
+    const unsigned long long t = global_ns();
+    if (st->t_last && acc) *acc += t - st->t_last;
+    st->t_last = t;
+}
+
 __global__ void __launch_bounds__(kMzThreads) k_mz_direction(MzDev d, cudaGraphConditionalHandle h_fused,
                                                              cudaGraphConditionalHandle h_multi,
                                                              cudaGraphConditionalHandle h_dir,
@@ -35,6 +47,7 @@ __global__ void __launch_bounds__(kMzThreads) k_mz_direction(MzDev d, cudaGraphC
     multi = __syncthreads_or(multi);
     sd = __syncthreads_or(sd);
     if (threadIdx.x == 0) {
+        stage_mark(d.status, &d.status->t_post);
         cudaGraphSetConditional(h_fused, fused ? 1u : 0u);
         cudaGraphSetConditional(h_multi, multi ? 1u : 0u);
         cudaGraphSetConditional(h_dir, (fused | multi) ? 1u : 0u);
@@ -57,7 +70,10 @@ __global__ void __launch_bounds__(kMzThreads) k_mz_eval(MzDev d) {
         if (a) d.tops[i] = s.top;
     }
     joined = __syncthreads_or(joined);
-    if (threadIdx.x == 0 && joined && d.contact_flags) d.contact_flags[2] = 1u;
+    if (threadIdx.x == 0) {
+        stage_mark(d.status, &d.status->t_dir);
+        if (joined && d.contact_flags) d.contact_flags[2] = 1u;
+    }
 }
 
 __global__ void __launch_bounds__(kMzThreads) k_mz_decide(MzDev d, MzParams p, cudaGraphConditionalHandle h_post,
@@ -65,6 +81,7 @@ __global__ void __launch_bounds__(kMzThreads) k_mz_decide(MzDev d, MzParams p, c
     // an evaluation that overflowed a contact buffer decided nothing: the host grows the
     // buffers and the next launch repeats the round's evaluation (stages A and B leave the
     // minimizers ready for it)
+    if (threadIdx.x == 0) stage_mark(d.status, &d.status->t_eval);
     if (d.out[0].overflow) {
         if (threadIdx.x == 0) {
             d.status->overflow = 1;
@@ -95,7 +112,7 @@ __global__ void __launch_bounds__(kMzThreads) k_mz_decide(MzDev d, MzParams p, c
 }
 
 __global__ void k_mz_reset(MzStatus* st) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *st = MzStatus{0, 0, 0, 0};
+    if (threadIdx.x == 0 && blockIdx.x == 0) *st = MzStatus{0, 0, 0, 0, 0, 0, 0, 0};
 }
 
 }  // namespace

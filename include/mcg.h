@@ -345,6 +345,12 @@ int mcg_set_kernel_shapes(mcg_ctx* ctx, int32_t beam_blocks, int32_t gather_bloc
  * could not be built it is switched off, and mcg_last_error then says why. */
 int mcg_set_solver_loop(mcg_ctx* ctx, int device);
 int mcg_solver_loop(mcg_ctx* ctx, int32_t* device);
+/* Time of the device-resident loop's rounds since the upload or the last
+ * mcg_set_solver_loop (no reference counterpart): ms4 = {directions, evaluations (with the
+ * vectors they read), decisions and accept steps} as device time between the rounds' stage
+ * kernels, and ms4[3] the host's wall time from each loop launch to its synchronisation;
+ * *rounds the rounds run. */
+int mcg_solver_times(mcg_ctx* ctx, double* ms4, int64_t* rounds);
 
 /* Candidate-list builds of the self-contact broad phase since the lattice was uploaded
  * (no reference counterpart): every evaluation checks whether a node moved farther than the
