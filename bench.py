@@ -451,8 +451,12 @@ def run_summary(frames):
 
 def load_unload(fd, abi, workloads):
     """The 32x32x16 cubic+BCC specimen, 60 % strain in 400 + 400 increments, mixed against
-    FP64: wall time of the whole run (minimize, commit, diagnostics on the device; host
-    decisions per round) and the run-level figures, with their errors against FP64."""
+    FP64: wall time of the whole run (minimize rounds in the device-resident graph loop,
+    commit and diagnostics on the device, the increment logic on the host) and the run-level
+    figures, with their errors against FP64.  "split_ms" divides the run: device time of the
+    loop's directions, evaluations and decisions/accept steps (global-timer stamps between
+    the rounds' stage kernels), and the rest of the wall time (loop launches, commits,
+    diagnostics, host increment logic)."""
     out = {}
     frames_of = {}
     for name, prec in (("mixed", abi.MCG_MIXED), ("fp64", abi.MCG_FP64)):
@@ -463,9 +467,17 @@ def load_unload(fd, abi, workloads):
         t0 = time.perf_counter()
         rc, frames = sol.run()
         dt = time.perf_counter() - t0
+        lt = sol.solver_times()
+        loop_on, why = sol.solver_loop()
+        builds = sol.contact_builds()
         sol.close()
         frames_of[name] = frames
-        out[name] = dict(run_summary(frames), seconds=dt, status=int(rc))
+        dev = lt["directions"] + lt["evaluations"] + lt["decisions_accept"]
+        out[name] = dict(run_summary(frames), seconds=dt, status=int(rc),
+                         iterations=int(sum(f["iterations"] for f in frames)), rounds=int(lt["rounds"]),
+                         contact_list_builds=int(builds), device_loop=bool(loop_on), device_loop_error=why,
+                         split_ms={"directions": lt["directions"], "evaluations": lt["evaluations"],
+                                   "decisions_accept": lt["decisions_accept"], "rest": 1e3 * dt - dev})
     m, f = out["mixed"], out["fp64"]
     out["speedup_mixed_over_fp64"] = f["seconds"] / m["seconds"]
     out["rel_err_mixed_vs_fp64"] = {k: abs(m[k] - f[k]) / abs(f[k]) for k in

@@ -318,9 +318,17 @@ int fused_direction_limit();
 // multi, the kOpDirection instances; then p = clamp(lock(-p)) and dg[i] = <g, p>; where
 // not dg < 0, steepest descent with the history cleared (sim.cpp:191).
 // History: H slots of `stride` doubles, state hist[I], rho and alpha [I * H].
+// State of the grid barrier of the one-launch two-loop (zeroed once; err: a wait gave up).
+struct GridBarrier {
+    unsigned count, gen;
+    int err, pad_;
+};
+// Blocks the one-launch two-loop may use on `device` (all resident at once; 0: cooperative
+// launches unavailable, the multi-block two-loop then runs as 2 H + 4 launches).
+int two_loop_coop_blocks(int device);
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s);
+                  double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar = nullptr, int coop_blocks = 0);
 // The pieces of bl_direction, for callers that launch them under separate conditions: the
 // one-CTA directions (kOpDirFused), the multi-block two-loop (kOpDirection), and the
 // steepest-descent fallback of either kind where <g, p> >= 0.
@@ -329,7 +337,8 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
                         double mr, cudaStream_t s);
 void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
                         const double* S, const double* Y, long long stride, const double* rho, double* alpha,
-                        double* part, double* dg, double mt, double mr, cudaStream_t s);
+                        double* part, double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar = nullptr,
+                        int coop_blocks = 0);
 void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
                     double* dg, double mt, double mr, cudaStream_t s);
 // The steepest-descent retry for the kOpSteepest instances: history cleared,

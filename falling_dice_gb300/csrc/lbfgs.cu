@@ -11,6 +11,8 @@
 // summing its blocks in order: the same partition whether an instance is solved alone or
 // with others, so a batch reproduces the separate runs bit for bit.  The two-loop scalars
 // (alpha_h, H0) never leave the device.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -37,7 +39,9 @@ __device__ __forceinline__ SolveCtl load_ctl(const SolveCtl* __restrict__ ctl, c
 
 // One instance's sum of its block partials part[k * nblk + b], b in its node-block range,
 // for k < K (one block per instance; fixed order).
-template <int K>
+// kL2: the partials were written by other blocks of the same launch (the cooperative
+// two-loop): read them from L2, past this SM's L1.
+template <int K, bool kL2 = false>
 __device__ __forceinline__ void instance_sum(const DevTopo& t, const double* __restrict__ part, int inst,
                                              double (&acc)[K], double* sm) {
     const int4 r = t.irange[inst];
@@ -45,8 +49,17 @@ __device__ __forceinline__ void instance_sum(const DevTopo& t, const double* __r
     for (int k = 0; k < K; k++) acc[k] = 0;
     for (int b = r.x + int(threadIdx.x); b < r.y; b += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < K; k++) acc[k] += part[size_t(k) * t.n_nblk + b];
+        for (int k = 0; k < K; k++) {
+            const double* q = part + size_t(k) * t.n_nblk + b;
+            acc[k] += kL2 ? __ldcg(q) : *q;
+        }
     block_sum<K>(acc, sm);
+}
+
+// The node block vb of the node-block map as (node, instance, valid) for this thread.
+__device__ __forceinline__ MapPos map_pos_at(const int4* __restrict__ blk, int vb) {
+    const int4 q = blk[vb];
+    return MapPos{q.x + int(threadIdx.x), q.z, int(threadIdx.x) < q.y};
 }
 
 __device__ __forceinline__ double dot6(const double* a, const double* b) {
@@ -66,29 +79,28 @@ __device__ __forceinline__ double dot6(const double* a, const double* b) {
 // its partial of step j + 1's dot product with the updated p to `nxt`.
 //   loop 1 (newest first, h = m - 1 - j): alpha = rho <s, p> (kept), p -= alpha y;
 //   loop 2 (oldest first, h = j):         beta = rho <y, p>, p += s (alpha - beta).
-template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* __restrict__ ctl,
-                                                    const int2* __restrict__ hist, int H, int j,
-                                                    double* __restrict__ p, const double* __restrict__ S,
-                                                    const double* __restrict__ Y, long long stride,
-                                                    const double* __restrict__ rho, double* __restrict__ alpha,
-                                                    const double* __restrict__ cur, double* __restrict__ nxt) {
-    __shared__ double sm[kBlock / 32];
-    __shared__ double coef;
-    const MapPos mp = map_pos(t.nblk);
+template <int LOOP, bool kL2>
+__device__ __forceinline__ void tl_step(const DevTopo& t, const SolveCtl* __restrict__ ctl,
+                                        const int2* __restrict__ hist, int H, int j, double* __restrict__ p,
+                                        const double* __restrict__ S, const double* __restrict__ Y,
+                                        long long stride, const double* __restrict__ rho,
+                                        double* __restrict__ alpha, const double* __restrict__ cur,
+                                        double* __restrict__ nxt, int vb, double* sm, double& coef) {
+    const MapPos mp = map_pos_at(t.nblk, vb);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
     const int h = LOOP == 1 ? c.m - 1 - j : j;
     const int slot = ring_slot(c, H, h);
     double acc[1];
-    instance_sum<1>(t, cur, mp.inst, acc, sm);
+    instance_sum<1, kL2>(t, cur, mp.inst, acc, sm);
     if (threadIdx.x == 0) {
         const double r = rho[size_t(mp.inst) * H + slot] * acc[0];
         if (LOOP == 1) {
             coef = r;
-            if (blockIdx.x == t.irange[mp.inst].x) alpha[size_t(mp.inst) * H + h] = r;
+            if (vb == t.irange[mp.inst].x) alpha[size_t(mp.inst) * H + h] = r;
         } else {
-            coef = alpha[size_t(mp.inst) * H + h] - r;
+            const double* ah = alpha + size_t(mp.inst) * H + h;
+            coef = (kL2 ? __ldcg(ah) : *ah) - r;
         }
     }
     __syncthreads();
@@ -114,19 +126,31 @@ __global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* _
     double a2[1] = {0};
     if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
     block_sum<1>(a2, sm);
-    if (threadIdx.x == 0) nxt[blockIdx.x] = a2[0];
+    if (threadIdx.x == 0) nxt[vb] = a2[0];
+}
+
+template <int LOOP>
+__global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                    const int2* __restrict__ hist, int H, int j,
+                                                    double* __restrict__ p, const double* __restrict__ S,
+                                                    const double* __restrict__ Y, long long stride,
+                                                    const double* __restrict__ rho, double* __restrict__ alpha,
+                                                    const double* __restrict__ cur, double* __restrict__ nxt) {
+    __shared__ double sm[kBlock / 32];
+    __shared__ double coef;
+    tl_step<LOOP, false>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, cur, nxt, int(blockIdx.x), sm, coef);
 }
 
 // Partials of <s, y> and <y, y> of the newest pair (for H0, into h0part), the copy p = g
 // that starts the recursion and the partial of loop 1's first dot product <s, g> (into
 // part0).
-__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
-                                                     double* __restrict__ p, const double* __restrict__ g,
-                                                     const double* __restrict__ S, const double* __restrict__ Y,
-                                                     long long stride, double* __restrict__ h0part,
-                                                     double* __restrict__ part0) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    const MapPos mp = map_pos(t.nblk);
+__device__ __forceinline__ void tl_start(const DevTopo& t, const SolveCtl* __restrict__ ctl,
+                                         const int2* __restrict__ hist, int H, double* __restrict__ p,
+                                         const double* __restrict__ g, const double* __restrict__ S,
+                                         const double* __restrict__ Y, long long stride,
+                                         double* __restrict__ h0part, double* __restrict__ part0, int vb,
+                                         double* sm) {
+    const MapPos mp = map_pos_at(t.nblk, vb);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (mp.valid)
@@ -144,26 +168,35 @@ __global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* 
     }
     block_sum<3>(acc, sm);
     if (threadIdx.x == 0) {
-        h0part[blockIdx.x] = acc[0];
-        h0part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
-        part0[blockIdx.x] = acc[2];
+        h0part[vb] = acc[0];
+        h0part[size_t(t.n_nblk) + vb] = acc[1];
+        part0[vb] = acc[2];
     }
+}
+
+__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
+                                                     double* __restrict__ p, const double* __restrict__ g,
+                                                     const double* __restrict__ S, const double* __restrict__ Y,
+                                                     long long stride, double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    tl_start(t, ctl, hist, H, p, g, S, Y, stride, h0part, part0, int(blockIdx.x), sm);
 }
 
 // p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186), and
 // the partial of loop 2's first dot product <y, p> (into part0).
-__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
-                                                     int H, double* __restrict__ p, const double* __restrict__ Y,
-                                                     long long stride, const double* __restrict__ h0part,
-                                                     double* __restrict__ part0) {
-    __shared__ double sm[2 * (kBlock / 32)];
-    __shared__ double h0;
-    const MapPos mp = map_pos(t.nblk);
+template <bool kL2>
+__device__ __forceinline__ void tl_scale(const DevTopo& t, const SolveCtl* __restrict__ ctl,
+                                         const int2* __restrict__ hist, int H, double* __restrict__ p,
+                                         const double* __restrict__ Y, long long stride,
+                                         const double* __restrict__ h0part, double* __restrict__ part0, int vb,
+                                         double* sm, double& h0) {
+    const MapPos mp = map_pos_at(t.nblk, vb);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (c.m > 0) {
         double acc[2];
-        instance_sum<2>(t, h0part, mp.inst, acc, sm);
+        instance_sum<2, kL2>(t, h0part, mp.inst, acc, sm);
         if (threadIdx.x == 0) {
             double v = .10;
             if (acc[0] > 1e-20 && acc[1] > 1e-20) v = clampd(acc[0] / acc[1], 1e-7, 1e4);
@@ -186,17 +219,25 @@ __global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* 
     double a2[1] = {0};
     if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
     block_sum<1>(a2, sm);
-    if (threadIdx.x == 0) part0[blockIdx.x] = a2[0];
+    if (threadIdx.x == 0) part0[vb] = a2[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
+                                                     int H, double* __restrict__ p, const double* __restrict__ Y,
+                                                     long long stride, const double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
+    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ double h0;
+    tl_scale<false>(t, ctl, hist, H, p, Y, stride, h0part, part0, int(blockIdx.x), sm, h0);
 }
 
 // Direction finish for the instances with `bit` set: p = clamp(lock(-src)) per node
 // (sim.cpp:188-190, clampDirection sim.cpp:46), and the partial of <g, p>.
-__global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
-                                                   double* __restrict__ p, const double* __restrict__ src,
-                                                   const double* __restrict__ g, double mt, double mr,
-                                                   double* __restrict__ part) {
-    __shared__ double sm[kBlock / 32];
-    const MapPos mp = map_pos(t.nblk);
+__device__ __forceinline__ void dir_finish(const DevTopo& t, const SolveCtl* __restrict__ ctl, int bit,
+                                           double* __restrict__ p, const double* __restrict__ src,
+                                           const double* __restrict__ g, double mt, double mr,
+                                           double* __restrict__ part, int vb, double* sm) {
+    const MapPos mp = map_pos_at(t.nblk, vb);
     if (!(ctl[mp.inst].flags & bit)) return;
     double acc[1] = {0};
     if (mp.valid) {
@@ -226,7 +267,15 @@ __global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __
         acc[0] = dot6(g + b, v);
     }
     block_sum<1>(acc, sm);
-    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
+    if (threadIdx.x == 0) part[vb] = acc[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
+                                                   double* __restrict__ p, const double* __restrict__ src,
+                                                   const double* __restrict__ g, double mt, double mr,
+                                                   double* __restrict__ part) {
+    __shared__ double sm[kBlock / 32];
+    dir_finish(t, ctl, bit, p, src, g, mt, mr, part, int(blockIdx.x), sm);
 }
 
 // One block per instance with `bit` set: out[K i + k] = sum of its partials.
@@ -241,6 +290,79 @@ __global__ void __launch_bounds__(kBlock) k_inst_final(DevTopo t, const SolveCtl
     if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < K; k++) out[size_t(K) * inst + k] = acc[k];
+}
+
+// ---- the multi-block two-loop in one launch --------------------------------------------------
+// k_tl_start, H x k_tl_step<1>, k_tl_scale, H x k_tl_step<2>, k_finish and k_inst_final<1> as
+// one cooperative launch: its blocks, all resident at once, walk the node blocks (block b
+// takes node blocks b, b + grid, ...) through the same step functions, and meet at a grid
+// barrier where the separate launches had their boundaries.  Every node block's arithmetic
+// and every partial sum is the same, so the direction is bit for bit that of the separate
+// launches.  Partials and coefficients written by other blocks are read from L2.
+constexpr unsigned kBarrierSpin = 1u << 22;  // polls of a barrier wait (~0.3 s) before it gives up
+
+// Grid-wide barrier of a cooperative launch.  A wait that gives up (it cannot while all
+// blocks are resident) sets bar->err, which the host reports, and goes on.
+__device__ __forceinline__ void grid_barrier(GridBarrier* bar, unsigned nblocks) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = &bar->gen;
+        const unsigned g = *gen;
+        __threadfence();
+        if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            unsigned it = 0;
+            while (*gen == g) {
+                if (++it > kBarrierSpin) {
+                    atomicOr(&bar->err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBlock) k_two_loop_coop(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                          const int2* __restrict__ hist, int H, double* __restrict__ p,
+                                                          const double* __restrict__ g, const double* __restrict__ S,
+                                                          const double* __restrict__ Y, long long stride,
+                                                          const double* __restrict__ rho, double* __restrict__ alpha,
+                                                          double* __restrict__ part, double* __restrict__ dg,
+                                                          double mt, double mr, GridBarrier* bar) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    __shared__ double coef;
+    const int nb = t.n_nblk;
+    const int G = int(gridDim.x);
+    double* pp[2] = {part, part + size_t(nb)};
+    double* h0part = part + 2 * size_t(nb);
+    for (int vb = int(blockIdx.x); vb < nb; vb += G) tl_start(t, ctl, hist, H, p, g, S, Y, stride, h0part, pp[0], vb, sm);
+    for (int j = 0; j < H; j++) {
+        grid_barrier(bar, unsigned(G));
+        for (int vb = int(blockIdx.x); vb < nb; vb += G)
+            tl_step<1, true>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1], pp[(j + 1) & 1], vb, sm, coef);
+    }
+    grid_barrier(bar, unsigned(G));
+    for (int vb = int(blockIdx.x); vb < nb; vb += G) tl_scale<true>(t, ctl, hist, H, p, Y, stride, h0part, pp[0], vb, sm, coef);
+    for (int j = 0; j < H; j++) {
+        grid_barrier(bar, unsigned(G));
+        for (int vb = int(blockIdx.x); vb < nb; vb += G)
+            tl_step<2, true>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1], pp[(j + 1) & 1], vb, sm, coef);
+    }
+    grid_barrier(bar, unsigned(G));
+    for (int vb = int(blockIdx.x); vb < nb; vb += G) dir_finish(t, ctl, kOpDirection, p, p, g, mt, mr, part, vb, sm);
+    grid_barrier(bar, unsigned(G));
+    for (int inst = int(blockIdx.x); inst < t.I; inst += G) {
+        if (!(ctl[inst].flags & kOpDirection)) continue;  // block-uniform
+        double acc[1];
+        instance_sum<1, true>(t, part, inst, acc, sm);
+        if (threadIdx.x == 0) dg[inst] = acc[0];
+    }
 }
 
 // ---- vectors around an evaluation ------------------------------------------------------------
@@ -589,10 +711,34 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
     (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
 }
 
+int two_loop_coop_blocks(int device) {
+    int per_sm = 0, sms = 0, coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_two_loop_coop, kBlock, 0) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    return per_sm * sms;
+}
+
 void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
                         const double* S, const double* Y, long long stride, const double* rho, double* alpha,
-                        double* part, double* dg, double mt, double mr, cudaStream_t s) {
+                        double* part, double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar,
+                        int coop_blocks) {
     const int nb = t.n_nblk;
+    if (bar && coop_blocks > 0) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(unsigned(std::min(nb, coop_blocks)));
+        cfg.blockDim = dim3(kBlock);
+        cfg.stream = s;
+        cudaLaunchAttribute attr{};
+        attr.id = cudaLaunchAttributeCooperative;
+        attr.val.cooperative = 1;
+        cfg.attrs = &attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_two_loop_coop, t, ctl, const_cast<const int2*>(hist), H, p, g, S, Y, stride, rho,
+                           alpha, part, dg, mt, mr, bar);
+        note_launches(1);
+        return;
+    }
     // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
     double* pp[2] = {part, part + size_t(nb)};
     double* h0part = part + 2 * size_t(nb);
@@ -619,9 +765,9 @@ void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p
 
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s) {
+                  double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar, int coop_blocks) {
     bl_direction_fused(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s);
-    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s);
+    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s, bar, coop_blocks);
     bl_descent_fix(t, ctl, hist, p, g, part, dg, mt, mr, s);
 }
 
