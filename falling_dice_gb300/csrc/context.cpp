@@ -1564,7 +1564,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     h2d(c->d_fused, c->fused.data(), size_t(I), s);
     c->d_bar = Q.get<GridBarrier>(1);
     ck(cudaMemsetAsync(c->d_bar, 0, sizeof(GridBarrier), s), "memset");
-    c->coop_blocks = two_loop_coop_blocks(c->device);
+    c->coop_blocks = two_loop_coop_blocks(c->device, s, reinterpret_cast<int*>(&c->d_bar->pad_));
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
         launch_mixed_constants(c->topo, c->mb, s);
@@ -2165,7 +2165,11 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
         ck(cudaEventCreate(&t0), "cudaEventCreate");
         ck(cudaEventCreate(&t1), "cudaEventCreate");
         c->contact_skin = 0.f;
-        auto time_variant = [&](int bv, int gv) {
+        // each variant is timed on its own kernel (the evaluation's phase events): its share
+        // of a whole evaluation is small enough to drown in the other kernels' variation
+        if (!c->ev_t[0])
+            for (auto& ev : c->ev_t) ck(cudaEventCreate(&ev), "cudaEventCreate");
+        auto time_variant = [&](int bv, int gv, int phase) {
             c->set_kernel_variants(bv, gv);
             const EvalOut* o = c->eval_read(c->d_zin, false, c->d_grad);
             for (int i = 0; i < c->I; i++) e[size_t(i)] = o[i].energy;
@@ -2174,6 +2178,37 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
             if (std::memcmp(e.data(), ref_e.data(), e.size() * sizeof(double)) != 0 ||
                 std::memcmp(g.data(), ref_g.data(), n * sizeof(double)) != 0)
                 throw Fail(MCG_ERR_MISMATCH, "a kernel occupancy variant changed an evaluation");
+            const bool timing_was = c->timing;
+            double saved[mcg_ctx::kPhases];
+            std::copy(c->phase_ms, c->phase_ms + mcg_ctx::kPhases, saved);
+            const long long saved_n = c->phase_n;
+            c->timing = true;
+            std::fill(c->phase_ms, c->phase_ms + mcg_ctx::kPhases, 0.0);
+            c->phase_n = 0;
+            const int runs = std::max(reps, 5);
+            for (int r = 0; r < runs; r++) c->eval(c->d_zin, false, c->d_grad);
+            c->read_outs();
+            const double ms = c->phase_ms[phase] / double(std::max(1LL, c->phase_n));
+            c->timing = timing_was;
+            std::copy(saved, saved + mcg_ctx::kPhases, c->phase_ms);
+            c->phase_n = saved_n;
+            tried++;
+            return ms;
+        };
+        try {
+            int bv = 0, gv = 0;
+            double best_beam = time_variant(0, 0, 1);  // phase 1: the beam kernel
+            for (int v = 1; v < shape_variants(beam_kernel); v++) {
+                const double ms = time_variant(v, gv, 1);
+                if (ms < 0.99 * best_beam) { best_beam = ms; bv = v; }
+            }
+            double best_gather = time_variant(bv, 0, 5);  // phase 5: the gather
+            for (int v = 1; v < shape_variants(ShapeKernel::kGather); v++) {
+                const double ms = time_variant(bv, v, 5);
+                if (ms < 0.99 * best_gather) { best_gather = ms; gv = v; }
+            }
+            c->set_kernel_variants(bv, gv);
+            // the whole evaluation with the chosen shapes
             c->eval(c->d_zin, false, c->d_grad);  // captures the graph
             ck(cudaEventRecord(t0, s), "cudaEventRecord");
             for (int r = 0; r < reps; r++) c->eval(c->d_zin, false, c->d_grad);
@@ -2181,21 +2216,7 @@ int mcg_autotune(mcg_ctx* c, const double* z, const double* tops, int32_t reps, 
             c->read_outs();
             float ms = 0;
             ck(cudaEventElapsedTime(&ms, t0, t1), "cudaEventElapsedTime");
-            tried++;
-            return double(ms) / reps;
-        };
-        try {
-            int bv = 0, gv = 0;
-            best_ms = time_variant(0, 0);
-            for (int v = 1; v < shape_variants(beam_kernel); v++) {
-                const double ms = time_variant(v, gv);
-                if (ms < 0.99 * best_ms) { best_ms = ms; bv = v; }
-            }
-            for (int v = 1; v < shape_variants(ShapeKernel::kGather); v++) {
-                const double ms = time_variant(bv, v);
-                if (ms < 0.99 * best_ms) { best_ms = ms; gv = v; }
-            }
-            c->set_kernel_variants(bv, gv);
+            best_ms = double(ms) / reps;
         } catch (...) {
             cudaEventDestroy(t0);
             cudaEventDestroy(t1);

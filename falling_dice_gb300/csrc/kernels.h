@@ -324,8 +324,9 @@ struct GridBarrier {
     int err, pad_;
 };
 // Blocks the one-launch two-loop may use on `device` (all resident at once; 0: cooperative
-// launches unavailable, the multi-block two-loop then runs as 2 H + 4 launches).
-int two_loop_coop_blocks(int device);
+// launches, or their capture into graphs, unavailable: the multi-block two-loop then runs as
+// 2 H + 4 launches).  Checks the capture with one small launch on `s` (scratch: 1 int).
+int two_loop_coop_blocks(int device, cudaStream_t s, int* scratch);
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
                   double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar = nullptr, int coop_blocks = 0);

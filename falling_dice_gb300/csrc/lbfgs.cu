@@ -711,11 +711,43 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
     (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
 }
 
-int two_loop_coop_blocks(int device) {
+__global__ void k_coop_probe(int* out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = 1;
+}
+
+// Cooperative launches must also work inside captured graphs (every solver launch sequence
+// is captured): one is captured, instantiated and run on `s` before the path is used.
+bool coop_capture_works(cudaStream_t s, int* scratch) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(32);
+    cfg.stream = s;
+    cudaLaunchAttribute attr{};
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        const bool launched = cudaLaunchKernelEx(&cfg, k_coop_probe, scratch) == cudaSuccess;
+        ok = cudaStreamEndCapture(s, &g) == cudaSuccess && launched;
+    }
+    ok = ok && cudaGraphInstantiate(&x, g, 0) == cudaSuccess;
+    ok = ok && cudaGraphLaunch(x, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+    if (x) cudaGraphExecDestroy(x);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return ok;
+}
+
+int two_loop_coop_blocks(int device, cudaStream_t s, int* scratch) {
     int per_sm = 0, sms = 0, coop = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_two_loop_coop, kBlock, 0) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
+    if (!coop_capture_works(s, scratch)) return 0;
     return per_sm * sms;
 }
 

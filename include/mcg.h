@@ -317,7 +317,8 @@ int mcg_set_contact_shapes(mcg_ctx* ctx, double cell, int32_t pair_blocks);
  * platen heights `tops` (NULL: each lattice's top0), with the candidate list rebuilt at
  * every evaluation; the fastest by CUDA-event time is kept for the context (broad phase:
  * among candidates within 1 % of it, the one with the most pair blocks, then the smallest
- * cell; kernel occupancy: a variant must be 1 % faster than the one before to replace it).
+ * cell; kernel occupancy: timed on the kernel itself, a variant must be 1 % faster than the
+ * one before to replace it).
  * All candidates must agree bit for bit on energies and gradients (pair sets and sums do
  * not depend on the grid, nor arithmetic on register allocation); MCG_ERR_MISMATCH if one
  * does not. */
