@@ -264,7 +264,11 @@ def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world, sh
     if shapes:  # fixed shapes (a saved tuning), e.g. for a profiler run
         sol.set_contact_shapes(shapes[0], shapes[1])
         kb = shapes[2:4] if len(shapes) >= 4 else (0, 0)
-        sol.set_kernel_shapes(*kb)
+        try:
+            sol.set_kernel_shapes(*kb)
+        except fd.MCGError:  # the occupancy variants differ between the two forms
+            kb = (0, 0)
+            sol.set_kernel_shapes(*kb)
         tune = {"cell": shapes[0], "pair_blocks": shapes[1], "beam_blocks": kb[0], "gather_blocks": kb[1],
                 "tried": 0}
     else:

@@ -239,12 +239,12 @@ struct mcg_ctx {
     uint8_t* d_fused = nullptr;
     uint8_t* d_trial = nullptr;   // per-instance trial mask of the loop's evaluations
     MzStatus* d_mz = nullptr;
-    // the multi-block two-loop as one cooperative launch (lbfgs.cu): its grid barrier and
-    // the blocks it may use (0: the 2 H + 4 launches)
-    GridBarrier* d_bar = nullptr;
-    int coop_blocks = 0;
+    // the direction of multi-block instances in one launch, one thread-block cluster each
+    // (lbfgs.cu): CTAs per cluster, 0 for the 2 H + 4 launches (no clusters on the device,
+    // or an instance with more node blocks than a cluster holds)
+    int dir_cluster = 0;
     bool one_launch_direction = true;
-    int coop_for_launch() const { return one_launch_direction ? coop_blocks : 0; }
+    int cluster_for_launch() const { return one_launch_direction ? dir_cluster : 0; }
     cudaGraphExec_t loop_exec = nullptr;
     cudaStream_t side = nullptr;  // captures the bodies of the loop's conditional nodes
     bool device_loop = true;
@@ -626,7 +626,7 @@ struct mcg_ctx {
             replay(1 | (any_dir ? 2 : 0) | (any_multi ? 4 : 0) | (any_sd ? 8 : 0), [&] {
                 if (any_dir)
                     bl_direction(topo, d_ctl, d_hist, std::max(H, 1), any_multi, d_p, d_g, d_S, d_Y, 6LL * N, d_rho,
-                                 d_alpha, d_part, d_dg, mt, mr, stream, d_bar, coop_for_launch());
+                                 d_alpha, d_part, d_dg, mt, mr, stream, cluster_for_launch());
                 if (any_sd) bl_steepest(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, stream);
             });
         }
@@ -654,9 +654,7 @@ struct mcg_ctx {
         upload_tops();
         replay(16, [&] { bl_prepare(topo, d_ctl, d_hist, d_z, d_best, d_zeval, d_p, d_zfinal, stream); });
         d2h(hp.dg, d_dg, size_t(I), stream);  // read back with the evaluation's totals
-        d2h(hp.u32 + 6, reinterpret_cast<const uint32_t*>(&d_bar->err), 1, stream);
         const EvalOut* out = eval_read(d_zeval, trials, d_geval);
-        check_barrier();
         // C. decisions (the reference's, per instance) and the vectors they imply
         clear_ctl(2);
         SolveCtl* cc = ctl_stage(2);
@@ -756,7 +754,7 @@ struct mcg_ctx {
                 });
                 capture_if(hm, [&](cudaStream_t s2) {
                     bl_direction_multi(topo, d_ctl, d_hist, Hs, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_alpha, d_part,
-                                       d_dg, mt, mr, s2, d_bar, coop_for_launch());
+                                       d_dg, mt, mr, s2, cluster_for_launch());
                 });
                 capture_if(hd, [&](cudaStream_t s2) {
                     bl_descent_fix(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, s2);
@@ -807,10 +805,8 @@ struct mcg_ctx {
             d2h(hp.mz, d_mz, 1, stream);
             d2h(hp.outs, ev.out, size_t(I), stream);
             if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
-            d2h(hp.u32 + 6, reinterpret_cast<const uint32_t*>(&d_bar->err), 1, stream);
             sync();
             check_launch();
-            check_barrier();
             loop_wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             loop_ns[0] += hp.mz->t_dir;
             loop_ns[1] += hp.mz->t_eval;
@@ -834,18 +830,6 @@ struct mcg_ctx {
         if (cfg.self_contact) last_contacts = hp.u32[0];
         contacts_stale = false;
         return true;
-    }
-    // A grid-barrier wait of the one-launch two-loop that gave up (hp.u32[6], read with the
-    // round's totals) leaves its direction invalid: an error, and the two-loop goes back to
-    // separate launches.
-    void check_barrier() {
-        if (!hp.u32[6]) return;
-        hp.u32[6] = 0;
-        ck(cudaMemsetAsync(d_bar, 0, sizeof(GridBarrier), stream), "memset");
-        sync();
-        coop_blocks = 0;
-        drop_graphs();
-        throw Fail(MCG_ERR_CUDA, "a grid-barrier wait of the one-launch two-loop gave up");
     }
     // Kernels one loop round launches (the device counts no launches; this estimate keeps
     // the library's launch counter meaningful): stage kernels plus the evaluation's.
@@ -1562,9 +1546,13 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->d_mz = Q.get<MzStatus>(1);
     c->d_fused = Q.get<uint8_t>(size_t(I));
     h2d(c->d_fused, c->fused.data(), size_t(I), s);
-    c->d_bar = Q.get<GridBarrier>(1);
-    ck(cudaMemsetAsync(c->d_bar, 0, sizeof(GridBarrier), s), "memset");
-    c->coop_blocks = two_loop_coop_blocks(c->device, s, reinterpret_cast<int*>(&c->d_bar->pad_));
+    {
+        int widest = 0;  // node blocks of the largest instance the one-CTA direction does not take
+        for (int k = 0; k < I; k++)
+            if (!c->fused[size_t(k)]) widest = std::max(widest, irange[size_t(k)].y - irange[size_t(k)].x);
+        const int C = widest > 0 ? direction_cluster_size(c->device, s) : 0;
+        c->dir_cluster = C > 0 && widest <= C * kDirClusterChunks && c->H <= 64 ? C : 0;
+    }
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
         launch_mixed_constants(c->topo, c->mb, s);

@@ -11,7 +11,7 @@
 // summing its blocks in order: the same partition whether an instance is solved alone or
 // with others, so a batch reproduces the separate runs bit for bit.  The two-loop scalars
 // (alpha_h, H0) never leave the device.
-#include <algorithm>
+#include <cooperative_groups.h>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -39,9 +39,7 @@ __device__ __forceinline__ SolveCtl load_ctl(const SolveCtl* __restrict__ ctl, c
 
 // One instance's sum of its block partials part[k * nblk + b], b in its node-block range,
 // for k < K (one block per instance; fixed order).
-// kL2: the partials were written by other blocks of the same launch (the cooperative
-// two-loop): read them from L2, past this SM's L1.
-template <int K, bool kL2 = false>
+template <int K>
 __device__ __forceinline__ void instance_sum(const DevTopo& t, const double* __restrict__ part, int inst,
                                              double (&acc)[K], double* sm) {
     const int4 r = t.irange[inst];
@@ -49,17 +47,8 @@ __device__ __forceinline__ void instance_sum(const DevTopo& t, const double* __r
     for (int k = 0; k < K; k++) acc[k] = 0;
     for (int b = r.x + int(threadIdx.x); b < r.y; b += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < K; k++) {
-            const double* q = part + size_t(k) * t.n_nblk + b;
-            acc[k] += kL2 ? __ldcg(q) : *q;
-        }
+        for (int k = 0; k < K; k++) acc[k] += part[size_t(k) * t.n_nblk + b];
     block_sum<K>(acc, sm);
-}
-
-// The node block vb of the node-block map as (node, instance, valid) for this thread.
-__device__ __forceinline__ MapPos map_pos_at(const int4* __restrict__ blk, int vb) {
-    const int4 q = blk[vb];
-    return MapPos{q.x + int(threadIdx.x), q.z, int(threadIdx.x) < q.y};
 }
 
 __device__ __forceinline__ double dot6(const double* a, const double* b) {
@@ -79,28 +68,29 @@ __device__ __forceinline__ double dot6(const double* a, const double* b) {
 // its partial of step j + 1's dot product with the updated p to `nxt`.
 //   loop 1 (newest first, h = m - 1 - j): alpha = rho <s, p> (kept), p -= alpha y;
 //   loop 2 (oldest first, h = j):         beta = rho <y, p>, p += s (alpha - beta).
-template <int LOOP, bool kL2>
-__device__ __forceinline__ void tl_step(const DevTopo& t, const SolveCtl* __restrict__ ctl,
-                                        const int2* __restrict__ hist, int H, int j, double* __restrict__ p,
-                                        const double* __restrict__ S, const double* __restrict__ Y,
-                                        long long stride, const double* __restrict__ rho,
-                                        double* __restrict__ alpha, const double* __restrict__ cur,
-                                        double* __restrict__ nxt, int vb, double* sm, double& coef) {
-    const MapPos mp = map_pos_at(t.nblk, vb);
+template <int LOOP>
+__global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                    const int2* __restrict__ hist, int H, int j,
+                                                    double* __restrict__ p, const double* __restrict__ S,
+                                                    const double* __restrict__ Y, long long stride,
+                                                    const double* __restrict__ rho, double* __restrict__ alpha,
+                                                    const double* __restrict__ cur, double* __restrict__ nxt) {
+    __shared__ double sm[kBlock / 32];
+    __shared__ double coef;
+    const MapPos mp = map_pos(t.nblk);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection) || j >= c.m) return;  // block-uniform
     const int h = LOOP == 1 ? c.m - 1 - j : j;
     const int slot = ring_slot(c, H, h);
     double acc[1];
-    instance_sum<1, kL2>(t, cur, mp.inst, acc, sm);
+    instance_sum<1>(t, cur, mp.inst, acc, sm);
     if (threadIdx.x == 0) {
         const double r = rho[size_t(mp.inst) * H + slot] * acc[0];
         if (LOOP == 1) {
             coef = r;
-            if (vb == t.irange[mp.inst].x) alpha[size_t(mp.inst) * H + h] = r;
+            if (blockIdx.x == t.irange[mp.inst].x) alpha[size_t(mp.inst) * H + h] = r;
         } else {
-            const double* ah = alpha + size_t(mp.inst) * H + h;
-            coef = (kL2 ? __ldcg(ah) : *ah) - r;
+            coef = alpha[size_t(mp.inst) * H + h] - r;
         }
     }
     __syncthreads();
@@ -126,31 +116,19 @@ __device__ __forceinline__ void tl_step(const DevTopo& t, const SolveCtl* __rest
     double a2[1] = {0};
     if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
     block_sum<1>(a2, sm);
-    if (threadIdx.x == 0) nxt[vb] = a2[0];
-}
-
-template <int LOOP>
-__global__ void __launch_bounds__(kBlock) k_tl_step(DevTopo t, const SolveCtl* __restrict__ ctl,
-                                                    const int2* __restrict__ hist, int H, int j,
-                                                    double* __restrict__ p, const double* __restrict__ S,
-                                                    const double* __restrict__ Y, long long stride,
-                                                    const double* __restrict__ rho, double* __restrict__ alpha,
-                                                    const double* __restrict__ cur, double* __restrict__ nxt) {
-    __shared__ double sm[kBlock / 32];
-    __shared__ double coef;
-    tl_step<LOOP, false>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, cur, nxt, int(blockIdx.x), sm, coef);
+    if (threadIdx.x == 0) nxt[blockIdx.x] = a2[0];
 }
 
 // Partials of <s, y> and <y, y> of the newest pair (for H0, into h0part), the copy p = g
 // that starts the recursion and the partial of loop 1's first dot product <s, g> (into
 // part0).
-__device__ __forceinline__ void tl_start(const DevTopo& t, const SolveCtl* __restrict__ ctl,
-                                         const int2* __restrict__ hist, int H, double* __restrict__ p,
-                                         const double* __restrict__ g, const double* __restrict__ S,
-                                         const double* __restrict__ Y, long long stride,
-                                         double* __restrict__ h0part, double* __restrict__ part0, int vb,
-                                         double* sm) {
-    const MapPos mp = map_pos_at(t.nblk, vb);
+__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
+                                                     double* __restrict__ p, const double* __restrict__ g,
+                                                     const double* __restrict__ S, const double* __restrict__ Y,
+                                                     long long stride, double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
+    __shared__ double sm[3 * (kBlock / 32)];
+    const MapPos mp = map_pos(t.nblk);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (mp.valid)
@@ -168,35 +146,26 @@ __device__ __forceinline__ void tl_start(const DevTopo& t, const SolveCtl* __res
     }
     block_sum<3>(acc, sm);
     if (threadIdx.x == 0) {
-        h0part[vb] = acc[0];
-        h0part[size_t(t.n_nblk) + vb] = acc[1];
-        part0[vb] = acc[2];
+        h0part[blockIdx.x] = acc[0];
+        h0part[size_t(t.n_nblk) + blockIdx.x] = acc[1];
+        part0[blockIdx.x] = acc[2];
     }
-}
-
-__global__ void __launch_bounds__(kBlock) k_tl_start(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist, int H,
-                                                     double* __restrict__ p, const double* __restrict__ g,
-                                                     const double* __restrict__ S, const double* __restrict__ Y,
-                                                     long long stride, double* __restrict__ h0part,
-                                                     double* __restrict__ part0) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    tl_start(t, ctl, hist, H, p, g, S, Y, stride, h0part, part0, int(blockIdx.x), sm);
 }
 
 // p *= H0, H0 = clamp(sy/yy, 1e-7, 1e4) when both are positive, else 0.1 (sim.cpp:186), and
 // the partial of loop 2's first dot product <y, p> (into part0).
-template <bool kL2>
-__device__ __forceinline__ void tl_scale(const DevTopo& t, const SolveCtl* __restrict__ ctl,
-                                         const int2* __restrict__ hist, int H, double* __restrict__ p,
-                                         const double* __restrict__ Y, long long stride,
-                                         const double* __restrict__ h0part, double* __restrict__ part0, int vb,
-                                         double* sm, double& h0) {
-    const MapPos mp = map_pos_at(t.nblk, vb);
+__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
+                                                     int H, double* __restrict__ p, const double* __restrict__ Y,
+                                                     long long stride, const double* __restrict__ h0part,
+                                                     double* __restrict__ part0) {
+    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ double h0;
+    const MapPos mp = map_pos(t.nblk);
     const SolveCtl c = load_ctl(ctl, hist, mp.inst);
     if (!(c.flags & kOpDirection)) return;
     if (c.m > 0) {
         double acc[2];
-        instance_sum<2, kL2>(t, h0part, mp.inst, acc, sm);
+        instance_sum<2>(t, h0part, mp.inst, acc, sm);
         if (threadIdx.x == 0) {
             double v = .10;
             if (acc[0] > 1e-20 && acc[1] > 1e-20) v = clampd(acc[0] / acc[1], 1e-7, 1e4);
@@ -219,25 +188,17 @@ __device__ __forceinline__ void tl_scale(const DevTopo& t, const SolveCtl* __res
     double a2[1] = {0};
     if (mp.valid) a2[0] = dot6(v + 6 * size_t(mp.i), pn);
     block_sum<1>(a2, sm);
-    if (threadIdx.x == 0) part0[vb] = a2[0];
-}
-
-__global__ void __launch_bounds__(kBlock) k_tl_scale(DevTopo t, const SolveCtl* __restrict__ ctl, const int2* __restrict__ hist,
-                                                     int H, double* __restrict__ p, const double* __restrict__ Y,
-                                                     long long stride, const double* __restrict__ h0part,
-                                                     double* __restrict__ part0) {
-    __shared__ double sm[2 * (kBlock / 32)];
-    __shared__ double h0;
-    tl_scale<false>(t, ctl, hist, H, p, Y, stride, h0part, part0, int(blockIdx.x), sm, h0);
+    if (threadIdx.x == 0) part0[blockIdx.x] = a2[0];
 }
 
 // Direction finish for the instances with `bit` set: p = clamp(lock(-src)) per node
 // (sim.cpp:188-190, clampDirection sim.cpp:46), and the partial of <g, p>.
-__device__ __forceinline__ void dir_finish(const DevTopo& t, const SolveCtl* __restrict__ ctl, int bit,
-                                           double* __restrict__ p, const double* __restrict__ src,
-                                           const double* __restrict__ g, double mt, double mr,
-                                           double* __restrict__ part, int vb, double* sm) {
-    const MapPos mp = map_pos_at(t.nblk, vb);
+__global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
+                                                   double* __restrict__ p, const double* __restrict__ src,
+                                                   const double* __restrict__ g, double mt, double mr,
+                                                   double* __restrict__ part) {
+    __shared__ double sm[kBlock / 32];
+    const MapPos mp = map_pos(t.nblk);
     if (!(ctl[mp.inst].flags & bit)) return;
     double acc[1] = {0};
     if (mp.valid) {
@@ -267,15 +228,7 @@ __device__ __forceinline__ void dir_finish(const DevTopo& t, const SolveCtl* __r
         acc[0] = dot6(g + b, v);
     }
     block_sum<1>(acc, sm);
-    if (threadIdx.x == 0) part[vb] = acc[0];
-}
-
-__global__ void __launch_bounds__(kBlock) k_finish(DevTopo t, const SolveCtl* __restrict__ ctl, int bit,
-                                                   double* __restrict__ p, const double* __restrict__ src,
-                                                   const double* __restrict__ g, double mt, double mr,
-                                                   double* __restrict__ part) {
-    __shared__ double sm[kBlock / 32];
-    dir_finish(t, ctl, bit, p, src, g, mt, mr, part, int(blockIdx.x), sm);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
 }
 
 // One block per instance with `bit` set: out[K i + k] = sum of its partials.
@@ -290,79 +243,6 @@ __global__ void __launch_bounds__(kBlock) k_inst_final(DevTopo t, const SolveCtl
     if (threadIdx.x == 0)
 #pragma unroll
         for (int k = 0; k < K; k++) out[size_t(K) * inst + k] = acc[k];
-}
-
-// ---- the multi-block two-loop in one launch --------------------------------------------------
-// k_tl_start, H x k_tl_step<1>, k_tl_scale, H x k_tl_step<2>, k_finish and k_inst_final<1> as
-// one cooperative launch: its blocks, all resident at once, walk the node blocks (block b
-// takes node blocks b, b + grid, ...) through the same step functions, and meet at a grid
-// barrier where the separate launches had their boundaries.  Every node block's arithmetic
-// and every partial sum is the same, so the direction is bit for bit that of the separate
-// launches.  Partials and coefficients written by other blocks are read from L2.
-constexpr unsigned kBarrierSpin = 1u << 22;  // polls of a barrier wait (~0.3 s) before it gives up
-
-// Grid-wide barrier of a cooperative launch.  A wait that gives up (it cannot while all
-// blocks are resident) sets bar->err, which the host reports, and goes on.
-__device__ __forceinline__ void grid_barrier(GridBarrier* bar, unsigned nblocks) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* gen = &bar->gen;
-        const unsigned g = *gen;
-        __threadfence();
-        if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            unsigned it = 0;
-            while (*gen == g) {
-                if (++it > kBarrierSpin) {
-                    atomicOr(&bar->err, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-}
-
-__global__ void __launch_bounds__(kBlock) k_two_loop_coop(DevTopo t, const SolveCtl* __restrict__ ctl,
-                                                          const int2* __restrict__ hist, int H, double* __restrict__ p,
-                                                          const double* __restrict__ g, const double* __restrict__ S,
-                                                          const double* __restrict__ Y, long long stride,
-                                                          const double* __restrict__ rho, double* __restrict__ alpha,
-                                                          double* __restrict__ part, double* __restrict__ dg,
-                                                          double mt, double mr, GridBarrier* bar) {
-    __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ double coef;
-    const int nb = t.n_nblk;
-    const int G = int(gridDim.x);
-    double* pp[2] = {part, part + size_t(nb)};
-    double* h0part = part + 2 * size_t(nb);
-    for (int vb = int(blockIdx.x); vb < nb; vb += G) tl_start(t, ctl, hist, H, p, g, S, Y, stride, h0part, pp[0], vb, sm);
-    for (int j = 0; j < H; j++) {
-        grid_barrier(bar, unsigned(G));
-        for (int vb = int(blockIdx.x); vb < nb; vb += G)
-            tl_step<1, true>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1], pp[(j + 1) & 1], vb, sm, coef);
-    }
-    grid_barrier(bar, unsigned(G));
-    for (int vb = int(blockIdx.x); vb < nb; vb += G) tl_scale<true>(t, ctl, hist, H, p, Y, stride, h0part, pp[0], vb, sm, coef);
-    for (int j = 0; j < H; j++) {
-        grid_barrier(bar, unsigned(G));
-        for (int vb = int(blockIdx.x); vb < nb; vb += G)
-            tl_step<2, true>(t, ctl, hist, H, j, p, S, Y, stride, rho, alpha, pp[j & 1], pp[(j + 1) & 1], vb, sm, coef);
-    }
-    grid_barrier(bar, unsigned(G));
-    for (int vb = int(blockIdx.x); vb < nb; vb += G) dir_finish(t, ctl, kOpDirection, p, p, g, mt, mr, part, vb, sm);
-    grid_barrier(bar, unsigned(G));
-    for (int inst = int(blockIdx.x); inst < t.I; inst += G) {
-        if (!(ctl[inst].flags & kOpDirection)) continue;  // block-uniform
-        double acc[1];
-        instance_sum<1, true>(t, part, inst, acc, sm);
-        if (threadIdx.x == 0) dg[inst] = acc[0];
-    }
 }
 
 // ---- vectors around an evaluation ------------------------------------------------------------
@@ -619,6 +499,194 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
     if (threadIdx.x == 0) dg[inst] = acc[0];
 }
 
+// ---- the whole direction in one cluster per instance ---------------------------------------
+// For instances of more node blocks than one CTA takes: the steps of k_direction_fused, with
+// the instance's chunks (node blocks) dealt round-robin to the C CTAs of a thread-block
+// cluster (chunk b to CTA b mod C).  Each CTA keeps its chunks' partial sums in its shared
+// memory; after a cluster barrier every CTA reads all partials through distributed shared
+// memory in the order instance_sum reads them, so every CTA forms the same coefficient, and
+// the direction is bit for bit that of the 2 H + 4 launches.  Partials are double-buffered
+// by step parity: a CTA rewrites a buffer only after the next barrier, which all CTAs reach
+// after they finished reading it.  The hardware cluster barrier replaces the kernel
+// boundaries of the separate launches; no thread spins.
+struct ClusterPart {
+    double v[2][2][kDirClusterChunks];  // [parity][value][local chunk]
+};
+
+// Sum over the instance's nchunk partials (value k of buffer par), thread t taking chunks
+// t, t + blockDim.x, ... in order, then the block tree: instance_sum's arithmetic.
+template <int K>
+__device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& cl, ClusterPart* mine, int par,
+                                            int nchunk, double (&acc)[K], double* sm) {
+    const int C = int(cl.num_blocks());
+#pragma unroll
+    for (int k = 0; k < K; k++) acc[k] = 0;
+    for (int b = int(threadIdx.x); b < nchunk; b += blockDim.x) {
+        const ClusterPart* src = cl.map_shared_rank(mine, unsigned(b % C));
+#pragma unroll
+        for (int k = 0; k < K; k++) acc[k] += src->v[par][k][b / C];
+    }
+    block_sum<K>(acc, sm);
+}
+
+__global__ void __launch_bounds__(kBlock) k_direction_cluster(DevTopo t, const SolveCtl* __restrict__ ctl,
+                                                              const int2* __restrict__ hist, int H,
+                                                              double* __restrict__ p, const double* __restrict__ g,
+                                                              const double* __restrict__ S,
+                                                              const double* __restrict__ Y, long long stride,
+                                                              const double* __restrict__ rho,
+                                                              double* __restrict__ dg, double mt, double mr) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    __shared__ double sm[2 * (kBlock / 32)];
+    __shared__ ClusterPart part;
+    __shared__ double alpha[64];
+    __shared__ double coef;
+    const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
+    const int inst = int(blockIdx.x) / C;
+    const SolveCtl c = load_ctl(ctl, hist, inst);
+    if (!(c.flags & kOpDirection)) return;  // the whole cluster
+    const int4 r = t.irange[inst];
+    const int nchunk = r.y - r.x;
+    int par = 0;
+    // p = g; partials of <s, y>, <y, y> of the newest pair
+    for (int b = rank; b < nchunk; b += C) {
+        const int4 q = t.nblk[r.x + b];
+        if (int(threadIdx.x) < q.y)
+#pragma unroll
+            for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] = g[6 * size_t(q.x + threadIdx.x) + d];
+        if (c.m > 0) {
+            const int slot = ring_slot(c, H, c.m - 1);
+            double acc[2] = {0, 0};
+            if (int(threadIdx.x) < q.y) {
+                const double* sv = hist_slot(S, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                const double* yv = hist_slot(Y, stride, slot) + 6 * size_t(q.x + threadIdx.x);
+                acc[0] = dot6(sv, yv);
+                acc[1] = dot6(yv, yv);
+            }
+            block_sum<2>(acc, sm);
+            if (threadIdx.x == 0) {
+                part.v[par][0][b / C] = acc[0];
+                part.v[par][1][b / C] = acc[1];
+            }
+        }
+    }
+    cl.sync();
+    double h0acc[2] = {0, 0};
+    if (c.m > 0) cluster_sum<2>(cl, &part, par, nchunk, h0acc, sm);
+    par ^= 1;
+    // loop 1, newest first
+    for (int j = 0; j < c.m; j++) {
+        const int h = c.m - 1 - j, slot = ring_slot(c, H, h);
+        for (int b = rank; b < nchunk; b += C) {
+            const int4 q = t.nblk[r.x + b];
+            const double v = chunk_dot(hist_slot(S, stride, slot), p, q.x, q.y, sm);
+            if (threadIdx.x == 0) part.v[par][0][b / C] = v;
+        }
+        cl.sync();
+        double acc[1];
+        cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
+        par ^= 1;
+        if (threadIdx.x == 0) {
+            coef = rho[size_t(inst) * H + slot] * acc[0];
+            alpha[h] = coef;
+        }
+        __syncthreads();
+        const double k = coef;
+        const double* yv = hist_slot(Y, stride, slot);
+        for (int b = rank; b < nchunk; b += C) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] -= k * yv[6 * size_t(q.x + threadIdx.x) + d];
+        }
+        __syncthreads();
+    }
+    // H0 (sim.cpp:186); the sums are complete in thread 0 only
+    if (threadIdx.x == 0) {
+        double v = .10;
+        if (c.m > 0 && h0acc[0] > 1e-20 && h0acc[1] > 1e-20) v = clampd(h0acc[0] / h0acc[1], 1e-7, 1e4);
+        coef = v;
+    }
+    __syncthreads();
+    {
+        const double v = coef;
+        for (int b = rank; b < nchunk; b += C) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] *= v;
+        }
+        __syncthreads();
+    }
+    // loop 2, oldest first
+    for (int j = 0; j < c.m; j++) {
+        const int slot = ring_slot(c, H, j);
+        for (int b = rank; b < nchunk; b += C) {
+            const int4 q = t.nblk[r.x + b];
+            const double v = chunk_dot(hist_slot(Y, stride, slot), p, q.x, q.y, sm);
+            if (threadIdx.x == 0) part.v[par][0][b / C] = v;
+        }
+        cl.sync();
+        double acc[1];
+        cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
+        par ^= 1;
+        if (threadIdx.x == 0) coef = alpha[j] - rho[size_t(inst) * H + slot] * acc[0];
+        __syncthreads();
+        const double k = coef;
+        const double* sv = hist_slot(S, stride, slot);
+        for (int b = rank; b < nchunk; b += C) {
+            const int4 q = t.nblk[r.x + b];
+            if (int(threadIdx.x) < q.y)
+#pragma unroll
+                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] += sv[6 * size_t(q.x + threadIdx.x) + d] * k;
+        }
+        __syncthreads();
+    }
+    // finish: clamp (sim.cpp:188-190, 46) and <g, p>
+    for (int b = rank; b < nchunk; b += C) {
+        const int4 q = t.nblk[r.x + b];
+        double acc[1] = {0};
+        if (int(threadIdx.x) < q.y) {
+            const size_t o = 6 * size_t(q.x + threadIdx.x);
+            const uint8_t* lk = t.locked + o;
+            double v[6];
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                v[k] = -p[o + k];
+                if (lk[k]) v[k] = 0;
+            }
+            const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+            if (lt > mt) {
+                const double f = mt / lt;
+                v[0] *= f; v[1] *= f; v[2] *= f;
+            }
+            const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
+            if (lr > mr) {
+                const double f = mr / lr;
+                v[3] *= f; v[4] *= f; v[5] *= f;
+            }
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                v[k] = lk[k] ? 0.0 : v[k];
+                p[o + k] = v[k];
+            }
+            acc[0] = dot6(g + o, v);
+        }
+        block_sum<1>(acc, sm);
+        if (threadIdx.x == 0) part.v[par][0][b / C] = acc[0];
+    }
+    cl.sync();
+    double acc[1];
+    cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
+    if (rank == 0 && threadIdx.x == 0) dg[inst] = acc[0];
+    cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+__global__ void k_cluster_probe(int* out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *out = 1;
+}
+
 // ---- decisions the device takes itself ------------------------------------------------------
 // Not a descent direction (sim.cpp:191): steepest descent instead.  For the instances that
 // computed a direction and found dg >= 0: p = clamp(lock(-g)) and the partial of <g, p>.
@@ -711,64 +779,12 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
     (k_direction_fused<<<t.I, kBlock, 0, s>>>(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr), note_launches(1));
 }
 
-__global__ void k_coop_probe(int* out) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *out = 1;
-}
-
-// Cooperative launches must also work inside captured graphs (every solver launch sequence
-// is captured): one is captured, instantiated and run on `s` before the path is used.
-bool coop_capture_works(cudaStream_t s, int* scratch) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(2);
-    cfg.blockDim = dim3(32);
-    cfg.stream = s;
-    cudaLaunchAttribute attr{};
-    attr.id = cudaLaunchAttributeCooperative;
-    attr.val.cooperative = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t x = nullptr;
-    bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-    if (ok) {
-        const bool launched = cudaLaunchKernelEx(&cfg, k_coop_probe, scratch) == cudaSuccess;
-        ok = cudaStreamEndCapture(s, &g) == cudaSuccess && launched;
-    }
-    ok = ok && cudaGraphInstantiate(&x, g, 0) == cudaSuccess;
-    ok = ok && cudaGraphLaunch(x, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
-    if (x) cudaGraphExecDestroy(x);
-    if (g) cudaGraphDestroy(g);
-    cudaGetLastError();
-    return ok;
-}
-
-int two_loop_coop_blocks(int device, cudaStream_t s, int* scratch) {
-    int per_sm = 0, sms = 0, coop = 0;
-    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_two_loop_coop, kBlock, 0) != cudaSuccess) return 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return 0;
-    if (!coop_capture_works(s, scratch)) return 0;
-    return per_sm * sms;
-}
-
 void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
                         const double* S, const double* Y, long long stride, const double* rho, double* alpha,
-                        double* part, double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar,
-                        int coop_blocks) {
+                        double* part, double* dg, double mt, double mr, cudaStream_t s, int cluster) {
     const int nb = t.n_nblk;
-    if (bar && coop_blocks > 0) {
-        cudaLaunchConfig_t cfg{};
-        cfg.gridDim = dim3(unsigned(std::min(nb, coop_blocks)));
-        cfg.blockDim = dim3(kBlock);
-        cfg.stream = s;
-        cudaLaunchAttribute attr{};
-        attr.id = cudaLaunchAttributeCooperative;
-        attr.val.cooperative = 1;
-        cfg.attrs = &attr;
-        cfg.numAttrs = 1;
-        cudaLaunchKernelEx(&cfg, k_two_loop_coop, t, ctl, const_cast<const int2*>(hist), H, p, g, S, Y, stride, rho,
-                           alpha, part, dg, mt, mr, bar);
-        note_launches(1);
+    if (cluster > 0) {
+        launch_direction_cluster(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s, cluster);
         return;
     }
     // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
@@ -797,9 +813,9 @@ void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p
 
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s, GridBarrier* bar, int coop_blocks) {
+                  double* dg, double mt, double mr, cudaStream_t s, int cluster) {
     bl_direction_fused(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s);
-    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s, bar, coop_blocks);
+    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s, cluster);
     bl_descent_fix(t, ctl, hist, p, g, part, dg, mt, mr, s);
 }
 
@@ -824,6 +840,87 @@ void bl_accept(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double*
      note_launches(1));
     (k_inst_final<3><<<t.I, kBlock, 0, s>>>(t, ctl, kOpAccept, part, out3), note_launches(1));
     (k_history_update<<<(t.I + kBlock - 1) / kBlock, kBlock, 0, s>>>(t.I, H, ctl, out3, hist, rho), note_launches(1));
+}
+
+}  // namespace mcg
+
+namespace mcg {
+
+namespace {
+
+cudaError_t launch_cluster_kernel_cfg(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& attr, dim3 grid, int C,
+                                      cudaStream_t s) {
+    cfg = cudaLaunchConfig_t{};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kBlock);
+    cfg.stream = s;
+    attr = cudaLaunchAttribute{};
+    attr.id = cudaLaunchAttributeClusterDimension;
+    attr.val.clusterDim.x = unsigned(C);
+    attr.val.clusterDim.y = 1;
+    attr.val.clusterDim.z = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+void launch_direction_cluster(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
+                              const double* S, const double* Y, long long stride, const double* rho, double* dg,
+                              double mt, double mr, cudaStream_t s, int cluster) {
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute attr;
+    launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(t.I * cluster)), cluster, s);
+    cudaLaunchKernelEx(&cfg, k_direction_cluster, t, ctl, const_cast<const int2*>(hist), H, p, g, S, Y, stride, rho,
+                       dg, mt, mr);
+    note_launches(1);
+}
+
+int direction_cluster_size(int device, cudaStream_t s) {
+    int supported = 0;
+    if (cudaDeviceGetAttribute(&supported, cudaDevAttrClusterLaunch, device) != cudaSuccess || !supported) return 0;
+    for (int C : {16, 8}) {
+        if (C > 8 && cudaFuncSetAttribute(k_direction_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                         cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        cudaLaunchConfig_t cfg;
+        cudaLaunchAttribute attr;
+        launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(C)), C, s);
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_direction_cluster, &cfg) != cudaSuccess || clusters < 1) {
+            cudaGetLastError();
+            continue;
+        }
+        // the launch must also work captured into a graph, as every solver launch is
+        int* scratch = nullptr;
+        if (cudaMallocAsync(&scratch, sizeof(int), s) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        cudaGraph_t gr = nullptr;
+        cudaGraphExec_t x = nullptr;
+        bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            cudaLaunchConfig_t pc;
+            cudaLaunchAttribute pa;
+            launch_cluster_kernel_cfg(pc, pa, dim3(unsigned(C)), C, s);
+            pc.blockDim = dim3(32);
+            const bool launched = cudaLaunchKernelEx(&pc, k_cluster_probe, scratch) == cudaSuccess;
+            ok = cudaStreamEndCapture(s, &gr) == cudaSuccess && launched;
+        }
+        ok = ok && cudaGraphInstantiate(&x, gr, 0) == cudaSuccess;
+        ok = ok && cudaGraphLaunch(x, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+        if (x) cudaGraphExecDestroy(x);
+        if (gr) cudaGraphDestroy(gr);
+        cudaGetLastError();
+        cudaFreeAsync(scratch, s);
+        cudaStreamSynchronize(s);
+        if (ok) return C;
+    }
+    return 0;
 }
 
 }  // namespace mcg

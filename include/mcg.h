@@ -348,9 +348,9 @@ int mcg_set_solver_loop(mcg_ctx* ctx, int device);
 int mcg_solver_loop(mcg_ctx* ctx, int32_t* device);
 /* How the two-loop recursion (sim.cpp:184-187) of a lattice too large for one CTA is
  * launched (no reference counterpart): one_launch != 0 (the default, where the device
- * supports cooperative launches) runs its 2 H + 2 steps in one launch whose blocks meet at a
- * grid barrier between steps; 0 runs each step as a launch of its own.  The same result bit
- * for bit. */
+ * supports thread-block clusters) runs its 2 H + 2 steps in one launch, one cluster of up to
+ * 16 CTAs per lattice exchanging partial sums through distributed shared memory; 0 runs
+ * each step as a launch of its own.  The same result bit for bit. */
 int mcg_set_direction_launch(mcg_ctx* ctx, int one_launch);
 /* Time of the device-resident loop's rounds since the upload or the last
  * mcg_set_solver_loop (no reference counterpart): ms4 = {directions, evaluations (with the
