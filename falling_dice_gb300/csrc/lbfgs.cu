@@ -500,23 +500,26 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
 }
 
 // ---- the whole direction in one cluster per instance ---------------------------------------
-// For instances of more node blocks than one CTA takes: the steps of k_direction_fused, with
-// the instance's chunks (node blocks) dealt round-robin to the C CTAs of a thread-block
-// cluster (chunk b to CTA b mod C).  Each CTA keeps its chunks' partial sums in its shared
-// memory; after a cluster barrier every CTA reads all partials through distributed shared
-// memory in the order instance_sum reads them, so every CTA forms the same coefficient, and
-// the direction is bit for bit that of the 2 H + 4 launches.  Partials are double-buffered
-// by step parity: a CTA rewrites a buffer only after the next barrier, which all CTAs reach
-// after they finished reading it.  The hardware cluster barrier replaces the kernel
-// boundaries of the separate launches; no thread spins.
+// For instances of more node blocks than one CTA takes: the steps of the 2 H + 4 launches
+// (k_tl_start, k_tl_step, k_tl_scale, k_finish, k_inst_final) in one launch, the instance's
+// chunks (node blocks) dealt round-robin to the C CTAs of a thread-block cluster (chunk b to
+// CTA b mod C).  A pass streams the CTA's chunks once: each thread updates its node of every
+// chunk and forms that chunk's next partial with the same tree as block_sum (warp shuffles,
+// then the 8 warp sums in order), the chunks' loads in flight together.  The partials stay
+// in the CTA's shared memory; after the hardware cluster barrier every CTA reads all of them
+// through distributed shared memory in the order instance_sum reads them, so every CTA forms
+// the same coefficient, and the direction is bit for bit that of the separate launches.
+// Partials are double-buffered by step parity: a CTA rewrites a buffer only after the next
+// barrier, which every CTA reaches after it read the buffer.  No thread spins.
 struct ClusterPart {
-    double v[2][2][kDirClusterChunks];  // [parity][value][local chunk]
+    double v[2][3][kDirClusterChunks];  // [parity][value][local chunk]
 };
 
-// Sum over the instance's nchunk partials (value k of buffer par), thread t taking chunks
-// t, t + blockDim.x, ... in order, then the block tree: instance_sum's arithmetic.
+// Sum over the instance's nchunk partials (value k0 .. k0 + K - 1 of buffer par), thread t
+// taking chunks t, t + blockDim.x, ... in order, then the block tree: instance_sum's
+// arithmetic.  Complete in thread 0.
 template <int K>
-__device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& cl, ClusterPart* mine, int par,
+__device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& cl, ClusterPart* mine, int par, int k0,
                                             int nchunk, double (&acc)[K], double* sm) {
     const int C = int(cl.num_blocks());
 #pragma unroll
@@ -524,9 +527,41 @@ __device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& c
     for (int b = int(threadIdx.x); b < nchunk; b += blockDim.x) {
         const ClusterPart* src = cl.map_shared_rank(mine, unsigned(b % C));
 #pragma unroll
-        for (int k = 0; k < K; k++) acc[k] += src->v[par][k][b / C];
+        for (int k = 0; k < K; k++) acc[k] += src->v[par][k0 + k][b / C];
     }
     block_sum<K>(acc, sm);
+}
+
+// One pass over the CTA's chunks: f(node, v) updates node's entries and returns in v[0..K-1]
+// its terms of the next partial sums; each chunk's K partials (block_sum's tree) go to
+// part->v[par][k][local chunk].  smw holds K x kDirClusterChunks x 8 warp sums.
+template <int K, typename F>
+__device__ __forceinline__ void chunk_pass(const DevTopo& t, int4 r, int rank, int C, int nchunk, ClusterPart* part,
+                                           int par, double* smw, F&& f) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int nw = kBlock / 32;
+    __syncthreads();  // the previous pass's reads of smw are done
+    int lc = 0;
+#pragma unroll 2
+    for (int b = rank; b < nchunk; b += C, lc++) {
+        const int4 q = t.nblk[r.x + b];
+        double v[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) v[k] = 0;
+        if (int(threadIdx.x) < q.y) f(q.x + int(threadIdx.x), v);
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const double w = warp_sum(v[k]);
+            if (lane == 0) smw[(k * kDirClusterChunks + lc) * nw + warp] = w;
+        }
+    }
+    __syncthreads();
+    for (int i = int(threadIdx.x); i < K * lc; i += blockDim.x) {
+        const int k = i / lc, l = i - k * lc;
+        double sum = 0;
+        for (int w = 0; w < nw; w++) sum += smw[(k * kDirClusterChunks + l) * nw + w];
+        part->v[par][k][l] = sum;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_direction_cluster(DevTopo t, const SolveCtl* __restrict__ ctl,
@@ -538,148 +573,149 @@ __global__ void __launch_bounds__(kBlock) k_direction_cluster(DevTopo t, const S
                                                               double* __restrict__ dg, double mt, double mr) {
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
-    __shared__ double sm[2 * (kBlock / 32)];
+    extern __shared__ double smw[];  // 3 x kDirClusterChunks x 8 warp sums
+    __shared__ double sm[3 * (kBlock / 32)];
     __shared__ ClusterPart part;
     __shared__ double alpha[64];
-    __shared__ double coef;
+    __shared__ double coef_sh;
     const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
     const int inst = int(blockIdx.x) / C;
     const SolveCtl c = load_ctl(ctl, hist, inst);
     if (!(c.flags & kOpDirection)) return;  // the whole cluster
     const int4 r = t.irange[inst];
-    const int nchunk = r.y - r.x;
+    const int nchunk = r.y - r.x, m = c.m;
     int par = 0;
-    // p = g; partials of <s, y>, <y, y> of the newest pair
-    for (int b = rank; b < nchunk; b += C) {
-        const int4 q = t.nblk[r.x + b];
-        if (int(threadIdx.x) < q.y)
+    // the coefficient of the step the barrier just completed (every CTA forms the same one)
+    auto sum1 = [&](int k0) {
+        double acc[1];
+        cluster_sum<1>(cl, &part, par, k0, nchunk, acc, sm);
+        return acc[0];  // thread 0
+    };
+    // start (k_tl_start): p = g; partials of <s, y>, <y, y> of the newest pair and <s, g>
+    {
+        const int slot = m > 0 ? ring_slot(c, H, m - 1) : 0;
+        const double* sv = hist_slot(S, stride, slot);
+        const double* yv = hist_slot(Y, stride, slot);
+        chunk_pass<3>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[3]) {
+            const size_t o = 6 * size_t(i);
 #pragma unroll
-            for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] = g[6 * size_t(q.x + threadIdx.x) + d];
-        if (c.m > 0) {
-            const int slot = ring_slot(c, H, c.m - 1);
-            double acc[2] = {0, 0};
-            if (int(threadIdx.x) < q.y) {
-                const double* sv = hist_slot(S, stride, slot) + 6 * size_t(q.x + threadIdx.x);
-                const double* yv = hist_slot(Y, stride, slot) + 6 * size_t(q.x + threadIdx.x);
-                acc[0] = dot6(sv, yv);
-                acc[1] = dot6(yv, yv);
+            for (int d = 0; d < 6; d++) p[o + d] = g[o + d];
+            if (m > 0) {
+                v[0] = dot6(sv + o, yv + o);
+                v[1] = dot6(yv + o, yv + o);
+                v[2] = dot6(sv + o, g + o);
             }
-            block_sum<2>(acc, sm);
-            if (threadIdx.x == 0) {
-                part.v[par][0][b / C] = acc[0];
-                part.v[par][1][b / C] = acc[1];
-            }
-        }
+        });
     }
     cl.sync();
     double h0acc[2] = {0, 0};
-    if (c.m > 0) cluster_sum<2>(cl, &part, par, nchunk, h0acc, sm);
-    par ^= 1;
-    // loop 1, newest first
-    for (int j = 0; j < c.m; j++) {
-        const int h = c.m - 1 - j, slot = ring_slot(c, H, h);
-        for (int b = rank; b < nchunk; b += C) {
-            const int4 q = t.nblk[r.x + b];
-            const double v = chunk_dot(hist_slot(S, stride, slot), p, q.x, q.y, sm);
-            if (threadIdx.x == 0) part.v[par][0][b / C] = v;
-        }
-        cl.sync();
-        double acc[1];
-        cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
-        par ^= 1;
+    if (m > 0) {
+        cluster_sum<2>(cl, &part, par, 0, nchunk, h0acc, sm);
+        const double a = sum1(2);
         if (threadIdx.x == 0) {
-            coef = rho[size_t(inst) * H + slot] * acc[0];
-            alpha[h] = coef;
+            const int slot = ring_slot(c, H, m - 1);
+            alpha[m - 1] = rho[size_t(inst) * H + slot] * a;
         }
-        __syncthreads();
-        const double k = coef;
-        const double* yv = hist_slot(Y, stride, slot);
-        for (int b = rank; b < nchunk; b += C) {
-            const int4 q = t.nblk[r.x + b];
-            if (int(threadIdx.x) < q.y)
-#pragma unroll
-                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] -= k * yv[6 * size_t(q.x + threadIdx.x) + d];
-        }
-        __syncthreads();
     }
-    // H0 (sim.cpp:186); the sums are complete in thread 0 only
+    par ^= 1;
+    // loop 1, newest first (k_tl_step<1>): p -= alpha_h y_h, then the partial of the next step
+    for (int j = 0; j < m; j++) {
+        const int h = m - 1 - j;
+        __syncthreads();
+        const double k = alpha[h];
+        const double* yv = hist_slot(Y, stride, ring_slot(c, H, h));
+        const bool more = j + 1 < m;
+        const double* sv = hist_slot(S, stride, ring_slot(c, H, more ? h - 1 : h));
+        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
+            const size_t o = 6 * size_t(i);
+            double pn[6];
+#pragma unroll
+            for (int d = 0; d < 6; d++) {
+                pn[d] = p[o + d] - k * yv[o + d];
+                p[o + d] = pn[d];
+            }
+            if (more) v[0] = dot6(sv + o, pn);
+        });
+        if (!more) break;
+        cl.sync();
+        const double a = sum1(0);
+        if (threadIdx.x == 0) alpha[h - 1] = rho[size_t(inst) * H + ring_slot(c, H, h - 1)] * a;
+        par ^= 1;
+    }
+    // H0 (sim.cpp:186) and p *= H0 (k_tl_scale), then the partial of loop 2's first step
     if (threadIdx.x == 0) {
         double v = .10;
-        if (c.m > 0 && h0acc[0] > 1e-20 && h0acc[1] > 1e-20) v = clampd(h0acc[0] / h0acc[1], 1e-7, 1e4);
-        coef = v;
+        if (m > 0 && h0acc[0] > 1e-20 && h0acc[1] > 1e-20) v = clampd(h0acc[0] / h0acc[1], 1e-7, 1e4);
+        coef_sh = v;
     }
     __syncthreads();
     {
-        const double v = coef;
-        for (int b = rank; b < nchunk; b += C) {
-            const int4 q = t.nblk[r.x + b];
-            if (int(threadIdx.x) < q.y)
+        const double k = coef_sh;
+        const double* yv = hist_slot(Y, stride, ring_slot(c, H, 0));
+        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
+            const size_t o = 6 * size_t(i);
+            double pn[6];
 #pragma unroll
-                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] *= v;
-        }
-        __syncthreads();
+            for (int d = 0; d < 6; d++) {
+                pn[d] = p[o + d] * k;
+                p[o + d] = pn[d];
+            }
+            if (m > 0) v[0] = dot6(yv + o, pn);
+        });
     }
-    // loop 2, oldest first
-    for (int j = 0; j < c.m; j++) {
-        const int slot = ring_slot(c, H, j);
-        for (int b = rank; b < nchunk; b += C) {
-            const int4 q = t.nblk[r.x + b];
-            const double v = chunk_dot(hist_slot(Y, stride, slot), p, q.x, q.y, sm);
-            if (threadIdx.x == 0) part.v[par][0][b / C] = v;
-        }
+    // loop 2, oldest first (k_tl_step<2>): p += s_j (alpha_j - beta_j), then the next partial
+    for (int j = 0; j < m; j++) {
         cl.sync();
-        double acc[1];
-        cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
+        const double a = sum1(0);
+        if (threadIdx.x == 0) coef_sh = alpha[j] - rho[size_t(inst) * H + ring_slot(c, H, j)] * a;
         par ^= 1;
-        if (threadIdx.x == 0) coef = alpha[j] - rho[size_t(inst) * H + slot] * acc[0];
         __syncthreads();
-        const double k = coef;
-        const double* sv = hist_slot(S, stride, slot);
-        for (int b = rank; b < nchunk; b += C) {
-            const int4 q = t.nblk[r.x + b];
-            if (int(threadIdx.x) < q.y)
+        const double k = coef_sh;
+        const double* sv = hist_slot(S, stride, ring_slot(c, H, j));
+        const bool more = j + 1 < m;
+        const double* yv = hist_slot(Y, stride, ring_slot(c, H, more ? j + 1 : j));
+        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
+            const size_t o = 6 * size_t(i);
+            double pn[6];
 #pragma unroll
-                for (int d = 0; d < 6; d++) p[6 * size_t(q.x + threadIdx.x) + d] += sv[6 * size_t(q.x + threadIdx.x) + d] * k;
-        }
-        __syncthreads();
+            for (int d = 0; d < 6; d++) {
+                pn[d] = p[o + d] + sv[o + d] * k;
+                p[o + d] = pn[d];
+            }
+            if (more) v[0] = dot6(yv + o, pn);
+        });
     }
-    // finish: clamp (sim.cpp:188-190, 46) and <g, p>
-    for (int b = rank; b < nchunk; b += C) {
-        const int4 q = t.nblk[r.x + b];
-        double acc[1] = {0};
-        if (int(threadIdx.x) < q.y) {
-            const size_t o = 6 * size_t(q.x + threadIdx.x);
-            const uint8_t* lk = t.locked + o;
-            double v[6];
+    // finish (k_finish): p = clamp(lock(-p)) (sim.cpp:188-190, 46) and <g, p>, into the buffer
+    // the last pass left (that pass's partials are not read)
+    chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
+        const size_t o = 6 * size_t(i);
+        const uint8_t* lk = t.locked + o;
+        double w[6];
 #pragma unroll
-            for (int k = 0; k < 6; k++) {
-                v[k] = -p[o + k];
-                if (lk[k]) v[k] = 0;
-            }
-            const double lt = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-            if (lt > mt) {
-                const double f = mt / lt;
-                v[0] *= f; v[1] *= f; v[2] *= f;
-            }
-            const double lr = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);
-            if (lr > mr) {
-                const double f = mr / lr;
-                v[3] *= f; v[4] *= f; v[5] *= f;
-            }
-#pragma unroll
-            for (int k = 0; k < 6; k++) {
-                v[k] = lk[k] ? 0.0 : v[k];
-                p[o + k] = v[k];
-            }
-            acc[0] = dot6(g + o, v);
+        for (int d = 0; d < 6; d++) {
+            w[d] = -p[o + d];
+            if (lk[d]) w[d] = 0;
         }
-        block_sum<1>(acc, sm);
-        if (threadIdx.x == 0) part.v[par][0][b / C] = acc[0];
-    }
+        const double lt = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        if (lt > mt) {
+            const double f = mt / lt;
+            w[0] *= f; w[1] *= f; w[2] *= f;
+        }
+        const double lr = sqrt(w[3] * w[3] + w[4] * w[4] + w[5] * w[5]);
+        if (lr > mr) {
+            const double f = mr / lr;
+            w[3] *= f; w[4] *= f; w[5] *= f;
+        }
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            w[d] = lk[d] ? 0.0 : w[d];
+            p[o + d] = w[d];
+        }
+        v[0] = dot6(g + o, w);
+    });
     cl.sync();
-    double acc[1];
-    cluster_sum<1>(cl, &part, par, nchunk, acc, sm);
-    if (rank == 0 && threadIdx.x == 0) dg[inst] = acc[0];
+    const double gp = sum1(0);
+    if (rank == 0 && threadIdx.x == 0) dg[inst] = gp;
     cl.sync();  // no CTA leaves while another may still read its shared memory
 }
 
@@ -848,6 +884,8 @@ namespace mcg {
 
 namespace {
 
+constexpr size_t kClusterWarpSums = 3 * kDirClusterChunks * (kBlock / 32) * sizeof(double);
+
 cudaError_t launch_cluster_kernel_cfg(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& attr, dim3 grid, int C,
                                       cudaStream_t s) {
     cfg = cudaLaunchConfig_t{};
@@ -872,6 +910,7 @@ void launch_direction_cluster(const DevTopo& t, const SolveCtl* ctl, int2* hist,
     cudaLaunchConfig_t cfg;
     cudaLaunchAttribute attr;
     launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(t.I * cluster)), cluster, s);
+    cfg.dynamicSmemBytes = kClusterWarpSums;
     cudaLaunchKernelEx(&cfg, k_direction_cluster, t, ctl, const_cast<const int2*>(hist), H, p, g, S, Y, stride, rho,
                        dg, mt, mr);
     note_launches(1);
@@ -886,9 +925,15 @@ int direction_cluster_size(int device, cudaStream_t s) {
             cudaGetLastError();
             continue;
         }
+        if (cudaFuncSetAttribute(k_direction_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(kClusterWarpSums)) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
         cudaLaunchConfig_t cfg;
         cudaLaunchAttribute attr;
         launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(C)), C, s);
+        cfg.dynamicSmemBytes = kClusterWarpSums;
         int clusters = 0;
         if (cudaOccupancyMaxActiveClusters(&clusters, k_direction_cluster, &cfg) != cudaSuccess || clusters < 1) {
             cudaGetLastError();
