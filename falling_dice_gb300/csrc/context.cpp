@@ -546,7 +546,18 @@ struct mcg_ctx {
     void read_outs() {
         d2h(hp.outs, ev.out, size_t(I), stream);
         if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
+        d2h(hp.u32 + 6, ev.err, 1, stream);
         sync();
+        check_kernel_error();
+    }
+    // A kernel's bounded wait that gave up (ev.err, read into hp.u32[6] with the totals)
+    // leaves its evaluation invalid: an error, after which the context stays usable.
+    void check_kernel_error() {
+        if (!hp.u32[6]) return;
+        hp.u32[6] = 0;
+        ck(cudaMemsetAsync(ev.err, 0, sizeof(unsigned), stream), "memset");
+        sync();
+        throw Fail(MCG_ERR_CUDA, "a staging wait of the beam kernel gave up; the evaluation is invalid");
     }
     // Totals of the last evaluation, repeating it if it overflowed a contact buffer.
     EvalOut read_out() {
@@ -805,8 +816,10 @@ struct mcg_ctx {
             d2h(hp.mz, d_mz, 1, stream);
             d2h(hp.outs, ev.out, size_t(I), stream);
             if (cfg.self_contact) d2h(hp.u32, cb.hoff + contact_chunks(), 1, stream);
+            d2h(hp.u32 + 6, ev.err, 1, stream);
             sync();
             check_launch();
+            check_kernel_error();
             loop_wall_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
             loop_ns[0] += hp.mz->t_dir;
             loop_ns[1] += hp.mz->t_eval;
@@ -1440,6 +1453,8 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     e.slotB = V.get<double>(6 * size_t(B));
     e.part_state = V.get<double>(9 * size_t(T.n_nblk));
     e.part_beam = V.get<double>(3 * size_t(std::max(T.n_bblk, 1)));
+    e.err = V.get<unsigned>(1);
+    ck(cudaMemsetAsync(e.err, 0, sizeof(unsigned), s), "memset");
     e.part_node = V.get<double>(kNodeParts * size_t(T.n_nblk));
     e.part_fin = V.get<double>(size_t(kFinPartDoubles) * size_t(I));
     e.cen = V.get<double>(9 * size_t(I + 1));
@@ -1555,6 +1570,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     }
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
+        prepare_beams_mixed(c->device);
         launch_mixed_constants(c->topo, c->mb, s);
         launch_plastic_mixed(c->topo, nullptr, c->d_plastic, nullptr, c->mb, s);
         c->rebase();

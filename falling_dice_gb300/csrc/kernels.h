@@ -175,6 +175,7 @@ struct EvalBufs {
     double* slotB;          // [6B] (+F, Gb) per beam, added to node b
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
     double* part_beam;      // [3 * nb_beams]
+    unsigned* err;          // [1] a kernel's bounded wait gave up (the host reports it)
     double* part_node;      // [kNodeParts * nb_nodes]
     double* part_fin;       // [I * kFinPartDoubles] first-stage totals of the finalize
     double* cen;            // [9 (I + 1)] per instance mean, min, max of the node positions (min/max
@@ -229,6 +230,9 @@ enum class ShapeKernel { kBeams, kBeamsMixed, kGather };
 int shape_variants(ShapeKernel k);
 int shape_blocks(ShapeKernel k, int variant);
 int beams_mixed_variants();
+// Once per context, outside any stream capture: the staged variants' shared-memory limit and
+// the SM count that sizes their persistent grid.
+void prepare_beams_mixed(int device);
 int beams_mixed_blocks(int variant);
 void launch_beams(const DevTopo& t, const Material& m, const double* plastic, int trials,
                   EvalBufs& e, cudaStream_t s, int variant = 0);

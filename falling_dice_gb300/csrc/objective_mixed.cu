@@ -27,6 +27,8 @@
 // reference's degenerate-beam branch (chord below 1e-10 m, sim.cpp:139) lies below the
 // FP32 resolution of a position increment, so the mixed form resolves chords only down to
 // about 1e-9 m.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -300,6 +302,158 @@ __device__ __forceinline__ void section_constants(const MixedBeams& m, int b, fl
 }
 
 // ---- beam kernel (MC/src/sim.cpp:139-141, FP32 with the split above) ---------------------
+// The per-beam records of beam b: base chord and c0, the two base shear vectors with L0 and
+// |d0|, the base relative rotation, the plastic state and the radius.
+struct BeamRec {
+    float4 B0, B1, B2, B5, P0, P1;
+};
+// The node increments of its two ends and the base orientation of end a.
+struct BeamNodes {
+    float4 ua4, ub4, ea, eb, ra0;
+};
+
+// One beam: energies into ue (elastic) and up (plastic dissipation), its two end 6-vectors
+// into the gradient slots, its trial state when `trials`.
+template <bool kStreamed>
+__device__ __forceinline__ void beam_mixed(const Material& mat, const MixedBeams& m, int trials, EvalBufs& e, int B, int b,
+                                           const BeamRec& R, const BeamNodes& Nd, float4 ic, float& ue, float& up) {
+    const float4 B0 = R.B0, B1 = R.B1, B2 = R.B2, B5 = R.B5, P0 = R.P0, P1 = R.P1;
+    const float4 ua4 = Nd.ua4, ub4 = Nd.ub4, ea = Nd.ea, eb = Nd.eb, ra0 = Nd.ra0;
+    const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
+    const float c0 = B0.w, L0 = B1.w, Lb = B2.w;
+    const float q = c0 + 2.f * fdot(d0, du) + fdot(du, du);  // |d|^2 - L0^2
+    const f3 d = d0 + du;
+    const float L = sqrtf(fmaxf(L0 * L0 + q, 0.f));
+    float* sa = e.slotAf + 6 * size_t(b);
+    float* sb = e.slotBf + 6 * size_t(b);
+    if (L < 1e-10f) {
+        ue = 1e8f * (1e-10f - L) * (1e-10f - L);
+#pragma unroll
+        for (int k = 0; k < 6; k++) { sa[k] = 0.f; sb[k] = 0.f; }
+        if (trials) {
+#pragma unroll
+            for (int k = 0; k < 7; k++) { e.trial_nextf[k * size_t(B) + b] = 0.f; e.trial_auxf[k * size_t(B) + b] = 0.f; }
+#pragma unroll
+            for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
+        }
+    } else {
+        // Divisions are the approximate single-instruction form (__fdividef, relative
+        // error ~2 ulp): every divisor is a length or a small positive sum, well inside
+        // its range, and the form's error budget is set by FP32 itself.
+        const float invL = __fdividef(1.f, L);
+        const f3 tt = d * invL;
+        const float eps = __fdividef(q, (L + L0) * L0);
+        float4 C0, C1;  // (kb, kt, my, ty), (cs, aL, area, aLsy)
+        section_constants<kStreamed>(m, b, P1.w, L0, ic, C0, C1);
+        const float E = mat.Ef, H = mat.Hf, sy = ic.x;
+        // axial
+        const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
+        const float uax = C1.y * (ax.energy + ax.hard);
+        const float dax = C1.w * ax.dg;
+        f3 F = tt * (C1.z * ax.force);
+        // shear from the split director/chord differences
+        const f3 va = xyz(make_float4(ea.y, ea.z, ea.w, 0.f)), vb = xyz(make_float4(eb.y, eb.z, eb.w, 0.f));
+        const float wa = 1.f + ea.x, wb = 1.f + eb.x;
+        // base directors d_a0 = t0 + s_a0, d_b0 = t0 + s_b0: they only enter multiplied by
+        // a small vector (the rotation increment, the shear vector), so the ~1e-7 of the
+        // FP32 t0 is harmless; the small s_a0, s_b0 themselves come exact from FP64
+        const f3 sa0 = xyz(B1), sb0 = xyz(B2);
+        const float invLb = __fdividef(1.f, Lb);
+        const f3 t0 = d0 * invLb;
+        const f3 da0 = t0 + sa0, db0 = t0 + sb0;
+        const f3 dda = rot_inc(wa, va, da0), ddb = rot_inc(wb, vb, db0);
+        const f3 da = da0 + dda, db = db0 + ddb;
+        const float dLb = __fdividef(2.f * fdot(d0, du) + fdot(du, du), L + Lb);
+        const f3 tdiff = (du * Lb - d0 * dLb) * (invL * invLb);  // t - t0
+        const f3 ma = dda + sa0 - tdiff, mb = ddb + sb0 - tdiff;
+        const float cs = C1.x;
+        const float us = .5f * cs * (fdot(ma, ma) + fdot(mb, mb));
+        const f3 gt = (ma + mb) * (-cs);  // cs (2t - da - db)
+        const f3 trans = (gt - tt * fdot(gt, tt)) * invL;
+        F = F + trans;
+        // -cs (d x t) = cs d x (d - t): the moment from the small shear vector, so the
+        // independent FP32 roundings of d and t leave no residual moment at rest
+        f3 Ga = fcross(da, ma) * cs;
+        f3 Gb = fcross(db, mb) * cs;
+        // relative rotation (Ra0^* delta Ra0) Q0, delta = e_a^* e_b, near-identity forms
+        const float dw1 = ea.x + eb.x + ea.x * eb.x + fdot(va, vb);
+        const f3 dv0 = (vb - va) + vb * ea.x - va * eb.x - fcross(va, vb);
+        const f3 ra0v{ra0.y, ra0.z, ra0.w};
+        const f3 dv = rot_conj(ra0.x, ra0v, dv0);
+        const float a0 = B5.x;
+        const f3 v0{B5.y, B5.z, B5.w};
+        const float qw1 = dw1 + a0 + dw1 * a0 - fdot(dv, v0);
+        f3 qv = dv + v0 + v0 * dw1 + dv * a0 + fcross(dv, v0);
+        float qw = 1.f + qw1;
+        if (qw < 0.f) { qw = -qw; qv = -qv; }
+        const f3 phi = rotvec_f(qw, qv);
+        // axis = unit(Ra^T t), Ra = e_a Ra0
+        f3 ax_ = rot_conj(ra0.x, ra0v, rot_conj(wa, va, tt));
+        const float al2 = fdot(ax_, ax_);
+        const f3 axis = (isfinite(al2) && al2 > 1e-30f) ? ax_ * rsqrtf(al2) : f3{0.f, 1.f, 0.f};
+        const f3 rotp{P1.x, P1.y, P1.z};
+        const float tw = fdot(phi, axis), ptw = fdot(rotp, axis);
+        const f3 bend = phi - axis * tw, pbv = rotp - axis * ptw;
+        const float kb = C0.x, kt = C0.y, my = C0.z, ty = C0.w;
+        const R3 br = ret3(bend, pbv, P0.z, kb, my, mat.bend_hf * kb);
+        const R1 tor = ret1(tw, ptw, P0.w, kt, ty, mat.torsion_hf * kt);
+        const f3 moment = br.force + axis * tor.force;
+        const float ur = br.energy + br.hard + tor.energy + tor.hard;
+        const float dr = my * br.dg + ty * tor.dg;
+        const f3 world = rot(wa, va, rot(ra0.x, ra0v, jl_inv_t_f(phi, moment)));
+        Ga = Ga - world;
+        Gb = Gb + world;
+        ue = uax + us + ur;
+        up = dax + dr;
+        sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
+        sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
+        if (trials) {
+            const size_t S = size_t(B);
+            const f3 nrot = br.p + axis * tor.p;
+            e.trial_nextf[b] = ax.p;
+            e.trial_nextf[S + b] = ax.a;
+            e.trial_nextf[2 * S + b] = nrot.x;
+            e.trial_nextf[3 * S + b] = nrot.y;
+            e.trial_nextf[4 * S + b] = nrot.z;
+            e.trial_nextf[5 * S + b] = br.a;
+            e.trial_nextf[6 * S + b] = tor.a;
+            e.trial_auxf[b] = eps;
+            e.trial_auxf[S + b] = ax.force;
+            e.trial_auxf[2 * S + b] = moment.x;
+            e.trial_auxf[3 * S + b] = moment.y;
+            e.trial_auxf[4 * S + b] = moment.z;
+            e.trial_auxf[5 * S + b] = ue;
+            e.trial_auxf[6 * S + b] = up;
+            e.trial_flags[b] = ax.yielded;
+            e.trial_flags[S + b] = br.yielded;
+            e.trial_flags[2 * S + b] = tor.yielded;
+        }
+    }
+}
+
+__device__ __forceinline__ BeamNodes load_nodes(int2 ab, const float4* __restrict__ U, const float4* __restrict__ Ei,
+                                                const float4* __restrict__ R0f) {
+    return BeamNodes{U[ab.x], U[ab.y], Ei[ab.x], Ei[ab.y], R0f[ab.x]};
+}
+
+// Block totals: warp 0 sums the elastic and the plastic energies of the block (compensated,
+// fixed order) while the other warps only store theirs; the beam energy total is the FP64
+// sum of the two.  All threads call it; sm holds 2 kBlock floats.
+__device__ __forceinline__ void beam_block_totals(float ue, float up, float* sm, double* out3) {
+    sm[threadIdx.x] = ue;
+    sm[kBlock + threadIdx.x] = up;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const double se = warp_sum_smem(sm, threadIdx.x);
+        const double sp = warp_sum_smem(sm + kBlock, threadIdx.x);
+        if (threadIdx.x == 0) {
+            out3[0] = se + sp;
+            out3[1] = se;
+            out3[2] = sp;
+        }
+    }
+}
+
 // kMinBlocks: the occupancy variant (CTAs per SM), picked by mcg_autotune.
 template <bool kStreamed, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
@@ -309,145 +463,133 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
     const MapPos mp = map_pos(t.bblk);
     if (!t.active[mp.inst]) return;
     if (trials == 2) trials = t.trial_inst[mp.inst];  // per instance (device-resident solver)
-    const int b = mp.i;
-    const int B = t.B;
     float ue = 0.f, up = 0.f;  // elastic energy, plastic dissipation of this beam
     if (mp.valid) {
         // Every load is issued here, before any arithmetic: the streamed beam records and,
         // one step behind the end indices, the node increments, so that each thread keeps
         // all of its memory requests in flight at once (the kernel is latency-bound).
+        const int b = mp.i;
         const int2 ab = t.ab[b];
-        const float4 B0 = m.B0[b], B1 = m.B1[b], B2 = m.B2[b], B5 = m.B5[b];
-        const float4 P0 = m.P0[b], P1 = m.P1[b];  // (epsp, alpha, alphaB, alphaT), (rotp, r)
-        const float4 ua4 = U[ab.x], ub4 = U[ab.y];
-        const float4 ea = Ei[ab.x], eb = Ei[ab.y];
-        const float4 ra0 = R0f[ab.x];
-        const float4 ic = m.ic[mp.inst];
-        const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
-        const float c0 = B0.w, L0 = B1.w, Lb = B2.w;
-        const float q = c0 + 2.f * fdot(d0, du) + fdot(du, du);  // |d|^2 - L0^2
-        const f3 d = d0 + du;
-        const float L = sqrtf(fmaxf(L0 * L0 + q, 0.f));
-        float* sa = e.slotAf + 6 * size_t(b);
-        float* sb = e.slotBf + 6 * size_t(b);
-        if (L < 1e-10f) {
-            ue = 1e8f * (1e-10f - L) * (1e-10f - L);
-#pragma unroll
-            for (int k = 0; k < 6; k++) { sa[k] = 0.f; sb[k] = 0.f; }
-            if (trials) {
-#pragma unroll
-                for (int k = 0; k < 7; k++) { e.trial_nextf[k * size_t(B) + b] = 0.f; e.trial_auxf[k * size_t(B) + b] = 0.f; }
-#pragma unroll
-                for (int k = 0; k < 3; k++) e.trial_flags[k * size_t(B) + b] = 0;
-            }
-        } else {
-            // Divisions are the approximate single-instruction form (__fdividef, relative
-            // error ~2 ulp): every divisor is a length or a small positive sum, well inside
-            // its range, and the form's error budget is set by FP32 itself.
-            const float invL = __fdividef(1.f, L);
-            const f3 tt = d * invL;
-            const float eps = __fdividef(q, (L + L0) * L0);
-            float4 C0, C1;  // (kb, kt, my, ty), (cs, aL, area, aLsy)
-            section_constants<kStreamed>(m, b, P1.w, L0, ic, C0, C1);
-            const float E = mat.Ef, H = mat.Hf, sy = ic.x;
-            // axial
-            const R1 ax = ret1(eps, P0.x, P0.y, E, sy, H);
-            const float uax = C1.y * (ax.energy + ax.hard);
-            const float dax = C1.w * ax.dg;
-            f3 F = tt * (C1.z * ax.force);
-            // shear from the split director/chord differences
-            const f3 va = xyz(make_float4(ea.y, ea.z, ea.w, 0.f)), vb = xyz(make_float4(eb.y, eb.z, eb.w, 0.f));
-            const float wa = 1.f + ea.x, wb = 1.f + eb.x;
-            // base directors d_a0 = t0 + s_a0, d_b0 = t0 + s_b0: they only enter multiplied by
-            // a small vector (the rotation increment, the shear vector), so the ~1e-7 of the
-            // FP32 t0 is harmless; the small s_a0, s_b0 themselves come exact from FP64
-            const f3 sa0 = xyz(B1), sb0 = xyz(B2);
-            const float invLb = __fdividef(1.f, Lb);
-            const f3 t0 = d0 * invLb;
-            const f3 da0 = t0 + sa0, db0 = t0 + sb0;
-            const f3 dda = rot_inc(wa, va, da0), ddb = rot_inc(wb, vb, db0);
-            const f3 da = da0 + dda, db = db0 + ddb;
-            const float dLb = __fdividef(2.f * fdot(d0, du) + fdot(du, du), L + Lb);
-            const f3 tdiff = (du * Lb - d0 * dLb) * (invL * invLb);  // t - t0
-            const f3 ma = dda + sa0 - tdiff, mb = ddb + sb0 - tdiff;
-            const float cs = C1.x;
-            const float us = .5f * cs * (fdot(ma, ma) + fdot(mb, mb));
-            const f3 gt = (ma + mb) * (-cs);  // cs (2t - da - db)
-            const f3 trans = (gt - tt * fdot(gt, tt)) * invL;
-            F = F + trans;
-            // -cs (d x t) = cs d x (d - t): the moment from the small shear vector, so the
-            // independent FP32 roundings of d and t leave no residual moment at rest
-            f3 Ga = fcross(da, ma) * cs;
-            f3 Gb = fcross(db, mb) * cs;
-            // relative rotation (Ra0^* delta Ra0) Q0, delta = e_a^* e_b, near-identity forms
-            const float dw1 = ea.x + eb.x + ea.x * eb.x + fdot(va, vb);
-            const f3 dv0 = (vb - va) + vb * ea.x - va * eb.x - fcross(va, vb);
-            const f3 ra0v{ra0.y, ra0.z, ra0.w};
-            const f3 dv = rot_conj(ra0.x, ra0v, dv0);
-            const float a0 = B5.x;
-            const f3 v0{B5.y, B5.z, B5.w};
-            const float qw1 = dw1 + a0 + dw1 * a0 - fdot(dv, v0);
-            f3 qv = dv + v0 + v0 * dw1 + dv * a0 + fcross(dv, v0);
-            float qw = 1.f + qw1;
-            if (qw < 0.f) { qw = -qw; qv = -qv; }
-            const f3 phi = rotvec_f(qw, qv);
-            // axis = unit(Ra^T t), Ra = e_a Ra0
-            f3 ax_ = rot_conj(ra0.x, ra0v, rot_conj(wa, va, tt));
-            const float al2 = fdot(ax_, ax_);
-            const f3 axis = (isfinite(al2) && al2 > 1e-30f) ? ax_ * rsqrtf(al2) : f3{0.f, 1.f, 0.f};
-            const f3 rotp{P1.x, P1.y, P1.z};
-            const float tw = fdot(phi, axis), ptw = fdot(rotp, axis);
-            const f3 bend = phi - axis * tw, pbv = rotp - axis * ptw;
-            const float kb = C0.x, kt = C0.y, my = C0.z, ty = C0.w;
-            const R3 br = ret3(bend, pbv, P0.z, kb, my, mat.bend_hf * kb);
-            const R1 tor = ret1(tw, ptw, P0.w, kt, ty, mat.torsion_hf * kt);
-            const f3 moment = br.force + axis * tor.force;
-            const float ur = br.energy + br.hard + tor.energy + tor.hard;
-            const float dr = my * br.dg + ty * tor.dg;
-            const f3 world = rot(wa, va, rot(ra0.x, ra0v, jl_inv_t_f(phi, moment)));
-            Ga = Ga - world;
-            Gb = Gb + world;
-            ue = uax + us + ur;
-            up = dax + dr;
-            sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
-            sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
-            if (trials) {
-                const size_t S = size_t(B);
-                const f3 nrot = br.p + axis * tor.p;
-                e.trial_nextf[b] = ax.p;
-                e.trial_nextf[S + b] = ax.a;
-                e.trial_nextf[2 * S + b] = nrot.x;
-                e.trial_nextf[3 * S + b] = nrot.y;
-                e.trial_nextf[4 * S + b] = nrot.z;
-                e.trial_nextf[5 * S + b] = br.a;
-                e.trial_nextf[6 * S + b] = tor.a;
-                e.trial_auxf[b] = eps;
-                e.trial_auxf[S + b] = ax.force;
-                e.trial_auxf[2 * S + b] = moment.x;
-                e.trial_auxf[3 * S + b] = moment.y;
-                e.trial_auxf[4 * S + b] = moment.z;
-                e.trial_auxf[5 * S + b] = ue;
-                e.trial_auxf[6 * S + b] = up;
-                e.trial_flags[b] = ax.yielded;
-                e.trial_flags[S + b] = br.yielded;
-                e.trial_flags[2 * S + b] = tor.yielded;
-            }
-        }
+        const BeamRec R{m.B0[b], m.B1[b], m.B2[b], m.B5[b], m.P0[b], m.P1[b]};
+        const BeamNodes Nd = load_nodes(ab, U, Ei, R0f);
+        beam_mixed<kStreamed>(mat, m, trials, e, t.B, b, R, Nd, m.ic[mp.inst], ue, up);
     }
-    // Block totals: warp 0 sums the elastic and the plastic energies of the block
-    // (compensated, fixed order) while the other warps only store theirs; the beam energy
-    // total is the FP64 sum of the two.
-    sm[threadIdx.x] = ue;
-    sm[kBlock + threadIdx.x] = up;
+    beam_block_totals(ue, up, sm, e.part_beam + 3 * size_t(blockIdx.x));
+}
+
+// ---- the same kernel with its records staged by bulk copies --------------------------------
+// Persistent CTAs (kMinBlocks per SM) walk the beam blocks b = blockIdx.x, + gridDim.x, ...;
+// the six float4 records of a block's beams (4 KB each, contiguous) arrive in shared memory
+// by cp.async.bulk on an mbarrier, two blocks ahead of the arithmetic (double buffer), so
+// the streamed bytes are in flight during a whole block's computation without holding
+// registers; the threads still load the end indices and the node increments (mostly L2
+// hits) themselves.  Arithmetic, block partials and their order are those of
+// k_beams_mixed, bit for bit.  Every wait on a barrier is bounded: one that gives up sets
+// e.err (the host reports it), waits (bounded) for the CTA's copies in flight and returns.
+constexpr int kStageFields = 6;
+constexpr unsigned kStageWaitPolls = 1u << 20;  // a normal wait ends within microseconds
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return uint32_t(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, unsigned parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for the phase of `parity` to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (unsigned it = 0; it < kStageWaitPolls; it++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+template <bool kStreamed, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed_staged(DevTopo t, Material mat, MixedBeams m,
+                                                                           int trials, const float4* __restrict__ U,
+                                                                           const float4* __restrict__ Ei,
+                                                                           const float4* __restrict__ R0f, EvalBufs e) {
+    extern __shared__ __align__(128) float4 stage[];  // [2][kStageFields][kBlock]
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ float sm[2 * kBlock];
+    const int nt = t.n_bblk, G = int(gridDim.x);
+    const float4* src[kStageFields] = {m.B0, m.B1, m.B2, m.B5, m.P0, m.P1};
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
-    if (threadIdx.x < 32) {
-        const double se = warp_sum_smem(sm, threadIdx.x);
-        const double sp = warp_sum_smem(sm + kBlock, threadIdx.x);
-        if (threadIdx.x == 0) {
-            e.part_beam[3 * blockIdx.x] = se + sp;
-            e.part_beam[3 * blockIdx.x + 1] = se;
-            e.part_beam[3 * blockIdx.x + 2] = sp;
+    // tile i of this CTA is beam block blockIdx.x + i G; thread 0 issues its copies (a
+    // plain arrival for an inactive instance, whose block is skipped)
+    auto issue = [&](int i) {
+        const int vb = int(blockIdx.x) + i * G;
+        if (vb >= nt) return;
+        const int4 q = t.bblk[vb];
+        uint64_t* br = &bar[i & 1];
+        if (!t.active[q.z] || q.y <= 0) {
+            mbar_arrive(br);
+            return;
         }
+        const unsigned bytes = unsigned(q.y) * 16u;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // after the generic reads
+        mbar_arrive_tx(br, kStageFields * bytes);
+        float4* dst = stage + size_t(i & 1) * kStageFields * kBlock;
+        for (int f = 0; f < kStageFields; f++) bulk_to_smem(dst + f * kBlock, src[f] + q.x, bytes, br);
+    };
+    if (threadIdx.x == 0) {
+        issue(0);
+        issue(1);
+    }
+    for (int i = 0;; i++) {
+        const int vb = int(blockIdx.x) + i * G;
+        if (vb >= nt) break;
+        const int4 q = t.bblk[vb];
+        const bool ok = __syncthreads_and(mbar_wait(&bar[i & 1], unsigned(i >> 1) & 1u));
+        if (!ok) {
+            // give up: report, let the copies in flight land (bounded), return
+            if (threadIdx.x == 0) {
+                atomicOr(e.err, 1u);
+                mbar_wait(&bar[i & 1], unsigned(i >> 1) & 1u);
+                if (vb + G < nt) mbar_wait(&bar[(i + 1) & 1], unsigned((i + 1) >> 1) & 1u);
+            }
+            __syncthreads();
+            return;
+        }
+        if (t.active[q.z]) {  // block-uniform
+            const int tr = trials == 2 ? int(t.trial_inst[q.z]) : trials;
+            float ue = 0.f, up = 0.f;
+            if (int(threadIdx.x) < q.y) {
+                const int b = q.x + int(threadIdx.x);
+                const int2 ab = t.ab[b];
+                const BeamNodes Nd = load_nodes(ab, U, Ei, R0f);
+                const float4* st = stage + size_t(i & 1) * kStageFields * kBlock + threadIdx.x;
+                const BeamRec R{st[0], st[kBlock], st[2 * kBlock], st[3 * kBlock], st[4 * kBlock], st[5 * kBlock]};
+                beam_mixed<kStreamed>(mat, m, tr, e, t.B, b, R, Nd, m.ic[q.z], ue, up);
+            }
+            beam_block_totals(ue, up, sm, e.part_beam + 3 * size_t(vb));
+        }
+        __syncthreads();  // every read of this buffer (and of sm) is done
+        if (threadIdx.x == 0) issue(i + 2);
     }
 }
 
@@ -498,11 +640,29 @@ void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, 
     launch_center(t, e, s);
 }
 
-// Occupancy variants (CTAs per SM) of the mixed beam kernel; the streamed-constants form
-// (sections that are not circular) has the default one only.
-constexpr int kMixedBlocks[] = {3, 4, 5, 6};
-int beams_mixed_variants() { return 4; }
+// Variants of the mixed beam kernel: the plain kernel at 3, 4, 5 or 6 CTAs per SM, and the
+// kernel with bulk-copy staged records at 3 or 4 (reported as -3, -4); the
+// streamed-constants form (sections that are not circular) has the default one only.
+constexpr int kMixedBlocks[] = {3, 4, 5, 6, -3, -4};
+int beams_mixed_variants() { return 6; }
 int beams_mixed_blocks(int v) { return kMixedBlocks[v]; }
+
+namespace {
+constexpr size_t kStageBytes = size_t(2) * kStageFields * kBlock * sizeof(float4);
+int g_stage_sms = 0;  // SMs of the device (set by prepare_beams_mixed)
+template <int kMin>
+void launch_staged(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, int tr, EvalBufs& e,
+                   cudaStream_t s) {
+    const int grid = std::min(t.n_bblk, kMin * std::max(g_stage_sms, 1));  // persistent: all resident
+    k_beams_mixed_staged<false, kMin><<<grid, kBlock, kStageBytes, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e);
+}
+}  // namespace
+
+void prepare_beams_mixed(int device) {
+    cudaDeviceGetAttribute(&g_stage_sms, cudaDevAttrMultiProcessorCount, device);
+    cudaFuncSetAttribute(k_beams_mixed_staged<false, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes));
+    cudaFuncSetAttribute(k_beams_mixed_staged<false, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes));
+}
 
 void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, int trials,
                         EvalBufs& e, cudaStream_t s, int variant) {
@@ -515,6 +675,8 @@ void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& m
             case 1: k_beams_mixed<false, kMixedBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
             case 2: k_beams_mixed<false, kMixedBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
             case 3: k_beams_mixed<false, kMixedBlocks[3]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            case 4: launch_staged<3>(t, m, mb, mn, tr, e, s); break;
+            case 5: launch_staged<4>(t, m, mb, mn, tr, e, s); break;
             default: k_beams_mixed<false, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
         }
     }

@@ -311,8 +311,10 @@ int mcg_set_contact_shapes(mcg_ctx* ctx, double cell, int32_t pair_blocks);
  * First the self-contact broad phase: grid cells 0.9, 1, 1.1, 1.25 and 1.4 times the
  * reference's max(2.8 joint radius, 0.72 cell_size), and pair-enumeration grids of 152 ..
  * 1216 blocks (at most one warp per 32 shapes) besides the default; then the occupancy of the
- * beam kernel (FP64: 1, 2 or 3 CTAs of 256 threads per SM; mixed: 3, 4, 5 or 6) and of the
- * gradient gather (1, 2 or 4), one after the other.  Each candidate evaluates every lattice
+ * beam kernel (FP64: 1, 2 or 3 CTAs of 256 threads per SM; mixed: 3, 4, 5 or 6, and -3 or
+ * -4 for the mixed kernel whose beam records arrive in shared memory by bulk copies, two
+ * blocks ahead, in persistent CTAs at 3 or 4 per SM) and of the gradient gather (1, 2 or
+ * 4), one after the other.  Each candidate evaluates every lattice
  * `reps` times at z (host, 6 N values in the layout of mcg_batch_objective; NULL: z = 0) and
  * platen heights `tops` (NULL: each lattice's top0), with the candidate list rebuilt at
  * every evaluation; the fastest by CUDA-event time is kept for the context (broad phase:

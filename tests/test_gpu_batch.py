@@ -114,11 +114,12 @@ def test_fixed_shapes_leave_evaluations_unchanged(mcg):
         b.set_contact_shapes(-1.0, 0)
 
 
-@pytest.mark.parametrize("precision,beam_blocks", [(0, (1, 2, 3)), (1, (3, 4, 5, 6))])
+@pytest.mark.parametrize("precision,beam_blocks", [(0, (1, 2, 3)), (1, (3, 4, 5, 6, -3, -4))])
 def test_kernel_occupancy_variants_leave_evaluations_unchanged(mcg, precision, beam_blocks):
     """The beam kernel's and the gather's occupancy variants (CTAs per SM, which set their
-    register budgets; mcg_set_kernel_shapes / mcg_autotune) do the same arithmetic: every
-    variant gives the default's evaluation bit for bit, in both precision forms."""
+    register budgets; mcg_set_kernel_shapes / mcg_autotune), and the mixed beam kernel with
+    its records staged by bulk copies (-3, -4), do the same arithmetic: every variant gives the
+    default's evaluation bit for bit, in both precision forms."""
     cfg, lats, ys = make(mcg)
     cfg.precision = precision
     states = [mcg.random_state(lat, 0.04, 0.08, 0.02, 4000 + k) for k, lat in enumerate(lats)]
