@@ -56,7 +56,6 @@ SIGNATURES = {
     "mcg_contact_builds": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "mcg_set_solver_loop": (C.c_int, [_P, C.c_int]),
     "mcg_solver_loop": (C.c_int, [_P, C.POINTER(C.c_int32)]),
-    "mcg_set_direction_launch": (C.c_int, [_P, C.c_int]),
     "mcg_solver_times": (C.c_int, [_P, _d, C.POINTER(C.c_int64)]),
     "mcg_upload_batch": (C.c_int, [_P, C.c_int32, C.POINTER(abi.Topology), C.POINTER(abi.Geometry),
                                    C.POINTER(_d), C.POINTER(_d), _d]),
@@ -294,10 +293,6 @@ class Solver:
         """Solver rounds as a device-resident graph loop (True, the default) or stepped from the
         host (False); mcg_set_solver_loop."""
         self._check(self.lib.mcg_set_solver_loop(self.h, int(bool(device))), "mcg_set_solver_loop")
-
-    def set_direction_launch(self, one_launch):
-        """The multi-block two-loop as one cooperative launch (True) or 2 H + 4 launches."""
-        self._check(self.lib.mcg_set_direction_launch(self.h, int(bool(one_launch))), "mcg_set_direction_launch")
 
     def solver_times(self):
         """Device-resident loop time by stage (ms) and rounds (mcg_solver_times)."""

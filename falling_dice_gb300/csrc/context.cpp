@@ -239,12 +239,6 @@ struct mcg_ctx {
     uint8_t* d_fused = nullptr;
     uint8_t* d_trial = nullptr;   // per-instance trial mask of the loop's evaluations
     MzStatus* d_mz = nullptr;
-    // the direction of multi-block instances in one launch, one thread-block cluster each
-    // (lbfgs.cu): CTAs per cluster, 0 for the 2 H + 4 launches (no clusters on the device,
-    // or an instance with more node blocks than a cluster holds)
-    int dir_cluster = 0;
-    bool one_launch_direction = true;
-    int cluster_for_launch() const { return one_launch_direction ? dir_cluster : 0; }
     cudaGraphExec_t loop_exec = nullptr;
     cudaStream_t side = nullptr;  // captures the bodies of the loop's conditional nodes
     bool device_loop = true;
@@ -637,7 +631,7 @@ struct mcg_ctx {
             replay(1 | (any_dir ? 2 : 0) | (any_multi ? 4 : 0) | (any_sd ? 8 : 0), [&] {
                 if (any_dir)
                     bl_direction(topo, d_ctl, d_hist, std::max(H, 1), any_multi, d_p, d_g, d_S, d_Y, 6LL * N, d_rho,
-                                 d_alpha, d_part, d_dg, mt, mr, stream, cluster_for_launch());
+                                 d_alpha, d_part, d_dg, mt, mr, stream);
                 if (any_sd) bl_steepest(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, stream);
             });
         }
@@ -765,7 +759,7 @@ struct mcg_ctx {
                 });
                 capture_if(hm, [&](cudaStream_t s2) {
                     bl_direction_multi(topo, d_ctl, d_hist, Hs, d_p, d_g, d_S, d_Y, 6LL * N, d_rho, d_alpha, d_part,
-                                       d_dg, mt, mr, s2, cluster_for_launch());
+                                       d_dg, mt, mr, s2);
                 });
                 capture_if(hd, [&](cudaStream_t s2) {
                     bl_descent_fix(topo, d_ctl, d_hist, d_p, d_g, d_part, d_dg, mt, mr, s2);
@@ -1561,13 +1555,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     c->d_mz = Q.get<MzStatus>(1);
     c->d_fused = Q.get<uint8_t>(size_t(I));
     h2d(c->d_fused, c->fused.data(), size_t(I), s);
-    {
-        int widest = 0;  // node blocks of the largest instance the one-CTA direction does not take
-        for (int k = 0; k < I; k++)
-            if (!c->fused[size_t(k)]) widest = std::max(widest, irange[size_t(k)].y - irange[size_t(k)].x);
-        const int C = widest > 0 ? direction_cluster_size(c->device, s) : 0;
-        c->dir_cluster = C > 0 && widest <= C * kDirClusterChunks && c->H <= 64 ? C : 0;
-    }
+
     ck(cudaMemsetAsync(c->d_z, 0, n * sizeof(double), s), "memset");
     if (c->mixed) {
         prepare_beams_mixed(c->device);
@@ -2000,14 +1988,6 @@ int mcg_set_solver_loop(mcg_ctx* c, int device) {
         for (auto& v : c->loop_ns) v = 0;
         c->loop_rounds = 0;
         c->loop_wall_ms = 0;
-        c->drop_graphs();
-    });
-}
-
-int mcg_set_direction_launch(mcg_ctx* c, int one_launch) {
-    return guarded(c, [&] {
-        c->sync();
-        c->one_launch_direction = one_launch != 0;
         c->drop_graphs();
     });
 }

@@ -322,21 +322,9 @@ int fused_direction_limit();
 // multi, the kOpDirection instances; then p = clamp(lock(-p)) and dg[i] = <g, p>; where
 // not dg < 0, steepest descent with the history cleared (sim.cpp:191).
 // History: H slots of `stride` doubles, state hist[I], rho and alpha [I * H].
-// CTAs per cluster of the one-launch two-loop of multi-block instances on `device` (0:
-// clusters unavailable or not capturable into graphs: the two-loop then runs as 2 H + 4
-// launches).  Checks the capture with one small launch on `s`.
-int direction_cluster_size(int device, cudaStream_t s);
-// Chunks (node blocks) a CTA of that cluster holds; instances up to cluster x this many node
-// blocks take the one-launch path.
-constexpr int kDirClusterChunks = 256;
-// The direction of the kOpDirection instances by one cluster of `cluster` CTAs each: the
-// same steps and partial sums as the 2 H + 4 launches, bit for bit.
-void launch_direction_cluster(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
-                              const double* S, const double* Y, long long stride, const double* rho, double* dg,
-                              double mt, double mr, cudaStream_t s, int cluster);
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s, int cluster = 0);
+                  double* dg, double mt, double mr, cudaStream_t s);
 // The pieces of bl_direction, for callers that launch them under separate conditions: the
 // one-CTA directions (kOpDirFused), the multi-block two-loop (kOpDirection), and the
 // steepest-descent fallback of either kind where <g, p> >= 0.
@@ -345,7 +333,7 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
                         double mr, cudaStream_t s);
 void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
                         const double* S, const double* Y, long long stride, const double* rho, double* alpha,
-                        double* part, double* dg, double mt, double mr, cudaStream_t s, int cluster = 0);
+                        double* part, double* dg, double mt, double mr, cudaStream_t s);
 void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p, const double* g, double* part,
                     double* dg, double mt, double mr, cudaStream_t s);
 // The steepest-descent retry for the kOpSteepest instances: history cleared,

@@ -11,8 +11,6 @@
 // summing its blocks in order: the same partition whether an instance is solved alone or
 // with others, so a batch reproduces the separate runs bit for bit.  The two-loop scalars
 // (alpha_h, H0) never leave the device.
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 #include "kernels.h"
 
@@ -499,230 +497,6 @@ __global__ void __launch_bounds__(kBlock) k_direction_fused(DevTopo t, const Sol
     if (threadIdx.x == 0) dg[inst] = acc[0];
 }
 
-// ---- the whole direction in one cluster per instance ---------------------------------------
-// For instances of more node blocks than one CTA takes: the steps of the 2 H + 4 launches
-// (k_tl_start, k_tl_step, k_tl_scale, k_finish, k_inst_final) in one launch, the instance's
-// chunks (node blocks) dealt round-robin to the C CTAs of a thread-block cluster (chunk b to
-// CTA b mod C).  A pass streams the CTA's chunks once: each thread updates its node of every
-// chunk and forms that chunk's next partial with the same tree as block_sum (warp shuffles,
-// then the 8 warp sums in order), the chunks' loads in flight together.  The partials stay
-// in the CTA's shared memory; after the hardware cluster barrier every CTA reads all of them
-// through distributed shared memory in the order instance_sum reads them, so every CTA forms
-// the same coefficient, and the direction is bit for bit that of the separate launches.
-// Partials are double-buffered by step parity: a CTA rewrites a buffer only after the next
-// barrier, which every CTA reaches after it read the buffer.  No thread spins.
-struct ClusterPart {
-    double v[2][3][kDirClusterChunks];  // [parity][value][local chunk]
-};
-
-// Sum over the instance's nchunk partials (value k0 .. k0 + K - 1 of buffer par), thread t
-// taking chunks t, t + blockDim.x, ... in order, then the block tree: instance_sum's
-// arithmetic.  Complete in thread 0.
-template <int K>
-__device__ __forceinline__ void cluster_sum(cooperative_groups::cluster_group& cl, ClusterPart* mine, int par, int k0,
-                                            int nchunk, double (&acc)[K], double* sm) {
-    const int C = int(cl.num_blocks());
-#pragma unroll
-    for (int k = 0; k < K; k++) acc[k] = 0;
-    for (int b = int(threadIdx.x); b < nchunk; b += blockDim.x) {
-        const ClusterPart* src = cl.map_shared_rank(mine, unsigned(b % C));
-#pragma unroll
-        for (int k = 0; k < K; k++) acc[k] += src->v[par][k0 + k][b / C];
-    }
-    block_sum<K>(acc, sm);
-}
-
-// One pass over the CTA's chunks: f(node, v) updates node's entries and returns in v[0..K-1]
-// its terms of the next partial sums; each chunk's K partials (block_sum's tree) go to
-// part->v[par][k][local chunk].  smw holds K x kDirClusterChunks x 8 warp sums.
-template <int K, typename F>
-__device__ __forceinline__ void chunk_pass(const DevTopo& t, int4 r, int rank, int C, int nchunk, ClusterPart* part,
-                                           int par, double* smw, F&& f) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    constexpr int nw = kBlock / 32;
-    __syncthreads();  // the previous pass's reads of smw are done
-    int lc = 0;
-#pragma unroll 2
-    for (int b = rank; b < nchunk; b += C, lc++) {
-        const int4 q = t.nblk[r.x + b];
-        double v[K];
-#pragma unroll
-        for (int k = 0; k < K; k++) v[k] = 0;
-        if (int(threadIdx.x) < q.y) f(q.x + int(threadIdx.x), v);
-#pragma unroll
-        for (int k = 0; k < K; k++) {
-            const double w = warp_sum(v[k]);
-            if (lane == 0) smw[(k * kDirClusterChunks + lc) * nw + warp] = w;
-        }
-    }
-    __syncthreads();
-    for (int i = int(threadIdx.x); i < K * lc; i += blockDim.x) {
-        const int k = i / lc, l = i - k * lc;
-        double sum = 0;
-        for (int w = 0; w < nw; w++) sum += smw[(k * kDirClusterChunks + l) * nw + w];
-        part->v[par][k][l] = sum;
-    }
-}
-
-__global__ void __launch_bounds__(kBlock) k_direction_cluster(DevTopo t, const SolveCtl* __restrict__ ctl,
-                                                              const int2* __restrict__ hist, int H,
-                                                              double* __restrict__ p, const double* __restrict__ g,
-                                                              const double* __restrict__ S,
-                                                              const double* __restrict__ Y, long long stride,
-                                                              const double* __restrict__ rho,
-                                                              double* __restrict__ dg, double mt, double mr) {
-    namespace cg = cooperative_groups;
-    cg::cluster_group cl = cg::this_cluster();
-    extern __shared__ double smw[];  // 3 x kDirClusterChunks x 8 warp sums
-    __shared__ double sm[3 * (kBlock / 32)];
-    __shared__ ClusterPart part;
-    __shared__ double alpha[64];
-    __shared__ double coef_sh;
-    const int C = int(cl.num_blocks()), rank = int(cl.block_rank());
-    const int inst = int(blockIdx.x) / C;
-    const SolveCtl c = load_ctl(ctl, hist, inst);
-    if (!(c.flags & kOpDirection)) return;  // the whole cluster
-    const int4 r = t.irange[inst];
-    const int nchunk = r.y - r.x, m = c.m;
-    int par = 0;
-    // the coefficient of the step the barrier just completed (every CTA forms the same one)
-    auto sum1 = [&](int k0) {
-        double acc[1];
-        cluster_sum<1>(cl, &part, par, k0, nchunk, acc, sm);
-        return acc[0];  // thread 0
-    };
-    // start (k_tl_start): p = g; partials of <s, y>, <y, y> of the newest pair and <s, g>
-    {
-        const int slot = m > 0 ? ring_slot(c, H, m - 1) : 0;
-        const double* sv = hist_slot(S, stride, slot);
-        const double* yv = hist_slot(Y, stride, slot);
-        chunk_pass<3>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[3]) {
-            const size_t o = 6 * size_t(i);
-#pragma unroll
-            for (int d = 0; d < 6; d++) p[o + d] = g[o + d];
-            if (m > 0) {
-                v[0] = dot6(sv + o, yv + o);
-                v[1] = dot6(yv + o, yv + o);
-                v[2] = dot6(sv + o, g + o);
-            }
-        });
-    }
-    cl.sync();
-    double h0acc[2] = {0, 0};
-    if (m > 0) {
-        cluster_sum<2>(cl, &part, par, 0, nchunk, h0acc, sm);
-        const double a = sum1(2);
-        if (threadIdx.x == 0) {
-            const int slot = ring_slot(c, H, m - 1);
-            alpha[m - 1] = rho[size_t(inst) * H + slot] * a;
-        }
-    }
-    par ^= 1;
-    // loop 1, newest first (k_tl_step<1>): p -= alpha_h y_h, then the partial of the next step
-    for (int j = 0; j < m; j++) {
-        const int h = m - 1 - j;
-        __syncthreads();
-        const double k = alpha[h];
-        const double* yv = hist_slot(Y, stride, ring_slot(c, H, h));
-        const bool more = j + 1 < m;
-        const double* sv = hist_slot(S, stride, ring_slot(c, H, more ? h - 1 : h));
-        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
-            const size_t o = 6 * size_t(i);
-            double pn[6];
-#pragma unroll
-            for (int d = 0; d < 6; d++) {
-                pn[d] = p[o + d] - k * yv[o + d];
-                p[o + d] = pn[d];
-            }
-            if (more) v[0] = dot6(sv + o, pn);
-        });
-        if (!more) break;
-        cl.sync();
-        const double a = sum1(0);
-        if (threadIdx.x == 0) alpha[h - 1] = rho[size_t(inst) * H + ring_slot(c, H, h - 1)] * a;
-        par ^= 1;
-    }
-    // H0 (sim.cpp:186) and p *= H0 (k_tl_scale), then the partial of loop 2's first step
-    if (threadIdx.x == 0) {
-        double v = .10;
-        if (m > 0 && h0acc[0] > 1e-20 && h0acc[1] > 1e-20) v = clampd(h0acc[0] / h0acc[1], 1e-7, 1e4);
-        coef_sh = v;
-    }
-    __syncthreads();
-    {
-        const double k = coef_sh;
-        const double* yv = hist_slot(Y, stride, ring_slot(c, H, 0));
-        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
-            const size_t o = 6 * size_t(i);
-            double pn[6];
-#pragma unroll
-            for (int d = 0; d < 6; d++) {
-                pn[d] = p[o + d] * k;
-                p[o + d] = pn[d];
-            }
-            if (m > 0) v[0] = dot6(yv + o, pn);
-        });
-    }
-    // loop 2, oldest first (k_tl_step<2>): p += s_j (alpha_j - beta_j), then the next partial
-    for (int j = 0; j < m; j++) {
-        cl.sync();
-        const double a = sum1(0);
-        if (threadIdx.x == 0) coef_sh = alpha[j] - rho[size_t(inst) * H + ring_slot(c, H, j)] * a;
-        par ^= 1;
-        __syncthreads();
-        const double k = coef_sh;
-        const double* sv = hist_slot(S, stride, ring_slot(c, H, j));
-        const bool more = j + 1 < m;
-        const double* yv = hist_slot(Y, stride, ring_slot(c, H, more ? j + 1 : j));
-        chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
-            const size_t o = 6 * size_t(i);
-            double pn[6];
-#pragma unroll
-            for (int d = 0; d < 6; d++) {
-                pn[d] = p[o + d] + sv[o + d] * k;
-                p[o + d] = pn[d];
-            }
-            if (more) v[0] = dot6(yv + o, pn);
-        });
-    }
-    // finish (k_finish): p = clamp(lock(-p)) (sim.cpp:188-190, 46) and <g, p>, into the buffer
-    // the last pass left (that pass's partials are not read)
-    chunk_pass<1>(t, r, rank, C, nchunk, &part, par, smw, [&](int i, double (&v)[1]) {
-        const size_t o = 6 * size_t(i);
-        const uint8_t* lk = t.locked + o;
-        double w[6];
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            w[d] = -p[o + d];
-            if (lk[d]) w[d] = 0;
-        }
-        const double lt = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
-        if (lt > mt) {
-            const double f = mt / lt;
-            w[0] *= f; w[1] *= f; w[2] *= f;
-        }
-        const double lr = sqrt(w[3] * w[3] + w[4] * w[4] + w[5] * w[5]);
-        if (lr > mr) {
-            const double f = mr / lr;
-            w[3] *= f; w[4] *= f; w[5] *= f;
-        }
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            w[d] = lk[d] ? 0.0 : w[d];
-            p[o + d] = w[d];
-        }
-        v[0] = dot6(g + o, w);
-    });
-    cl.sync();
-    const double gp = sum1(0);
-    if (rank == 0 && threadIdx.x == 0) dg[inst] = gp;
-    cl.sync();  // no CTA leaves while another may still read its shared memory
-}
-
-__global__ void k_cluster_probe(int* out) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) *out = 1;
-}
-
 // ---- decisions the device takes itself ------------------------------------------------------
 // Not a descent direction (sim.cpp:191): steepest descent instead.  For the instances that
 // computed a direction and found dg >= 0: p = clamp(lock(-g)) and the partial of <g, p>.
@@ -817,12 +591,8 @@ void bl_direction_fused(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H
 
 void bl_direction_multi(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
                         const double* S, const double* Y, long long stride, const double* rho, double* alpha,
-                        double* part, double* dg, double mt, double mr, cudaStream_t s, int cluster) {
+                        double* part, double* dg, double mt, double mr, cudaStream_t s) {
     const int nb = t.n_nblk;
-    if (cluster > 0) {
-        launch_direction_cluster(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s, cluster);
-        return;
-    }
     // partials: step dot products ping-pong between part and part + nb; H0's in part + 2 nb
     double* pp[2] = {part, part + size_t(nb)};
     double* h0part = part + 2 * size_t(nb);
@@ -849,9 +619,9 @@ void bl_descent_fix(const DevTopo& t, const SolveCtl* ctl, int2* hist, double* p
 
 void bl_direction(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, bool multi, double* p, const double* g,
                   const double* S, const double* Y, long long stride, const double* rho, double* alpha, double* part,
-                  double* dg, double mt, double mr, cudaStream_t s, int cluster) {
+                  double* dg, double mt, double mr, cudaStream_t s) {
     bl_direction_fused(t, ctl, hist, H, p, g, S, Y, stride, rho, dg, mt, mr, s);
-    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s, cluster);
+    if (multi) bl_direction_multi(t, ctl, hist, H, p, g, S, Y, stride, rho, alpha, part, dg, mt, mr, s);
     bl_descent_fix(t, ctl, hist, p, g, part, dg, mt, mr, s);
 }
 
@@ -880,92 +650,3 @@ void bl_accept(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double*
 
 }  // namespace mcg
 
-namespace mcg {
-
-namespace {
-
-constexpr size_t kClusterWarpSums = 3 * kDirClusterChunks * (kBlock / 32) * sizeof(double);
-
-cudaError_t launch_cluster_kernel_cfg(cudaLaunchConfig_t& cfg, cudaLaunchAttribute& attr, dim3 grid, int C,
-                                      cudaStream_t s) {
-    cfg = cudaLaunchConfig_t{};
-    cfg.gridDim = grid;
-    cfg.blockDim = dim3(kBlock);
-    cfg.stream = s;
-    attr = cudaLaunchAttribute{};
-    attr.id = cudaLaunchAttributeClusterDimension;
-    attr.val.clusterDim.x = unsigned(C);
-    attr.val.clusterDim.y = 1;
-    attr.val.clusterDim.z = 1;
-    cfg.attrs = &attr;
-    cfg.numAttrs = 1;
-    return cudaSuccess;
-}
-
-}  // namespace
-
-void launch_direction_cluster(const DevTopo& t, const SolveCtl* ctl, int2* hist, int H, double* p, const double* g,
-                              const double* S, const double* Y, long long stride, const double* rho, double* dg,
-                              double mt, double mr, cudaStream_t s, int cluster) {
-    cudaLaunchConfig_t cfg;
-    cudaLaunchAttribute attr;
-    launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(t.I * cluster)), cluster, s);
-    cfg.dynamicSmemBytes = kClusterWarpSums;
-    cudaLaunchKernelEx(&cfg, k_direction_cluster, t, ctl, const_cast<const int2*>(hist), H, p, g, S, Y, stride, rho,
-                       dg, mt, mr);
-    note_launches(1);
-}
-
-int direction_cluster_size(int device, cudaStream_t s) {
-    int supported = 0;
-    if (cudaDeviceGetAttribute(&supported, cudaDevAttrClusterLaunch, device) != cudaSuccess || !supported) return 0;
-    for (int C : {16, 8}) {
-        if (C > 8 && cudaFuncSetAttribute(k_direction_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                         cudaSuccess) {
-            cudaGetLastError();
-            continue;
-        }
-        if (cudaFuncSetAttribute(k_direction_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(kClusterWarpSums)) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
-        cudaLaunchConfig_t cfg;
-        cudaLaunchAttribute attr;
-        launch_cluster_kernel_cfg(cfg, attr, dim3(unsigned(C)), C, s);
-        cfg.dynamicSmemBytes = kClusterWarpSums;
-        int clusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&clusters, k_direction_cluster, &cfg) != cudaSuccess || clusters < 1) {
-            cudaGetLastError();
-            continue;
-        }
-        // the launch must also work captured into a graph, as every solver launch is
-        int* scratch = nullptr;
-        if (cudaMallocAsync(&scratch, sizeof(int), s) != cudaSuccess) {
-            cudaGetLastError();
-            return 0;
-        }
-        cudaGraph_t gr = nullptr;
-        cudaGraphExec_t x = nullptr;
-        bool ok = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-        if (ok) {
-            cudaLaunchConfig_t pc;
-            cudaLaunchAttribute pa;
-            launch_cluster_kernel_cfg(pc, pa, dim3(unsigned(C)), C, s);
-            pc.blockDim = dim3(32);
-            const bool launched = cudaLaunchKernelEx(&pc, k_cluster_probe, scratch) == cudaSuccess;
-            ok = cudaStreamEndCapture(s, &gr) == cudaSuccess && launched;
-        }
-        ok = ok && cudaGraphInstantiate(&x, gr, 0) == cudaSuccess;
-        ok = ok && cudaGraphLaunch(x, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
-        if (x) cudaGraphExecDestroy(x);
-        if (gr) cudaGraphDestroy(gr);
-        cudaGetLastError();
-        cudaFreeAsync(scratch, s);
-        cudaStreamSynchronize(s);
-        if (ok) return C;
-    }
-    return 0;
-}
-
-}  // namespace mcg

@@ -348,12 +348,6 @@ int mcg_set_kernel_shapes(mcg_ctx* ctx, int32_t beam_blocks, int32_t gather_bloc
  * could not be built it is switched off, and mcg_last_error then says why. */
 int mcg_set_solver_loop(mcg_ctx* ctx, int device);
 int mcg_solver_loop(mcg_ctx* ctx, int32_t* device);
-/* How the two-loop recursion (sim.cpp:184-187) of a lattice too large for one CTA is
- * launched (no reference counterpart): one_launch != 0 (the default, where the device
- * supports thread-block clusters) runs its 2 H + 2 steps in one launch, one cluster of up to
- * 16 CTAs per lattice exchanging partial sums through distributed shared memory; 0 runs
- * each step as a launch of its own.  The same result bit for bit. */
-int mcg_set_direction_launch(mcg_ctx* ctx, int one_launch);
 /* Time of the device-resident loop's rounds since the upload or the last
  * mcg_set_solver_loop (no reference counterpart): ms4 = {directions, evaluations (with the
  * vectors they read), decisions and accept steps} as device time between the rounds' stage

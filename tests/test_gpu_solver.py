@@ -263,28 +263,3 @@ def test_device_loop_takes_the_host_loops_decisions(mcg, precision):
         res[device] = (z, st, fe, fd)
     assert np.array_equal(res[True][0], res[False][0])
     assert res[True][1] == res[False][1] and res[True][2] == res[False][2] and res[True][3] == res[False][3]
-
-
-def test_one_launch_two_loop_is_the_separate_launches(mcg):
-    """A lattice too large for the one-CTA direction (20x20x20 cubic+BCC, 17,261 nodes: 68
-    node blocks) runs its two-loop recursion in one launch, one thread-block cluster sharing
-    partial sums through distributed shared memory, or as 2 H + 4 separate launches: a
-    minimization takes the same steps bit for bit either way, with the rounds stepped from
-    the host and on the device."""
-    from falling_dice_gb300 import workloads
-    cfg, spec = workloads.bcc((20, 20, 20), contact_stiffness=workloads.CONTACT_STIFF)
-    lat = mcg.generate_lattice(spec, cfg)
-    assert lat.n_nodes > 64 * 256
-    top = lat.geometry.top0 - 0.01 * lat.geometry.height
-    res = []
-    for one_launch, device in ((True, True), (False, True), (True, False)):
-        sol = mcg.Solver(cfg, lat)
-        sol.set_direction_launch(one_launch)
-        sol.set_solver_loop(device)
-        z, st, fe, fd = sol.minimize(top, np.zeros(6 * lat.n_nodes))
-        assert sol.solver_loop()[0] == device
-        res.append((z, st, fe))
-    print("two-loop launches:", res[0][1])
-    assert res[0][1]["iterations"] >= 3
-    for z, st, fe in res[1:]:
-        assert np.array_equal(z, res[0][0]) and st == res[0][1] and fe == res[0][2]
