@@ -43,11 +43,11 @@ NODE_BYTES = 166    # per node, FP64: z[6] + baseX[3] + baseR[4] + mass + grad[6
 # DRAM bytes (read + write, ncu dram__bytes_read.sum + dram__bytes_write.sum) of one launch,
 # captured with ncu on GB300 and scaled to the workload:
 #   k_beams (FP64), 32x32x16 cubic+BCC: 40.35 MB for 184,400 beams, scaled by beam count;
-#   k_beams_mixed, 64x64x32 cubic+BCC: 323.53 MB for 1,458,336 beams, scaled by beam count;
+#   k_beams_mixed, 64x64x32 cubic+BCC: 212.75 MB for 1,458,336 beams, scaled by beam count;
 #   k_bin_pairs, 64x64x32 cubic+BCC at the tuned shapes (4.5 mm cell, 1216 blocks): 107.87 MB
 #   where the algorithmic bytes below come to 123.55 MB, scaled by the algorithmic bytes.
 BEAM_TRAFFIC_PER_BEAM = 40.348160e6 / 184400
-BEAM_TRAFFIC_PER_BEAM_MIXED = 322.980608e6 / 1458336
+BEAM_TRAFFIC_PER_BEAM_MIXED = 212.748800e6 / 1458336
 PAIR_TRAFFIC_PER_ALGORITHMIC_BYTE = 107.870720e6 / 123.545196e6
 BEAM_BYTES_MIXED = 68    # per beam, mixed: a, b (2 x 4 B) + 15 reals as FP32
 NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 + locked[6]
