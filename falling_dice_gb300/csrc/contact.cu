@@ -474,15 +474,29 @@ __device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __r
                                              long long cand_cap, uint2* __restrict__ cand,
                                              uint32_t* __restrict__ ncand, uint32_t* __restrict__ flags) {
     const int half = m >> 1;
-    int src = lane;
     uint32_t bits = 0;
-    for (int k = 1; k <= half; k++) {
-        src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
-        const uint4 r = srec[base + src];
-        const int2 q = snd[base + src];
-        const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
-        const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
-        bits |= uint32_t(active && pair_test(me, o)) << (k - 1);
+    if (m == 32) {
+        // a full group (the common case): partners (lane + k) & 31, every lane active but in
+        // the last round, fully unrolled so that the hit bits' shifts are constants
+#pragma unroll
+        for (int k = 1; k <= 16; k++) {
+            const int src = base + ((lane + k) & 31);
+            const uint4 r = srec[src];
+            const int2 q = snd[src];
+            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
+            const bool hit = pair_test(me, o) && (k < 16 || lane < 16);
+            bits |= uint32_t(hit) << (k - 1);
+        }
+    } else {
+        int src = lane;
+        for (int k = 1; k <= half; k++) {
+            src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
+            const uint4 r = srec[base + src];
+            const int2 q = snd[base + src];
+            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
+            const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
+            bits |= uint32_t(active && pair_test(me, o)) << (k - 1);
+        }
     }
     append_bits(bits, me.id & kIdMask,
                 [&](int k) {
@@ -573,12 +587,22 @@ __global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* _
                     for (int r0 = 32 * (g + 1); r0 < n; r0 += 32) {
                         const int rn = min(32, n - r0);
                         uint32_t bits = 0;
+                        if (rn == 32) {  // a full window: constant shifts
+#pragma unroll
+                            for (int k = 0; k < 32; k++) {
+                                const uint4 q = srec[r0 + k];
+                                const int2 nq = snd[r0 + k];
+                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                                bits |= uint32_t(pair_test(me, o)) << k;
+                            }
+                        } else {
 #pragma unroll 4
-                        for (int k = 0; k < rn; k++) {
-                            const uint4 q = srec[r0 + k];
-                            const int2 nq = snd[r0 + k];
-                            const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                            bits |= uint32_t(pair_test(me, o)) << k;
+                            for (int k = 0; k < rn; k++) {
+                                const uint4 q = srec[r0 + k];
+                                const int2 nq = snd[r0 + k];
+                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                                bits |= uint32_t(pair_test(me, o)) << k;
+                            }
                         }
                         append_bits(bits, me.id & kIdMask, [&](int k) { return srec[r0 + k].x & kIdMask; }, lane,
                                     cand_cap, cand, ncand, flags);
