@@ -217,8 +217,9 @@ __device__ __noinline__ PairHit narrow_phase(const DevTopo& t, const PhysParams&
 
 // ---- candidate-list reuse -------------------------------------------------------------------
 // The list built with boxes inflated by `skin` holds every pair whose boxes overlap at any
-// state where no node has moved more than skin (per axis) from its position at the build:
-// each current box lies inside the inflated box of the build.  flags[1] = rebuild now.
+// state where no node has moved farther than skin (Euclidean, so no farther on any axis)
+// from its position at the build: each current box lies inside the inflated box of the
+// build.  flags[1] = rebuild now.
 // A node's displacement is bounded from its FP32 interval [lo, hi] and the stored lower end
 // of its interval at the build (one FP32 ulp wide at most), rounding upward.
 __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const float4* __restrict__ xf_lo,
@@ -230,11 +231,13 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const f
     if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
     if (i < N && !moved && t.active[t.node_inst[i]]) {
         const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
-        const float d = fmaxf(fmaxf(fmaxf(__fsub_ru(h.x, r.x), __fsub_ru(r.x, l.x)),
-                                    fmaxf(__fsub_ru(h.y, r.y), __fsub_ru(r.y, l.y))),
-                              fmaxf(__fsub_ru(h.z, r.z), __fsub_ru(r.z, l.z)));
+        // per-axis bounds of the move, then its Euclidean length, all rounded upward
         const float ulp = 1.2e-7f * fmaxf(fmaxf(fabsf(r.x), fabsf(r.y)), fabsf(r.z)) + 1e-30f;
-        moved = !(__fadd_ru(d, ulp) <= skin);  // also when not finite
+        const float dx = __fadd_ru(fmaxf(__fsub_ru(h.x, r.x), __fsub_ru(r.x, l.x)), ulp);
+        const float dy = __fadd_ru(fmaxf(__fsub_ru(h.y, r.y), __fsub_ru(r.y, l.y)), ulp);
+        const float dz = __fadd_ru(fmaxf(__fsub_ru(h.z, r.z), __fsub_ru(r.z, l.z)), ulp);
+        const float d2 = __fadd_ru(__fadd_ru(__fmul_ru(dx, dx), __fmul_ru(dy, dy)), __fmul_ru(dz, dz));
+        moved = !(__fsqrt_ru(d2) <= skin);  // also when not finite
     }
     if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(flags + 1, 1u);
 }
@@ -744,8 +747,8 @@ __device__ __forceinline__ int distance_class(const DevTopo& t, const PhysParams
 
 // Candidate filter, once per list build: keeps, in order, the candidates of one
 // instance whose certified distance lower bound at the build does not exceed the pads plus
-// `reach` (2 sqrt(3) skin: two endpoints that each move at most skin per axis close a gap by
-// at most that) and whose nodes are not connected (sim.cpp:24-39).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
+// `reach` (2 skin: every point of a segment whose endpoints move at most skin moves at most
+// skin, so two segments close a gap by at most 2 skin) and whose nodes are not connected (sim.cpp:24-39).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
 // counts): the kept candidates, compacted.
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf,
@@ -978,7 +981,7 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
     if (pairs_end) cudaEventRecord(pairs_end, s);
     // filtered list (only when rebuilding)
     const long long chunks = c.cand_cap / 32;
-    const float reach = skin > 0.f ? 3.4642f * skin : 0.f;  // >= 2 sqrt(3) skin
+    const float reach = skin > 0.f ? 2.0001f * skin : 0.f;  // >= 2 skin
     (k_filter<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.cand_cap, c.cand, c.ncand, reach, c.fbits,
                                                 c.fcount, c.foff, c.cand2, gate), note_launches(1));
     exclusive_scan_u32(c.fcount, c.foff, chunks, c.scan_tmp, s, gate, c.ncand, 31, 5);
