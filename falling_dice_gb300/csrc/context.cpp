@@ -1482,7 +1482,7 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
                             float(kPiD));
         c->mb = mb;
         c->sync();  // ic goes out of scope
-        c->mn = MixedNodes{V.get<float4>(size_t(N)), V.get<float4>(size_t(N)), V.get<float4>(size_t(N))};
+        c->mn = MixedNodes{V.get<float4>(2 * size_t(N)), V.get<float4>(size_t(N))};
     }
     c->ev = e;
     for (int k = 0; k < I; k++) c->hp.tops[k] = ih[size_t(k)].geom.top0;

@@ -210,8 +210,8 @@ struct MixedBeams {
 };
 // Per-node data of the mixed-precision form.
 struct MixedNodes {
-    float4* U;    // increment displacement s t since the base state
-    float4* E;    // increment rotation exp(r) as (w - 1, v)
+    float4* UE;   // [2 N] per node, one 32-byte sector: the increment displacement s t since
+                  // the base state, then the increment rotation exp(r) as (w - 1, v)
     float4* R0f;  // base orientation (w, x, y, z)
 };
 

@@ -170,8 +170,8 @@ __device__ __forceinline__ f3 rotvec_f(float qw, f3 qv) {
 // u = s t (FP32), e = exp(r) as (w - 1, v) (FP32), x = x_base + u (FP64, for contact,
 // platen and centering), FP32 position bounds; block partial sums and extrema of x.
 __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, const double* __restrict__ z,
-                                                        const double* __restrict__ bx, float4* __restrict__ U,
-                                                        float4* __restrict__ Ei, double4_32a* __restrict__ x4,
+                                                        const double* __restrict__ bx, float4* __restrict__ UE,
+                                                        double4_32a* __restrict__ x4,
                                                         float4* __restrict__ xf_lo, float4* __restrict__ xf_hi,
                                                         double* __restrict__ part) {
     __shared__ double sm[3 * kBlock];
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
             tr[d] = li[d] ? 0.f : float(zi[d] * ts);
             r[d] = li[d + 3] ? 0.f : float(zi[d + 3]);
         }
-        U[i] = make_float4(tr[0], tr[1], tr[2], 0.f);
+        UE[2 * size_t(i)] = make_float4(tr[0], tr[1], tr[2], 0.f);
         const float th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
         float wm1, sv;  // cos(th/2) - 1 and sin(th/2)/th
         if (th2 < 1e-6f) {
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(kBlock) k_state_mixed(DevTopo t, double ts, co
             wm1 = -2.f * s4 * s4;
             sv = 2.f * s4 * c4 / th;
         }
-        Ei[i] = make_float4(wm1, r[0] * sv, r[1] * sv, r[2] * sv);
+        UE[2 * size_t(i) + 1] = make_float4(wm1, r[0] * sv, r[1] * sv, r[2] * sv);
         const double xx = bx[3 * size_t(i)] + double(tr[0]);
         const double xy = bx[3 * size_t(i) + 1] + double(tr[1]);
         const double xz = bx[3 * size_t(i) + 2] + double(tr[2]);
@@ -431,9 +431,11 @@ __device__ __forceinline__ void beam_mixed(const Material& mat, const MixedBeams
     }
 }
 
-__device__ __forceinline__ BeamNodes load_nodes(int2 ab, const float4* __restrict__ U, const float4* __restrict__ Ei,
-                                                const float4* __restrict__ R0f) {
-    return BeamNodes{U[ab.x], U[ab.y], Ei[ab.x], Ei[ab.y], R0f[ab.x]};
+// Both halves of a node's increment record share one 32-byte sector.
+__device__ __forceinline__ BeamNodes load_nodes(int2 ab, const float4* __restrict__ UE, const float4* __restrict__ R0f) {
+    const float4* a = UE + 2 * size_t(ab.x);
+    const float4* b = UE + 2 * size_t(ab.y);
+    return BeamNodes{a[0], b[0], a[1], b[1], R0f[ab.x]};
 }
 
 // Block totals: warp 0 sums the elastic and the plastic energies of the block (compensated,
@@ -457,7 +459,7 @@ __device__ __forceinline__ void beam_block_totals(float ue, float up, float* sm,
 // kMinBlocks: the occupancy variant (CTAs per SM), picked by mcg_autotune.
 template <bool kStreamed, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, Material mat, MixedBeams m, int trials,
-                                                        const float4* __restrict__ U, const float4* __restrict__ Ei,
+                                                        const float4* __restrict__ UE,
                                                         const float4* __restrict__ R0f, EvalBufs e) {
     __shared__ float sm[2 * kBlock];  // per-thread elastic and plastic energies
     const MapPos mp = map_pos(t.bblk);
@@ -471,7 +473,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
         const int b = mp.i;
         const int2 ab = t.ab[b];
         const BeamRec R{m.B0[b], m.B1[b], m.B2[b], m.B5[b], m.P0[b], m.P1[b]};
-        const BeamNodes Nd = load_nodes(ab, U, Ei, R0f);
+        const BeamNodes Nd = load_nodes(ab, UE, R0f);
         beam_mixed<kStreamed>(mat, m, trials, e, t.B, b, R, Nd, m.ic[mp.inst], ue, up);
     }
     beam_block_totals(ue, up, sm, e.part_beam + 3 * size_t(blockIdx.x));
@@ -525,8 +527,7 @@ __device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigne
 
 template <bool kStreamed, int kMinBlocks>
 __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed_staged(DevTopo t, Material mat, MixedBeams m,
-                                                                           int trials, const float4* __restrict__ U,
-                                                                           const float4* __restrict__ Ei,
+                                                                           int trials, const float4* __restrict__ UE,
                                                                            const float4* __restrict__ R0f, EvalBufs e) {
     extern __shared__ __align__(128) float4 stage[];  // [2][kStageFields][kBlock]
     __shared__ __align__(8) uint64_t bar[2];
@@ -581,7 +582,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed_staged(DevTo
             if (int(threadIdx.x) < q.y) {
                 const int b = q.x + int(threadIdx.x);
                 const int2 ab = t.ab[b];
-                const BeamNodes Nd = load_nodes(ab, U, Ei, R0f);
+                const BeamNodes Nd = load_nodes(ab, UE, R0f);
                 const float4* st = stage + size_t(i & 1) * kStageFields * kBlock + threadIdx.x;
                 const BeamRec R{st[0], st[kBlock], st[2 * kBlock], st[3 * kBlock], st[4 * kBlock], st[5 * kBlock]};
                 beam_mixed<kStreamed>(mat, m, tr, e, t.B, b, R, Nd, m.ic[q.z], ue, up);
@@ -634,7 +635,7 @@ __global__ void k_f32_to_f64(long long n, const float* __restrict__ a, double* _
 
 void launch_state_mixed(const DevTopo& t, const PhysParams& p, const double* z, const double* base_x,
                         const MixedNodes& mn, EvalBufs& e, cudaStream_t s) {
-    k_state_mixed<<<t.n_nblk, kBlock, 0, s>>>(t, p.translation_scale, z, base_x, mn.U, mn.E, e.x, e.xf_lo, e.xf_hi,
+    k_state_mixed<<<t.n_nblk, kBlock, 0, s>>>(t, p.translation_scale, z, base_x, mn.UE, e.x, e.xf_lo, e.xf_hi,
                                               e.part_state);
     note_launches(1);
     launch_center(t, e, s);
@@ -654,7 +655,7 @@ template <int kMin>
 void launch_staged(const DevTopo& t, const Material& m, const MixedBeams& mb, const MixedNodes& mn, int tr, EvalBufs& e,
                    cudaStream_t s) {
     const int grid = std::min(t.n_bblk, kMin * std::max(g_stage_sms, 1));  // persistent: all resident
-    k_beams_mixed_staged<false, kMin><<<grid, kBlock, kStageBytes, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e);
+    k_beams_mixed_staged<false, kMin><<<grid, kBlock, kStageBytes, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e);
 }
 }  // namespace
 
@@ -669,15 +670,15 @@ void launch_beams_mixed(const DevTopo& t, const Material& m, const MixedBeams& m
     if (t.B == 0) return;
     const int tr = trials;  // 0, 1, or 2: per instance (t.trial_inst)
     if (mb.C0) {
-        k_beams_mixed<true, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e);
+        k_beams_mixed<true, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e);
     } else {
         switch (variant) {
-            case 1: k_beams_mixed<false, kMixedBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
-            case 2: k_beams_mixed<false, kMixedBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
-            case 3: k_beams_mixed<false, kMixedBlocks[3]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            case 1: k_beams_mixed<false, kMixedBlocks[1]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e); break;
+            case 2: k_beams_mixed<false, kMixedBlocks[2]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e); break;
+            case 3: k_beams_mixed<false, kMixedBlocks[3]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e); break;
             case 4: launch_staged<3>(t, m, mb, mn, tr, e, s); break;
             case 5: launch_staged<4>(t, m, mb, mn, tr, e, s); break;
-            default: k_beams_mixed<false, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.U, mn.E, mn.R0f, e); break;
+            default: k_beams_mixed<false, kMixedBlocks[0]><<<t.n_bblk, kBlock, 0, s>>>(t, m, mb, tr, mn.UE, mn.R0f, e); break;
         }
     }
     note_launches(1);
