@@ -378,48 +378,27 @@ __global__ void __launch_bounds__(kBlock) k_shape_prep(DevTopo t, PhysParams p, 
 // Entries of shape s: one per cell of its range, written straight into the bin's slot that
 // the bin counter hands out.  A bin that fills up keeps counting (kOverEntries, and the
 // largest count in nentries[1] so the host can size bin_slots).
-__global__ void __launch_bounds__(kBlock, 4) k_emit(int S, const int* __restrict__ grid, const int4* __restrict__ cell_lo,
+__global__ void __launch_bounds__(kBlock) k_emit(int S, const int* __restrict__ grid, const int4* __restrict__ cell_lo,
                                                  const int4* __restrict__ cell_hi, int bin_slots,
                                                  uint32_t* __restrict__ bin_count, uint32_t* __restrict__ bin_items,
                                                  uint32_t* __restrict__ nentries, uint32_t* __restrict__ flags) {
     if (!flags[1]) return;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= S) return;
-    const int4 lo = cell_lo[s], hi = cell_hi[s];
-    auto put = [&](uint32_t b, uint32_t slot) {
-        if (slot < uint32_t(bin_slots)) {
-            bin_items[size_t(b) * size_t(bin_slots) + slot] = uint32_t(s);
-        } else {
-            atomicOr(flags, uint32_t(kOverEntries));
-            atomicMax(nentries + 1, slot + 1);
-        }
-    };
-    const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
-    const int n = nx > 0 ? nx * ny * nz : 0;  // an empty range has hi.x < lo.x
-    if (n <= 8) {
-        // the common case: all the shape's counter atomics in flight together, then the
-        // stores (the slots' order within a bin does not matter)
-        uint32_t b[8], slot[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-            if (q < n) {
-                const int i = q % nx, r = q / nx;
-                b[q] = bin_of(grid, lo.x + i, lo.y + r / nz, lo.z + r % nz);
-            }
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-            if (q < n) slot[q] = atomicAdd(&bin_count[b[q]], 1u);
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-            if (q < n) put(b[q], slot[q]);
-        return;
+    if (s < S) {
+        const int4 lo = cell_lo[s], hi = cell_hi[s];
+        for (int j = lo.y; j <= hi.y; j++)
+            for (int k = lo.z; k <= hi.z; k++)
+                for (int i = lo.x; i <= hi.x; i++) {
+                    const uint32_t b = bin_of(grid, i, j, k);
+                    const uint32_t slot = atomicAdd(&bin_count[b], 1u);
+                    if (slot < uint32_t(bin_slots)) {
+                        bin_items[size_t(b) * size_t(bin_slots) + slot] = uint32_t(s);
+                    } else {
+                        atomicOr(flags, uint32_t(kOverEntries));
+                        atomicMax(nentries + 1, slot + 1);
+                    }
+                }
     }
-    for (int j = lo.y; j <= hi.y; j++)
-        for (int k = lo.z; k <= hi.z; k++)
-            for (int i = lo.x; i <= hi.x; i++) {
-                const uint32_t bb = bin_of(grid, i, j, k);
-                put(bb, atomicAdd(&bin_count[bb], 1u));
-            }
 }
 
 // One shape as the pair test sees it inside one bin: id with the first-cell flags in the
