@@ -1194,19 +1194,13 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
         beam0 += Bi;
     }
     // incidence CSR in ascending beam order (the reference's scatter order)
-    // and, per beam, the CSR positions of its two ends: the beam kernel writes each end's
-    // 6-vector at its position, so that the gather reads a node's vectors contiguously
     std::vector<int> inc_start(size_t(N) + 1, 0), inc(2 * size_t(B));
-    std::vector<int2> slotpos(static_cast<size_t>(B));
     for (int i = 0; i < N; i++) inc_start[size_t(i) + 1] = inc_start[size_t(i)] + deg[size_t(i)];
     {
         std::vector<int> cur(inc_start.begin(), inc_start.end() - 1);
         for (int b = 0; b < B; b++) {
-            const int pa = cur[size_t(ab[size_t(b)].x)]++;
-            inc[size_t(pa)] = (b << 1) | 0;
-            const int pb = cur[size_t(ab[size_t(b)].y)]++;
-            inc[size_t(pb)] = (b << 1) | 1;
-            slotpos[size_t(b)] = make_int2(pa, pb);
+            inc[size_t(cur[size_t(ab[size_t(b)].x)]++)] = (b << 1) | 0;
+            inc[size_t(cur[size_t(ab[size_t(b)].y)]++)] = (b << 1) | 1;
         }
     }
     // connected pairs as an open-addressing hash set (at most half full)
@@ -1334,9 +1328,6 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     int* di = M.get<int>(inc.size());
     h2d(di, inc.data(), inc.size(), s);
     T.inc = di;
-    int2* dsp = M.get<int2>(slotpos.size());
-    h2d(dsp, slotpos.data(), slotpos.size(), s);
-    T.slotpos = dsp;
     {
         unsigned long long* dh = M.get<unsigned long long>(conn_hash.size());
         h2d(dh, conn_hash.data(), conn_hash.size(), s);
@@ -1452,7 +1443,8 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     e.M = V.get<double4_32a>(3 * size_t(N));
     e.xf_lo = V.get<float4>(size_t(N));
     e.xf_hi = V.get<float4>(size_t(N));
-    e.slot = V.get<double>(12 * size_t(B));
+    e.slotA = V.get<double>(6 * size_t(B));
+    e.slotB = V.get<double>(6 * size_t(B));
     e.part_state = V.get<double>(9 * size_t(T.n_nblk));
     e.part_beam = V.get<double>(3 * size_t(std::max(T.n_bblk, 1)));
     e.err = V.get<unsigned>(1);
@@ -1467,7 +1459,8 @@ void upload_instances(mcg_ctx* c, const std::vector<InstIn>& ins) {
     e.trial_flags = V.get<uint8_t>(3 * size_t(B));
     c->mixed = cf.precision == MCG_MIXED;
     if (c->mixed) {
-        e.slotf = V.get<float>(12 * size_t(B));
+        e.slotAf = V.get<float>(6 * size_t(B));
+        e.slotBf = V.get<float>(6 * size_t(B));
         e.trial_nextf = V.get<float>(7 * size_t(B));
         e.trial_auxf = V.get<float>(7 * size_t(B));
         MixedBeams mb{};

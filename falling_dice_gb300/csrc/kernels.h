@@ -39,7 +39,6 @@ struct DevTopo {
     const uint8_t* locked;    // [6N]
     const int* inc_start;     // [N+1]
     const int* inc;           // [2B]
-    const int2* slotpos;      // [B] CSR positions of the beam's ends a and b
     // connected node pairs (the reference's connected_ set) as an open-addressing hash set
     // of keys u << 32 | v, u <= v; empty slots hold ~0; at most half full
     const unsigned long long* conn_hash;
@@ -172,8 +171,8 @@ struct EvalBufs {
     double4_32a* M;             // [3N] rotation matrix rows of R (x, y, z, pad)
     float4* xf_lo;              // [N] position rounded down to single precision
     float4* xf_hi;              // [N] position rounded up
-    double* slot;           // [12B] per incidence (CSR position): the 6-vector the beam adds
-                            // to the node, (-F, Ga) at end a and (+F, Gb) at end b
+    double* slotA;          // [6B] (-F, Ga) per beam, added to node a
+    double* slotB;          // [6B] (+F, Gb) per beam, added to node b
     double* part_state;     // [9 * nb_nodes] sum, -min, max of x per block
     double* part_beam;      // [3 * nb_beams]
     unsigned* err;          // [1] a kernel's bounded wait gave up (the host reports it)
@@ -187,7 +186,8 @@ struct EvalBufs {
     double* trial_aux;      // [7B] SoA
     uint8_t* trial_flags;   // [3B] SoA
     // mixed-precision form
-    float* slotf;           // [12B] the same in the mixed form
+    float* slotAf;          // [6B]
+    float* slotBf;          // [6B]
     float* trial_nextf;     // [7B] SoA
     float* trial_auxf;      // [7B] SoA
 };

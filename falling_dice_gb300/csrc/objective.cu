@@ -208,9 +208,8 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams(DevTopo t, Materia
         // that a beam at its rest length has exactly zero strain here too
         const d3 d{__dsub_rn(xb.x, xa.x), __dsub_rn(xb.y, xa.y), __dsub_rn(xb.z, xa.z)};
         const double L = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d.x, d.x), __dmul_rn(d.y, d.y)), __dmul_rn(d.z, d.z)));
-        const int2 sp = t.slotpos[b];
-        double* sa = e.slot + 6 * size_t(sp.x);
-        double* sb = e.slot + 6 * size_t(sp.y);
+        double* sa = e.slotA + 6 * size_t(b);
+        double* sb = e.slotB + 6 * size_t(b);
         if (L < 1e-10) {
             // Degenerate element: penalty energy only, no gradient and a default trial.
             acc[0] = 1e8 * sqr(1e-10 - L);
@@ -352,7 +351,8 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
     if (!F32) {
 #pragma unroll 4
         for (int k = k0; k < k1; k++) {
-            const double* s = e.slot + 6 * size_t(k);
+            const int v = t.inc[k];
+            const double* s = ((v & 1) ? e.slotB : e.slotA) + 6 * size_t(v >> 1);
             gx.x += s[0]; gx.y += s[1]; gx.z += s[2];
             gr.x += s[3]; gr.y += s[4]; gr.z += s[5];
         }
@@ -360,7 +360,8 @@ __device__ __forceinline__ void sum_slots(const DevTopo& t, const EvalBufs& e, i
         float hi[6] = {0, 0, 0, 0, 0, 0}, lo[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll 4
         for (int k = k0; k < k1; k++) {
-            const float* s = e.slotf + 6 * size_t(k);
+            const int v = t.inc[k];
+            const float* s = ((v & 1) ? e.slotBf : e.slotAf) + 6 * size_t(v >> 1);
 #pragma unroll
             for (int j = 0; j < 6; j++) {  // two-sum
                 const float a = s[j], sum = hi[j] + a, bp = sum - hi[j];

@@ -316,8 +316,7 @@ struct BeamNodes {
 // into the gradient slots, its trial state when `trials`.
 template <bool kStreamed>
 __device__ __forceinline__ void beam_mixed(const Material& mat, const MixedBeams& m, int trials, EvalBufs& e, int B, int b,
-                                           const int2* __restrict__ slotpos, const BeamRec& R, const BeamNodes& Nd,
-                                           float4 ic, float& ue, float& up) {
+                                           const BeamRec& R, const BeamNodes& Nd, float4 ic, float& ue, float& up) {
     const float4 B0 = R.B0, B1 = R.B1, B2 = R.B2, B5 = R.B5, P0 = R.P0, P1 = R.P1;
     const float4 ua4 = Nd.ua4, ub4 = Nd.ub4, ea = Nd.ea, eb = Nd.eb, ra0 = Nd.ra0;
     const f3 d0 = xyz(B0), du = xyz(ub4) - xyz(ua4);
@@ -325,11 +324,10 @@ __device__ __forceinline__ void beam_mixed(const Material& mat, const MixedBeams
     const float q = c0 + 2.f * fdot(d0, du) + fdot(du, du);  // |d|^2 - L0^2
     const f3 d = d0 + du;
     const float L = sqrtf(fmaxf(L0 * L0 + q, 0.f));
+    float* sa = e.slotAf + 6 * size_t(b);
+    float* sb = e.slotBf + 6 * size_t(b);
     if (L < 1e-10f) {
         ue = 1e8f * (1e-10f - L) * (1e-10f - L);
-        const int2 sp = slotpos[b];  // the ends' CSR positions, loaded where they are written
-        float* sa = e.slotf + 6 * size_t(sp.x);
-        float* sb = e.slotf + 6 * size_t(sp.y);
 #pragma unroll
         for (int k = 0; k < 6; k++) { sa[k] = 0.f; sb[k] = 0.f; }
         if (trials) {
@@ -407,9 +405,6 @@ __device__ __forceinline__ void beam_mixed(const Material& mat, const MixedBeams
         Gb = Gb + world;
         ue = uax + us + ur;
         up = dax + dr;
-        const int2 sp = slotpos[b];  // the ends' CSR positions, loaded where they are written
-        float* sa = e.slotf + 6 * size_t(sp.x);
-        float* sb = e.slotf + 6 * size_t(sp.y);
         sa[0] = -F.x; sa[1] = -F.y; sa[2] = -F.z; sa[3] = Ga.x; sa[4] = Ga.y; sa[5] = Ga.z;
         sb[0] = F.x;  sb[1] = F.y;  sb[2] = F.z;  sb[3] = Gb.x; sb[4] = Gb.y; sb[5] = Gb.z;
         if (trials) {
@@ -479,7 +474,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed(DevTopo t, M
         const int2 ab = t.ab[b];
         const BeamRec R{m.B0[b], m.B1[b], m.B2[b], m.B5[b], m.P0[b], m.P1[b]};
         const BeamNodes Nd = load_nodes(ab, UE, R0f);
-        beam_mixed<kStreamed>(mat, m, trials, e, t.B, b, t.slotpos, R, Nd, m.ic[mp.inst], ue, up);
+        beam_mixed<kStreamed>(mat, m, trials, e, t.B, b, R, Nd, m.ic[mp.inst], ue, up);
     }
     beam_block_totals(ue, up, sm, e.part_beam + 3 * size_t(blockIdx.x));
 }
@@ -590,7 +585,7 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_beams_mixed_staged(DevTo
                 const BeamNodes Nd = load_nodes(ab, UE, R0f);
                 const float4* st = stage + size_t(i & 1) * kStageFields * kBlock + threadIdx.x;
                 const BeamRec R{st[0], st[kBlock], st[2 * kBlock], st[3 * kBlock], st[4 * kBlock], st[5 * kBlock]};
-                beam_mixed<kStreamed>(mat, m, tr, e, t.B, b, t.slotpos, R, Nd, m.ic[q.z], ue, up);
+                beam_mixed<kStreamed>(mat, m, tr, e, t.B, b, R, Nd, m.ic[q.z], ue, up);
             }
             beam_block_totals(ue, up, sm, e.part_beam + 3 * size_t(vb));
         }
