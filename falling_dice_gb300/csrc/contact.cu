@@ -227,8 +227,12 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const f
                                                        const float4* __restrict__ xref, float skin,
                                                        uint32_t* __restrict__ flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!(skin > 0.f)) {  // no reuse: every evaluation builds, no position to compare
+        if (i == 0) atomicOr(flags + 1, 1u);
+        return;
+    }
     bool moved = false;
-    if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
+    if (i == 0 && flags[2]) moved = true;
     if (i < N && !moved && t.active[t.node_inst[i]]) {
         const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
         // per-axis bounds of the move, then its Euclidean length, all rounded upward
@@ -256,18 +260,11 @@ __global__ void __launch_bounds__(kBlock) k_skin_commit(int N, const float4* __r
         flags[2] = (flags[0] & uint32_t(kOverEntries | kOverBins | kOverSpan | kOverCandidates)) ? 1u : 0u;
 }
 
-__global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __restrict__ a,
-                                                       const uint32_t* __restrict__ gate) {
-    if (!*gate) return;
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-        a[k] = 0;
-}
 
 // ---- kernels -------------------------------------------------------------------------------
 // Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
-__global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
-                              uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
+__device__ void grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
+                            uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
     flags[4]++;  // builds since the buffers were allocated
     *ncand = 0;  // the candidate list and entry counts of this build
     nentries[0] = 0;
@@ -315,6 +312,18 @@ __global__ void k_grid_params(const double* __restrict__ cen, double pad, double
     grid[6] = mode;
     grid[7] = ok ? 1 : 0;
     grid[8] = ok ? int(nb) : 0;
+}
+
+// The start of a list build (when flags[1]): the bins' counters zeroed and, by block 0's
+// thread 0, the grid's origin, extent and numbering (grid_params).
+__global__ void __launch_bounds__(kBlock) k_build_begin(long long n, uint32_t* __restrict__ bin_count,
+                                                        const double* __restrict__ cen, double pad, double cell,
+                                                        long long bin_cap, int* grid, uint32_t* flags,
+                                                        uint32_t* ncand, uint32_t* nentries) {
+    if (!flags[1]) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) grid_params(cen, pad, cell, bin_cap, grid, flags, ncand, nentries);
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        bin_count[k] = 0;
 }
 
 // Per-shape bounding box and cell range, in single precision rounded outward: the box
@@ -947,14 +956,13 @@ int contact_pair_blocks(long long shapes) {
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
                      float skin, cudaStream_t s, cudaEvent_t pairs_begin, cudaEvent_t pairs_end) {
     const int S = t.N + t.B;
-    const uint32_t* gate = c.flags + 1;
     cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
     cudaMemsetAsync(c.flags + 3, 0, sizeof(uint32_t), s);  // the pair pass's bin cursor
     (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t, t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
     // candidate list (only when rebuilding)
-    (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
-    (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
-                                    c.bin_cap, c.grid, c.flags, c.ncand, c.nentries),
+    (k_build_begin<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, e.cen + 9 * size_t(t.I),
+                                                  pad + double(skin > 0.f ? skin : 0.f), p.broad_cell, c.bin_cap,
+                                                  c.grid, c.flags, c.ncand, c.nentries),
      note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
                                                  skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
