@@ -194,6 +194,9 @@ int mcg_objective(mcg_ctx* ctx, const double* z, double top, int trials, double*
  * calls on a device share the array, which keeps the last call's contents: calls that
  * overlap on the GPU race.  After such a call mcg_contact_pairs and mcg_contact_stats
  * return MCG_ERR_STATE until the next allocating evaluation (its contacts are not kept).
+ * A call made while another stream captures a CUDA graph (in relaxed capture mode, or in
+ * thread-local mode from a thread other than the capturing one) runs at once on the
+ * context's own stream and returns its results: none of its work enters that graph.
  * No counterpart in the reference. */
 int mcg_objective_noalloc(mcg_ctx* ctx, const double* z, double top, double* energy, double* grad,
                           mcg_diag* diag);

@@ -135,3 +135,41 @@ def test_contact_queries_refuse_after_a_noalloc_evaluation(mcg):
     assert e.value.status == abi.MCG_ERR_STATE
     sol.objective(s["z"], s["top"])  # an allocating evaluation makes them current again
     assert np.array_equal(sol.contact_pairs(), s["pairs"])
+
+
+def test_noalloc_runs_beside_a_graph_capture_and_adds_nothing_to_it(mcg):
+    """A caller may evaluate while one of its streams captures a CUDA graph: in relaxed
+    capture mode on the capturing thread, and in thread-local mode from another thread.  The
+    evaluation runs at once with unchanged results, and the capture still ends in a graph
+    that holds only the caller's own work."""
+    torch = pytest.importorskip("torch")
+    import threading
+
+    g = golden("ref242")
+    s = g.state(3)
+    sol = mcg.Solver(g.cfg, g.lattice)
+    sol.set_state(plastic=s["plastic"])
+    rc, e0, g0, _ = noalloc(sol, s["z"], s["top"])  # sets up before any capture
+    assert rc == abi.MCG_OK, sol.lib.mcg_last_error(sol.h)
+    x = torch.zeros(256, device="cuda")
+    got = []
+    for mode in ("relaxed", "thread_local"):
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, capture_error_mode=mode):
+            x.add_(1.0)
+            if mode == "relaxed":
+                got.append(noalloc(sol, s["z"], s["top"]))
+            else:
+                t = threading.Thread(target=lambda: got.append(noalloc(sol, s["z"], s["top"])))
+                t.start()
+                t.join()
+            assert torch.cuda.is_current_stream_capturing()
+            x.add_(1.0)
+        x.zero_()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.all(x == 2.0).item(), mode  # the graph holds the two additions only
+    for rc, energy, grad, _ in got:
+        assert rc == abi.MCG_OK, sol.lib.mcg_last_error(sol.h)
+        assert abs(energy - e0) <= 1e-14 * abs(e0)
+        assert rel_err(grad, g0) <= 1e-14
