@@ -51,11 +51,10 @@ BEAM_TRAFFIC_PER_BEAM_MIXED = 212.748800e6 / 1458336
 PAIR_TRAFFIC_PER_ALGORITHMIC_BYTE = 107.870720e6 / 123.545196e6
 BEAM_BYTES_MIXED = 68    # per beam, mixed: a, b (2 x 4 B) + 15 reals as FP32
 NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 + locked[6]
-# Pair enumeration with the list build's filter (k_bin_pairs), algorithmic bytes: every cell
-# entry's shape id (4 B), each shape's pair-test record once (16 B box/cell record + 8 B
-# nodes), each node's FP32 position once (16 B, the filter's distance bounds), each occupied
-# bin's count, start and list slot (12 B), each kept candidate written (8 B).
-PAIR_ENTRY_BYTES, PAIR_SHAPE_BYTES, PAIR_NODE_BYTES, PAIR_BIN_BYTES, PAIR_CAND_BYTES = 4, 24, 16, 12, 8
+# Pair enumeration (k_bin_pairs), algorithmic bytes: every cell entry's shape id (4 B), each
+# shape's pair-test record once (16 B box/cell record + 8 B nodes), each occupied bin's
+# count, start and list slot (12 B), each candidate written (8 B).
+PAIR_ENTRY_BYTES, PAIR_SHAPE_BYTES, PAIR_BIN_BYTES, PAIR_CAND_BYTES = 4, 24, 12, 8
 
 
 def parse():
@@ -391,8 +390,8 @@ def main():
 
     def roofline_pairs(r):
         st = r["contact_stats"]
-        nbytes = (PAIR_ENTRY_BYTES * st["entries"] + PAIR_SHAPE_BYTES * (N + B) + PAIR_NODE_BYTES * N +
-                  PAIR_BIN_BYTES * st["occupied_bins"] + PAIR_CAND_BYTES * st["filtered"])
+        nbytes = (PAIR_ENTRY_BYTES * st["entries"] + PAIR_SHAPE_BYTES * (N + B) +
+                  PAIR_BIN_BYTES * st["occupied_bins"] + PAIR_CAND_BYTES * st["candidates"])
         ms = r["phases"]["pairs"]
         ach = nbytes / (ms * 1e-3) / 1e9
         return {"bound": "hbm", "kernel": "k_bin_pairs", "achieved": ach, "peak": peak, "unit": "GB/s",

@@ -227,12 +227,8 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const f
                                                        const float4* __restrict__ xref, float skin,
                                                        uint32_t* __restrict__ flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (!(skin > 0.f)) {  // no reuse: every evaluation builds, no position to compare
-        if (i == 0) atomicOr(flags + 1, 1u);
-        return;
-    }
     bool moved = false;
-    if (i == 0 && flags[2]) moved = true;
+    if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
     if (i < N && !moved && t.active[t.node_inst[i]]) {
         const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
         // per-axis bounds of the move, then its Euclidean length, all rounded upward
@@ -260,17 +256,23 @@ __global__ void __launch_bounds__(kBlock) k_skin_commit(int N, const float4* __r
         flags[2] = (flags[0] & uint32_t(kOverEntries | kOverBins | kOverSpan | kOverCandidates)) ? 1u : 0u;
 }
 
+__global__ void __launch_bounds__(kBlock) k_zero_gated(long long n, uint32_t* __restrict__ a,
+                                                       const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+        a[k] = 0;
+}
 
 // ---- kernels -------------------------------------------------------------------------------
 // Grid origin, extent and bin numbering from the node bounding box (e.cen[3..8]).
-__device__ void grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
-                            uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
+__global__ void k_grid_params(const double* __restrict__ cen, double pad, double cell, long long bin_cap, int* grid,
+                              uint32_t* flags, uint32_t* ncand, uint32_t* nentries) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || !flags[1]) return;
     flags[4]++;  // builds since the buffers were allocated
     *ncand = 0;  // the candidate list and entry counts of this build
     nentries[0] = 0;
     nentries[1] = 0;
     nentries[2] = 0;
-    nentries[3] = 0;
     bool ok = true;
     long long lo[3], dim[3];
     for (int d = 0; d < 3; d++) {
@@ -312,18 +314,6 @@ __device__ void grid_params(const double* __restrict__ cen, double pad, double c
     grid[6] = mode;
     grid[7] = ok ? 1 : 0;
     grid[8] = ok ? int(nb) : 0;
-}
-
-// The start of a list build (when flags[1]): the bins' counters zeroed and, by block 0's
-// thread 0, the grid's origin, extent and numbering (grid_params).
-__global__ void __launch_bounds__(kBlock) k_build_begin(long long n, uint32_t* __restrict__ bin_count,
-                                                        const double* __restrict__ cen, double pad, double cell,
-                                                        long long bin_cap, int* grid, uint32_t* flags,
-                                                        uint32_t* ncand, uint32_t* nentries) {
-    if (!flags[1]) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) grid_params(cen, pad, cell, bin_cap, grid, flags, ncand, nentries);
-    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
-        bin_count[k] = 0;
 }
 
 // Per-shape bounding box and cell range, in single precision rounded outward: the box
@@ -445,6 +435,231 @@ __device__ __forceinline__ bool pair_test(const PairRec& A, const PairRec& B) {
 
 constexpr uint32_t kIdMask = (1u << kShapeBits) - 1u;
 
+// Appends every lane's hits to the flat candidate list: lane l's hits are the set bits of
+// `bits`, bit k standing for its pair with the record partner(k) returns; the lanes' counts
+// are placed by a warp scan behind one atomic on ncand.  Past cand_cap the pairs are counted
+// but not stored and kOverCandidates is raised.  All lanes of the warp call it.
+template <typename Partner>
+__device__ __forceinline__ void append_bits(uint32_t bits, uint32_t me, Partner partner, int lane,
+                                            long long cand_cap, uint2* __restrict__ cand,
+                                            uint32_t* __restrict__ ncand, uint32_t* __restrict__ flags) {
+    const uint32_t cnt = uint32_t(__popc(bits));
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;  // warp-uniform
+    uint32_t base = 0;
+    if (lane == 0) {
+        base = atomicAdd(ncand, total);
+        if ((long long)base + total > cand_cap) atomicOr(flags, uint32_t(kOverCandidates));
+    }
+    long long at = (long long)__shfl_sync(0xffffffffu, base, 0) + (incl - cnt);
+    while (bits) {
+        const int k = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const uint32_t o = partner(k);
+        if (at < cand_cap) cand[at] = make_uint2(min(me, o), max(me, o));
+        at++;
+    }
+}
+
+// Every unordered pair of the records at ranks base .. base + m - 1 (m <= 32; lane i holds
+// rank base + i in `me`, and all of them are staged in shared memory), by rotation: in
+// round k lane i meets rank base + (i + k) mod m, k = 1 .. m/2 (the last round of an even m
+// only from the lower half), the partner's record read from shared memory.  Hits are kept as
+// one bit per round and appended at the end.
+__device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __restrict__ srec,
+                                             const int2* __restrict__ snd, int base, int m, int lane,
+                                             long long cand_cap, uint2* __restrict__ cand,
+                                             uint32_t* __restrict__ ncand, uint32_t* __restrict__ flags) {
+    const int half = m >> 1;
+    uint32_t bits = 0;
+    if (m == 32) {
+        // a full group (the common case): partners (lane + k) & 31, every lane active but in
+        // the last round, fully unrolled so that the hit bits' shifts are constants
+#pragma unroll
+        for (int k = 1; k <= 16; k++) {
+            const int src = base + ((lane + k) & 31);
+            const uint4 r = srec[src];
+            const int2 q = snd[src];
+            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
+            const bool hit = pair_test(me, o) && (k < 16 || lane < 16);
+            bits |= uint32_t(hit) << (k - 1);
+        }
+    } else {
+        int src = lane;
+        for (int k = 1; k <= half; k++) {
+            src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
+            const uint4 r = srec[base + src];
+            const int2 q = snd[base + src];
+            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
+            const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
+            bits |= uint32_t(active && pair_test(me, o)) << (k - 1);
+        }
+    }
+    append_bits(bits, me.id & kIdMask,
+                [&](int k) {
+                    int j = lane + k + 1;
+                    j = j >= m ? j - m : j;
+                    return srec[base + j].x & kIdMask;
+                },
+                lane, cand_cap, cand, ncand, flags);
+}
+
+// Candidate pairs of every bin holding two or more shapes.  Warps claim the grid's bins
+// kPairGrab at a time (single bins near the end) from a cursor (flags[3]) and skip the empty
+// ones (one ballot), so bins of uneven size balance over the grid; they count the build's
+// cell entries and occupied bins into nentries[0] and [2] on the way, and append their
+// candidate pairs (lower shape, higher shape) to the flat list in warp-sized batches, one
+// atomic on ncand per batch, without a counting pass.  The list's length is the number of
+// pairs, whatever the order.
+// Enumeration inside a bin, entries in bin order:
+//   n <= 128  the entries in groups of 32, lane i holding entry 32 g + i of group g and every
+//             record staged in shared memory: the pairs inside each group by rotation
+//             (rotate_pairs), then each full group against every record of the later groups
+//             (one record read by all lanes per round), hits kept as bits over windows of 32
+//             partners;
+//   larger    the same by groups of 32: each group is staged in turn and then meets every
+//             later group, staged 32 records at a time.
+__global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
+                                                      const uint32_t* __restrict__ bin_count, int bin_slots,
+                                                      uint32_t* __restrict__ nentries,
+                                                      const uint32_t* __restrict__ bin_items,
+                                                      const uint4* __restrict__ rec, long long cand_cap,
+                                                      uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
+                                                      uint32_t* __restrict__ flags) {
+    __shared__ uint4 rec_all[kPairWarps][kPairRanks];  // the bin's records, staged for the partner reads
+    __shared__ int2 nd_all[kPairWarps][kPairRanks];
+    if (!flags[1]) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t nbins = uint32_t(grid[8]);
+    uint4* srec = rec_all[w];
+    int2* snd = nd_all[w];
+    uint32_t* cursor = flags + 3;
+    auto stage_rec = [&](const PairRec& r, int rank) {
+        srec[rank] = make_uint4(r.id, r.w0, r.w1, r.w2);
+        snd[rank] = make_int2(r.n0, r.n1);
+    };
+    uint32_t entries = 0, occupied = 0;  // this lane's share of the build's counts
+    // kPairGrab bins per claim, then single bins for the last 4 per warp of the grid, so that
+    // a few heavy bins do not end up queued behind one warp
+    const uint32_t tail = 4u * gridDim.x * kPairWarps;
+    const uint32_t single_from = nbins > tail ? nbins - tail : 0u;
+    uint32_t grab = kPairGrab;  // warp-uniform
+    for (;;) {
+        uint32_t b0 = 0;
+        if (lane == 0) b0 = atomicAdd(cursor, grab);
+        b0 = __shfl_sync(0xffffffffu, b0, 0);
+        if (b0 >= nbins) break;
+        const uint32_t cnt = lane < int(grab) && b0 + lane < nbins ? bin_count[b0 + lane] : 0u;
+        if (b0 + grab >= single_from) grab = 1;
+        entries += cnt;
+        unsigned todo = __ballot_sync(0xffffffffu, cnt >= 2);  // the claimed bins holding pairs
+        occupied += lane == 0 ? uint32_t(__popc(todo)) : 0u;
+        while (todo) {
+            const int j = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t b = b0 + uint32_t(j);
+            // a full bin repeats the build (kOverEntries), so clamping only keeps reads in bounds
+            const int n = int(min(__shfl_sync(0xffffffffu, cnt, j), uint32_t(bin_slots)));
+            const uint32_t* items = bin_items + size_t(b) * size_t(bin_slots);
+            const int3 cc = cell_of(grid, b);
+            const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
+            __syncwarp();  // the previous bin's partner reads are done
+            if (n <= kPairRanks) {
+                // ranks 32 g + lane in group g = 0 .. G-1, all staged in shared memory
+                const int G = (n + 31) >> 5;
+                for (int g = 0; g < G; g++)
+                    if (32 * g + lane < n) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), 32 * g + lane);
+                __syncwarp();
+                for (int g = 0; g < G; g++) {
+                    const int mg = min(32, n - 32 * g);
+                    PairRec me{};
+                    if (lane < mg) {
+                        const uint4 q = srec[32 * g + lane];
+                        const int2 nq = snd[32 * g + lane];
+                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                    }
+                    rotate_pairs(me, srec, snd, 32 * g, mg, lane, cand_cap, cand, ncand, flags);  // within group g
+                    // group g (full: a later group exists) against the records of the later
+                    // groups, 32 partners per window of hit bits
+                    for (int r0 = 32 * (g + 1); r0 < n; r0 += 32) {
+                        const int rn = min(32, n - r0);
+                        uint32_t bits = 0;
+                        if (rn == 32) {  // a full window: constant shifts
+#pragma unroll
+                            for (int k = 0; k < 32; k++) {
+                                const uint4 q = srec[r0 + k];
+                                const int2 nq = snd[r0 + k];
+                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                                bits |= uint32_t(pair_test(me, o)) << k;
+                            }
+                        } else {
+#pragma unroll 4
+                            for (int k = 0; k < rn; k++) {
+                                const uint4 q = srec[r0 + k];
+                                const int2 nq = snd[r0 + k];
+                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                                bits |= uint32_t(pair_test(me, o)) << k;
+                            }
+                        }
+                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[r0 + k].x & kIdMask; }, lane,
+                                    cand_cap, cand, ncand, flags);
+                    }
+                }
+            } else {
+                // large bin: its groups of 32 entries in turn.  Group g is staged in shared
+                // ranks 0..31 (lane i holding entry 32 g + i) and its pairs found by
+                // rotation; each later group is then staged in ranks 32..63 and met 32
+                // partners per window of hit bits.  A group with a later group is full, so
+                // every lane holds an entry there.
+                const int G = (n + 31) >> 5;
+                for (int g = 0; g < G; g++) {
+                    const int mg = min(32, n - 32 * g);
+                    __syncwarp();  // the previous group's partner reads are done
+                    if (lane < mg) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), lane);
+                    __syncwarp();
+                    PairRec me{};
+                    if (lane < mg) {
+                        const uint4 q = srec[lane];
+                        const int2 nq = snd[lane];
+                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                    }
+                    rotate_pairs(me, srec, snd, 0, mg, lane, cand_cap, cand, ncand, flags);
+                    for (int h = g + 1; h < G; h++) {
+                        const int rn = min(32, n - 32 * h);
+                        __syncwarp();
+                        if (lane < rn) stage_rec(load_rec(t, items[32 * h + lane], rec, ccp), 32 + lane);
+                        __syncwarp();
+                        uint32_t bits = 0;
+#pragma unroll 4
+                        for (int k = 0; k < rn; k++) {
+                            const uint4 q = srec[32 + k];
+                            const int2 nq = snd[32 + k];
+                            const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
+                            bits |= uint32_t(pair_test(me, o)) << k;
+                        }
+                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[32 + k].x & kIdMask; }, lane,
+                                    cand_cap, cand, ncand, flags);
+                    }
+                }
+                __syncwarp();
+            }
+        }
+    }
+    entries = __reduce_add_sync(0xffffffffu, entries);
+    if (lane == 0) {
+        if (entries) atomicAdd(nentries, entries);
+        if (occupied) atomicAdd(nentries + 2, occupied);
+    }
+}
+
+
+
 // Certified single-precision distance bounds of a candidate pair.  A pair certainly farther
 // apart than pad_a + pad_b (>= the reference's target ra + rb + margin) fails the reference's
 // test dist < target; a pair certainly closer than the target passes it.
@@ -530,278 +745,67 @@ __device__ __forceinline__ int distance_class(const DevTopo& t, const PhysParams
     return d.far_ok && d.far > d.pad_sum ? -1 : 0;
 }
 
-// The list build's filter of a box-overlapping pair (sa < sb) that shares no node: kept when
-// both shapes belong to one instance, their certified distance lower bound at the build does
-// not exceed the pads plus `reach` (2 skin: every point of a segment whose endpoints move at
-// most skin moves at most skin, so two segments close a gap by at most 2 skin), and their
-// nodes are not connected (sim.cpp:24-39; local pairs never make contact, so the narrow
-// phase of every evaluation needs no hash lookups).
-struct CandFilter {
-    PhysParams p;
-    const float4* __restrict__ xf;  // FP32 positions rounded down
-    float reach;
-    uint32_t* __restrict__ tested;  // [1] box-overlapping pairs seen (statistics)
-};
-__device__ __forceinline__ bool keep_pair(const DevTopo& t, const CandFilter& f, uint32_t sa, uint32_t sb) {
-    const int2 na = shape_nodes(t, sa), nb = shape_nodes(t, sb);
-    if (t.node_inst[na.x] != t.node_inst[nb.x]) return false;
-    const DistBounds d = dist_bounds(t, f.p, f.xf, sa, sb);
-    if (d.far_ok && d.far > d.pad_sum + f.reach) return false;
-    return !any_connected(t, na, nb);
-}
-
-// Appends every lane's kept hits to the flat candidate list: lane l's hits are the set bits
-// of `bits`, bit k standing for its pair with the record partner(k) returns; each hit passes
-// the build's filter (keep_pair) first; the lanes' counts are placed by a warp scan behind
-// one atomic on ncand.  Past cand_cap the pairs are counted but not stored and
-// kOverCandidates is raised.  All lanes of the warp call it.
-template <typename Partner>
-__device__ __forceinline__ void append_bits(uint32_t bits, uint32_t me, Partner partner, int lane,
-                                            const DevTopo& t, const CandFilter& filt, long long cand_cap,
-                                            uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
-                                            uint32_t* __restrict__ flags) {
-    const uint32_t hits = __reduce_add_sync(0xffffffffu, uint32_t(__popc(bits)));
-    if (hits == 0) return;  // warp-uniform
-    if (lane == 0) atomicAdd(filt.tested, hits);
-    uint32_t kept = 0;
-    for (uint32_t r = bits; r; r &= r - 1) {
-        const int k = __ffs(r) - 1;
-        const uint32_t o = partner(k);
-        if (keep_pair(t, filt, min(me, o), max(me, o))) kept |= 1u << k;
-    }
-    bits = kept;
-    const uint32_t cnt = uint32_t(__popc(bits));
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += v;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) return;  // warp-uniform
-    uint32_t base = 0;
-    if (lane == 0) {
-        base = atomicAdd(ncand, total);
-        if ((long long)base + total > cand_cap) atomicOr(flags, uint32_t(kOverCandidates));
-    }
-    long long at = (long long)__shfl_sync(0xffffffffu, base, 0) + (incl - cnt);
-    while (bits) {
-        const int k = __ffs(bits) - 1;
-        bits &= bits - 1;
-        const uint32_t o = partner(k);
-        if (at < cand_cap) cand[at] = make_uint2(min(me, o), max(me, o));
-        at++;
-    }
-}
-
-// Every unordered pair of the records at ranks base .. base + m - 1 (m <= 32; lane i holds
-// rank base + i in `me`, and all of them are staged in shared memory), by rotation: in
-// round k lane i meets rank base + (i + k) mod m, k = 1 .. m/2 (the last round of an even m
-// only from the lower half), the partner's record read from shared memory.  Hits are kept as
-// one bit per round and appended at the end.
-__device__ __forceinline__ void rotate_pairs(const PairRec& me, const uint4* __restrict__ srec,
-                                             const int2* __restrict__ snd, int base, int m, int lane,
-                                             const DevTopo& t, const CandFilter& filt, long long cand_cap,
-                                             uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
-                                             uint32_t* __restrict__ flags) {
-    const int half = m >> 1;
-    uint32_t bits = 0;
-    if (m == 32) {
-        // a full group (the common case): partners (lane + k) & 31, every lane active but in
-        // the last round, fully unrolled so that the hit bits' shifts are constants
-#pragma unroll
-        for (int k = 1; k <= 16; k++) {
-            const int src = base + ((lane + k) & 31);
-            const uint4 r = srec[src];
-            const int2 q = snd[src];
-            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
-            const bool hit = pair_test(me, o) && (k < 16 || lane < 16);
-            bits |= uint32_t(hit) << (k - 1);
+// Candidate filter, once per list build: keeps, in order, the candidates of one
+// instance whose certified distance lower bound at the build does not exceed the pads plus
+// `reach` (2 skin: every point of a segment whose endpoints move at most skin moves at most
+// skin, so two segments close a gap by at most 2 skin) and whose nodes are not connected (sim.cpp:24-39).  Pass 0: keep bits and counts per chunk of 32; pass 1 (after a scan of the
+// counts): the kept candidates, compacted.
+template <int pass>
+__global__ void __launch_bounds__(kBlock) k_filter(DevTopo t, PhysParams p, const float4* __restrict__ xf,
+                                                   long long cand_cap, const uint2* __restrict__ cand,
+                                                   const uint32_t* __restrict__ ncand, float reach,
+                                                   uint32_t* __restrict__ fbits, uint32_t* __restrict__ fcount,
+                                                   const uint32_t* __restrict__ foff, uint2* __restrict__ cand2,
+                                                   const uint32_t* __restrict__ gate) {
+    if (!*gate) return;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const uint32_t total = uint32_t(min((long long)*ncand, cand_cap));
+    const long long nchunk = (total + 31) / 32;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
+        const uint32_t g = uint32_t(ch * 32 + lane);
+        if constexpr (pass == 1) {
+            if (!fbits[ch]) continue;  // warp-uniform
         }
-    } else {
-        int src = lane;
-        for (int k = 1; k <= half; k++) {
-            src = src + 1 < m ? src + 1 : 0;  // (lane + k) mod m for lanes below m
-            const uint4 r = srec[base + src];
-            const int2 q = snd[base + src];
-            const PairRec o{r.x, r.y, r.z, r.w, q.x, q.y};
-            const bool active = lane < m && !((m & 1) == 0 && k == half && lane >= half);
-            bits |= uint32_t(active && pair_test(me, o)) << (k - 1);
-        }
-    }
-    append_bits(bits, me.id & kIdMask,
-                [&](int k) {
-                    int j = lane + k + 1;
-                    j = j >= m ? j - m : j;
-                    return srec[base + j].x & kIdMask;
-                },
-                lane, t, filt, cand_cap, cand, ncand, flags);
-}
-
-// Candidate pairs of every bin holding two or more shapes.  Warps claim the grid's bins
-// kPairGrab at a time (single bins near the end) from a cursor (flags[3]) and skip the empty
-// ones (one ballot), so bins of uneven size balance over the grid; they count the build's
-// cell entries and occupied bins into nentries[0] and [2] on the way, and append their
-// candidate pairs (lower shape, higher shape) to the flat list in warp-sized batches, one
-// atomic on ncand per batch, without a counting pass.  The list's length is the number of
-// pairs, whatever the order.
-// Enumeration inside a bin, entries in bin order:
-//   n <= 128  the entries in groups of 32, lane i holding entry 32 g + i of group g and every
-//             record staged in shared memory: the pairs inside each group by rotation
-//             (rotate_pairs), then each full group against every record of the later groups
-//             (one record read by all lanes per round), hits kept as bits over windows of 32
-//             partners;
-//   larger    the same by groups of 32: each group is staged in turn and then meets every
-//             later group, staged 32 records at a time.
-__global__ void __launch_bounds__(kBlock, 6) k_bin_pairs(DevTopo t, const int* __restrict__ grid,
-                                                      const uint32_t* __restrict__ bin_count, int bin_slots,
-                                                      uint32_t* __restrict__ nentries,
-                                                      const uint32_t* __restrict__ bin_items,
-                                                      const uint4* __restrict__ rec, long long cand_cap,
-                                                      uint2* __restrict__ cand, uint32_t* __restrict__ ncand,
-                                                      uint32_t* __restrict__ flags, CandFilter filt) {
-    __shared__ uint4 rec_all[kPairWarps][kPairRanks];  // the bin's records, staged for the partner reads
-    __shared__ int2 nd_all[kPairWarps][kPairRanks];
-    if (!flags[1]) return;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t nbins = uint32_t(grid[8]);
-    uint4* srec = rec_all[w];
-    int2* snd = nd_all[w];
-    uint32_t* cursor = flags + 3;
-    auto stage_rec = [&](const PairRec& r, int rank) {
-        srec[rank] = make_uint4(r.id, r.w0, r.w1, r.w2);
-        snd[rank] = make_int2(r.n0, r.n1);
-    };
-    uint32_t entries = 0, occupied = 0;  // this lane's share of the build's counts
-    // kPairGrab bins per claim, then single bins for the last 4 per warp of the grid, so that
-    // a few heavy bins do not end up queued behind one warp
-    const uint32_t tail = 4u * gridDim.x * kPairWarps;
-    const uint32_t single_from = nbins > tail ? nbins - tail : 0u;
-    uint32_t grab = kPairGrab;  // warp-uniform
-    for (;;) {
-        uint32_t b0 = 0;
-        if (lane == 0) b0 = atomicAdd(cursor, grab);
-        b0 = __shfl_sync(0xffffffffu, b0, 0);
-        if (b0 >= nbins) break;
-        const uint32_t cnt = lane < int(grab) && b0 + lane < nbins ? bin_count[b0 + lane] : 0u;
-        if (b0 + grab >= single_from) grab = 1;
-        entries += cnt;
-        unsigned todo = __ballot_sync(0xffffffffu, cnt >= 2);  // the claimed bins holding pairs
-        occupied += lane == 0 ? uint32_t(__popc(todo)) : 0u;
-        while (todo) {
-            const int j = __ffs(todo) - 1;
-            todo &= todo - 1;
-            const uint32_t b = b0 + uint32_t(j);
-            // a full bin repeats the build (kOverEntries), so clamping only keeps reads in bounds
-            const int n = int(min(__shfl_sync(0xffffffffu, cnt, j), uint32_t(bin_slots)));
-            const uint32_t* items = bin_items + size_t(b) * size_t(bin_slots);
-            const int3 cc = cell_of(grid, b);
-            const uint32_t ccp = pack_cell(cc.x, cc.y, cc.z);
-            __syncwarp();  // the previous bin's partner reads are done
-            if (n <= kPairRanks) {
-                // ranks 32 g + lane in group g = 0 .. G-1, all staged in shared memory
-                const int G = (n + 31) >> 5;
-                for (int g = 0; g < G; g++)
-                    if (32 * g + lane < n) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), 32 * g + lane);
-                __syncwarp();
-                for (int g = 0; g < G; g++) {
-                    const int mg = min(32, n - 32 * g);
-                    PairRec me{};
-                    if (lane < mg) {
-                        const uint4 q = srec[32 * g + lane];
-                        const int2 nq = snd[32 * g + lane];
-                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                    }
-                    rotate_pairs(me, srec, snd, 32 * g, mg, lane, t, filt, cand_cap, cand, ncand, flags);  // within group g
-                    // group g (full: a later group exists) against the records of the later
-                    // groups, 32 partners per window of hit bits
-                    for (int r0 = 32 * (g + 1); r0 < n; r0 += 32) {
-                        const int rn = min(32, n - r0);
-                        uint32_t bits = 0;
-                        if (rn == 32) {  // a full window: constant shifts
-#pragma unroll
-                            for (int k = 0; k < 32; k++) {
-                                const uint4 q = srec[r0 + k];
-                                const int2 nq = snd[r0 + k];
-                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                                bits |= uint32_t(pair_test(me, o)) << k;
-                            }
-                        } else {
-#pragma unroll 4
-                            for (int k = 0; k < rn; k++) {
-                                const uint4 q = srec[r0 + k];
-                                const int2 nq = snd[r0 + k];
-                                const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                                bits |= uint32_t(pair_test(me, o)) << k;
-                            }
-                        }
-                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[r0 + k].x & kIdMask; }, lane,
-                                    t, filt, cand_cap, cand, ncand, flags);
-                    }
+        if constexpr (pass == 0) {
+            bool keep = false;
+            if (g < total) {
+                const uint2 q = cand[g];
+                const int2 na = shape_nodes(t, q.x), nb = shape_nodes(t, q.y);
+                if (t.node_inst[na.x] == t.node_inst[nb.x]) {
+                    const DistBounds d = dist_bounds(t, p, xf, q.x, q.y);
+                    keep = !(d.far_ok && d.far > d.pad_sum + reach);
+                    // local pairs (sim.cpp:24-39) never make contact: dropped here, once per
+                    // build, so the narrow phase of every evaluation needs no hash lookups
+                    if (keep) keep = !any_connected(t, na, nb);
                 }
-            } else {
-                // large bin: its groups of 32 entries in turn.  Group g is staged in shared
-                // ranks 0..31 (lane i holding entry 32 g + i) and its pairs found by
-                // rotation; each later group is then staged in ranks 32..63 and met 32
-                // partners per window of hit bits.  A group with a later group is full, so
-                // every lane holds an entry there.
-                const int G = (n + 31) >> 5;
-                for (int g = 0; g < G; g++) {
-                    const int mg = min(32, n - 32 * g);
-                    __syncwarp();  // the previous group's partner reads are done
-                    if (lane < mg) stage_rec(load_rec(t, items[32 * g + lane], rec, ccp), lane);
-                    __syncwarp();
-                    PairRec me{};
-                    if (lane < mg) {
-                        const uint4 q = srec[lane];
-                        const int2 nq = snd[lane];
-                        me = PairRec{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                    }
-                    rotate_pairs(me, srec, snd, 0, mg, lane, t, filt, cand_cap, cand, ncand, flags);
-                    for (int h = g + 1; h < G; h++) {
-                        const int rn = min(32, n - 32 * h);
-                        __syncwarp();
-                        if (lane < rn) stage_rec(load_rec(t, items[32 * h + lane], rec, ccp), 32 + lane);
-                        __syncwarp();
-                        uint32_t bits = 0;
-#pragma unroll 4
-                        for (int k = 0; k < rn; k++) {
-                            const uint4 q = srec[32 + k];
-                            const int2 nq = snd[32 + k];
-                            const PairRec o{q.x, q.y, q.z, q.w, nq.x, nq.y};
-                            bits |= uint32_t(pair_test(me, o)) << k;
-                        }
-                        append_bits(bits, me.id & kIdMask, [&](int k) { return srec[32 + k].x & kIdMask; }, lane,
-                                    t, filt, cand_cap, cand, ncand, flags);
-                    }
-                }
-                __syncwarp();
             }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) {
+                fbits[ch] = m;
+                fcount[ch] = __popc(m);
+            }
+        } else {
+            const unsigned m = fbits[ch];
+            if (m & (1u << lane)) cand2[foff[ch] + __popc(m & below)] = cand[g];
         }
-    }
-    entries = __reduce_add_sync(0xffffffffu, entries);
-    if (lane == 0) {
-        if (entries) atomicAdd(nentries, entries);
-        if (occupied) atomicAdd(nentries + 2, occupied);
     }
 }
 
-
-
-// Narrow phase over the candidate list (flat, kept by the build's filter), one candidate per
-// thread.
+// Narrow phase over the filtered list (flat, in order), one candidate per thread.
 // Pass 0: test every candidate; one hit bit per candidate and the hit count per chunk of
 // 32.  Pass 1 (after a scan of the chunk counts of the list's length): the hits' candidate
 // indices, compacted in candidate order (into c_a, overwritten by k_contacts).
 template <int pass>
 __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                   const float4* __restrict__ xf, const uint2* __restrict__ cand,
-                                                   const uint32_t* __restrict__ ncand, long long cand_cap,
+                                                   const float4* __restrict__ xf, const uint2* __restrict__ cand2,
+                                                   const uint32_t* __restrict__ ntotal,
                                                    uint32_t* __restrict__ hitbits, uint32_t* __restrict__ hcount,
                                                    const uint32_t* __restrict__ hoff, ContactBufs c) {
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
-    const uint32_t total = uint32_t(min((long long)*ncand, cand_cap));
+    const uint32_t total = *ntotal;
     const long long nchunk = (total + 31) / 32;
     const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
     for (long long ch = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ch < nchunk; ch += warps) {
@@ -816,7 +820,7 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
         } else {
             bool hit = false;
             if (g < total) {
-                const uint2 q = cand[g];  // not a local pair (keep_pair)
+                const uint2 q = cand2[g];  // not a local pair (k_filter)
                 const int cls = distance_class(t, p, xf, q.x, q.y);
                 if (cls > 0) hit = true;  // certainly within the target
                 else if (cls == 0) hit = narrow_phase(t, p, x, q.x, q.y).hit;
@@ -831,13 +835,13 @@ __global__ void __launch_bounds__(kBlock) k_narrow(DevTopo t, PhysParams p, cons
 }
 
 // The contacts, one hit per thread (dense: the FP64 closest points run with full warps):
-// contact o is candidate c_a[o] of the list, written in candidate order.
+// contact o is candidate c_a[o] of the filtered list, written in candidate order.
 __global__ void __launch_bounds__(kBlock) k_contacts(DevTopo t, PhysParams p, const double4_32a* __restrict__ x,
-                                                     const uint2* __restrict__ cand,
+                                                     const uint2* __restrict__ cand2,
                                                      const uint32_t* __restrict__ total, ContactBufs c) {
     const long long nc = min((long long)*total, c.contact_cap);
     for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < nc; o += (long long)gridDim.x * blockDim.x) {
-        const uint2 q = cand[c.c_a[o]];
+        const uint2 q = cand2[c.c_a[o]];
         const PairHit h = narrow_phase(t, p, x, q.x, q.y);
         c.c_a[o] = q.x;
         c.c_b[o] = q.y;
@@ -956,13 +960,14 @@ int contact_pair_blocks(long long shapes) {
 void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, ContactBufs& c, double pad,
                      float skin, cudaStream_t s, cudaEvent_t pairs_begin, cudaEvent_t pairs_end) {
     const int S = t.N + t.B;
+    const uint32_t* gate = c.flags + 1;
     cudaMemsetAsync(c.flags, 0, 2 * sizeof(uint32_t), s);
     cudaMemsetAsync(c.flags + 3, 0, sizeof(uint32_t), s);  // the pair pass's bin cursor
     (k_skin_check<<<grid_for(t.N), kBlock, 0, s>>>(t, t.N, e.xf_lo, e.xf_hi, c.xref, skin, c.flags), note_launches(1));
     // candidate list (only when rebuilding)
-    (k_build_begin<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, e.cen + 9 * size_t(t.I),
-                                                  pad + double(skin > 0.f ? skin : 0.f), p.broad_cell, c.bin_cap,
-                                                  c.grid, c.flags, c.ncand, c.nentries),
+    (k_zero_gated<<<kStreamBlocks, kBlock, 0, s>>>(c.bin_cap + 1, c.bin_count, gate), note_launches(1));
+    (k_grid_params<<<1, 32, 0, s>>>(e.cen + 9 * size_t(t.I), pad + double(skin > 0.f ? skin : 0.f), p.broad_cell,
+                                    c.bin_cap, c.grid, c.flags, c.ncand, c.nentries),
      note_launches(1));
     (k_shape_prep<<<grid_for(S), kBlock, 0, s>>>(t, p, e.xf_lo, e.xf_hi, c.grid, c.cell_lo, c.cell_hi, c.rec,
                                                  skin > 0.f ? skin : 0.f, c.flags), note_launches(1));
@@ -970,24 +975,28 @@ void launch_contacts(const DevTopo& t, const PhysParams& p, const EvalBufs& e, C
                                            c.nentries, c.flags), note_launches(1));
     // occupied bins, then the candidate list
     if (pairs_begin) cudaEventRecord(pairs_begin, s);
-    const float reach = skin > 0.f ? 2.0001f * skin : 0.f;  // >= 2 skin
-    const CandFilter filt{p, e.xf_lo, reach, c.nentries + 3};
     (k_bin_pairs<<<c.pair_blocks, kBlock, 0, s>>>(t, c.grid, c.bin_count, c.bin_slots, c.nentries, c.bin_items,
-                                                c.rec, c.cand_cap, c.cand, c.ncand, c.flags, filt),
+                                                c.rec, c.cand_cap, c.cand, c.ncand, c.flags),
      note_launches(1));
     if (pairs_end) cudaEventRecord(pairs_end, s);
-    (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
-    // narrow phase over the list: hit bits and counts per chunk, scan, contacts
+    // filtered list (only when rebuilding)
     const long long chunks = c.cand_cap / 32;
-    (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand, c.ncand, c.cand_cap, c.hitbits, c.hcount,
-                                                c.hoff, c),
+    const float reach = skin > 0.f ? 2.0001f * skin : 0.f;  // >= 2 skin
+    (k_filter<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.cand_cap, c.cand, c.ncand, reach, c.fbits,
+                                                c.fcount, c.foff, c.cand2, gate), note_launches(1));
+    exclusive_scan_u32(c.fcount, c.foff, chunks, c.scan_tmp, s, gate, c.ncand, 31, 5);
+    (k_filter<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.xf_lo, c.cand_cap, c.cand, c.ncand, reach, c.fbits,
+                                                c.fcount, c.foff, c.cand2, gate), note_launches(1));
+    (k_skin_commit<<<grid_for(t.N), kBlock, 0, s>>>(t.N, e.xf_lo, c.xref, c.flags), note_launches(1));
+    // narrow phase over the filtered list: hit bits and counts per chunk, scan, contacts
+    const uint32_t* nkept = c.foff + chunks;
+    (k_narrow<0><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
      note_launches(1));
-    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, c.ncand, 31, 5);
-    (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand, c.ncand, c.cand_cap, c.hitbits, c.hcount,
-                                                c.hoff, c),
+    exclusive_scan_u32(c.hcount, c.hoff, chunks, c.scan_tmp, s, nullptr, nkept, 31, 5);
+    (k_narrow<1><<<kStreamBlocks, kBlock, 0, s>>>(t, p, e.x, e.xf_lo, c.cand2, nkept, c.hitbits, c.hcount, c.hoff, c),
      note_launches(1));
     // one warp per block: the few thousand contacts spread over every SM's FP64 pipe
-    (k_contacts<<<8 * kStreamBlocks, 32, 0, s>>>(t, p, e.x, c.cand, c.hoff + chunks, c), note_launches(1));
+    (k_contacts<<<8 * kStreamBlocks, 32, 0, s>>>(t, p, e.x, c.cand2, c.hoff + chunks, c), note_launches(1));
     const uint32_t* total = c.hoff + chunks;
     cudaMemsetAsync(c.n_count, 0, size_t(t.N + 1) * sizeof(uint32_t), s);
     cudaMemsetAsync(c.n_cursor, 0, size_t(t.N) * sizeof(uint32_t), s);

@@ -325,12 +325,16 @@ struct mcg_ctx {
         c.bin_cap = bin_cap;
         c.bin_count = contact_mem.get<uint32_t>(size_t(bin_cap + 1));
         c.bin_items = contact_mem.get<uint32_t>(size_t(bin_cap) * size_t(slots));
-        c.nentries = contact_mem.get<uint32_t>(4);
+        c.nentries = contact_mem.get<uint32_t>(3);
         c.pair_blocks = pair_blocks_for(S);
         c.cand_cap = std::max<long long>(1024, (cand_cap + 31) / 32 * 32);
         c.cand = contact_mem.get<uint2>(size_t(c.cand_cap));
         c.ncand = contact_mem.get<uint32_t>(1);
         const long long chunks = c.cand_cap / 32;
+        c.cand2 = contact_mem.get<uint2>(size_t(c.cand_cap));
+        c.fbits = contact_mem.get<uint32_t>(size_t(chunks));
+        c.fcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
+        c.foff = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.hitbits = contact_mem.get<uint32_t>(size_t(chunks));
         c.hcount = contact_mem.get<uint32_t>(size_t(chunks + 1));
         c.hoff = contact_mem.get<uint32_t>(size_t(chunks + 1));
@@ -351,7 +355,7 @@ struct mcg_ctx {
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 5 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.ncand, 0, sizeof(uint32_t), stream), "memset");
-        ck(cudaMemsetAsync(c.nentries, 0, 4 * sizeof(uint32_t), stream), "memset");
+        ck(cudaMemsetAsync(c.nentries, 0, 3 * sizeof(uint32_t), stream), "memset");
         ck(cudaMemsetAsync(c.flags + 2, 1, 1, stream), "memset");  // the first evaluation builds the list
         cb = c;
     }
@@ -1968,8 +1972,8 @@ int mcg_contact_stats(mcg_ctx* c, int64_t* out5) {
             throw Fail(MCG_ERR_STATE, "the last evaluation was mcg_objective_noalloc's, whose contact statistics are not kept");
         d2h(c->hp.u32, c->cb.nentries, 1, c->stream);
         d2h(c->hp.u32 + 1, c->cb.nentries + 2, 1, c->stream);
-        d2h(c->hp.u32 + 2, c->cb.nentries + 3, 1, c->stream);
-        d2h(c->hp.u32 + 3, c->cb.ncand, 1, c->stream);
+        d2h(c->hp.u32 + 2, c->cb.ncand, 1, c->stream);
+        d2h(c->hp.u32 + 3, c->cb.foff + c->contact_chunks(), 1, c->stream);
         d2h(c->hp.u32 + 4, c->cb.hoff + c->contact_chunks(), 1, c->stream);
         c->sync();
         for (int k = 0; k < 5; k++) out5[k] = c->hp.u32[k];

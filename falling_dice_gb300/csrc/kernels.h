@@ -125,17 +125,20 @@ struct ContactBufs {
     int bin_slots;          // entries a bin holds, a power of two
     uint32_t* bin_count;    // [bin_cap+1] entries counted per bin (may exceed bin_slots)
     uint32_t* bin_items;    // [bin_cap * bin_slots]
-    uint32_t* nentries;     // [4]: [0] cell entries of the last build, [1] the largest bin count
+    uint32_t* nentries;     // [3]: [0] cell entries of the last build, [1] the largest bin count
                             //      above bin_slots (0 when every bin fitted), [2] bins holding
-                            //      two or more entries, [3] box-overlapping pairs the build's
-                            //      filter saw
-    // narrow-phase candidates: one flat list, appended by the pair grid's warps (the pairs
-    // its filter keeps, contact.cu keep_pair)
+                            //      two or more entries
+    // narrow-phase candidates: one flat list, appended by the pair grid's warps in chunks
     int pair_blocks;        // blocks of the pair grid (8 warps each)
     long long cand_cap;     // candidate slots, a multiple of 32
     uint2* cand;            // [cand_cap] (lower shape, higher shape)
-    uint32_t* ncand;        // [1] candidates kept by the last build (may exceed cand_cap)
-    // narrow phase, per chunk of 32 consecutive candidates
+    uint32_t* ncand;        // [1] candidates found by the last build (may exceed cand_cap)
+    // filtered candidates (the ones that can reach contact before the next build), in order
+    uint2* cand2;           // [cand_cap]
+    uint32_t* fbits;        // [chunks] keep bit per candidate (chunks = cand_cap / 32)
+    uint32_t* fcount;       // [chunks + 1] kept per chunk
+    uint32_t* foff;         // [chunks + 1] scan of fcount; foff[chunks] = filtered list length
+    // narrow phase, per chunk of 32 consecutive filtered candidates
     uint32_t* hitbits;      // [chunks] contact bit per candidate
     uint32_t* hcount;       // [chunks + 1] contacts per chunk
     uint32_t* hoff;         // [chunks + 1] scan of hcount; hoff[chunks] = contact count

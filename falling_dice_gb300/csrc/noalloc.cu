@@ -90,12 +90,16 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.bin_slots = kNoAllocBinSlots;
     c.bin_count = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins + 1) * 4));
     c.bin_items = reinterpret_cast<uint32_t*>(take(size_t(kNoAllocBins) * kNoAllocBinSlots * 4));
-    c.nentries = reinterpret_cast<uint32_t*>(take(4 * 4));
+    c.nentries = reinterpret_cast<uint32_t*>(take(3 * 4));
     c.pair_blocks = contact_pair_blocks(S);
     c.cand_cap = kNoAllocCandidates;
     c.cand = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
     c.ncand = reinterpret_cast<uint32_t*>(take(4));
     const long long chunks = kNoAllocCandidates / 32;
+    c.cand2 = reinterpret_cast<uint2*>(take(size_t(kNoAllocCandidates) * sizeof(uint2)));
+    c.fbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
+    c.fcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
+    c.foff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.hitbits = reinterpret_cast<uint32_t*>(take(size_t(chunks) * 4));
     c.hcount = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));
     c.hoff = reinterpret_cast<uint32_t*>(take(size_t(chunks + 1) * 4));

@@ -364,8 +364,8 @@ int mcg_solver_times(mcg_ctx* ctx, double* ms4, int64_t* rounds);
 int mcg_contact_builds(mcg_ctx* ctx, int64_t* builds);
 
 /* Sizes of the last self-contact candidate-list build and evaluation (no reference
- * counterpart): out5 = {cell entries, occupied bins, box-overlapping pairs sharing no node,
- * candidates kept by the build's distance and connectivity filter, contacts}. */
+ * counterpart): out5 = {cell entries, occupied bins, box-overlap candidates, candidates kept
+ * by the distance filter, contacts}. */
 int mcg_contact_stats(mcg_ctx* ctx, int64_t* out5);
 
 /* Per-phase timing of evaluations with CUDA events on the context stream (no reference
