@@ -227,8 +227,12 @@ __global__ void __launch_bounds__(kBlock) k_skin_check(DevTopo t, int N, const f
                                                        const float4* __restrict__ xref, float skin,
                                                        uint32_t* __restrict__ flags) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (!(skin > 0.f)) {  // no reuse: every evaluation builds, no position to compare
+        if (i == 0) atomicOr(flags + 1, 1u);
+        return;
+    }
     bool moved = false;
-    if (i == 0 && (flags[2] || !(skin > 0.f))) moved = true;
+    if (i == 0 && flags[2]) moved = true;
     if (i < N && !moved && t.active[t.node_inst[i]]) {
         const float4 l = xf_lo[i], h = xf_hi[i], r = xref[i];
         // per-axis bounds of the move, then its Euclidean length, all rounded upward
