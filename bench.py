@@ -442,6 +442,7 @@ def main():
         "energy": mixed["energy"], "contacts": mixed["contacts"],
     }
     if not a.no_extras and world == 1:
+        line["dense_contact"] = dense_contact(fd, abi, workloads, torch)
         line["load_unload"] = load_unload(fd, abi, workloads)
         line["sweep"] = sweep(fd, abi, workloads)
     print(json.dumps(line), flush=True)
@@ -451,6 +452,58 @@ def run_summary(frames):
     return {"frames": len(frames), "iterations": int(sum(f["iterations"] for f in frames)),
             "peak_force": max(f["reaction_force"] for f in frames), "absorbed_energy": frames[-1]["loading_work"],
             "dissipated_work": frames[-1]["dissipated_work"], "permanent_set": frames[-1]["permanent_set"]}
+
+
+def squeezed_state(fd, lat, cfg, squeeze=0.6):
+    """The 32x32x16 specimen squeezed to 1 - squeeze of its height with lateral noise: the
+    dense self-contact state of the full-size parity test (~42,000 contacting shape pairs)."""
+    z, pl = fd.random_state(lat, 0.15, 0.1, 0.02, 77)
+    y = lat.x0[1::3]
+    z[1::6] += -squeeze * (y - y.min()) / cfg.translation_scale
+    z[lat.locked.astype(bool)] = 0
+    return z, pl, lat.geometry.top0 - squeeze * lat.geometry.height + 1e-3
+
+
+def dense_contact(fd, abi, workloads, torch, steps=100):
+    """Evaluations/s in dense self-contact, mixed and FP64: the squeezed 32x32x16 state, the
+    contact list rebuilt at every evaluation, device-resident evaluations timed by CUDA events
+    (its arrays fit in L2, so these are warm-cache figures), the phase split and the contact
+    statistics.  The headline state has no self-contact within reach (its contacts are platen
+    contacts); here the filter, the narrow phase and the per-node contact lists carry load."""
+    out = {}
+    for name, prec in (("mixed", abi.MCG_MIXED), ("fp64", abi.MCG_FP64)):
+        cfg, spec = workloads.bcc32()
+        cfg.precision = prec
+        lat = fd.generate_lattice(spec, cfg)
+        z, pl, top = squeezed_state(fd, lat, cfg)
+        sol = fd.Solver(cfg, lat)
+        sol.set_contact_skin(0.0)
+        sol.set_state(plastic=pl)
+        sol.upload_z(z)
+        for _ in range(5):
+            sol.objective_resident(top)
+        res = sol.read_result(grad=False)
+        stream = torch.cuda.ExternalStream(sol.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            sol.objective_resident(top)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        sol.set_timing(True)
+        for _ in range(10):
+            sol.objective_resident(top)
+        phases, nev = sol.phase_times()
+        sol.set_timing(False)
+        st = sol.contact_stats()
+        sol.close()
+        out[name] = {"evals_per_s": 1e3 / ms, "ms_per_eval": ms, "contacts": int(res["diag"]["contacts"]),
+                     "phase_ms": {k: v / nev for k, v in phases.items()}, "contact_stats": st}
+    out["workload"] = (f"bcc32 squeezed to 40 % of its height: {lat.n_nodes} nodes, {lat.n_beams} beams, "
+                       f"{out['fp64']['contact_stats']['contacts']} contacting shape pairs")
+    return out
 
 
 def load_unload(fd, abi, workloads):
