@@ -913,7 +913,11 @@ __global__ void __launch_bounds__(kBlock) k_node_sort(int N, ContactBufs c) {
             const long long i = i0 + b;
             const uint32_t cnt = __shfl_sync(0xffffffffu, mine, b), s0 = c.n_start[i];
             if (cnt > 32) {
-                if (lane == 0) c.n_long[1 + atomicAdd(c.n_long, 1u)] = uint32_t(i);
+                if (lane == 0) {
+                    const uint32_t at = atomicAdd(c.n_long, 1u);
+                    c.n_long[1 + at] = uint32_t(i);
+                    c.n_cursor[i] = at;  // the fill is done with it
+                }
                 continue;
             }
             uint32_t item = 0;

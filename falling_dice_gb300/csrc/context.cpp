@@ -351,6 +351,7 @@ struct mcg_ctx {
         c.n_items = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_sorted = contact_mem.get<uint32_t>(size_t(4 * contact_cap));
         c.n_long = contact_mem.get<uint32_t>(size_t(N + 1));
+        c.long_sum = contact_mem.get<double>(6 * size_t(std::max(N, 1)));
         c.scan_tmp_bytes = scan_tmp_bytes(std::max({(long long)N + 1, chunks + 1}));
         c.scan_tmp = contact_mem.get<unsigned char>(c.scan_tmp_bytes);
         ck(cudaMemsetAsync(c.flags, 0, 5 * sizeof(uint32_t), stream), "memset");

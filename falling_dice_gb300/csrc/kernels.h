@@ -152,10 +152,14 @@ struct ContactBufs {
     // per-node contact force lists (CSR built per evaluation)
     uint32_t* n_count;      // [N+1]
     uint32_t* n_start;      // [N+1]
-    uint32_t* n_cursor;     // [N]
+    uint32_t* n_cursor;     // [N] fill cursor; then, for a node in n_long, its place there
     uint32_t* n_items;      // [4 * contact_cap]  (contact << 2 | slot), in arrival order
     uint32_t* n_sorted;     // [4 * contact_cap]  the same per node, by (lower shape, higher shape, slot)
     uint32_t* n_long;       // [N + 1] count, then the nodes whose lists exceed one warp
+    // [6 * N] or null: per node of n_long (by its place there), the sums of its list --
+    // force (3), self-contact energy, contacts, largest penetration -- taken by the gather
+    // instead of walking the list (null: the gather walks every list)
+    double* long_sum;
     void* scan_tmp;
     size_t scan_tmp_bytes;
 };

@@ -116,6 +116,7 @@ bool carve(unsigned char* base, long long N, long long S, ContactBufs& c) {
     c.n_items = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_sorted = reinterpret_cast<uint32_t*>(take(size_t(4 * kNoAllocContacts) * 4));
     c.n_long = reinterpret_cast<uint32_t*>(take(size_t(N + 1) * 4));
+    c.long_sum = nullptr;  // the gather walks every list (no room for the long lists' sums)
     long long scan_n = N + 1;
     if (chunks + 1 > scan_n) scan_n = chunks + 1;
     c.scan_tmp_bytes = scan_tmp_bytes(scan_n);

@@ -340,6 +340,43 @@ __device__ __forceinline__ void add_contact_item(const ContactBufs& c, const Phy
     }
 }
 
+// The sums of each long list (n_long) for the gather, one warp per node: lane l takes items
+// l, l + 32, ... in list order, then the lanes' partial sums meet in a fixed butterfly, so
+// the sums do not depend on the order of the queue or of the contact list.  A node of a
+// densely compressed lattice holds a few hundred items; walked by one thread in the gather,
+// its dependent loads set the gather's time.
+__global__ void __launch_bounds__(kBlock) k_node_contact_long(DevTopo t, PhysParams p, ContactBufs c) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nl = c.n_long[0];
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long j = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < nl; j += warps) {
+        const uint32_t i = c.n_long[1 + j];
+        const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
+        d3 f{0, 0, 0};
+        double energy = 0, count = 0, pen_max = 0;
+        for (uint32_t k = uint32_t(lane); k < cnt; k += 32)
+            add_contact_item(c, p, t.N, c.n_sorted[s0 + k], f, energy, count, pen_max);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            f.x += __shfl_xor_sync(0xffffffffu, f.x, o);
+            f.y += __shfl_xor_sync(0xffffffffu, f.y, o);
+            f.z += __shfl_xor_sync(0xffffffffu, f.z, o);
+            energy += __shfl_xor_sync(0xffffffffu, energy, o);
+            count += __shfl_xor_sync(0xffffffffu, count, o);
+            pen_max = fmax(pen_max, __shfl_xor_sync(0xffffffffu, pen_max, o));
+        }
+        if (lane == 0) {
+            double* q = c.long_sum + 6 * size_t(j);
+            q[0] = f.x;
+            q[1] = f.y;
+            q[2] = f.z;
+            q[3] = energy;
+            q[4] = count;
+            q[5] = pen_max;
+        }
+    }
+}
+
 // ---- per-node gather: the scatter of MC/src/sim.cpp:139-172, as a deterministic CSR sum ---
 // Sums the incident beams' end vectors of node i in ascending beam order: FP64 slots
 // directly, FP32 slots (mixed form) with compensated FP32 sums.
@@ -410,8 +447,15 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_gather(DevTopo t, PhysPa
         // order (the list is sorted by the contact pipeline), and the self-contact energy of
         // each contact on the first node of its lower shape: both independent of the order
         // of the contact list
-        if (use_contacts) {
-            const uint32_t s0 = c.n_start[i], cnt = c.n_count[i];
+        const uint32_t cnt = use_contacts ? c.n_count[i] : 0u;
+        if (cnt > 32 && c.long_sum) {  // summed by k_node_contact_long
+            const double* q = c.long_sum + 6 * size_t(c.n_cursor[i]);
+            gx = gx + d3{q[0], q[1], q[2]};
+            acc[4] += q[3];
+            acc[3] += q[4];
+            pen_max = fmax(pen_max, q[5]);
+        } else if (use_contacts) {
+            const uint32_t s0 = c.n_start[i];
             uint32_t k = 0;
             // four items at a time: their loads in flight together (a joint of a densely
             // compressed lattice can hold a few hundred items), the additions in list order
@@ -715,12 +759,17 @@ void launch_beams(const DevTopo& t, const Material& m, const double* plastic, in
     note_launches(1);
 }
 
+constexpr int kLongListBlocks = 4 * 152;  // eight long lists per block, grid-stride
+
 template <bool F32>
 void gather_variant(const DevTopo& t, const PhysParams& p, const ContactBufs* c, double* grad, EvalBufs& e,
                     cudaStream_t s, int variant) {
     ContactBufs cc{};
     if (c) cc = *c;
     const int uc = c ? 1 : 0;
+    if (c && c->long_sum) {
+        (k_node_contact_long<<<kLongListBlocks, kBlock, 0, s>>>(t, p, cc), note_launches(1));
+    }
     switch (variant) {
         case 1: k_gather<F32, kGatherBlocks[1]><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, uc, e, grad); break;
         case 2: k_gather<F32, kGatherBlocks[2]><<<t.n_nblk, kBlock, 0, s>>>(t, p, cc, uc, e, grad); break;
