@@ -55,6 +55,28 @@ NODE_BYTES_MIXED = 98    # per node, mixed: baseX (3 x 8 B) + 17 reals as FP32 +
 # shape's pair-test record once (16 B box/cell record + 8 B nodes), each occupied bin's
 # count, start and list slot (12 B), each candidate written (8 B).
 PAIR_ENTRY_BYTES, PAIR_SHAPE_BYTES, PAIR_BIN_BYTES, PAIR_CAND_BYTES = 4, 24, 12, 8
+# The pair enumeration is bound by instruction issue, not by memory: its second roofline is
+# warp instructions per second against the issue peak of one warp instruction per clock on
+# each of the 4 x 152 SM sub-partitions.  Instructions per launch from ncu
+# (smsp__inst_executed.sum, profiles/k_bin_pairs_bcc64.md) at the benchmark state of the
+# 64x64x32 specimen with the 4.5 mm cell and 1216 pair blocks; other shapes have no figure.
+PAIR_WARP_INSTRUCTIONS = {("bcc64", 0.0045, 1216): 304137669}
+SM_SUBPARTITIONS = 4 * 152
+
+
+def pair_issue_roofline(workload, cell, pair_blocks, ms, sm_mhz):
+    """Warp instructions/s of one k_bin_pairs launch against the issue peak, or None when no
+    instruction count was measured for these shapes."""
+    key = next((k for k in PAIR_WARP_INSTRUCTIONS
+                if k[0] == workload and abs(k[1] - cell) < 1e-9 and k[2] == pair_blocks), None)
+    if key is None or not ms or not sm_mhz:
+        return None
+    inst = PAIR_WARP_INSTRUCTIONS[key]
+    ach = inst / (ms * 1e-3) / 1e9
+    peak_issue = SM_SUBPARTITIONS * sm_mhz * 1e6 / 1e9
+    return {"bound": "issue", "achieved": ach, "peak": peak_issue, "unit": "G warp-instructions/s",
+            "frac": ach / peak_issue, "warp_instructions_per_launch": inst, "sm_mhz": sm_mhz,
+            "source": "ncu smsp__inst_executed.sum of one launch with the same shapes"}
 
 
 def parse():
@@ -402,7 +424,10 @@ def main():
                 "frac": ach / peak, "peak_source": peak_kind,
                 "traffic": nbytes * PAIR_TRAFFIC_PER_ALGORITHMIC_BYTE, "bytes_per_launch": nbytes,
                 "ms_per_launch": ms, "share_of_evaluation": ms / r["ms_step"],
-                "counts": st, "note": "issue-bound integer work (pair tests); the fraction is of HBM"}
+                "counts": st, "note": "issue-bound integer work (pair tests); the fraction is of HBM",
+                "issue": pair_issue_roofline(a.workload, r["tuning"].get("cell") or 0.0,
+                                             r["tuning"].get("pair_blocks") or 0, ms,
+                                             (r["clocks"] or {}).get("sm_mhz"))}
     cpu = None
     if not a.no_cpu_baseline:
         t_s, e_cpu, N_s, B_s = cpu_one_core(a.workload)
