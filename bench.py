@@ -279,6 +279,49 @@ def _counts():
     return _worker_args[2], _worker_args[3]
 
 
+def _sweep_cpu_run(k):
+    """One lattice of the sweep solved by the reference's own run (the oracle port) on one
+    core: (lattice index, beams, status, frames, seconds)."""
+    sys.path.insert(0, ROOT)
+    from falling_dice_gb300 import abi, workloads
+    from oracle import oracle as orc
+    cfg, specs, ys = workloads.sweep()
+    c = abi.Config.from_buffer_copy(cfg)
+    c.material.yield_ = ys[k]
+    m = orc.Model("mco", c, lattice=specs[k])
+    beams = m.export().n_beams
+    t = time.perf_counter()
+    rc, frames = m.run()
+    return k, beams, int(rc), len(frames), time.perf_counter() - t
+
+
+def sweep_cpu_reference(workloads, batched_rate):
+    """The sweep's CPU reference (one reference process per host core): the reference's own
+    run of the sweep's smallest lattices, one per core, on all cores at once.  A whole sweep
+    on the CPU takes hours (its smallest lattice alone ~50 s of one core), so this times the
+    cheapest lattices only; their rate bounds the CPU's sweep rate from above."""
+    import multiprocessing as mp
+    from oracle import oracle as orc
+    orc.build("mco")
+    cores = cpu_model()["cores"]
+    cfg, specs, ys = workloads.sweep()
+    order = sorted(range(len(specs)), key=lambda k: (specs[k].cells_x * specs[k].cells_y * specs[k].cells_z, k))
+    pick = order[:cores]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        t0 = time.perf_counter()
+        res = pool.map(_sweep_cpu_run, pick, chunksize=1)
+        wall = time.perf_counter() - t0
+    secs = [r[4] for r in res]
+    rate = len(pick) / wall
+    return {"metric": "lattices/s", "cores": cores, "cpu": cpu_model()["model"], "kind": "port",
+            "lattices": len(pick), "beams": [r[1] for r in res], "status": [r[2] for r in res],
+            "wall_s": wall, "seconds_per_lattice_mean": float(np.mean(secs)),
+            "all_cores_lattices_per_s": rate, "one_core_lattices_per_s": 1.0 / float(np.mean(secs)),
+            "batched_gpu_over_all_cores": batched_rate / rate,
+            "sample": f"the {len(pick)} smallest of the {len(specs)} lattices (by cell count), each solved "
+                      f"by the reference's run in its own process; an upper bound of the CPU's sweep rate"}
+
+
 def measure(fd, torch, cfg, lat, z, pl, top, steps, warmup, local, pg, world, shapes=None):
     """Times one precision form: device-resident evaluations, e2e through the C ABI, phases."""
     import ctypes as C
@@ -666,6 +709,10 @@ def sweep(fd, abi, workloads, sample=32):
     mean_t = float(np.mean(times))
     se_t = float(np.std(times, ddof=1) / np.sqrt(len(times)))
     batched, seq = len(lats) / dt, 1.0 / mean_t
+    try:
+        cpu_ref = sweep_cpu_reference(workloads, batched)
+    except Exception as e:  # the CPU leg never costs the GPU figures
+        cpu_ref = {"error": f"{type(e).__name__}: {e}"}
     return {"metric": "lattices/s", "batched_fp64": batched, "sequential_fp64": seq, "speedup": batched / seq,
             "speedup_range_1se": [batched * (mean_t - se_t), batched * (mean_t + se_t)],
             "batched_seconds": dt,
@@ -673,7 +720,7 @@ def sweep(fd, abi, workloads, sample=32):
                                  f"{mean_t:.3f} +/- {se_t:.3f} s per lattice (standard error), {sum(times):.1f} s",
             "completed": int((np.asarray(status) == 0).sum()), "lattices": len(lats),
             "beams": int(sum(l.n_beams for l in lats)), "sample_frames_identical_to_batch": bool(same),
-            "broad_phase": tune,
+            "broad_phase": tune, "cpu_reference": cpu_ref,
             "workload": "256 cubic+BCC lattices, 4-16 cells per side, radius 0.3 mm + U[0, 0.1] mm/cell "
                         "(capped 0.7 mm), yield U[30, 70] MPa, 30 % strain in 100 increments"}
 
